@@ -1,0 +1,312 @@
+#!/usr/bin/env python
+"""Benchmark of the parquet-iteration hot path (one JSON line on stdout).
+
+Metric: seconds per parquet iteration (one iterate_solver!, fdPA, update_Σ) on the plain FP64 GPU
+path, with time-to-converge at residual 1e-8 reported beside it.  Workload: the Hubbard 8x8
+nonlocal fdPA configuration (t=1, t'=0, μ=0, U=2, β=5, nK1=32, nK2=(16,16), nK3=(8,12), nG=32,
+mΠν_factor=32, seeded synthetic RefVertex), init_sym_grp! symmetry groups.
+
+  value  device-resident: the iteration graph replayed K times on a fixed state, CUDA events on
+         the solver's stream; working set (bubbles 4 x 132 MB) larger than L2.
+  e2e    fixed_point!(R, x, S) through the C ABI with pinned host x and R: H2D + iteration + D2H.
+  --impl reference  the CPU oracle (C++ restatement of the reference algorithm, all host threads);
+         the reference itself is Julia and cannot run on this machine.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fddgasolver.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "s per parquet iteration (plain FP64, fdPA, Hubbard 8x8 config)"
+UNIT = "s/iteration"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="config2")
+    ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks on the host (gloo); a no-op for one process."""
+
+    def __init__(self, world):
+        self.world = world
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_problem(cfg_name, impl):
+    from fdgasolver.workloads import CONFIGS, make_inputs, make_solver
+    cfg = dict(CONFIGS[cfg_name])
+    if impl == "ours":
+        return cfg, make_solver(cfg, True)
+    from oracle import oracle as O  # CPU baseline leg only
+    Gb, G0, S0, rv = make_inputs(cfg)
+    local = cfg["kind"] == "siam"
+    s = O.OracleSolver(nG=cfg["nG"], nK1=cfg["nK1"], nK2=cfg["nK2"], nK3=cfg["nK3"], T=cfg["T"], U=cfg["U"],
+                       L=1 if local else cfg["L"], local=local, mPi_factor=cfg["mPi_factor"], nR=rv.nR)
+    for name, a in (("Gbare", Gb), ("G0", G0), ("Sigma0", S0)):
+        s.set(name, a)
+    for name, a in zip(["Fp_p", "Fp_x", "Ft_p", "Ft_x"], rv.arrays):
+        s.set(name, a)
+    s.finalize()
+    s.init_sym_grp()
+    return cfg, s
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def stage_work(cfg, stage, S):
+    """Algorithmic bytes moved by one launch-group of a stage (the roofline numerator)."""
+    L = cfg["L"]
+    Nq = L * L
+    NPO = 2 * cfg["nK1"] - 1
+    NPn = 2 * cfg["nK1"] * cfg["mPi_factor"]
+    N2 = (2 * cfg["nK2"][0] - 1) * 2 * cfg["nK2"][1] * Nq
+    N3 = (2 * cfg["nK3"][0] - 1) * (2 * cfg["nK3"][1]) ** 2 * Nq
+    B = 16
+    if stage == "dyson_bubble":
+        return 2 * NPO * NPn * Nq * B  # write Πpp, Πph
+    if stage in ("bse_K2", "sde"):
+        # each representative row streams Π and Π0 (K2) or Π (L) over the bubble mesh: at least
+        # every (P, Ω) row of both bubbles once, plus the K2-sized outputs
+        return 2 * NPO * NPn * Nq * B * (1 if stage == "sde" else 2) // 2 + 3 * N2 * B
+    if stage == "k3_cache":
+        return 10 * N3 * B + 3 * N3 * B
+    if stage in ("bse_K3", "bse_L_K3"):
+        return 3 * (4 * N3 * B)
+    return 3 * N2 * B
+
+
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    from fdgasolver.solver import PinnedBuffer
+    cfg, S = build_problem(args.config, "ours")
+    rng = np.random.default_rng(1)
+    # a representative state: a few damped iterations from the PA start
+    x = S.flatten()
+    for _ in range(3):
+        x = x + 0.5 * S.fixed_point(x)
+    x = x + 1e-3 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))
+    S.unflatten(x)
+    for _ in range(max(args.warmup, 3)):
+        S.map_repeat(1)
+    S.synchronize()
+    launches = S.launches_per_iteration()
+    # ---- device-resident timed region ----
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    dist.barrier()
+    S.synchronize()
+    S.event_record(0)
+    S.map_repeat(args.steps)
+    S.event_record(1)
+    S.synchronize()
+    dist.barrier()
+    ms_dev = S.event_elapsed_ms(0, 1) / args.steps
+    # ---- e2e through the C ABI with pinned host buffers ----
+    xb, Rb = PinnedBuffer(S.state_len), PinnedBuffer(S.state_len)
+    xb.array[:] = x
+    for _ in range(max(args.warmup, 3)):
+        S.fixed_point_ptr(xb.ptr, Rb.ptr)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.fixed_point_ptr(xb.ptr, Rb.ptr)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    dist.barrier()
+    clk = clocks.stop()
+    xb.free()
+    Rb.free()
+    ms_dev = dist.max(ms_dev)
+    t_e2e = dist.max(t_e2e)
+    # ---- per-stage device times (eager run, CUDA events between stages) ----
+    S.unflatten(x)
+    stages = S.stage_times("fdPA", nrep=3)
+    top = max(stages, key=stages.get)
+    peaks = measured_peaks()
+    work = stage_work(cfg, top, S)
+    achieved = work / (stages[top] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel_stage": top, "achieved": achieved, "peak": peaks.get("hbm_gbs"),
+                "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None,
+                "stage_ms": {k: round(v, 4) for k, v in stages.items()},
+                "peak_source": "fallback" if peaks.get("fallback") else "measured"}
+    # ---- time to converge (plain Anderson, tol 1e-8) ----
+    conv = None
+    if not args.no_converge:
+        cfg2, S2 = build_problem(args.config, "ours")
+        t0 = time.perf_counter()
+        r = S2.solve("fdPA", maxiter=100, tol=1e-8, delta=0.5, mem=8)
+        t_conv = time.perf_counter() - t0
+        conv = {"seconds": dist.max(t_conv), "iterations": r["iterations"], "converged": r["converged"],
+                "final_residual": r["residual"], "method": "Anderson m=8, beta=0.5 (NLsolve restated), plain FP64"}
+        S2.close()
+    nstate = S.state_len
+    out = {
+        "metric": METRIC, "value": ms_dev * 1e-3, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128 (FP64 complex)", "data": "synthetic (seeded; reference inputs restated)",
+        "config": {"workload": "Hubbard 8x8 NL fdPA: t=1 t'=0 mu=0 U=2 beta=5 nK1=32 nK2=(16,16) nK3=(8,12) nG=32 "
+                               "mPi=32, synthetic RefVertex, init_sym_grp",
+                   "name": args.config, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "bubble working set 0.53 GB > 129 MB L2; no flush"},
+        "e2e": {"value": t_e2e, "unit": UNIT, "h2d_bytes_per_step": nstate * 16, "d2h_bytes_per_step": nstate * 16},
+        "gpu_launches": launches * args.steps,
+        "launches_per_iteration": launches,
+        "time_to_converge": conv,
+        "roofline": roofline,
+        "clocks": clk,
+    }
+    S.close()
+    return out
+
+
+def run_reference(args, rank, world):
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    cfg, S = build_problem(args.config, "reference")
+    x = S.flatten()
+    for _ in range(args.warmup):
+        S.residual(x)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.residual(x)
+    dt = (time.perf_counter() - t0) / args.steps
+    return {
+        "impl": "reference", "metric": METRIC, "value": dt, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128 (FP64 complex)", "data": "synthetic (seeded)",
+        "config": {"workload": "Hubbard 8x8 NL fdPA (same as ours)", "name": args.config},
+        "cpu_baseline": {"value": dt, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full iterations of the workload (C++ restatement of the reference "
+                                   f"algorithm; Julia reference not runnable here)"},
+        "e2e": {"value": dt, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def cpu_baseline_sample(args):
+    """Oracle timed on the host cores for one iteration of the same workload (bounded sample)."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    cfg, S = build_problem(args.config, "reference")
+    x = S.flatten()
+    S.residual(x)
+    t0 = time.perf_counter()
+    S.residual(x)
+    dt = time.perf_counter() - t0
+    return {"value": dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "1 iteration of the workload after 1 warm-up (C++ restatement, OpenMP)"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args, rank, 1)))
+        return 0
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    dist = Dist(world)
+    out = run_ours(args, rank, world, dist)
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline_sample(args)
+        print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

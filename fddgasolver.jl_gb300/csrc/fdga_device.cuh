@@ -1,0 +1,237 @@
+// fdga_device.cuh -- device-side types, layouts and vertex evaluators of libfdga.
+//
+// Device layout (row-major, last index fastest; chosen so that each (P, Ω) block of a K3-shaped
+// array is one contiguous Nν x Nν matrix and every ω-sum streams contiguous memory):
+//   G-like  [k][ν]          (identical to the reference's column-major [ν, k])
+//   Π       [P][Ω][ν]
+//   K1      [P][Ω]          K2 [P][Ω][ν]          K3 [P][Ω][ν][ν']
+// The reference stores the same data column-major with Ω fastest; flatten/unflatten permute.
+//
+// Mesh-index arithmetic follows the reference conventions (src/types.jl, src/convention.jl):
+// fermion n <-> (2n+1)πT on [-N, N-1]; boson m <-> 2mπT on [-(N-1), N-1];
+// Ω_m - ν_n -> fermion m-n-1, Ω_m + ν_n -> m+n, ν_n - ν_n' -> boson n-n', ν_n + ν_n' -> n+n'+1.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fdga {
+
+struct cplx {
+    double x, y;
+};
+__host__ __device__ __forceinline__ cplx mk(double a, double b) { return cplx{a, b}; }
+__host__ __device__ __forceinline__ cplx operator+(cplx a, cplx b) { return cplx{a.x + b.x, a.y + b.y}; }
+__host__ __device__ __forceinline__ cplx operator-(cplx a, cplx b) { return cplx{a.x - b.x, a.y - b.y}; }
+__host__ __device__ __forceinline__ cplx operator-(cplx a) { return cplx{-a.x, -a.y}; }
+__host__ __device__ __forceinline__ cplx operator*(cplx a, cplx b) {
+    return cplx{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+__host__ __device__ __forceinline__ cplx operator*(cplx a, double s) { return cplx{a.x * s, a.y * s}; }
+__host__ __device__ __forceinline__ cplx operator*(double s, cplx a) { return cplx{a.x * s, a.y * s}; }
+__host__ __device__ __forceinline__ cplx& operator+=(cplx& a, cplx b) { a.x += b.x; a.y += b.y; return a; }
+__host__ __device__ __forceinline__ cplx& operator-=(cplx& a, cplx b) { a.x -= b.x; a.y -= b.y; return a; }
+__host__ __device__ __forceinline__ cplx conjg(cplx a) { return cplx{a.x, -a.y}; }
+__device__ __forceinline__ cplx cdiv(cplx a, cplx b) {
+    // a / b with Smith's scaling
+    if (fabs(b.x) >= fabs(b.y)) {
+        double r = b.y / b.x, den = b.x + b.y * r;
+        return cplx{(a.x + a.y * r) / den, (a.y - a.x * r) / den};
+    }
+    double r = b.x / b.y, den = b.x * r + b.y;
+    return cplx{(a.x * r + a.y) / den, (a.y * r - a.x) / den};
+}
+__device__ __forceinline__ cplx ldg(const cplx* p) {
+    double2 v = __ldg(reinterpret_cast<const double2*>(p));
+    return cplx{v.x, v.y};
+}
+// symmetry operation bits: 1 = negate, 2 = conjugate (MatsubaraFunctions Operation(sgn, con))
+__device__ __forceinline__ cplx apply_op(int op, cplx v) {
+    if (op & 2) v.y = -v.y;
+    if (op & 1) { v.x = -v.x; v.y = -v.y; }
+    return v;
+}
+
+static constexpr int FINF = -(1 << 30);  // νInf
+static constexpr int KAVG = -1;          // kSW: momentum average
+enum { CH_P = 0, CH_T = 1, CH_A = 2 };
+enum { SP_P = 0, SP_X = 1, SP_D = 2 };
+
+__host__ __device__ __forceinline__ bool bin(int m, int N) { return m > -N && m < N; }
+__host__ __device__ __forceinline__ bool fin(int n, int N) { return n >= -N && n < N; }
+
+// Problem dimensions, passed by value to every kernel.
+struct Dims {
+    int nG, NG, Nk, L, Nq;
+    int n1, N1, n2O, N2O, n2n, N2n, n3O, N3O, n3n, N3n;
+    int nPO, NPO, nPn, NPn;
+    int nRO, NRO, nRn, NRn;
+    int local;
+    double T, U;
+};
+
+// One channel's K1/K2/K3 and their momentum averages (A* alias K* for the local solver).
+struct ChanP {
+    const cplx* K1;
+    const cplx* K2;
+    const cplx* K3;
+    const cplx* A1;
+    const cplx* A2;
+    const cplx* A3;
+};
+// Target vertex F: RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x) + γp + γt + γa
+struct VertP {
+    ChanP g[3];
+    const cplx* Fp_p;
+    const cplx* Fp_x;
+    const cplx* Ft_p;
+    const cplx* Ft_x;
+};
+
+__device__ __forceinline__ size_t ix1(const Dims& d, int P, int m) { return (size_t)P * d.N1 + (m + d.n1 - 1); }
+__device__ __forceinline__ size_t ix2(const Dims& d, int P, int m, int n) {
+    return ((size_t)P * d.N2O + (m + d.n2O - 1)) * d.N2n + (n + d.n2n);
+}
+__device__ __forceinline__ size_t ix3(const Dims& d, int P, int m, int n, int np) {
+    return (((size_t)P * d.N3O + (m + d.n3O - 1)) * d.N3n + (n + d.n3n)) * d.N3n + (np + d.n3n);
+}
+__device__ __forceinline__ size_t ixPi(const Dims& d, int P, int m, int n) {
+    return ((size_t)P * d.NPO + (m + d.nPO - 1)) * d.NPn + (n + d.nPn);
+}
+__device__ __forceinline__ size_t ixG(const Dims& d, int k, int n) { return (size_t)k * d.NG + (n + d.nG); }
+
+__device__ __forceinline__ cplx k1v(const ChanP& c, const Dims& d, int m, int P) {
+    return P == KAVG ? ldg(c.A1 + (m + d.n1 - 1)) : ldg(c.K1 + ix1(d, P, m));
+}
+__device__ __forceinline__ cplx k2v(const ChanP& c, const Dims& d, int m, int n, int P) {
+    return P == KAVG ? ldg(c.A2 + ix2(d, 0, m, n)) : ldg(c.K2 + ix2(d, P, m, n));
+}
+__device__ __forceinline__ cplx k3v(const ChanP& c, const Dims& d, int m, int n, int np, int P) {
+    return P == KAVG ? ldg(c.A3 + ix3(d, 0, m, n, np)) : ldg(c.K3 + ix3(d, P, m, n, np));
+}
+
+// Channel evaluator γ(Ω, ν, ν', P): src/channel.jl:220-339, src/nonlocal/channel.jl:246-382.
+__device__ __forceinline__ cplx chan_eval(const ChanP& c, const Dims& d, int m, int n, int np, int P) {
+    cplx v = mk(0, 0);
+    const bool ninf = (n == FINF), npinf = (np == FINF);
+    if (!bin(m, d.n1)) return v;
+    v += k1v(c, d, m, P);
+    if (!bin(m, d.n2O)) return v;
+    if (!ninf && !npinf) {
+        const bool a = fin(n, d.n2n), b = fin(np, d.n2n);
+        if (a && b) {
+            v += k2v(c, d, m, n, P) + k2v(c, d, m, np, P);
+            if (bin(m, d.n3O) && fin(n, d.n3n) && fin(np, d.n3n)) v += k3v(c, d, m, n, np, P);
+        } else if (a) {
+            v += k2v(c, d, m, n, P);
+        } else if (b) {
+            v += k2v(c, d, m, np, P);
+        }
+    } else if (ninf && !npinf) {
+        if (fin(np, d.n2n)) v += k2v(c, d, m, np, P);
+    } else if (!ninf && npinf) {
+        if (fin(n, d.n2n)) v += k2v(c, d, m, n, P);
+    }
+    return v;
+}
+
+// Frequency conversion between channel representations (src/convention.jl:4-36).
+__device__ __forceinline__ void conv(int from, int to, int m, int n, int np, int& mo, int& no, int& npo) {
+    if (from == to) { mo = m; no = n; npo = np; return; }
+    if (from == CH_P) {
+        if (to == CH_T) { mo = m - n - np - 1; no = np; npo = n; }
+        else            { mo = n - np; no = m - n - 1; npo = np; }
+    } else if (from == CH_T) {
+        if (to == CH_P) { mo = m + n + np + 1; no = np; npo = n; }
+        else            { mo = np - n; no = m + n; npo = n; }
+    } else {
+        if (to == CH_P) { mo = m + np + n + 1; no = m + np; npo = np; }
+        else            { mo = n - np; no = np; npo = m + np; }
+    }
+}
+
+// RefVertex corrections: MeshFunction call, zero outside the box.
+__device__ __forceinline__ cplx ref_call(const cplx* f, const Dims& d, int m, int n, int np) {
+    if (!bin(m, d.nRO) || !fin(n, d.nRn) || !fin(np, d.nRn)) return mk(0, 0);
+    return ldg(f + (size_t)(m + d.nRO - 1) + (size_t)d.NRO * ((size_t)(n + d.nRn) + (size_t)d.NRn * (np + d.nRn)));
+}
+// RefVertex in the parallel spin component (src/refvertex.jl:90-125, 178-216).
+__device__ __forceinline__ cplx ref_pSp(const VertP& F, const Dims& d, int ch, int m, int n, int np) {
+    if (n == FINF || np == FINF) return mk(d.U, 0);
+    if (ch == CH_P) return ref_call(F.Fp_p, d, m, n, np) + mk(d.U, 0);
+    if (ch == CH_T) return ref_call(F.Ft_p, d, m, n, np) + mk(d.U, 0);
+    return mk(d.U, 0) - ref_call(F.Ft_x, d, m, np, n);
+}
+// RefVertex in the crossed spin component (src/refvertex.jl:127-164).
+__device__ __forceinline__ cplx ref_xSp(const VertP& F, const Dims& d, int ch, int m, int n, int np) {
+    if (n == FINF || np == FINF) return mk(-d.U, 0);
+    if (ch == CH_P) return ref_call(F.Fp_x, d, m, n, np) - mk(d.U, 0);
+    if (ch == CH_T) return ref_call(F.Ft_x, d, m, n, np) - mk(d.U, 0);
+    return -ref_call(F.Ft_p, d, m, np, n) - mk(d.U, 0);
+}
+__device__ __forceinline__ cplx ref_eval(const VertP& F, const Dims& d, int ch, int sp, int m, int n, int np) {
+    if (sp == SP_P) return ref_pSp(F, d, ch, m, n, np);
+    if (sp == SP_X) return ref_xSp(F, d, ch, m, n, np);
+    return 2.0 * ref_pSp(F, d, ch, m, n, np) + ref_xSp(F, d, ch, m, n, np);
+}
+
+// Flags of the vertex evaluator: bit 0 F0, bit 1 γp, bit 2 γt, bit 3 γa.
+enum { FL_F0 = 1, FL_GP = 2, FL_GT = 4, FL_GA = 8, FL_ALL = 15 };
+__device__ __forceinline__ int swap_ta(int fl) {
+    return (fl & (FL_F0 | FL_GP)) | ((fl & FL_GA) ? FL_GT : 0) | ((fl & FL_GT) ? FL_GA : 0);
+}
+
+// Vertex in the parallel spin component with momenta (P, kSW, kSW):
+// src/vertex.jl:209-284, src/nonlocal/vertex.jl:69-153, 216-379.
+__device__ __forceinline__ cplx vert_pSp(const VertP& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
+    cplx v = mk(0, 0);
+    if (fl & FL_F0) v += ref_pSp(F, d, ch, m, n, np);
+    if (n == FINF || np == FINF) {
+        const int bit = (ch == CH_P) ? FL_GP : (ch == CH_T ? FL_GT : FL_GA);
+        if (fl & bit) v += chan_eval(F.g[ch], d, m, n, np, P);
+        return v;
+    }
+    const int Pc = (d.Nq == 1) ? 0 : KAVG;
+    if (fl & FL_GP) { int a, b, c; conv(ch, CH_P, m, n, np, a, b, c); v += chan_eval(F.g[CH_P], d, a, b, c, ch == CH_P ? P : Pc); }
+    if (fl & FL_GT) { int a, b, c; conv(ch, CH_T, m, n, np, a, b, c); v += chan_eval(F.g[CH_T], d, a, b, c, ch == CH_T ? P : Pc); }
+    if (fl & FL_GA) { int a, b, c; conv(ch, CH_A, m, n, np, a, b, c); v += chan_eval(F.g[CH_A], d, a, b, c, ch == CH_A ? P : Pc); }
+    return v;
+}
+// Crossed component via crossing symmetry (src/vertex.jl:288-313).
+__device__ __forceinline__ cplx vert_xSp(const VertP& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
+    const int sw = swap_ta(fl);
+    if (ch == CH_P) return -vert_pSp(F, d, CH_P, m, n, (np == FINF) ? FINF : m - np - 1, P, sw);
+    if (ch == CH_T) return -vert_pSp(F, d, CH_A, m, n, np, P, sw);
+    return -vert_pSp(F, d, CH_T, m, n, np, P, sw);
+}
+__device__ __forceinline__ cplx vert_eval(const VertP& F, const Dims& d, int ch, int sp, int m, int n, int np, int P,
+                                          int fl = FL_ALL) {
+    if (sp == SP_P) return vert_pSp(F, d, ch, m, n, np, P, fl);
+    if (sp == SP_X) return vert_xSp(F, d, ch, m, n, np, P, fl);
+    cplx v = vert_pSp(F, d, ch, m, n, np, P, fl) * 2.0;
+    v += vert_xSp(F, d, ch, m, n, np, P, fl);
+    return v;
+}
+
+// FL(Ω, ω, νInf, Ch, Sp): FL has F0 = RefVertex(0) and K1 = 0, so only its K2 survives.
+__device__ __forceinline__ cplx fl_right(const cplx* FLK2p, const cplx* FLK2t, const cplx* FLK2a, const Dims& d,
+                                         int ch, int m, int n, int P) {
+    if (!bin(m, d.n2O) || !fin(n, d.n2n)) return mk(0, 0);
+    const size_t i = ix2(d, P, m, n);
+    if (ch == CH_P) return ldg(FLK2p + i);
+    if (ch == CH_A) return ldg(FLK2a + i);
+    return 2.0 * ldg(FLK2t + i) - ldg(FLK2a + i);  // dSp = 2 pSp + xSp, xSp(t) = -pSp(a)
+}
+
+__device__ __forceinline__ int cross(int ch, int m, int n) { return ch == CH_P ? m - n - 1 : n; }
+
+// warp reduction of a complex double
+__device__ __forceinline__ cplx warp_sum(cplx v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+}  // namespace fdga

@@ -1,0 +1,750 @@
+// fdga_kernels.cu -- sm_103a kernels of one parquet iteration (FP64 plain path).
+//
+// Each kernel restates one reference function (cited per kernel).  Work items of the
+// symmetry-grouped sums are class representatives (device indices); the remaining elements
+// are filled by k_expand with the class operation, as MatsubaraFunctions' SymmetryGroup does.
+#include "fdga_device.cuh"
+#include "fdga_kernels.h"
+
+#include <algorithm>
+
+namespace fdga {
+
+// ---------------------------------------------------------------------------------------------
+// Elementwise: Dyson G = 1/(1/Gbare + Σ)  (src/dyson.jl:5-31; G, Σ store iG, iΣ)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_dyson(cplx* G, const cplx* Sig, const cplx* Gb, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const cplx one = mk(1.0, 0.0);
+    G[i] = cdiv(one, cdiv(one, Gb[i]) + Sig[i]);
+}
+
+// n = 1/2 + T Im(Σ G) / Nk  (src/dyson.jl:33-41); single block, deterministic order.
+__global__ void k_occupation(const cplx* G, size_t n, double T, int Nk, double* out) {
+    __shared__ double red[1024];
+    double s = 0.0;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) s += G[i].y;
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = 0.5 + red[0] * T / (double)Nk;
+}
+
+// ---------------------------------------------------------------------------------------------
+// G(R) = (1/N) Σ_k G(k) e^{-2πi k·R/L}  (fft(...)/L² of src/nonlocal/bubble.jl:110-111)
+// tw[j] = e^{-2πi j/L}, j < L.   GR layout [R][ν]
+// ---------------------------------------------------------------------------------------------
+__global__ void k_g_realspace(const cplx* G, cplx* GR, const cplx* tw, Dims d) {
+    const int NR = d.L * d.L;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= (size_t)NR * d.NG) return;
+    const int nu = (int)(i % d.NG), R = (int)(i / d.NG);
+    const int Rx = R % d.L, Ry = R / d.L;
+    cplx s = mk(0, 0);
+    for (int k = 0; k < NR; ++k) {
+        const int kx = k % d.L, ky = k / d.L;
+        const int ph = (kx * Rx + ky * Ry) % d.L;
+        s += G[(size_t)k * d.NG + nu] * tw[ph];
+    }
+    GR[i] = s * (1.0 / NR);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Local bubbles Πpp(Ω,ν) = G(ν) G(Ω-ν), Πph(Ω,ν) = G(ν) G(Ω+ν), G -> 1/ν outside its box
+// (src/bubble.jl:9-36).
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ cplx g_tail(const cplx* G, const Dims& d, int k, int n) {
+    if (fin(n, d.nG)) return G[ixG(d, k, n)];
+    return mk(1.0 / ((2.0 * n + 1.0) * M_PI * d.T), 0.0);
+}
+
+__global__ void k_bubble_local(const cplx* G, cplx* pp, cplx* ph, Dims d) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= (size_t)d.NPO * d.NPn) return;
+    const int n = (int)(i % d.NPn) - d.nPn, m = (int)(i / d.NPn) - (d.nPO - 1);
+    const cplx Gn = g_tail(G, d, 0, n);
+    pp[i] = Gn * g_tail(G, d, 0, m - n - 1);
+    ph[i] = Gn * g_tail(G, d, 0, m + n);
+}
+
+// Nonlocal bubbles in real space (src/nonlocal/bubble.jl:87-158) for L_G = L:
+//   Πpp(R) = G(R, Ω-ν) G(R, ν),  Πph(R) = G(R, Ω+ν) G(-R, ν),  R = 0 with the 1/ν tail,
+//   Π(P) = Σ_R Π(R) e^{+2πi P·R/L}  (bfft).  For L_G = L the ±L/2 half weights of the reference's
+//   R scan sum to one per lattice site, so the scan is one pass over the L x L sites.
+// One CTA = one Ω and a tile of TV fermionic frequencies; shared: Π(R) then the P transform.
+__global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp, Dims d, int TV) {
+    extern __shared__ cplx sh[];
+    const int L = d.L, NR = L * L;
+    cplx* A = sh;                     // [2][TV][NR]   (pp, ph) in R
+    cplx* B = sh + 2 * (size_t)TV * NR;  // [2][TV][NR]  after the x transform
+    const int m = blockIdx.y - (d.nPO - 1);
+    const int n0 = blockIdx.x * TV - d.nPn;
+    for (int e = threadIdx.x; e < TV * NR; e += blockDim.x) {
+        const int v = e / NR, R = e % NR;
+        const int n = n0 + v;
+        cplx vpp = mk(0, 0), vph = mk(0, 0);
+        if (n < d.nPn) {
+            const int Rx = R % L, Ry = R / L;
+            const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
+            if (R == 0) {
+                vpp = g_tail(GR, d, 0, m - n - 1) * g_tail(GR, d, 0, n);
+                vph = g_tail(GR, d, 0, m + n) * g_tail(GR, d, 0, n);
+            } else {
+                const int a = m - n - 1, b = m + n;
+                if (fin(a, d.nG) && fin(n, d.nG)) vpp = GR[ixG(d, R, a)] * GR[ixG(d, R, n)];
+                if (fin(b, d.nG) && fin(n, d.nG)) vph = GR[ixG(d, R, b)] * GR[ixG(d, mR, n)];
+            }
+        }
+        A[(size_t)v * NR + R] = vpp;
+        A[(size_t)(TV + v) * NR + R] = vph;
+    }
+    __syncthreads();
+    // transform along x: B[v][Py*L + Px] = Σ_x A[v][y*L + x] w^{Px x}, stored as (Px, y)
+    for (int e = threadIdx.x; e < 2 * TV * NR; e += blockDim.x) {
+        const int row = e / NR, r = e % NR;
+        const int Px = r % L, y = r / L;
+        const cplx* a = A + (size_t)row * NR + (size_t)y * L;
+        cplx s = mk(0, 0);
+        for (int x = 0; x < L; ++x) s += a[x] * twp[(Px * x) % L];
+        B[(size_t)row * NR + r] = s;
+    }
+    __syncthreads();
+    // transform along y and write Π[P][Ω][ν]
+    for (int e = threadIdx.x; e < 2 * TV * NR; e += blockDim.x) {
+        const int v = e % TV;               // ν fastest across threads for coalesced stores
+        const int rest = e / TV;
+        const int P = rest % NR, which = rest / NR;
+        const int Px = P % L, Py = P / L;
+        const int n = n0 + v;
+        if (n >= d.nPn) continue;
+        const cplx* b = B + (size_t)(which * TV + v) * NR;
+        cplx s = mk(0, 0);
+        for (int y = 0; y < L; ++y) s += b[(size_t)y * L + Px] * twp[(Py * y) % L];
+        (which ? ph : pp)[ixPi(d, P, m, n)] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Momentum averages A = Σ_P K[P] / Nq (s-wave evaluation, src/nonlocal/swave.jl:32-72)
+// blockIdx.y = channel*3 + class
+// ---------------------------------------------------------------------------------------------
+__global__ void k_qavg(const ChanArrays in, ChanArraysW out, Dims d) {
+    const int ch = blockIdx.y / 3, cl = blockIdx.y % 3;
+    const size_t per = cl == 0 ? (size_t)d.N1 : (cl == 1 ? (size_t)d.N2O * d.N2n : (size_t)d.N3O * d.N3n * d.N3n);
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= per) return;
+    const cplx* src = cl == 0 ? in.K1[ch] : (cl == 1 ? in.K2[ch] : in.K3[ch]);
+    cplx* dst = cl == 0 ? out.K1[ch] : (cl == 1 ? out.K2[ch] : out.K3[ch]);
+    cplx s = mk(0, 0);
+    for (int P = 0; P < d.Nq; ++P) s += src[(size_t)P * per + i];
+    dst[i] = s * (1.0 / d.Nq);
+}
+
+// ---------------------------------------------------------------------------------------------
+// K3 caches (src/build_K3_cache.jl:20-95, src/nonlocal/build_K3_cache.jl:18-94).
+// One thread per K3 mesh point (P, Ω, a, b); "left" caches use (Ω, ω=a, ν'=b),
+// "right" caches (Ω, ν=a, ω=b).  Output order: Γpx F0p F0a F0t Γpp Γa Γt Fp Fa Ft.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_build_cache(VertP F, Caches C, Dims d) {
+    const size_t n3 = (size_t)d.Nq * d.N3O * d.N3n * d.N3n;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n3) return;
+    const int b = (int)(i % d.N3n) - d.n3n;
+    const int a = (int)((i / d.N3n) % d.N3n) - d.n3n;
+    const int m = (int)((i / ((size_t)d.N3n * d.N3n)) % d.N3O) - (d.n3O - 1);
+    const int P = (int)(i / ((size_t)d.N3n * d.N3n * d.N3O));
+    // left
+    C.c[0][i] = vert_eval(F, d, CH_P, SP_X, m, a, b, P, FL_GT | FL_GA);
+    C.c[1][i] = ref_xSp(F, d, CH_P, m, a, b) - ref_xSp(F, d, CH_P, m, a, FINF);
+    const cplx f0a = ref_pSp(F, d, CH_A, m, a, b) - ref_pSp(F, d, CH_A, m, a, FINF);
+    const cplx f0t = ref_pSp(F, d, CH_T, m, a, b) - ref_pSp(F, d, CH_T, m, a, FINF);
+    C.c[2][i] = f0a;
+    C.c[3][i] = 2.0 * f0t - f0a;
+    // right
+    const cplx gpp = vert_pSp(F, d, CH_P, m, a, b, P, FL_GT | FL_GA);
+    const cplx ga = vert_pSp(F, d, CH_A, m, a, b, P, FL_GP | FL_GT);
+    const cplx gt = vert_pSp(F, d, CH_T, m, a, b, P, FL_GP | FL_GA);
+    const cplx fp = vert_pSp(F, d, CH_P, m, a, b, P, FL_F0 | FL_GP) - vert_pSp(F, d, CH_P, m, FINF, b, P, FL_F0 | FL_GP) + gpp;
+    const cplx fa = vert_pSp(F, d, CH_A, m, a, b, P, FL_F0 | FL_GA) - vert_pSp(F, d, CH_A, m, FINF, b, P, FL_F0 | FL_GA) + ga;
+    const cplx ft = vert_pSp(F, d, CH_T, m, a, b, P, FL_F0 | FL_GT) - vert_pSp(F, d, CH_T, m, FINF, b, P, FL_F0 | FL_GT) + gt;
+    C.c[4][i] = gpp;
+    C.c[5][i] = ga;
+    C.c[6][i] = gt * 2.0 - ga;
+    C.c[7][i] = fp;
+    C.c[8][i] = fa;
+    C.c[9][i] = ft * 2.0 - fa;
+}
+
+// ---------------------------------------------------------------------------------------------
+// K1 BSE (src/BSEa/BSEa_K1.jl:2-54, src/nonlocal/BSEa/BSEa_K1.jl:2-57), warp per item:
+//   K1(Ω,P) = T s Σ_ω F(Ω,∞,ω) [(Π-Π0)(Ω,ω) U + Π(Ω,ω) FL(Ω,ω̃,∞)]
+// ---------------------------------------------------------------------------------------------
+template <int CH>
+__global__ void k_bse_K1(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, cplx* out, const int* items, int nitems,
+                         Dims d) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nitems) return;
+    const int idx = items ? items[w] : w;
+    const int m = idx % d.N1 - (d.n1 - 1), P = idx / d.N1;
+    constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
+    cplx acc = mk(0, 0);
+    for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
+        const int wt = cross(CH, m, n);
+        const cplx Fl = vert_eval(F, d, CH, SP, m, FINF, n, P);
+        const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
+        const size_t ip = ixPi(d, P, m, n);
+        const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
+        acc += Fl * ((pi - pi0) * d.U + pi * FLr);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) out[idx] = acc * (d.T * (CH == CH_T ? -1.0 : 1.0));
+}
+
+// ---------------------------------------------------------------------------------------------
+// Left K2 BSE (fdPA), warp per item:
+//   local (src/BSEa/BSEa_K2.jl:1-40):        Σ_{ω∈Π mesh} Γ_irr(Ω,ν,ω) Π0(Ω,ω) U
+//   nonlocal (src/nonlocal/BSEa/BSEa_K2.jl:1-39): Σ_{ω∈K2 mesh} Γ_irr(Ω,ν,ω̃) Π0(Ω,ω) U
+// ---------------------------------------------------------------------------------------------
+template <int CH>
+__global__ void k_bse_L_K2(VertP F, const cplx* Pi0, cplx* out, const int* items, int nitems, Dims d) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nitems) return;
+    const int idx = items ? items[w] : w;
+    const int nu = idx % d.N2n - d.n2n;
+    const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
+    const int P = idx / (d.N2n * d.N2O);
+    constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
+    constexpr int IRR = (CH == CH_P) ? (FL_GT | FL_GA) : (CH == CH_T ? (FL_GP | FL_GA) : (FL_GP | FL_GT));
+    cplx acc = mk(0, 0);
+    if (d.local) {
+        for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
+            const cplx Gp = vert_eval(F, d, CH, SP, m, nu, n, P, IRR);
+            acc += Gp * ldg(Pi0 + ixPi(d, P, m, n)) * d.U;
+        }
+    } else {
+        for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
+            const cplx Gl = vert_eval(F, d, CH, SP, m, nu, cross(CH, m, n), P, IRR);
+            acc += Gl * ldg(Pi0 + ixPi(d, P, m, n)) * d.U;
+        }
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) out[idx] = acc * (d.T * (CH == CH_T ? -1.0 : 1.0));
+}
+
+// ---------------------------------------------------------------------------------------------
+// K2 BSE (src/BSEa/BSEa_K2.jl:43-103, src/nonlocal/BSEa/BSEa_K2.jl:43-105), warp per item:
+//   T s Σ_ω [F(Ω,ν,ω) - F(Ω,∞,ω)] [(Π-Π0)(Ω,ω) U + Π(Ω,ω) FL(Ω,ω̃,∞)]
+// ---------------------------------------------------------------------------------------------
+template <int CH>
+__global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, cplx* out, const int* items, int nitems,
+                         Dims d) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nitems) return;
+    const int idx = items ? items[w] : w;
+    const int nu = idx % d.N2n - d.n2n;
+    const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
+    const int P = idx / (d.N2n * d.N2O);
+    constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
+    cplx acc = mk(0, 0);
+    for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
+        const int wt = cross(CH, m, n);
+        const cplx Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - vert_eval(F, d, CH, SP, m, FINF, n, P);
+        const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
+        const size_t ip = ixPi(d, P, m, n);
+        const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
+        acc += Fl * ((pi - pi0) * d.U + pi * FLr);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) out[idx] = acc * (d.T * (CH == CH_T ? -1.0 : 1.0));
+}
+
+// ---------------------------------------------------------------------------------------------
+// K3 BSE as one complex GEMM per (P, Ω) block, C = A·M (src/BSEa/BSEa_K3.jl:1-128,
+// src/nonlocal/BSEa/BSEa_K3.jl:1-128):
+//   MODE 0 (BSE_L_K3):  A = cacheΓ(ν,ω),  M(ω,ν') = Π0(ω) cacheF0(ω,ν');          out = T s C
+//   MODE 1 (BSE_K3):    A = cacheF(ν,ω),  M(ω,ν') = s1[(Π-Π0)(ω) cacheF0(ω,ν') + Π(ω) Γs(ω,ν')]
+//                                                    + s2 Π(ω) γL(ω̃,ν')[ω̃ in box]; out = T C + γL(ν,ν')
+// 32x32 output tile, 16x16 threads with 2x2 outputs each, K chunks of 8.
+// ---------------------------------------------------------------------------------------------
+template <int MODE, int CH>
+__global__ void __launch_bounds__(256) k_bse_K3_gemm(K3Args a, Dims d) {
+    constexpr int TM = 32, TK = 8;
+    __shared__ cplx As[TM][TK + 1];
+    __shared__ cplx Ms[TK][TM + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int col0 = blockIdx.x * TM, row0 = blockIdx.y * TM;
+    const int blk = blockIdx.z;  // P * N3O + iΩ
+    const int m = blk % d.N3O - (d.n3O - 1), P = blk / d.N3O;
+    const int N = d.N3n;
+    const size_t base = (size_t)blk * N * N;
+    const double s1 = (CH == CH_A) ? 1.0 : -1.0, s2 = (CH == CH_T) ? -1.0 : 1.0;
+    cplx acc[2][2] = {{mk(0, 0), mk(0, 0)}, {mk(0, 0), mk(0, 0)}};
+    for (int k0 = 0; k0 < N; k0 += TK) {
+        {  // A tile: 32 x 8, one element per thread
+            const int r = threadIdx.x / TK, kk = threadIdx.x % TK;
+            const int row = row0 + r, k = k0 + kk;
+            As[r][kk] = (row < N && k < N) ? ldg(a.A + base + (size_t)row * N + k) : mk(0, 0);
+        }
+        {  // M tile: 8 x 32
+            const int kk = threadIdx.x / TM, c = threadIdx.x % TM;
+            const int k = k0 + kk, col = col0 + c;
+            cplx v = mk(0, 0);
+            if (k < N && col < N) {
+                const int o = k - d.n3n;  // ω as fermion index
+                const size_t ip = ixPi(d, P, m, o);
+                const cplx pi0 = ldg(a.Pi0 + ip);
+                const cplx f0 = ldg(a.B0 + base + (size_t)k * N + col);
+                if (MODE == 0) {
+                    v = pi0 * f0;
+                } else {
+                    const cplx pi = ldg(a.Pi + ip);
+                    const cplx gs = (CH == CH_P) ? ldg(a.G + base + (size_t)k * N + col) : ldg(a.G + base + (size_t)col * N + k);
+                    v = ((pi - pi0) * f0 + pi * gs) * s1;
+                    const int ot = cross(CH, m, o);
+                    if (fin(ot, d.n3n)) {
+                        const size_t il = base + (size_t)(ot + d.n3n) * N + col;
+                        const cplx gl = (CH == CH_T) ? 2.0 * ldg(a.FLt + il) - ldg(a.FLa + il) : ldg(a.FLc + il);
+                        v += pi * gl * s2;
+                    }
+                }
+            }
+            Ms[kk][c] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < TK; ++kk) {
+            const cplx a0 = As[ty][kk], a1 = As[ty + 16][kk];
+            const cplx b0 = Ms[kk][tx], b1 = Ms[kk][tx + 16];
+            acc[0][0] += a0 * b0;
+            acc[0][1] += a0 * b1;
+            acc[1][0] += a1 * b0;
+            acc[1][1] += a1 * b1;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int row = row0 + ty + 16 * i, col = col0 + tx + 16 * j;
+            if (row >= N || col >= N) continue;
+            const size_t io = base + (size_t)row * N + col;
+            if (MODE == 0) {
+                a.out[io] = acc[i][j] * (d.T * ((CH == CH_A) ? 1.0 : -1.0));
+            } else {
+                const cplx gl = (CH == CH_T) ? 2.0 * ldg(a.FLt + io) - ldg(a.FLa + io) : ldg(a.FLc + io);
+                a.out[io] = acc[i][j] * d.T + gl;
+            }
+        }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Symmetry expansion: X[i] = op(X[rep(i)]) for every non-representative i; map = rep*4 + op.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_expand(cplx* X, const uint32_t* map, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t e = map[i];
+    const size_t r = e >> 2;
+    if (r == i) return;
+    X[i] = apply_op((int)(e & 3u), X[r]);
+}
+
+// out = (out + other) * 0.5   (t-channel pSp recombination, src/BSE_templates.jl:35-38)
+__global__ void k_half_sum(cplx* out, const cplx* other, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = (out[i] + other[i]) * 0.5;
+}
+// K2 epilogue of BSE_K2!: a,p: K2 += FL.K2;  t: K2 += 2 FLt.K2 - FLa.K2, then (K2 + K2a)/2
+__global__ void k_k2_epilogue(cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa, const cplx* outA, int ch,
+                              size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cplx v = out[i];
+    if (ch == CH_T) {
+        v += FLt[i] * 2.0;
+        v += FLa[i] * -1.0;
+        v = (v + outA[i]) * 0.5;
+    } else {
+        v += FLc[i];
+    }
+    out[i] = v;
+}
+
+// ---------------------------------------------------------------------------------------------
+// SDE: L_pp, L_ph (src/SDE.jl:79-217, src/nonlocal/SDE.jl:3-143), warp per item.
+//   vertex part:    L_pp = T U Σ_ω Πpp(Ω,ω) γp(Ω,Ω-ω,ν),  L_ph = T U Σ_ω Πph(Ω,ω) (γt+γa)(Ω,ν,ω)
+//   RefVertex part: L_pp = T U Σ_ω Πpp (F0_p(Ω,Ω-ω,ν) - U),  L_ph = T U Σ_ω Πph (F0_a + F0_t - 2U)
+// WHICH: 0 = pp, 1 = ph.  REF: 0 vertex, 1 RefVertex.  out = vertex part + ref part / 3 is formed
+// by the caller through 'scale'.
+// ---------------------------------------------------------------------------------------------
+template <int WHICH, int REF>
+__global__ void k_sde_L(VertP F, const cplx* Pi, cplx* out, const int* items, int nitems, double scale, int accumulate,
+                        Dims d) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nitems) return;
+    const int idx = items ? items[w] : w;
+    const int nu = idx % d.N2n - d.n2n;
+    const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
+    const int P = idx / (d.N2n * d.N2O);
+    cplx acc = mk(0, 0);
+    for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
+        const cplx up = ldg(Pi + ixPi(d, P, m, n)) * d.U;
+        cplx g;
+        if (REF == 0) {
+            if (WHICH == 0) g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P);
+            else g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P);
+        } else {
+            if (WHICH == 0) g = ref_pSp(F, d, CH_P, m, m - n - 1, nu) - mk(d.U, 0);
+            else g = ref_pSp(F, d, CH_A, m, nu, n) + ref_pSp(F, d, CH_T, m, nu, n) - mk(d.U, 0) - mk(d.U, 0);
+        }
+        acc += up * g;
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+        const cplx v = acc * (d.T * scale);
+        out[idx] = accumulate ? out[idx] + v : v;
+    }
+}
+
+// Σ_inner(ν,k) = T/N Σ_{Ω,P} [G(Ω-ν, P-k) Lpp(Ω,ν,P) + G(Ω+ν, P+k) Lph(Ω,ν,P)]
+// (momentum-space form of src/nonlocal/SDE.jl:208-280 for L_G = L; local: src/SDE.jl:241-263)
+__global__ void k_sde_sigma(const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, Dims d) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= (size_t)d.Nk * d.NG) return;
+    const int nu = (int)(i % d.NG) - d.nG, k = (int)(i / d.NG);
+    cplx acc = mk(0, 0);
+    if (fin(nu, d.n2n)) {
+        const int L = d.L, kx = k % L, ky = k / L;
+        for (int P = 0; P < d.Nq; ++P) {
+            const int Px = P % L, Py = P / L;
+            const int kmP = ((Px - kx + L) % L) + L * ((Py - ky + L) % L);
+            const int kpP = ((Px + kx) % L) + L * ((Py + ky) % L);
+            for (int m = -(d.n2O - 1); m <= d.n2O - 1; ++m) {
+                const size_t il = ix2(d, P, m, nu);
+                const int a = m - nu - 1, b = m + nu;
+                if (fin(a, d.nG)) acc += G[ixG(d, kmP, a)] * Lpp[il];
+                if (fin(b, d.nG)) acc += G[ixG(d, kpP, b)] * Lph[il];
+            }
+        }
+    }
+    S[i] = acc * (d.T / d.Nq);
+}
+
+// U² term (src/SDE.jl:328-364, src/nonlocal/SDE.jl:400-447), factorised:
+//   C_R(s) = Σ_{n1} G(-R, n1) G(R, n1 + s);   Σ_U²(ν, R) = U² T² Σ_{n2} G(R, n2) C_R(ν - n2)
+// GR layout [R][ν] (G(R)); s in [-(2nG-1), 2nG-1].
+__global__ void k_u2_corr(const cplx* GR, cplx* C, Dims d) {
+    const int NS = 2 * d.NG - 1;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int NR = d.L * d.L;
+    if (i >= (size_t)NR * NS) return;
+    const int s = (int)(i % NS) - (d.NG - 1), R = (int)(i / NS);
+    const int L = d.L, Rx = R % L, Ry = R / L;
+    const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
+    cplx acc = mk(0, 0);
+    for (int n1 = -d.nG; n1 < d.nG; ++n1) {
+        const int n3 = n1 + s;
+        if (!fin(n3, d.nG)) continue;
+        acc += GR[ixG(d, mR, n1)] * GR[ixG(d, R, n3)];
+    }
+    C[i] = acc;
+}
+__global__ void k_u2_sum(const cplx* GR, const cplx* C, cplx* out, Dims d) {
+    const int NS = 2 * d.NG - 1;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int NR = d.L * d.L;
+    if (i >= (size_t)NR * d.NG) return;
+    const int nu = (int)(i % d.NG) - d.nG, R = (int)(i / d.NG);
+    cplx acc = mk(0, 0);
+    for (int n2 = -d.nG; n2 < d.nG; ++n2) {
+        const int s = nu - n2;  // in [-(2nG-1), 2nG-1]
+        acc += GR[ixG(d, R, n2)] * C[(size_t)R * NS + (s + d.NG - 1)];
+    }
+    out[i] = acc * (d.U * d.U * d.T * d.T);
+}
+// out[k][ν] = Σ_R e^{+2πi k·R/L} in[R][ν]   (bfft over the momentum axes); twc[j] = e^{+2πi j/L}
+__global__ void k_R_to_k(const cplx* in, cplx* out, const cplx* twc, Dims d) {
+    const int NR = d.L * d.L;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= (size_t)NR * d.NG) return;
+    const int nu = (int)(i % d.NG), k = (int)(i / d.NG);
+    const int kx = k % d.L, ky = k / d.L;
+    cplx s = mk(0, 0);
+    for (int R = 0; R < NR; ++R) {
+        const int Rx = R % d.L, Ry = R / d.L;
+        s += in[(size_t)R * d.NG + nu] * twc[(kx * Rx + ky * Ry) % d.L];
+    }
+    out[i] = s;
+}
+
+// Σ assembly (src/SDE.jl:3-33, 219-283): Σ = op(Σin + Σ_U²)[rep] + H  (+ fdPA: - C0 + Σ0 - H0)
+__global__ void k_sigma_assemble(const cplx* Sin, const cplx* SU2, const uint32_t* map, const double* occ,
+                                 const cplx* C0, const cplx* Sig0, cplx* Sig, double U, int hartree, int fdpa,
+                                 double n0, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t r = i;
+    int op = 0;
+    if (map) { const uint32_t e = map[i]; r = e >> 2; op = (int)(e & 3u); }
+    cplx v = apply_op(op, Sin[r] + SU2[r]);
+    if (hartree) v += mk(0.0, (*occ - 0.5) * U);
+    if (fdpa) {
+        v = v + (C0[i] * -1.0);
+        v += Sig0[i];
+        if (hartree) v = v + mk(0.0, -(n0 - 0.5) * U) + mk(0.0, -(n0 - 0.5) * U);
+    }
+    Sig[i] = v;
+}
+
+// ---------------------------------------------------------------------------------------------
+// State-vector helpers
+// ---------------------------------------------------------------------------------------------
+__global__ void k_gather(cplx* dst, const cplx* src, const uint32_t* perm, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[perm[i]];
+}
+__global__ void k_scatter(cplx* dst, const cplx* src, const uint32_t* perm, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[perm[i]] = src[i];
+}
+// fx = y - x ; g = x + beta fx ; partial max|fx| per block
+__global__ void k_residual(const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax, size_t n) {
+    __shared__ double red[256];
+    double mx = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const cplx f = y[i] - x[i];
+        fx[i] = f;
+        if (g) g[i] = x[i] + f * beta;
+        mx = fmax(mx, hypot(f.x, f.y));
+    }
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) pmax[blockIdx.x] = red[0];
+}
+// partial sums of conj(a)·b per block
+__global__ void k_dot(const cplx* a, const cplx* b, cplx* part, size_t n) {
+    __shared__ double rx[256], ry[256];
+    double sx = 0.0, sy = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const cplx u = a[i], v = b[i];
+        sx += u.x * v.x + u.y * v.y;
+        sy += u.x * v.y - u.y * v.x;
+    }
+    rx[threadIdx.x] = sx;
+    ry[threadIdx.x] = sy;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) { rx[threadIdx.x] += rx[threadIdx.x + o]; ry[threadIdx.x] += ry[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = mk(rx[0], ry[0]);
+}
+// y += a * x (complex a)
+__global__ void k_axpy(cplx* y, const cplx* x, cplx a, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+// y = a * y + b * x
+__global__ void k_rot(cplx* qa, cplx* qb, double c, cplx s, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const cplx a = qa[i], b = qb[i];
+    qa[i] = a * c + conjg(s) * b;
+    qb[i] = (-s) * a + b * c;
+}
+__global__ void k_sub(cplx* out, const cplx* a, const cplx* b, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] - b[i];
+}
+__global__ void k_scale(cplx* out, const cplx* a, double s, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] * s;
+}
+// count of non-finite values
+__global__ void k_nonfinite(const cplx* a, size_t n, unsigned int* count) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n && !(isfinite(a[i].x) && isfinite(a[i].y))) atomicAdd(count, 1u);
+}
+
+// =============================================================================================
+// Launchers
+// =============================================================================================
+static inline unsigned blocks_for(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+#define LAUNCH_CHECK() do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return e_; } while (0)
+
+cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n) {
+    k_dyson<<<blocks_for(n, 256), 256, 0, s>>>(G, Sig, Gb, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_occupation(cudaStream_t s, const cplx* G, size_t n, double T, int Nk, double* out) {
+    k_occupation<<<1, 1024, 0, s>>>(G, n, T, Nk, out);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_g_realspace(cudaStream_t s, const cplx* G, cplx* GR, const cplx* tw, const Dims& d) {
+    const size_t n = (size_t)d.L * d.L * d.NG;
+    k_g_realspace<<<blocks_for(n, 128), 128, 0, s>>>(G, GR, tw, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+int bubble_tile(const Dims& d) {
+    const int NR = d.L * d.L;
+    int tv = 32;
+    while (tv > 1 && (size_t)4 * tv * NR * sizeof(cplx) > 160 * 1024) tv >>= 1;
+    return tv;
+}
+cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
+                          const Dims& d) {
+    if (d.local) {
+        const size_t n = (size_t)d.NPO * d.NPn;
+        k_bubble_local<<<blocks_for(n, 256), 256, 0, s>>>(G, pp, ph, d);
+    } else {
+        const int tv = bubble_tile(d);
+        const size_t shm = (size_t)4 * tv * d.L * d.L * sizeof(cplx);
+        static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
+        if (shm > 48 * 1024 && shm > shm_set) {
+            cudaFuncSetAttribute(k_bubble_nl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+            shm_set = shm;
+        }
+        dim3 grid((d.NPn + tv - 1) / tv, d.NPO);
+        k_bubble_nl<<<grid, 256, shm, s>>>(GR, pp, ph, twp, d, tv);
+    }
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d) {
+    const size_t per = std::max((size_t)d.N1, std::max((size_t)d.N2O * d.N2n, (size_t)d.N3O * d.N3n * d.N3n));
+    dim3 grid(blocks_for(per, 256), 9);
+    k_qavg<<<grid, 256, 0, s>>>(in, out, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const Dims& d) {
+    const size_t n = (size_t)d.Nq * d.N3O * d.N3n * d.N3n;
+    k_build_cache<<<blocks_for(n, 128), 128, 0, s>>>(F, C, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+                          cplx* out, const int* items, int nitems, const Dims& d) {
+    const unsigned g = blocks_for((size_t)nitems * 32, 128);
+    if (ch == CH_P) k_bse_K1<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    else if (ch == CH_T) k_bse_K1<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    else k_bse_K1<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* Pi0, cplx* out, const int* items,
+                            int nitems, const Dims& d) {
+    const unsigned g = blocks_for((size_t)nitems * 32, 128);
+    if (ch == CH_P) k_bse_L_K2<CH_P><<<g, 128, 0, s>>>(F, Pi0, out, items, nitems, d);
+    else if (ch == CH_T) k_bse_L_K2<CH_T><<<g, 128, 0, s>>>(F, Pi0, out, items, nitems, d);
+    else k_bse_L_K2<CH_A><<<g, 128, 0, s>>>(F, Pi0, out, items, nitems, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_bse_K2(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+                          cplx* out, const int* items, int nitems, const Dims& d) {
+    const unsigned g = blocks_for((size_t)nitems * 32, 128);
+    if (ch == CH_P) k_bse_K2<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    else if (ch == CH_T) k_bse_K2<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    else k_bse_K2<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, int ch, const K3Args& a, const Dims& d) {
+    dim3 grid((d.N3n + 31) / 32, (d.N3n + 31) / 32, d.Nq * d.N3O);
+    if (mode == 0) {
+        if (ch == CH_P) k_bse_K3_gemm<0, CH_P><<<grid, 256, 0, s>>>(a, d);
+        else if (ch == CH_T) k_bse_K3_gemm<0, CH_T><<<grid, 256, 0, s>>>(a, d);
+        else k_bse_K3_gemm<0, CH_A><<<grid, 256, 0, s>>>(a, d);
+    } else {
+        if (ch == CH_P) k_bse_K3_gemm<1, CH_P><<<grid, 256, 0, s>>>(a, d);
+        else if (ch == CH_T) k_bse_K3_gemm<1, CH_T><<<grid, 256, 0, s>>>(a, d);
+        else k_bse_K3_gemm<1, CH_A><<<grid, 256, 0, s>>>(a, d);
+    }
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_expand(cudaStream_t s, cplx* X, const uint32_t* map, size_t n) {
+    k_expand<<<blocks_for(n, 256), 256, 0, s>>>(X, map, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_half_sum(cudaStream_t s, cplx* out, const cplx* other, size_t n) {
+    k_half_sum<<<blocks_for(n, 256), 256, 0, s>>>(out, other, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa,
+                               const cplx* outA, int ch, size_t n) {
+    k_k2_epilogue<<<blocks_for(n, 256), 256, 0, s>>>(out, FLc, FLt, FLa, outA, ch, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_sde_L(cudaStream_t s, int which, int ref, const VertP& F, const cplx* Pi, cplx* out,
+                         const int* items, int nitems, double scale, int accumulate, const Dims& d) {
+    const unsigned g = blocks_for((size_t)nitems * 32, 128);
+    if (which == 0 && ref == 0) k_sde_L<0, 0><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
+    else if (which == 1 && ref == 0) k_sde_L<1, 0><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
+    else if (which == 0) k_sde_L<0, 1><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
+    else k_sde_L<1, 1><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, const Dims& d) {
+    const size_t n = (size_t)d.Nk * d.NG;
+    k_sde_sigma<<<blocks_for(n, 64), 64, 0, s>>>(G, Lpp, Lph, S, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_u2(cudaStream_t s, const cplx* GR, cplx* C, cplx* SR, cplx* out, const cplx* twc, const Dims& d) {
+    const int NR = d.L * d.L, NS = 2 * d.NG - 1;
+    k_u2_corr<<<blocks_for((size_t)NR * NS, 128), 128, 0, s>>>(GR, C, d);
+    LAUNCH_CHECK();
+    k_u2_sum<<<blocks_for((size_t)NR * d.NG, 128), 128, 0, s>>>(GR, C, SR, d);
+    LAUNCH_CHECK();
+    k_R_to_k<<<blocks_for((size_t)NR * d.NG, 128), 128, 0, s>>>(SR, out, twc, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_sigma_assemble(cudaStream_t s, const cplx* Sin, const cplx* SU2, const uint32_t* map,
+                                  const double* occ, const cplx* C0, const cplx* Sig0, cplx* Sig, double U, int hartree,
+                                  int fdpa, double n0, size_t n) {
+    k_sigma_assemble<<<blocks_for(n, 256), 256, 0, s>>>(Sin, SU2, map, occ, C0, Sig0, Sig, U, hartree, fdpa, n0, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_gather(cudaStream_t s, cplx* dst, const cplx* src, const uint32_t* perm, size_t n) {
+    k_gather<<<blocks_for(n, 256), 256, 0, s>>>(dst, src, perm, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_scatter(cudaStream_t s, cplx* dst, const cplx* src, const uint32_t* perm, size_t n) {
+    k_scatter<<<blocks_for(n, 256), 256, 0, s>>>(dst, src, perm, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_residual(cudaStream_t s, const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax,
+                            int nblk, size_t n) {
+    k_residual<<<nblk, 256, 0, s>>>(y, x, fx, g, beta, pmax, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_dot(cudaStream_t s, const cplx* a, const cplx* b, cplx* part, int nblk, size_t n) {
+    k_dot<<<nblk, 256, 0, s>>>(a, b, part, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_axpy(cudaStream_t s, cplx* y, const cplx* x, cplx a, size_t n) {
+    k_axpy<<<blocks_for(n, 256), 256, 0, s>>>(y, x, a, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_rot(cudaStream_t s, cplx* qa, cplx* qb, double c, cplx sn, size_t n) {
+    k_rot<<<blocks_for(n, 256), 256, 0, s>>>(qa, qb, c, sn, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_sub(cudaStream_t s, cplx* out, const cplx* a, const cplx* b, size_t n) {
+    k_sub<<<blocks_for(n, 256), 256, 0, s>>>(out, a, b, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_scale(cudaStream_t s, cplx* out, const cplx* a, double sc, size_t n) {
+    k_scale<<<blocks_for(n, 256), 256, 0, s>>>(out, a, sc, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count) {
+    k_nonfinite<<<blocks_for(n, 256), 256, 0, s>>>(a, n, count);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+
+}  // namespace fdga

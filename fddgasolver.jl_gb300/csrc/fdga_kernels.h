@@ -1,0 +1,76 @@
+// fdga_kernels.h -- kernel argument bundles and launchers (host-visible).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "fdga_device.cuh"
+
+namespace fdga {
+
+struct ChanArrays {  // read-only K arrays of the three channels
+    const cplx* K1[3];
+    const cplx* K2[3];
+    const cplx* K3[3];
+};
+struct ChanArraysW {  // written arrays of the three channels
+    cplx* K1[3];
+    cplx* K2[3];
+    cplx* K3[3];
+};
+struct Caches {  // Γpx F0p F0a F0t Γpp Γa Γt Fp Fa Ft
+    cplx* c[10];
+};
+struct FLP {  // left vertex FL: only K2 enters the K1/K2 BSE through FL(Ω, ω, νInf)
+    const cplx* K2[3];
+};
+struct K3Args {
+    const cplx* A;    // cacheΓ (L_K3) or cacheF (K3)
+    const cplx* B0;   // cacheF0
+    const cplx* G;    // cacheΓ (K3, right part)
+    const cplx* Pi;
+    const cplx* Pi0;
+    const cplx* FLc;  // FL.γ_ch.K3 (a, p)
+    const cplx* FLt;  // FL.γt.K3
+    const cplx* FLa;  // FL.γa.K3
+    cplx* out;
+};
+
+cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n);
+cudaError_t launch_occupation(cudaStream_t s, const cplx* G, size_t n, double T, int Nk, double* out);
+cudaError_t launch_g_realspace(cudaStream_t s, const cplx* G, cplx* GR, const cplx* tw, const Dims& d);
+int bubble_tile(const Dims& d);
+cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
+                          const Dims& d);
+cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d);
+cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const Dims& d);
+cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+                          cplx* out, const int* items, int nitems, const Dims& d);
+cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* Pi0, cplx* out, const int* items,
+                            int nitems, const Dims& d);
+cudaError_t launch_bse_K2(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+                          cplx* out, const int* items, int nitems, const Dims& d);
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, int ch, const K3Args& a, const Dims& d);
+cudaError_t launch_expand(cudaStream_t s, cplx* X, const uint32_t* map, size_t n);
+cudaError_t launch_half_sum(cudaStream_t s, cplx* out, const cplx* other, size_t n);
+cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa,
+                               const cplx* outA, int ch, size_t n);
+cudaError_t launch_sde_L(cudaStream_t s, int which, int ref, const VertP& F, const cplx* Pi, cplx* out,
+                         const int* items, int nitems, double scale, int accumulate, const Dims& d);
+cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, const Dims& d);
+cudaError_t launch_u2(cudaStream_t s, const cplx* GR, cplx* C, cplx* SR, cplx* out, const cplx* twc, const Dims& d);
+cudaError_t launch_sigma_assemble(cudaStream_t s, const cplx* Sin, const cplx* SU2, const uint32_t* map,
+                                  const double* occ, const cplx* C0, const cplx* Sig0, cplx* Sig, double U, int hartree,
+                                  int fdpa, double n0, size_t n);
+cudaError_t launch_gather(cudaStream_t s, cplx* dst, const cplx* src, const uint32_t* perm, size_t n);
+cudaError_t launch_scatter(cudaStream_t s, cplx* dst, const cplx* src, const uint32_t* perm, size_t n);
+cudaError_t launch_residual(cudaStream_t s, const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax,
+                            int nblk, size_t n);
+cudaError_t launch_dot(cudaStream_t s, const cplx* a, const cplx* b, cplx* part, int nblk, size_t n);
+cudaError_t launch_axpy(cudaStream_t s, cplx* y, const cplx* x, cplx a, size_t n);
+cudaError_t launch_rot(cudaStream_t s, cplx* qa, cplx* qb, double c, cplx sn, size_t n);
+cudaError_t launch_sub(cudaStream_t s, cplx* out, const cplx* a, const cplx* b, size_t n);
+cudaError_t launch_scale(cudaStream_t s, cplx* out, const cplx* a, double sc, size_t n);
+cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count);
+
+}  // namespace fdga

@@ -1,0 +1,1021 @@
+// fdga_runtime.cu -- host runtime of libfdga: handle, device state, symmetry groups, the
+// per-iteration launch sequence (captured once into a CUDA graph), the Anderson driver and the
+// C ABI declared in include/fdga.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "../../include/fdga.h"
+#include "fdga_kernels.h"
+
+using namespace fdga;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+enum ArrKind { AK_G = 0, AK_K1, AK_K2, AK_K3, AK_PI };
+
+struct Group {
+    bool trivial = true;
+    int* d_items = nullptr;       // representative device indices
+    int nitems = 0;
+    uint32_t* d_map = nullptr;    // per device index: rep*4 + op
+    size_t n = 0;
+};
+
+struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    int nodes = 0;
+};
+
+}  // namespace
+
+struct fdga_handle {
+    fdga_config cfg{};
+    Dims d{};
+    cudaStream_t st = nullptr;
+    std::string err;
+    bool finalized = false;
+    bool c0_dirty = true;
+    bool ref_nonzero = false;
+    size_t nGk = 0, n1 = 0, n2 = 0, n3 = 0, nPi = 0, nRef = 0, nchan = 0, nstate = 0;
+    // device state
+    cplx *Gbare = nullptr, *G0 = nullptr, *Sig0 = nullptr, *G = nullptr;
+    cplx *Pi0pp = nullptr, *Pi0ph = nullptr, *Pipp = nullptr, *Piph = nullptr;
+    cplx *Fref[4] = {nullptr, nullptr, nullptr, nullptr};  // Fp_p Fp_x Ft_p Ft_x
+    cplx *xS = nullptr, *yS = nullptr, *tmpS = nullptr;
+    cplx *avg = nullptr, *cache = nullptr, *FLK2 = nullptr, *FLK3 = nullptr;
+    cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
+    cplx *GR = nullptr, *u2C = nullptr, *u2R = nullptr, *twm = nullptr, *twp = nullptr;
+    double* occ = nullptr;
+    double n0 = 0.5;
+    uint32_t* perm = nullptr;  // reference flatten index -> device index
+    Group gSig, gK1, gK2pp, gK2ph, gK3pp, gK3ph, gK3ppL, gK3phL;
+    Graph graphs[2][2][2];
+    int last_launches = 0;
+    cudaEvent_t ev[8] = {};
+    // Anderson
+    std::vector<cplx*> aa_buf;
+    double* d_part = nullptr;
+    cplx* d_cpart = nullptr;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+const int NBLK_RED = 296;
+
+int fail(fdga_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+int cuda_fail(fdga_handle* h, cudaError_t e, const char* where) {
+    return fail(h, FDGA_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t e__ = (call);                                       \
+        if (e__ != cudaSuccess) return cuda_fail(h, e__, #call);        \
+    } while (0)
+
+template <class T>
+int dalloc(fdga_handle* h, T** p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) return fail(h, FDGA_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    h->allocs.push_back((void*)*p);
+    return cudaMemsetAsync(*p, 0, n * sizeof(T), h->st) == cudaSuccess ? FDGA_OK : FDGA_ERR_CUDA;
+}
+#define AL(ptr, n)                                           \
+    do {                                                     \
+        int r__ = dalloc(h, &(ptr), (n));                    \
+        if (r__) return r__;                                 \
+    } while (0)
+
+// ---- channel views into a state vector ----
+cplx* chanK(const fdga_handle* h, cplx* S, int ch, int cls) {
+    cplx* base = S + (size_t)ch * h->nchan;
+    return cls == 1 ? base : (cls == 2 ? base + h->n1 : base + h->n1 + h->n2);
+}
+cplx* sigmaOf(const fdga_handle* h, cplx* S) { return S + 3 * h->nchan; }
+
+// ---- reference column-major index <-> device index ----
+size_t dev_index(const Dims& d, int kind, size_t j) {
+    switch (kind) {
+        case AK_G:
+        case AK_K1:
+            return j;
+        case AK_K2: {
+            size_t iO = j % d.N2O; j /= d.N2O;
+            size_t in = j % d.N2n; size_t P = j / d.N2n;
+            return (P * d.N2O + iO) * d.N2n + in;
+        }
+        case AK_K3: {
+            size_t iO = j % d.N3O; j /= d.N3O;
+            size_t a = j % d.N3n; j /= d.N3n;
+            size_t b = j % d.N3n; size_t P = j / d.N3n;
+            return ((P * d.N3O + iO) * d.N3n + a) * d.N3n + b;
+        }
+        default: {  // Π [Ω, ν, P]
+            size_t iO = j % d.NPO; j /= d.NPO;
+            size_t in = j % d.NPn; size_t P = j / d.NPn;
+            return (P * d.NPO + iO) * d.NPn + in;
+        }
+    }
+}
+
+int make_dims(const fdga_config* c, Dims& d) {
+    d.nG = c->nG; d.NG = 2 * c->nG; d.L = c->L; d.Nq = c->L * c->L; d.Nk = d.Nq;
+    d.n1 = c->nK1; d.N1 = 2 * c->nK1 - 1;
+    d.n2O = c->nK2[0]; d.N2O = 2 * c->nK2[0] - 1; d.n2n = c->nK2[1]; d.N2n = 2 * c->nK2[1];
+    d.n3O = c->nK3[0]; d.N3O = 2 * c->nK3[0] - 1; d.n3n = c->nK3[1]; d.N3n = 2 * c->nK3[1];
+    d.nPO = c->nK1; d.NPO = 2 * c->nK1 - 1; d.nPn = c->nK1 * c->mPi_factor; d.NPn = 2 * d.nPn;
+    d.nRO = c->nR[0]; d.NRO = 2 * c->nR[0] - 1; d.nRn = c->nR[1]; d.NRn = 2 * c->nR[1];
+    d.local = c->local ? 1 : 0;
+    d.T = c->T; d.U = c->U;
+    return FDGA_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Symmetry classes (MatsubaraFunctions SymmetryGroup semantics): mesh points joined by the
+// listed symmetries (images outside the box are dropped) form a class; classes are seeded in
+// the reference's linear order, so the representative is the class's first point in that
+// order; each member carries the composed Operation (1 = sign, 2 = conjugation).
+// Symmetry maps: src/symmetries.jl:2-94 and src/nonlocal/symmetries.jl:4-133.
+// ---------------------------------------------------------------------------------------------
+struct Pt { int m, n, np, P; };
+using SymF = std::function<int(const Pt&, Pt&)>;
+
+struct ShapeDesc {
+    int kind;             // AK_G (Σ), AK_K1, AK_K2, AK_K3
+    int nO = 0, nf = 0;   // boson / fermion mesh parameters (Σ: nf = nG)
+    int Nq = 1;
+    size_t size() const {
+        size_t s = (size_t)Nq;
+        if (kind == AK_G) return s * 2 * nf;
+        s *= (size_t)(2 * nO - 1);
+        if (kind == AK_K2) s *= 2 * nf;
+        if (kind == AK_K3) s *= (size_t)(2 * nf) * (2 * nf);
+        return s;
+    }
+    Pt decode(size_t j) const {  // reference column-major
+        Pt p{0, 0, 0, 0};
+        if (kind == AK_G) { p.n = (int)(j % (2 * nf)) - nf; p.P = (int)(j / (2 * nf)); return p; }
+        const int NO = 2 * nO - 1;
+        p.m = (int)(j % NO) - (nO - 1); j /= NO;
+        if (kind == AK_K1) { p.P = (int)j; return p; }
+        p.n = (int)(j % (2 * nf)) - nf; j /= 2 * nf;
+        if (kind == AK_K2) { p.P = (int)j; return p; }
+        p.np = (int)(j % (2 * nf)) - nf; p.P = (int)(j / (2 * nf));
+        return p;
+    }
+    bool inb(const Pt& p) const {
+        if (kind == AK_G) return fin(p.n, nf);
+        if (!bin(p.m, nO)) return false;
+        if (kind == AK_K1) return true;
+        if (!fin(p.n, nf)) return false;
+        return kind == AK_K2 ? true : fin(p.np, nf);
+    }
+    size_t encode(const Pt& p) const {
+        if (kind == AK_G) return (size_t)(p.n + nf) + (size_t)(2 * nf) * p.P;
+        const int NO = 2 * nO - 1;
+        size_t j = (size_t)(p.m + nO - 1);
+        if (kind == AK_K1) return j + (size_t)NO * p.P;
+        j += (size_t)NO * (p.n + nf);
+        if (kind == AK_K2) return j + (size_t)NO * (2 * nf) * p.P;
+        return j + (size_t)NO * (2 * nf) * ((p.np + nf) + (size_t)(2 * nf) * p.P);
+    }
+};
+
+int pmod(int a, int L) { int r = a % L; return r < 0 ? r + L : r; }
+int kneg(int P, int L) { return pmod(-(P % L), L) + L * pmod(-(P / L), L); }
+int kref(int P, int L) { return (P / L) + L * (P % L); }
+int krot(int P, int L) { return (P / L) + L * pmod(-(P % L), L); }
+
+struct HostGroup {
+    std::vector<uint32_t> map;  // device index -> rep*4 + op
+    std::vector<int> items;     // representative device indices, sorted
+};
+
+void compute_group(const Dims& d, HostGroup& hg, const ShapeDesc& sh, int kind_dev, const std::vector<SymF>& syms) {
+    const size_t n = sh.size();
+    std::vector<int32_t> cls(n, -1);
+    std::vector<uint8_t> op(n, 0);
+    std::vector<size_t> rep_of_class;
+    // Depth-first with a LIFO work list, symmetries applied in list order: where a cycle of
+    // symmetries composes to a non-identity Operation the member's op depends on the traversal,
+    // and this is the order of MatsubaraFunctions' class construction (pop! of the unprocessed list).
+    std::vector<size_t> q;
+    for (size_t s = 0; s < n; ++s) {
+        if (cls[s] >= 0) continue;
+        const int c = (int)rep_of_class.size();
+        rep_of_class.push_back(s);
+        cls[s] = c;
+        op[s] = 0;
+        q.clear();
+        q.push_back(s);
+        while (!q.empty()) {
+            const size_t j = q.back();
+            q.pop_back();
+            const Pt p = sh.decode(j);
+            for (const auto& f : syms) {
+                Pt o = p;
+                const int o_op = f(p, o);
+                if (!sh.inb(o)) continue;
+                const size_t k = sh.encode(o);
+                if (cls[k] >= 0) continue;
+                cls[k] = c;
+                op[k] = (uint8_t)(op[j] ^ o_op);
+                q.push_back(k);
+            }
+        }
+    }
+    hg.map.assign(n, 0);
+    hg.items.clear();
+    hg.items.reserve(rep_of_class.size());
+    for (size_t j = 0; j < n; ++j) {
+        const size_t dj = dev_index(d, kind_dev, j);
+        const size_t dr = dev_index(d, kind_dev, rep_of_class[cls[j]]);
+        hg.map[dj] = (uint32_t)(dr << 2) | op[j];
+    }
+    for (size_t r : rep_of_class) hg.items.push_back((int)dev_index(d, kind_dev, r));
+    std::sort(hg.items.begin(), hg.items.end());
+}
+
+// The eight groups of init_sym_grp!, in the order Σ, K1, K2pp, K2ph, K3pp, K3ph, K3ppL, K3phL.
+void compute_all_groups(const Dims& d, std::vector<HostGroup>& out) {
+    const int L = d.L;
+    const bool nl = !d.local;
+    auto kn = [nl, L](int P) { return nl ? kneg(P, L) : P; };
+    std::vector<SymF> sig = {[kn](const Pt& p, Pt& o) { o.n = -p.n - 1; o.P = kn(p.P); return 3; }};
+    std::vector<SymF> k1 = {[kn](const Pt& p, Pt& o) { o.m = -p.m; o.P = kn(p.P); return 2; }};
+    SymF k2pp1 = [kn](const Pt& p, Pt& o) { o.m = -p.m; o.n = -p.n - 1; o.P = kn(p.P); return 2; };
+    SymF k2pp2 = [](const Pt& p, Pt& o) { o.n = p.m - p.n - 1; return 0; };
+    SymF k2ph2 = [kn](const Pt& p, Pt& o) { o.m = -p.m; o.n = p.m + p.n; o.P = kn(p.P); return 0; };
+    SymF k3pp1 = [kn](const Pt& p, Pt& o) { o.m = -p.m; o.n = -p.n - 1; o.np = -p.np - 1; o.P = kn(p.P); return 2; };
+    SymF k3pp2 = [](const Pt& p, Pt& o) { o.n = p.np; o.np = p.n; return 0; };
+    SymF k3pp3 = [](const Pt& p, Pt& o) { o.n = p.m - p.n - 1; o.np = p.m - p.np - 1; return 0; };
+    SymF k3ph3 = [kn](const Pt& p, Pt& o) { o.m = -p.m; o.n = p.m + p.n; o.np = p.m + p.np; o.P = kn(p.P); return 0; };
+    SymF ref = [L](const Pt& p, Pt& o) { o.P = kref(p.P, L); return 0; };
+    SymF rot = [L](const Pt& p, Pt& o) { o.P = krot(p.P, L); return 0; };
+    std::vector<SymF> k2pp = {k2pp1, k2pp2}, k2ph = {k2pp1, k2ph2};
+    std::vector<SymF> k3pp = {k3pp1, k3pp2, k3pp3}, k3ppL = {k3pp1, k3pp3};
+    std::vector<SymF> k3ph = {k3pp1, k3pp2, k3ph3}, k3phL = {k3pp1, k3ph3};
+    if (nl) {
+        for (auto* v : {&sig, &k1, &k2pp, &k2ph, &k3pp, &k3ppL, &k3ph, &k3phL}) { v->push_back(ref); v->push_back(rot); }
+    }
+    const ShapeDesc sS{AK_G, 0, d.nG, d.Nk}, s1{AK_K1, d.n1, 0, d.Nq}, s2{AK_K2, d.n2O, d.n2n, d.Nq},
+        s3{AK_K3, d.n3O, d.n3n, d.Nq};
+    out.assign(8, HostGroup());
+    compute_group(d, out[0], sS, AK_G, sig);
+    compute_group(d, out[1], s1, AK_K1, k1);
+    compute_group(d, out[2], s2, AK_K2, k2pp);
+    compute_group(d, out[3], s2, AK_K2, k2ph);
+    compute_group(d, out[4], s3, AK_K3, k3pp);
+    compute_group(d, out[5], s3, AK_K3, k3ph);
+    compute_group(d, out[6], s3, AK_K3, k3ppL);
+    compute_group(d, out[7], s3, AK_K3, k3phL);
+}
+
+int upload_group(fdga_handle* h, Group& g, const HostGroup& hg) {
+    const size_t n = hg.map.size();
+    if (!g.d_map) AL(g.d_map, n);
+    if (!g.d_items) AL(g.d_items, n);
+    CK(cudaMemcpyAsync(g.d_map, hg.map.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(g.d_items, hg.items.data(), hg.items.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    g.trivial = false;
+    g.nitems = (int)hg.items.size();
+    g.n = n;
+    return FDGA_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Launch sequence of one iteration: src/solve.jl:4-116
+// ---------------------------------------------------------------------------------------------
+VertP vertex_view(fdga_handle* h, cplx* S) {
+    VertP F;
+    for (int c = 0; c < 3; ++c) {
+        F.g[c].K1 = chanK(h, S, c, 1);
+        F.g[c].K2 = chanK(h, S, c, 2);
+        F.g[c].K3 = chanK(h, S, c, 3);
+        if (h->d.Nq == 1) {
+            F.g[c].A1 = F.g[c].K1; F.g[c].A2 = F.g[c].K2; F.g[c].A3 = F.g[c].K3;
+        } else {
+            const size_t per1 = h->d.N1, per2 = (size_t)h->d.N2O * h->d.N2n, per3 = (size_t)h->d.N3O * h->d.N3n * h->d.N3n;
+            cplx* a = h->avg + (size_t)c * (per1 + per2 + per3);
+            F.g[c].A1 = a; F.g[c].A2 = a + per1; F.g[c].A3 = a + per1 + per2;
+        }
+    }
+    F.Fp_p = h->Fref[0]; F.Fp_x = h->Fref[1]; F.Ft_p = h->Fref[2]; F.Ft_x = h->Fref[3];
+    return F;
+}
+
+const Group& k2group(fdga_handle* h, int ch) { return ch == CH_P ? h->gK2pp : h->gK2ph; }
+
+#define LC(call)                                                     \
+    do {                                                             \
+        cudaError_t e__ = (call);                                    \
+        if (e__ != cudaSuccess) return cuda_fail(h, e__, #call);     \
+        ++nl;                                                        \
+    } while (0)
+
+using StageHook = std::function<void(const char*)>;
+
+int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree, int& nl,
+                      const StageHook& mark = StageHook()) {
+    cudaStream_t s = h->st;
+    auto stage = [&](const char* name) { if (mark) mark(name); };
+    const Dims& d = h->d;
+    nl = 0;
+    VertP F = vertex_view(h, h->xS);
+    VertP Fn = vertex_view(h, h->yS);  // Fbuff, i.e. the new F used by the SDE
+    // momentum averages of F (kSW evaluation)
+    if (d.Nq > 1) {
+        ChanArrays in;
+        ChanArraysW out;
+        for (int c = 0; c < 3; ++c) {
+            in.K1[c] = F.g[c].K1; in.K2[c] = F.g[c].K2; in.K3[c] = F.g[c].K3;
+            out.K1[c] = (cplx*)F.g[c].A1; out.K2[c] = (cplx*)F.g[c].A2; out.K3[c] = (cplx*)F.g[c].A3;
+        }
+        LC(launch_qavg(s, in, out, d));
+        stage("qavg");
+    }
+    if (update_sigma) {
+        LC(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
+        LC(launch_g_realspace(s, h->G, h->GR, h->twm, d));
+        LC(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
+        stage("dyson_bubble");
+    }
+    Caches C;
+    for (int i = 0; i < 10; ++i) C.c[i] = h->cache + (size_t)i * h->n3;
+    LC(launch_build_cache(s, F, C, d));
+    stage("k3_cache");
+    FLP FL;
+    for (int c = 0; c < 3; ++c) FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
+    const int order[3] = {CH_P, CH_A, CH_T};
+    auto Pi = [&](int ch) { return ch == CH_P ? h->Pipp : h->Piph; };
+    auto Pi0 = [&](int ch) { return ch == CH_P ? h->Pi0pp : h->Pi0ph; };
+    if (strategy == FDGA_FDPA) {
+        for (int ch : order) {
+            const Group& g = k2group(h, ch);
+            cplx* out = h->FLK2 + (size_t)ch * h->n2;
+            LC(launch_bse_L_K2(s, ch, F, Pi0(ch), out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n2 : g.nitems, d));
+            if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n2));
+            if (ch == CH_T) LC(launch_half_sum(s, out, h->FLK2 + (size_t)CH_A * h->n2, h->n2));
+        }
+        stage("bse_L_K2");
+        for (int ch : order) {
+            const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+            K3Args a{};
+            a.A = C.c[cg]; a.B0 = C.c[cf0]; a.Pi0 = Pi0(ch);
+            a.out = h->FLK3 + (size_t)ch * h->n3;
+            LC(launch_bse_K3(s, 0, ch, a, d));
+            const Group& g = ch == CH_P ? h->gK3ppL : h->gK3phL;
+            if (!g.trivial) LC(launch_expand(s, a.out, g.d_map, h->n3));
+            if (ch == CH_T) LC(launch_half_sum(s, a.out, h->FLK3 + (size_t)CH_A * h->n3, h->n3));
+        }
+        stage("bse_L_K3");
+    }
+    // K1
+    for (int ch : order) {
+        cplx* out = chanK(h, h->yS, ch, 1);
+        const Group& g = h->gK1;
+        LC(launch_bse_K1(s, ch, F, FL, Pi(ch), Pi0(ch), out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n1 : g.nitems, d));
+        if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n1));
+        if (ch == CH_T) LC(launch_half_sum(s, out, chanK(h, h->yS, CH_A, 1), h->n1));
+    }
+    stage("bse_K1");
+    // K2
+    for (int ch : order) {
+        cplx* out = chanK(h, h->yS, ch, 2);
+        const Group& g = k2group(h, ch);
+        LC(launch_bse_K2(s, ch, F, FL, Pi(ch), Pi0(ch), out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n2 : g.nitems, d));
+        if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n2));
+        LC(launch_k2_epilogue(s, out, h->FLK2 + (size_t)ch * h->n2, h->FLK2 + (size_t)CH_T * h->n2,
+                              h->FLK2 + (size_t)CH_A * h->n2, chanK(h, h->yS, CH_A, 2), ch, h->n2));
+    }
+    stage("bse_K2");
+    // K3
+    for (int ch : order) {
+        const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
+        const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+        K3Args a{};
+        a.A = C.c[cf]; a.B0 = C.c[cf0]; a.G = C.c[cg]; a.Pi = Pi(ch); a.Pi0 = Pi0(ch);
+        a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3; a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
+        a.out = chanK(h, h->yS, ch, 3);
+        LC(launch_bse_K3(s, 1, ch, a, d));
+        const Group& g = ch == CH_P ? h->gK3pp : h->gK3ph;
+        if (!g.trivial) LC(launch_expand(s, a.out, g.d_map, h->n3));
+        if (ch == CH_T) LC(launch_half_sum(s, a.out, chanK(h, h->yS, CH_A, 3), h->n3));
+    }
+    stage("bse_K3");
+    // SDE (src/SDE.jl:3-33) with the new F
+    cplx* SigOut = sigmaOf(h, h->yS);
+    if (update_sigma) {
+        const Group& gp = h->gK2pp;
+        const Group& gh = h->gK2ph;
+        const int* ip = gp.trivial ? nullptr : gp.d_items;
+        const int* ih = gh.trivial ? nullptr : gh.d_items;
+        const int np_ = gp.trivial ? (int)h->n2 : gp.nitems, nh_ = gh.trivial ? (int)h->n2 : gh.nitems;
+        LC(launch_sde_L(s, 0, 0, Fn, h->Pipp, h->Lpp, ip, np_, 1.0, 0, d));
+        LC(launch_sde_L(s, 1, 0, Fn, h->Piph, h->Lph, ih, nh_, 1.0, 0, d));
+        if (h->ref_nonzero) {
+            LC(launch_sde_L(s, 0, 1, Fn, h->Pipp, h->Lpp, ip, np_, 1.0 / 3.0, 1, d));
+            LC(launch_sde_L(s, 1, 1, Fn, h->Piph, h->Lph, ih, nh_, 1.0 / 3.0, 1, d));
+        }
+        if (!gp.trivial) LC(launch_expand(s, h->Lpp, gp.d_map, h->n2));
+        if (!gh.trivial) LC(launch_expand(s, h->Lph, gh.d_map, h->n2));
+        LC(launch_sde_sigma(s, h->G, h->Lpp, h->Lph, h->SigIn, d));
+        LC(launch_u2(s, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
+        nl += 2;
+        LC(launch_occupation(s, h->G, h->nGk, d.T, d.Nk, h->occ));
+        LC(launch_sigma_assemble(s, h->SigIn, h->SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, h->occ, h->C0,
+                                 h->Sig0, SigOut, d.U, hartree ? 1 : 0, strategy == FDGA_FDPA ? 1 : 0, h->n0, h->nGk));
+    } else {
+        LC(cudaMemcpyAsync(SigOut, sigmaOf(h, h->xS), h->nGk * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    }
+    stage("sde");
+    return FDGA_OK;
+}
+
+// Constant reference-system part of the fdPA SDE: C0 = SDE(F0, G0, Π0) without Hartree.
+int compute_C0(fdga_handle* h) {
+    cudaStream_t s = h->st;
+    const Dims& d = h->d;
+    int nl = 0;
+    VertP F0 = vertex_view(h, h->yS);  // only the RefVertex fields are read by the REF kernels
+    const Group& gp = h->gK2pp;
+    const Group& gh = h->gK2ph;
+    LC(launch_sde_L(s, 0, 1, F0, h->Pi0pp, h->Lpp, gp.trivial ? nullptr : gp.d_items, gp.trivial ? (int)h->n2 : gp.nitems, 1.0 / 3.0, 0, d));
+    LC(launch_sde_L(s, 1, 1, F0, h->Pi0ph, h->Lph, gh.trivial ? nullptr : gh.d_items, gh.trivial ? (int)h->n2 : gh.nitems, 1.0 / 3.0, 0, d));
+    if (!gp.trivial) LC(launch_expand(s, h->Lpp, gp.d_map, h->n2));
+    if (!gh.trivial) LC(launch_expand(s, h->Lph, gh.d_map, h->n2));
+    LC(launch_sde_sigma(s, h->G0, h->Lpp, h->Lph, h->SigIn, d));
+    LC(launch_g_realspace(s, h->G0, h->GR, h->twm, d));
+    LC(launch_u2(s, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
+    LC(launch_sigma_assemble(s, h->SigIn, h->SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, h->occ, nullptr,
+                             nullptr, h->C0, d.U, 0, 0, 0.0, h->nGk));
+    LC(launch_occupation(s, h->G0, h->nGk, d.T, d.Nk, h->occ));
+    double n0 = 0.5;
+    CK(cudaMemcpyAsync(&n0, h->occ, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    h->n0 = n0;
+    h->c0_dirty = false;
+    (void)nl;
+    return FDGA_OK;
+}
+
+void drop_graphs(fdga_handle* h) {
+    for (auto& a : h->graphs)
+        for (auto& b : a)
+            for (auto& g : b)
+                if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+}
+
+int run_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA) return fail(h, FDGA_ERR_ARG, "unknown strategy");
+    if (h->c0_dirty) {
+        int r = compute_C0(h);
+        if (r) return r;
+    }
+    Graph& g = h->graphs[strategy][update_sigma][hartree];
+    if (!g.exec) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        int nl = 0;
+        int r = enqueue_iteration(h, strategy, update_sigma, hartree, nl);
+        cudaError_t ee = cudaStreamEndCapture(h->st, &graph);
+        if (r) return r;
+        if (ee != cudaSuccess) return cuda_fail(h, ee, "cudaStreamEndCapture");
+        ee = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ee != cudaSuccess) { g.exec = nullptr; return cuda_fail(h, ee, "cudaGraphInstantiate"); }
+        g.nodes = nl;
+    }
+    CK(cudaGraphLaunch(g.exec, h->st));
+    h->last_launches = g.nodes;
+    return FDGA_OK;
+}
+
+double reduce_max(fdga_handle* h, int nblk, int& status) {
+    std::vector<double> part(nblk);
+    cudaError_t e = cudaMemcpyAsync(part.data(), h->d_part, nblk * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) { status = cuda_fail(h, e, "reduce_max"); return 0.0; }
+    double m = 0.0;
+    for (double v : part) m = std::max(m, v);
+    status = FDGA_OK;
+    return m;
+}
+
+std::complex<double> dot(fdga_handle* h, const cplx* a, const cplx* b, int& status) {
+    cudaError_t e = launch_dot(h->st, a, b, h->d_cpart, NBLK_RED, h->nstate);
+    std::vector<cplx> part(NBLK_RED);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), h->d_cpart, NBLK_RED * sizeof(cplx), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) { status = cuda_fail(h, e, "dot"); return 0.0; }
+    std::complex<double> s = 0.0;
+    for (auto& v : part) s += std::complex<double>(v.x, v.y);
+    status = FDGA_OK;
+    return s;
+}
+
+bool names_vertex(const std::string& n, std::string& vn, int& ch, int& cls) {
+    const size_t dot_ = n.find('.');
+    if (dot_ == std::string::npos || n.size() != dot_ + 5) return false;
+    vn = n.substr(0, dot_);
+    const char c = n[dot_ + 1];
+    ch = c == 'p' ? CH_P : (c == 't' ? CH_T : (c == 'a' ? CH_A : -1));
+    if (ch < 0 || n[dot_ + 2] != '.' || n[dot_ + 3] != 'K') return false;
+    cls = n[dot_ + 4] - '0';
+    return cls >= 1 && cls <= 3;
+}
+
+// named array -> (device pointer, kind, length)
+bool lookup(fdga_handle* h, const std::string& n, cplx*& p, int& kind, size_t& len) {
+    if (n == "G") { p = h->G; kind = AK_G; len = h->nGk; return true; }
+    if (n == "Sigma") { p = sigmaOf(h, h->xS); kind = AK_G; len = h->nGk; return true; }
+    if (n == "Gbare") { p = h->Gbare; kind = AK_G; len = h->nGk; return true; }
+    if (n == "G0") { p = h->G0; kind = AK_G; len = h->nGk; return true; }
+    if (n == "Sigma0") { p = h->Sig0; kind = AK_G; len = h->nGk; return true; }
+    if (n == "Pipp") { p = h->Pipp; kind = AK_PI; len = h->nPi; return true; }
+    if (n == "Piph") { p = h->Piph; kind = AK_PI; len = h->nPi; return true; }
+    if (n == "Pi0pp") { p = h->Pi0pp; kind = AK_PI; len = h->nPi; return true; }
+    if (n == "Pi0ph") { p = h->Pi0ph; kind = AK_PI; len = h->nPi; return true; }
+    if (n == "Lpp") { p = h->Lpp; kind = AK_K2; len = h->n2; return true; }
+    if (n == "Lph") { p = h->Lph; kind = AK_K2; len = h->n2; return true; }
+    static const char* cn[10] = {"cache_Gpx", "cache_F0p", "cache_F0a", "cache_F0t", "cache_Gpp",
+                                 "cache_Ga",  "cache_Gt",  "cache_Fp",  "cache_Fa",  "cache_Ft"};
+    for (int i = 0; i < 10; ++i)
+        if (n == cn[i]) { p = h->cache + (size_t)i * h->n3; kind = AK_K3; len = h->n3; return true; }
+    std::string vn;
+    int ch, cls;
+    if (!names_vertex(n, vn, ch, cls)) return false;
+    if (vn == "F") {
+        p = chanK(h, h->xS, ch, cls);
+    } else if (vn == "FL") {
+        if (cls == 1) return false;
+        p = cls == 2 ? h->FLK2 + (size_t)ch * h->n2 : h->FLK3 + (size_t)ch * h->n3;
+    } else {
+        return false;
+    }
+    kind = cls == 1 ? AK_K1 : (cls == 2 ? AK_K2 : AK_K3);
+    len = cls == 1 ? h->n1 : (cls == 2 ? h->n2 : h->n3);
+    return true;
+}
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+const char* fdga_create_error(void) { return g_create_error.c_str(); }
+const char* fdga_last_error(const fdga_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int fdga_create(const fdga_config* c, fdga_handle** out) {
+    if (!c || !out) { g_create_error = "null argument"; return FDGA_ERR_ARG; }
+    *out = nullptr;
+    auto bad = [&](const std::string& m) { g_create_error = m; return FDGA_ERR_ARG; };
+    if (c->nG < 1 || c->nK1 < 1 || c->nK2[0] < 1 || c->nK2[1] < 1 || c->nK3[0] < 1 || c->nK3[1] < 1)
+        return bad("mesh sizes must be >= 1");
+    if (c->nK1 < c->nK2[0] || c->nK1 < c->nK2[1])
+        return bad("No. bosonic frequencies in K1 must be larger than the K2 box (src/channel.jl:33-34)");
+    if (c->nK2[0] < c->nK3[0] || c->nK2[1] < c->nK3[1])
+        return bad("Number of frequencies in K2 must be larger than in K3 (src/channel.jl:40)");
+    if (c->L < 1 || c->mPi_factor < 1 || !(c->T > 0)) return bad("L, mPi_factor and T must be positive");
+    if (c->local && c->L != 1) return bad("the local solver has L = 1");
+    if (c->LG != c->L) { g_create_error = "L_G != L is not supported by this build"; return FDGA_ERR_UNSUPPORTED; }
+    if (c->precision != FDGA_FP64) { g_create_error = "only FDGA_FP64 is provided"; return FDGA_ERR_UNSUPPORTED; }
+    if (c->nR[0] < 1 || c->nR[1] < 1) return bad("RefVertex box must be >= 1");
+    fdga_handle* h = new fdga_handle();
+    h->cfg = *c;
+    make_dims(c, h->d);
+    Dims& d = h->d;
+    h->nGk = (size_t)d.NG * d.Nk;
+    h->n1 = (size_t)d.N1 * d.Nq;
+    h->n2 = (size_t)d.N2O * d.N2n * d.Nq;
+    h->n3 = (size_t)d.N3O * d.N3n * d.N3n * d.Nq;
+    h->nPi = (size_t)d.NPO * d.NPn * d.Nq;
+    h->nRef = (size_t)d.NRO * d.NRn * d.NRn;
+    h->nchan = h->n1 + h->n2 + h->n3;
+    h->nstate = 3 * h->nchan + h->nGk;
+    if (h->nstate >= ((size_t)1 << 32) || h->n3 >= ((size_t)1 << 30)) {
+        delete h;
+        g_create_error = "problem too large for 32-bit index maps";
+        return FDGA_ERR_UNSUPPORTED;
+    }
+    int r = FDGA_OK;
+    auto fin_err = [&](int code) { g_create_error = h->err; fdga_destroy(h); return code; };
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+        g_create_error = "cudaStreamCreate failed (no CUDA device?)";
+        delete h;
+        return FDGA_ERR_CUDA;
+    }
+    for (auto& e : h->ev) cudaEventCreate(&e);
+#define ALC(ptr, n) do { r = dalloc(h, &(ptr), (n)); if (r) return fin_err(r); } while (0)
+    ALC(h->Gbare, h->nGk); ALC(h->G0, h->nGk); ALC(h->Sig0, h->nGk); ALC(h->G, h->nGk);
+    ALC(h->Pi0pp, h->nPi); ALC(h->Pi0ph, h->nPi); ALC(h->Pipp, h->nPi); ALC(h->Piph, h->nPi);
+    for (auto& f : h->Fref) ALC(f, h->nRef);
+    ALC(h->xS, h->nstate); ALC(h->yS, h->nstate); ALC(h->tmpS, h->nstate);
+    if (d.Nq > 1) ALC(h->avg, 3 * ((size_t)d.N1 + (size_t)d.N2O * d.N2n + (size_t)d.N3O * d.N3n * d.N3n));
+    ALC(h->cache, 10 * h->n3);
+    ALC(h->FLK2, 3 * h->n2); ALC(h->FLK3, 3 * h->n3);
+    ALC(h->Lpp, h->n2); ALC(h->Lph, h->n2); ALC(h->SigIn, h->nGk); ALC(h->SigU2, h->nGk); ALC(h->C0, h->nGk);
+    ALC(h->GR, h->nGk); ALC(h->u2C, (size_t)d.Nq * (2 * d.NG - 1)); ALC(h->u2R, h->nGk);
+    ALC(h->twm, d.L); ALC(h->twp, d.L);
+    ALC(h->occ, 1);
+    ALC(h->perm, h->nstate);
+    ALC(h->d_part, NBLK_RED); ALC(h->d_cpart, NBLK_RED);
+    {
+        std::vector<cplx> tm(d.L), tp(d.L);
+        for (int j = 0; j < d.L; ++j) {
+            const double a = 2.0 * M_PI * j / d.L;
+            tm[j] = mk(std::cos(a), -std::sin(a));
+            tp[j] = mk(std::cos(a), std::sin(a));
+        }
+        if (cudaMemcpy(h->twm, tm.data(), d.L * sizeof(cplx), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(h->twp, tp.data(), d.L * sizeof(cplx), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fin_err(fail(h, FDGA_ERR_CUDA, "twiddle upload"));
+        // flatten permutation
+        std::vector<uint32_t> perm(h->nstate);
+        size_t j = 0;
+        for (int ch : {CH_P, CH_T, CH_A}) {
+            const size_t off = (size_t)ch * h->nchan;
+            for (size_t i = 0; i < h->n1; ++i) perm[j++] = (uint32_t)(off + dev_index(h->d, AK_K1, i));
+            for (size_t i = 0; i < h->n2; ++i) perm[j++] = (uint32_t)(off + h->n1 + dev_index(h->d, AK_K2, i));
+            for (size_t i = 0; i < h->n3; ++i) perm[j++] = (uint32_t)(off + h->n1 + h->n2 + dev_index(h->d, AK_K3, i));
+        }
+        for (size_t i = 0; i < h->nGk; ++i) perm[j++] = (uint32_t)(3 * h->nchan + i);
+        if (cudaMemcpy(h->perm, perm.data(), h->nstate * sizeof(uint32_t), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fin_err(fail(h, FDGA_ERR_CUDA, "permutation upload"));
+    }
+#undef ALC
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) return fin_err(fail(h, FDGA_ERR_CUDA, "create sync"));
+    *out = h;
+    return FDGA_OK;
+}
+
+void fdga_destroy(fdga_handle* h) {
+    if (!h) return;
+    if (h->st) cudaStreamSynchronize(h->st);
+    drop_graphs(h);
+    for (void* p : h->allocs) cudaFree(p);
+    for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+}
+
+int fdga_set_input(fdga_handle* h, int which, const double* re_im, size_t n) {
+    if (!h || !re_im) return fail(h, FDGA_ERR_ARG, "null argument");
+    cplx* dst = nullptr;
+    size_t len = 0;
+    switch (which) {
+        case FDGA_IN_GBARE: dst = h->Gbare; len = h->nGk; break;
+        case FDGA_IN_G0: dst = h->G0; len = h->nGk; break;
+        case FDGA_IN_SIGMA0: dst = h->Sig0; len = h->nGk; break;
+        case FDGA_IN_FP_P: case FDGA_IN_FP_X: case FDGA_IN_FT_P: case FDGA_IN_FT_X:
+            dst = h->Fref[which - FDGA_IN_FP_P]; len = h->nRef; break;
+        default: return fail(h, FDGA_ERR_ARG, "unknown input id");
+    }
+    if (n != len) return fail(h, FDGA_ERR_ARG, "input size mismatch: got " + std::to_string(n) + ", expected " + std::to_string(len));
+    for (size_t i = 0; i < 2 * n; ++i)
+        if (!std::isfinite(re_im[i])) return fail(h, FDGA_ERR_NONFINITE, "non-finite value in input");
+    if (which >= FDGA_IN_FP_P) {
+        for (size_t i = 0; i < 2 * n; ++i) if (re_im[i] != 0.0) { h->ref_nonzero = true; break; }
+    }
+    CK(cudaMemcpyAsync(dst, re_im, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->c0_dirty = true;
+    drop_graphs(h);
+    return FDGA_OK;
+}
+
+int fdga_finalize(fdga_handle* h) {
+    if (!h) return FDGA_ERR_ARG;
+    const Dims& d = h->d;
+    cudaStream_t s = h->st;
+    CK(launch_g_realspace(s, h->G0, h->GR, h->twm, d));
+    CK(launch_bubble(s, h->G0, h->GR, h->Pi0pp, h->Pi0ph, h->twp, d));
+    CK(cudaMemsetAsync(h->xS, 0, h->nstate * sizeof(cplx), s));
+    CK(cudaMemsetAsync(h->yS, 0, h->nstate * sizeof(cplx), s));
+    CK(cudaMemsetAsync(h->FLK2, 0, 3 * h->n2 * sizeof(cplx), s));
+    CK(cudaMemsetAsync(h->FLK3, 0, 3 * h->n3 * sizeof(cplx), s));
+    CK(cudaMemcpyAsync(sigmaOf(h, h->xS), h->Sig0, h->nGk * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    CK(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
+    CK(launch_g_realspace(s, h->G, h->GR, h->twm, d));
+    CK(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
+    CK(cudaStreamSynchronize(s));
+    h->finalized = true;
+    h->c0_dirty = true;
+    return FDGA_OK;
+}
+
+int fdga_init_sym_grp(fdga_handle* h) {
+    if (!h) return FDGA_ERR_ARG;
+    std::vector<HostGroup> hg;
+    compute_all_groups(h->d, hg);
+    Group* dst[8] = {&h->gSig, &h->gK1, &h->gK2pp, &h->gK2ph, &h->gK3pp, &h->gK3ph, &h->gK3ppL, &h->gK3phL};
+    for (int i = 0; i < 8; ++i) {
+        int r = upload_group(h, *dst[i], hg[i]);
+        if (r) return r;
+    }
+    drop_graphs(h);
+    h->c0_dirty = true;
+    return FDGA_OK;
+}
+
+int fdga_group_map(const fdga_config* c, int which, uint32_t* map, size_t n, int* nclasses) {
+    if (!c || which < 0 || which >= 8) return FDGA_ERR_ARG;
+    Dims d;
+    int r = make_dims(c, d);
+    if (r) return r;
+    std::vector<HostGroup> hg;
+    compute_all_groups(d, hg);
+    if (nclasses) *nclasses = (int)hg[which].items.size();
+    if (map) {
+        if (n != hg[which].map.size()) return FDGA_ERR_ARG;
+        std::memcpy(map, hg[which].map.data(), n * sizeof(uint32_t));
+    }
+    return FDGA_OK;
+}
+
+int fdga_state_len(const fdga_handle* h, size_t* n) {
+    if (!h || !n) return FDGA_ERR_ARG;
+    *n = h->nstate;
+    return FDGA_OK;
+}
+
+int fdga_flatten(fdga_handle* h, double* x, size_t n) {
+    if (!h || !x) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
+    CK(launch_gather(h->st, h->tmpS, h->xS, h->perm, n));
+    CK(cudaMemcpyAsync(x, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_unflatten(fdga_handle* h, const double* x, size_t n) {
+    if (!h || !x) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
+    CK(cudaMemcpyAsync(h->tmpS, x, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
+    CK(launch_scatter(h->st, h->xS, h->tmpS, h->perm, n));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_iterate(fdga_handle* h, int strategy, int update_sigma, int compute_hartree) {
+    if (!h) return FDGA_ERR_ARG;
+    int r = run_iteration(h, strategy, update_sigma != 0, compute_hartree != 0);
+    if (r) return r;
+    CK(cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size_t n) {
+    if (!h || !x || !R) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
+    CK(cudaMemcpyAsync(h->tmpS, x, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
+    CK(launch_scatter(h->st, h->xS, h->tmpS, h->perm, n));
+    int r = run_iteration(h, strategy, true, true);
+    if (r) return r;
+    // R = flatten(Φ(x)) - x, formed in device layout then permuted
+    CK(launch_sub(h->st, h->tmpS, h->yS, h->xS, n));
+    CK(cudaMemcpyAsync(h->xS, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_gather(h->st, h->yS, h->tmpS, h->perm, n));
+    CK(cudaMemcpyAsync(R, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int* iters, double* res,
+               double* trace) {
+    if (!h) return FDGA_ERR_ARG;
+    if (maxiter < 1 || mem < 0 || !(tol >= 0)) return fail(h, FDGA_ERR_ARG, "invalid solver parameters");
+    const size_t n = h->nstate;
+    const int m = (int)std::min<size_t>((size_t)mem, n);
+    // buffers: fx g fxold gold | dG[m] | Q[m]
+    const size_t need = 4 + 2 * (size_t)m;
+    while (h->aa_buf.size() < need) {
+        cplx* p = nullptr;
+        int r = dalloc(h, &p, n);
+        if (r) return r;
+        h->aa_buf.push_back(p);
+    }
+    cplx *fx = h->aa_buf[0], *g = h->aa_buf[1], *fxold = h->aa_buf[2], *gold = h->aa_buf[3];
+    std::vector<cplx*> dG(h->aa_buf.begin() + 4, h->aa_buf.begin() + 4 + m);
+    std::vector<cplx*> Q(h->aa_buf.begin() + 4 + m, h->aa_buf.begin() + 4 + 2 * m);
+    std::vector<std::complex<double>> R((size_t)m * m, 0.0), gam(m);
+    auto Rr = [&](int i, int j) -> std::complex<double>& { return R[(size_t)i + (size_t)m * j]; };
+    int m_eff = 0, it = 0, status = 0;
+    double resid = 0.0;
+    bool converged = false;
+    for (it = 1; it <= maxiter; ++it) {
+        int r = run_iteration(h, strategy, true, true);
+        if (r) return r;
+        CK(launch_residual(h->st, h->yS, h->xS, fx, g, beta, h->d_part, NBLK_RED, n));
+        resid = reduce_max(h, NBLK_RED, status);
+        if (status) return status;
+        if (!std::isfinite(resid)) return fail(h, FDGA_ERR_NONFINITE, "non-finite residual in solve");
+        if (trace) trace[it - 1] = resid;
+        if (resid < tol) { converged = true; break; }
+        CK(cudaMemcpyAsync(h->xS, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        if (m == 0) continue;
+        if (it == 1) {
+            CK(cudaMemcpyAsync(fxold, fx, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+            CK(cudaMemcpyAsync(gold, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+            continue;
+        }
+        m_eff += 1;
+        if (m_eff > m) {
+            std::rotate(dG.begin(), dG.begin() + 1, dG.end());
+            for (int i = 1; i < m; ++i) {
+                const std::complex<double> f = Rr(i - 1, i), gg = Rr(i, i);
+                double c;
+                std::complex<double> sn;
+                const double af = std::abs(f), ag = std::abs(gg);
+                if (ag == 0.0) { c = 1.0; sn = 0.0; }
+                else if (af == 0.0) { c = 0.0; sn = std::conj(gg) / ag; }
+                else { const double rr = std::hypot(af, ag); c = af / rr; sn = (f / af) * std::conj(gg) / rr; }
+                for (int j = 0; j < m; ++j) {
+                    const std::complex<double> a = Rr(i - 1, j), b = Rr(i, j);
+                    Rr(i - 1, j) = c * a + sn * b;
+                    Rr(i, j) = -std::conj(sn) * a + c * b;
+                }
+                CK(launch_rot(h->st, Q[i - 1], Q[i], c, mk(sn.real(), sn.imag()), n));
+            }
+            for (int j = 0; j < m - 1; ++j)
+                for (int i = 0; i < m - 1; ++i) Rr(i, j) = Rr(i, j + 1);
+            m_eff = m;
+        }
+        const int k = m_eff - 1;
+        CK(launch_sub(h->st, dG[k], g, gold, n));
+        CK(launch_sub(h->st, fxold, fx, fxold, n));
+        for (int i = 0; i < k; ++i) {
+            const std::complex<double> rr = dot(h, Q[i], fxold, status);
+            if (status) return status;
+            Rr(i, k) = rr;
+            CK(launch_axpy(h->st, fxold, Q[i], mk(-rr.real(), -rr.imag()), n));
+        }
+        const double nrm = std::sqrt(std::max(0.0, dot(h, fxold, fxold, status).real()));
+        if (status) return status;
+        Rr(k, k) = nrm;
+        CK(launch_scale(h->st, Q[k], fxold, nrm > 0 ? 1.0 / nrm : 0.0, n));
+        for (int i = 0; i < m_eff; ++i) {
+            gam[i] = dot(h, Q[i], fx, status);
+            if (status) return status;
+        }
+        for (int i = m_eff - 1; i >= 0; --i) {
+            std::complex<double> v = gam[i];
+            for (int j = i + 1; j < m_eff; ++j) v -= Rr(i, j) * gam[j];
+            gam[i] = v / Rr(i, i);
+        }
+        for (int i = 0; i < m_eff; ++i) CK(launch_axpy(h->st, h->xS, dG[i], mk(-gam[i].real(), -gam[i].imag()), n));
+        CK(cudaMemcpyAsync(fxold, fx, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        CK(cudaMemcpyAsync(gold, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    }
+    if (it > maxiter) it = maxiter;
+    // S holds Φ(x) of the last evaluation, as after the reference's solve!
+    CK(cudaMemcpyAsync(h->xS, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (iters) *iters = converged ? it : -it;
+    if (res) *res = resid;
+    return FDGA_OK;
+}
+
+int fdga_named_len(const fdga_handle* h, const char* name, size_t* n) {
+    if (!h || !name || !n) return FDGA_ERR_ARG;
+    cplx* p;
+    int kind;
+    if (!lookup(const_cast<fdga_handle*>(h), name, p, kind, *n)) return FDGA_ERR_ARG;
+    return FDGA_OK;
+}
+
+int fdga_get_named(fdga_handle* h, const char* name, double* out, size_t n) {
+    if (!h || !name || !out) return fail(h, FDGA_ERR_ARG, "null argument");
+    cplx* p;
+    int kind;
+    size_t len;
+    if (!lookup(h, name, p, kind, len)) return fail(h, FDGA_ERR_ARG, std::string("unknown array ") + name);
+    if (n != len) return fail(h, FDGA_ERR_ARG, "size mismatch for " + std::string(name));
+    std::vector<cplx> dev(len);
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaMemcpy(dev.data(), p, len * sizeof(cplx), cudaMemcpyDeviceToHost));
+    cplx* o = reinterpret_cast<cplx*>(out);
+    for (size_t j = 0; j < len; ++j) o[j] = dev[dev_index(h->d, kind, j)];
+    return FDGA_OK;
+}
+
+int fdga_occupation(fdga_handle* h, double* n) {
+    if (!h || !n) return FDGA_ERR_ARG;
+    CK(launch_occupation(h->st, h->G, h->nGk, h->d.T, h->d.Nk, h->occ));
+    CK(cudaMemcpyAsync(n, h->occ, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_event_record(fdga_handle* h, int slot) {
+    if (!h || slot < 0 || slot >= 8) return FDGA_ERR_ARG;
+    CK(cudaEventRecord(h->ev[slot], h->st));
+    return FDGA_OK;
+}
+int fdga_event_elapsed_ms(fdga_handle* h, int a, int b, float* ms) {
+    if (!h || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) return FDGA_ERR_ARG;
+    CK(cudaEventSynchronize(h->ev[b]));
+    CK(cudaEventElapsedTime(ms, h->ev[a], h->ev[b]));
+    return FDGA_OK;
+}
+int fdga_synchronize(fdga_handle* h) {
+    if (!h) return FDGA_ERR_ARG;
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms, int max_stages,
+                     int* nstages) {
+    if (!h || !ms || !nstages || nrep < 1) return FDGA_ERR_ARG;
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (h->c0_dirty) { int r = compute_C0(h); if (r) return r; }
+    std::vector<std::string> nm;
+    std::vector<double> acc;
+    for (int rep = 0; rep < nrep; ++rep) {
+        std::vector<cudaEvent_t> evs;
+        std::vector<std::string> cur;
+        cudaEvent_t e0;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventRecord(e0, h->st));
+        evs.push_back(e0);
+        int nl = 0;
+        StageHook hook = [&](const char* name) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            cudaEventRecord(e, h->st);
+            evs.push_back(e);
+            cur.push_back(name);
+        };
+        int r = enqueue_iteration(h, strategy, true, true, nl, hook);
+        if (r) return r;
+        CK(cudaStreamSynchronize(h->st));
+        if (rep == 0) { nm = cur; acc.assign(cur.size(), 0.0); }
+        for (size_t i = 0; i + 1 < evs.size() && i < acc.size(); ++i) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, evs[i], evs[i + 1]);
+            acc[i] += t;
+        }
+        for (auto e : evs) cudaEventDestroy(e);
+        CK(cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    const int n = (int)std::min<size_t>(nm.size(), (size_t)max_stages);
+    std::string joined;
+    for (int i = 0; i < n; ++i) {
+        ms[i] = acc[i] / nrep;
+        joined += nm[i];
+        if (i + 1 < n) joined += ",";
+    }
+    if (names && names_cap > 0) {
+        std::strncpy(names, joined.c_str(), names_cap - 1);
+        names[names_cap - 1] = 0;
+    }
+    *nstages = n;
+    return FDGA_OK;
+}
+
+int fdga_map_repeat(fdga_handle* h, int strategy, int n) {
+    if (!h || n < 0) return FDGA_ERR_ARG;
+    for (int i = 0; i < n; ++i) {
+        int r = run_iteration(h, strategy, true, true);
+        if (r) return r;
+    }
+    return FDGA_OK;
+}
+
+int fdga_host_alloc(size_t bytes, void** p) {
+    if (!p) return FDGA_ERR_ARG;
+    cudaError_t e = cudaHostAlloc(p, bytes ? bytes : 1, cudaHostAllocDefault);
+    if (e != cudaSuccess) { g_create_error = cudaGetErrorString(e); *p = nullptr; return FDGA_ERR_OOM; }
+    return FDGA_OK;
+}
+int fdga_host_free(void* p) {
+    return cudaFreeHost(p) == cudaSuccess ? FDGA_OK : FDGA_ERR_CUDA;
+}
+
+int fdga_launches_per_iteration(const fdga_handle* h, int* n) {
+    if (!h || !n) return FDGA_ERR_ARG;
+    *n = h->last_launches;
+    return FDGA_OK;
+}
+
+}  // extern "C"

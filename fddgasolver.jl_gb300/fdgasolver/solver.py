@@ -1,0 +1,256 @@
+"""Host-side mirror of fdDGAsolver.jl's solver API over libfdga.
+
+Names, arguments and defaults follow the reference:
+  ParquetSolver(nK1, nK2, nK3, Gbare, G0, Σ0, F0; mΠν_factor=6)        src/ParquetSolver.jl:277-352
+  NL_ParquetSolver(nK1, nK2, nK3, L, Gbare, G0, Σ0, F0; mΠν_factor=32) src/nonlocal/ParquetSolver.jl:77-152
+  parquet_solver_siam_parquet_approximation(nG, nK1, nK2, nK3; e, Δ, D, T, U)   src/ParquetSolver.jl:170-200
+  parquet_solver_hubbard_parquet_approximation(nG, nK1, nK2, nK3, L; T, U, μ, t1, t2, t3)
+                                                                       src/nonlocal/ParquetSolver.jl:166-194
+  init_sym_grp!(S)                    -> init_sym_grp(S)              src/ParquetSolver.jl:203-231
+  iterate_solver!(S; strategy, update_Σ, compute_Hartree) -> iterate_solver(S, ...)  src/solve.jl:4-116
+  fixed_point!(R, x, S)               -> fixed_point(S, x)            src/solve.jl:119-157
+  solve!(S; maxiter, tol, δ, mem)     -> solve(S, ...)                src/solve.jl:160-196
+  flatten(S) / unflatten!(S, x)       -> flatten(S) / unflatten(S, x) src/ParquetSolver.jl:277-306
+Complex arrays are numpy complex128 in the reference's column-major order.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .models import hubbard_bare_Green, siam_bare_Green
+
+STRATEGIES = {"fdPA": _lib.FDGA_FDPA, "scPA": _lib.FDGA_SCPA}
+
+
+class RefVertex:
+    """RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x) (src/refvertex.jl:1-35); corrections optional.
+
+    Correction arrays have the K3 shape (2nR0-1, 2nR1, 2nR1), column-major [Ω, ν, ν']."""
+
+    def __init__(self, T, U, Fp_p=None, Fp_x=None, Ft_p=None, Ft_x=None):
+        self.T = float(T)
+        self.U = float(U)
+        arrs = [Fp_p, Fp_x, Ft_p, Ft_x]
+        if all(a is None for a in arrs):
+            self.nR = (1, 1)
+            self.arrays = [np.zeros((1, 2, 2), dtype=np.complex128) for _ in range(4)]
+        else:
+            shp = next(a.shape for a in arrs if a is not None)
+            if len(shp) != 3 or shp[1] != shp[2] or shp[0] % 2 != 1 or shp[1] % 2 != 0:
+                raise ValueError("RefVertex corrections must have shape (2nΩ-1, 2nν, 2nν)")
+            self.nR = ((shp[0] + 1) // 2, shp[1] // 2)
+            self.arrays = [np.zeros(shp, dtype=np.complex128) if a is None else np.asarray(a, dtype=np.complex128)
+                           for a in arrs]
+            if any(a.shape != shp for a in self.arrays):
+                raise ValueError("all RefVertex corrections must share one shape")
+
+
+def _as_f(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.complex128).reshape(-1, order="F"))
+
+
+class _Solver:
+    local = True
+
+    def __init__(self, nK1, nK2, nK3, L, Gbare, G0, Sigma0, F0, *, mPi_factor, precision=0):
+        if not isinstance(F0, RefVertex):
+            raise NotImplementedError("this build takes a RefVertex reference vertex")
+        lib = _lib.load()
+        Gbare = np.asarray(Gbare, dtype=np.complex128)
+        nG = Gbare.shape[0] // 2
+        c = _lib.fdga_config()
+        c.nG, c.nK1 = nG, int(nK1)
+        c.nK2[0], c.nK2[1] = nK2
+        c.nK3[0], c.nK3[1] = nK3
+        c.L = c.LG = int(L)
+        c.mPi_factor = int(mPi_factor)
+        c.local = 1 if self.local else 0
+        c.T, c.U = F0.T, F0.U
+        c.nR[0], c.nR[1] = F0.nR
+        c.precision = int(precision)
+        h = ctypes.c_void_p()
+        _lib.check(lib.fdga_create(ctypes.byref(c), ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+        self.T, self.U = F0.T, F0.U
+        self.nG, self.nK1, self.nK2, self.nK3, self.L = nG, nK1, tuple(nK2), tuple(nK3), L
+        self.F0 = F0
+        self._set(_lib.IN_GBARE, Gbare)
+        self._set(_lib.IN_G0, G0)
+        self._set(_lib.IN_SIGMA0, Sigma0)
+        for k, a in enumerate(F0.arrays):
+            self._set(_lib.IN_FP_P + k, a)
+        self._check(lib.fdga_finalize(h))
+        n = ctypes.c_size_t()
+        self._check(lib.fdga_state_len(h, ctypes.byref(n)))
+        self.state_len = n.value
+
+    # -- plumbing --
+    def _check(self, rc):
+        _lib.check(rc, self._h)
+
+    def _set(self, which, a):
+        a = _as_f(a)
+        self._check(self._lib.fdga_set_input(self._h, which, a.ctypes.data, a.size))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fdga_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- reference API --
+    def init_sym_grp(self):
+        self._check(self._lib.fdga_init_sym_grp(self._h))
+
+    def flatten(self):
+        x = np.empty(self.state_len, dtype=np.complex128)
+        self._check(self._lib.fdga_flatten(self._h, x.ctypes.data, x.size))
+        return x
+
+    def unflatten(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        if x.size != self.state_len:
+            raise ValueError("state length mismatch")
+        self._check(self._lib.fdga_unflatten(self._h, x.ctypes.data, x.size))
+
+    def iterate_solver(self, strategy="fdPA", update_Sigma=True, compute_Hartree=True):
+        self._check(self._lib.fdga_iterate(self._h, STRATEGIES[strategy], int(update_Sigma), int(compute_Hartree)))
+
+    def fixed_point(self, x, strategy="fdPA"):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        R = np.empty_like(x)
+        self._check(self._lib.fdga_residual(self._h, STRATEGIES[strategy], x.ctypes.data, R.ctypes.data, x.size))
+        return R
+
+    def solve(self, strategy="fdPA", maxiter=100, tol=1e-4, delta=0.85, mem=8):
+        trace = np.zeros(maxiter, dtype=np.float64)
+        it = ctypes.c_int()
+        res = ctypes.c_double()
+        self._check(self._lib.fdga_solve(self._h, STRATEGIES[strategy], int(maxiter), float(tol), float(delta), int(mem),
+                                         ctypes.byref(it), ctypes.byref(res), trace.ctypes.data))
+        n = abs(it.value)
+        return {"converged": it.value > 0, "iterations": n, "residual": res.value, "trace": trace[:n]}
+
+    def get(self, name):
+        n = ctypes.c_size_t()
+        self._check(self._lib.fdga_named_len(self._h, name.encode(), ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.complex128)
+        self._check(self._lib.fdga_get_named(self._h, name.encode(), out.ctypes.data, out.size))
+        return out
+
+    def occupation(self):
+        v = ctypes.c_double()
+        self._check(self._lib.fdga_occupation(self._h, ctypes.byref(v)))
+        return v.value
+
+    # -- timing helpers on the solver's stream --
+    def event_record(self, slot):
+        self._check(self._lib.fdga_event_record(self._h, slot))
+
+    def event_elapsed_ms(self, a, b):
+        v = ctypes.c_float()
+        self._check(self._lib.fdga_event_elapsed_ms(self._h, a, b, ctypes.byref(v)))
+        return v.value
+
+    def synchronize(self):
+        self._check(self._lib.fdga_synchronize(self._h))
+
+    def stage_times(self, strategy="fdPA", nrep=3):
+        """Per-stage device milliseconds of an eager iteration (CUDA events on the solver stream)."""
+        names = ctypes.create_string_buffer(1024)
+        ms = np.zeros(32, dtype=np.float64)
+        n = ctypes.c_int()
+        self._check(self._lib.fdga_stage_times(self._h, STRATEGIES[strategy], int(nrep), names, 1024, ms.ctypes.data,
+                                               32, ctypes.byref(n)))
+        keys = names.value.decode().split(",") if n.value else []
+        return dict(zip(keys, ms[: n.value].tolist()))
+
+    def map_repeat(self, n, strategy="fdPA"):
+        """Apply the iteration map n times to the unchanged device state (no host sync)."""
+        self._check(self._lib.fdga_map_repeat(self._h, STRATEGIES[strategy], int(n)))
+
+    def fixed_point_ptr(self, x_ptr, R_ptr, strategy="fdPA"):
+        """fixed_point! on caller-owned host buffers (e.g. pinned) of state_len complex values."""
+        self._check(self._lib.fdga_residual(self._h, STRATEGIES[strategy], x_ptr, R_ptr, self.state_len))
+
+    def launches_per_iteration(self):
+        v = ctypes.c_int()
+        self._check(self._lib.fdga_launches_per_iteration(self._h, ctypes.byref(v)))
+        return v.value
+
+
+class ParquetSolver(_Solver):
+    local = True
+
+    def __init__(self, nK1, nK2, nK3, Gbare, G0, Sigma0, F0, *, mPi_factor=6, precision=0):
+        super().__init__(nK1, nK2, nK3, 1, Gbare, G0, Sigma0, F0, mPi_factor=mPi_factor, precision=precision)
+
+
+class NL_ParquetSolver(_Solver):
+    local = False
+
+    def __init__(self, nK1, nK2, nK3, L, Gbare, G0, Sigma0, F0, *, mPi_factor=32, precision=0):
+        super().__init__(nK1, nK2, nK3, L, Gbare, G0, Sigma0, F0, mPi_factor=mPi_factor, precision=precision)
+
+
+def parquet_solver_siam_parquet_approximation(nG, nK1, nK2, nK3, *, e, Delta, D, T, U, mPi_factor=6, F0=None):
+    Gbare = siam_bare_Green(T, nG, Delta=Delta, e=e, D=D)
+    z = np.zeros_like(Gbare)
+    return ParquetSolver(nK1, nK2, nK3, Gbare, z, z, F0 or RefVertex(T, U), mPi_factor=mPi_factor)
+
+
+def parquet_solver_hubbard_parquet_approximation(nG, nK1, nK2, nK3, L, *, T, U, mu, t1, t2=0.0, t3=0.0,
+                                                 mPi_factor=32, F0=None):
+    Gbare = hubbard_bare_Green(T, nG, L, mu=mu, t1=t1, t2=t2, t3=t3)
+    z = np.zeros_like(Gbare)
+    return NL_ParquetSolver(nK1, nK2, nK3, L, Gbare, z, z, F0 or RefVertex(T, U), mPi_factor=mPi_factor)
+
+
+class PinnedBuffer:
+    """Page-locked host buffer of complex128 values (fdga_host_alloc)."""
+
+    def __init__(self, n):
+        lib = _lib.load()
+        self._lib = lib
+        p = ctypes.c_void_p()
+        _lib.check(lib.fdga_host_alloc(int(n) * 16, ctypes.byref(p)))
+        self.ptr = p.value
+        self.n = int(n)
+        self.array = np.ctypeslib.as_array((ctypes.c_double * (2 * self.n)).from_address(self.ptr)).view(np.complex128)
+
+    def free(self):
+        if self.ptr:
+            self._lib.fdga_host_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+
+# Julia-style free functions
+def init_sym_grp(S):
+    S.init_sym_grp()
+
+
+def iterate_solver(S, strategy="fdPA", update_Sigma=True, compute_Hartree=True):
+    S.iterate_solver(strategy, update_Sigma, compute_Hartree)
+
+
+def fixed_point(S, x, strategy="fdPA"):
+    return S.fixed_point(x, strategy)
+
+
+def solve(S, strategy="fdPA", maxiter=100, tol=1e-4, delta=0.85, mem=8):
+    return S.solve(strategy, maxiter, tol, delta, mem)
+
+
+def flatten(S):
+    return S.flatten()
+
+
+def unflatten(S, x):
+    S.unflatten(x)

@@ -1,0 +1,75 @@
+"""Seeded synthetic workloads of the benchmark configurations (host-side input generation).
+
+The reference names no dataset; these reproduce the configuration text: model, parameters, box
+sizes (read as the reference constructor arguments) and, for the nonlocal plain-method case, a
+seeded synthetic RefVertex.
+
+config1: SIAM, local fdPA, β=10, U=1, flat band Δ(iν) = -iΓ sign ν, Γ = 0.5 (D = ∞), e = 0,
+         nK1=64, nK2=(32,32), nK3=(16,16), nG=64, mΠν_factor=6.
+config2: Hubbard 8x8, nonlocal fdPA, t=1, t'=0, μ=0, U=2, β=5, nK1=32, nK2=(16,16), nK3=(8,12),
+         nG=32, mΠν_factor=32; F0 = RefVertex(U) with corrections on the K3 box drawn as
+         complex Gaussian noise σ = 0.05 U, symmetrised ν<->ν', scaled 1/sqrt((1+|ν|)(1+|ν'|)).
+"""
+import numpy as np
+
+from .models import fermionic_values
+from .solver import RefVertex
+
+CONFIGS = {
+    "config1": dict(kind="siam", T=0.1, U=1.0, e=0.0, Delta=0.5, D=float("inf"), nG=64, nK1=64, nK2=(32, 32),
+                    nK3=(16, 16), mPi_factor=6),
+    "config2": dict(kind="hubbard", T=0.2, U=2.0, mu=0.0, t1=1.0, t2=0.0, L=8, nG=32, nK1=32, nK2=(16, 16),
+                    nK3=(8, 12), mPi_factor=32, refvertex_noise=0.05, seed=20261203),
+    "config3": dict(kind="hubbard", T=0.1, U=3.0, mu=None, filling=0.9, t1=1.0, t2=-0.2, L=16, nG=80, nK1=80,
+                    nK2=(40, 40), nK3=(20, 40), mPi_factor=32),
+    "config5": dict(kind="hubbard", T=0.125, U=2.5, mu=0.0, t1=1.0, t2=0.0, L=24, nG=96, nK1=96, nK2=(48, 48),
+                    nK3=(24, 48), mPi_factor=32),
+}
+
+
+def synthetic_refvertex(T, U, nK3, sigma, seed):
+    """Seeded RefVertex corrections on the K3 box (see module docstring)."""
+    rng = np.random.default_rng(seed)
+    nO, nn = nK3
+    NO, Nn = 2 * nO - 1, 2 * nn
+    nu = np.abs(fermionic_values(T, nn))
+    w = 1.0 / np.sqrt((1 + nu[:, None]) * (1 + nu[None, :]))
+    out = []
+    for _ in range(4):
+        z = (rng.standard_normal((NO, Nn, Nn)) + 1j * rng.standard_normal((NO, Nn, Nn))) * (sigma * U / np.sqrt(2))
+        z = 0.5 * (z + np.transpose(z, (0, 2, 1)))
+        out.append(z * w[None, :, :])
+    return RefVertex(T, U, *out)
+
+
+def make_inputs(cfg):
+    """(Gbare, G0, Σ0, RefVertex) of a workload dict: kind 'siam' (local) or 'hubbard' (nonlocal)."""
+    from .models import hubbard_bare_Green, siam_bare_Green
+    T, U = cfg["T"], cfg["U"]
+    if cfg["kind"] == "siam":
+        Gb = siam_bare_Green(T, cfg["nG"], Delta=cfg["Delta"], e=cfg["e"], D=cfg["D"])
+    else:
+        Gb = hubbard_bare_Green(T, cfg["nG"], cfg["L"], mu=cfg["mu"], t1=cfg["t1"], t2=cfg.get("t2", 0.0))
+    G0 = cfg.get("G0")
+    S0 = cfg.get("Sigma0")
+    G0 = np.zeros_like(Gb) if G0 is None else G0
+    S0 = np.zeros_like(Gb) if S0 is None else S0
+    if cfg.get("refvertex_noise"):
+        rv = synthetic_refvertex(T, U, cfg.get("nR", cfg["nK3"]), cfg["refvertex_noise"], cfg.get("seed", 1))
+    else:
+        rv = RefVertex(T, U)
+    return Gb, G0, S0, rv
+
+
+def make_solver(cfg, sym=True):
+    """libfdga solver of a workload dict, with init_sym_grp! applied when sym."""
+    from .solver import NL_ParquetSolver, ParquetSolver
+    Gb, G0, S0, rv = make_inputs(cfg)
+    if cfg["kind"] == "siam":
+        S = ParquetSolver(cfg["nK1"], cfg["nK2"], cfg["nK3"], Gb, G0, S0, rv, mPi_factor=cfg["mPi_factor"])
+    else:
+        S = NL_ParquetSolver(cfg["nK1"], cfg["nK2"], cfg["nK3"], cfg["L"], Gb, G0, S0, rv,
+                             mPi_factor=cfg["mPi_factor"])
+    if sym:
+        S.init_sym_grp()
+    return S

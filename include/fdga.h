@@ -1,0 +1,137 @@
+/* fdga.h -- C ABI of libfdga, the GB300 (sm_103a) implementation of the parquet-iteration hot
+ * path of fdDGAsolver.jl.  Plain pointers and sizes only; complex arrays are interleaved
+ * (re, im) doubles, i.e. Julia ComplexF64 / C double _Complex, in the reference's own
+ * column-major layout (first mesh index fastest).  Every call returns 0 on success or a
+ * nonzero FDGA_ERR_* status; fdga_last_error() gives the message.  No entry point aborts
+ * or traps; there is no CPU fallback inside the library.
+ *
+ * One handle owns one solver's device state and one CUDA stream.  Calls on a handle must be
+ * serialised by the caller; distinct handles may be used concurrently.
+ */
+#ifndef FDGA_H
+#define FDGA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fdga_handle fdga_handle;
+
+enum {
+    FDGA_OK = 0,
+    FDGA_ERR_ARG = 1,        /* invalid dimensions, names or sizes */
+    FDGA_ERR_UNSUPPORTED = 2,/* a reference feature this build does not provide */
+    FDGA_ERR_CUDA = 3,       /* CUDA runtime / launch error (message has the CUDA text) */
+    FDGA_ERR_OOM = 4,        /* device allocation failed */
+    FDGA_ERR_NONFINITE = 5,  /* NaN/Inf in an input or state vector */
+    FDGA_ERR_STATE = 6       /* call order violated (e.g. iterate before finalize) */
+};
+
+enum { FDGA_FDPA = 0, FDGA_SCPA = 1 };          /* iterate_solver! strategy (src/solve.jl:10) */
+enum { FDGA_FP64 = 0 };                          /* arithmetic of the plain path */
+
+/* Solver dimensions: the reference constructor arguments
+ * ParquetSolver(nK1, nK2, nK3, Gbare, G0, Σ0, F0; mΠν_factor)         (src/ParquetSolver.jl:277-352)
+ * NL_ParquetSolver(nK1, nK2, nK3, mK_Γ, Gbare, G0, Σ0, F0; mΠν_factor) (src/nonlocal/ParquetSolver.jl:77-152)
+ * with the RefVertex reference vertex F0 = RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x)  (src/refvertex.jl:1-35). */
+typedef struct fdga_config {
+    int32_t nG;          /* Green-function mesh: 2nG fermionic frequencies */
+    int32_t nK1;         /* K1 box: 2nK1-1 bosonic frequencies */
+    int32_t nK2[2];      /* K2 box (bosonic, fermionic) */
+    int32_t nK3[2];      /* K3 box (bosonic, fermionic) */
+    int32_t L;           /* vertex momentum mesh L x L (1 for the local solver) */
+    int32_t LG;          /* Green-function momentum mesh; must equal L in this build */
+    int32_t mPi_factor;  /* bubble fermionic mesh = nK1 * mPi_factor (reference default 6 local, 32 NL) */
+    int32_t local;       /* 1: ParquetSolver (local BSE forms), 0: NL_ParquetSolver */
+    double T;            /* temperature */
+    double U;            /* bare interaction of the RefVertex */
+    int32_t nR[2];       /* box of the RefVertex corrections Fp_p .. Ft_x; (1,1) = bare U */
+    int32_t precision;   /* FDGA_FP64 */
+} fdga_config;
+
+/* Inputs uploaded with fdga_set_input (reference column-major layout). */
+enum {
+    FDGA_IN_GBARE = 0,   /* [2nG, L*L]          Gbare (stores i*G)                      */
+    FDGA_IN_G0 = 1,      /* [2nG, L*L]          G0                                       */
+    FDGA_IN_SIGMA0 = 2,  /* [2nG, L*L]          Σ0 (stores i*Σ)                          */
+    FDGA_IN_FP_P = 3,    /* [2nR0-1, 2nR1, 2nR1] RefVertex corrections                    */
+    FDGA_IN_FP_X = 4,
+    FDGA_IN_FT_P = 5,
+    FDGA_IN_FT_X = 6
+};
+
+/* Creates a handle (replaces the reference constructors above; allocates all device state). */
+int fdga_create(const fdga_config* cfg, fdga_handle** out);
+void fdga_destroy(fdga_handle* h);
+const char* fdga_last_error(const fdga_handle* h);
+/* Library-level error text for failures that happen before a handle exists. */
+const char* fdga_create_error(void);
+
+/* Uploads one input array; n = number of complex elements. */
+int fdga_set_input(fdga_handle* h, int which, const double* re_im, size_t n);
+
+/* Constructor tail: Π0 = bubble(G0), Σ = Σ0, G = Dyson(Σ), Π = bubble(G), F = 0
+ * (src/ParquetSolver.jl:291-310, src/nonlocal/ParquetSolver.jl:91-110). */
+int fdga_finalize(fdga_handle* h);
+
+/* init_sym_grp!(S) (src/ParquetSolver.jl:203-231, src/nonlocal/ParquetSolver.jl:198-300).
+ * Without it every element is evaluated directly (the constructor's trivial groups). */
+int fdga_init_sym_grp(fdga_handle* h);
+/* Host-only (no device needed): the class map of one init_sym_grp! group for a configuration,
+ * which = 0 Σ, 1 K1, 2 K2pp, 3 K2ph, 4 K3pp, 5 K3ph, 6 K3ppL, 7 K3phL; map[i] (device index i)
+ * = representative*4 + op (bit 0 sign, bit 1 conjugation); n = number of mesh points. */
+int fdga_group_map(const fdga_config* cfg, int which, uint32_t* map, size_t n, int* nclasses);
+
+/* Length (complex elements) of flatten(S) = [γp(K1,K2,K3), γt, γa, Σ] (src/ParquetSolver.jl:277-306). */
+int fdga_state_len(const fdga_handle* h, size_t* n);
+int fdga_flatten(fdga_handle* h, double* x, size_t n);
+int fdga_unflatten(fdga_handle* h, const double* x, size_t n);
+
+/* iterate_solver!(S; strategy, update_Σ, compute_Hartree) (src/solve.jl:4-116): one parquet
+ * iteration on the device state, replayed as one CUDA graph. */
+int fdga_iterate(fdga_handle* h, int strategy, int update_sigma, int compute_hartree);
+
+/* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.
+ * x and R are host arrays of fdga_state_len elements. */
+int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size_t n);
+
+/* solve!(S; maxiter, tol, δ, mem) (src/solve.jl:160-196): Anderson acceleration (NLsolve
+ * method=:anderson, m = mem, beta = δ, ftol = tol on max|R|) run on the device.
+ * Returns the iteration count in *iters (negative when not converged), the last max|R| in
+ * *res and, if trace != NULL, max|R| per iteration (maxiter doubles). */
+int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem,
+               int* iters, double* res, double* trace);
+
+/* Named device arrays in the reference layout, for inspection and tests:
+ * "G", "Sigma", "Gbare", "G0", "Sigma0", "Pipp", "Piph", "Pi0pp", "Pi0ph", "Lpp", "Lph",
+ * "F.<p|t|a>.<K1|K2|K3>", "FL.<p|t|a>.<K2|K3>", "cache_<Gpx|F0p|F0a|F0t|Gpp|Ga|Gt|Fp|Fa|Ft>". */
+int fdga_get_named(fdga_handle* h, const char* name, double* out, size_t n);
+int fdga_named_len(const fdga_handle* h, const char* name, size_t* n);
+
+/* Occupation n = 1/2 + T Im Σ G / Nk of the current G (src/dyson.jl:33-41). */
+int fdga_occupation(fdga_handle* h, double* n);
+
+/* Device timing on the handle's stream (CUDA events), for benchmarks. slot in [0, 8). */
+int fdga_event_record(fdga_handle* h, int slot);
+int fdga_event_elapsed_ms(fdga_handle* h, int slot_a, int slot_b, float* ms);
+int fdga_synchronize(fdga_handle* h);
+/* Per-stage device time of one eager (non-graph) iteration, averaged over nrep runs; the state
+ * advances by nrep iterations.  names receives a comma-separated stage list. */
+int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms,
+                     int max_stages, int* nstages);
+/* Applies the iteration map n times to the unchanged device state x (graph replays, no host
+ * synchronisation): the device-resident timing loop of the benchmark. */
+int fdga_map_repeat(fdga_handle* h, int strategy, int n);
+/* Page-locked host buffers for host<->device copies of state vectors. */
+int fdga_host_alloc(size_t bytes, void** p);
+int fdga_host_free(void* p);
+/* Number of kernel launches made by the last fdga_iterate (graph nodes). */
+int fdga_launches_per_iteration(const fdga_handle* h, int* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDGA_H */
