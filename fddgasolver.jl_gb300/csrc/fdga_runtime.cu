@@ -39,6 +39,10 @@ struct Graph {
 
 }  // namespace
 
+namespace fdga_internal {
+void set_create_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace fdga_internal
+
 struct fdga_handle {
     fdga_config cfg{};
     Dims d{};

@@ -51,6 +51,8 @@ EXPORTS = {
     "fdga_map_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "fdga_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "fdga_host_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "fdga_bubble_noalloc": (ctypes.c_int, [ctypes.POINTER(fdga_config), ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p]),
     "fdga_launches_per_iteration": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
 }
 

@@ -131,6 +131,27 @@ int fdga_host_free(void* p);
 /* Number of kernel launches made by the last fdga_iterate (graph nodes). */
 int fdga_launches_per_iteration(const fdga_handle* h, int* n);
 
+/* ---- Allocation-free bubble (no counterpart in the reference) ----------------------------
+ * For callers that cannot call cudaMalloc: a host whose own pool allocator owns the device
+ * memory (for example a Julia CUDA.jl or PyTorch process), or code on a path where cudaMalloc's
+ * implicit device synchronisation is not allowed.  The caller passes DEVICE pointers:
+ *   G     [2nG, L*L] complex (i*G, column-major [ν, k]),
+ *   Pipp, Piph  [2nK1-1, 2nK1*mPi_factor, L*L] complex outputs (column-major [Ω, ν, P]),
+ * and cfg supplies nG, nK1, mPi_factor, L (= LG), T, local.  The result equals the bubbles that
+ * fdga_finalize computes for G0 (src/nonlocal/bubble.jl:87-158, src/bubble.jl:9-36).
+ * No device or host memory is allocated: the work array G(R) lives in one file-scope __device__
+ * buffer of FDGA_BUBBLE_NOALLOC_MAX_ELEMS complex values (2 MiB), which every GPU that loads the
+ * library holds until the process exits.  Larger problems (2nG*L*L above the maximum, or L > 64)
+ * are rejected with FDGA_ERR_ARG and a message in fdga_last_error(NULL).
+ * The first call on a device looks up the buffer's device address (cudaGetSymbolAddress with that
+ * device current); make that first call before any stream capture.
+ * Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and the call returns
+ * without synchronising.  All calls share the one buffer and it keeps the last call's contents,
+ * so calls whose kernels overlap on the GPU (different streams or threads without ordering)
+ * race on it: serialise them. */
+#define FDGA_BUBBLE_NOALLOC_MAX_ELEMS 131072
+int fdga_bubble_noalloc(const fdga_config* cfg, const double* G, double* Pipp, double* Piph, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
