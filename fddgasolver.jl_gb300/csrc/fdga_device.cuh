@@ -224,6 +224,42 @@ __device__ __forceinline__ cplx fl_right(const cplx* FLK2p, const cplx* FLK2t, c
 
 __device__ __forceinline__ int cross(int ch, int m, int n) { return ch == CH_P ? m - n - 1 : n; }
 
+// A union of at most 6 closed ω intervals, merged and ordered; used to visit only the bubble
+// frequencies at which a vertex factor differs from its ω-independent value.
+struct Windows {
+    int lo[6], hi[6];
+    int n = 0, total = 0;
+    __device__ __forceinline__ void add(int a, int b, int clo, int chi) {
+        a = max(a, clo);
+        b = min(b, chi);
+        if (a <= b && n < 6) { lo[n] = a; hi[n] = b; ++n; }
+    }
+    __device__ __forceinline__ void merge() {
+        for (int i = 1; i < n; ++i)  // insertion sort by lo
+            for (int j = i; j > 0 && lo[j] < lo[j - 1]; --j) {
+                int t = lo[j]; lo[j] = lo[j - 1]; lo[j - 1] = t;
+                t = hi[j]; hi[j] = hi[j - 1]; hi[j - 1] = t;
+            }
+        int m = 0;
+        for (int i = 0; i < n; ++i) {
+            if (m > 0 && lo[i] <= hi[m - 1] + 1) { hi[m - 1] = max(hi[m - 1], hi[i]); }
+            else { lo[m] = lo[i]; hi[m] = hi[i]; ++m; }
+        }
+        n = m;
+        total = 0;
+        for (int i = 0; i < n; ++i) total += hi[i] - lo[i] + 1;
+    }
+    // t-th frequency of the union, t < total
+    __device__ __forceinline__ int at(int t) const {
+        for (int i = 0; i < n; ++i) {
+            const int len = hi[i] - lo[i] + 1;
+            if (t < len) return lo[i] + t;
+            t -= len;
+        }
+        return lo[0];
+    }
+};
+
 // warp reduction of a complex double
 __device__ __forceinline__ cplx warp_sum(cplx v) {
 #pragma unroll

@@ -7,6 +7,7 @@
 #include "fdga_kernels.h"
 
 #include <algorithm>
+#include <cmath>
 
 namespace fdga {
 
@@ -128,6 +129,102 @@ __global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
     }
 }
 
+// Radix-2 FFT variant of k_bubble_nl for power-of-two L (same mathematics; the R->P transform
+// costs O(L log L) per row instead of O(L²)).  c_twp32[j] = e^{+2πi j/32}.
+__constant__ cplx c_twp32[32];
+
+template <int L>
+__host__ __device__ constexpr int bitrev(int i) {
+    int r = 0;
+    for (int b = 1; b < L; b <<= 1) { r = (r << 1) | (i & 1); i >>= 1; }
+    return r;
+}
+
+// in-place backward DFT (e^{+2πi jk/L}) of v[0..L) held in registers
+template <int L>
+__device__ __forceinline__ void fft_bwd(cplx (&v)[L]) {
+#pragma unroll
+    for (int i = 0; i < L; ++i) {
+        const int j = bitrev<L>(i);
+        if (j > i) { const cplx t = v[i]; v[i] = v[j]; v[j] = t; }
+    }
+#pragma unroll
+    for (int len = 2; len <= L; len <<= 1) {
+        const int half = len / 2;
+#pragma unroll
+        for (int i = 0; i < L; i += len) {
+#pragma unroll
+            for (int k = 0; k < half; ++k) {
+                const cplx b = v[i + k + half];
+                cplx t;
+                if (k == 0) t = b;
+                else if (4 * k == len) t = mk(-b.y, b.x);  // multiply by i
+                else t = b * c_twp32[k * (32 / len)];
+                const cplx u = v[i + k];
+                v[i + k] = u + t;
+                v[i + k + half] = u - t;
+            }
+        }
+    }
+}
+
+template <int L>
+__global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV) {
+    extern __shared__ cplx sh[];
+    constexpr int NR = L * L, RS = L + 1, BS = L * (L + 1) + 1;
+    const int m = blockIdx.y - (d.nPO - 1);
+    const int n0 = blockIdx.x * TV - d.nPn;
+    for (int e = threadIdx.x; e < TV * NR; e += blockDim.x) {
+        const int v = e / NR, R = e % NR;
+        const int n = n0 + v;
+        const int Rx = R % L, Ry = R / L;
+        cplx vpp = mk(0, 0), vph = mk(0, 0);
+        if (n < d.nPn) {
+            const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
+            if (R == 0) {
+                vpp = g_tail(GR, d, 0, m - n - 1) * g_tail(GR, d, 0, n);
+                vph = g_tail(GR, d, 0, m + n) * g_tail(GR, d, 0, n);
+            } else {
+                const int a = m - n - 1, b = m + n;
+                if (fin(a, d.nG) && fin(n, d.nG)) vpp = GR[ixG(d, R, a)] * GR[ixG(d, R, n)];
+                if (fin(b, d.nG) && fin(n, d.nG)) vph = GR[ixG(d, R, b)] * GR[ixG(d, mR, n)];
+            }
+        }
+        sh[(size_t)v * BS + Ry * RS + Rx] = vpp;
+        sh[(size_t)(TV + v) * BS + Ry * RS + Rx] = vph;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < 2 * TV * L; r += blockDim.x) {  // along x
+        cplx* row = sh + (size_t)(r / L) * BS + (r % L) * RS;
+        cplx v[L];
+#pragma unroll
+        for (int x = 0; x < L; ++x) v[x] = row[x];
+        fft_bwd<L>(v);
+#pragma unroll
+        for (int x = 0; x < L; ++x) row[x] = v[x];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < 2 * TV * L; c += blockDim.x) {  // along y
+        cplx* col = sh + (size_t)(c / L) * BS + (c % L);
+        cplx v[L];
+#pragma unroll
+        for (int y = 0; y < L; ++y) v[y] = col[y * RS];
+        fft_bwd<L>(v);
+#pragma unroll
+        for (int y = 0; y < L; ++y) col[y * RS] = v[y];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 2 * TV * NR; e += blockDim.x) {
+        const int v = e % TV;
+        const int rest = e / TV;
+        const int P = rest % NR, which = rest / NR;
+        const int n = n0 + v;
+        if (n >= d.nPn) continue;
+        const cplx val = sh[(size_t)(which * TV + v) * BS + (P / L) * RS + (P % L)];
+        (which ? ph : pp)[ixPi(d, P, m, n)] = val;
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Momentum averages A = Σ_P K[P] / Nq (s-wave evaluation, src/nonlocal/swave.jl:32-72)
 // blockIdx.y = channel*3 + class
@@ -180,28 +277,84 @@ __global__ void k_build_cache(VertP F, Caches C, Dims d) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// Bubble row sums SΠ(P, Ω) = Σ_ν Π(P, Ω, ν) over the whole bubble mesh; blockIdx.y = array.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_rowsum(const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, int rowlen) {
+    __shared__ double rx[256], ry[256];
+    const cplx* A = blockIdx.y ? A1 : A0;
+    cplx* S = blockIdx.y ? S1 : S0;
+    const size_t row = blockIdx.x;
+    double sx = 0.0, sy = 0.0;
+    for (int i = threadIdx.x; i < rowlen; i += blockDim.x) {
+        const cplx v = A[row * rowlen + i];
+        sx += v.x;
+        sy += v.y;
+    }
+    rx[threadIdx.x] = sx;
+    ry[threadIdx.x] = sy;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) { rx[threadIdx.x] += rx[threadIdx.x + o]; ry[threadIdx.x] += ry[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) S[row] = mk(rx[0], ry[0]);
+}
+
+// S_X(ch, P, Ω) = Σ_ω [(Π-Π0)(Ω,ω,P) U + Π(Ω,ω,P) FL(Ω,ω̃,∞)]: the ω-sum of the BSE's right factor
+// (src/BSEa/BSEa_K1.jl:43, BSEa_K2.jl:185), from the row sums and the K2 window of FL.
+// Layout SX[ch][P][Ω] with Ω over the K1 box; SPi/SPi0 [w][P][Ω] with w = 0 pp, 1 ph.
+__global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0, FLP FL, cplx* SX, Dims d) {
+    const size_t per = (size_t)d.Nq * d.NPO;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= 3 * per) return;
+    const int ch = (int)(i / per);
+    const size_t r = i % per;
+    const int m = (int)(r % d.NPO) - (d.nPO - 1), P = (int)(r / d.NPO);
+    const int w = (ch == CH_P) ? 0 : 1;
+    const cplx* Pi = w ? Piph : Pipp;
+    cplx v = (SPi[w * per + r] - SPi0[w * per + r]) * d.U;
+    if (bin(m, d.n2O)) {
+        for (int nt = -d.n2n; nt < d.n2n; ++nt) {
+            const int n = (ch == CH_P) ? m - nt - 1 : nt;
+            if (!fin(n, d.nPn)) continue;
+            v += Pi[ixPi(d, P, m, n)] * fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, ch, m, nt, P);
+        }
+    }
+    SX[i] = v;
+}
+
+// ---------------------------------------------------------------------------------------------
 // K1 BSE (src/BSEa/BSEa_K1.jl:2-54, src/nonlocal/BSEa/BSEa_K1.jl:2-57), warp per item:
-//   K1(Ω,P) = T s Σ_ω F(Ω,∞,ω) [(Π-Π0)(Ω,ω) U + Π(Ω,ω) FL(Ω,ω̃,∞)]
+//   K1(Ω,P) = T s Σ_ω F(Ω,∞,ω) X(ω),  X(ω) = (Π-Π0)(Ω,ω) U + Π(Ω,ω) FL(Ω,ω̃,∞).
+// F(Ω,∞,ω) depends on ω only through the same channel's K2(Ω, ω) (ω in the K2 box), so the sum is
+// evaluated exactly as c·S_X + Σ_{ω ∈ K2 box} (F(Ω,∞,ω) - c) X(ω), c = F(Ω,∞,∞).
 // ---------------------------------------------------------------------------------------------
 template <int CH>
-__global__ void k_bse_K1(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, cplx* out, const int* items, int nitems,
-                         Dims d) {
+__global__ void k_bse_K1(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const cplx* SX, cplx* out,
+                         const int* items, int nitems, Dims d) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
     const int m = idx % d.N1 - (d.n1 - 1), P = idx / d.N1;
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
+    const cplx c = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
     cplx acc = mk(0, 0);
-    for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
-        const int wt = cross(CH, m, n);
-        const cplx Fl = vert_eval(F, d, CH, SP, m, FINF, n, P);
-        const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
-        const size_t ip = ixPi(d, P, m, n);
-        const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
-        acc += Fl * ((pi - pi0) * d.U + pi * FLr);
+    if (bin(m, d.n2O)) {
+        for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
+            if (!fin(n, d.nPn)) continue;
+            const int wt = cross(CH, m, n);
+            const cplx Fl = vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
+            const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
+            const size_t ip = ixPi(d, P, m, n);
+            const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
+            acc += Fl * ((pi - pi0) * d.U + pi * FLr);
+        }
     }
     acc = warp_sum(acc);
-    if (lane == 0) out[idx] = acc * (d.T * (CH == CH_T ? -1.0 : 1.0));
+    if (lane == 0) {
+        const cplx sx = SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)];
+        out[idx] = (c * sx + acc) * (d.T * (CH == CH_T ? -1.0 : 1.0));
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -237,11 +390,16 @@ __global__ void k_bse_L_K2(VertP F, const cplx* Pi0, cplx* out, const int* items
 
 // ---------------------------------------------------------------------------------------------
 // K2 BSE (src/BSEa/BSEa_K2.jl:43-103, src/nonlocal/BSEa/BSEa_K2.jl:43-105), warp per item:
-//   T s Σ_ω [F(Ω,ν,ω) - F(Ω,∞,ω)] [(Π-Π0)(Ω,ω) U + Π(Ω,ω) FL(Ω,ω̃,∞)]
+//   T s Σ_ω [F(Ω,ν,ω) - F(Ω,∞,ω)] X(ω).
+// Outside the union of (i) the K2 and RefVertex fermionic boxes and (ii) the ω for which a
+// converted bosonic frequency of another channel lies in the K1 box (centres ν, -(Ω+ν+1) and,
+// for the p channel, Ω-ν-1; src/convention.jl:4-36), F(Ω,ν,ω) - F(Ω,∞,ω) equals its
+// ω-independent value c = F(Ω,ν,∞) - F(Ω,∞,∞); the sum is evaluated exactly as
+// c·S_X + Σ_{ω ∈ union} (F(Ω,ν,ω) - F(Ω,∞,ω) - c) X(ω).
 // ---------------------------------------------------------------------------------------------
 template <int CH>
-__global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, cplx* out, const int* items, int nitems,
-                         Dims d) {
+__global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const cplx* SX, cplx* out,
+                         const int* items, int nitems, Dims d) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
@@ -249,48 +407,67 @@ __global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, cplx*
     const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
     const int P = idx / (d.N2n * d.N2O);
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
+    const cplx c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    Windows win;
+    const int lo = -d.nPn, hi = d.nPn - 1, h1 = d.n1 - 1;
+    win.add(-d.n2n, d.n2n - 1, lo, hi);
+    win.add(-d.nRn, d.nRn - 1, lo, hi);
+    win.add(nu - h1, nu + h1, lo, hi);
+    win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
+    if (CH == CH_P) win.add(m - nu - 1 - h1, m - nu - 1 + h1, lo, hi);
+    win.merge();
     cplx acc = mk(0, 0);
-    for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
+    for (int t = lane; t < win.total; t += 32) {
+        const int n = win.at(t);
         const int wt = cross(CH, m, n);
-        const cplx Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - vert_eval(F, d, CH, SP, m, FINF, n, P);
+        const cplx Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
         const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
         const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
         acc += Fl * ((pi - pi0) * d.U + pi * FLr);
     }
     acc = warp_sum(acc);
-    if (lane == 0) out[idx] = acc * (d.T * (CH == CH_T ? -1.0 : 1.0));
+    if (lane == 0) {
+        const cplx sx = SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)];
+        out[idx] = (c * sx + acc) * (d.T * (CH == CH_T ? -1.0 : 1.0));
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
-// K3 BSE as one complex GEMM per (P, Ω) block, C = A·M (src/BSEa/BSEa_K3.jl:1-128,
+// K3 BSE as one complex GEMM per (ch, P, Ω) block, C = A·M (src/BSEa/BSEa_K3.jl:1-128,
 // src/nonlocal/BSEa/BSEa_K3.jl:1-128):
 //   MODE 0 (BSE_L_K3):  A = cacheΓ(ν,ω),  M(ω,ν') = Π0(ω) cacheF0(ω,ν');          out = T s C
 //   MODE 1 (BSE_K3):    A = cacheF(ν,ω),  M(ω,ν') = s1[(Π-Π0)(ω) cacheF0(ω,ν') + Π(ω) Γs(ω,ν')]
 //                                                    + s2 Π(ω) γL(ω̃,ν')[ω̃ in box]; out = T C + γL(ν,ν')
-// 32x32 output tile, 16x16 threads with 2x2 outputs each, K chunks of 8.
+// TILE x TILE output tile per CTA (TILE = 16, 24 or 32 chosen to fit Nν), (TILE/2)^2 threads with
+// 2x2 outputs each, K chunks of 8.  blockIdx.x = channel-slot * (Nq·NΩ3) + (P·NΩ3 + iΩ), blockIdx.y /
+// blockIdx.z = row / column tile; the three channels of one mode share a launch.
 // ---------------------------------------------------------------------------------------------
-template <int MODE, int CH>
-__global__ void __launch_bounds__(256) k_bse_K3_gemm(K3Args a, Dims d) {
-    constexpr int TM = 32, TK = 8;
-    __shared__ cplx As[TM][TK + 1];
-    __shared__ cplx Ms[TK][TM + 1];
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    const int col0 = blockIdx.x * TM, row0 = blockIdx.y * TM;
-    const int blk = blockIdx.z;  // P * N3O + iΩ
+template <int MODE, int TILE>
+__global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3 args, Dims d) {
+    constexpr int TK = 8, H = TILE / 2, NT = H * H;
+    __shared__ cplx As[TILE][TK + 1];
+    __shared__ cplx Ms[TK][TILE + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % H, ty = tid / H;
+    const int col0 = blockIdx.z * TILE, row0 = blockIdx.y * TILE;
+    const int nblk = d.Nq * d.N3O;
+    const int slot = blockIdx.x / nblk, blk = blockIdx.x % nblk;
+    const K3Args& a = args.a[slot];
+    const int CH = args.ch[slot];
     const int m = blk % d.N3O - (d.n3O - 1), P = blk / d.N3O;
     const int N = d.N3n;
     const size_t base = (size_t)blk * N * N;
     const double s1 = (CH == CH_A) ? 1.0 : -1.0, s2 = (CH == CH_T) ? -1.0 : 1.0;
     cplx acc[2][2] = {{mk(0, 0), mk(0, 0)}, {mk(0, 0), mk(0, 0)}};
     for (int k0 = 0; k0 < N; k0 += TK) {
-        {  // A tile: 32 x 8, one element per thread
-            const int r = threadIdx.x / TK, kk = threadIdx.x % TK;
+        for (int e = tid; e < TILE * TK; e += NT) {
+            const int r = e / TK, kk = e % TK;
             const int row = row0 + r, k = k0 + kk;
             As[r][kk] = (row < N && k < N) ? ldg(a.A + base + (size_t)row * N + k) : mk(0, 0);
         }
-        {  // M tile: 8 x 32
-            const int kk = threadIdx.x / TM, c = threadIdx.x % TM;
+        for (int e = tid; e < TK * TILE; e += NT) {
+            const int kk = e / TILE, c = e % TILE;
             const int k = k0 + kk, col = col0 + c;
             cplx v = mk(0, 0);
             if (k < N && col < N) {
@@ -317,8 +494,8 @@ __global__ void __launch_bounds__(256) k_bse_K3_gemm(K3Args a, Dims d) {
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < TK; ++kk) {
-            const cplx a0 = As[ty][kk], a1 = As[ty + 16][kk];
-            const cplx b0 = Ms[kk][tx], b1 = Ms[kk][tx + 16];
+            const cplx a0 = As[ty][kk], a1 = As[ty + H][kk];
+            const cplx b0 = Ms[kk][tx], b1 = Ms[kk][tx + H];
             acc[0][0] += a0 * b0;
             acc[0][1] += a0 * b1;
             acc[1][0] += a1 * b0;
@@ -330,7 +507,7 @@ __global__ void __launch_bounds__(256) k_bse_K3_gemm(K3Args a, Dims d) {
     for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const int row = row0 + ty + 16 * i, col = col0 + tx + 16 * j;
+            const int row = row0 + ty + H * i, col = col0 + tx + H * j;
             if (row >= N || col >= N) continue;
             const size_t io = base + (size_t)row * N + col;
             if (MODE == 0) {
@@ -380,60 +557,82 @@ __global__ void k_k2_epilogue(cplx* out, const cplx* FLc, const cplx* FLt, const
 // SDE: L_pp, L_ph (src/SDE.jl:79-217, src/nonlocal/SDE.jl:3-143), warp per item.
 //   vertex part:    L_pp = T U Σ_ω Πpp(Ω,ω) γp(Ω,Ω-ω,ν),  L_ph = T U Σ_ω Πph(Ω,ω) (γt+γa)(Ω,ν,ω)
 //   RefVertex part: L_pp = T U Σ_ω Πpp (F0_p(Ω,Ω-ω,ν) - U),  L_ph = T U Σ_ω Πph (F0_a + F0_t - 2U)
-// WHICH: 0 = pp, 1 = ph.  REF: 0 vertex, 1 RefVertex.  out = vertex part + ref part / 3 is formed
-// by the caller through 'scale'.
+// The channel factor depends on ω only where the ω-argument lies in the K2 (vertex) or RefVertex
+// box; elsewhere it equals c = γ(…, ν, ∞), so the vertex sum is c·SΠ + Σ_{window} Π (γ - c).
+// out = T [vertex part] + T ref_scale [RefVertex part].
 // ---------------------------------------------------------------------------------------------
-template <int WHICH, int REF>
-__global__ void k_sde_L(VertP F, const cplx* Pi, cplx* out, const int* items, int nitems, double scale, int accumulate,
-                        Dims d) {
+template <int WHICH>
+__global__ void k_sde_L(VertP F, const cplx* Pi, const cplx* SPi, cplx* out, const int* items, int nitems,
+                        int use_vertex, double ref_scale, Dims d) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
     const int nu = idx % d.N2n - d.n2n;
     const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
     const int P = idx / (d.N2n * d.N2O);
-    cplx acc = mk(0, 0);
-    for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
-        const cplx up = ldg(Pi + ixPi(d, P, m, n)) * d.U;
-        cplx g;
-        if (REF == 0) {
-            if (WHICH == 0) g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P);
-            else g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P);
+    cplx acc = mk(0, 0), accr = mk(0, 0), c = mk(0, 0);
+    if (use_vertex) {
+        if (WHICH == 0) {
+            c = chan_eval(F.g[CH_P], d, m, FINF, nu, P);
+            for (int t = lane; t < d.N2n; t += 32) {
+                const int n = m - (t - d.n2n) - 1;  // Ω-ω runs over the K2 box
+                if (!fin(n, d.nPn)) continue;
+                const cplx g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P) - c;
+                acc += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
+            }
         } else {
+            c = chan_eval(F.g[CH_T], d, m, nu, FINF, P) + chan_eval(F.g[CH_A], d, m, nu, FINF, P);
+            for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
+                if (!fin(n, d.nPn)) continue;
+                const cplx g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P) - c;
+                acc += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
+            }
+        }
+    }
+    if (ref_scale != 0.0) {
+        for (int t = lane; t < d.NRn; t += 32) {
+            const int r = t - d.nRn;
+            const int n = (WHICH == 0) ? m - r - 1 : r;
+            if (!fin(n, d.nPn)) continue;
+            cplx g;
             if (WHICH == 0) g = ref_pSp(F, d, CH_P, m, m - n - 1, nu) - mk(d.U, 0);
             else g = ref_pSp(F, d, CH_A, m, nu, n) + ref_pSp(F, d, CH_T, m, nu, n) - mk(d.U, 0) - mk(d.U, 0);
+            accr += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
         }
-        acc += up * g;
     }
     acc = warp_sum(acc);
+    accr = warp_sum(accr);
     if (lane == 0) {
-        const cplx v = acc * (d.T * scale);
-        out[idx] = accumulate ? out[idx] + v : v;
+        if (use_vertex) acc += c * (ldg(SPi + (size_t)P * d.NPO + (m + d.nPO - 1)) * d.U);
+        out[idx] = acc * d.T + accr * (d.T * ref_scale);
     }
 }
 
 // Σ_inner(ν,k) = T/N Σ_{Ω,P} [G(Ω-ν, P-k) Lpp(Ω,ν,P) + G(Ω+ν, P+k) Lph(Ω,ν,P)]
-// (momentum-space form of src/nonlocal/SDE.jl:208-280 for L_G = L; local: src/SDE.jl:241-263)
+// (momentum-space form of src/nonlocal/SDE.jl:208-280 for L_G = L; local: src/SDE.jl:241-263);
+// one warp per output, lanes over (P, Ω).
 __global__ void k_sde_sigma(const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, Dims d) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= (size_t)d.Nk * d.NG) return;
-    const int nu = (int)(i % d.NG) - d.nG, k = (int)(i / d.NG);
+    const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (size_t)d.Nk * d.NG) return;
+    const int nu = (int)(w % d.NG) - d.nG, k = (int)(w / d.NG);
     cplx acc = mk(0, 0);
     if (fin(nu, d.n2n)) {
         const int L = d.L, kx = k % L, ky = k / L;
-        for (int P = 0; P < d.Nq; ++P) {
+        const int npair = d.Nq * d.N2O;
+        for (int t = lane; t < npair; t += 32) {
+            const int P = t / d.N2O, m = t % d.N2O - (d.n2O - 1);
             const int Px = P % L, Py = P / L;
             const int kmP = ((Px - kx + L) % L) + L * ((Py - ky + L) % L);
             const int kpP = ((Px + kx) % L) + L * ((Py + ky) % L);
-            for (int m = -(d.n2O - 1); m <= d.n2O - 1; ++m) {
-                const size_t il = ix2(d, P, m, nu);
-                const int a = m - nu - 1, b = m + nu;
-                if (fin(a, d.nG)) acc += G[ixG(d, kmP, a)] * Lpp[il];
-                if (fin(b, d.nG)) acc += G[ixG(d, kpP, b)] * Lph[il];
-            }
+            const size_t il = ix2(d, P, m, nu);
+            const int a = m - nu - 1, b = m + nu;
+            if (fin(a, d.nG)) acc += ldg(G + ixG(d, kmP, a)) * ldg(Lpp + il);
+            if (fin(b, d.nG)) acc += ldg(G + ixG(d, kpP, b)) * ldg(Lph + il);
         }
     }
-    S[i] = acc * (d.T / d.Nq);
+    acc = warp_sum(acc);
+    if (lane == 0) S[w] = acc * (d.T / d.Nq);
 }
 
 // U² term (src/SDE.jl:328-364, src/nonlocal/SDE.jl:400-447), factorised:
@@ -601,24 +800,67 @@ int bubble_tile(const Dims& d) {
     while (tv > 1 && (size_t)4 * tv * NR * sizeof(cplx) > 160 * 1024) tv >>= 1;
     return tv;
 }
+template <int L>
+static cudaError_t launch_bubble_fft(cudaStream_t s, const cplx* GR, cplx* pp, cplx* ph, const Dims& d) {
+    constexpr int BS = L * (L + 1) + 1;
+    int tv = 32;
+    while (tv > 1 && (size_t)2 * tv * BS * sizeof(cplx) > 80 * 1024) tv >>= 1;
+    const size_t shm = (size_t)2 * tv * BS * sizeof(cplx);
+    static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
+    if (shm > 48 * 1024 && shm > shm_set) {
+        cudaFuncSetAttribute(k_bubble_fft<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        shm_set = shm;
+    }
+    dim3 grid((d.NPn + tv - 1) / tv, d.NPO);
+    k_bubble_fft<L><<<grid, 256, shm, s>>>(GR, pp, ph, d, tv);
+    return cudaGetLastError();
+}
+
+cudaError_t set_fft_twiddles() {
+    cplx tw[32];
+    for (int j = 0; j < 32; ++j) tw[j] = mk(std::cos(2.0 * M_PI * j / 32.0), std::sin(2.0 * M_PI * j / 32.0));
+    return cudaMemcpyToSymbol(c_twp32, tw, sizeof(tw));
+}
+
 cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
                           const Dims& d) {
     if (d.local) {
         const size_t n = (size_t)d.NPO * d.NPn;
         k_bubble_local<<<blocks_for(n, 256), 256, 0, s>>>(G, pp, ph, d);
-    } else {
-        const int tv = bubble_tile(d);
-        const size_t shm = (size_t)4 * tv * d.L * d.L * sizeof(cplx);
-        static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
-        if (shm > 48 * 1024 && shm > shm_set) {
-            cudaFuncSetAttribute(k_bubble_nl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-            shm_set = shm;
-        }
-        dim3 grid((d.NPn + tv - 1) / tv, d.NPO);
-        k_bubble_nl<<<grid, 256, shm, s>>>(GR, pp, ph, twp, d, tv);
+        LAUNCH_CHECK(); return cudaSuccess;
     }
+    switch (d.L) {
+        case 2: return launch_bubble_fft<2>(s, GR, pp, ph, d);
+        case 4: return launch_bubble_fft<4>(s, GR, pp, ph, d);
+        case 8: return launch_bubble_fft<8>(s, GR, pp, ph, d);
+        case 16: return launch_bubble_fft<16>(s, GR, pp, ph, d);
+        case 32: return launch_bubble_fft<32>(s, GR, pp, ph, d);
+        default: break;
+    }
+    const int tv = bubble_tile(d);
+    const size_t shm = (size_t)4 * tv * d.L * d.L * sizeof(cplx);
+    static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
+    if (shm > 48 * 1024 && shm > shm_set) {
+        cudaFuncSetAttribute(k_bubble_nl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        shm_set = shm;
+    }
+    dim3 grid((d.NPn + tv - 1) / tv, d.NPO);
+    k_bubble_nl<<<grid, 256, shm, s>>>(GR, pp, ph, twp, d, tv);
     LAUNCH_CHECK(); return cudaSuccess;
 }
+
+cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, const Dims& d) {
+    dim3 grid((unsigned)(d.Nq * d.NPO), 2);
+    k_rowsum<<<grid, 256, 0, s>>>(A0, A1, S0, S1, d.NPn);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
+                      const FLP& FL, cplx* SX, const Dims& d) {
+    const size_t n = (size_t)3 * d.Nq * d.NPO;
+    k_sx<<<blocks_for(n, 128), 128, 0, s>>>(Pipp, Piph, SPi, SPi0, FL, SX, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+
 cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d) {
     const size_t per = std::max((size_t)d.N1, std::max((size_t)d.N2O * d.N2n, (size_t)d.N3O * d.N3n * d.N3n));
     dim3 grid(blocks_for(per, 256), 9);
@@ -631,11 +873,11 @@ cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, 
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          cplx* out, const int* items, int nitems, const Dims& d) {
+                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
     const unsigned g = blocks_for((size_t)nitems * 32, 128);
-    if (ch == CH_P) k_bse_K1<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
-    else if (ch == CH_T) k_bse_K1<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
-    else k_bse_K1<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    if (ch == CH_P) k_bse_K1<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
+    else if (ch == CH_T) k_bse_K1<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
+    else k_bse_K1<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* Pi0, cplx* out, const int* items,
@@ -647,25 +889,30 @@ cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* 
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_bse_K2(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          cplx* out, const int* items, int nitems, const Dims& d) {
+                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
     const unsigned g = blocks_for((size_t)nitems * 32, 128);
-    if (ch == CH_P) k_bse_K2<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
-    else if (ch == CH_T) k_bse_K2<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
-    else k_bse_K2<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, out, items, nitems, d);
+    if (ch == CH_P) k_bse_K2<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
+    else if (ch == CH_T) k_bse_K2<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
+    else k_bse_K2<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_bse_K3(cudaStream_t s, int mode, int ch, const K3Args& a, const Dims& d) {
-    dim3 grid((d.N3n + 31) / 32, (d.N3n + 31) / 32, d.Nq * d.N3O);
+template <int MODE, int TILE>
+static cudaError_t launch_k3_tile(cudaStream_t s, const K3Args3& a, int nslots, const Dims& d) {
+    const unsigned tiles = (unsigned)((d.N3n + TILE - 1) / TILE);
+    dim3 grid((unsigned)(nslots * d.Nq * d.N3O), tiles, tiles);
+    k_bse_K3_gemm<MODE, TILE><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
+    return cudaGetLastError();
+}
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d) {
+    const int N = d.N3n;
     if (mode == 0) {
-        if (ch == CH_P) k_bse_K3_gemm<0, CH_P><<<grid, 256, 0, s>>>(a, d);
-        else if (ch == CH_T) k_bse_K3_gemm<0, CH_T><<<grid, 256, 0, s>>>(a, d);
-        else k_bse_K3_gemm<0, CH_A><<<grid, 256, 0, s>>>(a, d);
-    } else {
-        if (ch == CH_P) k_bse_K3_gemm<1, CH_P><<<grid, 256, 0, s>>>(a, d);
-        else if (ch == CH_T) k_bse_K3_gemm<1, CH_T><<<grid, 256, 0, s>>>(a, d);
-        else k_bse_K3_gemm<1, CH_A><<<grid, 256, 0, s>>>(a, d);
+        if (N <= 16) return launch_k3_tile<0, 16>(s, a, nslots, d);
+        if (N <= 24) return launch_k3_tile<0, 24>(s, a, nslots, d);
+        return launch_k3_tile<0, 32>(s, a, nslots, d);
     }
-    LAUNCH_CHECK(); return cudaSuccess;
+    if (N <= 16) return launch_k3_tile<1, 16>(s, a, nslots, d);
+    if (N <= 24) return launch_k3_tile<1, 24>(s, a, nslots, d);
+    return launch_k3_tile<1, 32>(s, a, nslots, d);
 }
 cudaError_t launch_expand(cudaStream_t s, cplx* X, const uint32_t* map, size_t n) {
     k_expand<<<blocks_for(n, 256), 256, 0, s>>>(X, map, n);
@@ -680,18 +927,16 @@ cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const
     k_k2_epilogue<<<blocks_for(n, 256), 256, 0, s>>>(out, FLc, FLt, FLa, outA, ch, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_sde_L(cudaStream_t s, int which, int ref, const VertP& F, const cplx* Pi, cplx* out,
-                         const int* items, int nitems, double scale, int accumulate, const Dims& d) {
+cudaError_t launch_sde_L(cudaStream_t s, int which, const VertP& F, const cplx* Pi, const cplx* SPi, cplx* out,
+                         const int* items, int nitems, int use_vertex, double ref_scale, const Dims& d) {
     const unsigned g = blocks_for((size_t)nitems * 32, 128);
-    if (which == 0 && ref == 0) k_sde_L<0, 0><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
-    else if (which == 1 && ref == 0) k_sde_L<1, 0><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
-    else if (which == 0) k_sde_L<0, 1><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
-    else k_sde_L<1, 1><<<g, 128, 0, s>>>(F, Pi, out, items, nitems, scale, accumulate, d);
+    if (which == 0) k_sde_L<0><<<g, 128, 0, s>>>(F, Pi, SPi, out, items, nitems, use_vertex, ref_scale, d);
+    else k_sde_L<1><<<g, 128, 0, s>>>(F, Pi, SPi, out, items, nitems, use_vertex, ref_scale, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, const Dims& d) {
-    const size_t n = (size_t)d.Nk * d.NG;
-    k_sde_sigma<<<blocks_for(n, 64), 64, 0, s>>>(G, Lpp, Lph, S, d);
+    const size_t n = (size_t)d.Nk * d.NG * 32;
+    k_sde_sigma<<<blocks_for(n, 128), 128, 0, s>>>(G, Lpp, Lph, S, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_u2(cudaStream_t s, const cplx* GR, cplx* C, cplx* SR, cplx* out, const cplx* twc, const Dims& d) {

@@ -36,6 +36,15 @@ struct K3Args {
     cplx* out;
 };
 
+struct K3Args3 {  // the three channels of one K3 launch
+    K3Args a[3];
+    int ch[3];
+};
+
+cudaError_t set_fft_twiddles();
+cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, const Dims& d);
+cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
+                      const FLP& FL, cplx* SX, const Dims& d);
 cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n);
 cudaError_t launch_occupation(cudaStream_t s, const cplx* G, size_t n, double T, int Nk, double* out);
 cudaError_t launch_g_realspace(cudaStream_t s, const cplx* G, cplx* GR, const cplx* tw, const Dims& d);
@@ -45,18 +54,18 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
 cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d);
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const Dims& d);
 cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          cplx* out, const int* items, int nitems, const Dims& d);
+                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d);
 cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* Pi0, cplx* out, const int* items,
                             int nitems, const Dims& d);
 cudaError_t launch_bse_K2(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          cplx* out, const int* items, int nitems, const Dims& d);
-cudaError_t launch_bse_K3(cudaStream_t s, int mode, int ch, const K3Args& a, const Dims& d);
+                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d);
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d);
 cudaError_t launch_expand(cudaStream_t s, cplx* X, const uint32_t* map, size_t n);
 cudaError_t launch_half_sum(cudaStream_t s, cplx* out, const cplx* other, size_t n);
 cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa,
                                const cplx* outA, int ch, size_t n);
-cudaError_t launch_sde_L(cudaStream_t s, int which, int ref, const VertP& F, const cplx* Pi, cplx* out,
-                         const int* items, int nitems, double scale, int accumulate, const Dims& d);
+cudaError_t launch_sde_L(cudaStream_t s, int which, const VertP& F, const cplx* Pi, const cplx* SPi, cplx* out,
+                         const int* items, int nitems, int use_vertex, double ref_scale, const Dims& d);
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, const Dims& d);
 cudaError_t launch_u2(cudaStream_t s, const cplx* GR, cplx* C, cplx* SR, cplx* out, const cplx* twc, const Dims& d);
 cudaError_t launch_sigma_assemble(cudaStream_t s, const cplx* Sin, const cplx* SU2, const uint32_t* map,

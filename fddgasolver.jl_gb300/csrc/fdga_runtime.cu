@@ -60,6 +60,7 @@ struct fdga_handle {
     cplx *avg = nullptr, *cache = nullptr, *FLK2 = nullptr, *FLK3 = nullptr;
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
     cplx *GR = nullptr, *u2C = nullptr, *u2R = nullptr, *twm = nullptr, *twp = nullptr;
+    cplx *SPi = nullptr, *SPi0 = nullptr, *SX = nullptr;  // bubble row sums [2][Nq][NΠΩ]; S_X [3][Nq][NΠΩ]
     double* occ = nullptr;
     double n0 = 0.5;
     uint32_t* perm = nullptr;  // reference flatten index -> device index
@@ -358,6 +359,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         LC(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
         LC(launch_g_realspace(s, h->G, h->GR, h->twm, d));
         LC(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
+        LC(launch_rowsum(s, h->Pipp, h->Piph, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
         stage("dyson_bubble");
     }
     Caches C;
@@ -378,23 +380,30 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             if (ch == CH_T) LC(launch_half_sum(s, out, h->FLK2 + (size_t)CH_A * h->n2, h->n2));
         }
         stage("bse_L_K2");
-        for (int ch : order) {
+        K3Args3 a3{};
+        for (int i = 0; i < 3; ++i) {
+            const int ch = order[i];
             const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
-            K3Args a{};
+            K3Args& a = a3.a[i];
             a.A = C.c[cg]; a.B0 = C.c[cf0]; a.Pi0 = Pi0(ch);
             a.out = h->FLK3 + (size_t)ch * h->n3;
-            LC(launch_bse_K3(s, 0, ch, a, d));
-            const Group& g = ch == CH_P ? h->gK3ppL : h->gK3phL;
-            if (!g.trivial) LC(launch_expand(s, a.out, g.d_map, h->n3));
-            if (ch == CH_T) LC(launch_half_sum(s, a.out, h->FLK3 + (size_t)CH_A * h->n3, h->n3));
+            a3.ch[i] = ch;
         }
+        LC(launch_bse_K3(s, 0, a3, 3, d));
+        for (int ch : order) {
+            const Group& g = ch == CH_P ? h->gK3ppL : h->gK3phL;
+            if (!g.trivial) LC(launch_expand(s, h->FLK3 + (size_t)ch * h->n3, g.d_map, h->n3));
+        }
+        LC(launch_half_sum(s, h->FLK3 + (size_t)CH_T * h->n3, h->FLK3 + (size_t)CH_A * h->n3, h->n3));
         stage("bse_L_K3");
     }
+    // ω-sums of the right BSE factor (needs FL.K2 of this iteration)
+    LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FL, h->SX, d));
     // K1
     for (int ch : order) {
         cplx* out = chanK(h, h->yS, ch, 1);
         const Group& g = h->gK1;
-        LC(launch_bse_K1(s, ch, F, FL, Pi(ch), Pi0(ch), out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n1 : g.nitems, d));
+        LC(launch_bse_K1(s, ch, F, FL, Pi(ch), Pi0(ch), h->SX, out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n1 : g.nitems, d));
         if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n1));
         if (ch == CH_T) LC(launch_half_sum(s, out, chanK(h, h->yS, CH_A, 1), h->n1));
     }
@@ -403,24 +412,31 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     for (int ch : order) {
         cplx* out = chanK(h, h->yS, ch, 2);
         const Group& g = k2group(h, ch);
-        LC(launch_bse_K2(s, ch, F, FL, Pi(ch), Pi0(ch), out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n2 : g.nitems, d));
+        LC(launch_bse_K2(s, ch, F, FL, Pi(ch), Pi0(ch), h->SX, out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n2 : g.nitems, d));
         if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n2));
         LC(launch_k2_epilogue(s, out, h->FLK2 + (size_t)ch * h->n2, h->FLK2 + (size_t)CH_T * h->n2,
                               h->FLK2 + (size_t)CH_A * h->n2, chanK(h, h->yS, CH_A, 2), ch, h->n2));
     }
     stage("bse_K2");
     // K3
-    for (int ch : order) {
-        const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
-        const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
-        K3Args a{};
-        a.A = C.c[cf]; a.B0 = C.c[cf0]; a.G = C.c[cg]; a.Pi = Pi(ch); a.Pi0 = Pi0(ch);
-        a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3; a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
-        a.out = chanK(h, h->yS, ch, 3);
-        LC(launch_bse_K3(s, 1, ch, a, d));
-        const Group& g = ch == CH_P ? h->gK3pp : h->gK3ph;
-        if (!g.trivial) LC(launch_expand(s, a.out, g.d_map, h->n3));
-        if (ch == CH_T) LC(launch_half_sum(s, a.out, chanK(h, h->yS, CH_A, 3), h->n3));
+    {
+        K3Args3 a3{};
+        for (int i = 0; i < 3; ++i) {
+            const int ch = order[i];
+            const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
+            const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+            K3Args& a = a3.a[i];
+            a.A = C.c[cf]; a.B0 = C.c[cf0]; a.G = C.c[cg]; a.Pi = Pi(ch); a.Pi0 = Pi0(ch);
+            a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3; a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
+            a.out = chanK(h, h->yS, ch, 3);
+            a3.ch[i] = ch;
+        }
+        LC(launch_bse_K3(s, 1, a3, 3, d));
+        for (int ch : order) {
+            const Group& g = ch == CH_P ? h->gK3pp : h->gK3ph;
+            if (!g.trivial) LC(launch_expand(s, chanK(h, h->yS, ch, 3), g.d_map, h->n3));
+        }
+        LC(launch_half_sum(s, chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3), h->n3));
     }
     stage("bse_K3");
     // SDE (src/SDE.jl:3-33) with the new F
@@ -431,12 +447,10 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         const int* ip = gp.trivial ? nullptr : gp.d_items;
         const int* ih = gh.trivial ? nullptr : gh.d_items;
         const int np_ = gp.trivial ? (int)h->n2 : gp.nitems, nh_ = gh.trivial ? (int)h->n2 : gh.nitems;
-        LC(launch_sde_L(s, 0, 0, Fn, h->Pipp, h->Lpp, ip, np_, 1.0, 0, d));
-        LC(launch_sde_L(s, 1, 0, Fn, h->Piph, h->Lph, ih, nh_, 1.0, 0, d));
-        if (h->ref_nonzero) {
-            LC(launch_sde_L(s, 0, 1, Fn, h->Pipp, h->Lpp, ip, np_, 1.0 / 3.0, 1, d));
-            LC(launch_sde_L(s, 1, 1, Fn, h->Piph, h->Lph, ih, nh_, 1.0 / 3.0, 1, d));
-        }
+        const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
+        const size_t nS = (size_t)d.Nq * d.NPO;
+        LC(launch_sde_L(s, 0, Fn, h->Pipp, h->SPi, h->Lpp, ip, np_, 1, rs, d));
+        LC(launch_sde_L(s, 1, Fn, h->Piph, h->SPi + nS, h->Lph, ih, nh_, 1, rs, d));
         if (!gp.trivial) LC(launch_expand(s, h->Lpp, gp.d_map, h->n2));
         if (!gh.trivial) LC(launch_expand(s, h->Lph, gh.d_map, h->n2));
         LC(launch_sde_sigma(s, h->G, h->Lpp, h->Lph, h->SigIn, d));
@@ -460,8 +474,9 @@ int compute_C0(fdga_handle* h) {
     VertP F0 = vertex_view(h, h->yS);  // only the RefVertex fields are read by the REF kernels
     const Group& gp = h->gK2pp;
     const Group& gh = h->gK2ph;
-    LC(launch_sde_L(s, 0, 1, F0, h->Pi0pp, h->Lpp, gp.trivial ? nullptr : gp.d_items, gp.trivial ? (int)h->n2 : gp.nitems, 1.0 / 3.0, 0, d));
-    LC(launch_sde_L(s, 1, 1, F0, h->Pi0ph, h->Lph, gh.trivial ? nullptr : gh.d_items, gh.trivial ? (int)h->n2 : gh.nitems, 1.0 / 3.0, 0, d));
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    LC(launch_sde_L(s, 0, F0, h->Pi0pp, h->SPi0, h->Lpp, gp.trivial ? nullptr : gp.d_items, gp.trivial ? (int)h->n2 : gp.nitems, 0, 1.0 / 3.0, d));
+    LC(launch_sde_L(s, 1, F0, h->Pi0ph, h->SPi0 + nS, h->Lph, gh.trivial ? nullptr : gh.d_items, gh.trivial ? (int)h->n2 : gh.nitems, 0, 1.0 / 3.0, d));
     if (!gp.trivial) LC(launch_expand(s, h->Lpp, gp.d_map, h->n2));
     if (!gh.trivial) LC(launch_expand(s, h->Lph, gh.d_map, h->n2));
     LC(launch_sde_sigma(s, h->G0, h->Lpp, h->Lph, h->SigIn, d));
@@ -623,7 +638,7 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     }
     int r = FDGA_OK;
     auto fin_err = [&](int code) { g_create_error = h->err; fdga_destroy(h); return code; };
-    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess || set_fft_twiddles() != cudaSuccess) {
         g_create_error = "cudaStreamCreate failed (no CUDA device?)";
         delete h;
         return FDGA_ERR_CUDA;
@@ -640,6 +655,7 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     ALC(h->Lpp, h->n2); ALC(h->Lph, h->n2); ALC(h->SigIn, h->nGk); ALC(h->SigU2, h->nGk); ALC(h->C0, h->nGk);
     ALC(h->GR, h->nGk); ALC(h->u2C, (size_t)d.Nq * (2 * d.NG - 1)); ALC(h->u2R, h->nGk);
     ALC(h->twm, d.L); ALC(h->twp, d.L);
+    ALC(h->SPi, 2 * (size_t)d.Nq * d.NPO); ALC(h->SPi0, 2 * (size_t)d.Nq * d.NPO); ALC(h->SX, 3 * (size_t)d.Nq * d.NPO);
     ALC(h->occ, 1);
     ALC(h->perm, h->nstate);
     ALC(h->d_part, NBLK_RED); ALC(h->d_cpart, NBLK_RED);
@@ -713,6 +729,8 @@ int fdga_finalize(fdga_handle* h) {
     cudaStream_t s = h->st;
     CK(launch_g_realspace(s, h->G0, h->GR, h->twm, d));
     CK(launch_bubble(s, h->G0, h->GR, h->Pi0pp, h->Pi0ph, h->twp, d));
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    CK(launch_rowsum(s, h->Pi0pp, h->Pi0ph, h->SPi0, h->SPi0 + nS, d));
     CK(cudaMemsetAsync(h->xS, 0, h->nstate * sizeof(cplx), s));
     CK(cudaMemsetAsync(h->yS, 0, h->nstate * sizeof(cplx), s));
     CK(cudaMemsetAsync(h->FLK2, 0, 3 * h->n2 * sizeof(cplx), s));
@@ -721,6 +739,7 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
     CK(launch_g_realspace(s, h->G, h->GR, h->twm, d));
     CK(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
+    CK(launch_rowsum(s, h->Pipp, h->Piph, h->SPi, h->SPi + nS, d));
     CK(cudaStreamSynchronize(s));
     h->finalized = true;
     h->c0_dirty = true;
