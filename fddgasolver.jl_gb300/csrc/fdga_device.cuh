@@ -3,7 +3,8 @@
 // Device layout (row-major, last index fastest; chosen so that each (P, Ω) block of a K3-shaped
 // array is one contiguous Nν x Nν matrix and every ω-sum streams contiguous memory):
 //   G-like  [k][ν]          (identical to the reference's column-major [ν, k])
-//   Π       [P][Ω][ν]
+//   Π       [P][Ω][ν]       ν over the stored window [-nPw, nPw) of the bubble mesh (every ω at
+//                           which a BSE/SDE sum reads Π lies in it; full-mesh sums use row sums)
 //   K1      [P][Ω]          K2 [P][Ω][ν]          K3 [P][Ω][ν][ν']
 // The reference stores the same data column-major with Ω fastest; flatten/unflatten permute.
 //
@@ -64,6 +65,7 @@ struct Dims {
     int nG, NG, Nk, L, Nq;
     int n1, N1, n2O, N2O, n2n, N2n, n3O, N3O, n3n, N3n;
     int nPO, NPO, nPn, NPn;
+    int nPw, NPw;  // stored bubble window: fermion indices [-nPw, nPw) of the mesh [-nPn, nPn)
     int nRO, NRO, nRn, NRn;
     int local;
     double T, U;
@@ -95,7 +97,7 @@ __device__ __forceinline__ size_t ix3(const Dims& d, int P, int m, int n, int np
     return (((size_t)P * d.N3O + (m + d.n3O - 1)) * d.N3n + (n + d.n3n)) * d.N3n + (np + d.n3n);
 }
 __device__ __forceinline__ size_t ixPi(const Dims& d, int P, int m, int n) {
-    return ((size_t)P * d.NPO + (m + d.nPO - 1)) * d.NPn + (n + d.nPn);
+    return ((size_t)P * d.NPO + (m + d.nPO - 1)) * d.NPw + (n + d.nPw);
 }
 __device__ __forceinline__ size_t ixG(const Dims& d, int k, int n) { return (size_t)k * d.NG + (n + d.nG); }
 

@@ -65,8 +65,8 @@ __device__ __forceinline__ cplx g_tail(const cplx* G, const Dims& d, int k, int 
 
 __global__ void k_bubble_local(const cplx* G, cplx* pp, cplx* ph, Dims d) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= (size_t)d.NPO * d.NPn) return;
-    const int n = (int)(i % d.NPn) - d.nPn, m = (int)(i / d.NPn) - (d.nPO - 1);
+    if (i >= (size_t)d.NPO * d.NPw) return;
+    const int n = (int)(i % d.NPw) - d.nPw, m = (int)(i / d.NPw) - (d.nPO - 1);
     const cplx Gn = g_tail(G, d, 0, n);
     pp[i] = Gn * g_tail(G, d, 0, m - n - 1);
     ph[i] = Gn * g_tail(G, d, 0, m + n);
@@ -83,12 +83,12 @@ __global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
     cplx* A = sh;                     // [2][TV][NR]   (pp, ph) in R
     cplx* B = sh + 2 * (size_t)TV * NR;  // [2][TV][NR]  after the x transform
     const int m = blockIdx.y - (d.nPO - 1);
-    const int n0 = blockIdx.x * TV - d.nPn;
+    const int n0 = blockIdx.x * TV - d.nPw;
     for (int e = threadIdx.x; e < TV * NR; e += blockDim.x) {
         const int v = e / NR, R = e % NR;
         const int n = n0 + v;
         cplx vpp = mk(0, 0), vph = mk(0, 0);
-        if (n < d.nPn) {
+        if (n < d.nPw) {
             const int Rx = R % L, Ry = R / L;
             const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
             if (R == 0) {
@@ -121,7 +121,7 @@ __global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
         const int P = rest % NR, which = rest / NR;
         const int Px = P % L, Py = P / L;
         const int n = n0 + v;
-        if (n >= d.nPn) continue;
+        if (n >= d.nPw) continue;
         const cplx* b = B + (size_t)(which * TV + v) * NR;
         cplx s = mk(0, 0);
         for (int y = 0; y < L; ++y) s += b[(size_t)y * L + Px] * twp[(Py * y) % L];
@@ -173,13 +173,13 @@ __global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV)
     extern __shared__ cplx sh[];
     constexpr int NR = L * L, RS = L + 1, BS = L * (L + 1) + 1;
     const int m = blockIdx.y - (d.nPO - 1);
-    const int n0 = blockIdx.x * TV - d.nPn;
+    const int n0 = blockIdx.x * TV - d.nPw;
     for (int e = threadIdx.x; e < TV * NR; e += blockDim.x) {
         const int v = e / NR, R = e % NR;
         const int n = n0 + v;
         const int Rx = R % L, Ry = R / L;
         cplx vpp = mk(0, 0), vph = mk(0, 0);
-        if (n < d.nPn) {
+        if (n < d.nPw) {
             const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
             if (R == 0) {
                 vpp = g_tail(GR, d, 0, m - n - 1) * g_tail(GR, d, 0, n);
@@ -219,7 +219,7 @@ __global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV)
         const int rest = e / TV;
         const int P = rest % NR, which = rest / NR;
         const int n = n0 + v;
-        if (n >= d.nPn) continue;
+        if (n >= d.nPw) continue;
         const cplx val = sh[(size_t)(which * TV + v) * BS + (P / L) * RS + (P % L)];
         (which ? ph : pp)[ixPi(d, P, m, n)] = val;
     }
@@ -243,17 +243,21 @@ __global__ void k_qavg(const ChanArrays in, ChanArraysW out, Dims d) {
 
 // ---------------------------------------------------------------------------------------------
 // K3 caches (src/build_K3_cache.jl:20-95, src/nonlocal/build_K3_cache.jl:18-94).
-// One thread per K3 mesh point (P, Ω, a, b); "left" caches use (Ω, ω=a, ν'=b),
+// One thread per K3 mesh point (P, Ω, a, b) of the listed (P, Ω) blocks (the blocks holding
+// symmetry-class representatives; all blocks without groups); "left" caches use (Ω, ω=a, ν'=b),
 // "right" caches (Ω, ν=a, ω=b).  Output order: Γpx F0p F0a F0t Γpp Γa Γt Fp Fa Ft.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_build_cache(VertP F, Caches C, Dims d) {
-    const size_t n3 = (size_t)d.Nq * d.N3O * d.N3n * d.N3n;
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= n3) return;
-    const int b = (int)(i % d.N3n) - d.n3n;
-    const int a = (int)((i / d.N3n) % d.N3n) - d.n3n;
-    const int m = (int)((i / ((size_t)d.N3n * d.N3n)) % d.N3O) - (d.n3O - 1);
-    const int P = (int)(i / ((size_t)d.N3n * d.N3n * d.N3O));
+__global__ void k_build_cache(VertP F, Caches C, const int* blocks, int nblocks, Dims d) {
+    const size_t bs = (size_t)d.N3n * d.N3n;
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)nblocks * bs) return;
+    const int bl = blocks ? blocks[t / bs] : (int)(t / bs);  // block = P * NΩ3 + iΩ
+    const size_t e = t % bs;
+    const size_t i = (size_t)bl * bs + e;
+    const int b = (int)(e % d.N3n) - d.n3n;
+    const int a = (int)(e / d.N3n) - d.n3n;
+    const int m = bl % d.N3O - (d.n3O - 1);
+    const int P = bl / d.N3O;
     // left
     C.c[0][i] = vert_eval(F, d, CH_P, SP_X, m, a, b, P, FL_GT | FL_GA);
     C.c[1][i] = ref_xSp(F, d, CH_P, m, a, b) - ref_xSp(F, d, CH_P, m, a, FINF);
@@ -300,6 +304,55 @@ __global__ void k_rowsum(const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, int
     if (threadIdx.x == 0) S[row] = mk(rx[0], ry[0]);
 }
 
+// Full-mesh bubble row sums in real space, for a stored window narrower than the mesh:
+//   SR[w][Ω][R] = Σ_{ν ∈ bubble mesh} Π_R^w(Ω, ν, R),   S^w(P, Ω) = Σ_R e^{+2πi P·R/L} SR[w][Ω][R],
+// with Π_R as in k_bubble_nl (R = 0 carries the 1/ν tail; R ≠ 0 needs both G in their box).
+__global__ void k_pisum_R(const cplx* GR, cplx* SR, Dims d) {
+    const int NR = d.L * d.L;
+    const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (size_t)2 * d.NPO * NR) return;
+    const int which = (int)(w / ((size_t)d.NPO * NR));
+    const int rest = (int)(w % ((size_t)d.NPO * NR));
+    const int m = rest / NR - (d.nPO - 1), R = rest % NR;
+    const int L = d.L, Rx = R % L, Ry = R / L;
+    const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
+    cplx acc = mk(0, 0);
+    if (R == 0) {
+        for (int n = -d.nPn + lane; n < d.nPn; n += 32)
+            acc += which ? g_tail(GR, d, 0, m + n) * g_tail(GR, d, 0, n) : g_tail(GR, d, 0, m - n - 1) * g_tail(GR, d, 0, n);
+    } else {
+        for (int n = -d.nG + lane; n < d.nG; n += 32) {
+            if (!fin(n, d.nPn)) continue;
+            if (which) {
+                const int b = m + n;
+                if (fin(b, d.nG)) acc += GR[ixG(d, R, b)] * GR[ixG(d, mR, n)];
+            } else {
+                const int a = m - n - 1;
+                if (fin(a, d.nG)) acc += GR[ixG(d, R, a)] * GR[ixG(d, R, n)];
+            }
+        }
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) SR[w] = acc;
+}
+__global__ void k_pisum_P(const cplx* SR, cplx* S0, cplx* S1, const cplx* twp, Dims d) {
+    const int NR = d.L * d.L;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= (size_t)2 * d.NPO * NR) return;
+    const int which = (int)(i / ((size_t)d.NPO * NR));
+    const int rest = (int)(i % ((size_t)d.NPO * NR));
+    const int P = rest / d.NPO, iO = rest % d.NPO;
+    const int Px = P % d.L, Py = P / d.L;
+    const cplx* sr = SR + ((size_t)which * d.NPO + iO) * NR;
+    cplx acc = mk(0, 0);
+    for (int R = 0; R < NR; ++R) {
+        const int Rx = R % d.L, Ry = R / d.L;
+        acc += sr[R] * twp[(Px * Rx + Py * Ry) % d.L];
+    }
+    (which ? S1 : S0)[(size_t)P * d.NPO + iO] = acc;
+}
+
 // S_X(ch, P, Ω) = Σ_ω [(Π-Π0)(Ω,ω,P) U + Π(Ω,ω,P) FL(Ω,ω̃,∞)]: the ω-sum of the BSE's right factor
 // (src/BSEa/BSEa_K1.jl:43, BSEa_K2.jl:185), from the row sums and the K2 window of FL.
 // Layout SX[ch][P][Ω] with Ω over the K1 box; SPi/SPi0 [w][P][Ω] with w = 0 pp, 1 ph.
@@ -316,7 +369,7 @@ __global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const 
     if (bin(m, d.n2O)) {
         for (int nt = -d.n2n; nt < d.n2n; ++nt) {
             const int n = (ch == CH_P) ? m - nt - 1 : nt;
-            if (!fin(n, d.nPn)) continue;
+            if (!fin(n, d.nPw)) continue;
             v += Pi[ixPi(d, P, m, n)] * fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, ch, m, nt, P);
         }
     }
@@ -341,7 +394,7 @@ __global__ void k_bse_K1(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const
     cplx acc = mk(0, 0);
     if (bin(m, d.n2O)) {
         for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
-            if (!fin(n, d.nPn)) continue;
+            if (!fin(n, d.nPw)) continue;
             const int wt = cross(CH, m, n);
             const cplx Fl = vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
             const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
@@ -374,7 +427,7 @@ __global__ void k_bse_L_K2(VertP F, const cplx* Pi0, cplx* out, const int* items
     constexpr int IRR = (CH == CH_P) ? (FL_GT | FL_GA) : (CH == CH_T ? (FL_GP | FL_GA) : (FL_GP | FL_GT));
     cplx acc = mk(0, 0);
     if (d.local) {
-        for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
+        for (int n = -d.nPw + lane; n < d.nPw; n += 32) {  // local solver: nPw = nPn
             const cplx Gp = vert_eval(F, d, CH, SP, m, nu, n, P, IRR);
             acc += Gp * ldg(Pi0 + ixPi(d, P, m, n)) * d.U;
         }
@@ -409,7 +462,7 @@ __global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     const cplx c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - vert_eval(F, d, CH, SP, m, FINF, FINF, P);
     Windows win;
-    const int lo = -d.nPn, hi = d.nPn - 1, h1 = d.n1 - 1;
+    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
     win.add(-d.n2n, d.n2n - 1, lo, hi);
     win.add(-d.nRn, d.nRn - 1, lo, hi);
     win.add(nu - h1, nu + h1, lo, hi);
@@ -451,8 +504,9 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
     const int tid = threadIdx.x;
     const int tx = tid % H, ty = tid / H;
     const int col0 = blockIdx.z * TILE, row0 = blockIdx.y * TILE;
-    const int nblk = d.Nq * d.N3O;
-    const int slot = blockIdx.x / nblk, blk = blockIdx.x % nblk;
+    const int nb = args.nblocks;
+    const int slot = blockIdx.x / nb;
+    const int blk = args.blocks ? args.blocks[blockIdx.x % nb] : (int)(blockIdx.x % nb);
     const K3Args& a = args.a[slot];
     const int CH = args.ch[slot];
     const int m = blk % d.N3O - (d.n3O - 1), P = blk / d.N3O;
@@ -576,14 +630,14 @@ __global__ void k_sde_L(VertP F, const cplx* Pi, const cplx* SPi, cplx* out, con
             c = chan_eval(F.g[CH_P], d, m, FINF, nu, P);
             for (int t = lane; t < d.N2n; t += 32) {
                 const int n = m - (t - d.n2n) - 1;  // Ω-ω runs over the K2 box
-                if (!fin(n, d.nPn)) continue;
+                if (!fin(n, d.nPw)) continue;
                 const cplx g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P) - c;
                 acc += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
             }
         } else {
             c = chan_eval(F.g[CH_T], d, m, nu, FINF, P) + chan_eval(F.g[CH_A], d, m, nu, FINF, P);
             for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
-                if (!fin(n, d.nPn)) continue;
+                if (!fin(n, d.nPw)) continue;
                 const cplx g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P) - c;
                 acc += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
             }
@@ -593,7 +647,7 @@ __global__ void k_sde_L(VertP F, const cplx* Pi, const cplx* SPi, cplx* out, con
         for (int t = lane; t < d.NRn; t += 32) {
             const int r = t - d.nRn;
             const int n = (WHICH == 0) ? m - r - 1 : r;
-            if (!fin(n, d.nPn)) continue;
+            if (!fin(n, d.nPw)) continue;
             cplx g;
             if (WHICH == 0) g = ref_pSp(F, d, CH_P, m, m - n - 1, nu) - mk(d.U, 0);
             else g = ref_pSp(F, d, CH_A, m, nu, n) + ref_pSp(F, d, CH_T, m, nu, n) - mk(d.U, 0) - mk(d.U, 0);
@@ -811,7 +865,7 @@ static cudaError_t launch_bubble_fft(cudaStream_t s, const cplx* GR, cplx* pp, c
         cudaFuncSetAttribute(k_bubble_fft<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         shm_set = shm;
     }
-    dim3 grid((d.NPn + tv - 1) / tv, d.NPO);
+    dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
     k_bubble_fft<L><<<grid, 256, shm, s>>>(GR, pp, ph, d, tv);
     return cudaGetLastError();
 }
@@ -825,7 +879,7 @@ cudaError_t set_fft_twiddles() {
 cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
                           const Dims& d) {
     if (d.local) {
-        const size_t n = (size_t)d.NPO * d.NPn;
+        const size_t n = (size_t)d.NPO * d.NPw;
         k_bubble_local<<<blocks_for(n, 256), 256, 0, s>>>(G, pp, ph, d);
         LAUNCH_CHECK(); return cudaSuccess;
     }
@@ -844,14 +898,22 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
         cudaFuncSetAttribute(k_bubble_nl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         shm_set = shm;
     }
-    dim3 grid((d.NPn + tv - 1) / tv, d.NPO);
+    dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
     k_bubble_nl<<<grid, 256, shm, s>>>(GR, pp, ph, twp, d, tv);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 
-cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, const Dims& d) {
-    dim3 grid((unsigned)(d.Nq * d.NPO), 2);
-    k_rowsum<<<grid, 256, 0, s>>>(A0, A1, S0, S1, d.NPn);
+cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
+                          cplx* S0, cplx* S1, const Dims& d) {
+    if (d.nPw == d.nPn) {  // the full mesh is stored: sum the rows
+        dim3 grid((unsigned)(d.Nq * d.NPO), 2);
+        k_rowsum<<<grid, 256, 0, s>>>(A0, A1, S0, S1, d.NPw);
+        LAUNCH_CHECK(); return cudaSuccess;
+    }
+    const int NR = d.L * d.L;
+    k_pisum_R<<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GR, SRtmp, d);
+    LAUNCH_CHECK();
+    k_pisum_P<<<blocks_for((size_t)2 * d.NPO * NR, 128), 128, 0, s>>>(SRtmp, S0, S1, twp, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
@@ -867,9 +929,10 @@ cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW&
     k_qavg<<<grid, 256, 0, s>>>(in, out, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const Dims& d) {
-    const size_t n = (size_t)d.Nq * d.N3O * d.N3n * d.N3n;
-    k_build_cache<<<blocks_for(n, 128), 128, 0, s>>>(F, C, d);
+cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
+                               const Dims& d) {
+    const size_t n = (size_t)nblocks * d.N3n * d.N3n;
+    k_build_cache<<<blocks_for(n, 128), 128, 0, s>>>(F, C, blocks, nblocks, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
@@ -899,7 +962,7 @@ cudaError_t launch_bse_K2(cudaStream_t s, int ch, const VertP& F, const FLP& FL,
 template <int MODE, int TILE>
 static cudaError_t launch_k3_tile(cudaStream_t s, const K3Args3& a, int nslots, const Dims& d) {
     const unsigned tiles = (unsigned)((d.N3n + TILE - 1) / TILE);
-    dim3 grid((unsigned)(nslots * d.Nq * d.N3O), tiles, tiles);
+    dim3 grid((unsigned)(nslots * a.nblocks), tiles, tiles);
     k_bse_K3_gemm<MODE, TILE><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
     return cudaGetLastError();
 }

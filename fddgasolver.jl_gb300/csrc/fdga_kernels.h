@@ -36,13 +36,16 @@ struct K3Args {
     cplx* out;
 };
 
-struct K3Args3 {  // the three channels of one K3 launch
+struct K3Args3 {  // the three channels of one K3 launch over a list of (P, Ω) blocks
     K3Args a[3];
     int ch[3];
+    const int* blocks;  // block = P * NΩ3 + iΩ; nullptr = all blocks
+    int nblocks;
 };
 
 cudaError_t set_fft_twiddles();
-cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, const Dims& d);
+cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
+                          cplx* S0, cplx* S1, const Dims& d);
 cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
                       const FLP& FL, cplx* SX, const Dims& d);
 cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n);
@@ -52,7 +55,8 @@ int bubble_tile(const Dims& d);
 cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
                           const Dims& d);
 cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d);
-cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const Dims& d);
+cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
+                               const Dims& d);
 cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
                           const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d);
 cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* Pi0, cplx* out, const int* items,

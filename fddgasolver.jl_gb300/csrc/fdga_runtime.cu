@@ -61,6 +61,11 @@ struct fdga_handle {
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
     cplx *GR = nullptr, *u2C = nullptr, *u2R = nullptr, *twm = nullptr, *twp = nullptr;
     cplx *SPi = nullptr, *SPi0 = nullptr, *SX = nullptr;  // bubble row sums [2][Nq][NΠΩ]; S_X [3][Nq][NΠΩ]
+    cplx* SRtmp = nullptr;                                 // real-space row sums [2][NΠΩ][L*L]
+    int* d_k3blocks = nullptr;                             // (P, Ω) blocks holding K3 class representatives
+    void* flush_buf = nullptr;                             // L2 flush buffer (benchmarks)
+    size_t flush_bytes = 0;
+    int nk3blocks = 0;
     double* occ = nullptr;
     double n0 = 0.5;
     uint32_t* perm = nullptr;  // reference flatten index -> device index
@@ -145,6 +150,11 @@ int make_dims(const fdga_config* c, Dims& d) {
     d.n3O = c->nK3[0]; d.N3O = 2 * c->nK3[0] - 1; d.n3n = c->nK3[1]; d.N3n = 2 * c->nK3[1];
     d.nPO = c->nK1; d.NPO = 2 * c->nK1 - 1; d.nPn = c->nK1 * c->mPi_factor; d.NPn = 2 * d.nPn;
     d.nRO = c->nR[0]; d.NRO = 2 * c->nR[0] - 1; d.nRn = c->nR[1]; d.NRn = 2 * c->nR[1];
+    // Stored bubble window.  Every bubble frequency read by the nonlocal iteration satisfies
+    // |ω| <= nK2Ω + nK2ν + nK1 (K2 windows around -(Ω+ν+1) and Ω-ν-1), <= nK2Ω + nRν (SDE RefVertex
+    // window) or <= nK1 + nK2ν (S_X); the local solver's left K2 BSE sums the whole mesh.
+    d.nPw = c->local ? d.nPn : std::min(d.nPn, c->nK2[0] + c->nK2[1] + c->nK1 + c->nR[1] + 2);
+    d.NPw = 2 * d.nPw;
     d.local = c->local ? 1 : 0;
     d.T = c->T; d.U = c->U;
     return FDGA_OK;
@@ -359,12 +369,12 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         LC(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
         LC(launch_g_realspace(s, h->G, h->GR, h->twm, d));
         LC(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
-        LC(launch_rowsum(s, h->Pipp, h->Piph, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
+        LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
         stage("dyson_bubble");
     }
     Caches C;
     for (int i = 0; i < 10; ++i) C.c[i] = h->cache + (size_t)i * h->n3;
-    LC(launch_build_cache(s, F, C, d));
+    LC(launch_build_cache(s, F, C, h->d_k3blocks, h->nk3blocks, d));
     stage("k3_cache");
     FLP FL;
     for (int c = 0; c < 3; ++c) FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
@@ -389,6 +399,8 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             a.out = h->FLK3 + (size_t)ch * h->n3;
             a3.ch[i] = ch;
         }
+        a3.blocks = h->d_k3blocks;
+        a3.nblocks = h->nk3blocks;
         LC(launch_bse_K3(s, 0, a3, 3, d));
         for (int ch : order) {
             const Group& g = ch == CH_P ? h->gK3ppL : h->gK3phL;
@@ -431,6 +443,8 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             a.out = chanK(h, h->yS, ch, 3);
             a3.ch[i] = ch;
         }
+        a3.blocks = h->d_k3blocks;
+        a3.nblocks = h->nk3blocks;
         LC(launch_bse_K3(s, 1, a3, 3, d));
         for (int ch : order) {
             const Group& g = ch == CH_P ? h->gK3pp : h->gK3ph;
@@ -568,10 +582,11 @@ bool lookup(fdga_handle* h, const std::string& n, cplx*& p, int& kind, size_t& l
     if (n == "Gbare") { p = h->Gbare; kind = AK_G; len = h->nGk; return true; }
     if (n == "G0") { p = h->G0; kind = AK_G; len = h->nGk; return true; }
     if (n == "Sigma0") { p = h->Sig0; kind = AK_G; len = h->nGk; return true; }
-    if (n == "Pipp") { p = h->Pipp; kind = AK_PI; len = h->nPi; return true; }
-    if (n == "Piph") { p = h->Piph; kind = AK_PI; len = h->nPi; return true; }
-    if (n == "Pi0pp") { p = h->Pi0pp; kind = AK_PI; len = h->nPi; return true; }
-    if (n == "Pi0ph") { p = h->Pi0ph; kind = AK_PI; len = h->nPi; return true; }
+    const size_t nPiFull = (size_t)h->d.NPO * h->d.NPn * h->d.Nq;
+    if (n == "Pipp") { p = h->Pipp; kind = AK_PI; len = nPiFull; return true; }
+    if (n == "Piph") { p = h->Piph; kind = AK_PI; len = nPiFull; return true; }
+    if (n == "Pi0pp") { p = h->Pi0pp; kind = AK_PI; len = nPiFull; return true; }
+    if (n == "Pi0ph") { p = h->Pi0ph; kind = AK_PI; len = nPiFull; return true; }
     if (n == "Lpp") { p = h->Lpp; kind = AK_K2; len = h->n2; return true; }
     if (n == "Lph") { p = h->Lph; kind = AK_K2; len = h->n2; return true; }
     static const char* cn[10] = {"cache_Gpx", "cache_F0p", "cache_F0a", "cache_F0t", "cache_Gpp",
@@ -627,7 +642,7 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     h->n1 = (size_t)d.N1 * d.Nq;
     h->n2 = (size_t)d.N2O * d.N2n * d.Nq;
     h->n3 = (size_t)d.N3O * d.N3n * d.N3n * d.Nq;
-    h->nPi = (size_t)d.NPO * d.NPn * d.Nq;
+    h->nPi = (size_t)d.NPO * d.NPw * d.Nq;
     h->nRef = (size_t)d.NRO * d.NRn * d.NRn;
     h->nchan = h->n1 + h->n2 + h->n3;
     h->nstate = 3 * h->nchan + h->nGk;
@@ -656,6 +671,8 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     ALC(h->GR, h->nGk); ALC(h->u2C, (size_t)d.Nq * (2 * d.NG - 1)); ALC(h->u2R, h->nGk);
     ALC(h->twm, d.L); ALC(h->twp, d.L);
     ALC(h->SPi, 2 * (size_t)d.Nq * d.NPO); ALC(h->SPi0, 2 * (size_t)d.Nq * d.NPO); ALC(h->SX, 3 * (size_t)d.Nq * d.NPO);
+    ALC(h->SRtmp, 2 * (size_t)d.NPO * d.Nq);
+    h->nk3blocks = d.Nq * d.N3O;
     ALC(h->occ, 1);
     ALC(h->perm, h->nstate);
     ALC(h->d_part, NBLK_RED); ALC(h->d_cpart, NBLK_RED);
@@ -692,6 +709,7 @@ void fdga_destroy(fdga_handle* h) {
     if (!h) return;
     if (h->st) cudaStreamSynchronize(h->st);
     drop_graphs(h);
+    if (h->flush_buf) cudaFree(h->flush_buf);
     for (void* p : h->allocs) cudaFree(p);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     if (h->st) cudaStreamDestroy(h->st);
@@ -730,7 +748,7 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_g_realspace(s, h->G0, h->GR, h->twm, d));
     CK(launch_bubble(s, h->G0, h->GR, h->Pi0pp, h->Pi0ph, h->twp, d));
     const size_t nS = (size_t)d.Nq * d.NPO;
-    CK(launch_rowsum(s, h->Pi0pp, h->Pi0ph, h->SPi0, h->SPi0 + nS, d));
+    CK(launch_rowsum(s, h->Pi0pp, h->Pi0ph, h->GR, h->SRtmp, h->twp, h->SPi0, h->SPi0 + nS, d));
     CK(cudaMemsetAsync(h->xS, 0, h->nstate * sizeof(cplx), s));
     CK(cudaMemsetAsync(h->yS, 0, h->nstate * sizeof(cplx), s));
     CK(cudaMemsetAsync(h->FLK2, 0, 3 * h->n2 * sizeof(cplx), s));
@@ -739,7 +757,7 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
     CK(launch_g_realspace(s, h->G, h->GR, h->twm, d));
     CK(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
-    CK(launch_rowsum(s, h->Pipp, h->Piph, h->SPi, h->SPi + nS, d));
+    CK(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + nS, d));
     CK(cudaStreamSynchronize(s));
     h->finalized = true;
     h->c0_dirty = true;
@@ -754,6 +772,21 @@ int fdga_init_sym_grp(fdga_handle* h) {
     for (int i = 0; i < 8; ++i) {
         int r = upload_group(h, *dst[i], hg[i]);
         if (r) return r;
+    }
+    // (P, Ω) blocks of the K3 mesh that hold a representative of any K3 group: only these blocks
+    // of the caches and of the K3 GEMMs are computed; k_expand fills the rest.
+    {
+        const size_t bs = (size_t)h->d.N3n * h->d.N3n;
+        std::vector<char> used((size_t)h->d.Nq * h->d.N3O, 0);
+        for (int i = 4; i < 8; ++i)
+            for (int r : hg[i].items) used[(size_t)r / bs] = 1;
+        std::vector<int> blocks;
+        for (size_t b = 0; b < used.size(); ++b)
+            if (used[b]) blocks.push_back((int)b);
+        if (!h->d_k3blocks) AL(h->d_k3blocks, used.size());
+        CK(cudaMemcpyAsync(h->d_k3blocks, blocks.data(), blocks.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        h->nk3blocks = (int)blocks.size();
     }
     drop_graphs(h);
     h->c0_dirty = true;
@@ -936,6 +969,28 @@ int fdga_get_named(fdga_handle* h, const char* name, double* out, size_t n) {
     if (n != len) return fail(h, FDGA_ERR_ARG, "size mismatch for " + std::string(name));
     std::vector<cplx> dev(len);
     CK(cudaStreamSynchronize(h->st));
+    if (kind == AK_PI) {
+        // the iteration stores a window of the bubble mesh; inspection recomputes the whole mesh
+        const std::string nm(name);
+        const bool ref = nm == "Pi0pp" || nm == "Pi0ph";
+        const bool pp = nm == "Pipp" || nm == "Pi0pp";
+        Dims df = h->d;
+        df.nPw = df.nPn;
+        df.NPw = df.NPn;
+        cplx *tpp = nullptr, *tph = nullptr;
+        CK(cudaMalloc(&tpp, len * sizeof(cplx)));
+        cudaError_t e = cudaMalloc(&tph, len * sizeof(cplx));
+        if (e == cudaSuccess) e = launch_g_realspace(h->st, ref ? h->G0 : h->G, h->GR, h->twm, df);
+        if (e == cudaSuccess) e = launch_bubble(h->st, ref ? h->G0 : h->G, h->GR, tpp, tph, h->twp, df);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        if (e == cudaSuccess) e = cudaMemcpy(dev.data(), pp ? tpp : tph, len * sizeof(cplx), cudaMemcpyDeviceToHost);
+        cudaFree(tpp);
+        if (tph) cudaFree(tph);
+        if (e != cudaSuccess) return cuda_fail(h, e, "full bubble for inspection");
+        cplx* o = reinterpret_cast<cplx*>(out);
+        for (size_t j = 0; j < len; ++j) o[j] = dev[dev_index(h->d, kind, j)];
+        return FDGA_OK;
+    }
     CK(cudaMemcpy(dev.data(), p, len * sizeof(cplx), cudaMemcpyDeviceToHost));
     cplx* o = reinterpret_cast<cplx*>(out);
     for (size_t j = 0; j < len; ++j) o[j] = dev[dev_index(h->d, kind, j)];
@@ -1033,6 +1088,21 @@ int fdga_host_alloc(size_t bytes, void** p) {
 }
 int fdga_host_free(void* p) {
     return cudaFreeHost(p) == cudaSuccess ? FDGA_OK : FDGA_ERR_CUDA;
+}
+
+int fdga_flush_l2(fdga_handle* h, size_t bytes) {
+    if (!h || bytes == 0) return FDGA_ERR_ARG;
+    if (h->flush_bytes < bytes) {
+        if (h->flush_buf) cudaFree(h->flush_buf);
+        h->flush_buf = nullptr;
+        h->flush_bytes = 0;
+        cudaError_t e = cudaMalloc(&h->flush_buf, bytes);
+        if (e != cudaSuccess) return fail(h, FDGA_ERR_OOM, std::string("flush buffer: ") + cudaGetErrorString(e));
+        h->flush_bytes = bytes;
+    }
+    static unsigned char v = 0;
+    CK(cudaMemsetAsync(h->flush_buf, ++v, bytes, h->st));
+    return FDGA_OK;
 }
 
 int fdga_launches_per_iteration(const fdga_handle* h, int* n) {

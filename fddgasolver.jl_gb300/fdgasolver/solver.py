@@ -176,6 +176,10 @@ class _Solver:
         """Apply the iteration map n times to the unchanged device state (no host sync)."""
         self._check(self._lib.fdga_map_repeat(self._h, STRATEGIES[strategy], int(n)))
 
+    def flush_l2(self, nbytes=256 << 20):
+        """Overwrite the L2 with a device buffer write on the solver's stream."""
+        self._check(self._lib.fdga_flush_l2(self._h, int(nbytes)))
+
     def fixed_point_ptr(self, x_ptr, R_ptr, strategy="fdPA"):
         """fixed_point! on caller-owned host buffers (e.g. pinned) of state_len complex values."""
         self._check(self._lib.fdga_residual(self._h, STRATEGIES[strategy], x_ptr, R_ptr, self.state_len))

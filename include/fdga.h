@@ -125,6 +125,9 @@ int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t
 /* Applies the iteration map n times to the unchanged device state x (graph replays, no host
  * synchronisation): the device-resident timing loop of the benchmark. */
 int fdga_map_repeat(fdga_handle* h, int strategy, int n);
+/* Writes `bytes` of a device buffer on the handle's stream, evicting the L2 between timed
+ * iterations of a benchmark (the buffer is allocated on first use). */
+int fdga_flush_l2(fdga_handle* h, size_t bytes);
 /* Page-locked host buffers for host<->device copies of state vectors. */
 int fdga_host_alloc(size_t bytes, void** p);
 int fdga_host_free(void* p);
