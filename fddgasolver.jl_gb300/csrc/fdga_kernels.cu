@@ -225,6 +225,61 @@ __global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV)
     }
 }
 
+// Batched 2D transform over the L x L momentum grid: out[R][row] = scale Σ_P e^{sign 2πi P·R/L} in[P][row]
+// (momentum index x + L y outermost, `rows` contiguous values per momentum).  One CTA transforms TR
+// consecutive rows through shared memory (coalesced loads and stores along the rows).
+template <int L>
+__global__ void k_fft2_rows(const cplx* in, cplx* out, int rows, int sign, double scale, int TR) {
+    extern __shared__ cplx sh[];
+    constexpr int NR = L * L, RS = L + 1, BS = L * (L + 1) + 1;
+    const int r0 = blockIdx.x * TR;
+    for (int e = threadIdx.x; e < TR * NR; e += blockDim.x) {
+        const int r = e % TR, P = e / TR;
+        cplx v = (r0 + r < rows) ? in[(size_t)P * rows + r0 + r] : mk(0, 0);
+        if (sign < 0) v.y = -v.y;  // forward transform = conj(backward(conj))
+        sh[(size_t)r * BS + (P / L) * RS + (P % L)] = v;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < TR * L; q += blockDim.x) {
+        cplx* row = sh + (size_t)(q / L) * BS + (q % L) * RS;
+        cplx v[L];
+#pragma unroll
+        for (int x = 0; x < L; ++x) v[x] = row[x];
+        fft_bwd<L>(v);
+#pragma unroll
+        for (int x = 0; x < L; ++x) row[x] = v[x];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < TR * L; q += blockDim.x) {
+        cplx* col = sh + (size_t)(q / L) * BS + (q % L);
+        cplx v[L];
+#pragma unroll
+        for (int y = 0; y < L; ++y) v[y] = col[y * RS];
+        fft_bwd<L>(v);
+#pragma unroll
+        for (int y = 0; y < L; ++y) col[y * RS] = v[y];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < TR * NR; e += blockDim.x) {
+        const int r = e % TR, R = e / TR;
+        if (r0 + r >= rows) continue;
+        cplx v = sh[(size_t)r * BS + (R / L) * RS + (R % L)];
+        if (sign < 0) v.y = -v.y;
+        out[(size_t)R * rows + r0 + r] = v * scale;
+    }
+}
+// Direct-DFT fallback of k_fft2_rows for L that is not a power of two; one thread per output.
+__global__ void k_dft2_rows(const cplx* in, cplx* out, int rows, int L, const cplx* tw, double scale) {
+    const int NR = L * L;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= (size_t)NR * rows) return;
+    const int r = (int)(i % rows), R = (int)(i / rows);
+    const int Rx = R % L, Ry = R / L;
+    cplx acc = mk(0, 0);
+    for (int P = 0; P < NR; ++P) acc += in[(size_t)P * rows + r] * tw[((P % L) * Rx + (P / L) * Ry) % L];
+    out[i] = acc * scale;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Momentum averages A = Σ_P K[P] / Nq (s-wave evaluation, src/nonlocal/swave.jl:32-72)
 // blockIdx.y = channel*3 + class
@@ -314,7 +369,7 @@ __global__ void k_pisum_R(const cplx* GR, cplx* SR, Dims d) {
     if (w >= (size_t)2 * d.NPO * NR) return;
     const int which = (int)(w / ((size_t)d.NPO * NR));
     const int rest = (int)(w % ((size_t)d.NPO * NR));
-    const int m = rest / NR - (d.nPO - 1), R = rest % NR;
+    const int R = rest / d.NPO, m = rest % d.NPO - (d.nPO - 1);  // SR[w][R][Ω]
     const int L = d.L, Rx = R % L, Ry = R / L;
     const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
     cplx acc = mk(0, 0);
@@ -336,44 +391,30 @@ __global__ void k_pisum_R(const cplx* GR, cplx* SR, Dims d) {
     acc = warp_sum(acc);
     if (lane == 0) SR[w] = acc;
 }
-__global__ void k_pisum_P(const cplx* SR, cplx* S0, cplx* S1, const cplx* twp, Dims d) {
-    const int NR = d.L * d.L;
-    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= (size_t)2 * d.NPO * NR) return;
-    const int which = (int)(i / ((size_t)d.NPO * NR));
-    const int rest = (int)(i % ((size_t)d.NPO * NR));
-    const int P = rest / d.NPO, iO = rest % d.NPO;
-    const int Px = P % d.L, Py = P / d.L;
-    const cplx* sr = SR + ((size_t)which * d.NPO + iO) * NR;
-    cplx acc = mk(0, 0);
-    for (int R = 0; R < NR; ++R) {
-        const int Rx = R % d.L, Ry = R / d.L;
-        acc += sr[R] * twp[(Px * Rx + Py * Ry) % d.L];
-    }
-    (which ? S1 : S0)[(size_t)P * d.NPO + iO] = acc;
-}
-
 // S_X(ch, P, Ω) = Σ_ω [(Π-Π0)(Ω,ω,P) U + Π(Ω,ω,P) FL(Ω,ω̃,∞)]: the ω-sum of the BSE's right factor
 // (src/BSEa/BSEa_K1.jl:43, BSEa_K2.jl:185), from the row sums and the K2 window of FL.
 // Layout SX[ch][P][Ω] with Ω over the K1 box; SPi/SPi0 [w][P][Ω] with w = 0 pp, 1 ph.
 __global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0, FLP FL, cplx* SX, Dims d) {
     const size_t per = (size_t)d.Nq * d.NPO;
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t i = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;  // warp per output
+    const int lane = threadIdx.x & 31;
     if (i >= 3 * per) return;
     const int ch = (int)(i / per);
     const size_t r = i % per;
     const int m = (int)(r % d.NPO) - (d.nPO - 1), P = (int)(r / d.NPO);
     const int w = (ch == CH_P) ? 0 : 1;
     const cplx* Pi = w ? Piph : Pipp;
-    cplx v = (SPi[w * per + r] - SPi0[w * per + r]) * d.U;
+    cplx v = mk(0, 0);
     if (bin(m, d.n2O)) {
-        for (int nt = -d.n2n; nt < d.n2n; ++nt) {
+        for (int t = lane; t < d.N2n; t += 32) {
+            const int nt = t - d.n2n;
             const int n = (ch == CH_P) ? m - nt - 1 : nt;
             if (!fin(n, d.nPw)) continue;
             v += Pi[ixPi(d, P, m, n)] * fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, ch, m, nt, P);
         }
     }
-    SX[i] = v;
+    v = warp_sum(v);
+    if (lane == 0) SX[i] = (SPi[w * per + r] - SPi0[w * per + r]) * d.U + v;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -383,8 +424,8 @@ __global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const 
 // evaluated exactly as c·S_X + Σ_{ω ∈ K2 box} (F(Ω,∞,ω) - c) X(ω), c = F(Ω,∞,∞).
 // ---------------------------------------------------------------------------------------------
 template <int CH>
-__global__ void k_bse_K1(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const cplx* SX, cplx* out,
-                         const int* items, int nitems, Dims d) {
+__device__ __forceinline__ void bse_K1_body(const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+                                            const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
@@ -416,7 +457,8 @@ __global__ void k_bse_K1(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const
 //   nonlocal (src/nonlocal/BSEa/BSEa_K2.jl:1-39): Σ_{ω∈K2 mesh} Γ_irr(Ω,ν,ω̃) Π0(Ω,ω) U
 // ---------------------------------------------------------------------------------------------
 template <int CH>
-__global__ void k_bse_L_K2(VertP F, const cplx* Pi0, cplx* out, const int* items, int nitems, Dims d) {
+__device__ __forceinline__ void bse_L_K2_body(const VertP& F, const cplx* Pi0, cplx* out, const int* items, int nitems,
+                                              const Dims& d) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
@@ -451,8 +493,8 @@ __global__ void k_bse_L_K2(VertP F, const cplx* Pi0, cplx* out, const int* items
 // c·S_X + Σ_{ω ∈ union} (F(Ω,ν,ω) - F(Ω,∞,ω) - c) X(ω).
 // ---------------------------------------------------------------------------------------------
 template <int CH>
-__global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const cplx* SX, cplx* out,
-                         const int* items, int nitems, Dims d) {
+__device__ __forceinline__ void bse_K2_body(const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+                                            const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
@@ -460,7 +502,9 @@ __global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const
     const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
     const int P = idx / (d.N2n * d.N2O);
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
-    const cplx c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    // F(Ω,∞,ω) equals F(Ω,∞,∞) (bit for bit) unless ω is in the K2 box
+    const cplx cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    const cplx c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
     Windows win;
     const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
     win.add(-d.n2n, d.n2n - 1, lo, hi);
@@ -473,7 +517,8 @@ __global__ void k_bse_K2(VertP F, FLP FL, const cplx* Pi, const cplx* Pi0, const
     for (int t = lane; t < win.total; t += 32) {
         const int n = win.at(t);
         const int wt = cross(CH, m, n);
-        const cplx Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
+        const cplx Finf = fin(n, d.n2n) ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
+        const cplx Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
         const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
         const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
@@ -616,8 +661,8 @@ __global__ void k_k2_epilogue(cplx* out, const cplx* FLc, const cplx* FLt, const
 // out = T [vertex part] + T ref_scale [RefVertex part].
 // ---------------------------------------------------------------------------------------------
 template <int WHICH>
-__global__ void k_sde_L(VertP F, const cplx* Pi, const cplx* SPi, cplx* out, const int* items, int nitems,
-                        int use_vertex, double ref_scale, Dims d) {
+__device__ __forceinline__ void sde_L_body(const VertP& F, const cplx* Pi, const cplx* SPi, cplx* out, const int* items,
+                                           int nitems, int use_vertex, double ref_scale, const Dims& d) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
@@ -662,31 +707,90 @@ __global__ void k_sde_L(VertP F, const cplx* Pi, const cplx* SPi, cplx* out, con
     }
 }
 
-// Σ_inner(ν,k) = T/N Σ_{Ω,P} [G(Ω-ν, P-k) Lpp(Ω,ν,P) + G(Ω+ν, P+k) Lph(Ω,ν,P)]
-// (momentum-space form of src/nonlocal/SDE.jl:208-280 for L_G = L; local: src/SDE.jl:241-263);
-// one warp per output, lanes over (P, Ω).
-__global__ void k_sde_sigma(const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, Dims d) {
+// ---------------------------------------------------------------------------------------------
+// All-channel launches: blockIdx.y selects the channel (0 = p, 1 = t, 2 = a; SDE: 0 = pp, 1 = ph).
+// ---------------------------------------------------------------------------------------------
+__global__ void k_bse_K1_all(VertP F, FLP FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
+    switch (blockIdx.y) {
+        case CH_P: bse_K1_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
+        case CH_T: bse_K1_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
+        default:   bse_K1_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+    }
+}
+__global__ void k_bse_L_K2_all(VertP F, BubbleP B, ChanWork cw, Dims d) {
+    switch (blockIdx.y) {
+        case CH_P: bse_L_K2_body<CH_P>(F, B.pp0, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
+        case CH_T: bse_L_K2_body<CH_T>(F, B.ph0, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
+        default:   bse_L_K2_body<CH_A>(F, B.ph0, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+    }
+}
+__global__ void k_bse_K2_all(VertP F, FLP FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
+    switch (blockIdx.y) {
+        case CH_P: bse_K2_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
+        case CH_T: bse_K2_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
+        default:   bse_K2_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+    }
+}
+__global__ void k_sde_L_all(VertP F, BubbleP B, const cplx* SPpp, const cplx* SPph, ChanWork cw, int use_vertex,
+                            double ref_scale, Dims d) {
+    if (blockIdx.y == 0) sde_L_body<0>(F, B.pp, SPpp, cw.out[0], cw.items[0], cw.nitems[0], use_vertex, ref_scale, d);
+    else sde_L_body<1>(F, B.ph, SPph, cw.out[1], cw.items[1], cw.nitems[1], use_vertex, ref_scale, d);
+}
+
+// Finalize of one vertex class for the three channels (out-of-place from the representative
+// values): out_c[i] = op_c(raw_c[rep_c(i)]) (SymmetryGroup broadcast), then for K2 the FL terms of
+// BSE_K2! (src/BSEa/BSEa_K2.jl:95-101), then the t-channel pSp recombination (γtd + γa)/2
+// (src/BSE_templates.jl:35-38).  Slots are indexed by channel; an absent slot has out = nullptr.
+__global__ void k_finalize3(Finalize3 f, int k2_epilogue, int t_recombine, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cplx v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        v[c] = mk(0, 0);
+        if (!f.out[c]) continue;
+        if (f.map[c]) {
+            const uint32_t e = f.map[c][i];
+            v[c] = apply_op((int)(e & 3u), f.raw[c][e >> 2]);
+        } else {
+            v[c] = f.raw[c][i];
+        }
+    }
+    if (k2_epilogue) {
+        v[CH_P] += f.FL[CH_P][i];
+        v[CH_A] += f.FL[CH_A][i];
+        v[CH_T] += f.FL[CH_T][i] * 2.0;
+        v[CH_T] += f.FL[CH_A][i] * -1.0;
+    }
+    if (t_recombine) v[CH_T] = (v[CH_T] + v[CH_A]) * 0.5;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        if (f.out[c]) f.out[c][i] = v[c];
+}
+
+// Σ_inner in real space (src/nonlocal/SDE.jl:208-280; local src/SDE.jl:241-263 is the L = 1 case):
+//   Σ_R(ν, R) = Σ_Ω [G(-R, Ω-ν) Lpp(R, Ω, ν) + G(R, Ω+ν) Lph(-R, Ω, ν)],  L(R) = (1/N) Σ_P L(P) e^{-iP·R},
+//   Σ(ν, k) = T Σ_R e^{+ik·R} Σ_R(ν, R)   (the k transform is launch_fft2).  For L_G = L the ±L/2
+//   half weights of the reference's R scan sum to one per site.  Warp per (R, ν), lanes over Ω.
+__global__ void k_sde_sigma_R(const cplx* GR, const cplx* LppR, const cplx* LphR, cplx* SR, Dims d) {
     const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (w >= (size_t)d.Nk * d.NG) return;
-    const int nu = (int)(w % d.NG) - d.nG, k = (int)(w / d.NG);
+    const int NR = d.L * d.L;
+    if (w >= (size_t)NR * d.NG) return;
+    const int nu = (int)(w % d.NG) - d.nG, R = (int)(w / d.NG);
+    const int L = d.L, Rx = R % L, Ry = R / L;
+    const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
     cplx acc = mk(0, 0);
     if (fin(nu, d.n2n)) {
-        const int L = d.L, kx = k % L, ky = k / L;
-        const int npair = d.Nq * d.N2O;
-        for (int t = lane; t < npair; t += 32) {
-            const int P = t / d.N2O, m = t % d.N2O - (d.n2O - 1);
-            const int Px = P % L, Py = P / L;
-            const int kmP = ((Px - kx + L) % L) + L * ((Py - ky + L) % L);
-            const int kpP = ((Px + kx) % L) + L * ((Py + ky) % L);
-            const size_t il = ix2(d, P, m, nu);
+        for (int t = lane; t < d.N2O; t += 32) {
+            const int m = t - (d.n2O - 1);
             const int a = m - nu - 1, b = m + nu;
-            if (fin(a, d.nG)) acc += ldg(G + ixG(d, kmP, a)) * ldg(Lpp + il);
-            if (fin(b, d.nG)) acc += ldg(G + ixG(d, kpP, b)) * ldg(Lph + il);
+            if (fin(a, d.nG)) acc += GR[ixG(d, mR, a)] * LppR[ix2(d, R, m, nu)];
+            if (fin(b, d.nG)) acc += GR[ixG(d, R, b)] * LphR[ix2(d, mR, m, nu)];
         }
     }
     acc = warp_sum(acc);
-    if (lane == 0) S[w] = acc * (d.T / d.Nq);
+    if (lane == 0) SR[w] = acc;
 }
 
 // U² term (src/SDE.jl:328-364, src/nonlocal/SDE.jl:400-447), factorised:
@@ -694,48 +798,37 @@ __global__ void k_sde_sigma(const cplx* G, const cplx* Lpp, const cplx* Lph, cpl
 // GR layout [R][ν] (G(R)); s in [-(2nG-1), 2nG-1].
 __global__ void k_u2_corr(const cplx* GR, cplx* C, Dims d) {
     const int NS = 2 * d.NG - 1;
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     const int NR = d.L * d.L;
-    if (i >= (size_t)NR * NS) return;
-    const int s = (int)(i % NS) - (d.NG - 1), R = (int)(i / NS);
+    if (w >= (size_t)NR * NS) return;
+    const int s = (int)(w % NS) - (d.NG - 1), R = (int)(w / NS);
     const int L = d.L, Rx = R % L, Ry = R / L;
     const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
     cplx acc = mk(0, 0);
-    for (int n1 = -d.nG; n1 < d.nG; ++n1) {
+    for (int n1 = -d.nG + lane; n1 < d.nG; n1 += 32) {
         const int n3 = n1 + s;
         if (!fin(n3, d.nG)) continue;
         acc += GR[ixG(d, mR, n1)] * GR[ixG(d, R, n3)];
     }
-    C[i] = acc;
+    acc = warp_sum(acc);
+    if (lane == 0) C[w] = acc;
 }
 __global__ void k_u2_sum(const cplx* GR, const cplx* C, cplx* out, Dims d) {
     const int NS = 2 * d.NG - 1;
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     const int NR = d.L * d.L;
-    if (i >= (size_t)NR * d.NG) return;
-    const int nu = (int)(i % d.NG) - d.nG, R = (int)(i / d.NG);
+    if (w >= (size_t)NR * d.NG) return;
+    const int nu = (int)(w % d.NG) - d.nG, R = (int)(w / d.NG);
     cplx acc = mk(0, 0);
-    for (int n2 = -d.nG; n2 < d.nG; ++n2) {
+    for (int n2 = -d.nG + lane; n2 < d.nG; n2 += 32) {
         const int s = nu - n2;  // in [-(2nG-1), 2nG-1]
         acc += GR[ixG(d, R, n2)] * C[(size_t)R * NS + (s + d.NG - 1)];
     }
-    out[i] = acc * (d.U * d.U * d.T * d.T);
+    acc = warp_sum(acc);
+    if (lane == 0) out[w] = acc * (d.U * d.U * d.T * d.T);
 }
-// out[k][ν] = Σ_R e^{+2πi k·R/L} in[R][ν]   (bfft over the momentum axes); twc[j] = e^{+2πi j/L}
-__global__ void k_R_to_k(const cplx* in, cplx* out, const cplx* twc, Dims d) {
-    const int NR = d.L * d.L;
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= (size_t)NR * d.NG) return;
-    const int nu = (int)(i % d.NG), k = (int)(i / d.NG);
-    const int kx = k % d.L, ky = k / d.L;
-    cplx s = mk(0, 0);
-    for (int R = 0; R < NR; ++R) {
-        const int Rx = R % d.L, Ry = R / d.L;
-        s += in[(size_t)R * d.NG + nu] * twc[(kx * Rx + ky * Ry) % d.L];
-    }
-    out[i] = s;
-}
-
 // Σ assembly (src/SDE.jl:3-33, 219-283): Σ = op(Σin + Σ_U²)[rep] + H  (+ fdPA: - C0 + Σ0 - H0)
 __global__ void k_sigma_assemble(const cplx* Sin, const cplx* SU2, const uint32_t* map, const double* occ,
                                  const cplx* C0, const cplx* Sig0, cplx* Sig, double U, int hartree, int fdpa,
@@ -833,6 +926,8 @@ __global__ void k_nonfinite(const cplx* a, size_t n, unsigned int* count) {
 // Launchers
 // =============================================================================================
 static inline unsigned blocks_for(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,
+                        const cplx* tw_sign, const Dims& d);
 #define LAUNCH_CHECK() do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return e_; } while (0)
 
 cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n) {
@@ -844,9 +939,7 @@ cudaError_t launch_occupation(cudaStream_t s, const cplx* G, size_t n, double T,
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_g_realspace(cudaStream_t s, const cplx* G, cplx* GR, const cplx* tw, const Dims& d) {
-    const size_t n = (size_t)d.L * d.L * d.NG;
-    k_g_realspace<<<blocks_for(n, 128), 128, 0, s>>>(G, GR, tw, d);
-    LAUNCH_CHECK(); return cudaSuccess;
+    return launch_fft2(s, G, GR, d.NG, -1, 1.0 / (d.L * d.L), tw, d);
 }
 int bubble_tile(const Dims& d) {
     const int NR = d.L * d.L;
@@ -903,6 +996,30 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
     LAUNCH_CHECK(); return cudaSuccess;
 }
 
+template <int L>
+static cudaError_t launch_fft2_tpl(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale) {
+    constexpr int BS = L * (L + 1) + 1;
+    int tr = 32;
+    while (tr > 1 && (size_t)tr * BS * sizeof(cplx) > 48 * 1024) tr >>= 1;
+    const size_t shm = (size_t)tr * BS * sizeof(cplx);
+    k_fft2_rows<L><<<(unsigned)((rows + tr - 1) / tr), 256, shm, s>>>(in, out, rows, sign, scale, tr);
+    return cudaGetLastError();
+}
+cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,
+                        const cplx* tw_sign, const Dims& d) {
+    switch (d.L) {
+        case 1: return launch_fft2_tpl<1>(s, in, out, rows, sign, scale);
+        case 2: return launch_fft2_tpl<2>(s, in, out, rows, sign, scale);
+        case 4: return launch_fft2_tpl<4>(s, in, out, rows, sign, scale);
+        case 8: return launch_fft2_tpl<8>(s, in, out, rows, sign, scale);
+        case 16: return launch_fft2_tpl<16>(s, in, out, rows, sign, scale);
+        default: break;
+    }
+    const size_t n = (size_t)d.L * d.L * rows;
+    k_dft2_rows<<<blocks_for(n, 128), 128, 0, s>>>(in, out, rows, d.L, tw_sign, scale);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+
 cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
                           cplx* S0, cplx* S1, const Dims& d) {
     if (d.nPw == d.nPn) {  // the full mesh is stored: sum the rows
@@ -913,12 +1030,16 @@ cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const 
     const int NR = d.L * d.L;
     k_pisum_R<<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GR, SRtmp, d);
     LAUNCH_CHECK();
-    k_pisum_P<<<blocks_for((size_t)2 * d.NPO * NR, 128), 128, 0, s>>>(SRtmp, S0, S1, twp, d);
-    LAUNCH_CHECK(); return cudaSuccess;
+    // S^w[P][Ω] = Σ_R e^{+2πi P·R/L} SR[w][R][Ω]
+    cudaError_t e = launch_fft2(s, SRtmp, S0, d.NPO, +1, 1.0, twp, d);
+    if (e != cudaSuccess) return e;
+    e = launch_fft2(s, SRtmp + (size_t)NR * d.NPO, S1, d.NPO, +1, 1.0, twp, d);
+    if (e != cudaSuccess) return e;
+    return cudaSuccess;
 }
 cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
                       const FLP& FL, cplx* SX, const Dims& d) {
-    const size_t n = (size_t)3 * d.Nq * d.NPO;
+    const size_t n = (size_t)3 * d.Nq * d.NPO * 32;
     k_sx<<<blocks_for(n, 128), 128, 0, s>>>(Pipp, Piph, SPi, SPi0, FL, SX, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
@@ -935,28 +1056,32 @@ cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, 
     k_build_cache<<<blocks_for(n, 128), 128, 0, s>>>(F, C, blocks, nblocks, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
-    const unsigned g = blocks_for((size_t)nitems * 32, 128);
-    if (ch == CH_P) k_bse_K1<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
-    else if (ch == CH_T) k_bse_K1<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
-    else k_bse_K1<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
+static unsigned warp_grid(const ChanWork& cw, int nch) {
+    int mx = 0;
+    for (int c = 0; c < nch; ++c) mx = std::max(mx, cw.nitems[c]);
+    return blocks_for((size_t)mx * 32, 128);
+}
+cudaError_t launch_bse_K1_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                              const ChanWork& cw, const Dims& d) {
+    k_bse_K1_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* Pi0, cplx* out, const int* items,
-                            int nitems, const Dims& d) {
-    const unsigned g = blocks_for((size_t)nitems * 32, 128);
-    if (ch == CH_P) k_bse_L_K2<CH_P><<<g, 128, 0, s>>>(F, Pi0, out, items, nitems, d);
-    else if (ch == CH_T) k_bse_L_K2<CH_T><<<g, 128, 0, s>>>(F, Pi0, out, items, nitems, d);
-    else k_bse_L_K2<CH_A><<<g, 128, 0, s>>>(F, Pi0, out, items, nitems, d);
+cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VertP& F, const BubbleP& B, const ChanWork& cw, const Dims& d) {
+    k_bse_L_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, cw, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_bse_K2(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
-    const unsigned g = blocks_for((size_t)nitems * 32, 128);
-    if (ch == CH_P) k_bse_K2<CH_P><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
-    else if (ch == CH_T) k_bse_K2<CH_T><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
-    else k_bse_K2<CH_A><<<g, 128, 0, s>>>(F, FL, Pi, Pi0, SX, out, items, nitems, d);
+cudaError_t launch_bse_K2_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                              const ChanWork& cw, const Dims& d) {
+    k_bse_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_sde_L_all(cudaStream_t s, const VertP& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph,
+                             const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d) {
+    k_sde_L_all<<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n) {
+    k_finalize3<<<blocks_for(n, 256), 256, 0, s>>>(f, k2_epilogue, t_recombine, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 template <int MODE, int TILE>
@@ -990,26 +1115,24 @@ cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const
     k_k2_epilogue<<<blocks_for(n, 256), 256, 0, s>>>(out, FLc, FLt, FLa, outA, ch, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_sde_L(cudaStream_t s, int which, const VertP& F, const cplx* Pi, const cplx* SPi, cplx* out,
-                         const int* items, int nitems, int use_vertex, double ref_scale, const Dims& d) {
-    const unsigned g = blocks_for((size_t)nitems * 32, 128);
-    if (which == 0) k_sde_L<0><<<g, 128, 0, s>>>(F, Pi, SPi, out, items, nitems, use_vertex, ref_scale, d);
-    else k_sde_L<1><<<g, 128, 0, s>>>(F, Pi, SPi, out, items, nitems, use_vertex, ref_scale, d);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, const Dims& d) {
-    const size_t n = (size_t)d.Nk * d.NG * 32;
-    k_sde_sigma<<<blocks_for(n, 128), 128, 0, s>>>(G, Lpp, Lph, S, d);
-    LAUNCH_CHECK(); return cudaSuccess;
+cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
+                             cplx* S, const cplx* twm, const cplx* twp, const Dims& d) {
+    const int rows = d.N2O * d.N2n, NR = d.L * d.L;
+    const double invN = 1.0 / NR;
+    cudaError_t e = launch_fft2(s, Lpp, LR, rows, -1, invN, twm, d);
+    if (e == cudaSuccess) e = launch_fft2(s, Lph, LR + (size_t)NR * rows, rows, -1, invN, twm, d);
+    if (e != cudaSuccess) return e;
+    k_sde_sigma_R<<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(GR, LR, LR + (size_t)NR * rows, SR, d);
+    LAUNCH_CHECK();
+    return launch_fft2(s, SR, S, d.NG, +1, d.T, twp, d);
 }
 cudaError_t launch_u2(cudaStream_t s, const cplx* GR, cplx* C, cplx* SR, cplx* out, const cplx* twc, const Dims& d) {
     const int NR = d.L * d.L, NS = 2 * d.NG - 1;
-    k_u2_corr<<<blocks_for((size_t)NR * NS, 128), 128, 0, s>>>(GR, C, d);
+    k_u2_corr<<<blocks_for((size_t)NR * NS * 32, 128), 128, 0, s>>>(GR, C, d);
     LAUNCH_CHECK();
-    k_u2_sum<<<blocks_for((size_t)NR * d.NG, 128), 128, 0, s>>>(GR, C, SR, d);
+    k_u2_sum<<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(GR, C, SR, d);
     LAUNCH_CHECK();
-    k_R_to_k<<<blocks_for((size_t)NR * d.NG, 128), 128, 0, s>>>(SR, out, twc, d);
-    LAUNCH_CHECK(); return cudaSuccess;
+    return launch_fft2(s, SR, out, d.NG, +1, 1.0, twc, d);
 }
 cudaError_t launch_sigma_assemble(cudaStream_t s, const cplx* Sin, const cplx* SU2, const uint32_t* map,
                                   const double* occ, const cplx* C0, const cplx* Sig0, cplx* Sig, double U, int hartree,

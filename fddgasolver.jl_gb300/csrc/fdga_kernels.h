@@ -43,7 +43,33 @@ struct K3Args3 {  // the three channels of one K3 launch over a list of (P, Ω) 
     int nblocks;
 };
 
+struct ChanWork {  // per-channel work of an all-channel launch, indexed by channel (p, t, a) or (pp, ph)
+    const int* items[3];  // representative device indices (nullptr: item = index)
+    int nitems[3];
+    cplx* out[3];
+};
+struct BubbleP {
+    const cplx* pp;
+    const cplx* ph;
+    const cplx* pp0;
+    const cplx* ph0;
+};
+struct Finalize3 {  // indexed by channel (p, t, a)
+    const cplx* raw[3];
+    cplx* out[3];
+    const uint32_t* map[3];
+    const cplx* FL[3];
+};
+
 cudaError_t set_fft_twiddles();
+cudaError_t launch_bse_K1_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                              const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VertP& F, const BubbleP& B, const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_K2_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                              const ChanWork& cw, const Dims& d);
+cudaError_t launch_sde_L_all(cudaStream_t s, const VertP& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph,
+                             const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d);
+cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n);
 cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
                           cplx* S0, cplx* S1, const Dims& d);
 cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
@@ -57,20 +83,15 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
 cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d);
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
-cudaError_t launch_bse_K1(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d);
-cudaError_t launch_bse_L_K2(cudaStream_t s, int ch, const VertP& F, const cplx* Pi0, cplx* out, const int* items,
-                            int nitems, const Dims& d);
-cudaError_t launch_bse_K2(cudaStream_t s, int ch, const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
-                          const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d);
 cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d);
 cudaError_t launch_expand(cudaStream_t s, cplx* X, const uint32_t* map, size_t n);
 cudaError_t launch_half_sum(cudaStream_t s, cplx* out, const cplx* other, size_t n);
 cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa,
                                const cplx* outA, int ch, size_t n);
-cudaError_t launch_sde_L(cudaStream_t s, int which, const VertP& F, const cplx* Pi, const cplx* SPi, cplx* out,
-                         const int* items, int nitems, int use_vertex, double ref_scale, const Dims& d);
-cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* G, const cplx* Lpp, const cplx* Lph, cplx* S, const Dims& d);
+cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
+                             cplx* S, const cplx* twm, const cplx* twp, const Dims& d);
+cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,
+                        const cplx* tw_sign, const Dims& d);
 cudaError_t launch_u2(cudaStream_t s, const cplx* GR, cplx* C, cplx* SR, cplx* out, const cplx* twc, const Dims& d);
 cudaError_t launch_sigma_assemble(cudaStream_t s, const cplx* Sin, const cplx* SU2, const uint32_t* map,
                                   const double* occ, const cplx* C0, const cplx* Sig0, cplx* Sig, double U, int hartree,

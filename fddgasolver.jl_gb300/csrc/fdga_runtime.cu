@@ -61,7 +61,10 @@ struct fdga_handle {
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
     cplx *GR = nullptr, *u2C = nullptr, *u2R = nullptr, *twm = nullptr, *twp = nullptr;
     cplx *SPi = nullptr, *SPi0 = nullptr, *SX = nullptr;  // bubble row sums [2][Nq][NΠΩ]; S_X [3][Nq][NΠΩ]
-    cplx* SRtmp = nullptr;                                 // real-space row sums [2][NΠΩ][L*L]
+    cplx* SRtmp = nullptr;                                 // real-space row sums [2][L*L][NΠΩ]
+    cplx* LR = nullptr;                                    // L_pp, L_ph in real space [2][R][Ω][ν]
+    cplx* SigR = nullptr;                                  // Σ in real space [R][ν]
+    cplx *raw1 = nullptr, *raw2 = nullptr, *raw3 = nullptr;  // representative values [3 ch][K1|K2|K3]
     int* d_k3blocks = nullptr;                             // (P, Ω) blocks holding K3 class representatives
     void* flush_buf = nullptr;                             // L2 flush buffer (benchmarks)
     size_t flush_bytes = 0;
@@ -344,6 +347,30 @@ const Group& k2group(fdga_handle* h, int ch) { return ch == CH_P ? h->gK2pp : h-
         ++nl;                                                        \
     } while (0)
 
+// L_pp and L_ph (vertex part and/or RefVertex part / 3) at the K2-group representatives, then the
+// SymmetryGroup broadcast into h->Lpp, h->Lph.
+cudaError_t sde_L_pair(fdga_handle* h, const VertP& F, const BubbleP& B, const cplx* SPi, int use_vertex, double rs,
+                       int& nl) {
+    const Dims& d = h->d;
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    ChanWork cw{};
+    const Group* g[2] = {&h->gK2pp, &h->gK2ph};
+    for (int w = 0; w < 2; ++w) {
+        cw.items[w] = g[w]->trivial ? nullptr : g[w]->d_items;
+        cw.nitems[w] = g[w]->trivial ? (int)h->n2 : g[w]->nitems;
+        cw.out[w] = h->raw2 + (size_t)w * h->n2;
+    }
+    cudaError_t e = launch_sde_L_all(h->st, F, B, SPi, SPi + nS, cw, use_vertex, rs, d);
+    if (e != cudaSuccess) return e;
+    ++nl;
+    Finalize3 f{};
+    f.raw[0] = h->raw2; f.out[0] = h->Lpp; f.map[0] = g[0]->trivial ? nullptr : g[0]->d_map;
+    f.raw[2] = h->raw2 + h->n2; f.out[2] = h->Lph; f.map[2] = g[1]->trivial ? nullptr : g[1]->d_map;
+    e = launch_finalize3(h->st, f, 0, 0, h->n2);
+    if (e == cudaSuccess) ++nl;
+    return e;
+}
+
 using StageHook = std::function<void(const char*)>;
 
 int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree, int& nl,
@@ -379,59 +406,79 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     FLP FL;
     for (int c = 0; c < 3; ++c) FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
     const int order[3] = {CH_P, CH_A, CH_T};
+    BubbleP B{h->Pipp, h->Piph, h->Pi0pp, h->Pi0ph};
     auto Pi = [&](int ch) { return ch == CH_P ? h->Pipp : h->Piph; };
     auto Pi0 = [&](int ch) { return ch == CH_P ? h->Pi0pp : h->Pi0ph; };
+    // work lists of the K1 / K2 classes (p uses the pp groups, a and t the ph groups)
+    auto work = [&](int cls, cplx* raw) {
+        ChanWork cw{};
+        const size_t n = cls == 1 ? h->n1 : h->n2;
+        for (int ch = 0; ch < 3; ++ch) {
+            const Group& g = cls == 1 ? h->gK1 : k2group(h, ch);
+            cw.items[ch] = g.trivial ? nullptr : g.d_items;
+            cw.nitems[ch] = g.trivial ? (int)n : g.nitems;
+            cw.out[ch] = raw + (size_t)ch * n;
+        }
+        return cw;
+    };
+    auto fin = [&](int cls, cplx* raw, cplx* const out[3], const Group* const grp[3]) {
+        Finalize3 f{};
+        const size_t n = cls == 1 ? h->n1 : (cls == 2 ? h->n2 : h->n3);
+        for (int ch = 0; ch < 3; ++ch) {
+            f.raw[ch] = raw + (size_t)ch * n;
+            f.out[ch] = out[ch];
+            f.map[ch] = grp[ch]->trivial ? nullptr : grp[ch]->d_map;
+            f.FL[ch] = h->FLK2 + (size_t)ch * h->n2;
+        }
+        return f;
+    };
     if (strategy == FDGA_FDPA) {
-        for (int ch : order) {
-            const Group& g = k2group(h, ch);
-            cplx* out = h->FLK2 + (size_t)ch * h->n2;
-            LC(launch_bse_L_K2(s, ch, F, Pi0(ch), out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n2 : g.nitems, d));
-            if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n2));
-            if (ch == CH_T) LC(launch_half_sum(s, out, h->FLK2 + (size_t)CH_A * h->n2, h->n2));
+        {  // left K2 (FL.K2)
+            ChanWork cw = work(2, h->raw2);
+            LC(launch_bse_L_K2_all(s, F, B, cw, d));
+            cplx* out[3] = {h->FLK2, h->FLK2 + h->n2, h->FLK2 + 2 * h->n2};
+            const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
+            LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 0, 1, h->n2));
         }
         stage("bse_L_K2");
-        K3Args3 a3{};
-        for (int i = 0; i < 3; ++i) {
-            const int ch = order[i];
-            const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
-            K3Args& a = a3.a[i];
-            a.A = C.c[cg]; a.B0 = C.c[cf0]; a.Pi0 = Pi0(ch);
-            a.out = h->FLK3 + (size_t)ch * h->n3;
-            a3.ch[i] = ch;
+        {  // left K3 (FL.K3)
+            K3Args3 a3{};
+            for (int i = 0; i < 3; ++i) {
+                const int ch = order[i];
+                const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+                K3Args& a = a3.a[i];
+                a.A = C.c[cg]; a.B0 = C.c[cf0]; a.Pi0 = Pi0(ch);
+                a.out = h->raw3 + (size_t)ch * h->n3;
+                a3.ch[i] = ch;
+            }
+            a3.blocks = h->d_k3blocks;
+            a3.nblocks = h->nk3blocks;
+            LC(launch_bse_K3(s, 0, a3, 3, d));
+            cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
+            const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
+            LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
         }
-        a3.blocks = h->d_k3blocks;
-        a3.nblocks = h->nk3blocks;
-        LC(launch_bse_K3(s, 0, a3, 3, d));
-        for (int ch : order) {
-            const Group& g = ch == CH_P ? h->gK3ppL : h->gK3phL;
-            if (!g.trivial) LC(launch_expand(s, h->FLK3 + (size_t)ch * h->n3, g.d_map, h->n3));
-        }
-        LC(launch_half_sum(s, h->FLK3 + (size_t)CH_T * h->n3, h->FLK3 + (size_t)CH_A * h->n3, h->n3));
         stage("bse_L_K3");
     }
     // ω-sums of the right BSE factor (needs FL.K2 of this iteration)
     LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FL, h->SX, d));
-    // K1
-    for (int ch : order) {
-        cplx* out = chanK(h, h->yS, ch, 1);
-        const Group& g = h->gK1;
-        LC(launch_bse_K1(s, ch, F, FL, Pi(ch), Pi0(ch), h->SX, out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n1 : g.nitems, d));
-        if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n1));
-        if (ch == CH_T) LC(launch_half_sum(s, out, chanK(h, h->yS, CH_A, 1), h->n1));
+    {  // K1
+        ChanWork cw = work(1, h->raw1);
+        LC(launch_bse_K1_all(s, F, FL, B, h->SX, cw, d));
+        cplx* out[3] = {chanK(h, h->yS, CH_P, 1), chanK(h, h->yS, CH_T, 1), chanK(h, h->yS, CH_A, 1)};
+        const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
+        LC(launch_finalize3(s, fin(1, h->raw1, out, grp), 0, 1, h->n1));
     }
     stage("bse_K1");
-    // K2
-    for (int ch : order) {
-        cplx* out = chanK(h, h->yS, ch, 2);
-        const Group& g = k2group(h, ch);
-        LC(launch_bse_K2(s, ch, F, FL, Pi(ch), Pi0(ch), h->SX, out, g.trivial ? nullptr : g.d_items, g.trivial ? (int)h->n2 : g.nitems, d));
-        if (!g.trivial) LC(launch_expand(s, out, g.d_map, h->n2));
-        LC(launch_k2_epilogue(s, out, h->FLK2 + (size_t)ch * h->n2, h->FLK2 + (size_t)CH_T * h->n2,
-                              h->FLK2 + (size_t)CH_A * h->n2, chanK(h, h->yS, CH_A, 2), ch, h->n2));
+    {  // K2
+        ChanWork cw = work(2, h->raw2);
+        LC(launch_bse_K2_all(s, F, FL, B, h->SX, cw, d));
+        cplx* out[3] = {chanK(h, h->yS, CH_P, 2), chanK(h, h->yS, CH_T, 2), chanK(h, h->yS, CH_A, 2)};
+        const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
+        LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 1, 1, h->n2));
     }
     stage("bse_K2");
-    // K3
-    {
+    {  // K3
         K3Args3 a3{};
         for (int i = 0; i < 3; ++i) {
             const int ch = order[i];
@@ -440,34 +487,24 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             K3Args& a = a3.a[i];
             a.A = C.c[cf]; a.B0 = C.c[cf0]; a.G = C.c[cg]; a.Pi = Pi(ch); a.Pi0 = Pi0(ch);
             a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3; a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
-            a.out = chanK(h, h->yS, ch, 3);
+            a.out = h->raw3 + (size_t)ch * h->n3;
             a3.ch[i] = ch;
         }
         a3.blocks = h->d_k3blocks;
         a3.nblocks = h->nk3blocks;
         LC(launch_bse_K3(s, 1, a3, 3, d));
-        for (int ch : order) {
-            const Group& g = ch == CH_P ? h->gK3pp : h->gK3ph;
-            if (!g.trivial) LC(launch_expand(s, chanK(h, h->yS, ch, 3), g.d_map, h->n3));
-        }
-        LC(launch_half_sum(s, chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3), h->n3));
+        cplx* out[3] = {chanK(h, h->yS, CH_P, 3), chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3)};
+        const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
+        LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
     }
     stage("bse_K3");
     // SDE (src/SDE.jl:3-33) with the new F
     cplx* SigOut = sigmaOf(h, h->yS);
     if (update_sigma) {
-        const Group& gp = h->gK2pp;
-        const Group& gh = h->gK2ph;
-        const int* ip = gp.trivial ? nullptr : gp.d_items;
-        const int* ih = gh.trivial ? nullptr : gh.d_items;
-        const int np_ = gp.trivial ? (int)h->n2 : gp.nitems, nh_ = gh.trivial ? (int)h->n2 : gh.nitems;
         const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
-        const size_t nS = (size_t)d.Nq * d.NPO;
-        LC(launch_sde_L(s, 0, Fn, h->Pipp, h->SPi, h->Lpp, ip, np_, 1, rs, d));
-        LC(launch_sde_L(s, 1, Fn, h->Piph, h->SPi + nS, h->Lph, ih, nh_, 1, rs, d));
-        if (!gp.trivial) LC(launch_expand(s, h->Lpp, gp.d_map, h->n2));
-        if (!gh.trivial) LC(launch_expand(s, h->Lph, gh.d_map, h->n2));
-        LC(launch_sde_sigma(s, h->G, h->Lpp, h->Lph, h->SigIn, d));
+        LC(sde_L_pair(h, Fn, B, h->SPi, 1, rs, nl));
+        LC(launch_sde_sigma(s, h->GR, h->Lpp, h->Lph, h->LR, h->SigR, h->SigIn, h->twm, h->twp, d));
+        nl += 3;
         LC(launch_u2(s, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
         nl += 2;
         LC(launch_occupation(s, h->G, h->nGk, d.T, d.Nk, h->occ));
@@ -486,15 +523,10 @@ int compute_C0(fdga_handle* h) {
     const Dims& d = h->d;
     int nl = 0;
     VertP F0 = vertex_view(h, h->yS);  // only the RefVertex fields are read by the REF kernels
-    const Group& gp = h->gK2pp;
-    const Group& gh = h->gK2ph;
-    const size_t nS = (size_t)d.Nq * d.NPO;
-    LC(launch_sde_L(s, 0, F0, h->Pi0pp, h->SPi0, h->Lpp, gp.trivial ? nullptr : gp.d_items, gp.trivial ? (int)h->n2 : gp.nitems, 0, 1.0 / 3.0, d));
-    LC(launch_sde_L(s, 1, F0, h->Pi0ph, h->SPi0 + nS, h->Lph, gh.trivial ? nullptr : gh.d_items, gh.trivial ? (int)h->n2 : gh.nitems, 0, 1.0 / 3.0, d));
-    if (!gp.trivial) LC(launch_expand(s, h->Lpp, gp.d_map, h->n2));
-    if (!gh.trivial) LC(launch_expand(s, h->Lph, gh.d_map, h->n2));
-    LC(launch_sde_sigma(s, h->G0, h->Lpp, h->Lph, h->SigIn, d));
+    BubbleP B0{h->Pi0pp, h->Pi0ph, h->Pi0pp, h->Pi0ph};
+    LC(sde_L_pair(h, F0, B0, h->SPi0, 0, 1.0 / 3.0, nl));
     LC(launch_g_realspace(s, h->G0, h->GR, h->twm, d));
+    LC(launch_sde_sigma(s, h->GR, h->Lpp, h->Lph, h->LR, h->SigR, h->SigIn, h->twm, h->twp, d));
     LC(launch_u2(s, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
     LC(launch_sigma_assemble(s, h->SigIn, h->SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, h->occ, nullptr,
                              nullptr, h->C0, d.U, 0, 0, 0.0, h->nGk));
@@ -672,6 +704,8 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     ALC(h->twm, d.L); ALC(h->twp, d.L);
     ALC(h->SPi, 2 * (size_t)d.Nq * d.NPO); ALC(h->SPi0, 2 * (size_t)d.Nq * d.NPO); ALC(h->SX, 3 * (size_t)d.Nq * d.NPO);
     ALC(h->SRtmp, 2 * (size_t)d.NPO * d.Nq);
+    ALC(h->LR, 2 * h->n2); ALC(h->SigR, h->nGk);
+    ALC(h->raw1, 3 * h->n1); ALC(h->raw2, 3 * h->n2); ALC(h->raw3, 3 * h->n3);
     h->nk3blocks = d.Nq * d.N3O;
     ALC(h->occ, 1);
     ALC(h->perm, h->nstate);
