@@ -2,7 +2,7 @@
 //
 // Each kernel restates one reference function (cited per kernel).  Work items of the
 // symmetry-grouped sums are class representatives (device indices); the remaining elements
-// are filled by k_expand with the class operation, as MatsubaraFunctions' SymmetryGroup does.
+// are filled by k_finalize3 with the class operation, as MatsubaraFunctions' SymmetryGroup does.
 #include "fdga_device.cuh"
 #include "fdga_kernels.h"
 
@@ -618,39 +618,7 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
         }
 }
 
-// ---------------------------------------------------------------------------------------------
-// Symmetry expansion: X[i] = op(X[rep(i)]) for every non-representative i; map = rep*4 + op.
-// ---------------------------------------------------------------------------------------------
-__global__ void k_expand(cplx* X, const uint32_t* map, size_t n) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t e = map[i];
-    const size_t r = e >> 2;
-    if (r == i) return;
-    X[i] = apply_op((int)(e & 3u), X[r]);
-}
 
-// out = (out + other) * 0.5   (t-channel pSp recombination, src/BSE_templates.jl:35-38)
-__global__ void k_half_sum(cplx* out, const cplx* other, size_t n) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    out[i] = (out[i] + other[i]) * 0.5;
-}
-// K2 epilogue of BSE_K2!: a,p: K2 += FL.K2;  t: K2 += 2 FLt.K2 - FLa.K2, then (K2 + K2a)/2
-__global__ void k_k2_epilogue(cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa, const cplx* outA, int ch,
-                              size_t n) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    cplx v = out[i];
-    if (ch == CH_T) {
-        v += FLt[i] * 2.0;
-        v += FLa[i] * -1.0;
-        v = (v + outA[i]) * 0.5;
-    } else {
-        v += FLc[i];
-    }
-    out[i] = v;
-}
 
 // ---------------------------------------------------------------------------------------------
 // SDE: L_pp, L_ph (src/SDE.jl:79-217, src/nonlocal/SDE.jl:3-143), warp per item.
@@ -859,7 +827,8 @@ __global__ void k_scatter(cplx* dst, const cplx* src, const uint32_t* perm, size
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i < n) dst[perm[i]] = src[i];
 }
-// fx = y - x ; g = x + beta fx ; partial max|fx| per block
+// fx = y - x ; g = x + beta fx ; partial max|fx|² per block (the host takes the square root of the
+// maximum, which equals the maximum of |fx| since the square root is monotone)
 __global__ void k_residual(const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax, size_t n) {
     __shared__ double red[256];
     double mx = 0.0;
@@ -867,7 +836,7 @@ __global__ void k_residual(const cplx* y, const cplx* x, cplx* fx, cplx* g, doub
         const cplx f = y[i] - x[i];
         fx[i] = f;
         if (g) g[i] = x[i] + f * beta;
-        mx = fmax(mx, hypot(f.x, f.y));
+        mx = fmax(mx, f.x * f.x + f.y * f.y);
     }
     red[threadIdx.x] = mx;
     __syncthreads();
@@ -877,44 +846,28 @@ __global__ void k_residual(const cplx* y, const cplx* x, cplx* fx, cplx* g, doub
     }
     if (threadIdx.x == 0) pmax[blockIdx.x] = red[0];
 }
-// partial sums of conj(a)·b per block
-__global__ void k_dot(const cplx* a, const cplx* b, cplx* part, size_t n) {
-    __shared__ double rx[256], ry[256];
-    double sx = 0.0, sy = 0.0;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const cplx u = a[i], v = b[i];
-        sx += u.x * v.x + u.y * v.y;
-        sy += u.x * v.y - u.y * v.x;
-    }
-    rx[threadIdx.x] = sx;
-    ry[threadIdx.x] = sy;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) { rx[threadIdx.x] += rx[threadIdx.x + o]; ry[threadIdx.x] += ry[threadIdx.x + o]; }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[blockIdx.x] = mk(rx[0], ry[0]);
-}
-// y += a * x (complex a)
-__global__ void k_axpy(cplx* y, const cplx* x, cplx a, size_t n) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i < n) y[i] += a * x[i];
-}
-// y = a * y + b * x
-__global__ void k_rot(cplx* qa, cplx* qb, double c, cplx s, size_t n) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const cplx a = qa[i], b = qb[i];
-    qa[i] = a * c + conjg(s) * b;
-    qb[i] = (-s) * a + b * c;
-}
 __global__ void k_sub(cplx* out, const cplx* a, const cplx* b, size_t n) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = a[i] - b[i];
 }
-__global__ void k_scale(cplx* out, const cplx* a, double s, size_t n) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i < n) out[i] = a[i] * s;
+// χ_r from the K1 arrays ([P][Ω], identical to the reference's column-major [Ω, P]):
+// m: γa.K1/U², d: (γa.K1 - 2γt.K1)/U², s: -2γp.K1/U²; local != 0 averages over P (fixed order).
+__global__ void k_chi(const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double invU2, int NO, int Nq,
+                      int local, cplx* out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    auto chi = [&](size_t i) -> cplx {
+        if (which == 0) return K1a[i] * invU2;
+        if (which == 1) return (K1a[i] - K1t[i] * 2.0) * invU2;
+        return K1p[i] * (-2.0 * invU2);
+    };
+    if (local) {
+        if (j >= NO) return;
+        cplx s = mk(0.0, 0.0);
+        for (int P = 0; P < Nq; ++P) s += chi((size_t)P * NO + j);
+        out[j] = s * (1.0 / Nq);
+    } else if ((size_t)j < (size_t)NO * Nq) {
+        out[j] = chi(j);
+    }
 }
 // count of non-finite values
 __global__ void k_nonfinite(const cplx* a, size_t n, unsigned int* count) {
@@ -1102,19 +1055,6 @@ cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots
     if (N <= 24) return launch_k3_tile<1, 24>(s, a, nslots, d);
     return launch_k3_tile<1, 32>(s, a, nslots, d);
 }
-cudaError_t launch_expand(cudaStream_t s, cplx* X, const uint32_t* map, size_t n) {
-    k_expand<<<blocks_for(n, 256), 256, 0, s>>>(X, map, n);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_half_sum(cudaStream_t s, cplx* out, const cplx* other, size_t n) {
-    k_half_sum<<<blocks_for(n, 256), 256, 0, s>>>(out, other, n);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa,
-                               const cplx* outA, int ch, size_t n) {
-    k_k2_epilogue<<<blocks_for(n, 256), 256, 0, s>>>(out, FLc, FLt, FLa, outA, ch, n);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d) {
     const int rows = d.N2O * d.N2n, NR = d.L * d.L;
@@ -1153,24 +1093,14 @@ cudaError_t launch_residual(cudaStream_t s, const cplx* y, const cplx* x, cplx* 
     k_residual<<<nblk, 256, 0, s>>>(y, x, fx, g, beta, pmax, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_dot(cudaStream_t s, const cplx* a, const cplx* b, cplx* part, int nblk, size_t n) {
-    k_dot<<<nblk, 256, 0, s>>>(a, b, part, n);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_axpy(cudaStream_t s, cplx* y, const cplx* x, cplx a, size_t n) {
-    k_axpy<<<blocks_for(n, 256), 256, 0, s>>>(y, x, a, n);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_rot(cudaStream_t s, cplx* qa, cplx* qb, double c, cplx sn, size_t n) {
-    k_rot<<<blocks_for(n, 256), 256, 0, s>>>(qa, qb, c, sn, n);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
 cudaError_t launch_sub(cudaStream_t s, cplx* out, const cplx* a, const cplx* b, size_t n) {
     k_sub<<<blocks_for(n, 256), 256, 0, s>>>(out, a, b, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_scale(cudaStream_t s, cplx* out, const cplx* a, double sc, size_t n) {
-    k_scale<<<blocks_for(n, 256), 256, 0, s>>>(out, a, sc, n);
+cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double U,
+                       int NO, int Nq, int local, cplx* out) {
+    const size_t n = local ? (size_t)NO : (size_t)NO * Nq;
+    k_chi<<<blocks_for(n, 256), 256, 0, s>>>(K1p, K1t, K1a, which, 1.0 / (U * U), NO, Nq, local, out);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count) {

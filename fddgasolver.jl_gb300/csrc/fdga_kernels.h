@@ -61,6 +61,14 @@ struct Finalize3 {  // indexed by channel (p, t, a)
     const cplx* FL[3];
 };
 
+constexpr int AA_MAX = 64;  // largest Anderson memory of the device solver
+struct AAVecs {
+    const cplx* v[AA_MAX];
+};
+struct AAVecsW {
+    cplx* v[AA_MAX];
+};
+
 cudaError_t set_fft_twiddles();
 cudaError_t launch_bse_K1_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
                               const ChanWork& cw, const Dims& d);
@@ -84,10 +92,6 @@ cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW&
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
 cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d);
-cudaError_t launch_expand(cudaStream_t s, cplx* X, const uint32_t* map, size_t n);
-cudaError_t launch_half_sum(cudaStream_t s, cplx* out, const cplx* other, size_t n);
-cudaError_t launch_k2_epilogue(cudaStream_t s, cplx* out, const cplx* FLc, const cplx* FLt, const cplx* FLa,
-                               const cplx* outA, int ch, size_t n);
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d);
 cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,
@@ -100,11 +104,20 @@ cudaError_t launch_gather(cudaStream_t s, cplx* dst, const cplx* src, const uint
 cudaError_t launch_scatter(cudaStream_t s, cplx* dst, const cplx* src, const uint32_t* perm, size_t n);
 cudaError_t launch_residual(cudaStream_t s, const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax,
                             int nblk, size_t n);
-cudaError_t launch_dot(cudaStream_t s, const cplx* a, const cplx* b, cplx* part, int nblk, size_t n);
-cudaError_t launch_axpy(cudaStream_t s, cplx* y, const cplx* x, cplx a, size_t n);
-cudaError_t launch_rot(cudaStream_t s, cplx* qa, cplx* qb, double c, cplx sn, size_t n);
 cudaError_t launch_sub(cudaStream_t s, cplx* out, const cplx* a, const cplx* b, size_t n);
-cudaError_t launch_scale(cudaStream_t s, cplx* out, const cplx* a, double sc, size_t n);
+cudaError_t launch_aa_diff(cudaStream_t s, int nblk, cplx* dg, const cplx* g, const cplx* gold, cplx* df,
+                           const cplx* fx, const cplx* Qb, cplx* part_out, size_t n);
+cudaError_t launch_aa_mgs(cudaStream_t s, int nblk, cplx* df, const cplx* Qa, const cplx* part_in, cplx* Rentry,
+                          const cplx* Qb, cplx* part_out, size_t n);
+cudaError_t launch_aa_qnew(cudaStream_t s, int nblk, cplx* Qk, const cplx* df, const cplx* part_in, cplx* Rkk,
+                           size_t n);
+cudaError_t launch_aa_gamma(cudaStream_t s, int nblk, const AAVecs& Q, int meff, const cplx* fx, cplx* part,
+                            const cplx* R, int m, cplx* gam, size_t n);
+cudaError_t launch_aa_update(cudaStream_t s, int nblk, cplx* x, const cplx* g, const AAVecs& dG, const cplx* gam,
+                             int meff, const cplx* fx, cplx* fxold, cplx* gold, size_t n);
+cudaError_t launch_aa_delete(cudaStream_t s, int nblk, cplx* R, int m, cplx* rot, const AAVecsW& Q, size_t n);
+cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double U,
+                       int NO, int Nq, int local, cplx* out);
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count);
 
 }  // namespace fdga

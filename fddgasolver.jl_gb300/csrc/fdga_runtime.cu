@@ -79,7 +79,7 @@ struct fdga_handle {
     // Anderson
     std::vector<cplx*> aa_buf;
     double* d_part = nullptr;
-    cplx* d_cpart = nullptr;
+    cplx *aa_R = nullptr, *aa_rot = nullptr, *aa_gam = nullptr, *aa_part = nullptr;  // device QR state
     std::vector<void*> allocs;
 };
 
@@ -578,22 +578,10 @@ double reduce_max(fdga_handle* h, int nblk, int& status) {
     cudaError_t e = cudaMemcpyAsync(part.data(), h->d_part, nblk * sizeof(double), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     if (e != cudaSuccess) { status = cuda_fail(h, e, "reduce_max"); return 0.0; }
-    double m = 0.0;
+    double m = 0.0;  // the partials are squared magnitudes
     for (double v : part) m = std::max(m, v);
     status = FDGA_OK;
-    return m;
-}
-
-std::complex<double> dot(fdga_handle* h, const cplx* a, const cplx* b, int& status) {
-    cudaError_t e = launch_dot(h->st, a, b, h->d_cpart, NBLK_RED, h->nstate);
-    std::vector<cplx> part(NBLK_RED);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), h->d_cpart, NBLK_RED * sizeof(cplx), cudaMemcpyDeviceToHost, h->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-    if (e != cudaSuccess) { status = cuda_fail(h, e, "dot"); return 0.0; }
-    std::complex<double> s = 0.0;
-    for (auto& v : part) s += std::complex<double>(v.x, v.y);
-    status = FDGA_OK;
-    return s;
+    return std::sqrt(m);
 }
 
 bool names_vertex(const std::string& n, std::string& vn, int& ch, int& cls) {
@@ -709,7 +697,7 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     h->nk3blocks = d.Nq * d.N3O;
     ALC(h->occ, 1);
     ALC(h->perm, h->nstate);
-    ALC(h->d_part, NBLK_RED); ALC(h->d_cpart, NBLK_RED);
+    ALC(h->d_part, NBLK_RED);
     {
         std::vector<cplx> tm(d.L), tp(d.L);
         for (int j = 0; j < d.L; ++j) {
@@ -808,7 +796,7 @@ int fdga_init_sym_grp(fdga_handle* h) {
         if (r) return r;
     }
     // (P, Ω) blocks of the K3 mesh that hold a representative of any K3 group: only these blocks
-    // of the caches and of the K3 GEMMs are computed; k_expand fills the rest.
+    // of the caches and of the K3 GEMMs are computed; k_finalize3 fills the rest.
     {
         const size_t bs = (size_t)h->d.N3n * h->d.N3n;
         std::vector<char> used((size_t)h->d.Nq * h->d.N3O, 0);
@@ -905,11 +893,24 @@ int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double bet
         if (r) return r;
         h->aa_buf.push_back(p);
     }
+    if (m > AA_MAX) return fail(h, FDGA_ERR_ARG, "Anderson memory exceeds " + std::to_string(AA_MAX));
+    if (!h->aa_R) {
+        int r = dalloc(h, &h->aa_R, (size_t)AA_MAX * AA_MAX);
+        if (!r) r = dalloc(h, &h->aa_rot, 2 * (size_t)AA_MAX);
+        if (!r) r = dalloc(h, &h->aa_gam, (size_t)AA_MAX);
+        if (!r) r = dalloc(h, &h->aa_part, (size_t)(AA_MAX + 2) * NBLK_RED);
+        if (r) return r;
+    }
     cplx *fx = h->aa_buf[0], *g = h->aa_buf[1], *fxold = h->aa_buf[2], *gold = h->aa_buf[3];
     std::vector<cplx*> dG(h->aa_buf.begin() + 4, h->aa_buf.begin() + 4 + m);
-    std::vector<cplx*> Q(h->aa_buf.begin() + 4 + m, h->aa_buf.begin() + 4 + 2 * m);
-    std::vector<std::complex<double>> R((size_t)m * m, 0.0), gam(m);
-    auto Rr = [&](int i, int j) -> std::complex<double>& { return R[(size_t)i + (size_t)m * j]; };
+    AAVecsW Q{};
+    for (int i = 0; i < m; ++i) Q.v[i] = h->aa_buf[4 + m + i];
+    AAVecs Qc{};
+    for (int i = 0; i < m; ++i) Qc.v[i] = Q.v[i];
+    cplx* R = h->aa_R;
+    cplx* pp[2] = {h->aa_part, h->aa_part + NBLK_RED};  // ping-pong partials of the Gram-Schmidt passes
+    cplx* pdot = h->aa_part + 2 * NBLK_RED;              // partials of Qᴴ fx, [AA_MAX][NBLK_RED]
+    if (m > 0) CK(cudaMemsetAsync(R, 0, (size_t)m * m * sizeof(cplx), h->st));
     int m_eff = 0, it = 0, status = 0;
     double resid = 0.0;
     bool converged = false;
@@ -922,60 +923,35 @@ int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double bet
         if (!std::isfinite(resid)) return fail(h, FDGA_ERR_NONFINITE, "non-finite residual in solve");
         if (trace) trace[it - 1] = resid;
         if (resid < tol) { converged = true; break; }
-        CK(cudaMemcpyAsync(h->xS, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-        if (m == 0) continue;
-        if (it == 1) {
+        if (m == 0 || it == 1) {
+            CK(cudaMemcpyAsync(h->xS, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+            if (m == 0) continue;
             CK(cudaMemcpyAsync(fxold, fx, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
             CK(cudaMemcpyAsync(gold, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
             continue;
         }
         m_eff += 1;
         if (m_eff > m) {
+            // qrdelete!: Givens rotations on R and Q, Δg columns shift by one (pointer rotation)
             std::rotate(dG.begin(), dG.begin() + 1, dG.end());
-            for (int i = 1; i < m; ++i) {
-                const std::complex<double> f = Rr(i - 1, i), gg = Rr(i, i);
-                double c;
-                std::complex<double> sn;
-                const double af = std::abs(f), ag = std::abs(gg);
-                if (ag == 0.0) { c = 1.0; sn = 0.0; }
-                else if (af == 0.0) { c = 0.0; sn = std::conj(gg) / ag; }
-                else { const double rr = std::hypot(af, ag); c = af / rr; sn = (f / af) * std::conj(gg) / rr; }
-                for (int j = 0; j < m; ++j) {
-                    const std::complex<double> a = Rr(i - 1, j), b = Rr(i, j);
-                    Rr(i - 1, j) = c * a + sn * b;
-                    Rr(i, j) = -std::conj(sn) * a + c * b;
-                }
-                CK(launch_rot(h->st, Q[i - 1], Q[i], c, mk(sn.real(), sn.imag()), n));
-            }
-            for (int j = 0; j < m - 1; ++j)
-                for (int i = 0; i < m - 1; ++i) Rr(i, j) = Rr(i, j + 1);
+            if (m > 1) CK(launch_aa_delete(h->st, NBLK_RED, R, m, h->aa_rot, Q, n));
             m_eff = m;
         }
         const int k = m_eff - 1;
-        CK(launch_sub(h->st, dG[k], g, gold, n));
-        CK(launch_sub(h->st, fxold, fx, fxold, n));
+        // qradd!: modified Gram-Schmidt of Δf against Q_0..Q_{k-1}, one pass per column
+        CK(launch_aa_diff(h->st, NBLK_RED, dG[k], g, gold, fxold, fx, k > 0 ? Q.v[0] : nullptr, pp[0], n));
+        int cur = 0;
         for (int i = 0; i < k; ++i) {
-            const std::complex<double> rr = dot(h, Q[i], fxold, status);
-            if (status) return status;
-            Rr(i, k) = rr;
-            CK(launch_axpy(h->st, fxold, Q[i], mk(-rr.real(), -rr.imag()), n));
+            CK(launch_aa_mgs(h->st, NBLK_RED, fxold, Q.v[i], pp[cur], R + i + (size_t)m * k,
+                             i + 1 < k ? Q.v[i + 1] : nullptr, pp[cur ^ 1], n));
+            cur ^= 1;
         }
-        const double nrm = std::sqrt(std::max(0.0, dot(h, fxold, fxold, status).real()));
-        if (status) return status;
-        Rr(k, k) = nrm;
-        CK(launch_scale(h->st, Q[k], fxold, nrm > 0 ? 1.0 / nrm : 0.0, n));
-        for (int i = 0; i < m_eff; ++i) {
-            gam[i] = dot(h, Q[i], fx, status);
-            if (status) return status;
-        }
-        for (int i = m_eff - 1; i >= 0; --i) {
-            std::complex<double> v = gam[i];
-            for (int j = i + 1; j < m_eff; ++j) v -= Rr(i, j) * gam[j];
-            gam[i] = v / Rr(i, i);
-        }
-        for (int i = 0; i < m_eff; ++i) CK(launch_axpy(h->st, h->xS, dG[i], mk(-gam[i].real(), -gam[i].imag()), n));
-        CK(cudaMemcpyAsync(fxold, fx, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-        CK(cudaMemcpyAsync(gold, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        CK(launch_aa_qnew(h->st, NBLK_RED, Q.v[k], fxold, pp[cur], R + k + (size_t)m * k, n));
+        // γ = R⁻¹ Qᴴ fx ; x = g - Σ γ_i Δg_i ; fxold = fx ; gold = g
+        CK(launch_aa_gamma(h->st, NBLK_RED, Qc, m_eff, fx, pdot, R, m, h->aa_gam, n));
+        AAVecs dGc{};
+        for (int i = 0; i < m_eff; ++i) dGc.v[i] = dG[i];
+        CK(launch_aa_update(h->st, NBLK_RED, h->xS, g, dGc, h->aa_gam, m_eff, fx, fxold, gold, n));
     }
     if (it > maxiter) it = maxiter;
     // S holds Φ(x) of the last evaluation, as after the reference's solve!
@@ -1035,6 +1011,21 @@ int fdga_occupation(fdga_handle* h, double* n) {
     if (!h || !n) return FDGA_ERR_ARG;
     CK(launch_occupation(h->st, h->G, h->nGk, h->d.T, h->d.Nk, h->occ));
     CK(cudaMemcpyAsync(n, h->occ, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_susceptibility(fdga_handle* h, int channel, double* out, size_t n) {
+    if (!h || !out) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (channel < FDGA_CHI_M || channel > FDGA_CHI_S) return fail(h, FDGA_ERR_ARG, "unknown susceptibility channel");
+    const size_t NO = (size_t)h->d.N1, full = NO * h->d.Nq;
+    if (n != full && n != NO) return fail(h, FDGA_ERR_ARG, "susceptibility length must be NΩ1·Nq or NΩ1");
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (h->d.U == 0.0) return fail(h, FDGA_ERR_ARG, "susceptibility needs U != 0");
+    // tmpS holds at least NΩ1·Nq complex (the state contains the three K1 arrays)
+    CK(launch_chi(h->st, chanK(h, h->xS, CH_P, 1), chanK(h, h->xS, CH_T, 1), chanK(h, h->xS, CH_A, 1), channel,
+                  h->d.U, (int)NO, h->d.Nq, n == NO && full != NO ? 1 : 0, h->tmpS));
+    CK(cudaMemcpyAsync(out, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     return FDGA_OK;
 }

@@ -43,6 +43,7 @@ EXPORTS = {
     "fdga_get_named": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_named_len": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t)]),
     "fdga_occupation": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "fdga_susceptibility": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_event_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdga_event_elapsed_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "fdga_synchronize": (ctypes.c_int, [ctypes.c_void_p]),

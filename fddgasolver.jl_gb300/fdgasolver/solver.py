@@ -145,6 +145,22 @@ class _Solver:
         self._check(self._lib.fdga_get_named(self._h, name.encode(), out.ctypes.data, out.size))
         return out
 
+    def susceptibility(self, channel="m", local=False):
+        """Connected χ_m / χ_d / χ_s from K1 (K1_r = -U² χ_r, src/utility/load_triqs.jl:67-75,106-114).
+
+        Flat array in the reference's column-major [Ω, q] layout (length NΩ1·Nq), or the momentum
+        average χ_loc(Ω) (length NΩ1) when local."""
+        which = {"m": 0, "d": 1, "s": 2}[channel]
+        n = 2 * self.nK1 - 1 if local else self.get_len("F.a.K1")
+        out = np.empty(n, dtype=np.complex128)
+        self._check(self._lib.fdga_susceptibility(self._h, which, out.ctypes.data, n))
+        return out
+
+    def get_len(self, name):
+        n = ctypes.c_size_t()
+        self._check(self._lib.fdga_named_len(self._h, name.encode(), ctypes.byref(n)))
+        return n.value
+
     def occupation(self):
         v = ctypes.c_double()
         self._check(self._lib.fdga_occupation(self._h, ctypes.byref(v)))

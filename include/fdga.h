@@ -114,6 +114,20 @@ int fdga_named_len(const fdga_handle* h, const char* name, size_t* n);
 /* Occupation n = 1/2 + T Im Σ G / Nk of the current G (src/dyson.jl:33-41). */
 int fdga_occupation(fdga_handle* h, double* n);
 
+/* Connected two-particle susceptibility of the current state, from the K1 class of the vertex:
+ * K1_r = -U² χ_r in the physical spin channels (the reference's TRIQS import,
+ * src/utility/load_triqs.jl:67-75,106-114, and the spin algebra src/types.jl:34-66), hence
+ *   FDGA_CHI_M: χ_m(Ω,q) =  γa.K1(Ω,q) / U²
+ *   FDGA_CHI_D: χ_d(Ω,q) = (γa.K1 - 2 γt.K1)(Ω,q) / U²
+ *   FDGA_CHI_S: χ_s(Ω,q) = -2 γp.K1(Ω,q) / U²
+ * (χ_d without the disconnected 2n²/T at Ω = 0.)  n = NΩ1·Nq gives χ(Ω,q) in the reference's
+ * column-major [Ω, q] layout; n = NΩ1 gives the momentum average χ_loc(Ω) = (1/Nq) Σ_q χ(Ω,q).
+ * Computed on the device in FP64. */
+#define FDGA_CHI_M 0
+#define FDGA_CHI_D 1
+#define FDGA_CHI_S 2
+int fdga_susceptibility(fdga_handle* h, int channel, double* out, size_t n);
+
 /* Device timing on the handle's stream (CUDA events), for benchmarks. slot in [0, 8). */
 int fdga_event_record(fdga_handle* h, int slot);
 int fdga_event_elapsed_ms(fdga_handle* h, int slot_a, int slot_b, float* ms);
