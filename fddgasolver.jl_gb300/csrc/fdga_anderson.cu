@@ -228,6 +228,16 @@ cudaError_t launch_aa_update(cudaStream_t s, int nblk, cplx* x, const cplx* g, c
     k_aa_update<<<nblk, RT, 0, s>>>(x, g, dG, gam, meff, fx, fxold, gold, n);
     AA_CHECK(); return cudaSuccess;
 }
+cudaError_t launch_aa_givens(cudaStream_t s, cplx* R, int m, cplx* rot) {
+    if (m < 2 || m > AA_MAX) return cudaErrorInvalidValue;
+    k_aa_givens<<<1, 32, 0, s>>>(R, m, rot);
+    AA_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_aa_gamma_solve(cudaStream_t s, const cplx* part, int np, const cplx* R, int m, int meff, cplx* gam) {
+    if (meff < 1 || meff > AA_MAX) return cudaErrorInvalidValue;
+    k_aa_gamma<<<1, RT, 0, s>>>(part, np, R, m, meff, gam);
+    AA_CHECK(); return cudaSuccess;
+}
 cudaError_t launch_aa_delete(cudaStream_t s, int nblk, cplx* R, int m, cplx* rot, const AAVecsW& Q, size_t n) {
     if (m < 2 || m > AA_MAX) return cudaErrorInvalidValue;
     k_aa_givens<<<1, 32, 0, s>>>(R, m, rot);

@@ -45,6 +45,25 @@ __device__ __forceinline__ cplx ldg(const cplx* p) {
     double2 v = __ldg(reinterpret_cast<const double2*>(p));
     return cplx{v.x, v.y};
 }
+// FP32 complex for the mixed-precision contractions (storage stays cplx)
+struct cplxf {
+    float x, y;
+};
+__host__ __device__ __forceinline__ cplxf operator+(cplxf a, cplxf b) { return cplxf{a.x + b.x, a.y + b.y}; }
+__host__ __device__ __forceinline__ cplxf operator-(cplxf a, cplxf b) { return cplxf{a.x - b.x, a.y - b.y}; }
+__host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) {
+    return cplxf{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+__host__ __device__ __forceinline__ cplxf operator*(cplxf a, float s) { return cplxf{a.x * s, a.y * s}; }
+__host__ __device__ __forceinline__ cplxf& operator+=(cplxf& a, cplxf b) { a.x += b.x; a.y += b.y; return a; }
+// conversions between the storage type and the arithmetic type C of a templated kernel
+template <class C> __device__ __forceinline__ C to_c(cplx v);
+template <> __device__ __forceinline__ cplx to_c<cplx>(cplx v) { return v; }
+template <> __device__ __forceinline__ cplxf to_c<cplxf>(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+__device__ __forceinline__ cplx to_d(cplx v) { return v; }
+__device__ __forceinline__ cplx to_d(cplxf v) { return cplx{(double)v.x, (double)v.y}; }
+template <class C> __device__ __forceinline__ C czero() { return C{0, 0}; }
+
 // symmetry operation bits: 1 = negate, 2 = conjugate (MatsubaraFunctions Operation(sgn, con))
 __device__ __forceinline__ cplx apply_op(int op, cplx v) {
     if (op & 2) v.y = -v.y;

@@ -541,11 +541,14 @@ __device__ __forceinline__ void bse_K2_body(const VertP& F, const FLP& FL, const
 // 2x2 outputs each, K chunks of 8.  blockIdx.x = channel-slot * (Nq·NΩ3) + (P·NΩ3 + iΩ), blockIdx.y /
 // blockIdx.z = row / column tile; the three channels of one mode share a launch.
 // ---------------------------------------------------------------------------------------------
-template <int MODE, int TILE>
+// C = cplx: FP64 arithmetic (the plain path).  C = cplxf: operands converted to FP32 when staged
+// into shared memory, FP32 products and accumulation, FP64 epilogue (the mixed path).
+template <int MODE, int TILE, class C>
 __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3 args, Dims d) {
+    using R = decltype(C::x);
     constexpr int TK = 8, H = TILE / 2, NT = H * H;
-    __shared__ cplx As[TILE][TK + 1];
-    __shared__ cplx Ms[TK][TILE + 1];
+    __shared__ C As[TILE][TK + 1];
+    __shared__ C Ms[TK][TILE + 1];
     const int tid = threadIdx.x;
     const int tx = tid % H, ty = tid / H;
     const int col0 = blockIdx.z * TILE, row0 = blockIdx.y * TILE;
@@ -558,33 +561,35 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
     const int N = d.N3n;
     const size_t base = (size_t)blk * N * N;
     const double s1 = (CH == CH_A) ? 1.0 : -1.0, s2 = (CH == CH_T) ? -1.0 : 1.0;
-    cplx acc[2][2] = {{mk(0, 0), mk(0, 0)}, {mk(0, 0), mk(0, 0)}};
+    C acc[2][2] = {{czero<C>(), czero<C>()}, {czero<C>(), czero<C>()}};
     for (int k0 = 0; k0 < N; k0 += TK) {
         for (int e = tid; e < TILE * TK; e += NT) {
             const int r = e / TK, kk = e % TK;
             const int row = row0 + r, k = k0 + kk;
-            As[r][kk] = (row < N && k < N) ? ldg(a.A + base + (size_t)row * N + k) : mk(0, 0);
+            As[r][kk] = to_c<C>((row < N && k < N) ? ldg(a.A + base + (size_t)row * N + k) : mk(0, 0));
         }
         for (int e = tid; e < TK * TILE; e += NT) {
             const int kk = e / TILE, c = e % TILE;
             const int k = k0 + kk, col = col0 + c;
-            cplx v = mk(0, 0);
+            C v = czero<C>();
             if (k < N && col < N) {
                 const int o = k - d.n3n;  // ω as fermion index
                 const size_t ip = ixPi(d, P, m, o);
-                const cplx pi0 = ldg(a.Pi0 + ip);
-                const cplx f0 = ldg(a.B0 + base + (size_t)k * N + col);
+                const C pi0 = to_c<C>(ldg(a.Pi0 + ip));
+                const C f0 = to_c<C>(ldg(a.B0 + base + (size_t)k * N + col));
                 if (MODE == 0) {
                     v = pi0 * f0;
                 } else {
-                    const cplx pi = ldg(a.Pi + ip);
-                    const cplx gs = (CH == CH_P) ? ldg(a.G + base + (size_t)k * N + col) : ldg(a.G + base + (size_t)col * N + k);
-                    v = ((pi - pi0) * f0 + pi * gs) * s1;
+                    const C pi = to_c<C>(ldg(a.Pi + ip));
+                    const C gs = to_c<C>((CH == CH_P) ? ldg(a.G + base + (size_t)k * N + col)
+                                                      : ldg(a.G + base + (size_t)col * N + k));
+                    v = ((pi - pi0) * f0 + pi * gs) * (R)s1;
                     const int ot = cross(CH, m, o);
                     if (fin(ot, d.n3n)) {
                         const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                        const cplx gl = (CH == CH_T) ? 2.0 * ldg(a.FLt + il) - ldg(a.FLa + il) : ldg(a.FLc + il);
-                        v += pi * gl * s2;
+                        const C gl = (CH == CH_T) ? to_c<C>(ldg(a.FLt + il)) * (R)2 - to_c<C>(ldg(a.FLa + il))
+                                                  : to_c<C>(ldg(a.FLc + il));
+                        v += pi * gl * (R)s2;
                     }
                 }
             }
@@ -593,8 +598,8 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < TK; ++kk) {
-            const cplx a0 = As[ty][kk], a1 = As[ty + H][kk];
-            const cplx b0 = Ms[kk][tx], b1 = Ms[kk][tx + H];
+            const C a0 = As[ty][kk], a1 = As[ty + H][kk];
+            const C b0 = Ms[kk][tx], b1 = Ms[kk][tx + H];
             acc[0][0] += a0 * b0;
             acc[0][1] += a0 * b1;
             acc[1][0] += a1 * b0;
@@ -609,11 +614,12 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
             const int row = row0 + ty + H * i, col = col0 + tx + H * j;
             if (row >= N || col >= N) continue;
             const size_t io = base + (size_t)row * N + col;
+            const cplx r = to_d(acc[i][j]);
             if (MODE == 0) {
-                a.out[io] = acc[i][j] * (d.T * ((CH == CH_A) ? 1.0 : -1.0));
+                a.out[io] = r * (d.T * ((CH == CH_A) ? 1.0 : -1.0));
             } else {
                 const cplx gl = (CH == CH_T) ? 2.0 * ldg(a.FLt + io) - ldg(a.FLa + io) : ldg(a.FLc + io);
-                a.out[io] = acc[i][j] * d.T + gl;
+                a.out[io] = r * d.T + gl;
             }
         }
 }
@@ -1037,23 +1043,27 @@ cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue
     k_finalize3<<<blocks_for(n, 256), 256, 0, s>>>(f, k2_epilogue, t_recombine, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-template <int MODE, int TILE>
+template <int MODE, int TILE, class C>
 static cudaError_t launch_k3_tile(cudaStream_t s, const K3Args3& a, int nslots, const Dims& d) {
     const unsigned tiles = (unsigned)((d.N3n + TILE - 1) / TILE);
     dim3 grid((unsigned)(nslots * a.nblocks), tiles, tiles);
-    k_bse_K3_gemm<MODE, TILE><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
+    k_bse_K3_gemm<MODE, TILE, C><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
     return cudaGetLastError();
 }
-cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d) {
+template <class C>
+static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d) {
     const int N = d.N3n;
     if (mode == 0) {
-        if (N <= 16) return launch_k3_tile<0, 16>(s, a, nslots, d);
-        if (N <= 24) return launch_k3_tile<0, 24>(s, a, nslots, d);
-        return launch_k3_tile<0, 32>(s, a, nslots, d);
+        if (N <= 16) return launch_k3_tile<0, 16, C>(s, a, nslots, d);
+        if (N <= 24) return launch_k3_tile<0, 24, C>(s, a, nslots, d);
+        return launch_k3_tile<0, 32, C>(s, a, nslots, d);
     }
-    if (N <= 16) return launch_k3_tile<1, 16>(s, a, nslots, d);
-    if (N <= 24) return launch_k3_tile<1, 24>(s, a, nslots, d);
-    return launch_k3_tile<1, 32>(s, a, nslots, d);
+    if (N <= 16) return launch_k3_tile<1, 16, C>(s, a, nslots, d);
+    if (N <= 24) return launch_k3_tile<1, 24, C>(s, a, nslots, d);
+    return launch_k3_tile<1, 32, C>(s, a, nslots, d);
+}
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed) {
+    return mixed ? launch_bse_K3_t<cplxf>(s, mode, a, nslots, d) : launch_bse_K3_t<cplx>(s, mode, a, nslots, d);
 }
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d) {

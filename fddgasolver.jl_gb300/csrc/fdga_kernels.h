@@ -68,6 +68,12 @@ struct AAVecs {
 struct AAVecsW {
     cplx* v[AA_MAX];
 };
+struct AAVecs32 {
+    const cplxf* v[AA_MAX];
+};
+struct AAVecs32W {
+    cplxf* v[AA_MAX];
+};
 
 cudaError_t set_fft_twiddles();
 cudaError_t launch_bse_K1_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
@@ -91,7 +97,7 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
 cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d);
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
-cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d);
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed);
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d);
 cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,
@@ -116,6 +122,22 @@ cudaError_t launch_aa_gamma(cudaStream_t s, int nblk, const AAVecs& Q, int meff,
 cudaError_t launch_aa_update(cudaStream_t s, int nblk, cplx* x, const cplx* g, const AAVecs& dG, const cplx* gam,
                              int meff, const cplx* fx, cplx* fxold, cplx* gold, size_t n);
 cudaError_t launch_aa_delete(cudaStream_t s, int nblk, cplx* R, int m, cplx* rot, const AAVecsW& Q, size_t n);
+cudaError_t launch_aa_givens(cudaStream_t s, cplx* R, int m, cplx* rot);
+cudaError_t launch_aa_gamma_solve(cudaStream_t s, const cplx* part, int np, const cplx* R, int m, int meff, cplx* gam);
+// FP32-history Anderson (mixed-precision inner solves)
+cudaError_t launch_ma_residual(cudaStream_t s, int nblk, const cplx* y, const cplx* c, const cplx* x, cplxf* f32,
+                               cplx* g, double beta, double* pmax, size_t n);
+cudaError_t launch_ma_diff(cudaStream_t s, int nblk, cplxf* dg, const cplx* g, const cplx* gold, cplxf* df,
+                           const cplxf* f, const cplxf* Qb, cplx* part_out, size_t n);
+cudaError_t launch_ma_mgs(cudaStream_t s, int nblk, cplxf* df, const cplxf* Qa, const cplx* part_in, cplx* Rentry,
+                          const cplxf* Qb, cplx* part_out, size_t n);
+cudaError_t launch_ma_qnew(cudaStream_t s, int nblk, cplxf* Qk, const cplxf* df, const cplx* part_in, cplx* Rkk,
+                           size_t n);
+cudaError_t launch_ma_multidot(cudaStream_t s, int nblk, const AAVecs32& Q, int nv, const cplxf* f, cplx* part,
+                               size_t n);
+cudaError_t launch_ma_update(cudaStream_t s, int nblk, cplx* x, const cplx* g, const AAVecs32& dG, const cplx* gam,
+                             int meff, const cplxf* f, cplxf* fold, cplx* gold, size_t n);
+cudaError_t launch_ma_qrot(cudaStream_t s, int nblk, const AAVecs32W& Q, int m, const cplx* rot, size_t n);
 cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double U,
                        int NO, int Nq, int local, cplx* out);
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count);

@@ -11,6 +11,7 @@
 #include <deque>
 #include <functional>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fdga.h"
@@ -73,13 +74,16 @@ struct fdga_handle {
     double n0 = 0.5;
     uint32_t* perm = nullptr;  // reference flatten index -> device index
     Group gSig, gK1, gK2pp, gK2ph, gK3pp, gK3ph, gK3ppL, gK3phL;
-    Graph graphs[2][2][2];
+    Graph graphs[2][2][2][2];  // [precision][strategy][update_sigma][hartree]
+    int precision = FDGA_FP64;
     int last_launches = 0;
     cudaEvent_t ev[8] = {};
     // Anderson
     std::vector<cplx*> aa_buf;
     double* d_part = nullptr;
     cplx *aa_R = nullptr, *aa_rot = nullptr, *aa_gam = nullptr, *aa_part = nullptr;  // device QR state
+    std::vector<cplx*> ma_buf64;   // mixed solver: defect, g, g_old
+    std::vector<cplxf*> ma_buf32;  // mixed solver: f, Δf, Q, Δg (FP32 history)
     std::vector<void*> allocs;
 };
 
@@ -294,14 +298,14 @@ void compute_all_groups(const Dims& d, std::vector<HostGroup>& out) {
     const ShapeDesc sS{AK_G, 0, d.nG, d.Nk}, s1{AK_K1, d.n1, 0, d.Nq}, s2{AK_K2, d.n2O, d.n2n, d.Nq},
         s3{AK_K3, d.n3O, d.n3n, d.Nq};
     out.assign(8, HostGroup());
-    compute_group(d, out[0], sS, AK_G, sig);
-    compute_group(d, out[1], s1, AK_K1, k1);
-    compute_group(d, out[2], s2, AK_K2, k2pp);
-    compute_group(d, out[3], s2, AK_K2, k2ph);
-    compute_group(d, out[4], s3, AK_K3, k3pp);
-    compute_group(d, out[5], s3, AK_K3, k3ph);
-    compute_group(d, out[6], s3, AK_K3, k3ppL);
-    compute_group(d, out[7], s3, AK_K3, k3phL);
+    // the eight class constructions are independent: one host thread each
+    const ShapeDesc* shp[8] = {&sS, &s1, &s2, &s2, &s3, &s3, &s3, &s3};
+    const int kinds[8] = {AK_G, AK_K1, AK_K2, AK_K2, AK_K3, AK_K3, AK_K3, AK_K3};
+    const std::vector<SymF>* sy[8] = {&sig, &k1, &k2pp, &k2ph, &k3pp, &k3ph, &k3ppL, &k3phL};
+    std::vector<std::thread> th;
+    for (int i = 0; i < 8; ++i)
+        th.emplace_back([&, i]() { compute_group(d, out[i], *shp[i], kinds[i], *sy[i]); });
+    for (auto& t : th) t.join();
 }
 
 int upload_group(fdga_handle* h, Group& g, const HostGroup& hg) {
@@ -453,7 +457,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             }
             a3.blocks = h->d_k3blocks;
             a3.nblocks = h->nk3blocks;
-            LC(launch_bse_K3(s, 0, a3, 3, d));
+            LC(launch_bse_K3(s, 0, a3, 3, d, h->precision == FDGA_MIXED));
             cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
             const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
             LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
@@ -492,7 +496,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         }
         a3.blocks = h->d_k3blocks;
         a3.nblocks = h->nk3blocks;
-        LC(launch_bse_K3(s, 1, a3, 3, d));
+        LC(launch_bse_K3(s, 1, a3, 3, d, h->precision == FDGA_MIXED));
         cplx* out[3] = {chanK(h, h->yS, CH_P, 3), chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3)};
         const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
         LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
@@ -541,10 +545,11 @@ int compute_C0(fdga_handle* h) {
 }
 
 void drop_graphs(fdga_handle* h) {
-    for (auto& a : h->graphs)
-        for (auto& b : a)
-            for (auto& g : b)
-                if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    for (auto& p : h->graphs)
+        for (auto& a : p)
+            for (auto& b : a)
+                for (auto& g : b)
+                    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
 }
 
 int run_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
@@ -554,7 +559,7 @@ int run_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree)
         int r = compute_C0(h);
         if (r) return r;
     }
-    Graph& g = h->graphs[strategy][update_sigma][hartree];
+    Graph& g = h->graphs[h->precision][strategy][update_sigma][hartree];
     if (!g.exec) {
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
@@ -652,10 +657,14 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     if (c->L < 1 || c->mPi_factor < 1 || !(c->T > 0)) return bad("L, mPi_factor and T must be positive");
     if (c->local && c->L != 1) return bad("the local solver has L = 1");
     if (c->LG != c->L) { g_create_error = "L_G != L is not supported by this build"; return FDGA_ERR_UNSUPPORTED; }
-    if (c->precision != FDGA_FP64) { g_create_error = "only FDGA_FP64 is provided"; return FDGA_ERR_UNSUPPORTED; }
+    if (c->precision != FDGA_FP64 && c->precision != FDGA_MIXED) {
+        g_create_error = "precision must be FDGA_FP64 or FDGA_MIXED";
+        return FDGA_ERR_ARG;
+    }
     if (c->nR[0] < 1 || c->nR[1] < 1) return bad("RefVertex box must be >= 1");
     fdga_handle* h = new fdga_handle();
     h->cfg = *c;
+    h->precision = c->precision;
     make_dims(c, h->d);
     Dims& d = h->d;
     h->nGk = (size_t)d.NG * d.Nk;
@@ -698,6 +707,9 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     ALC(h->occ, 1);
     ALC(h->perm, h->nstate);
     ALC(h->d_part, NBLK_RED);
+    // the zero-fills of dalloc are queued on the (non-blocking) solver stream: finish them before
+    // any upload, and keep the uploads on the same stream
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) return fin_err(fail(h, FDGA_ERR_CUDA, "create sync"));
     {
         std::vector<cplx> tm(d.L), tp(d.L);
         for (int j = 0; j < d.L; ++j) {
@@ -705,8 +717,8 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
             tm[j] = mk(std::cos(a), -std::sin(a));
             tp[j] = mk(std::cos(a), std::sin(a));
         }
-        if (cudaMemcpy(h->twm, tm.data(), d.L * sizeof(cplx), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(h->twp, tp.data(), d.L * sizeof(cplx), cudaMemcpyHostToDevice) != cudaSuccess)
+        if (cudaMemcpyAsync(h->twm, tm.data(), d.L * sizeof(cplx), cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+            cudaMemcpyAsync(h->twp, tp.data(), d.L * sizeof(cplx), cudaMemcpyHostToDevice, h->st) != cudaSuccess)
             return fin_err(fail(h, FDGA_ERR_CUDA, "twiddle upload"));
         // flatten permutation
         std::vector<uint32_t> perm(h->nstate);
@@ -718,7 +730,9 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
             for (size_t i = 0; i < h->n3; ++i) perm[j++] = (uint32_t)(off + h->n1 + h->n2 + dev_index(h->d, AK_K3, i));
         }
         for (size_t i = 0; i < h->nGk; ++i) perm[j++] = (uint32_t)(3 * h->nchan + i);
-        if (cudaMemcpy(h->perm, perm.data(), h->nstate * sizeof(uint32_t), cudaMemcpyHostToDevice) != cudaSuccess)
+        if (cudaMemcpyAsync(h->perm, perm.data(), h->nstate * sizeof(uint32_t), cudaMemcpyHostToDevice, h->st) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(h->st) != cudaSuccess)
             return fin_err(fail(h, FDGA_ERR_CUDA, "permutation upload"));
     }
 #undef ALC
@@ -962,6 +976,155 @@ int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double bet
     return FDGA_OK;
 }
 
+int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int* iters, double* res,
+                     double* trace, int* evals) {
+    if (!h) return FDGA_ERR_ARG;
+    if (maxiter < 2 || mem < 0 || !(tol > 0)) return fail(h, FDGA_ERR_ARG, "invalid solver parameters");
+    const size_t n = h->nstate;
+    const int m = (int)std::min<size_t>((size_t)mem, n);
+    if (m > AA_MAX) return fail(h, FDGA_ERR_ARG, "Anderson memory exceeds " + std::to_string(AA_MAX));
+    // FP64: c (defect Φ64 - Φ32 at the outer iterate), g, gold ; FP32: f, Δf, Q[m], Δg[m]
+    while (h->ma_buf64.size() < 3) {
+        cplx* p = nullptr;
+        int r = dalloc(h, &p, n);
+        if (r) return r;
+        h->ma_buf64.push_back(p);
+    }
+    while (h->ma_buf32.size() < 2 + 2 * (size_t)m) {
+        cplxf* p = nullptr;
+        int r = dalloc(h, &p, n);
+        if (r) return r;
+        h->ma_buf32.push_back(p);
+    }
+    if (!h->aa_R) {
+        int r = dalloc(h, &h->aa_R, (size_t)AA_MAX * AA_MAX);
+        if (!r) r = dalloc(h, &h->aa_rot, 2 * (size_t)AA_MAX);
+        if (!r) r = dalloc(h, &h->aa_gam, (size_t)AA_MAX);
+        if (!r) r = dalloc(h, &h->aa_part, (size_t)(AA_MAX + 2) * NBLK_RED);
+        if (r) return r;
+    }
+    cplx *c = h->ma_buf64[0], *g = h->ma_buf64[1], *gold = h->ma_buf64[2];
+    cplxf *f = h->ma_buf32[0], *df = h->ma_buf32[1];
+    std::vector<cplxf*> dG(h->ma_buf32.begin() + 2, h->ma_buf32.begin() + 2 + m);
+    AAVecs32W Q{};
+    AAVecs32 Qc{};
+    for (int i = 0; i < m; ++i) Qc.v[i] = Q.v[i] = h->ma_buf32[2 + m + i];
+    cplx* R = h->aa_R;
+    cplx* pp[2] = {h->aa_part, h->aa_part + NBLK_RED};
+    cplx* pdot = h->aa_part + 2 * NBLK_RED;
+    const int prec0 = h->precision;
+    struct Restore {  // the handle's precision is restored on every exit
+        fdga_handle* h; int p;
+        ~Restore() { h->precision = p; }
+    } restore{h, prec0};
+    int n64 = 0, nmix = 0, nouter = 0, status = 0;
+    double resid = 0.0;
+    bool converged = false;
+    auto budget_left = [&]() { return n64 + nmix + 2 <= maxiter; };
+    // Anderson with the FP32 history on z -> Φ(z) (+ c), Φ in the handle's current precision, from
+    // z = xS with yS = Φ(xS) already evaluated.  Stops when the residual is below tin, after
+    // `stagnation` iterations without a new minimum (0: never), or at the evaluation budget.
+    // fp64_outer: the residuals are FP64 ones (no c): they are traced and tested against tol.
+    auto inner = [&](const cplx* cdef, double tin, int stagnation, bool fp64_outer) -> int {
+        if (m > 0) CK(cudaMemsetAsync(R, 0, (size_t)m * m * sizeof(cplx), h->st));
+        int m_eff = 0, since = 0;
+        double best = INFINITY;
+        for (int it = 1;; ++it) {
+            CK(launch_ma_residual(h->st, NBLK_RED, h->yS, cdef, h->xS, f, g, beta, h->d_part, n));
+            const double rin = reduce_max(h, NBLK_RED, status);
+            if (status) return status;
+            if (!std::isfinite(rin)) return fail(h, FDGA_ERR_NONFINITE, "non-finite residual in solve_mixed");
+            if (fp64_outer) {
+                resid = rin;
+                if (trace) trace[nouter] = rin;
+                ++nouter;
+                if (rin < tol) { converged = true; return FDGA_OK; }
+            }
+            if (rin < tin || !budget_left()) return FDGA_OK;
+            if (rin < 0.999 * best) { best = rin; since = 0; }
+            else if (stagnation > 0 && ++since >= stagnation) return FDGA_OK;
+            if (m == 0 || it == 1) {
+                CK(cudaMemcpyAsync(h->xS, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+                if (m > 0) {
+                    CK(cudaMemcpyAsync(df, f, n * sizeof(cplxf), cudaMemcpyDeviceToDevice, h->st));
+                    CK(cudaMemcpyAsync(gold, g, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+                }
+            } else {
+                m_eff += 1;
+                if (m_eff > m) {
+                    std::rotate(dG.begin(), dG.begin() + 1, dG.end());
+                    if (m > 1) {
+                        CK(launch_aa_givens(h->st, R, m, h->aa_rot));
+                        CK(launch_ma_qrot(h->st, NBLK_RED, Q, m, h->aa_rot, n));
+                    }
+                    m_eff = m;
+                }
+                const int k = m_eff - 1;
+                CK(launch_ma_diff(h->st, NBLK_RED, dG[k], g, gold, df, f, k > 0 ? Q.v[0] : nullptr, pp[0], n));
+                int cur = 0;
+                for (int i = 0; i < k; ++i) {
+                    CK(launch_ma_mgs(h->st, NBLK_RED, df, Q.v[i], pp[cur], R + i + (size_t)m * k,
+                                     i + 1 < k ? Q.v[i + 1] : nullptr, pp[cur ^ 1], n));
+                    cur ^= 1;
+                }
+                CK(launch_ma_qnew(h->st, NBLK_RED, Q.v[k], df, pp[cur], R + k + (size_t)m * k, n));
+                CK(launch_ma_multidot(h->st, NBLK_RED, Qc, m_eff, f, pdot, n));
+                CK(launch_aa_gamma_solve(h->st, pdot, NBLK_RED, R, m, m_eff, h->aa_gam));
+                AAVecs32 dGc{};
+                for (int i = 0; i < m_eff; ++i) dGc.v[i] = dG[i];
+                CK(launch_ma_update(h->st, NBLK_RED, h->xS, g, dGc, h->aa_gam, m_eff, f, df, gold, n));
+            }
+            int r = run_iteration(h, strategy, true, true);
+            if (r) return r;
+            if (h->precision == FDGA_FP64) ++n64; else ++nmix;
+        }
+    };
+    // Phase 1: iterative refinement.  Inner solves on the mixed map stop at 1e-3 of the outer FP64
+    // residual, or when they stagnate at the mixed map's rounding floor.  Phase 2 starts when an
+    // outer step reduced the FP64 residual by less than 10x (the floor is reached): the same
+    // Anderson iteration then runs on the FP64 map to tol.
+    const double eta = 1e-3;
+    for (;;) {
+        h->precision = FDGA_FP64;
+        int r = run_iteration(h, strategy, true, true);
+        if (r) return r;
+        ++n64;
+        CK(launch_residual(h->st, h->yS, h->xS, c, nullptr, 0.0, h->d_part, NBLK_RED, n));
+        const double rk = reduce_max(h, NBLK_RED, status);
+        if (status) return status;
+        if (!std::isfinite(rk)) return fail(h, FDGA_ERR_NONFINITE, "non-finite residual in solve_mixed");
+        if (trace) trace[nouter] = rk;
+        ++nouter;
+        const double prev = nouter > 1 ? resid : INFINITY;
+        resid = rk;
+        if (rk < tol) { converged = true; break; }
+        if (!budget_left()) break;
+        if (!(rk < 0.1 * prev)) {
+            // phase 2 from this iterate (yS = Φ64(x)); its first residual is this outer one
+            --nouter;
+            r = inner(nullptr, 0.0, 0, true);
+            if (r) return r;
+            break;
+        }
+        // defect c = Φ64(x) - Φ32(x): the inner equation z = Φ32(z) + c has the residual Φ64(x) - x at z = x
+        CK(cudaMemcpyAsync(c, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        h->precision = FDGA_MIXED;
+        r = run_iteration(h, strategy, true, true);
+        if (r) return r;
+        ++nmix;
+        CK(launch_sub(h->st, c, c, h->yS, n));
+        r = inner(c, std::max(eta * rk, 0.25 * tol), 8, false);
+        if (r) return r;
+    }
+    // S holds Φ64(x) of the last outer evaluation, as after the reference's solve!
+    CK(cudaMemcpyAsync(h->xS, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (iters) *iters = converged ? nouter : -nouter;
+    if (res) *res = resid;
+    if (evals) { evals[0] = n64; evals[1] = nmix; }
+    return FDGA_OK;
+}
+
 int fdga_named_len(const fdga_handle* h, const char* name, size_t* n) {
     if (!h || !name || !n) return FDGA_ERR_ARG;
     cplx* p;
@@ -993,7 +1156,9 @@ int fdga_get_named(fdga_handle* h, const char* name, double* out, size_t n) {
         if (e == cudaSuccess) e = launch_g_realspace(h->st, ref ? h->G0 : h->G, h->GR, h->twm, df);
         if (e == cudaSuccess) e = launch_bubble(h->st, ref ? h->G0 : h->G, h->GR, tpp, tph, h->twp, df);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-        if (e == cudaSuccess) e = cudaMemcpy(dev.data(), pp ? tpp : tph, len * sizeof(cplx), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dev.data(), pp ? tpp : tph, len * sizeof(cplx), cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
         cudaFree(tpp);
         if (tph) cudaFree(tph);
         if (e != cudaSuccess) return cuda_fail(h, e, "full bubble for inspection");
@@ -1001,7 +1166,8 @@ int fdga_get_named(fdga_handle* h, const char* name, double* out, size_t n) {
         for (size_t j = 0; j < len; ++j) o[j] = dev[dev_index(h->d, kind, j)];
         return FDGA_OK;
     }
-    CK(cudaMemcpy(dev.data(), p, len * sizeof(cplx), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(dev.data(), p, len * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     cplx* o = reinterpret_cast<cplx*>(out);
     for (size_t j = 0; j < len; ++j) o[j] = dev[dev_index(h->d, kind, j)];
     return FDGA_OK;
@@ -1012,6 +1178,13 @@ int fdga_occupation(fdga_handle* h, double* n) {
     CK(launch_occupation(h->st, h->G, h->nGk, h->d.T, h->d.Nk, h->occ));
     CK(cudaMemcpyAsync(n, h->occ, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_set_precision(fdga_handle* h, int precision) {
+    if (!h) return FDGA_ERR_ARG;
+    if (precision != FDGA_FP64 && precision != FDGA_MIXED) return fail(h, FDGA_ERR_ARG, "unknown precision");
+    h->precision = precision;
     return FDGA_OK;
 }
 

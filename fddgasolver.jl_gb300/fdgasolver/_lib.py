@@ -36,10 +36,14 @@ EXPORTS = {
     "fdga_flatten": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_unflatten": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_iterate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "fdga_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdga_residual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
                                   ctypes.c_void_p]),
+    "fdga_solve_mixed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                        ctypes.c_void_p, ctypes.c_void_p]),
     "fdga_get_named": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_named_len": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t)]),
     "fdga_occupation": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
@@ -59,6 +63,7 @@ EXPORTS = {
 }
 
 FDGA_FDPA, FDGA_SCPA = 0, 1
+FDGA_FP64, FDGA_MIXED = 0, 1
 IN_GBARE, IN_G0, IN_SIGMA0, IN_FP_P, IN_FP_X, IN_FT_P, IN_FT_X = range(7)
 
 _LIB = None

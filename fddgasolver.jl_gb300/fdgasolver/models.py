@@ -2,6 +2,7 @@
 
 siam_bare_Green     src/models/siam.jl:9-29
 hubbard_bare_Green  src/models/hubbard.jl:8-44   (k index x + L*y, k = 2π(x, y)/L)
+compute_hubbard_chemical_potential  src/dyson.jl:45-58
 """
 import numpy as np
 
@@ -41,3 +42,19 @@ def compute_occupation(G: np.ndarray, T: float) -> float:
     G = np.asarray(G)
     nk = 1 if G.ndim == 1 else G.shape[1]
     return 0.5 + np.imag(G.sum()) * T / nk
+
+
+def compute_hubbard_chemical_potential(occ_target: float, Sigma: np.ndarray, T: float, nG: int, L: int, *, t1: float,
+                                       t2: float = 0.0, t3: float = 0.0) -> float:
+    """μ with compute_occupation(Dyson(Σ, Gbare(μ))) = occ_target, bracketed in [-4|t1|, 4|t1|]
+    (src/dyson.jl:45-58; the reference uses Roots.find_zero on the same bracket, here Brent's
+    method to full double precision).  Σ and G are stored as i*Σ, i*G like the solver inputs, so
+    Dyson reads G = 1/(1/Gbare + Σ) (src/dyson.jl:5-31)."""
+    from scipy.optimize import brentq
+
+    def occ(mu):
+        Gb = hubbard_bare_Green(T, nG, L, mu=mu, t1=t1, t2=t2, t3=t3)
+        G = 1.0 / (1.0 / Gb + Sigma)
+        return compute_occupation(G, T) - occ_target
+
+    return brentq(occ, -4 * abs(t1), 4 * abs(t1), xtol=1e-15, rtol=4 * np.finfo(float).eps, maxiter=500)

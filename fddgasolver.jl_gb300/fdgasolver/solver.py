@@ -138,12 +138,29 @@ class _Solver:
         n = abs(it.value)
         return {"converged": it.value > 0, "iterations": n, "residual": res.value, "trace": trace[:n]}
 
+    def solve_mixed(self, strategy="fdPA", maxiter=300, tol=1e-8, delta=0.85, mem=8):
+        """The FP64 fixed point by iterative refinement around mixed-precision inner Anderson solves."""
+        trace = np.zeros(maxiter, dtype=np.float64)
+        it = ctypes.c_int()
+        res = ctypes.c_double()
+        ev = np.zeros(2, dtype=np.int32)
+        self._check(self._lib.fdga_solve_mixed(self._h, STRATEGIES[strategy], int(maxiter), float(tol), float(delta),
+                                               int(mem), ctypes.byref(it), ctypes.byref(res), trace.ctypes.data,
+                                               ev.ctypes.data))
+        n = abs(it.value)
+        return {"converged": it.value > 0, "outer": n, "residual": res.value, "trace": trace[:n],
+                "evals_fp64": int(ev[0]), "evals_mixed": int(ev[1])}
+
     def get(self, name):
         n = ctypes.c_size_t()
         self._check(self._lib.fdga_named_len(self._h, name.encode(), ctypes.byref(n)))
         out = np.empty(n.value, dtype=np.complex128)
         self._check(self._lib.fdga_get_named(self._h, name.encode(), out.ctypes.data, out.size))
         return out
+
+    def set_precision(self, precision):
+        """'fp64' (plain path) or 'mixed' (K3 contractions in FP32) for later iterate/residual calls."""
+        self._check(self._lib.fdga_set_precision(self._h, {"fp64": 0, "mixed": 1}[precision]))
 
     def susceptibility(self, channel="m", local=False):
         """Connected χ_m / χ_d / χ_s from K1 (K1_r = -U² χ_r, src/utility/load_triqs.jl:67-75,106-114).

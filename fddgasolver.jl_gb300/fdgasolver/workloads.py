@@ -9,6 +9,10 @@ config1: SIAM, local fdPA, β=10, U=1, flat band Δ(iν) = -iΓ sign ν, Γ = 0.
 config2: Hubbard 8x8, nonlocal fdPA, t=1, t'=0, μ=0, U=2, β=5, nK1=32, nK2=(16,16), nK3=(8,12),
          nG=32, mΠν_factor=32; F0 = RefVertex(U) with corrections on the K3 box drawn as
          complex Gaussian noise σ = 0.05 U, symmetrised ν<->ν', scaled 1/sqrt((1+|ν|)(1+|ν'|)).
+config3: Hubbard 16x16, nonlocal fdPA, t=1, t'=-0.2, U=3, β=10, nK1=80, nK2=(40,40), nK3=(20,40), nG=80,
+         mΠν_factor=32; μ tuned once on Gbare (Σ = 0) to density n = 0.9 (per-spin occupation 0.45).
+config5: Hubbard 24x24, nonlocal fdPA, t=1, t'=0, μ=0, U=2.5, β=8, nK1=96, nK2=(48,48), nK3=(24,48), nG=96,
+         mΠν_factor=32.
 """
 import numpy as np
 
@@ -49,7 +53,13 @@ def make_inputs(cfg):
     if cfg["kind"] == "siam":
         Gb = siam_bare_Green(T, cfg["nG"], Delta=cfg["Delta"], e=cfg["e"], D=cfg["D"])
     else:
-        Gb = hubbard_bare_Green(T, cfg["nG"], cfg["L"], mu=cfg["mu"], t1=cfg["t1"], t2=cfg.get("t2", 0.0))
+        mu = cfg["mu"]
+        if mu is None:  # tuned once on Gbare (Σ = 0) to the target filling
+            from .models import compute_hubbard_chemical_potential
+            # compute_occupation is per spin (1/2 at half filling): density n <-> occupation n/2
+            mu = compute_hubbard_chemical_potential(cfg["filling"] / 2, np.zeros((2 * cfg["nG"], cfg["L"] ** 2), complex),
+                                                    T, cfg["nG"], cfg["L"], t1=cfg["t1"], t2=cfg.get("t2", 0.0))
+        Gb = hubbard_bare_Green(T, cfg["nG"], cfg["L"], mu=mu, t1=cfg["t1"], t2=cfg.get("t2", 0.0))
     G0 = cfg.get("G0")
     S0 = cfg.get("Sigma0")
     G0 = np.zeros_like(Gb) if G0 is None else G0

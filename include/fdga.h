@@ -31,7 +31,12 @@ enum {
 };
 
 enum { FDGA_FDPA = 0, FDGA_SCPA = 1 };          /* iterate_solver! strategy (src/solve.jl:10) */
-enum { FDGA_FP64 = 0 };                          /* arithmetic of the plain path */
+/* Arithmetic of the iteration map.  FDGA_FP64: every kernel in FP64 (the plain path, parity
+ * with the reference).  FDGA_MIXED: the K3 Bethe-Salpeter contractions (the bulk of the work at
+ * large boxes) in FP32 arithmetic with FP32 accumulation; storage, Dyson, bubbles, SDE, residual
+ * and mixing stay FP64.  FDGA_MIXED maps are used inside fdga_solve_mixed, whose FP64 residual
+ * (iterative refinement) recovers the FP64 fixed point. */
+enum { FDGA_FP64 = 0, FDGA_MIXED = 1 };
 
 /* Solver dimensions: the reference constructor arguments
  * ParquetSolver(nK1, nK2, nK3, Gbare, G0, Σ0, F0; mΠν_factor)         (src/ParquetSolver.jl:277-352)
@@ -49,7 +54,7 @@ typedef struct fdga_config {
     double T;            /* temperature */
     double U;            /* bare interaction of the RefVertex */
     int32_t nR[2];       /* box of the RefVertex corrections Fp_p .. Ft_x; (1,1) = bare U */
-    int32_t precision;   /* FDGA_FP64 */
+    int32_t precision;   /* FDGA_FP64 or FDGA_MIXED: initial arithmetic of fdga_iterate / fdga_residual */
 } fdga_config;
 
 /* Inputs uploaded with fdga_set_input (reference column-major layout). */
@@ -94,6 +99,9 @@ int fdga_unflatten(fdga_handle* h, const double* x, size_t n);
  * iteration on the device state, replayed as one CUDA graph. */
 int fdga_iterate(fdga_handle* h, int strategy, int update_sigma, int compute_hartree);
 
+/* Arithmetic of subsequent fdga_iterate / fdga_residual / fdga_solve calls on this handle. */
+int fdga_set_precision(fdga_handle* h, int precision);
+
 /* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.
  * x and R are host arrays of fdga_state_len elements. */
 int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size_t n);
@@ -104,6 +112,21 @@ int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size
  * *res and, if trace != NULL, max|R| per iteration (maxiter doubles). */
 int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem,
                int* iters, double* res, double* trace);
+
+/* Mixed-precision solve of the same fixed point as fdga_solve, by iterative refinement (defect
+ * correction).  Phase 1: at each outer iterate x the FP64 residual Φ64(x) - x is formed; the inner
+ * equation z = Φ_mixed(z) + (Φ64(x) - Φ_mixed(x)) is solved from z = x by Anderson acceleration
+ * (m = mem, beta) with an FP32 history until its residual falls below max(1e-3 max|Φ64(x) - x|,
+ * tol/4) or stops improving (the rounding floor of the mixed map), and z becomes the next outer
+ * iterate.  Phase 2 starts when an outer step reduced the FP64 residual by less than 10x: the
+ * same FP32-history Anderson iteration then runs on the FP64 map until max|R| < tol.  The fixed
+ * point is the FP64 one; convergence is declared on FP64 residuals only.  maxiter bounds the map
+ * evaluations of both precisions together.  *iters = number of FP64 residuals formed (negative
+ * when not converged); *res = the last one; trace (maxiter doubles, may be NULL) = the FP64
+ * residuals in order; evals[0] = FP64 map evaluations, evals[1] = mixed map evaluations.  On
+ * return S holds Φ64 of the last iterate. */
+int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem,
+                     int* iters, double* res, double* trace, int* evals);
 
 /* Named device arrays in the reference layout, for inspection and tests:
  * "G", "Sigma", "Gbare", "G0", "Sigma0", "Pipp", "Piph", "Pi0pp", "Pi0ph", "Lpp", "Lph",

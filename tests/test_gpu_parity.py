@@ -22,6 +22,13 @@ ODD_NL = dict(kind="hubbard", T=0.4, U=1.5, mu=0.1, t1=1.0, L=3, nG=6, nK1=6, nK
               refvertex_noise=0.05, seed=3)
 
 
+# the lattice sizes of the precision (16x16, radix-2 FFT path) and differentiation (24x24, DFT path)
+# configurations, with small frequency boxes so that the oracle finishes in seconds
+NL16 = dict(kind="hubbard", T=0.5, U=3.0, mu=-0.3, t1=1.0, t2=-0.2, L=16, nG=4, nK1=4, nK2=(2, 2), nK3=(2, 2),
+            mPi_factor=3)
+NL24 = dict(kind="hubbard", T=0.5, U=2.5, mu=0.0, t1=1.0, L=24, nG=4, nK1=4, nK2=(2, 2), nK3=(2, 2), mPi_factor=3)
+
+
 def _state(S_or, rng, scale=0.05):
     x = S_or.flatten()
     return x + scale * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))
@@ -40,6 +47,20 @@ def test_map_parity(cfg, sym, strategy):
         R_gpu = gpu.fixed_point(x, strategy)
         y_orc = R_orc + x
         y_gpu = R_gpu + x
+        assert blockwise_rel_err(cfg, y_gpu, y_orc) < TOL
+        x = y_orc + 0.01 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))
+
+
+@pytest.mark.parametrize("cfg", [NL16, NL24], ids=["nl16", "nl24"])
+def test_map_parity_large_lattice(cfg):
+    """One map application from the PA start and one from a perturbed state, init_sym_grp! groups."""
+    rng = np.random.default_rng(2)
+    orc = make_oracle(cfg, True)
+    gpu = make_gpu(cfg, True)
+    x = orc.flatten()
+    for _ in range(2):
+        y_orc = orc.residual(x, "fdPA") + x
+        y_gpu = gpu.fixed_point(x, "fdPA") + x
         assert blockwise_rel_err(cfg, y_gpu, y_orc) < TOL
         x = y_orc + 0.01 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))
 
