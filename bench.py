@@ -2,7 +2,8 @@
 """Benchmark of the parquet-iteration hot path (one JSON line on stdout).
 
 Metric: seconds per parquet iteration (one iterate_solver!, fdPA, update_Σ) on the plain FP64 GPU
-path, with time-to-converge at residual 1e-8 reported beside it.  Workload: the Hubbard 8x8
+path, with time-to-converge at max|R| < 1e-8 reported beside it for the plain FP64 solver and the
+mixed-precision iterative-refinement solver (and the mixed map's error per result).  Workload: the Hubbard 8x8
 nonlocal fdPA configuration (t=1, t'=0, μ=0, U=2, β=5, nK1=32, nK2=(16,16), nK3=(8,12), nG=32,
 mΠν_factor=32, seeded synthetic RefVertex), init_sym_grp! symmetry groups.
 
@@ -28,6 +29,15 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "s per parquet iteration (plain FP64, fdPA, Hubbard 8x8 config)"
+WORKLOADS = {
+    "config1": "SIAM local fdPA: beta=10 U=1 Gamma=0.5 flat band nK1=64 nK2=(32,32) nK3=(16,16) nG=64 mPi=6, init_sym_grp",
+    "config2": "Hubbard 8x8 NL fdPA: t=1 t'=0 mu=0 U=2 beta=5 nK1=32 nK2=(16,16) nK3=(8,12) nG=32 mPi=32, "
+               "synthetic RefVertex, init_sym_grp",
+    "config3": "Hubbard 16x16 NL fdPA: t=1 t'=-0.2 n=0.9 U=3 beta=10 nK1=80 nK2=(40,40) nK3=(20,40) nG=80 mPi=32, "
+               "init_sym_grp",
+    "config5": "Hubbard 24x24 NL fdPA: t=1 t'=0 mu=0 U=2.5 beta=8 nK1=96 nK2=(48,48) nK3=(24,48) nG=96 mPi=32, "
+               "init_sym_grp",
+}
 UNIT = "s/iteration"
 
 
@@ -39,6 +49,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge leg")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the oracle timing (for the large configurations, where one oracle iteration takes hours)")
     return ap.parse_args()
 
 
@@ -146,26 +158,75 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
 
 
-def stage_work(cfg, stage, S):
-    """Algorithmic bytes moved by one launch-group of a stage (the roofline numerator)."""
-    L = cfg["L"]
-    Nq = L * L
-    NPO = 2 * cfg["nK1"] - 1
-    NPn = 2 * cfg["nK1"] * cfg["mPi_factor"]
-    N2 = (2 * cfg["nK2"][0] - 1) * 2 * cfg["nK2"][1] * Nq
-    N3 = (2 * cfg["nK3"][0] - 1) * (2 * cfg["nK3"][1]) ** 2 * Nq
-    B = 16
-    if stage == "dyson_bubble":
-        return 2 * NPO * NPn * Nq * B  # write Πpp, Πph
-    if stage in ("bse_K2", "sde"):
-        # each representative row streams Π and Π0 (K2) or Π (L) over the bubble mesh: at least
-        # every (P, Ω) row of both bubbles once, plus the K2-sized outputs
-        return 2 * NPO * NPn * Nq * B * (1 if stage == "sde" else 2) // 2 + 3 * N2 * B
-    if stage == "k3_cache":
-        return 10 * N3 * B + 3 * N3 * B
-    if stage in ("bse_K3", "bse_L_K3"):
-        return 3 * (4 * N3 * B)
-    return 3 * N2 * B
+def flatten_blocks(cfg):
+    """(name, start, stop) of the flatten(S) blocks: γp(K1,K2,K3), γt, γa, Σ."""
+    local = cfg["kind"] == "siam"
+    Nq = 1 if local else cfg["L"] ** 2
+    n1 = (2 * cfg["nK1"] - 1) * Nq
+    n2 = (2 * cfg["nK2"][0] - 1) * 2 * cfg["nK2"][1] * Nq
+    n3 = (2 * cfg["nK3"][0] - 1) * (2 * cfg["nK3"][1]) ** 2 * Nq
+    out, o = [], 0
+    for ch in "pta":
+        for nm, n in (("K1", n1), ("K2", n2), ("K3", n3)):
+            out.append((f"{ch}.{nm}", o, o + n))
+            o += n
+    out.append(("Sigma", o, o + 2 * cfg["nG"] * Nq))
+    return out
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch of a kernel, from the committed ncu summary under profiles/ (or None)."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_launch"):
+                return int(line.split("=")[1].split()[0].replace(",", ""))
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
+def k3_gemm_roofline(S, stages, cfg_name):
+    """Roofline of the fused K3 BSE GEMM (k_bse_K3_gemm, MODE 1): one complex Nν3 x Nν3 x Nν3 product
+    per (channel, representative (P, Ω) block); complex MAC = 8 real flops; FP64 pipe bound."""
+    nb, N = S.query("k3_blocks"), S.query("k3_block_dim")
+    ms = stages["bse_K3_gemm"]
+    flops = 3 * nb * 8 * N ** 3
+    byts = 16 * nb * N * N * 16  # A, B0, Γ, FL (two for t) and the output, per channel: 16 N² complex
+    fp64_peak = S.query("fp64_gflops") / 1e3
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved = flops / (ms * 1e-3) / 1e12
+    traffic = profile_traffic(f"k_bse_K3_gemm_{cfg_name}.md")
+    tile = 16 if N <= 16 else (24 if N <= 24 else 32)
+    return {"bound": "fp64", "kernel": f"k_bse_K3_gemm<1,{tile},cplx> (fused K3 BSE, FP64)", "achieved": achieved,
+            "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+            "peak_source": "measured: the library's FP64 FMA calibration kernel on this GPU (fdga_query fp64_gflops)",
+            "traffic": traffic, "algorithmic_bytes": byts, "hbm_achieved_gbs": byts / (ms * 1e-3) / 1e9,
+            "hbm_peak_gbs": hbm, "hbm_frac": byts / (ms * 1e-3) / 1e9 / hbm,
+            "hbm_peak_source": "fallback" if peaks.get("fallback") else "measured",
+            "launch_ms": ms, "flops_per_launch": flops, "share_of_iteration": ms / sum(stages.values()),
+            "stage_ms": {k: round(v, 4) for k, v in stages.items()}}
+
+
+def precision_report(cfg, S, x):
+    """Mixed map vs FP64 map at the same state: max relative error per flatten block and of χ."""
+    import numpy as np
+    y64 = S.fixed_point(x) + x
+    U = cfg["U"]
+    S.set_precision("mixed")
+    y32 = S.fixed_point(x) + x
+    S.set_precision("fp64")
+    rep = {}
+    for name, a, b in flatten_blocks(cfg):
+        ref = np.abs(y64[a:b]).max()
+        rep[name] = float(np.abs(y32[a:b] - y64[a:b]).max() / ref) if ref > 0 else 0.0
+    blk = {n: (a, b) for n, a, b in flatten_blocks(cfg)}
+    k1 = {c: (y64[slice(*blk[f"{c}.K1"])], y32[slice(*blk[f"{c}.K1"])]) for c in "ta"}
+    for ch, f in (("chi_m", lambda a, t: a / U ** 2), ("chi_d", lambda a, t: (a - 2 * t) / U ** 2)):
+        r64, r32 = f(k1["a"][0], k1["t"][0]), f(k1["a"][1], k1["t"][1])
+        rep[ch] = float(np.abs(r32 - r64).max() / np.abs(r64).max())
+    return rep
 
 
 def run_ours(args, rank, world, dist):
@@ -217,35 +278,47 @@ def run_ours(args, rank, world, dist):
     # ---- per-stage device times (eager run, CUDA events between stages) ----
     S.unflatten(x)
     stages = S.stage_times("fdPA", nrep=3)
-    top = max(stages, key=stages.get)
-    peaks = measured_peaks()
-    work = stage_work(cfg, top, S)
-    achieved = work / (stages[top] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel_stage": top, "achieved": achieved, "peak": peaks.get("hbm_gbs"),
-                "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None,
-                "stage_ms": {k: round(v, 4) for k, v in stages.items()},
-                "peak_source": "fallback" if peaks.get("fallback") else "measured"}
-    # ---- time to converge (plain Anderson with the reference's solve! defaults δ=0.85, m=8; tol 1e-8) ----
+    roofline = k3_gemm_roofline(S, stages, args.config)
+    precision = precision_report(cfg, S, x)
+    # ---- time to converge at max|R| < 1e-8 (Anderson with the reference's solve! defaults δ=0.85, m=8) ----
     conv = None
     if not args.no_converge:
-        cfg2, S2 = build_problem(args.config, "ours")
-        x0 = S2.flatten()
-        S2.iterate_solver("fdPA")  # captures the iteration graph outside the timed solve
-        S2.unflatten(x0)
-        t0 = time.perf_counter()
-        r = S2.solve("fdPA", maxiter=300, tol=1e-8, delta=0.85, mem=8)
-        t_conv = time.perf_counter() - t0
-        conv = {"seconds": dist.max(t_conv), "iterations": r["iterations"], "converged": r["converged"],
-                "final_residual": r["residual"], "method": "Anderson m=8, beta=0.85 (NLsolve restated, device-resident QR), plain FP64",
-                "ms_per_solver_iteration": 1e3 * t_conv / max(1, abs(r["iterations"]))}
-        S2.close()
+        conv = {}
+        res = {}
+        for mode in ("plain", "mixed"):
+            cfg2, S2 = build_problem(args.config, "ours")
+            x0 = S2.flatten()
+            S2.iterate_solver("fdPA")  # captures the iteration graphs outside the timed solves
+            S2.set_precision("mixed"); S2.iterate_solver("fdPA"); S2.set_precision("fp64")
+            S2.unflatten(x0)
+            S2.synchronize()
+            t0 = time.perf_counter()
+            if mode == "plain":
+                r = S2.solve("fdPA", maxiter=300, tol=1e-8, delta=0.85, mem=8)
+                info = {"iterations": r["iterations"],
+                        "method": "Anderson m=8, beta=0.85 (NLsolve restated, device-resident QR), FP64 map"}
+            else:
+                r = S2.solve_mixed("fdPA", maxiter=600, tol=1e-8, delta=0.85, mem=8)
+                info = {"fp64_maps": r["evals_fp64"], "mixed_maps": r["evals_mixed"],
+                        "method": "iterative refinement: FP64 residual outside, Anderson m=8 beta=0.85 with FP32 "
+                                  "history on the mixed map (FP32 K3 contractions) inside; FP64 Anderson phase "
+                                  "once the mixed map's rounding floor is reached"}
+            t = time.perf_counter() - t0
+            conv[mode] = {"seconds": dist.max(t), "converged": r["converged"], "final_residual": r["residual"], **info}
+            res[mode] = {c: S2.susceptibility(c) for c in ("m", "d")}
+            res[mode]["Sigma"] = S2.get("Sigma")
+            S2.close()
+        import numpy as np
+        conv["speedup_mixed_vs_plain"] = conv["plain"]["seconds"] / conv["mixed"]["seconds"]
+        conv["mixed_vs_plain_solution_rel_err"] = {
+            k: float(np.abs(res["mixed"][k] - res["plain"][k]).max() / np.abs(res["plain"][k]).max())
+            for k in ("m", "d", "Sigma")}
     nstate = S.state_len
     out = {
         "metric": METRIC, "value": ms_dev * 1e-3, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128 (FP64 complex)", "data": "synthetic (seeded; reference inputs restated)",
-        "config": {"workload": "Hubbard 8x8 NL fdPA: t=1 t'=0 mu=0 U=2 beta=5 nK1=32 nK2=(16,16) nK3=(8,12) nG=32 "
-                               "mPi=32, synthetic RefVertex, init_sym_grp",
+        "config": {"workload": WORKLOADS.get(args.config, args.config),
                    "name": args.config, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "L2 flushed (256 MB device write) before every timed iteration; flush not timed"},
         "e2e": {"value": t_e2e, "unit": UNIT, "h2d_bytes_per_step": nstate * 16, "d2h_bytes_per_step": nstate * 16},
@@ -253,6 +326,7 @@ def run_ours(args, rank, world, dist):
         "launches_per_iteration": launches,
         "time_to_converge": conv,
         "roofline": roofline,
+        "precision_mixed_map_vs_fp64": precision,
         "clocks": clk,
     }
     S.close()
@@ -311,7 +385,7 @@ def main():
     dist = Dist(world)
     out = run_ours(args, rank, world, dist)
     if rank == 0:
-        out["cpu_baseline"] = cpu_baseline_sample(args)
+        out["cpu_baseline"] = None if args.no_cpu_baseline else cpu_baseline_sample(args)
         print(json.dumps(out))
     return 0
 

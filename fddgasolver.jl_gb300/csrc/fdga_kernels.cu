@@ -875,6 +875,12 @@ __global__ void k_chi(const cplx* K1p, const cplx* K1t, const cplx* K1a, int whi
         out[j] = chi(j);
     }
 }
+// FP64 FMA throughput calibration: four independent FMA chains per thread
+__global__ void k_fp64_rate(double* out, double a, double b, int iters) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    for (int i = 0; i < iters; ++i) { x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b); }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
+}
 // count of non-finite values
 __global__ void k_nonfinite(const cplx* a, size_t n, unsigned int* count) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -1112,6 +1118,37 @@ cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const c
     const size_t n = local ? (size_t)NO : (size_t)NO * Nq;
     k_chi<<<blocks_for(n, 256), 256, 0, s>>>(K1p, K1t, K1a, which, 1.0 / (U * U), NO, Nq, local, out);
     LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t measure_fp64_rate(float* ms, double* gflops) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double* buf = nullptr;
+    e = cudaMalloc(&buf, (size_t)blocks * threads * sizeof(double));
+    if (e != cudaSuccess) return e;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0);
+        k_fp64_rate<<<blocks, threads>>>(buf, 0.999, 1e-3, iters);
+        cudaEventRecord(e1);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) break;
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        best = std::min(best, t);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    *ms = best;
+    *gflops = 2.0 * 4.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
+    return e;
 }
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count) {
     k_nonfinite<<<blocks_for(n, 256), 256, 0, s>>>(a, n, count);

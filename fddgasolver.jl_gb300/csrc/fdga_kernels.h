@@ -140,6 +140,7 @@ cudaError_t launch_ma_update(cudaStream_t s, int nblk, cplx* x, const cplx* g, c
 cudaError_t launch_ma_qrot(cudaStream_t s, int nblk, const AAVecs32W& Q, int m, const cplx* rot, size_t n);
 cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double U,
                        int NO, int Nq, int local, cplx* out);
+cudaError_t measure_fp64_rate(float* ms, double* gflops);
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count);
 
 }  // namespace fdga

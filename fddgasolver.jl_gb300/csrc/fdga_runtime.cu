@@ -458,11 +458,12 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             a3.blocks = h->d_k3blocks;
             a3.nblocks = h->nk3blocks;
             LC(launch_bse_K3(s, 0, a3, 3, d, h->precision == FDGA_MIXED));
+            stage("bse_L_K3_gemm");
             cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
             const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
             LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
         }
-        stage("bse_L_K3");
+        stage("bse_L_K3_finalize");
     }
     // ω-sums of the right BSE factor (needs FL.K2 of this iteration)
     LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FL, h->SX, d));
@@ -497,11 +498,12 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         a3.blocks = h->d_k3blocks;
         a3.nblocks = h->nk3blocks;
         LC(launch_bse_K3(s, 1, a3, 3, d, h->precision == FDGA_MIXED));
+        stage("bse_K3_gemm");
         cplx* out[3] = {chanK(h, h->yS, CH_P, 3), chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3)};
         const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
         LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
     }
-    stage("bse_K3");
+    stage("bse_K3_finalize");
     // SDE (src/SDE.jl:3-33) with the new F
     cplx* SigOut = sigmaOf(h, h->yS);
     if (update_sigma) {
@@ -1301,6 +1303,24 @@ int fdga_flush_l2(fdga_handle* h, size_t bytes) {
     static unsigned char v = 0;
     CK(cudaMemsetAsync(h->flush_buf, ++v, bytes, h->st));
     return FDGA_OK;
+}
+
+int fdga_query(fdga_handle* h, const char* key, double* value) {
+    if (!key || !value) return fail(h, FDGA_ERR_ARG, "null argument");
+    const std::string k(key);
+    if (k == "fp64_gflops") {  // device calibration: FP64 FMA throughput of this GPU
+        float ms = 0.f;
+        const cudaError_t e = measure_fp64_rate(&ms, value);
+        if (e != cudaSuccess) return cuda_fail(h, e, "fp64 calibration");
+        return FDGA_OK;
+    }
+    if (!h) return FDGA_ERR_ARG;
+    if (k == "k3_blocks") { *value = h->nk3blocks; return FDGA_OK; }
+    if (k == "k3_block_dim") { *value = h->d.N3n; return FDGA_OK; }
+    if (k == "state_len") { *value = (double)h->nstate; return FDGA_OK; }
+    if (k == "launches") { *value = h->last_launches; return FDGA_OK; }
+    if (k == "precision") { *value = h->precision; return FDGA_OK; }
+    return fail(h, FDGA_ERR_ARG, "unknown query key " + k);
 }
 
 int fdga_launches_per_iteration(const fdga_handle* h, int* n) {

@@ -59,6 +59,7 @@ EXPORTS = {
     "fdga_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "fdga_bubble_noalloc": (ctypes.c_int, [ctypes.POINTER(fdga_config), ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p]),
+    "fdga_query": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]),
     "fdga_launches_per_iteration": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
 }
 

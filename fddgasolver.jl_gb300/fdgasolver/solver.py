@@ -217,6 +217,11 @@ class _Solver:
         """fixed_point! on caller-owned host buffers (e.g. pinned) of state_len complex values."""
         self._check(self._lib.fdga_residual(self._h, STRATEGIES[strategy], x_ptr, R_ptr, self.state_len))
 
+    def query(self, key):
+        v = ctypes.c_double()
+        self._check(self._lib.fdga_query(self._h, key.encode(), ctypes.byref(v)))
+        return v.value
+
     def launches_per_iteration(self):
         v = ctypes.c_int()
         self._check(self._lib.fdga_launches_per_iteration(self._h, ctypes.byref(v)))

@@ -151,6 +151,12 @@ int fdga_occupation(fdga_handle* h, double* n);
 #define FDGA_CHI_S 2
 int fdga_susceptibility(fdga_handle* h, int channel, double* out, size_t n);
 
+/* Scalar facts of a handle, for benchmarks and tools: "k3_blocks" (the (P, Ω) blocks of the K3
+ * mesh that hold class representatives), "k3_block_dim" (2·nK3ν), "state_len", "launches"
+ * (kernels per iteration), "precision"; and, with h == NULL allowed, "fp64_gflops": a
+ * calibration of the GPU's FP64 FMA throughput (GFLOP/s, one short kernel). */
+int fdga_query(fdga_handle* h, const char* key, double* value);
+
 /* Device timing on the handle's stream (CUDA events), for benchmarks. slot in [0, 8). */
 int fdga_event_record(fdga_handle* h, int slot);
 int fdga_event_elapsed_ms(fdga_handle* h, int slot_a, int slot_b, float* ms);
