@@ -285,7 +285,7 @@ def run_ours(args, rank, world, dist):
     if not args.no_converge:
         conv = {}
         res = {}
-        for mode in ("plain", "mixed"):
+        for mode in ("plain", "mixed", "newton", "newton_mixed"):
             cfg2, S2 = build_problem(args.config, "ours")
             x0 = S2.flatten()
             S2.iterate_solver("fdPA")  # captures the iteration graphs outside the timed solves
@@ -297,6 +297,12 @@ def run_ours(args, rank, world, dist):
                 r = S2.solve("fdPA", maxiter=300, tol=1e-8, delta=0.85, mem=8)
                 info = {"iterations": r["iterations"],
                         "method": "Anderson m=8, beta=0.85 (NLsolve restated, device-resident QR), FP64 map"}
+            elif mode in ("newton", "newton_mixed"):
+                jvp = "fp64" if mode == "newton" else "mixed"
+                r = S2.solve_newton("fdPA", maxiter=600, tol=1e-8, restart=30, jvp=jvp)
+                info = {"newton_steps": r["newton"], "fp64_maps": r["evals_fp64"], "mixed_maps": r["evals_mixed"],
+                        "method": f"Newton-Krylov: GMRES(30) on (I-J)dx = R with forward-difference JVPs of the "
+                                  f"{jvp} map, Eisenstat-Walker forcing, backtracking on the FP64 residual"}
             else:
                 r = S2.solve_mixed("fdPA", maxiter=600, tol=1e-8, delta=0.85, mem=8)
                 info = {"fp64_maps": r["evals_fp64"], "mixed_maps": r["evals_mixed"],
@@ -309,10 +315,25 @@ def run_ours(args, rank, world, dist):
             res[mode]["Sigma"] = S2.get("Sigma")
             S2.close()
         import numpy as np
-        conv["speedup_mixed_vs_plain"] = conv["plain"]["seconds"] / conv["mixed"]["seconds"]
-        conv["mixed_vs_plain_solution_rel_err"] = {
-            k: float(np.abs(res["mixed"][k] - res["plain"][k]).max() / np.abs(res["plain"][k]).max())
-            for k in ("m", "d", "Sigma")}
+        for mode in ("mixed", "newton", "newton_mixed"):
+            conv[f"speedup_{mode}_vs_plain"] = conv["plain"]["seconds"] / conv[mode]["seconds"]
+            conv[f"{mode}_vs_plain_solution_rel_err"] = {
+                k: float(np.abs(res[mode][k] - res["plain"][k]).max() / np.abs(res["plain"][k]).max())
+                for k in ("m", "d", "Sigma")}
+        # linear response at the fixed point: dχ_m/dU(Ω = 0, q = (π, π)) through GMRES on (I − J)
+        cfg2, S2 = build_problem(args.config, "ours")
+        S2.solve_newton("fdPA", maxiter=600, tol=1e-12, restart=30, jvp="fp64")
+        t0 = time.perf_counter()
+        d, info = S2.dchi_dU("m", hU=1e-4, restart=40, cycles=4, rtol=1e-8)
+        t = time.perf_counter() - t0
+        nO = 2 * cfg2["nK1"] - 1
+        L = cfg2.get("L", 1)
+        iq = (L // 2 + L * (L // 2)) if cfg2["kind"] != "siam" else 0
+        v = d[iq * nO + cfg2["nK1"] - 1]
+        conv["dchi_m_dU"] = {"value_Omega0_q_pipi": [v.real, v.imag], "seconds": t, **info,
+                             "method": "GMRES(40) on (I-J) dx/dU = dPhi/dU at the converged state, central-difference "
+                                       "JVPs and dPhi/dU (h = 1e-4)"}
+        S2.close()
     nstate = S.state_len
     out = {
         "metric": METRIC, "value": ms_dev * 1e-3, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -68,6 +68,10 @@ struct AAVecs {
 struct AAVecsW {
     cplx* v[AA_MAX];
 };
+constexpr int KR_MAX = 64;  // largest Krylov basis of the GMRES solves
+struct KrVecs {
+    const cplxf* v[KR_MAX];
+};
 struct AAVecs32 {
     const cplxf* v[AA_MAX];
 };
@@ -141,6 +145,21 @@ cudaError_t launch_ma_qrot(cudaStream_t s, int nblk, const AAVecs32W& Q, int m, 
 cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double U,
                        int NO, int Nq, int local, cplx* out);
 cudaError_t measure_fp64_rate(float* ms, double* gflops);
+// GMRES building blocks (real inner products on the FP32 Krylov basis)
+cudaError_t launch_kr_point(cudaStream_t s, int nblk, const cplx* x, const cplxf* v, double eps, cplx* xp, size_t n);
+cudaError_t launch_kr_apply(cudaStream_t s, int nblk, const cplx* y, const cplx* y0, const cplxf* v, double a,
+                            double b, cplxf* w, size_t n);
+cudaError_t launch_kr_dots(cudaStream_t s, int nblk, const KrVecs& V, int nv, const cplxf* w, double* part,
+                           int norm_slot, size_t n);
+cudaError_t launch_kr_reduce(cudaStream_t s, const double* part, int np, int ncoef, double* coef);
+cudaError_t launch_kr_sub(cudaStream_t s, int nblk, const KrVecs& V, int nv, const double* c, cplxf* w, size_t n);
+cudaError_t launch_kr_scale(cudaStream_t s, int nblk, const cplxf* w, double nrm, cplxf* out, size_t n);
+cudaError_t launch_kr_update(cudaStream_t s, int nblk, cplx* x, const KrVecs& V, int nv, const double* y, double scale,
+                             size_t n);
+cudaError_t launch_kr_load(cudaStream_t s, int nblk, const cplx* a, cplxf* out, double* part, size_t n);
+cudaError_t launch_kr_resid(cudaStream_t s, int nblk, const cplx* b, const cplxf* v, double alpha, const cplx* y,
+                            const cplx* yb, double beta, cplx* r, size_t n);
+cudaError_t launch_kr_axpby(cudaStream_t s, int nblk, cplx* out, const cplx* a, double lam, const cplx* b, size_t n);
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count);
 
 }  // namespace fdga

@@ -1,0 +1,226 @@
+// fdga_krylov.cu -- GMRES building blocks for the Newton–Krylov solve of the parquet fixed point
+// and for the linear response dx*/dU.
+//
+// The map Φ is real-linear but not complex-linear in the state (the symmetry operations
+// conjugate), so the Jacobian acts on the state as a real vector of 2n components and GMRES runs
+// in real arithmetic: inner products are Re<a, b> = Σ (a.x b.x + a.y b.y).  The Krylov basis is
+// stored in FP32 (cplxf pairs); products accumulate in FP32 over runs of 64 terms and then in
+// FP64; reductions, the Hessenberg matrix and the iterate are FP64.  Jacobian-vector products are
+// forward differences of the map, (Φ(x + εv) − Φ(x)) / ε, evaluated by the same
+// graph-captured iteration as the plain solver.
+#include "fdga_kernels.h"
+
+#include <algorithm>
+
+namespace fdga {
+
+namespace {
+
+constexpr int RT = 256;
+constexpr int FLUSH = 64;
+constexpr int CHUNK = 8;
+
+__device__ __forceinline__ cplxf tof(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+
+struct RAcc {  // real accumulator: FP32 runs flushed into FP64
+    float s32 = 0.f;
+    double s64 = 0.0;
+    int k = 0;
+    __device__ __forceinline__ void add(float v) {
+        s32 += v;
+        if (++k == FLUSH) { s64 += (double)s32; s32 = 0.f; k = 0; }
+    }
+    __device__ __forceinline__ double total() const { return s64 + (double)s32; }
+};
+
+__device__ __forceinline__ void store_partial(double v, double* sh, double* out) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = RT / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+    __syncthreads();
+}
+__device__ __forceinline__ float rdot(cplxf a, cplxf b) { return a.x * b.x + a.y * b.y; }
+
+// xp = x + ε v
+__global__ void __launch_bounds__(RT) k_kr_point(const cplx* x, const cplxf* v, double eps, cplx* xp, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT)
+        xp[i] = x[i] + to_d(v[i]) * eps;
+}
+
+// w = a·v + b·(y − y0)   (A v = v − J v: a = 1, b = −1/ε; the right-hand side ∂Φ: a = 0, b = 1/(2h))
+__global__ void __launch_bounds__(RT) k_kr_apply(const cplx* y, const cplx* y0, const cplxf* v, double a, double b,
+                                                 cplxf* w, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
+        cplx d = (y[i] - y0[i]) * b;
+        if (v) d += to_d(v[i]) * a;
+        w[i] = tof(d);
+    }
+}
+
+// partials of Re<V_i, w> for the CHUNK vectors of chunk blockIdx.y: part[i * np + block]; when
+// norm_slot >= 0 the chunk-0 blocks also write the partial of |w|² to part[norm_slot * np + block]
+__global__ void __launch_bounds__(RT) k_kr_dots(KrVecs V, int nv, const cplxf* w, double* part, int np, int norm_slot,
+                                                size_t n) {
+    __shared__ double sh[RT];
+    const int i0 = blockIdx.y * CHUNK;
+    const int cnt = max(0, min(CHUNK, nv - i0));
+    const bool with_norm = norm_slot >= 0 && blockIdx.y == 0;
+    RAcc a[CHUNK], an;
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
+        const cplxf wi = w[i];
+#pragma unroll
+        for (int j = 0; j < CHUNK; ++j)
+            if (j < cnt) a[j].add(rdot(V.v[i0 + j][i], wi));
+        if (with_norm) an.add(rdot(wi, wi));
+    }
+    for (int j = 0; j < cnt; ++j) store_partial(a[j].total(), sh, part + (size_t)(i0 + j) * np);
+    if (with_norm) store_partial(an.total(), sh, part + (size_t)norm_slot * np);
+}
+
+// coef[i] = Σ_blocks part[i], i < ncoef (one block, fixed order)
+__global__ void __launch_bounds__(RT) k_kr_reduce(const double* part, int np, int ncoef, double* coef) {
+    __shared__ double sh[RT];
+    for (int i = 0; i < ncoef; ++i) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < np; b += RT) s += part[(size_t)i * np + b];
+        sh[threadIdx.x] = s;
+        __syncthreads();
+        for (int o = RT / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) coef[i] = sh[0];
+        __syncthreads();
+    }
+}
+
+// w -= Σ_{i<nv} c_i V_i (FP32)
+__global__ void __launch_bounds__(RT) k_kr_sub(KrVecs V, int nv, const double* c, cplxf* w, size_t n) {
+    __shared__ float cs[KR_MAX];
+    for (int i = threadIdx.x; i < nv; i += RT) cs[i] = (float)c[i];
+    __syncthreads();
+    for (size_t t = blockIdx.x * (size_t)RT + threadIdx.x; t < n; t += (size_t)gridDim.x * RT) {
+        cplxf s = w[t];
+        for (int i = 0; i < nv; ++i) {
+            const cplxf v = V.v[i][t];
+            s.x -= cs[i] * v.x;
+            s.y -= cs[i] * v.y;
+        }
+        w[t] = s;
+    }
+}
+
+// out = w / nrm
+__global__ void __launch_bounds__(RT) k_kr_scale(const cplxf* w, double nrm, cplxf* out, size_t n) {
+    const float inv = (float)(1.0 / nrm);
+    for (size_t t = blockIdx.x * (size_t)RT + threadIdx.x; t < n; t += (size_t)gridDim.x * RT) out[t] = w[t] * inv;
+}
+
+// x += Σ_{i<nv} y_i V_i (sum in FP32, added in FP64)
+__global__ void __launch_bounds__(RT) k_kr_update(cplx* x, KrVecs V, int nv, const double* y, double scale, size_t n) {
+    __shared__ float ys[KR_MAX];
+    for (int i = threadIdx.x; i < nv; i += RT) ys[i] = (float)y[i];
+    __syncthreads();
+    for (size_t t = blockIdx.x * (size_t)RT + threadIdx.x; t < n; t += (size_t)gridDim.x * RT) {
+        cplxf s{0.f, 0.f};
+        for (int i = 0; i < nv; ++i) {
+            const cplxf v = V.v[i][t];
+            s.x += ys[i] * v.x;
+            s.y += ys[i] * v.y;
+        }
+        x[t] = x[t] + to_d(s) * scale;
+    }
+}
+
+// out = a (FP64 -> FP32 copy), partial |a|²
+__global__ void __launch_bounds__(RT) k_kr_load(const cplx* a, cplxf* out, double* part, size_t n) {
+    __shared__ double sh[RT];
+    double s = 0.0;
+    for (size_t t = blockIdx.x * (size_t)RT + threadIdx.x; t < n; t += (size_t)gridDim.x * RT) {
+        const cplx v = a[t];
+        out[t] = tof(v);
+        s += v.x * v.x + v.y * v.y;
+    }
+    store_partial(s, sh, part);
+}
+
+// r = b + α v + β (y − yb)   (FP64; v FP32 or null)
+__global__ void __launch_bounds__(RT) k_kr_resid(const cplx* b, const cplxf* v, double alpha, const cplx* y,
+                                                 const cplx* yb, double beta, cplx* r, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
+        cplx t = b ? b[i] : mk(0.0, 0.0);
+        if (v) t += to_d(v[i]) * alpha;
+        if (y) t += (y[i] - yb[i]) * beta;
+        r[i] = t;
+    }
+}
+// out = a + λ b (FP64)
+__global__ void __launch_bounds__(RT) k_kr_axpby(cplx* out, const cplx* a, double lam, const cplx* b, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) out[i] = a[i] + b[i] * lam;
+}
+
+}  // namespace
+
+#define KR_CHECK()                                   \
+    do {                                             \
+        cudaError_t e__ = cudaGetLastError();        \
+        if (e__ != cudaSuccess) return e__;          \
+    } while (0)
+
+cudaError_t launch_kr_point(cudaStream_t s, int nblk, const cplx* x, const cplxf* v, double eps, cplx* xp, size_t n) {
+    k_kr_point<<<nblk, RT, 0, s>>>(x, v, eps, xp, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_apply(cudaStream_t s, int nblk, const cplx* y, const cplx* y0, const cplxf* v, double a,
+                            double b, cplxf* w, size_t n) {
+    k_kr_apply<<<nblk, RT, 0, s>>>(y, y0, v, a, b, w, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_dots(cudaStream_t s, int nblk, const KrVecs& V, int nv, const cplxf* w, double* part,
+                           int norm_slot, size_t n) {
+    if (nv > KR_MAX) return cudaErrorInvalidValue;
+    const int chunks = std::max(1, (nv + CHUNK - 1) / CHUNK);
+    k_kr_dots<<<dim3(nblk, chunks), RT, 0, s>>>(V, nv, w, part, nblk, norm_slot, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_reduce(cudaStream_t s, const double* part, int np, int ncoef, double* coef) {
+    k_kr_reduce<<<1, RT, 0, s>>>(part, np, ncoef, coef);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_sub(cudaStream_t s, int nblk, const KrVecs& V, int nv, const double* c, cplxf* w, size_t n) {
+    if (nv > KR_MAX) return cudaErrorInvalidValue;
+    k_kr_sub<<<nblk, RT, 0, s>>>(V, nv, c, w, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_scale(cudaStream_t s, int nblk, const cplxf* w, double nrm, cplxf* out, size_t n) {
+    k_kr_scale<<<nblk, RT, 0, s>>>(w, nrm, out, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_update(cudaStream_t s, int nblk, cplx* x, const KrVecs& V, int nv, const double* y, double scale,
+                             size_t n) {
+    if (nv > KR_MAX) return cudaErrorInvalidValue;
+    k_kr_update<<<nblk, RT, 0, s>>>(x, V, nv, y, scale, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_load(cudaStream_t s, int nblk, const cplx* a, cplxf* out, double* part, size_t n) {
+    k_kr_load<<<nblk, RT, 0, s>>>(a, out, part, n);
+    KR_CHECK(); return cudaSuccess;
+}
+
+}  // namespace fdga
+
+namespace fdga {
+cudaError_t launch_kr_resid(cudaStream_t s, int nblk, const cplx* b, const cplxf* v, double alpha, const cplx* y,
+                            const cplx* yb, double beta, cplx* r, size_t n) {
+    k_kr_resid<<<nblk, RT, 0, s>>>(b, v, alpha, y, yb, beta, r, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_axpby(cudaStream_t s, int nblk, cplx* out, const cplx* a, double lam, const cplx* b, size_t n) {
+    k_kr_axpby<<<nblk, RT, 0, s>>>(out, a, lam, b, n);
+    KR_CHECK(); return cudaSuccess;
+}
+}  // namespace fdga

@@ -82,6 +82,9 @@ struct fdga_handle {
     std::vector<cplx*> aa_buf;
     double* d_part = nullptr;
     cplx *aa_R = nullptr, *aa_rot = nullptr, *aa_gam = nullptr, *aa_part = nullptr;  // device QR state
+    std::vector<cplx*> kr64;       // Newton-Krylov / linear response: x, y0, F, dx, yb, r, y+
+    std::vector<cplxf*> kr32;      // Krylov basis V[0..m] (FP32), w, scratch
+    double *kr_part = nullptr, *kr_coef = nullptr;
     std::vector<cplx*> ma_buf64;   // mixed solver: defect, g, g_old
     std::vector<cplxf*> ma_buf32;  // mixed solver: f, Δf, Q, Δg (FP32 history)
     std::vector<void*> allocs;
@@ -1124,6 +1127,358 @@ int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, doub
     if (iters) *iters = converged ? nouter : -nouter;
     if (res) *res = resid;
     if (evals) { evals[0] = n64; evals[1] = nmix; }
+    return FDGA_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Newton–Krylov and linear response (GMRES on A = I − J, J the forward- or central-difference
+// Jacobian of the iteration map, real inner products; the kernels are in fdga_krylov.cu)
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+int ensure_krylov(fdga_handle* h, int m) {
+    const size_t n = h->nstate;
+    while (h->kr64.size() < 7) {
+        cplx* p = nullptr;
+        int r = dalloc(h, &p, n);
+        if (r) return r;
+        h->kr64.push_back(p);
+    }
+    while (h->kr32.size() < (size_t)m + 3) {
+        cplxf* p = nullptr;
+        int r = dalloc(h, &p, n);
+        if (r) return r;
+        h->kr32.push_back(p);
+    }
+    if (!h->kr_part) {
+        int r = dalloc(h, &h->kr_part, (size_t)(KR_MAX + 2) * NBLK_RED);
+        if (!r) r = dalloc(h, &h->kr_coef, 4 * (size_t)(KR_MAX + 2));
+        if (r) return r;
+    }
+    return FDGA_OK;
+}
+
+// 2-norm of an FP64 device vector as a real 2n-vector (scratch: an FP32 vector)
+int norm2_64(fdga_handle* h, const cplx* a, cplxf* scratch, double& out) {
+    const size_t n = h->nstate;
+    CK(launch_kr_load(h->st, NBLK_RED, a, scratch, h->kr_part, n));
+    CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, 1, h->kr_coef));
+    double v = 0.0;
+    CK(cudaMemcpyAsync(&v, h->kr_coef, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    out = std::sqrt(std::max(0.0, v));
+    return FDGA_OK;
+}
+
+// A v = v − J v at the base point xb (yb = Φ(xb)) for the unit FP32 direction v, into w (FP32).
+// Forward: J v = (Φ(xb + εv) − yb)/ε.  Central: J v = (Φ(xb + εv) − Φ(xb − εv))/(2ε).
+int apply_A(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplxf* v, double eps, bool central,
+            cplx* ytmp, cplxf* w, int& nmaps) {
+    const size_t n = h->nstate;
+    CK(launch_kr_point(h->st, NBLK_RED, xb, v, eps, h->xS, n));
+    int r = run_iteration(h, strategy, true, true);
+    if (r) return r;
+    ++nmaps;
+    if (!central) {
+        CK(launch_kr_apply(h->st, NBLK_RED, h->yS, yb, v, 1.0, -1.0 / eps, w, n));
+        return FDGA_OK;
+    }
+    CK(cudaMemcpyAsync(ytmp, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_kr_point(h->st, NBLK_RED, xb, v, -eps, h->xS, n));
+    r = run_iteration(h, strategy, true, true);
+    if (r) return r;
+    ++nmaps;
+    CK(launch_kr_apply(h->st, NBLK_RED, ytmp, h->yS, v, 1.0, -0.5 / eps, w, n));
+    return FDGA_OK;
+}
+
+// Restarted GMRES(m) for A dx = b, dx starting at 0.  Cycles after the first restart from the
+// true residual b − A dx (one more A application).  relres = final ‖b − A dx‖/‖b‖ estimate.
+int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplx* b, cplx* dx, int m,
+                int cycles, double rtol, double eps_rel, bool central, int max_maps, int& nmaps, int& iters,
+                double& relres) {
+    const size_t n = h->nstate;
+    int r = ensure_krylov(h, m);
+    if (r) return r;
+    KrVecs V{};
+    for (int i = 0; i <= m; ++i) V.v[i] = h->kr32[i];
+    const std::vector<cplxf*>& Vw = h->kr32;  // the same basis, writable
+    cplxf* w = h->kr32[m + 1];
+    cplxf* sc = h->kr32[m + 2];
+    cplx* rr = h->kr64[5];
+    cplx* ytmp = h->kr64[6];  // Φ(xb + εv) of a central difference
+    double xnorm = 0.0, bnorm = 0.0;
+    if ((r = norm2_64(h, xb, sc, xnorm)) || (r = norm2_64(h, b, sc, bnorm))) return r;
+    const double eps = eps_rel * (1.0 + xnorm);
+    CK(cudaMemsetAsync(dx, 0, n * sizeof(cplx), h->st));
+    relres = 1.0;
+    if (bnorm == 0.0) { relres = 0.0; return FDGA_OK; }
+    std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hc(2 * (KR_MAX + 2)), y(m);
+    auto Hij = [&](int i, int j) -> double& { return H[(size_t)i + (size_t)(m + 1) * j]; };
+    double* c1 = h->kr_coef;
+    double* c2 = h->kr_coef + (KR_MAX + 2);
+    double* cy = h->kr_coef + 2 * (KR_MAX + 2);
+    for (int cyc = 0; cyc < cycles; ++cyc) {
+        double beta = bnorm;
+        if (cyc == 0) {
+            CK(launch_kr_load(h->st, NBLK_RED, b, sc, h->kr_part, n));
+            CK(launch_kr_scale(h->st, NBLK_RED, sc, bnorm, Vw[0], n));
+        } else {
+            // true residual r = b − A dx, with A dx = ‖dx‖ A(dx/‖dx‖)
+            double dn = 0.0;
+            if ((r = norm2_64(h, dx, sc, dn))) return r;
+            if (dn == 0.0) break;
+            CK(launch_kr_load(h->st, NBLK_RED, dx, sc, h->kr_part, n));
+            CK(launch_kr_scale(h->st, NBLK_RED, sc, dn, sc, n));
+            if (nmaps + (central ? 2 : 1) > max_maps) break;
+            if ((r = apply_A(h, strategy, xb, yb, sc, eps, central, ytmp, w, nmaps))) return r;
+            // rr = b − dn·w  (w FP32)
+            CK(launch_kr_resid(h->st, NBLK_RED, b, w, -dn, nullptr, nullptr, 0.0, rr, n));
+            if ((r = norm2_64(h, rr, sc, beta))) return r;
+            relres = beta / bnorm;
+            if (relres <= rtol) break;
+            CK(launch_kr_load(h->st, NBLK_RED, rr, sc, h->kr_part, n));
+            CK(launch_kr_scale(h->st, NBLK_RED, sc, beta, Vw[0], n));
+        }
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int k = 0;
+        double est = beta;
+        for (int j = 0; j < m; ++j) {
+            if (nmaps + (central ? 2 : 1) > max_maps) break;
+            if ((r = apply_A(h, strategy, xb, yb, V.v[j], eps, central, ytmp, w, nmaps))) return r;
+            // classical Gram-Schmidt, twice
+            CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, h->kr_part, -1, n));
+            CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, j + 1, c1));
+            CK(launch_kr_sub(h->st, NBLK_RED, V, j + 1, c1, w, n));
+            CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, h->kr_part, -1, n));
+            CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, j + 1, c2));
+            CK(launch_kr_sub(h->st, NBLK_RED, V, j + 1, c2, w, n));
+            CK(launch_kr_dots(h->st, NBLK_RED, V, 0, w, h->kr_part + (size_t)(KR_MAX + 1) * NBLK_RED, 0, n));
+            CK(launch_kr_reduce(h->st, h->kr_part + (size_t)(KR_MAX + 1) * NBLK_RED, NBLK_RED, 1, c2 + KR_MAX + 1));
+            CK(cudaMemcpyAsync(hc.data(), h->kr_coef, 2 * (KR_MAX + 2) * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->st));
+            CK(cudaStreamSynchronize(h->st));
+            for (int i = 0; i <= j; ++i) Hij(i, j) = hc[i] + hc[(KR_MAX + 2) + i];
+            const double hn = std::sqrt(std::max(0.0, hc[(KR_MAX + 2) + KR_MAX + 1]));
+            Hij(j + 1, j) = hn;
+            if (hn > 0.0) CK(launch_kr_scale(h->st, NBLK_RED, w, hn, Vw[j + 1], n));
+            for (int i = 0; i < j; ++i) {  // previous rotations
+                const double a = Hij(i, j), bb = Hij(i + 1, j);
+                Hij(i, j) = cs[i] * a + sn[i] * bb;
+                Hij(i + 1, j) = -sn[i] * a + cs[i] * bb;
+            }
+            const double a = Hij(j, j), bb = Hij(j + 1, j), rho = std::hypot(a, bb);
+            cs[j] = rho > 0 ? a / rho : 1.0;
+            sn[j] = rho > 0 ? bb / rho : 0.0;
+            Hij(j, j) = rho;
+            Hij(j + 1, j) = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            ++iters;
+            k = j + 1;
+            est = std::fabs(g[j + 1]);
+            if (est <= rtol * bnorm || hn == 0.0) break;
+        }
+        if (k == 0) break;
+        for (int i = k - 1; i >= 0; --i) {
+            double v = g[i];
+            for (int jj = i + 1; jj < k; ++jj) v -= Hij(i, jj) * y[jj];
+            y[i] = Hij(i, i) != 0.0 ? v / Hij(i, i) : 0.0;
+        }
+        CK(cudaMemcpyAsync(cy, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        CK(launch_kr_update(h->st, NBLK_RED, dx, V, k, cy, 1.0, n));
+        relres = est / bnorm;
+        if (relres <= rtol) break;
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdga_set_U(fdga_handle* h, double U) {
+    if (!h) return FDGA_ERR_ARG;
+    if (!std::isfinite(U)) return fail(h, FDGA_ERR_ARG, "U must be finite");
+    h->d.U = U;
+    h->cfg.U = U;
+    h->c0_dirty = true;
+    drop_graphs(h);
+    return FDGA_OK;
+}
+
+int fdga_jvp(fdga_handle* h, int strategy, const double* v, double* Jv, size_t n) {
+    if (!h || !v || !Jv) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
+    int r = ensure_krylov(h, 1);
+    if (r) return r;
+    cplx *x = h->kr64[0], *tmp = h->kr64[1], *yp = h->kr64[2];
+    cplxf* dir = h->kr32[0];
+    CK(cudaMemcpyAsync(x, h->xS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(tmp, v, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
+    CK(launch_scatter(h->st, h->kr64[3], tmp, h->perm, n));  // reference layout -> device layout
+    double vn = 0.0, xn = 0.0;
+    if ((r = norm2_64(h, h->kr64[3], dir, vn)) || (r = norm2_64(h, x, dir, xn))) return r;
+    if (vn == 0.0) {
+        std::memset(Jv, 0, 2 * n * sizeof(double));
+        return FDGA_OK;
+    }
+    CK(launch_kr_load(h->st, NBLK_RED, h->kr64[3], dir, h->kr_part, n));
+    CK(launch_kr_scale(h->st, NBLK_RED, dir, vn, dir, n));
+    // central difference along the unit direction, scaled back by ‖v‖
+    const double eps = 1e-5 * (1.0 + xn);
+    CK(launch_kr_point(h->st, NBLK_RED, x, dir, eps, h->xS, n));
+    if ((r = run_iteration(h, strategy, true, true))) return r;
+    CK(cudaMemcpyAsync(yp, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_kr_point(h->st, NBLK_RED, x, dir, -eps, h->xS, n));
+    if ((r = run_iteration(h, strategy, true, true))) return r;
+    CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, h->yS, vn * 0.5 / eps, tmp, n));
+    CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_gather(h->st, h->yS, tmp, h->perm, n));
+    CK(cudaMemcpyAsync(Jv, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int restart, int jvp_precision,
+                      int* iters, double* res, double* trace, int* evals) {
+    if (!h) return FDGA_ERR_ARG;
+    if (maxiter < 2 || !(tol > 0) || restart < 1 || restart >= KR_MAX)
+        return fail(h, FDGA_ERR_ARG, "invalid solver parameters");
+    if (jvp_precision != FDGA_FP64 && jvp_precision != FDGA_MIXED) return fail(h, FDGA_ERR_ARG, "unknown precision");
+    const size_t n = h->nstate;
+    int r = ensure_krylov(h, restart);
+    if (r) return r;
+    const int prec0 = h->precision;
+    struct Restore {
+        fdga_handle* h; int p;
+        ~Restore() { h->precision = p; }
+    } restore{h, prec0};
+    cplx *x = h->kr64[0], *y0 = h->kr64[1], *F = h->kr64[2], *dx = h->kr64[3], *yb = h->kr64[4];
+    int n64 = 0, nmix = 0, nouter = 0, status = 0;
+    double resid = 0.0, prev = 0.0;
+    bool converged = false, have_y = false;
+    CK(cudaMemcpyAsync(x, h->xS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    for (;;) {
+        h->precision = FDGA_FP64;
+        if (!have_y) {
+            CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+            if ((r = run_iteration(h, strategy, true, true))) return r;
+            ++n64;
+        }
+        CK(cudaMemcpyAsync(y0, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        CK(launch_residual(h->st, y0, x, F, nullptr, 0.0, h->d_part, NBLK_RED, n));
+        prev = resid;
+        resid = reduce_max(h, NBLK_RED, status);
+        if (status) return status;
+        if (!std::isfinite(resid)) return fail(h, FDGA_ERR_NONFINITE, "non-finite residual in solve_newton");
+        if (trace) trace[nouter] = resid;
+        ++nouter;
+        if (resid < tol) { converged = true; break; }
+        if (n64 + nmix + 3 > maxiter) break;
+        // forcing term (Eisenstat–Walker choice 2, bounded); the mixed map's rounding floor bounds it below
+        double eta = nouter == 1 ? 0.1 : std::min(0.1, 0.9 * (resid / prev) * (resid / prev));
+        eta = std::max(eta, jvp_precision == FDGA_MIXED ? 1e-3 : 1e-6);
+        const cplx* base = y0;
+        if (jvp_precision == FDGA_MIXED) {
+            h->precision = FDGA_MIXED;
+            CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+            if ((r = run_iteration(h, strategy, true, true))) return r;
+            ++nmix;
+            CK(cudaMemcpyAsync(yb, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+            base = yb;
+        }
+        int nmaps = 0, its = 0;
+        double relres = 1.0;
+        const int left = maxiter - n64 - nmix - 1;
+        const double eps_rel = jvp_precision == FDGA_MIXED ? 3e-4 : 1e-7;
+        // (I − J) dx = F
+        r = gmres_solve(h, strategy, x, base, F, dx, restart, 1, eta, eps_rel, false, left, nmaps, its, relres);
+        if (r) return r;
+        if (h->precision == FDGA_FP64) n64 += nmaps; else nmix += nmaps;
+        // backtracking on max|R| of the FP64 map
+        h->precision = FDGA_FP64;
+        double lam = 1.0;
+        have_y = false;
+        for (int ls = 0; ls < 4 && n64 + nmix + 1 <= maxiter; ++ls) {
+            CK(launch_kr_axpby(h->st, NBLK_RED, h->xS, x, lam, dx, n));
+            if ((r = run_iteration(h, strategy, true, true))) return r;
+            ++n64;
+            CK(launch_residual(h->st, h->yS, h->xS, F, nullptr, 0.0, h->d_part, NBLK_RED, n));
+            const double rn = reduce_max(h, NBLK_RED, status);
+            if (status) return status;
+            if (std::isfinite(rn) && (rn < (1.0 - 1e-4 * lam) * resid || ls == 3)) {
+                CK(cudaMemcpyAsync(x, h->xS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+                have_y = true;
+                break;
+            }
+            lam *= 0.5;
+        }
+        if (!have_y) break;
+    }
+    // S holds Φ64 of the last iterate, as after the reference's solve!
+    CK(cudaMemcpyAsync(h->xS, y0, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (iters) *iters = converged ? nouter : -nouter;
+    if (res) *res = resid;
+    if (evals) { evals[0] = n64; evals[1] = nmix; }
+    return FDGA_OK;
+}
+
+int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int restart, int cycles, double rtol,
+                 double* out, size_t n_out, int* gmres_iters, double* relres_out) {
+    if (!h || !out) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (channel < FDGA_CHI_M || channel > FDGA_CHI_S) return fail(h, FDGA_ERR_ARG, "unknown susceptibility channel");
+    const size_t NO = (size_t)h->d.N1, full = NO * h->d.Nq;
+    if (n_out != full) return fail(h, FDGA_ERR_ARG, "dchi_dU length must be NΩ1·Nq");
+    if (!(hU > 0) || restart < 1 || restart >= KR_MAX || cycles < 1) return fail(h, FDGA_ERR_ARG, "invalid parameters");
+    const size_t n = h->nstate;
+    int r = ensure_krylov(h, restart);
+    if (r) return r;
+    const int prec0 = h->precision;
+    const double U = h->d.U;
+    struct Restore {
+        fdga_handle* h; int p; double U;
+        ~Restore() { h->precision = p; if (h->d.U != U) fdga_set_U(h, U); }
+    } restore{h, prec0, U};
+    h->precision = FDGA_FP64;
+    cplx *xs = h->kr64[0], *ys = h->kr64[1], *b = h->kr64[2], *dx = h->kr64[3], *yp = h->kr64[4];
+    CK(cudaMemcpyAsync(xs, h->xS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    // ∂Φ/∂U at the fixed point: central difference in U
+    if ((r = fdga_set_U(h, U + hU))) return r;
+    if ((r = run_iteration(h, strategy, true, true))) return r;
+    CK(cudaMemcpyAsync(yp, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    if ((r = fdga_set_U(h, U - hU))) return r;
+    if ((r = run_iteration(h, strategy, true, true))) return r;
+    CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, h->yS, 0.5 / hU, b, n));
+    if ((r = fdga_set_U(h, U))) return r;
+    if ((r = run_iteration(h, strategy, true, true))) return r;
+    CK(cudaMemcpyAsync(ys, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    // (I − J) dx = ∂Φ/∂U, central-difference Jacobian
+    int nmaps = 0, its = 0;
+    double relres = 1.0;
+    r = gmres_solve(h, strategy, xs, ys, b, dx, restart, cycles, rtol, 1e-5, true, 1 << 30, nmaps, its, relres);
+    if (r) return r;
+    // dχ/dU = χ(dx) − (2/U) χ(x*)   (χ = K1 combination / U²)
+    cplx* t1 = h->kr64[5];
+    CK(launch_chi(h->st, chanK(h, dx, CH_P, 1), chanK(h, dx, CH_T, 1), chanK(h, dx, CH_A, 1), channel, U, (int)NO,
+                  h->d.Nq, 0, t1));
+    CK(launch_chi(h->st, chanK(h, xs, CH_P, 1), chanK(h, xs, CH_T, 1), chanK(h, xs, CH_A, 1), channel, U, (int)NO,
+                  h->d.Nq, 0, t1 + full));
+    std::vector<cplx> hb(2 * full);
+    CK(cudaMemcpyAsync(hb.data(), t1, 2 * full * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->xS, xs, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (size_t i = 0; i < full; ++i) {
+        out[2 * i] = hb[i].x - 2.0 / U * hb[full + i].x;
+        out[2 * i + 1] = hb[i].y - 2.0 / U * hb[full + i].y;
+    }
+    if (gmres_iters) *gmres_iters = its;
+    if (relres_out) *relres_out = relres;
     return FDGA_OK;
 }
 

@@ -151,6 +151,40 @@ class _Solver:
         return {"converged": it.value > 0, "outer": n, "residual": res.value, "trace": trace[:n],
                 "evals_fp64": int(ev[0]), "evals_mixed": int(ev[1])}
 
+    def solve_newton(self, strategy="fdPA", maxiter=300, tol=1e-8, restart=30, jvp="fp64"):
+        """Newton–Krylov (GMRES(restart), forward-difference JVPs in 'fp64' or 'mixed') to max|R| < tol."""
+        trace = np.zeros(maxiter, dtype=np.float64)
+        it = ctypes.c_int()
+        res = ctypes.c_double()
+        ev = np.zeros(2, dtype=np.int32)
+        self._check(self._lib.fdga_solve_newton(self._h, STRATEGIES[strategy], int(maxiter), float(tol), int(restart),
+                                                {"fp64": 0, "mixed": 1}[jvp], ctypes.byref(it), ctypes.byref(res),
+                                                trace.ctypes.data, ev.ctypes.data))
+        n = abs(it.value)
+        return {"converged": it.value > 0, "newton": n, "residual": res.value, "trace": trace[:n],
+                "evals_fp64": int(ev[0]), "evals_mixed": int(ev[1])}
+
+    def jvp(self, v, strategy="fdPA"):
+        """dΦ/dx · v at the current state (flatten layout)."""
+        v = np.ascontiguousarray(v, dtype=np.complex128)
+        out = np.empty_like(v)
+        self._check(self._lib.fdga_jvp(self._h, STRATEGIES[strategy], v.ctypes.data, out.ctypes.data, v.size))
+        return out
+
+    def set_U(self, U):
+        self._check(self._lib.fdga_set_U(self._h, float(U)))
+
+    def dchi_dU(self, channel="m", strategy="fdPA", hU=1e-4, restart=40, cycles=4, rtol=1e-10):
+        """dχ/dU(Ω, q) at the converged state (linear response through GMRES), flat [Ω, q] layout."""
+        n = self.get_len("F.a.K1")
+        out = np.empty(n, dtype=np.complex128)
+        its = ctypes.c_int()
+        rel = ctypes.c_double()
+        self._check(self._lib.fdga_dchi_dU(self._h, STRATEGIES[strategy], {"m": 0, "d": 1, "s": 2}[channel],
+                                           float(hU), int(restart), int(cycles), float(rtol), out.ctypes.data, n,
+                                           ctypes.byref(its), ctypes.byref(rel)))
+        return out, {"gmres_iterations": its.value, "relres": rel.value}
+
     def get(self, name):
         n = ctypes.c_size_t()
         self._check(self._lib.fdga_named_len(self._h, name.encode(), ctypes.byref(n)))

@@ -128,6 +128,32 @@ int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double bet
 int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem,
                      int* iters, double* res, double* trace, int* evals);
 
+/* Newton–Krylov solve of the fixed point x = Φ(x): Newton steps (I − J) dx = Φ(x) − x solved by
+ * one GMRES(restart) cycle to an Eisenstat–Walker forcing tolerance, then a backtracking line
+ * search on the FP64 residual.  J is applied as forward differences of the map in jvp_precision
+ * (FDGA_FP64, or FDGA_MIXED for the FP32-contraction map); the state is real-linear, so GMRES
+ * runs on it as a real vector (Krylov basis in FP32, Hessenberg and iterate in FP64).
+ * Convergence is tested on the FP64 residual.  Outputs as fdga_solve_mixed (*iters = Newton
+ * residual evaluations). */
+int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int restart, int jvp_precision,
+                      int* iters, double* res, double* trace, int* evals);
+
+/* Jacobian-vector product of the iteration map at the current state S: Jv = dΦ/dx · v, central
+ * differences with step 1e-5 (1 + ‖x‖₂) along v/‖v‖₂, in the handle's precision.  v and Jv are
+ * host arrays in the flatten(S) layout; J is real-linear (v and i·v give unrelated products). */
+int fdga_jvp(fdga_handle* h, int strategy, const double* v, double* Jv, size_t n);
+
+/* Bare interaction U of the handle (the RefVertex's bare part, the SDE and Hartree terms); the
+ * reference builds a new solver for another U.  Drops the captured graphs. */
+int fdga_set_U(fdga_handle* h, double U);
+
+/* Linear response of the susceptibility to U at a converged state S = x*: solves
+ * (I − J) dx/dU = ∂Φ/∂U by restarted GMRES (central-difference Jacobian; ∂Φ/∂U by central
+ * differences with step hU) and returns dχ/dU(Ω, q) = χ[dx/dU] − (2/U) χ[x*] (χ linear in K1 over
+ * U²), n_out = NΩ1·Nq complex, column-major [Ω, q].  *gmres_iters and *relres report the solve. */
+int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int restart, int cycles, double rtol,
+                 double* out, size_t n_out, int* gmres_iters, double* relres);
+
 /* Named device arrays in the reference layout, for inspection and tests:
  * "G", "Sigma", "Gbare", "G0", "Sigma0", "Pipp", "Piph", "Pi0pp", "Pi0ph", "Lpp", "Lph",
  * "F.<p|t|a>.<K1|K2|K3>", "FL.<p|t|a>.<K2|K3>", "cache_<Gpx|F0p|F0a|F0t|Gpp|Ga|Gt|Fp|Fa|Ft>". */
