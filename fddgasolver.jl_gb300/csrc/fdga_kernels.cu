@@ -1056,20 +1056,22 @@ static cudaError_t launch_k3_tile(cudaStream_t s, const K3Args3& a, int nslots, 
     k_bse_K3_gemm<MODE, TILE, C><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
     return cudaGetLastError();
 }
+int k3_default_tile(int N) { return N <= 16 ? 16 : (N <= 24 ? 24 : 32); }
 template <class C>
-static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d) {
-    const int N = d.N3n;
+static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int tile) {
+    if (tile != 16 && tile != 24 && tile != 32) tile = k3_default_tile(d.N3n);
     if (mode == 0) {
-        if (N <= 16) return launch_k3_tile<0, 16, C>(s, a, nslots, d);
-        if (N <= 24) return launch_k3_tile<0, 24, C>(s, a, nslots, d);
+        if (tile == 16) return launch_k3_tile<0, 16, C>(s, a, nslots, d);
+        if (tile == 24) return launch_k3_tile<0, 24, C>(s, a, nslots, d);
         return launch_k3_tile<0, 32, C>(s, a, nslots, d);
     }
-    if (N <= 16) return launch_k3_tile<1, 16, C>(s, a, nslots, d);
-    if (N <= 24) return launch_k3_tile<1, 24, C>(s, a, nslots, d);
+    if (tile == 16) return launch_k3_tile<1, 16, C>(s, a, nslots, d);
+    if (tile == 24) return launch_k3_tile<1, 24, C>(s, a, nslots, d);
     return launch_k3_tile<1, 32, C>(s, a, nslots, d);
 }
-cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed) {
-    return mixed ? launch_bse_K3_t<cplxf>(s, mode, a, nslots, d) : launch_bse_K3_t<cplx>(s, mode, a, nslots, d);
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed, int tile) {
+    return mixed ? launch_bse_K3_t<cplxf>(s, mode, a, nslots, d, tile)
+                 : launch_bse_K3_t<cplx>(s, mode, a, nslots, d, tile);
 }
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d) {

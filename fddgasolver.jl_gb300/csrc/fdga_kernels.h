@@ -101,7 +101,9 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
 cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d);
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
-cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed);
+// tile: 16, 24 or 32 (the output tile edge of the GEMM kernel); any other value picks the default for Nν3
+cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed, int tile);
+int k3_default_tile(int N);
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d);
 cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,

@@ -10,8 +10,11 @@
 #include <cstring>
 #include <deque>
 #include <functional>
+#include <map>
+#include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/fdga.h"
@@ -76,6 +79,7 @@ struct fdga_handle {
     Group gSig, gK1, gK2pp, gK2ph, gK3pp, gK3ph, gK3ppL, gK3phL;
     Graph graphs[2][2][2][2];  // [precision][strategy][update_sigma][hartree]
     int precision = FDGA_FP64;
+    int k3_tile[2][2] = {{0, 0}, {0, 0}};  // [precision][mode]: K3 GEMM tile chosen by fdga_autotune (0: default)
     int last_launches = 0;
     cudaEvent_t ev[8] = {};
     // Anderson
@@ -460,7 +464,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             }
             a3.blocks = h->d_k3blocks;
             a3.nblocks = h->nk3blocks;
-            LC(launch_bse_K3(s, 0, a3, 3, d, h->precision == FDGA_MIXED));
+            LC(launch_bse_K3(s, 0, a3, 3, d, h->precision == FDGA_MIXED, h->k3_tile[h->precision][0]));
             stage("bse_L_K3_gemm");
             cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
             const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
@@ -500,7 +504,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         }
         a3.blocks = h->d_k3blocks;
         a3.nblocks = h->nk3blocks;
-        LC(launch_bse_K3(s, 1, a3, 3, d, h->precision == FDGA_MIXED));
+        LC(launch_bse_K3(s, 1, a3, 3, d, h->precision == FDGA_MIXED, h->k3_tile[h->precision][1]));
         stage("bse_K3_gemm");
         cplx* out[3] = {chanK(h, h->yS, CH_P, 3), chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3)};
         const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
@@ -1676,6 +1680,201 @@ int fdga_query(fdga_handle* h, const char* key, double* value) {
     if (k == "launches") { *value = h->last_launches; return FDGA_OK; }
     if (k == "precision") { *value = h->precision; return FDGA_OK; }
     return fail(h, FDGA_ERR_ARG, "unknown query key " + k);
+}
+
+int fdga_autotune(fdga_handle* h, int strategy, int* tiles) {
+    if (!h) return FDGA_ERR_ARG;
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (h->c0_dirty) { int r = compute_C0(h); if (r) return r; }
+    // size classes shared by all handles of the process: (Nν3, local, precision) -> (tile L_K3, tile K3)
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int>, std::pair<int, int>> cache;
+    const int prec0 = h->precision;
+    const int cand[3] = {16, 24, 32};
+    for (int prec = FDGA_FP64; prec <= FDGA_MIXED; ++prec) {
+        const auto key = std::make_tuple(h->d.N3n, h->d.local, prec);
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            auto it = cache.find(key);
+            if (it != cache.end()) {
+                h->k3_tile[prec][0] = it->second.first;
+                h->k3_tile[prec][1] = it->second.second;
+                continue;
+            }
+        }
+        double best[2] = {INFINITY, INFINITY};
+        int pick[2] = {0, 0};
+        h->precision = prec;
+        for (int t : cand) {
+            h->k3_tile[prec][0] = h->k3_tile[prec][1] = t;
+            double acc[2] = {0.0, 0.0};
+            for (int rep = 0; rep < 3; ++rep) {
+                std::vector<cudaEvent_t> evs;
+                std::vector<std::string> names;
+                cudaEvent_t e0;
+                CK(cudaEventCreate(&e0));
+                CK(cudaEventRecord(e0, h->st));
+                evs.push_back(e0);
+                StageHook hook = [&](const char* name) {
+                    cudaEvent_t e;
+                    if (cudaEventCreate(&e) != cudaSuccess) return;
+                    cudaEventRecord(e, h->st);
+                    evs.push_back(e);
+                    names.push_back(name);
+                };
+                int nl = 0;
+                int r = enqueue_iteration(h, strategy, true, true, nl, hook);
+                if (r) { h->precision = prec0; return r; }
+                CK(cudaStreamSynchronize(h->st));
+                for (size_t i = 0; i + 1 < evs.size(); ++i) {
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, evs[i], evs[i + 1]);
+                    if (rep > 0 && names[i] == std::string("bse_L_K3_gemm")) acc[0] += ms;
+                    if (rep > 0 && names[i] == std::string("bse_K3_gemm")) acc[1] += ms;
+                }
+                for (auto e : evs) cudaEventDestroy(e);
+            }
+            for (int m = 0; m < 2; ++m)
+                if (acc[m] < best[m]) { best[m] = acc[m]; pick[m] = t; }
+        }
+        h->k3_tile[prec][0] = pick[0];
+        h->k3_tile[prec][1] = pick[1];
+        std::lock_guard<std::mutex> lk(mu);
+        cache[key] = {pick[0], pick[1]};
+    }
+    h->precision = prec0;
+    drop_graphs(h);
+    if (tiles)
+        for (int p = 0; p < 2; ++p)
+            for (int m = 0; m < 2; ++m) tiles[2 * p + m] = h->k3_tile[p][m];
+    return FDGA_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Batches of independent solvers: one CUDA graph holds one iteration of every instance, each
+// instance a branch forked from and joined into the batch stream.
+// ---------------------------------------------------------------------------------------------
+struct fdga_batch {
+    std::vector<fdga_handle*> hs;
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaGraphExec_t exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [strategy][precision]
+    int nodes[2][2] = {{0, 0}, {0, 0}};
+    std::string err;
+};
+
+extern "C" {
+
+int fdga_batch_create(fdga_handle* const* hs, int n, fdga_batch** out) {
+    if (!hs || n < 1 || !out) { g_create_error = "invalid batch arguments"; return FDGA_ERR_ARG; }
+    for (int i = 0; i < n; ++i)
+        if (!hs[i] || !hs[i]->finalized) { g_create_error = "every batch member must be a finalized handle"; return FDGA_ERR_STATE; }
+    fdga_batch* b = new fdga_batch();
+    b->hs.assign(hs, hs + n);
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->ev[0]) != cudaSuccess || cudaEventCreate(&b->ev[1]) != cudaSuccess) {
+        g_create_error = "batch stream/event creation failed";
+        delete b;
+        return FDGA_ERR_CUDA;
+    }
+    b->join.resize(n);
+    for (auto& e : b->join) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    *out = b;
+    return FDGA_OK;
+}
+
+void fdga_batch_destroy(fdga_batch* b) {
+    if (!b) return;
+    for (auto& a : b->exec)
+        for (auto& g : a)
+            if (g) cudaGraphExecDestroy(g);
+    for (auto e : b->join) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (auto e : b->ev) if (e) cudaEventDestroy(e);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+const char* fdga_batch_last_error(const fdga_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+// S_i <- Φ_i(S_i) for every member (iterate_solver! of each), as one graph launch on the batch stream
+int fdga_batch_iterate(fdga_batch* b, int strategy, int precision) {
+    if (!b) return FDGA_ERR_ARG;
+    if ((strategy != FDGA_FDPA && strategy != FDGA_SCPA) || (precision != FDGA_FP64 && precision != FDGA_MIXED)) {
+        b->err = "invalid strategy or precision";
+        return FDGA_ERR_ARG;
+    }
+    cudaGraphExec_t& ex = b->exec[strategy][precision];
+    if (!ex) {
+        for (auto* h : b->hs)
+            if (h->c0_dirty) {
+                int r = compute_C0(h);
+                if (r) { b->err = h->err; return r; }
+            }
+        cudaGraph_t graph;
+        cudaError_t e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { b->err = cudaGetErrorString(e); return FDGA_ERR_CUDA; }
+        e = cudaEventRecord(b->fork, b->st);
+        int total = 0, r = FDGA_OK;
+        for (size_t i = 0; i < b->hs.size() && e == cudaSuccess && r == FDGA_OK; ++i) {
+            fdga_handle* h = b->hs[i];
+            e = cudaStreamWaitEvent(h->st, b->fork, 0);
+            if (e != cudaSuccess) break;
+            const int p0 = h->precision;
+            h->precision = precision;
+            int nl = 0;
+            r = enqueue_iteration(h, strategy, true, true, nl);
+            h->precision = p0;
+            if (r) { b->err = h->err; break; }
+            e = cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st);
+            if (e == cudaSuccess) e = cudaEventRecord(b->join[i], h->st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->join[i], 0);
+            total += nl;
+        }
+        const cudaError_t ee = cudaStreamEndCapture(b->st, &graph);
+        if (r) return r;
+        if (e != cudaSuccess || ee != cudaSuccess) {
+            b->err = std::string("batch capture: ") + cudaGetErrorString(e != cudaSuccess ? e : ee);
+            return FDGA_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&ex, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { ex = nullptr; b->err = cudaGetErrorString(e); return FDGA_ERR_CUDA; }
+        b->nodes[strategy][precision] = total;
+    }
+    const cudaError_t e = cudaGraphLaunch(ex, b->st);
+    if (e != cudaSuccess) { b->err = cudaGetErrorString(e); return FDGA_ERR_CUDA; }
+    return FDGA_OK;
+}
+
+int fdga_batch_synchronize(fdga_batch* b) {
+    if (!b) return FDGA_ERR_ARG;
+    const cudaError_t e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) { b->err = cudaGetErrorString(e); return FDGA_ERR_CUDA; }
+    return FDGA_OK;
+}
+
+// device time of `iters` batch iterations (CUDA events on the batch stream), and the kernels per batch iteration
+int fdga_batch_time(fdga_batch* b, int strategy, int precision, int iters, float* ms, int* kernels) {
+    if (!b || !ms || iters < 1) return FDGA_ERR_ARG;
+    int r = fdga_batch_iterate(b, strategy, precision);  // capture outside the timed region
+    if (r) return r;
+    cudaError_t e = cudaEventRecord(b->ev[0], b->st);
+    for (int i = 0; i < iters && e == cudaSuccess; ++i) {
+        r = fdga_batch_iterate(b, strategy, precision);
+        if (r) return r;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev[1], b->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, b->ev[0], b->ev[1]);
+    if (e != cudaSuccess) { b->err = cudaGetErrorString(e); return FDGA_ERR_CUDA; }
+    if (kernels) *kernels = b->nodes[strategy][precision];
+    return FDGA_OK;
 }
 
 int fdga_launches_per_iteration(const fdga_handle* h, int* n) {

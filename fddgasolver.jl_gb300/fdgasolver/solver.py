@@ -185,6 +185,12 @@ class _Solver:
                                            ctypes.byref(its), ctypes.byref(rel)))
         return out, {"gmres_iterations": its.value, "relres": rel.value}
 
+    def autotune(self, strategy="fdPA"):
+        """Pick the K3 GEMM tiles per size class by timing; returns {fp64: (L_K3, K3), mixed: (L_K3, K3)}."""
+        t = np.zeros(4, dtype=np.int32)
+        self._check(self._lib.fdga_autotune(self._h, STRATEGIES[strategy], t.ctypes.data))
+        return {"fp64": (int(t[0]), int(t[1])), "mixed": (int(t[2]), int(t[3]))}
+
     def get(self, name):
         n = ctypes.c_size_t()
         self._check(self._lib.fdga_named_len(self._h, name.encode(), ctypes.byref(n)))
@@ -330,3 +336,49 @@ def flatten(S):
 
 def unflatten(S, x):
     S.unflatten(x)
+
+
+class Batch:
+    """Independent solvers iterated together: one CUDA graph launch performs one iterate_solver! of
+    every member, the members' kernels running as concurrent graph branches."""
+
+    def __init__(self, solvers):
+        from . import _lib
+        self._lib = _lib.load()
+        self.solvers = list(solvers)
+        arr = (ctypes.c_void_p * len(self.solvers))(*[s._h for s in self.solvers])
+        b = ctypes.c_void_p()
+        rc = self._lib.fdga_batch_create(arr, len(self.solvers), ctypes.byref(b))
+        if rc != 0:
+            raise _lib.FdgaError(rc, self._lib.fdga_create_error().decode())
+        self._b = b
+
+    def _check(self, rc):
+        if rc != 0:
+            from . import _lib
+            raise _lib.FdgaError(rc, (self._lib.fdga_batch_last_error(self._b) or b"").decode())
+
+    def iterate(self, strategy="fdPA", precision="fp64"):
+        self._check(self._lib.fdga_batch_iterate(self._b, STRATEGIES[strategy], {"fp64": 0, "mixed": 1}[precision]))
+
+    def synchronize(self):
+        self._check(self._lib.fdga_batch_synchronize(self._b))
+
+    def time(self, iters, strategy="fdPA", precision="fp64"):
+        """(device ms of `iters` batch iterations, kernels per batch iteration)."""
+        ms = ctypes.c_float()
+        k = ctypes.c_int()
+        self._check(self._lib.fdga_batch_time(self._b, STRATEGIES[strategy], {"fp64": 0, "mixed": 1}[precision],
+                                              int(iters), ctypes.byref(ms), ctypes.byref(k)))
+        return ms.value, k.value
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._lib.fdga_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -11,6 +11,9 @@ config2: Hubbard 8x8, nonlocal fdPA, t=1, t'=0, μ=0, U=2, β=5, nK1=32, nK2=(16
          complex Gaussian noise σ = 0.05 U, symmetrised ν<->ν', scaled 1/sqrt((1+|ν|)(1+|ν'|)).
 config3: Hubbard 16x16, nonlocal fdPA, t=1, t'=-0.2, U=3, β=10, nK1=80, nK2=(40,40), nK3=(20,40), nG=80,
          mΠν_factor=32; μ tuned once on Gbare (Σ = 0) to density n = 0.9 (per-spin occupation 0.45).
+config4: 48 SIAM instances, local fdPA, flat band (D = ∞), e = 0, seeded U ~ U[0.5, 3], β ∈ {5, 10, 20, 40},
+         Γ ~ U[0.3, 1]; boxes scale with β: nK3 = (nν/2, nν) with nν = 16, 32, 48, 64 for β = 5, 10, 20,
+         40, nK2 = (nν, nν), nK1 = nG = 2nν, mΠν_factor = 6 (batch_instances).
 config5: Hubbard 24x24, nonlocal fdPA, t=1, t'=0, μ=0, U=2.5, β=8, nK1=96, nK2=(48,48), nK3=(24,48), nG=96,
          mΠν_factor=32.
 """
@@ -83,3 +86,18 @@ def make_solver(cfg, sym=True):
     if sym:
         S.init_sym_grp()
     return S
+
+
+def batch_instances(n=48, seed=20261204):
+    """The config-4 instance list (see the module docstring)."""
+    rng = np.random.default_rng(seed)
+    nnu_of = {5: 16, 10: 32, 20: 48, 40: 64}
+    out = []
+    for _ in range(n):
+        U = float(rng.uniform(0.5, 3.0))
+        beta = int(rng.choice([5, 10, 20, 40]))
+        gamma = float(rng.uniform(0.3, 1.0))
+        nnu = nnu_of[beta]
+        out.append(dict(kind="siam", T=1.0 / beta, U=U, e=0.0, Delta=gamma, D=float("inf"), nG=2 * nnu, nK1=2 * nnu,
+                        nK2=(nnu, nnu), nK3=(nnu // 2, nnu), mPi_factor=6))
+    return out

@@ -154,6 +154,26 @@ int fdga_set_U(fdga_handle* h, double U);
 int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int restart, int cycles, double rtol,
                  double* out, size_t n_out, int* gmres_iters, double* relres);
 
+/* K3 GEMM tile autotuner: times the 16/24/32 output-tile variants of both K3 contractions on
+ * this handle's data, in FP64 and mixed precision, and keeps the fastest.  Size classes
+ * (Nν3, local/nonlocal, precision) are tuned once per process and shared by all handles.
+ * tiles (4 ints, may be NULL) = {FP64 L_K3, FP64 K3, mixed L_K3, mixed K3}. */
+int fdga_autotune(fdga_handle* h, int strategy, int* tiles);
+
+/* Batches of independent solvers (e.g. many impurity models): one CUDA graph launch performs one
+ * iteration (iterate_solver!, update_Σ, Hartree) of every member; the members' kernels run
+ * concurrently as branches of the graph.  Members must be finalized handles; a handle may belong
+ * to one batch at a time and must not be used on its own while a batch call is in flight. */
+typedef struct fdga_batch fdga_batch;
+int fdga_batch_create(fdga_handle* const* hs, int n, fdga_batch** out);
+void fdga_batch_destroy(fdga_batch* b);
+const char* fdga_batch_last_error(const fdga_batch* b);
+int fdga_batch_iterate(fdga_batch* b, int strategy, int precision);
+int fdga_batch_synchronize(fdga_batch* b);
+/* Device milliseconds of `iters` batch iterations (CUDA events on the batch stream) and the
+ * number of kernels one batch iteration launches. */
+int fdga_batch_time(fdga_batch* b, int strategy, int precision, int iters, float* ms, int* kernels);
+
 /* Named device arrays in the reference layout, for inspection and tests:
  * "G", "Sigma", "Gbare", "G0", "Sigma0", "Pipp", "Piph", "Pi0pp", "Pi0ph", "Lpp", "Lph",
  * "F.<p|t|a>.<K1|K2|K3>", "FL.<p|t|a>.<K2|K3>", "cache_<Gpx|F0p|F0a|F0t|Gpp|Ga|Gt|Fp|Fa|Ft>". */
