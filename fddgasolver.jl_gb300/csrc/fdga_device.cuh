@@ -56,6 +56,13 @@ __host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) {
 }
 __host__ __device__ __forceinline__ cplxf operator*(cplxf a, float s) { return cplxf{a.x * s, a.y * s}; }
 __host__ __device__ __forceinline__ cplxf& operator+=(cplxf& a, cplxf b) { a.x += b.x; a.y += b.y; return a; }
+// c + a·b with four fused multiply-adds (a complex product followed by an add costs six)
+__device__ __forceinline__ cplx cfma(cplx a, cplx b, cplx c) {
+    return cplx{fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y))};
+}
+__device__ __forceinline__ cplxf cfma(cplxf a, cplxf b, cplxf c) {
+    return cplxf{fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y))};
+}
 // conversions between the storage type and the arithmetic type C of a templated kernel
 template <class C> __device__ __forceinline__ C to_c(cplx v);
 template <> __device__ __forceinline__ cplx to_c<cplx>(cplx v) { return v; }

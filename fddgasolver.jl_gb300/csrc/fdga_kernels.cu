@@ -49,7 +49,7 @@ __global__ void k_g_realspace(const cplx* G, cplx* GR, const cplx* tw, Dims d) {
     for (int k = 0; k < NR; ++k) {
         const int kx = k % d.L, ky = k / d.L;
         const int ph = (kx * Rx + ky * Ry) % d.L;
-        s += G[(size_t)k * d.NG + nu] * tw[ph];
+        s = cfma(G[(size_t)k * d.NG + nu], tw[ph], s);
     }
     GR[i] = s * (1.0 / NR);
 }
@@ -110,7 +110,7 @@ __global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
         const int Px = r % L, y = r / L;
         const cplx* a = A + (size_t)row * NR + (size_t)y * L;
         cplx s = mk(0, 0);
-        for (int x = 0; x < L; ++x) s += a[x] * twp[(Px * x) % L];
+        for (int x = 0; x < L; ++x) s = cfma(a[x], twp[(Px * x) % L], s);
         B[(size_t)row * NR + r] = s;
     }
     __syncthreads();
@@ -124,7 +124,7 @@ __global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
         if (n >= d.nPw) continue;
         const cplx* b = B + (size_t)(which * TV + v) * NR;
         cplx s = mk(0, 0);
-        for (int y = 0; y < L; ++y) s += b[(size_t)y * L + Px] * twp[(Py * y) % L];
+        for (int y = 0; y < L; ++y) s = cfma(b[(size_t)y * L + Px], twp[(Py * y) % L], s);
         (which ? ph : pp)[ixPi(d, P, m, n)] = s;
     }
 }
@@ -276,7 +276,7 @@ __global__ void k_dft2_rows(const cplx* in, cplx* out, int rows, int L, const cp
     const int r = (int)(i % rows), R = (int)(i / rows);
     const int Rx = R % L, Ry = R / L;
     cplx acc = mk(0, 0);
-    for (int P = 0; P < NR; ++P) acc += in[(size_t)P * rows + r] * tw[((P % L) * Rx + (P / L) * Ry) % L];
+    for (int P = 0; P < NR; ++P) acc = cfma(in[(size_t)P * rows + r], tw[((P % L) * Rx + (P / L) * Ry) % L], acc);
     out[i] = acc * scale;
 }
 
@@ -375,16 +375,16 @@ __global__ void k_pisum_R(const cplx* GR, cplx* SR, Dims d) {
     cplx acc = mk(0, 0);
     if (R == 0) {
         for (int n = -d.nPn + lane; n < d.nPn; n += 32)
-            acc += which ? g_tail(GR, d, 0, m + n) * g_tail(GR, d, 0, n) : g_tail(GR, d, 0, m - n - 1) * g_tail(GR, d, 0, n);
+            acc = cfma(which ? g_tail(GR, d, 0, m + n) : g_tail(GR, d, 0, m - n - 1), g_tail(GR, d, 0, n), acc);
     } else {
         for (int n = -d.nG + lane; n < d.nG; n += 32) {
             if (!fin(n, d.nPn)) continue;
             if (which) {
                 const int b = m + n;
-                if (fin(b, d.nG)) acc += GR[ixG(d, R, b)] * GR[ixG(d, mR, n)];
+                if (fin(b, d.nG)) acc = cfma(GR[ixG(d, R, b)], GR[ixG(d, mR, n)], acc);
             } else {
                 const int a = m - n - 1;
-                if (fin(a, d.nG)) acc += GR[ixG(d, R, a)] * GR[ixG(d, R, n)];
+                if (fin(a, d.nG)) acc = cfma(GR[ixG(d, R, a)], GR[ixG(d, R, n)], acc);
             }
         }
     }
@@ -441,7 +441,7 @@ __device__ __forceinline__ void bse_K1_body(const VertP& F, const FLP& FL, const
             const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
             const size_t ip = ixPi(d, P, m, n);
             const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
-            acc += Fl * ((pi - pi0) * d.U + pi * FLr);
+            acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * d.U), acc);
         }
     }
     acc = warp_sum(acc);
@@ -471,16 +471,16 @@ __device__ __forceinline__ void bse_L_K2_body(const VertP& F, const cplx* Pi0, c
     if (d.local) {
         for (int n = -d.nPw + lane; n < d.nPw; n += 32) {  // local solver: nPw = nPn
             const cplx Gp = vert_eval(F, d, CH, SP, m, nu, n, P, IRR);
-            acc += Gp * ldg(Pi0 + ixPi(d, P, m, n)) * d.U;
+            acc = cfma(Gp, ldg(Pi0 + ixPi(d, P, m, n)), acc);
         }
     } else {
         for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
             const cplx Gl = vert_eval(F, d, CH, SP, m, nu, cross(CH, m, n), P, IRR);
-            acc += Gl * ldg(Pi0 + ixPi(d, P, m, n)) * d.U;
+            acc = cfma(Gl, ldg(Pi0 + ixPi(d, P, m, n)), acc);
         }
     }
     acc = warp_sum(acc);
-    if (lane == 0) out[idx] = acc * (d.T * (CH == CH_T ? -1.0 : 1.0));
+    if (lane == 0) out[idx] = acc * (d.U * d.T * (CH == CH_T ? -1.0 : 1.0));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -522,7 +522,7 @@ __device__ __forceinline__ void bse_K2_body(const VertP& F, const FLP& FL, const
         const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
         const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
-        acc += Fl * ((pi - pi0) * d.U + pi * FLr);
+        acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * d.U), acc);
     }
     acc = warp_sum(acc);
     if (lane == 0) {
@@ -600,10 +600,10 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
         for (int kk = 0; kk < TK; ++kk) {
             const C a0 = As[ty][kk], a1 = As[ty + H][kk];
             const C b0 = Ms[kk][tx], b1 = Ms[kk][tx + H];
-            acc[0][0] += a0 * b0;
-            acc[0][1] += a0 * b1;
-            acc[1][0] += a1 * b0;
-            acc[1][1] += a1 * b1;
+            acc[0][0] = cfma(a0, b0, acc[0][0]);
+            acc[0][1] = cfma(a0, b1, acc[0][1]);
+            acc[1][0] = cfma(a1, b0, acc[1][0]);
+            acc[1][1] = cfma(a1, b1, acc[1][1]);
         }
         __syncthreads();
     }
@@ -651,14 +651,14 @@ __device__ __forceinline__ void sde_L_body(const VertP& F, const cplx* Pi, const
                 const int n = m - (t - d.n2n) - 1;  // Ω-ω runs over the K2 box
                 if (!fin(n, d.nPw)) continue;
                 const cplx g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P) - c;
-                acc += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
+                acc = cfma(ldg(Pi + ixPi(d, P, m, n)), g, acc);
             }
         } else {
             c = chan_eval(F.g[CH_T], d, m, nu, FINF, P) + chan_eval(F.g[CH_A], d, m, nu, FINF, P);
             for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
                 if (!fin(n, d.nPw)) continue;
                 const cplx g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P) - c;
-                acc += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
+                acc = cfma(ldg(Pi + ixPi(d, P, m, n)), g, acc);
             }
         }
     }
@@ -670,11 +670,11 @@ __device__ __forceinline__ void sde_L_body(const VertP& F, const cplx* Pi, const
             cplx g;
             if (WHICH == 0) g = ref_pSp(F, d, CH_P, m, m - n - 1, nu) - mk(d.U, 0);
             else g = ref_pSp(F, d, CH_A, m, nu, n) + ref_pSp(F, d, CH_T, m, nu, n) - mk(d.U, 0) - mk(d.U, 0);
-            accr += ldg(Pi + ixPi(d, P, m, n)) * d.U * g;
+            accr = cfma(ldg(Pi + ixPi(d, P, m, n)), g, accr);
         }
     }
-    acc = warp_sum(acc);
-    accr = warp_sum(accr);
+    acc = warp_sum(acc) * d.U;
+    accr = warp_sum(accr) * d.U;
     if (lane == 0) {
         if (use_vertex) acc += c * (ldg(SPi + (size_t)P * d.NPO + (m + d.nPO - 1)) * d.U);
         out[idx] = acc * d.T + accr * (d.T * ref_scale);
@@ -759,8 +759,8 @@ __global__ void k_sde_sigma_R(const cplx* GR, const cplx* LppR, const cplx* LphR
         for (int t = lane; t < d.N2O; t += 32) {
             const int m = t - (d.n2O - 1);
             const int a = m - nu - 1, b = m + nu;
-            if (fin(a, d.nG)) acc += GR[ixG(d, mR, a)] * LppR[ix2(d, R, m, nu)];
-            if (fin(b, d.nG)) acc += GR[ixG(d, R, b)] * LphR[ix2(d, mR, m, nu)];
+            if (fin(a, d.nG)) acc = cfma(GR[ixG(d, mR, a)], LppR[ix2(d, R, m, nu)], acc);
+            if (fin(b, d.nG)) acc = cfma(GR[ixG(d, R, b)], LphR[ix2(d, mR, m, nu)], acc);
         }
     }
     acc = warp_sum(acc);
@@ -783,7 +783,7 @@ __global__ void k_u2_corr(const cplx* GR, cplx* C, Dims d) {
     for (int n1 = -d.nG + lane; n1 < d.nG; n1 += 32) {
         const int n3 = n1 + s;
         if (!fin(n3, d.nG)) continue;
-        acc += GR[ixG(d, mR, n1)] * GR[ixG(d, R, n3)];
+        acc = cfma(GR[ixG(d, mR, n1)], GR[ixG(d, R, n3)], acc);
     }
     acc = warp_sum(acc);
     if (lane == 0) C[w] = acc;
@@ -798,7 +798,7 @@ __global__ void k_u2_sum(const cplx* GR, const cplx* C, cplx* out, Dims d) {
     cplx acc = mk(0, 0);
     for (int n2 = -d.nG + lane; n2 < d.nG; n2 += 32) {
         const int s = nu - n2;  // in [-(2nG-1), 2nG-1]
-        acc += GR[ixG(d, R, n2)] * C[(size_t)R * NS + (s + d.NG - 1)];
+        acc = cfma(GR[ixG(d, R, n2)], C[(size_t)R * NS + (s + d.NG - 1)], acc);
     }
     acc = warp_sum(acc);
     if (lane == 0) out[w] = acc * (d.U * d.U * d.T * d.T);
