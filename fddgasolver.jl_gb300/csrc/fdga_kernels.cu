@@ -834,14 +834,15 @@ __global__ void k_scatter(cplx* dst, const cplx* src, const uint32_t* perm, size
     if (i < n) dst[perm[i]] = src[i];
 }
 // fx = y - x ; g = x + beta fx ; partial max|fx|² per block (the host takes the square root of the
-// maximum, which equals the maximum of |fx| since the square root is monotone)
+// maximum, which equals the maximum of |fx| since the square root is monotone).  x == nullptr
+// reads as zero; fx and g may be nullptr (not written).
 __global__ void k_residual(const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax, size_t n) {
     __shared__ double red[256];
     double mx = 0.0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const cplx f = y[i] - x[i];
-        fx[i] = f;
-        if (g) g[i] = x[i] + f * beta;
+        const cplx f = x ? y[i] - x[i] : y[i];
+        if (fx) fx[i] = f;
+        if (g && x) g[i] = x[i] + f * beta;
         mx = fmax(mx, f.x * f.x + f.y * f.y);
     }
     red[threadIdx.x] = mx;

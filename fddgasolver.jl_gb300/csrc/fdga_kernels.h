@@ -151,14 +151,27 @@ cudaError_t measure_fp64_rate(float* ms, double* gflops);
 cudaError_t launch_kr_point(cudaStream_t s, int nblk, const cplx* x, const cplxf* v, double eps, cplx* xp, size_t n);
 cudaError_t launch_kr_apply(cudaStream_t s, int nblk, const cplx* y, const cplx* y0, const cplxf* v, double a,
                             double b, cplxf* w, size_t n);
-cudaError_t launch_kr_dots(cudaStream_t s, int nblk, const KrVecs& V, int nv, const cplxf* w, double* part,
-                           int norm_slot, size_t n);
+cudaError_t launch_kr_dots(cudaStream_t s, int nblk, const KrVecs& V, int nv, const cplxf* w, const float* wgt,
+                           double* part, int norm_slot, size_t n);
 cudaError_t launch_kr_reduce(cudaStream_t s, const double* part, int np, int ncoef, double* coef);
 cudaError_t launch_kr_sub(cudaStream_t s, int nblk, const KrVecs& V, int nv, const double* c, cplxf* w, size_t n);
 cudaError_t launch_kr_scale(cudaStream_t s, int nblk, const cplxf* w, double nrm, cplxf* out, size_t n);
 cudaError_t launch_kr_update(cudaStream_t s, int nblk, cplx* x, const KrVecs& V, int nv, const double* y, double scale,
                              size_t n);
-cudaError_t launch_kr_load(cudaStream_t s, int nblk, const cplx* a, cplxf* out, double* part, size_t n);
+cudaError_t launch_kr_load(cudaStream_t s, int nblk, const cplx* a, const float* wgt, cplxf* out, double* part,
+                           size_t n);
+// symmetric-subspace (one value per symmetry class) storage of Krylov vectors
+cudaError_t launch_kc_point(cudaStream_t s, int nblk, const cplx* x, const cplxf* v, const uint32_t* code, double eps,
+                            cplx* xp, size_t n);
+cudaError_t launch_kc_axpy(cudaStream_t s, int nblk, const cplx* x, const cplx* d, const uint32_t* code, double lam,
+                           cplx* out, size_t n);
+cudaError_t launch_kc_apply(cudaStream_t s, int nblk, const cplx* y, const cplx* y0, const uint32_t* pos,
+                            const cplxf* v, double a, double b, cplxf* w, size_t nc);
+cudaError_t launch_kc_gather(cudaStream_t s, int nblk, const cplx* y, const cplx* x, const uint32_t* pos, double sc,
+                             cplx* out, size_t nc);
+cudaError_t launch_kc_count(cudaStream_t s, int nblk, const uint32_t* code, float* w, size_t n);
+cudaError_t launch_kc_codes(cudaStream_t s, const uint32_t* map, const int* items, int nitems, size_t nblock,
+                            size_t base, uint32_t off, uint32_t* code, uint32_t* pos);
 cudaError_t launch_kr_resid(cudaStream_t s, int nblk, const cplx* b, const cplxf* v, double alpha, const cplx* y,
                             const cplx* yb, double beta, cplx* r, size_t n);
 cudaError_t launch_kr_axpby(cudaStream_t s, int nblk, cplx* out, const cplx* a, double lam, const cplx* b, size_t n);

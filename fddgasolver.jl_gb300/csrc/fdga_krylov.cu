@@ -63,19 +63,21 @@ __global__ void __launch_bounds__(RT) k_kr_apply(const cplx* y, const cplx* y0, 
 
 // partials of Re<V_i, w> for the CHUNK vectors of chunk blockIdx.y: part[i * np + block]; when
 // norm_slot >= 0 the chunk-0 blocks also write the partial of |w|² to part[norm_slot * np + block]
-__global__ void __launch_bounds__(RT) k_kr_dots(KrVecs V, int nv, const cplxf* w, double* part, int np, int norm_slot,
-                                                size_t n) {
+__global__ void __launch_bounds__(RT) k_kr_dots(KrVecs V, int nv, const cplxf* w, const float* wgt, double* part,
+                                                int np, int norm_slot, size_t n) {
     __shared__ double sh[RT];
     const int i0 = blockIdx.y * CHUNK;
     const int cnt = max(0, min(CHUNK, nv - i0));
     const bool with_norm = norm_slot >= 0 && blockIdx.y == 0;
     RAcc a[CHUNK], an;
     for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
-        const cplxf wi = w[i];
+        cplxf wi = w[i];
+        const cplxf wraw = wi;
+        if (wgt) wi = wi * wgt[i];  // class-size weight of a compact (representative) entry
 #pragma unroll
         for (int j = 0; j < CHUNK; ++j)
             if (j < cnt) a[j].add(rdot(V.v[i0 + j][i], wi));
-        if (with_norm) an.add(rdot(wi, wi));
+        if (with_norm) an.add(rdot(wraw, wi));
     }
     for (int j = 0; j < cnt; ++j) store_partial(a[j].total(), sh, part + (size_t)(i0 + j) * np);
     if (with_norm) store_partial(an.total(), sh, part + (size_t)norm_slot * np);
@@ -136,16 +138,83 @@ __global__ void __launch_bounds__(RT) k_kr_update(cplx* x, KrVecs V, int nv, con
     }
 }
 
-// out = a (FP64 -> FP32 copy), partial |a|²
-__global__ void __launch_bounds__(RT) k_kr_load(const cplx* a, cplxf* out, double* part, size_t n) {
+// out = a (FP64 -> FP32 copy), partial of the (weighted) |a|²
+__global__ void __launch_bounds__(RT) k_kr_load(const cplx* a, const float* wgt, cplxf* out, double* part, size_t n) {
     __shared__ double sh[RT];
     double s = 0.0;
     for (size_t t = blockIdx.x * (size_t)RT + threadIdx.x; t < n; t += (size_t)gridDim.x * RT) {
         const cplx v = a[t];
         out[t] = tof(v);
-        s += v.x * v.x + v.y * v.y;
+        s += (v.x * v.x + v.y * v.y) * (wgt ? (double)wgt[t] : 1.0);
     }
     store_partial(s, sh, part);
+}
+
+// Symmetric-subspace (representative) storage.  Every iterate, residual and Jacobian-vector
+// product of the map is invariant under the solver's symmetry groups (the map expands its class
+// representatives), so Krylov vectors are kept as one value per class: code[j] = compact index * 4
+// + operation of full element j, pos[i] = full index of compact entry i.
+
+// xp[j] = x[j] + ε op_j(v[code_j])   (v compact FP32)
+__global__ void __launch_bounds__(RT) k_kc_point(const cplx* x, const cplxf* v, const uint32_t* code, double eps,
+                                                 cplx* xp, size_t n) {
+    for (size_t j = blockIdx.x * (size_t)RT + threadIdx.x; j < n; j += (size_t)gridDim.x * RT) {
+        const uint32_t c = code[j];
+        xp[j] = x[j] + apply_op((int)(c & 3u), to_d(v[c >> 2])) * eps;
+    }
+}
+// out[j] = x[j] + λ op_j(d[code_j])   (d compact FP64)
+__global__ void __launch_bounds__(RT) k_kc_axpy(const cplx* x, const cplx* d, const uint32_t* code, double lam,
+                                                cplx* out, size_t n) {
+    for (size_t j = blockIdx.x * (size_t)RT + threadIdx.x; j < n; j += (size_t)gridDim.x * RT) {
+        const uint32_t c = code[j];
+        out[j] = x[j] + apply_op((int)(c & 3u), d[c >> 2]) * lam;
+    }
+}
+// w[i] = a·v[i] + b·(y[pos_i] − y0[i])   (y full FP64, y0 compact FP64 or null, w compact FP32)
+__global__ void __launch_bounds__(RT) k_kc_apply(const cplx* y, const cplx* y0, const uint32_t* pos, const cplxf* v,
+                                                 double a, double b, cplxf* w, size_t nc) {
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < nc; i += (size_t)gridDim.x * RT) {
+        cplx d = y[pos[i]];
+        if (y0) d -= y0[i];
+        d = d * b;
+        if (v) d += to_d(v[i]) * a;
+        w[i] = tof(d);
+    }
+}
+// out[i] = (y[pos_i] − x[pos_i]) · s  (x may be null)   compact FP64 gather of a full difference
+__global__ void __launch_bounds__(RT) k_kc_gather(const cplx* y, const cplx* x, const uint32_t* pos, double s,
+                                                  cplx* out, size_t nc) {
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < nc; i += (size_t)gridDim.x * RT) {
+        cplx d = y[pos[i]];
+        if (x) d -= x[pos[i]];
+        out[i] = d * s;
+    }
+}
+// class sizes: w[code_j >> 2] += 1
+__global__ void __launch_bounds__(RT) k_kc_count(const uint32_t* code, float* w, size_t n) {
+    for (size_t j = blockIdx.x * (size_t)RT + threadIdx.x; j < n; j += (size_t)gridDim.x * RT)
+        atomicAdd(&w[code[j] >> 2], 1.0f);
+}
+// compact codes of one state block from its group map (rep*4 + op; nullptr = identity) and its
+// sorted representative list: code = (off + lower_bound(items, rep)) * 4 + op
+__global__ void __launch_bounds__(RT) k_kc_codes(const uint32_t* map, const int* items, int nitems, size_t nblock,
+                                                 size_t base, uint32_t off, uint32_t* code, uint32_t* pos) {
+    for (size_t j = blockIdx.x * (size_t)RT + threadIdx.x; j < nblock; j += (size_t)gridDim.x * RT) {
+        uint32_t rep = (uint32_t)j, op = 0;
+        if (map) { rep = map[j] >> 2; op = map[j] & 3u; }
+        uint32_t ci = rep;
+        if (items) {
+            int lo = 0, hi = nitems;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if ((uint32_t)items[mid] < rep) lo = mid + 1; else hi = mid;
+            }
+            ci = (uint32_t)lo;
+        }
+        code[base + j] = ((off + ci) << 2) | op;
+        if (rep == (uint32_t)j) pos[off + ci] = (uint32_t)(base + j);
+    }
 }
 
 // r = b + α v + β (y − yb)   (FP64; v FP32 or null)
@@ -180,11 +249,11 @@ cudaError_t launch_kr_apply(cudaStream_t s, int nblk, const cplx* y, const cplx*
     k_kr_apply<<<nblk, RT, 0, s>>>(y, y0, v, a, b, w, n);
     KR_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_kr_dots(cudaStream_t s, int nblk, const KrVecs& V, int nv, const cplxf* w, double* part,
-                           int norm_slot, size_t n) {
+cudaError_t launch_kr_dots(cudaStream_t s, int nblk, const KrVecs& V, int nv, const cplxf* w, const float* wgt,
+                           double* part, int norm_slot, size_t n) {
     if (nv > KR_MAX) return cudaErrorInvalidValue;
     const int chunks = std::max(1, (nv + CHUNK - 1) / CHUNK);
-    k_kr_dots<<<dim3(nblk, chunks), RT, 0, s>>>(V, nv, w, part, nblk, norm_slot, n);
+    k_kr_dots<<<dim3(nblk, chunks), RT, 0, s>>>(V, nv, w, wgt, part, nblk, norm_slot, n);
     KR_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_kr_reduce(cudaStream_t s, const double* part, int np, int ncoef, double* coef) {
@@ -206,8 +275,39 @@ cudaError_t launch_kr_update(cudaStream_t s, int nblk, cplx* x, const KrVecs& V,
     k_kr_update<<<nblk, RT, 0, s>>>(x, V, nv, y, scale, n);
     KR_CHECK(); return cudaSuccess;
 }
-cudaError_t launch_kr_load(cudaStream_t s, int nblk, const cplx* a, cplxf* out, double* part, size_t n) {
-    k_kr_load<<<nblk, RT, 0, s>>>(a, out, part, n);
+cudaError_t launch_kr_load(cudaStream_t s, int nblk, const cplx* a, const float* wgt, cplxf* out, double* part,
+                           size_t n) {
+    k_kr_load<<<nblk, RT, 0, s>>>(a, wgt, out, part, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_point(cudaStream_t s, int nblk, const cplx* x, const cplxf* v, const uint32_t* code, double eps,
+                            cplx* xp, size_t n) {
+    k_kc_point<<<nblk, RT, 0, s>>>(x, v, code, eps, xp, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_axpy(cudaStream_t s, int nblk, const cplx* x, const cplx* d, const uint32_t* code, double lam,
+                           cplx* out, size_t n) {
+    k_kc_axpy<<<nblk, RT, 0, s>>>(x, d, code, lam, out, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_apply(cudaStream_t s, int nblk, const cplx* y, const cplx* y0, const uint32_t* pos,
+                            const cplxf* v, double a, double b, cplxf* w, size_t nc) {
+    k_kc_apply<<<nblk, RT, 0, s>>>(y, y0, pos, v, a, b, w, nc);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_gather(cudaStream_t s, int nblk, const cplx* y, const cplx* x, const uint32_t* pos, double sc,
+                             cplx* out, size_t nc) {
+    k_kc_gather<<<nblk, RT, 0, s>>>(y, x, pos, sc, out, nc);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_count(cudaStream_t s, int nblk, const uint32_t* code, float* w, size_t n) {
+    k_kc_count<<<nblk, RT, 0, s>>>(code, w, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_codes(cudaStream_t s, const uint32_t* map, const int* items, int nitems, size_t nblock,
+                            size_t base, uint32_t off, uint32_t* code, uint32_t* pos) {
+    const unsigned g = (unsigned)std::min<size_t>((nblock + RT - 1) / RT, 65535u * 16u);
+    k_kc_codes<<<g, RT, 0, s>>>(map, items, nitems, nblock, base, off, code, pos);
     KR_CHECK(); return cudaSuccess;
 }
 

@@ -86,9 +86,16 @@ struct fdga_handle {
     std::vector<cplx*> aa_buf;
     double* d_part = nullptr;
     cplx *aa_R = nullptr, *aa_rot = nullptr, *aa_gam = nullptr, *aa_part = nullptr;  // device QR state
-    std::vector<cplx*> kr64;       // Newton-Krylov / linear response: x, y0, F, dx, yb, r, y+
-    std::vector<cplxf*> kr32;      // Krylov basis V[0..m] (FP32), w, scratch
+    std::vector<cplx*> kr64;       // Newton-Krylov / linear response, compact (one value per class) FP64
+    std::vector<cplxf*> kr32;      // Krylov basis V[0..m], w, scratch: compact FP32
+    size_t kr_nc = 0;              // compact length the kr buffers were sized for
+    cplx* kr_x = nullptr;          // full FP64 Newton iterate / fixed point
+    std::vector<cplx*> jv;         // fdga_jvp work vectors (full FP64)
     double *kr_part = nullptr, *kr_coef = nullptr;
+    uint32_t *kc_code = nullptr, *kc_pos = nullptr;  // compact index of the state (symmetry classes)
+    float* kc_w = nullptr;                           // class sizes
+    size_t nc = 0;
+    int groups_version = 0, kc_version = -1;
     std::vector<cplx*> ma_buf64;   // mixed solver: defect, g, g_old
     std::vector<cplxf*> ma_buf32;  // mixed solver: f, Δf, Q, Δg (FP32 history)
     std::vector<void*> allocs;
@@ -813,6 +820,7 @@ int fdga_init_sym_grp(fdga_handle* h) {
     if (!h) return FDGA_ERR_ARG;
     std::vector<HostGroup> hg;
     compute_all_groups(h->d, hg);
+    ++h->groups_version;
     Group* dst[8] = {&h->gSig, &h->gK1, &h->gK2pp, &h->gK2ph, &h->gK3pp, &h->gK3ph, &h->gK3ppL, &h->gK3phL};
     for (int i = 0; i < 8; ++i) {
         int r = upload_group(h, *dst[i], hg[i]);
@@ -1138,36 +1146,77 @@ int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, doub
 
 // ---------------------------------------------------------------------------------------------
 // Newton–Krylov and linear response (GMRES on A = I − J, J the forward- or central-difference
-// Jacobian of the iteration map, real inner products; the kernels are in fdga_krylov.cu)
+// Jacobian of the iteration map, real inner products; the kernels are in fdga_krylov.cu).
+// Krylov vectors live in the symmetric subspace: one value per symmetry class of every state
+// block, inner products weighted by the class sizes (equal to the full-vector inner products).
 // ---------------------------------------------------------------------------------------------
 namespace {
 
-int ensure_krylov(fdga_handle* h, int m) {
+// compact (one value per class) index of the state: code[j] = compact*4 + op, pos[i] = full index
+int ensure_compact(fdga_handle* h) {
+    if (h->kc_code && h->kc_version == h->groups_version) return FDGA_OK;
     const size_t n = h->nstate;
-    while (h->kr64.size() < 7) {
+    if (!h->kc_code) {
+        AL(h->kc_code, n);
+        AL(h->kc_pos, n);
+        AL(h->kc_w, n);
+    }
+    struct Blk { const Group* g; size_t base, len; };
+    std::vector<Blk> blk;
+    for (int ch : {CH_P, CH_T, CH_A}) {
+        const size_t off = (size_t)ch * h->nchan;
+        blk.push_back({&h->gK1, off, h->n1});
+        blk.push_back({ch == CH_P ? &h->gK2pp : &h->gK2ph, off + h->n1, h->n2});
+        blk.push_back({ch == CH_P ? &h->gK3pp : &h->gK3ph, off + h->n1 + h->n2, h->n3});
+    }
+    blk.push_back({&h->gSig, 3 * h->nchan, h->nGk});
+    uint32_t off = 0;
+    for (const auto& b : blk) {
+        const bool triv = b.g->trivial;
+        CK(launch_kc_codes(h->st, triv ? nullptr : b.g->d_map, triv ? nullptr : b.g->d_items,
+                           triv ? (int)b.len : b.g->nitems, b.len, b.base, off, h->kc_code, h->kc_pos));
+        off += triv ? (uint32_t)b.len : (uint32_t)b.g->nitems;
+    }
+    h->nc = off;
+    CK(cudaMemsetAsync(h->kc_w, 0, h->nc * sizeof(float), h->st));
+    CK(launch_kc_count(h->st, NBLK_RED, h->kc_code, h->kc_w, n));
+    CK(cudaStreamSynchronize(h->st));
+    h->kc_version = h->groups_version;
+    return FDGA_OK;
+}
+
+// buffers: compact FP64 [yb, F, dx, r, yp, tmp], compact FP32 [V0..Vm, w, scratch], full FP64 [x]
+int ensure_krylov(fdga_handle* h, int m) {
+    int r = ensure_compact(h);
+    if (r) return r;
+    const size_t nc = h->nc;
+    if (h->kr_nc != nc) {  // compact length changed (symmetry groups set): drop the compact buffers
+        h->kr64.clear();
+        h->kr32.clear();
+        h->kr_nc = nc;
+    }
+    while (h->kr64.size() < 6) {
         cplx* p = nullptr;
-        int r = dalloc(h, &p, n);
-        if (r) return r;
+        if ((r = dalloc(h, &p, nc))) return r;
         h->kr64.push_back(p);
     }
     while (h->kr32.size() < (size_t)m + 3) {
         cplxf* p = nullptr;
-        int r = dalloc(h, &p, n);
-        if (r) return r;
+        if ((r = dalloc(h, &p, nc))) return r;
         h->kr32.push_back(p);
     }
+    if (!h->kr_x && (r = dalloc(h, &h->kr_x, h->nstate))) return r;
     if (!h->kr_part) {
-        int r = dalloc(h, &h->kr_part, (size_t)(KR_MAX + 2) * NBLK_RED);
+        r = dalloc(h, &h->kr_part, (size_t)(KR_MAX + 2) * NBLK_RED);
         if (!r) r = dalloc(h, &h->kr_coef, 4 * (size_t)(KR_MAX + 2));
         if (r) return r;
     }
     return FDGA_OK;
 }
 
-// 2-norm of an FP64 device vector as a real 2n-vector (scratch: an FP32 vector)
-int norm2_64(fdga_handle* h, const cplx* a, cplxf* scratch, double& out) {
-    const size_t n = h->nstate;
-    CK(launch_kr_load(h->st, NBLK_RED, a, scratch, h->kr_part, n));
+// weighted 2-norm of a compact FP64 vector (scratch: a compact FP32 vector)
+int cnorm(fdga_handle* h, const cplx* a, cplxf* scratch, double& out) {
+    CK(launch_kr_load(h->st, NBLK_RED, a, h->kc_w, scratch, h->kr_part, h->nc));
     CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, 1, h->kr_coef));
     double v = 0.0;
     CK(cudaMemcpyAsync(&v, h->kr_coef, sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -1176,47 +1225,57 @@ int norm2_64(fdga_handle* h, const cplx* a, cplxf* scratch, double& out) {
     return FDGA_OK;
 }
 
-// A v = v − J v at the base point xb (yb = Φ(xb)) for the unit FP32 direction v, into w (FP32).
-// Forward: J v = (Φ(xb + εv) − yb)/ε.  Central: J v = (Φ(xb + εv) − Φ(xb − εv))/(2ε).
+// max over the compact entries of |a|  (= the full max norm of a symmetric vector)
+int cmax(fdga_handle* h, const cplx* a, double& out) {
+    int status = 0;
+    CK(launch_residual(h->st, a, nullptr, nullptr, nullptr, 0.0, h->d_part, NBLK_RED, h->nc));
+    out = reduce_max(h, NBLK_RED, status);
+    return status;
+}
+
+// A v = v − J v at the base point xb (full) for the unit compact FP32 direction v, into w.
+// Forward: J v = (Φ(xb + εv) − yb)/ε (yb compact).  Central: (Φ(xb + εv) − Φ(xb − εv))/(2ε).
 int apply_A(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplxf* v, double eps, bool central,
-            cplx* ytmp, cplxf* w, int& nmaps) {
-    const size_t n = h->nstate;
-    CK(launch_kr_point(h->st, NBLK_RED, xb, v, eps, h->xS, n));
+            cplxf* w, int& nmaps) {
+    const size_t n = h->nstate, nc = h->nc;
+    CK(launch_kc_point(h->st, NBLK_RED, xb, v, h->kc_code, eps, h->xS, n));
     int r = run_iteration(h, strategy, true, true);
     if (r) return r;
     ++nmaps;
     if (!central) {
-        CK(launch_kr_apply(h->st, NBLK_RED, h->yS, yb, v, 1.0, -1.0 / eps, w, n));
+        CK(launch_kc_apply(h->st, NBLK_RED, h->yS, yb, h->kc_pos, v, 1.0, -1.0 / eps, w, nc));
         return FDGA_OK;
     }
-    CK(cudaMemcpyAsync(ytmp, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-    CK(launch_kr_point(h->st, NBLK_RED, xb, v, -eps, h->xS, n));
+    cplx* yp = h->kr64[4];
+    CK(launch_kc_gather(h->st, NBLK_RED, h->yS, nullptr, h->kc_pos, 1.0, yp, nc));
+    CK(launch_kc_point(h->st, NBLK_RED, xb, v, h->kc_code, -eps, h->xS, n));
     r = run_iteration(h, strategy, true, true);
     if (r) return r;
     ++nmaps;
-    CK(launch_kr_apply(h->st, NBLK_RED, ytmp, h->yS, v, 1.0, -0.5 / eps, w, n));
+    CK(launch_kc_apply(h->st, NBLK_RED, h->yS, yp, h->kc_pos, v, 1.0, 0.5 / eps, w, nc));  // v + (y− − y+)/(2ε)
     return FDGA_OK;
 }
 
-// Restarted GMRES(m) for A dx = b, dx starting at 0.  Cycles after the first restart from the
-// true residual b − A dx (one more A application).  relres = final ‖b − A dx‖/‖b‖ estimate.
+// Restarted GMRES(m) for A dx = b (compact vectors), dx starting at 0.  Cycles after the first
+// restart from the true residual b − A dx.  relres = final ‖b − A dx‖/‖b‖ estimate.
 int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplx* b, cplx* dx, int m,
                 int cycles, double rtol, double eps_rel, bool central, int max_maps, int& nmaps, int& iters,
                 double& relres) {
-    const size_t n = h->nstate;
-    int r = ensure_krylov(h, m);
-    if (r) return r;
+    const size_t nc = h->nc;
     KrVecs V{};
     for (int i = 0; i <= m; ++i) V.v[i] = h->kr32[i];
     const std::vector<cplxf*>& Vw = h->kr32;  // the same basis, writable
     cplxf* w = h->kr32[m + 1];
     cplxf* sc = h->kr32[m + 2];
-    cplx* rr = h->kr64[5];
-    cplx* ytmp = h->kr64[6];  // Φ(xb + εv) of a central difference
+    cplx* rr = h->kr64[3];
+    cplx* xc = h->kr64[5];
+    const float* W = h->kc_w;
+    int r;
     double xnorm = 0.0, bnorm = 0.0;
-    if ((r = norm2_64(h, xb, sc, xnorm)) || (r = norm2_64(h, b, sc, bnorm))) return r;
+    CK(launch_kc_gather(h->st, NBLK_RED, xb, nullptr, h->kc_pos, 1.0, xc, nc));
+    if ((r = cnorm(h, xc, sc, xnorm)) || (r = cnorm(h, b, sc, bnorm))) return r;
     const double eps = eps_rel * (1.0 + xnorm);
-    CK(cudaMemsetAsync(dx, 0, n * sizeof(cplx), h->st));
+    CK(cudaMemsetAsync(dx, 0, nc * sizeof(cplx), h->st));
     relres = 1.0;
     if (bnorm == 0.0) { relres = 0.0; return FDGA_OK; }
     std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hc(2 * (KR_MAX + 2)), y(m);
@@ -1227,24 +1286,23 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
     for (int cyc = 0; cyc < cycles; ++cyc) {
         double beta = bnorm;
         if (cyc == 0) {
-            CK(launch_kr_load(h->st, NBLK_RED, b, sc, h->kr_part, n));
-            CK(launch_kr_scale(h->st, NBLK_RED, sc, bnorm, Vw[0], n));
+            CK(launch_kr_load(h->st, NBLK_RED, b, W, sc, h->kr_part, nc));
+            CK(launch_kr_scale(h->st, NBLK_RED, sc, bnorm, Vw[0], nc));
         } else {
             // true residual r = b − A dx, with A dx = ‖dx‖ A(dx/‖dx‖)
             double dn = 0.0;
-            if ((r = norm2_64(h, dx, sc, dn))) return r;
+            if ((r = cnorm(h, dx, sc, dn))) return r;
             if (dn == 0.0) break;
-            CK(launch_kr_load(h->st, NBLK_RED, dx, sc, h->kr_part, n));
-            CK(launch_kr_scale(h->st, NBLK_RED, sc, dn, sc, n));
             if (nmaps + (central ? 2 : 1) > max_maps) break;
-            if ((r = apply_A(h, strategy, xb, yb, sc, eps, central, ytmp, w, nmaps))) return r;
-            // rr = b − dn·w  (w FP32)
-            CK(launch_kr_resid(h->st, NBLK_RED, b, w, -dn, nullptr, nullptr, 0.0, rr, n));
-            if ((r = norm2_64(h, rr, sc, beta))) return r;
+            CK(launch_kr_load(h->st, NBLK_RED, dx, W, sc, h->kr_part, nc));
+            CK(launch_kr_scale(h->st, NBLK_RED, sc, dn, sc, nc));
+            if ((r = apply_A(h, strategy, xb, yb, sc, eps, central, w, nmaps))) return r;
+            CK(launch_kr_resid(h->st, NBLK_RED, b, w, -dn, nullptr, nullptr, 0.0, rr, nc));
+            if ((r = cnorm(h, rr, sc, beta))) return r;
             relres = beta / bnorm;
             if (relres <= rtol) break;
-            CK(launch_kr_load(h->st, NBLK_RED, rr, sc, h->kr_part, n));
-            CK(launch_kr_scale(h->st, NBLK_RED, sc, beta, Vw[0], n));
+            CK(launch_kr_load(h->st, NBLK_RED, rr, W, sc, h->kr_part, nc));
+            CK(launch_kr_scale(h->st, NBLK_RED, sc, beta, Vw[0], nc));
         }
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
@@ -1252,15 +1310,15 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
         double est = beta;
         for (int j = 0; j < m; ++j) {
             if (nmaps + (central ? 2 : 1) > max_maps) break;
-            if ((r = apply_A(h, strategy, xb, yb, V.v[j], eps, central, ytmp, w, nmaps))) return r;
-            // classical Gram-Schmidt, twice
-            CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, h->kr_part, -1, n));
+            if ((r = apply_A(h, strategy, xb, yb, V.v[j], eps, central, w, nmaps))) return r;
+            // classical Gram-Schmidt, twice (weighted inner products)
+            CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, W, h->kr_part, -1, nc));
             CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, j + 1, c1));
-            CK(launch_kr_sub(h->st, NBLK_RED, V, j + 1, c1, w, n));
-            CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, h->kr_part, -1, n));
+            CK(launch_kr_sub(h->st, NBLK_RED, V, j + 1, c1, w, nc));
+            CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, W, h->kr_part, -1, nc));
             CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, j + 1, c2));
-            CK(launch_kr_sub(h->st, NBLK_RED, V, j + 1, c2, w, n));
-            CK(launch_kr_dots(h->st, NBLK_RED, V, 0, w, h->kr_part + (size_t)(KR_MAX + 1) * NBLK_RED, 0, n));
+            CK(launch_kr_sub(h->st, NBLK_RED, V, j + 1, c2, w, nc));
+            CK(launch_kr_dots(h->st, NBLK_RED, V, 0, w, W, h->kr_part + (size_t)(KR_MAX + 1) * NBLK_RED, 0, nc));
             CK(launch_kr_reduce(h->st, h->kr_part + (size_t)(KR_MAX + 1) * NBLK_RED, NBLK_RED, 1, c2 + KR_MAX + 1));
             CK(cudaMemcpyAsync(hc.data(), h->kr_coef, 2 * (KR_MAX + 2) * sizeof(double), cudaMemcpyDeviceToHost,
                                h->st));
@@ -1268,7 +1326,7 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
             for (int i = 0; i <= j; ++i) Hij(i, j) = hc[i] + hc[(KR_MAX + 2) + i];
             const double hn = std::sqrt(std::max(0.0, hc[(KR_MAX + 2) + KR_MAX + 1]));
             Hij(j + 1, j) = hn;
-            if (hn > 0.0) CK(launch_kr_scale(h->st, NBLK_RED, w, hn, Vw[j + 1], n));
+            if (hn > 0.0) CK(launch_kr_scale(h->st, NBLK_RED, w, hn, Vw[j + 1], nc));
             for (int i = 0; i < j; ++i) {  // previous rotations
                 const double a = Hij(i, j), bb = Hij(i + 1, j);
                 Hij(i, j) = cs[i] * a + sn[i] * bb;
@@ -1293,7 +1351,7 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
             y[i] = Hij(i, i) != 0.0 ? v / Hij(i, i) : 0.0;
         }
         CK(cudaMemcpyAsync(cy, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, h->st));
-        CK(launch_kr_update(h->st, NBLK_RED, dx, V, k, cy, 1.0, n));
+        CK(launch_kr_update(h->st, NBLK_RED, dx, V, k, cy, 1.0, nc));
         relres = est / bnorm;
         if (relres <= rtol) break;
     }
@@ -1318,29 +1376,43 @@ int fdga_set_U(fdga_handle* h, double U) {
 int fdga_jvp(fdga_handle* h, int strategy, const double* v, double* Jv, size_t n) {
     if (!h || !v || !Jv) return fail(h, FDGA_ERR_ARG, "null argument");
     if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
-    int r = ensure_krylov(h, 1);
-    if (r) return r;
-    cplx *x = h->kr64[0], *tmp = h->kr64[1], *yp = h->kr64[2];
-    cplxf* dir = h->kr32[0];
+    int r;
+    if (!h->kr_x && (r = dalloc(h, &h->kr_x, n))) return r;
+    if (h->jv.size() < 3)
+        while (h->jv.size() < 3) {
+            cplx* p = nullptr;
+            if ((r = dalloc(h, &p, n))) return r;
+            h->jv.push_back(p);
+        }
+    cplx *x = h->kr_x, *tmp = h->jv[0], *dir = h->jv[1], *yp = h->jv[2];
     CK(cudaMemcpyAsync(x, h->xS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
     CK(cudaMemcpyAsync(tmp, v, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
-    CK(launch_scatter(h->st, h->kr64[3], tmp, h->perm, n));  // reference layout -> device layout
-    double vn = 0.0, xn = 0.0;
-    if ((r = norm2_64(h, h->kr64[3], dir, vn)) || (r = norm2_64(h, x, dir, xn))) return r;
-    if (vn == 0.0) {
+    CK(launch_scatter(h->st, dir, tmp, h->perm, n));  // reference layout -> device layout
+    // full-space central difference (v need not be symmetric): Jv = (Φ(x + εv) − Φ(x − εv))/(2ε)
+    if (!h->kr_part) {
+        r = dalloc(h, &h->kr_part, (size_t)(KR_MAX + 2) * NBLK_RED);
+        if (!r) r = dalloc(h, &h->kr_coef, 4 * (size_t)(KR_MAX + 2));
+        if (r) return r;
+    }
+    double vn2 = 0.0, xn2 = 0.0;
+    cplxf* scratch = reinterpret_cast<cplxf*>(yp);  // n FP32 pairs fit in an FP64 vector
+    for (int k = 0; k < 2; ++k) {
+        CK(launch_kr_load(h->st, NBLK_RED, k ? x : dir, nullptr, scratch, h->kr_part, n));
+        CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, 1, h->kr_coef));
+        CK(cudaMemcpyAsync(k ? &xn2 : &vn2, h->kr_coef, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
+    if (vn2 == 0.0) {
         std::memset(Jv, 0, 2 * n * sizeof(double));
         return FDGA_OK;
     }
-    CK(launch_kr_load(h->st, NBLK_RED, h->kr64[3], dir, h->kr_part, n));
-    CK(launch_kr_scale(h->st, NBLK_RED, dir, vn, dir, n));
-    // central difference along the unit direction, scaled back by ‖v‖
-    const double eps = 1e-5 * (1.0 + xn);
-    CK(launch_kr_point(h->st, NBLK_RED, x, dir, eps, h->xS, n));
+    const double eps = 1e-5 * (1.0 + std::sqrt(xn2)) / std::sqrt(vn2);
+    CK(launch_kr_axpby(h->st, NBLK_RED, h->xS, x, eps, dir, n));
     if ((r = run_iteration(h, strategy, true, true))) return r;
     CK(cudaMemcpyAsync(yp, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-    CK(launch_kr_point(h->st, NBLK_RED, x, dir, -eps, h->xS, n));
+    CK(launch_kr_axpby(h->st, NBLK_RED, h->xS, x, -eps, dir, n));
     if ((r = run_iteration(h, strategy, true, true))) return r;
-    CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, h->yS, vn * 0.5 / eps, tmp, n));
+    CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, h->yS, 0.5 / eps, tmp, n));
     CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
     CK(launch_gather(h->st, h->yS, tmp, h->perm, n));
     CK(cudaMemcpyAsync(Jv, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
@@ -1357,62 +1429,79 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
     const size_t n = h->nstate;
     int r = ensure_krylov(h, restart);
     if (r) return r;
+    const size_t nc = h->nc;
     const int prec0 = h->precision;
     struct Restore {
         fdga_handle* h; int p;
         ~Restore() { h->precision = p; }
     } restore{h, prec0};
-    cplx *x = h->kr64[0], *y0 = h->kr64[1], *F = h->kr64[2], *dx = h->kr64[3], *yb = h->kr64[4];
-    int n64 = 0, nmix = 0, nouter = 0, status = 0;
+    cplx *x = h->kr_x, *yb = h->kr64[0], *F = h->kr64[1], *dx = h->kr64[2];
+    int n64 = 0, nmix = 0, nouter = 0;
     double resid = 0.0, prev = 0.0;
-    bool converged = false, have_y = false;
-    CK(cudaMemcpyAsync(x, h->xS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-    for (;;) {
+    bool converged = false;
+    // Φ(x) at the start; the Newton iterates start from Φ(x), which lies in the symmetric subspace
+    h->precision = FDGA_FP64;
+    if ((r = run_iteration(h, strategy, true, true))) return r;
+    ++n64;
+    CK(launch_kc_gather(h->st, NBLK_RED, h->yS, h->xS, h->kc_pos, 1.0, F, nc));
+    {
+        int status = 0;
+        CK(launch_residual(h->st, h->yS, h->xS, nullptr, nullptr, 0.0, h->d_part, NBLK_RED, n));
+        resid = reduce_max(h, NBLK_RED, status);
+        if (status) return status;
+    }
+    if (!std::isfinite(resid)) return fail(h, FDGA_ERR_NONFINITE, "non-finite residual in solve_newton");
+    if (trace) trace[nouter] = resid;
+    ++nouter;
+    if (resid < tol) converged = true;
+    CK(cudaMemcpyAsync(x, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    bool have_y = false;
+    while (!converged) {
         h->precision = FDGA_FP64;
         if (!have_y) {
+            if (n64 + nmix + 1 > maxiter) break;
             CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
             if ((r = run_iteration(h, strategy, true, true))) return r;
             ++n64;
         }
-        CK(cudaMemcpyAsync(y0, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-        CK(launch_residual(h->st, y0, x, F, nullptr, 0.0, h->d_part, NBLK_RED, n));
+        // F = Φ(x) − x (compact), yb = Φ(x) (compact)
+        CK(launch_kc_gather(h->st, NBLK_RED, h->yS, x, h->kc_pos, 1.0, F, nc));
+        CK(launch_kc_gather(h->st, NBLK_RED, h->yS, nullptr, h->kc_pos, 1.0, yb, nc));
         prev = resid;
-        resid = reduce_max(h, NBLK_RED, status);
-        if (status) return status;
+        if ((r = cmax(h, F, resid))) return r;
         if (!std::isfinite(resid)) return fail(h, FDGA_ERR_NONFINITE, "non-finite residual in solve_newton");
         if (trace) trace[nouter] = resid;
         ++nouter;
         if (resid < tol) { converged = true; break; }
         if (n64 + nmix + 3 > maxiter) break;
         // forcing term (Eisenstat–Walker choice 2, bounded); the mixed map's rounding floor bounds it below
-        double eta = nouter == 1 ? 0.1 : std::min(0.1, 0.9 * (resid / prev) * (resid / prev));
+        double eta = nouter <= 2 ? 0.1 : std::min(0.1, 0.9 * (resid / prev) * (resid / prev));
         eta = std::max(eta, jvp_precision == FDGA_MIXED ? 1e-3 : 1e-6);
-        const cplx* base = y0;
         if (jvp_precision == FDGA_MIXED) {
             h->precision = FDGA_MIXED;
             CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
             if ((r = run_iteration(h, strategy, true, true))) return r;
             ++nmix;
-            CK(cudaMemcpyAsync(yb, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-            base = yb;
+            CK(launch_kc_gather(h->st, NBLK_RED, h->yS, nullptr, h->kc_pos, 1.0, yb, nc));
         }
         int nmaps = 0, its = 0;
         double relres = 1.0;
         const int left = maxiter - n64 - nmix - 1;
         const double eps_rel = jvp_precision == FDGA_MIXED ? 3e-4 : 1e-7;
         // (I − J) dx = F
-        r = gmres_solve(h, strategy, x, base, F, dx, restart, 1, eta, eps_rel, false, left, nmaps, its, relres);
+        r = gmres_solve(h, strategy, x, yb, F, dx, restart, 1, eta, eps_rel, false, left, nmaps, its, relres);
         if (r) return r;
         if (h->precision == FDGA_FP64) n64 += nmaps; else nmix += nmaps;
-        // backtracking on max|R| of the FP64 map
+        // backtracking on the FP64 residual
         h->precision = FDGA_FP64;
         double lam = 1.0;
         have_y = false;
         for (int ls = 0; ls < 4 && n64 + nmix + 1 <= maxiter; ++ls) {
-            CK(launch_kr_axpby(h->st, NBLK_RED, h->xS, x, lam, dx, n));
+            CK(launch_kc_axpy(h->st, NBLK_RED, x, dx, h->kc_code, lam, h->xS, n));
             if ((r = run_iteration(h, strategy, true, true))) return r;
             ++n64;
-            CK(launch_residual(h->st, h->yS, h->xS, F, nullptr, 0.0, h->d_part, NBLK_RED, n));
+            int status = 0;
+            CK(launch_residual(h->st, h->yS, h->xS, nullptr, nullptr, 0.0, h->d_part, NBLK_RED, n));
             const double rn = reduce_max(h, NBLK_RED, status);
             if (status) return status;
             if (std::isfinite(rn) && (rn < (1.0 - 1e-4 * lam) * resid || ls == 3)) {
@@ -1425,7 +1514,17 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
         if (!have_y) break;
     }
     // S holds Φ64 of the last iterate, as after the reference's solve!
-    CK(cudaMemcpyAsync(h->xS, y0, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    if (!converged || nouter > 1) {
+        if (!have_y) {
+            h->precision = FDGA_FP64;
+            CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+            if ((r = run_iteration(h, strategy, true, true))) return r;
+            ++n64;
+        }
+        CK(cudaMemcpyAsync(h->xS, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    } else {
+        CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    }
     CK(cudaStreamSynchronize(h->st));
     if (iters) *iters = converged ? nouter : -nouter;
     if (res) *res = resid;
@@ -1443,6 +1542,7 @@ int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int resta
     const size_t n = h->nstate;
     int r = ensure_krylov(h, restart);
     if (r) return r;
+    const size_t nc = h->nc;
     const int prec0 = h->precision;
     const double U = h->d.U;
     struct Restore {
@@ -1450,31 +1550,31 @@ int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int resta
         ~Restore() { h->precision = p; if (h->d.U != U) fdga_set_U(h, U); }
     } restore{h, prec0, U};
     h->precision = FDGA_FP64;
-    cplx *xs = h->kr64[0], *ys = h->kr64[1], *b = h->kr64[2], *dx = h->kr64[3], *yp = h->kr64[4];
+    cplx *xs = h->kr_x, *b = h->kr64[1], *dx = h->kr64[2], *yp = h->kr64[4];
     CK(cudaMemcpyAsync(xs, h->xS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
-    // ∂Φ/∂U at the fixed point: central difference in U
+    // ∂Φ/∂U at the fixed point: central difference in U (compact)
     if ((r = fdga_set_U(h, U + hU))) return r;
     if ((r = run_iteration(h, strategy, true, true))) return r;
-    CK(cudaMemcpyAsync(yp, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_kc_gather(h->st, NBLK_RED, h->yS, nullptr, h->kc_pos, 1.0, yp, nc));
     if ((r = fdga_set_U(h, U - hU))) return r;
     if ((r = run_iteration(h, strategy, true, true))) return r;
-    CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, h->yS, 0.5 / hU, b, n));
+    CK(launch_kc_gather(h->st, NBLK_RED, h->yS, nullptr, h->kc_pos, 1.0, b, nc));
+    CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, b, 0.5 / hU, b, nc));  // b = (y+ − y−)/(2h)
     if ((r = fdga_set_U(h, U))) return r;
-    if ((r = run_iteration(h, strategy, true, true))) return r;
-    CK(cudaMemcpyAsync(ys, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
     // (I − J) dx = ∂Φ/∂U, central-difference Jacobian
     int nmaps = 0, its = 0;
     double relres = 1.0;
-    r = gmres_solve(h, strategy, xs, ys, b, dx, restart, cycles, rtol, 1e-5, true, 1 << 30, nmaps, its, relres);
+    r = gmres_solve(h, strategy, xs, nullptr, b, dx, restart, cycles, rtol, 1e-5, true, 1 << 30, nmaps, its, relres);
     if (r) return r;
-    // dχ/dU = χ(dx) − (2/U) χ(x*)   (χ = K1 combination / U²)
-    cplx* t1 = h->kr64[5];
-    CK(launch_chi(h->st, chanK(h, dx, CH_P, 1), chanK(h, dx, CH_T, 1), chanK(h, dx, CH_A, 1), channel, U, (int)NO,
-                  h->d.Nq, 0, t1));
+    // dχ/dU = χ(dx) − (2/U) χ(x*)   (χ = K1 combination / U²); dx expanded into the full layout
+    CK(cudaMemsetAsync(h->tmpS, 0, n * sizeof(cplx), h->st));
+    CK(launch_kc_axpy(h->st, NBLK_RED, h->tmpS, dx, h->kc_code, 1.0, h->tmpS, n));  // tmpS = expand(dx)
+    std::vector<cplx> hb(2 * full);  // χ(dx) and χ(x*), staged in yS (2 NΩ1·Nq <= state length)
+    CK(launch_chi(h->st, chanK(h, h->tmpS, CH_P, 1), chanK(h, h->tmpS, CH_T, 1), chanK(h, h->tmpS, CH_A, 1), channel, U,
+                  (int)NO, h->d.Nq, 0, h->yS));
     CK(launch_chi(h->st, chanK(h, xs, CH_P, 1), chanK(h, xs, CH_T, 1), chanK(h, xs, CH_A, 1), channel, U, (int)NO,
-                  h->d.Nq, 0, t1 + full));
-    std::vector<cplx> hb(2 * full);
-    CK(cudaMemcpyAsync(hb.data(), t1, 2 * full * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+                  h->d.Nq, 0, h->yS + full));
+    CK(cudaMemcpyAsync(hb.data(), h->yS, 2 * full * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(h->xS, xs, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
     for (size_t i = 0; i < full; ++i) {
