@@ -1,0 +1,274 @@
+// fdga_k3_tc.cu -- the K3 Bethe-Salpeter contractions of the mixed map on the 5th-generation
+// tensor cores (tcgen05, sm_103a).
+//
+// Per (channel, representative (P, Ω) block) the BSE is one complex product C = A·M of Nν3 x Nν3
+// matrices (src/BSEa/BSEa_K3.jl:1-128; M formed elementwise from the caches, Π, Π0 and FL).  It
+// runs as one real GEMM D[128 x 2N] += A_r[128 x 2N'] · B_r[2N' x 2N] with the complex product in
+// 2x2 real form (k = 2ω + q, n = 2ν' + p):
+//   A_r[ν][2ω] = Re A(ν,ω), A_r[ν][2ω+1] = Im A(ν,ω)
+//   B_r[2ω][2ν'] = Re M, B_r[2ω][2ν'+1] = Im M, B_r[2ω+1][2ν'] = −Im M, B_r[2ω+1][2ν'+1] = Re M
+// so that D[ν][2ν'] = Re C(ν,ν') and D[ν][2ν'+1] = Im C(ν,ν').  Operands are FP32 (the mixed map's
+// FP32 caches); each is split into TF32 hi + lo and the product accumulates hi·hi + hi·lo + lo·hi
+// (kind::tf32, FP32 accumulation in tensor memory), which keeps FP32-level accuracy.
+//
+// One CTA of 128 threads per block: rows ν < N of the 128-lane accumulator, 2N ≤ 256 columns.
+// K runs in chunks of 16 ω (32 real k); two shared-memory stages; the threads stage chunk c+1
+// while the tensor core works on chunk c (tcgen05.commit -> mbarrier).  Shared-memory operands use
+// the no-swizzle K-major canonical layout: 8-row x 16-byte core matrices, K-adjacent core
+// matrices 128 B apart (LBO), 8-row groups 1024 B apart (SBO).  Every wait is bounded; a timeout
+// sets *err and the kernel still releases its tensor memory.
+#include "fdga_kernels.h"
+
+namespace fdga {
+
+namespace {
+
+constexpr int TC_THREADS = 128;
+constexpr int KC = 32;                      // real K per chunk (16 ω)
+constexpr int A_BYTES = 128 * KC * 4;       // one A operand (hi or lo) of a chunk: 16 KB
+constexpr uint32_t SPIN_LIMIT = 1u << 22;   // bounded mbarrier polling
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+// byte offset of element (row r, k) in a K-major no-swizzle operand with KC columns of K
+__device__ __forceinline__ uint32_t op_off(int r, int k) {
+    return (uint32_t)((((r >> 3) * (KC / 4) + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
+}
+// shared-memory matrix descriptor: start, LBO = 128 B, SBO = 1024 B, fixed 0b001 at bits 46-48,
+// no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           (1ull << 46);
+}
+__device__ __forceinline__ void split_tf32(float v, float& hi, float& lo) {
+    hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+    lo = v - hi;
+}
+__device__ __forceinline__ void st_pair(uint8_t* base, uint32_t off, float v, uint8_t* base_lo) {
+    float hi, lo;
+    split_tf32(v, hi, lo);
+    *reinterpret_cast<float*>(base + off) = hi;
+    *reinterpret_cast<float*>(base_lo + off) = lo;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void mma_tf32(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+        :
+        : "r"(dt), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims d, int* err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ float pis[16][4];  // Π(ω), Π0(ω) of the chunk (re, im, re, im)
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = d.N3n, NN = 2 * N;
+    const int nchunks = (N + 15) / 16;
+    const int nb = args.nblocks;
+    const int slot = blockIdx.x / nb;
+    const int blk = args.blocks ? args.blocks[blockIdx.x % nb] : (int)(blockIdx.x % nb);
+    const K3ArgsF& a = args.a[slot];
+    const int CH = args.ch[slot];
+    const int m = blk % d.N3O - (d.n3O - 1), P = blk / d.N3O;
+    const size_t base = (size_t)blk * N * N;
+    const float s1 = (CH == CH_A) ? 1.f : -1.f, s2 = (CH == CH_T) ? -1.f : 1.f;
+    const int B_BYTES = NN * KC * 4;
+    const int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+    // tensor memory: 256 columns (2N ≤ 256)
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_base))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NN >> 3) << 17) | ((128u >> 4) << 24);
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+        const int st = c & 1;
+        if (c >= 2 && !mbar_wait(smem_u32(&mbar[st]), ((c - 2) >> 1) & 1)) ok = false;
+        uint8_t* Ahi = sm + (size_t)st * STAGE;
+        uint8_t* Alo = Ahi + A_BYTES;
+        uint8_t* Bhi = Alo + A_BYTES;
+        uint8_t* Blo = Bhi + B_BYTES;
+        const int w0 = 16 * c;
+        if (tid < 16) {
+            const int w = w0 + tid;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            if (w < N) {
+                const size_t ip = ixPi(d, P, m, w - d.n3n);
+                const cplx p0 = ldg(a.Pi0 + ip);
+                v[2] = (float)p0.x; v[3] = (float)p0.y;
+                if (MODE == 1) { const cplx p = ldg(a.Pi + ip); v[0] = (float)p.x; v[1] = (float)p.y; }
+            }
+            for (int j = 0; j < 4; ++j) pis[tid][j] = v[j];
+        }
+        __syncthreads();
+        // A: row ν = tid, 16 ω of the chunk
+        {
+            const int nu = tid;
+            for (int t = 0; t < 16; ++t) {
+                const int w = w0 + t;
+                cplxf v{0.f, 0.f};
+                if (nu < N && w < N) {
+                    const float2 q = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w));
+                    v = cplxf{q.x, q.y};
+                }
+                st_pair(Ahi, op_off(nu, 2 * t), v.x, Alo);
+                st_pair(Ahi, op_off(nu, 2 * t + 1), v.y, Alo);
+            }
+        }
+        // B: (t, ν') items of the chunk
+        for (int e = tid; e < 16 * N; e += TC_THREADS) {
+            const int t = e / N, col = e % N, w = w0 + t;
+            cplxf M{0.f, 0.f};
+            if (w < N) {
+                const cplxf pi0{pis[t][2], pis[t][3]};
+                const float2 q0 = __ldg(reinterpret_cast<const float2*>(a.B0 + base + (size_t)w * N + col));
+                const cplxf f0{q0.x, q0.y};
+                if (MODE == 0) {
+                    M = pi0 * f0;
+                } else {
+                    const cplxf pi{pis[t][0], pis[t][1]};
+                    const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
+                    const float2 qg = __ldg(reinterpret_cast<const float2*>(a.G + ig));
+                    const cplxf gs{qg.x, qg.y};
+                    M = ((pi - pi0) * f0 + pi * gs) * s1;
+                    const int ot = cross(CH, m, w - d.n3n);
+                    if (fin(ot, d.n3n)) {
+                        const size_t il = base + (size_t)(ot + d.n3n) * N + col;
+                        cplxf gl;
+                        if (CH == CH_T) {
+                            const float2 qt = __ldg(reinterpret_cast<const float2*>(a.FLt + il));
+                            const float2 qa = __ldg(reinterpret_cast<const float2*>(a.FLa + il));
+                            gl = cplxf{2.f * qt.x - qa.x, 2.f * qt.y - qa.y};
+                        } else {
+                            const float2 qc = __ldg(reinterpret_cast<const float2*>(a.FLc + il));
+                            gl = cplxf{qc.x, qc.y};
+                        }
+                        M += pi * gl * s2;
+                    }
+                }
+            }
+            st_pair(Bhi, op_off(2 * col, 2 * t), M.x, Blo);
+            st_pair(Bhi, op_off(2 * col + 1, 2 * t), M.y, Blo);
+            st_pair(Bhi, op_off(2 * col, 2 * t + 1), -M.y, Blo);
+            st_pair(Bhi, op_off(2 * col + 1, 2 * t + 1), M.x, Blo);
+        }
+        // generic-proxy writes -> visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo), bh = smem_u32(Bhi), bl = smem_u32(Blo);
+            for (int ks = 0; ks < KC / 8; ++ks) {
+                const uint32_t o = (uint32_t)ks * 256u;  // 8 tf32 of K = two core matrices
+                mma_tf32(tmem, sdesc(ah + o), sdesc(bh + o), idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                mma_tf32(tmem, sdesc(ah + o), sdesc(bl + o), idesc, 1u);
+                mma_tf32(tmem, sdesc(al + o), sdesc(bh + o), idesc, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&mbar[st]))
+                         : "memory");
+        }
+        __syncthreads();
+    }
+    // the last chunk of each stage
+    if (nchunks >= 2 && !mbar_wait(smem_u32(&mbar[nchunks & 1]), ((nchunks - 2) >> 1) & 1)) ok = false;
+    if (!mbar_wait(smem_u32(&mbar[(nchunks - 1) & 1]), ((nchunks - 1) >> 1) & 1)) ok = false;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        // epilogue: warp w reads lanes 32w..32w+31 (rows ν), 16 columns (8 complex) per load
+        const int nu = 32 * warp + lane;
+        const double T = d.T;
+        for (int c0 = 0; c0 < NN; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (nu < N) {
+                for (int j = 0; j < 8; ++j) {
+                    const int col = c0 / 2 + j;
+                    if (col >= N) break;
+                    const cplx v = cplx{(double)__uint_as_float(r[2 * j]), (double)__uint_as_float(r[2 * j + 1])};
+                    const size_t io = base + (size_t)nu * N + col;
+                    if (MODE == 0) {
+                        a.out[io] = v * (T * ((CH == CH_A) ? 1.0 : -1.0));
+                    } else {
+                        cplx gl;
+                        if (CH == CH_T) gl = 2.0 * to_d(cplxf{a.FLt[io].x, a.FLt[io].y}) - to_d(cplxf{a.FLa[io].x, a.FLa[io].y});
+                        else gl = to_d(cplxf{a.FLc[io].x, a.FLc[io].y});
+                        a.out[io] = v * T + gl;
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+}
+
+}  // namespace
+
+bool k3_tc_supported(const Dims& d) {
+    // 2N MMA columns: a multiple of 16, at most 256; the 128-lane accumulator holds N ≤ 128 rows
+    return d.N3n >= 32 && d.N3n <= 128 && (d.N3n % 8) == 0;
+}
+
+static size_t k3_tc_smem(const Dims& d) { return 2 * ((size_t)2 * A_BYTES + (size_t)2 * (2 * d.N3n) * KC * 4); }
+
+cudaError_t prepare_bse_K3_tc(const Dims& d) {
+    // the dynamic shared-memory limit is raised once per size, before any graph capture
+    static size_t smem_set = 0;
+    const size_t smem = k3_tc_smem(d);
+    if (smem <= smem_set) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_bse_K3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_bse_K3_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) smem_set = smem;
+    return e;
+}
+
+cudaError_t launch_bse_K3_tc(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int* err) {
+    if (!k3_tc_supported(d)) return cudaErrorInvalidValue;
+    const size_t smem = k3_tc_smem(d);
+    const unsigned grid = (unsigned)(nslots * a.nblocks);
+    if (mode) k_bse_K3_tc<1><<<grid, TC_THREADS, smem, s>>>(a, d, err);
+    else k_bse_K3_tc<0><<<grid, TC_THREADS, smem, s>>>(a, d, err);
+    return cudaGetLastError();
+}
+
+}  // namespace fdga

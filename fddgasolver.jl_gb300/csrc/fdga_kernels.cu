@@ -268,6 +268,49 @@ __global__ void k_fft2_rows(const cplx* in, cplx* out, int rows, int sign, doubl
         out[(size_t)R * rows + r0 + r] = v * scale;
     }
 }
+// Separable DFT variant of k_fft2_rows for L that is not a power of two: the TR rows of a CTA are
+// staged in shared memory and transformed along x then y, one output element per thread and pass
+// (2L products per output instead of L² for the direct 2D sum).  tw[j] = e^{sign 2πi j/L}.
+__global__ void k_dft2_sep(const cplx* in, cplx* out, int rows, int L, const cplx* tw, double scale, int TR) {
+    extern __shared__ cplx sh[];
+    const int NR = L * L, RS = L + 1, BS = L * (L + 1) + 1;
+    cplx* twS = sh + (size_t)2 * TR * BS;
+    for (int j = threadIdx.x; j < L; j += blockDim.x) twS[j] = tw[j];
+    const int r0 = blockIdx.x * TR;
+    cplx* A = sh;                         // [TR][L][L+1]
+    cplx* B = sh + (size_t)TR * BS;       // [TR][L][L+1]
+    for (int e = threadIdx.x; e < TR * NR; e += blockDim.x) {
+        const int r = e % TR, P = e / TR;
+        A[(size_t)r * BS + (P / L) * RS + (P % L)] = (r0 + r < rows) ? in[(size_t)P * rows + r0 + r] : mk(0, 0);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < TR * NR; e += blockDim.x) {  // along x: B[r][y][kx] = Σ_x A[r][y][x] w^{kx x}
+        const int r = e / NR, q = e % NR, y = q / L, kx = q % L;
+        const cplx* a = A + (size_t)r * BS + y * RS;
+        cplx s = mk(0, 0);
+        int ph = 0;
+        for (int x = 0; x < L; ++x) {
+            s = cfma(a[x], twS[ph], s);
+            ph += kx;
+            if (ph >= L) ph -= L;
+        }
+        B[(size_t)r * BS + y * RS + kx] = s;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < TR * NR; e += blockDim.x) {  // along y, written as out[R][row]
+        const int r = e % TR, R = e / TR, ky = R / L, kx = R % L;
+        if (r0 + r >= rows) continue;
+        const cplx* b = B + (size_t)r * BS + kx;
+        cplx s = mk(0, 0);
+        int ph = 0;
+        for (int y = 0; y < L; ++y) {
+            s = cfma(b[y * RS], twS[ph], s);
+            ph += ky;
+            if (ph >= L) ph -= L;
+        }
+        out[(size_t)R * rows + r0 + r] = s * scale;
+    }
+}
 // Direct-DFT fallback of k_fft2_rows for L that is not a power of two; one thread per output.
 __global__ void k_dft2_rows(const cplx* in, cplx* out, int rows, int L, const cplx* tw, double scale) {
     const int NR = L * L;
@@ -314,12 +357,13 @@ __global__ void k_build_cache(VertP F, Caches C, const int* blocks, int nblocks,
     const int m = bl % d.N3O - (d.n3O - 1);
     const int P = bl / d.N3O;
     // left
-    C.c[0][i] = vert_eval(F, d, CH_P, SP_X, m, a, b, P, FL_GT | FL_GA);
-    C.c[1][i] = ref_xSp(F, d, CH_P, m, a, b) - ref_xSp(F, d, CH_P, m, a, FINF);
+    cplx v[10];
+    v[0] = vert_eval(F, d, CH_P, SP_X, m, a, b, P, FL_GT | FL_GA);
+    v[1] = ref_xSp(F, d, CH_P, m, a, b) - ref_xSp(F, d, CH_P, m, a, FINF);
     const cplx f0a = ref_pSp(F, d, CH_A, m, a, b) - ref_pSp(F, d, CH_A, m, a, FINF);
     const cplx f0t = ref_pSp(F, d, CH_T, m, a, b) - ref_pSp(F, d, CH_T, m, a, FINF);
-    C.c[2][i] = f0a;
-    C.c[3][i] = 2.0 * f0t - f0a;
+    v[2] = f0a;
+    v[3] = 2.0 * f0t - f0a;
     // right
     const cplx gpp = vert_pSp(F, d, CH_P, m, a, b, P, FL_GT | FL_GA);
     const cplx ga = vert_pSp(F, d, CH_A, m, a, b, P, FL_GP | FL_GT);
@@ -327,12 +371,19 @@ __global__ void k_build_cache(VertP F, Caches C, const int* blocks, int nblocks,
     const cplx fp = vert_pSp(F, d, CH_P, m, a, b, P, FL_F0 | FL_GP) - vert_pSp(F, d, CH_P, m, FINF, b, P, FL_F0 | FL_GP) + gpp;
     const cplx fa = vert_pSp(F, d, CH_A, m, a, b, P, FL_F0 | FL_GA) - vert_pSp(F, d, CH_A, m, FINF, b, P, FL_F0 | FL_GA) + ga;
     const cplx ft = vert_pSp(F, d, CH_T, m, a, b, P, FL_F0 | FL_GT) - vert_pSp(F, d, CH_T, m, FINF, b, P, FL_F0 | FL_GT) + gt;
-    C.c[4][i] = gpp;
-    C.c[5][i] = ga;
-    C.c[6][i] = gt * 2.0 - ga;
-    C.c[7][i] = fp;
-    C.c[8][i] = fa;
-    C.c[9][i] = ft * 2.0 - fa;
+    v[4] = gpp;
+    v[5] = ga;
+    v[6] = gt * 2.0 - ga;
+    v[7] = fp;
+    v[8] = fa;
+    v[9] = ft * 2.0 - fa;
+    if (C.f[0]) {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) C.f[k][i] = to_c<cplxf>(v[k]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) C.c[k][i] = v[k];
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -541,10 +592,21 @@ __device__ __forceinline__ void bse_K2_body(const VertP& F, const FLP& FL, const
 // 2x2 outputs each, K chunks of 8.  blockIdx.x = channel-slot * (Nq·NΩ3) + (P·NΩ3 + iΩ), blockIdx.y /
 // blockIdx.z = row / column tile; the three channels of one mode share a launch.
 // ---------------------------------------------------------------------------------------------
-// C = cplx: FP64 arithmetic (the plain path).  C = cplxf: operands converted to FP32 when staged
-// into shared memory, FP32 products and accumulation, FP64 epilogue (the mixed path).
-template <int MODE, int TILE, class C>
-__global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3 args, Dims d) {
+// Operand loads of the K3 GEMM: FP64 storage converted to the arithmetic type, or FP32 storage
+// (the mixed map's caches and FL.K3 copy) read as is.
+template <class C> __device__ __forceinline__ C ldk(const cplx* p) { return to_c<C>(ldg(p)); }
+template <class C> __device__ __forceinline__ C ldk(const cplxf* p) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return C{v.x, v.y};
+}
+__device__ __forceinline__ cplx ldk_d(const cplx* p) { return ldg(p); }
+__device__ __forceinline__ cplx ldk_d(const cplxf* p) { return to_d(ldk<cplxf>(p)); }
+
+// ARGS = K3Args3 (FP64 operands) or K3Args3F (FP32 operands).  C = cplx: FP64 arithmetic (the plain
+// path).  C = cplxf: FP32 products and accumulation, FP64 epilogue (the mixed path; FP64 operands
+// are converted when they are staged into shared memory).
+template <int MODE, int TILE, class C, class ARGS>
+__global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS args, Dims d) {
     using R = decltype(C::x);
     constexpr int TK = 8, H = TILE / 2, NT = H * H;
     __shared__ C As[TILE][TK + 1];
@@ -555,7 +617,7 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
     const int nb = args.nblocks;
     const int slot = blockIdx.x / nb;
     const int blk = args.blocks ? args.blocks[blockIdx.x % nb] : (int)(blockIdx.x % nb);
-    const K3Args& a = args.a[slot];
+    const auto& a = args.a[slot];
     const int CH = args.ch[slot];
     const int m = blk % d.N3O - (d.n3O - 1), P = blk / d.N3O;
     const int N = d.N3n;
@@ -566,7 +628,7 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
         for (int e = tid; e < TILE * TK; e += NT) {
             const int r = e / TK, kk = e % TK;
             const int row = row0 + r, k = k0 + kk;
-            As[r][kk] = to_c<C>((row < N && k < N) ? ldg(a.A + base + (size_t)row * N + k) : mk(0, 0));
+            As[r][kk] = (row < N && k < N) ? ldk<C>(a.A + base + (size_t)row * N + k) : czero<C>();
         }
         for (int e = tid; e < TK * TILE; e += NT) {
             const int kk = e / TILE, c = e % TILE;
@@ -576,19 +638,19 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
                 const int o = k - d.n3n;  // ω as fermion index
                 const size_t ip = ixPi(d, P, m, o);
                 const C pi0 = to_c<C>(ldg(a.Pi0 + ip));
-                const C f0 = to_c<C>(ldg(a.B0 + base + (size_t)k * N + col));
+                const C f0 = ldk<C>(a.B0 + base + (size_t)k * N + col);
                 if (MODE == 0) {
                     v = pi0 * f0;
                 } else {
                     const C pi = to_c<C>(ldg(a.Pi + ip));
-                    const C gs = to_c<C>((CH == CH_P) ? ldg(a.G + base + (size_t)k * N + col)
-                                                      : ldg(a.G + base + (size_t)col * N + k));
+                    const C gs = (CH == CH_P) ? ldk<C>(a.G + base + (size_t)k * N + col)
+                                              : ldk<C>(a.G + base + (size_t)col * N + k);
                     v = ((pi - pi0) * f0 + pi * gs) * (R)s1;
                     const int ot = cross(CH, m, o);
                     if (fin(ot, d.n3n)) {
                         const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                        const C gl = (CH == CH_T) ? to_c<C>(ldg(a.FLt + il)) * (R)2 - to_c<C>(ldg(a.FLa + il))
-                                                  : to_c<C>(ldg(a.FLc + il));
+                        const C gl = (CH == CH_T) ? ldk<C>(a.FLt + il) * (R)2 - ldk<C>(a.FLa + il)
+                                                  : ldk<C>(a.FLc + il);
                         v += pi * gl * (R)s2;
                     }
                 }
@@ -618,7 +680,7 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(K3Args3
             if (MODE == 0) {
                 a.out[io] = r * (d.T * ((CH == CH_A) ? 1.0 : -1.0));
             } else {
-                const cplx gl = (CH == CH_T) ? 2.0 * ldg(a.FLt + io) - ldg(a.FLa + io) : ldg(a.FLc + io);
+                const cplx gl = (CH == CH_T) ? 2.0 * ldk_d(a.FLt + io) - ldk_d(a.FLa + io) : ldk_d(a.FLc + io);
                 a.out[io] = r * d.T + gl;
             }
         }
@@ -738,8 +800,10 @@ __global__ void k_finalize3(Finalize3 f, int k2_epilogue, int t_recombine, size_
     }
     if (t_recombine) v[CH_T] = (v[CH_T] + v[CH_A]) * 0.5;
 #pragma unroll
-    for (int c = 0; c < 3; ++c)
+    for (int c = 0; c < 3; ++c) {
         if (f.out[c]) f.out[c][i] = v[c];
+        if (f.outf[c]) f.outf[c][i] = to_c<cplxf>(v[c]);
+    }
 }
 
 // Σ_inner in real space (src/nonlocal/SDE.jl:208-280; local src/SDE.jl:241-263 is the L = 1 case):
@@ -981,8 +1045,16 @@ cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int
         case 16: return launch_fft2_tpl<16>(s, in, out, rows, sign, scale);
         default: break;
     }
-    const size_t n = (size_t)d.L * d.L * rows;
-    k_dft2_rows<<<blocks_for(n, 128), 128, 0, s>>>(in, out, rows, d.L, tw_sign, scale);
+    const int L = d.L, BS = L * (L + 1) + 1;
+    int tr = 16;
+    while (tr > 1 && (size_t)(2 * tr * BS + L) * sizeof(cplx) > 48 * 1024) tr >>= 1;
+    if ((size_t)(2 * tr * BS + L) * sizeof(cplx) <= 48 * 1024) {
+        const size_t shm = (size_t)(2 * tr * BS + L) * sizeof(cplx);
+        k_dft2_sep<<<(unsigned)((rows + tr - 1) / tr), 256, shm, s>>>(in, out, rows, L, tw_sign, scale, tr);
+        LAUNCH_CHECK(); return cudaSuccess;
+    }
+    const size_t n = (size_t)L * L * rows;
+    k_dft2_rows<<<blocks_for(n, 128), 128, 0, s>>>(in, out, rows, L, tw_sign, scale);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 
@@ -1050,16 +1122,16 @@ cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue
     k_finalize3<<<blocks_for(n, 256), 256, 0, s>>>(f, k2_epilogue, t_recombine, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-template <int MODE, int TILE, class C>
-static cudaError_t launch_k3_tile(cudaStream_t s, const K3Args3& a, int nslots, const Dims& d) {
+template <int MODE, int TILE, class C, class ARGS>
+static cudaError_t launch_k3_tile(cudaStream_t s, const ARGS& a, int nslots, const Dims& d) {
     const unsigned tiles = (unsigned)((d.N3n + TILE - 1) / TILE);
     dim3 grid((unsigned)(nslots * a.nblocks), tiles, tiles);
-    k_bse_K3_gemm<MODE, TILE, C><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
+    k_bse_K3_gemm<MODE, TILE, C, ARGS><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
     return cudaGetLastError();
 }
 int k3_default_tile(int N) { return N <= 16 ? 16 : (N <= 24 ? 24 : 32); }
-template <class C>
-static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int tile) {
+template <class C, class ARGS>
+static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const ARGS& a, int nslots, const Dims& d, int tile) {
     if (tile != 16 && tile != 24 && tile != 32) tile = k3_default_tile(d.N3n);
     if (mode == 0) {
         if (tile == 16) return launch_k3_tile<0, 16, C>(s, a, nslots, d);
@@ -1073,6 +1145,17 @@ static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const K3Args3& a, i
 cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed, int tile) {
     return mixed ? launch_bse_K3_t<cplxf>(s, mode, a, nslots, d, tile)
                  : launch_bse_K3_t<cplx>(s, mode, a, nslots, d, tile);
+}
+cudaError_t launch_bse_K3_f32(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int tile) {
+    return launch_bse_K3_t<cplxf>(s, mode, a, nslots, d, tile);
+}
+__global__ void k_to_f32(const cplx* in, cplxf* out, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = to_c<cplxf>(in[i]);
+}
+cudaError_t launch_to_f32(cudaStream_t s, const cplx* in, cplxf* out, size_t n) {
+    k_to_f32<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
+    LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d) {

@@ -20,6 +20,7 @@ struct ChanArraysW {  // written arrays of the three channels
 };
 struct Caches {  // Γpx F0p F0a F0t Γpp Γa Γt Fp Fa Ft
     cplx* c[10];
+    cplxf* f[10];  // FP32 copies written instead of c in the mixed map (nullptr: FP64 map)
 };
 struct FLP {  // left vertex FL: only K2 enters the K1/K2 BSE through FL(Ω, ω, νInf)
     const cplx* K2[3];
@@ -36,6 +37,23 @@ struct K3Args {
     cplx* out;
 };
 
+struct K3ArgsF {  // FP32 operands of the mixed map (the FP32 caches and FL.K3 copy)
+    const cplxf* A;
+    const cplxf* B0;
+    const cplxf* G;
+    const cplx* Pi;
+    const cplx* Pi0;
+    const cplxf* FLc;
+    const cplxf* FLt;
+    const cplxf* FLa;
+    cplx* out;
+};
+struct K3Args3F {
+    K3ArgsF a[3];
+    int ch[3];
+    const int* blocks;
+    int nblocks;
+};
 struct K3Args3 {  // the three channels of one K3 launch over a list of (P, Ω) blocks
     K3Args a[3];
     int ch[3];
@@ -59,6 +77,7 @@ struct Finalize3 {  // indexed by channel (p, t, a)
     cplx* out[3];
     const uint32_t* map[3];
     const cplx* FL[3];
+    cplxf* outf[3];  // optional FP32 copies of out (FL.K3 of the mixed map)
 };
 
 constexpr int AA_MAX = 64;  // largest Anderson memory of the device solver
@@ -104,6 +123,12 @@ cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, 
 // tile: 16, 24 or 32 (the output tile edge of the GEMM kernel); any other value picks the default for Nν3
 cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed, int tile);
 int k3_default_tile(int N);
+cudaError_t launch_bse_K3_f32(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int tile);
+cudaError_t launch_to_f32(cudaStream_t s, const cplx* in, cplxf* out, size_t n);
+// tcgen05 form of the mixed K3 contractions (2Nν3 ≤ 256 MMA columns); *err set on a wait timeout
+bool k3_tc_supported(const Dims& d);
+cudaError_t prepare_bse_K3_tc(const Dims& d);
+cudaError_t launch_bse_K3_tc(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int* err);
 cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, const cplx* Lph, cplx* LR, cplx* SR,
                              cplx* S, const cplx* twm, const cplx* twp, const Dims& d);
 cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,

@@ -62,6 +62,9 @@ struct fdga_handle {
     cplx *Fref[4] = {nullptr, nullptr, nullptr, nullptr};  // Fp_p Fp_x Ft_p Ft_x
     cplx *xS = nullptr, *yS = nullptr, *tmpS = nullptr;
     cplx *avg = nullptr, *cache = nullptr, *FLK2 = nullptr, *FLK3 = nullptr;
+    cplxf *cachef = nullptr, *FLK3f = nullptr;  // FP32 caches and FL.K3 of the mixed map
+    int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
+    int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
     cplx *GR = nullptr, *u2C = nullptr, *u2R = nullptr, *twm = nullptr, *twp = nullptr;
     cplx *SPi = nullptr, *SPi0 = nullptr, *SX = nullptr;  // bubble row sums [2][Nq][NΠΩ]; S_X [3][Nq][NΠΩ]
@@ -131,6 +134,29 @@ int dalloc(fdga_handle* h, T** p, size_t n) {
         int r__ = dalloc(h, &(ptr), (n));                    \
         if (r__) return r__;                                 \
     } while (0)
+
+// the FP32 caches and FL.K3 copy of the mixed map (zero-filled), allocated on first use
+int ensure_mixed(fdga_handle* h) {
+    if (h->cachef) return FDGA_OK;
+    AL(h->cachef, 10 * h->n3);
+    AL(h->FLK3f, 3 * h->n3);
+    AL(h->d_err, 1);
+    if (k3_tc_supported(h->d)) CK(prepare_bse_K3_tc(h->d));
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+// a tensor-core wait that timed out inside a kernel (bounded polling) is reported here
+int check_device_error(fdga_handle* h) {
+    if (!h->d_err) return FDGA_OK;
+    int v = 0;
+    CK(cudaMemcpyAsync(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (v) {
+        CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
+        return fail(h, FDGA_ERR_CUDA, "a tensor-core wait in the K3 contraction timed out");
+    }
+    return FDGA_OK;
+}
 
 // ---- channel views into a state vector ----
 cplx* chanK(const fdga_handle* h, cplx* S, int ch, int cls) {
@@ -417,9 +443,16 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
         stage("dyson_bubble");
     }
-    Caches C;
-    for (int i = 0; i < 10; ++i) C.c[i] = h->cache + (size_t)i * h->n3;
+    // the mixed map keeps the caches and FL.K3 in FP32: written once here, read by both K3 GEMMs
+    const bool mixed = h->precision == FDGA_MIXED;
+    if (mixed && (!h->cachef || !h->FLK3f)) return fail(h, FDGA_ERR_STATE, "mixed-precision buffers missing");
+    Caches C{};
+    for (int i = 0; i < 10; ++i) {
+        C.c[i] = h->cache + (size_t)i * h->n3;
+        C.f[i] = mixed ? h->cachef + (size_t)i * h->n3 : nullptr;
+    }
     LC(launch_build_cache(s, F, C, h->d_k3blocks, h->nk3blocks, d));
+    if (mixed && strategy != FDGA_FDPA) LC(launch_to_f32(s, h->FLK3, h->FLK3f, 3 * h->n3));
     stage("k3_cache");
     FLP FL;
     for (int c = 0; c < 3; ++c) FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
@@ -461,6 +494,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         stage("bse_L_K2");
         {  // left K3 (FL.K3)
             K3Args3 a3{};
+            K3Args3F a3f{};
             for (int i = 0; i < 3; ++i) {
                 const int ch = order[i];
                 const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
@@ -468,14 +502,23 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
                 a.A = C.c[cg]; a.B0 = C.c[cf0]; a.Pi0 = Pi0(ch);
                 a.out = h->raw3 + (size_t)ch * h->n3;
                 a3.ch[i] = ch;
+                K3ArgsF& af = a3f.a[i];
+                af.A = C.f[cg]; af.B0 = C.f[cf0]; af.Pi0 = Pi0(ch);
+                af.out = a.out;
+                a3f.ch[i] = ch;
             }
-            a3.blocks = h->d_k3blocks;
-            a3.nblocks = h->nk3blocks;
-            LC(launch_bse_K3(s, 0, a3, 3, d, h->precision == FDGA_MIXED, h->k3_tile[h->precision][0]));
+            a3.blocks = a3f.blocks = h->d_k3blocks;
+            a3.nblocks = a3f.nblocks = h->nk3blocks;
+            if (mixed && h->k3_tc && k3_tc_supported(d)) LC(launch_bse_K3_tc(s, 0, a3f, 3, d, h->d_err));
+            else if (mixed) LC(launch_bse_K3_f32(s, 0, a3f, 3, d, h->k3_tile[FDGA_MIXED][0]));
+            else LC(launch_bse_K3(s, 0, a3, 3, d, 0, h->k3_tile[FDGA_FP64][0]));
             stage("bse_L_K3_gemm");
             cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
             const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
-            LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
+            Finalize3 f3 = fin(3, h->raw3, out, grp);
+            if (mixed)
+                for (int c = 0; c < 3; ++c) f3.outf[c] = h->FLK3f + (size_t)c * h->n3;
+            LC(launch_finalize3(s, f3, 0, 1, h->n3));
         }
         stage("bse_L_K3_finalize");
     }
@@ -499,6 +542,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     stage("bse_K2");
     {  // K3
         K3Args3 a3{};
+        K3Args3F a3f{};
         for (int i = 0; i < 3; ++i) {
             const int ch = order[i];
             const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
@@ -508,10 +552,20 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3; a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
             a.out = h->raw3 + (size_t)ch * h->n3;
             a3.ch[i] = ch;
+            if (mixed) {
+                K3ArgsF& af = a3f.a[i];
+                af.A = C.f[cf]; af.B0 = C.f[cf0]; af.G = C.f[cg]; af.Pi = a.Pi; af.Pi0 = a.Pi0;
+                af.FLc = h->FLK3f + (size_t)ch * h->n3; af.FLt = h->FLK3f + (size_t)CH_T * h->n3;
+                af.FLa = h->FLK3f + (size_t)CH_A * h->n3;
+                af.out = a.out;
+                a3f.ch[i] = ch;
+            }
         }
-        a3.blocks = h->d_k3blocks;
-        a3.nblocks = h->nk3blocks;
-        LC(launch_bse_K3(s, 1, a3, 3, d, h->precision == FDGA_MIXED, h->k3_tile[h->precision][1]));
+        a3.blocks = a3f.blocks = h->d_k3blocks;
+        a3.nblocks = a3f.nblocks = h->nk3blocks;
+        if (mixed && h->k3_tc && k3_tc_supported(d)) LC(launch_bse_K3_tc(s, 1, a3f, 3, d, h->d_err));
+        else if (mixed) LC(launch_bse_K3_f32(s, 1, a3f, 3, d, h->k3_tile[FDGA_MIXED][1]));
+        else LC(launch_bse_K3(s, 1, a3, 3, d, 0, h->k3_tile[FDGA_FP64][1]));
         stage("bse_K3_gemm");
         cplx* out[3] = {chanK(h, h->yS, CH_P, 3), chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3)};
         const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
@@ -680,7 +734,7 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     if (c->nR[0] < 1 || c->nR[1] < 1) return bad("RefVertex box must be >= 1");
     fdga_handle* h = new fdga_handle();
     h->cfg = *c;
-    h->precision = c->precision;
+    h->precision = FDGA_FP64;  // the config's precision is applied once the buffers exist (below)
     make_dims(c, h->d);
     Dims& d = h->d;
     h->nGk = (size_t)d.NG * d.Nk;
@@ -753,6 +807,10 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     }
 #undef ALC
     if (cudaStreamSynchronize(h->st) != cudaSuccess) return fin_err(fail(h, FDGA_ERR_CUDA, "create sync"));
+    if (c->precision == FDGA_MIXED) {
+        if ((r = ensure_mixed(h))) return fin_err(r);
+        h->precision = FDGA_MIXED;
+    }
     *out = h;
     return FDGA_OK;
 }
@@ -891,7 +949,7 @@ int fdga_iterate(fdga_handle* h, int strategy, int update_sigma, int compute_har
     if (r) return r;
     CK(cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
-    return FDGA_OK;
+    return check_device_error(h);
 }
 
 int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size_t n) {
@@ -907,7 +965,7 @@ int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size
     CK(launch_gather(h->st, h->yS, h->tmpS, h->perm, n));
     CK(cudaMemcpyAsync(R, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    return FDGA_OK;
+    return check_device_error(h);
 }
 
 int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int* iters, double* res,
@@ -1029,6 +1087,7 @@ int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, doub
     cplx* R = h->aa_R;
     cplx* pp[2] = {h->aa_part, h->aa_part + NBLK_RED};
     cplx* pdot = h->aa_part + 2 * NBLK_RED;
+    if (int r = ensure_mixed(h)) return r;
     const int prec0 = h->precision;
     struct Restore {  // the handle's precision is restored on every exit
         fdga_handle* h; int p;
@@ -1430,6 +1489,7 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
     int r = ensure_krylov(h, restart);
     if (r) return r;
     const size_t nc = h->nc;
+    if (jvp_precision == FDGA_MIXED && (r = ensure_mixed(h))) return r;
     const int prec0 = h->precision;
     struct Restore {
         fdga_handle* h; int p;
@@ -1456,6 +1516,7 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
     if (resid < tol) converged = true;
     CK(cudaMemcpyAsync(x, h->yS, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
     bool have_y = false;
+    int jvp_prec = jvp_precision;  // mixed JVPs until a step gains less than 2x, FP64 JVPs after that
     while (!converged) {
         h->precision = FDGA_FP64;
         if (!have_y) {
@@ -1474,10 +1535,12 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
         ++nouter;
         if (resid < tol) { converged = true; break; }
         if (n64 + nmix + 3 > maxiter) break;
+        // the mixed JVPs' rounding floor stalls Newton on ill-conditioned Jacobians: switch to FP64
+        if (jvp_prec == FDGA_MIXED && nouter > 3 && !(resid < 0.5 * prev)) jvp_prec = FDGA_FP64;
         // forcing term (Eisenstat–Walker choice 2, bounded); the mixed map's rounding floor bounds it below
         double eta = nouter <= 2 ? 0.1 : std::min(0.1, 0.9 * (resid / prev) * (resid / prev));
-        eta = std::max(eta, jvp_precision == FDGA_MIXED ? 1e-3 : 1e-6);
-        if (jvp_precision == FDGA_MIXED) {
+        eta = std::max(eta, jvp_prec == FDGA_MIXED ? 1e-3 : 1e-6);
+        if (jvp_prec == FDGA_MIXED) {
             h->precision = FDGA_MIXED;
             CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
             if ((r = run_iteration(h, strategy, true, true))) return r;
@@ -1487,7 +1550,7 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
         int nmaps = 0, its = 0;
         double relres = 1.0;
         const int left = maxiter - n64 - nmix - 1;
-        const double eps_rel = jvp_precision == FDGA_MIXED ? 3e-4 : 1e-7;
+        const double eps_rel = jvp_prec == FDGA_MIXED ? 3e-4 : 1e-7;
         // (I − J) dx = F
         r = gmres_solve(h, strategy, x, yb, F, dx, restart, 1, eta, eps_rel, false, left, nmaps, its, relres);
         if (r) return r;
@@ -1645,8 +1708,23 @@ int fdga_occupation(fdga_handle* h, double* n) {
 int fdga_set_precision(fdga_handle* h, int precision) {
     if (!h) return FDGA_ERR_ARG;
     if (precision != FDGA_FP64 && precision != FDGA_MIXED) return fail(h, FDGA_ERR_ARG, "unknown precision");
+    if (precision == FDGA_MIXED) {
+        int r = ensure_mixed(h);
+        if (r) return r;
+    }
     h->precision = precision;
     return FDGA_OK;
+}
+
+int fdga_set_option(fdga_handle* h, const char* key, int value) {
+    if (!h || !key) return FDGA_ERR_ARG;
+    const std::string k(key);
+    if (k == "k3_tensor_cores") {
+        h->k3_tc = value ? 1 : 0;
+        drop_graphs(h);
+        return FDGA_OK;
+    }
+    return fail(h, FDGA_ERR_ARG, "unknown option " + k);
 }
 
 int fdga_susceptibility(fdga_handle* h, int channel, double* out, size_t n) {
@@ -1786,6 +1864,7 @@ int fdga_autotune(fdga_handle* h, int strategy, int* tiles) {
     if (!h) return FDGA_ERR_ARG;
     if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
     if (h->c0_dirty) { int r = compute_C0(h); if (r) return r; }
+    if (int r = ensure_mixed(h)) return r;
     // size classes shared by all handles of the process: (Nν3, local, precision) -> (tile L_K3, tile K3)
     static std::mutex mu;
     static std::map<std::tuple<int, int, int>, std::pair<int, int>> cache;
@@ -1911,6 +1990,8 @@ int fdga_batch_iterate(fdga_batch* b, int strategy, int precision) {
     }
     cudaGraphExec_t& ex = b->exec[strategy][precision];
     if (!ex) {
+        for (auto* h : b->hs)
+            if (precision == FDGA_MIXED && ensure_mixed(h)) { b->err = h->err; return FDGA_ERR_OOM; }
         for (auto* h : b->hs)
             if (h->c0_dirty) {
                 int r = compute_C0(h);

@@ -198,6 +198,9 @@ class _Solver:
         self._check(self._lib.fdga_get_named(self._h, name.encode(), out.ctypes.data, out.size))
         return out
 
+    def set_option(self, key, value):
+        self._check(self._lib.fdga_set_option(self._h, key.encode(), int(value)))
+
     def set_precision(self, precision):
         """'fp64' (plain path) or 'mixed' (K3 contractions in FP32) for later iterate/residual calls."""
         self._check(self._lib.fdga_set_precision(self._h, {"fp64": 0, "mixed": 1}[precision]))

@@ -102,6 +102,11 @@ int fdga_iterate(fdga_handle* h, int strategy, int update_sigma, int compute_har
 /* Arithmetic of subsequent fdga_iterate / fdga_residual / fdga_solve calls on this handle. */
 int fdga_set_precision(fdga_handle* h, int precision);
 
+/* Integer options: "k3_tensor_cores" (default 1): the mixed map's K3 contractions run on the
+ * tensor cores (tcgen05, TF32 hi/lo split, FP32 accumulation) when 2·Nν3 ≤ 256 and Nν3 is a
+ * multiple of 8, else as FP32 CUDA-core GEMMs. */
+int fdga_set_option(fdga_handle* h, const char* key, int value);
+
 /* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.
  * x and R are host arrays of fdga_state_len elements. */
 int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size_t n);
@@ -131,7 +136,8 @@ int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, doub
 /* Newton–Krylov solve of the fixed point x = Φ(x): Newton steps (I − J) dx = Φ(x) − x solved by
  * one GMRES(restart) cycle to an Eisenstat–Walker forcing tolerance, then a backtracking line
  * search on the FP64 residual.  J is applied as forward differences of the map in jvp_precision
- * (FDGA_FP64, or FDGA_MIXED for the FP32-contraction map); the state is real-linear, so GMRES
+ * (FDGA_FP64, or FDGA_MIXED for the FP32-contraction map, which gives way to FP64 JVPs once a
+ * Newton step gains less than 2x: its rounding floor); the state is real-linear, so GMRES
  * runs on it as a real vector (Krylov basis in FP32, Hessenberg and iterate in FP64).
  * Convergence is tested on the FP64 residual.  Outputs as fdga_solve_mixed (*iters = Newton
  * residual evaluations). */
