@@ -35,6 +35,8 @@ WORKLOADS = {
                "synthetic RefVertex, init_sym_grp",
     "config3": "Hubbard 16x16 NL fdPA: t=1 t'=-0.2 n=0.9 U=3 beta=10 nK1=80 nK2=(40,40) nK3=(20,40) nG=80 mPi=32, "
                "init_sym_grp",
+    "config3s": "Hubbard 4x4 NL fdPA with config 3's boxes: t=1 t'=-0.2 n=0.9 U=3 beta=10 nK1=80 nK2=(40,40) "
+                "nK3=(20,40) nG=80 mPi=32, init_sym_grp (profiling size)",
     "config5": "Hubbard 24x24 NL fdPA: t=1 t'=0 mu=0 U=2.5 beta=8 nK1=96 nK2=(48,48) nK3=(24,48) nG=96 mPi=32, "
                "init_sym_grp",
 }

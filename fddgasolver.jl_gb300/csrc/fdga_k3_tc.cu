@@ -11,7 +11,7 @@
 // FP32 caches); each is split into TF32 hi + lo and the product accumulates hi·hi + hi·lo + lo·hi
 // (kind::tf32, FP32 accumulation in tensor memory), which keeps FP32-level accuracy.
 //
-// One CTA of 128 threads per block: rows ν < N of the 128-lane accumulator, 2N ≤ 256 columns.
+// One CTA of 512 threads per block: rows ν < N of the 128-lane accumulator, 2N ≤ 256 columns.
 // K runs in chunks of 16 ω (32 real k); two shared-memory stages; the threads stage chunk c+1
 // while the tensor core works on chunk c (tcgen05.commit -> mbarrier).  Shared-memory operands use
 // the no-swizzle K-major canonical layout: 8-row x 16-byte core matrices, K-adjacent core
@@ -23,7 +23,7 @@ namespace fdga {
 
 namespace {
 
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 512;  // 16 warps stage the operands; warps 4q..4q+3 read TMEM lanes 32q..
 constexpr int KC = 32;                      // real K per chunk (16 ω)
 constexpr int A_BYTES = 128 * KC * 4;       // one A operand (hi or lo) of a chunk: 16 KB
 constexpr uint32_t SPIN_LIMIT = 1u << 22;   // bounded mbarrier polling
@@ -127,19 +127,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
             for (int j = 0; j < 4; ++j) pis[tid][j] = v[j];
         }
         __syncthreads();
-        // A: row ν = tid, 16 ω of the chunk
-        {
-            const int nu = tid;
-            for (int t = 0; t < 16; ++t) {
-                const int w = w0 + t;
-                cplxf v{0.f, 0.f};
-                if (nu < N && w < N) {
-                    const float2 q = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w));
-                    v = cplxf{q.x, q.y};
-                }
-                st_pair(Ahi, op_off(nu, 2 * t), v.x, Alo);
-                st_pair(Ahi, op_off(nu, 2 * t + 1), v.y, Alo);
+        // A: (row ν, ω) items, 16 consecutive ω of one row per 16 threads (coalesced loads)
+        for (int e = tid; e < 128 * 16; e += TC_THREADS) {
+            const int nu = e >> 4, t = e & 15, w = w0 + t;
+            cplxf v{0.f, 0.f};
+            if (nu < N && w < N) {
+                const float2 q = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w));
+                v = cplxf{q.x, q.y};
             }
+            st_pair(Ahi, op_off(nu, 2 * t), v.x, Alo);
+            st_pair(Ahi, op_off(nu, 2 * t + 1), v.y, Alo);
         }
         // B: (t, ν') items of the chunk
         for (int e = tid; e < 16 * N; e += TC_THREADS) {
@@ -203,12 +200,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
     } else {
-        // epilogue: warp w reads lanes 32w..32w+31 (rows ν), 16 columns (8 complex) per load
-        const int nu = 32 * warp + lane;
+        // epilogue: warp w reads lanes 32(w%4).. (rows ν), every 4th group of 16 columns from 16(w/4)
+        const int q = warp & 3, grp = warp >> 2;
+        const int nu = 32 * q + lane;
         const double T = d.T;
-        for (int c0 = 0; c0 < NN; c0 += 16) {
+        for (int c0 = 16 * grp; c0 < NN; c0 += 64) {
             uint32_t r[16];
-            const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+            const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0;
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
                 "[%16];"

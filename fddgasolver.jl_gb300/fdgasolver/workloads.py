@@ -29,6 +29,9 @@ CONFIGS = {
                     nK3=(8, 12), mPi_factor=32, refvertex_noise=0.05, seed=20261203),
     "config3": dict(kind="hubbard", T=0.1, U=3.0, mu=None, filling=0.9, t1=1.0, t2=-0.2, L=16, nG=80, nK1=80,
                     nK2=(40, 40), nK3=(20, 40), mPi_factor=32),
+    # config 3's frequency boxes on a 4x4 lattice: the size the K3 tensor-core kernel is profiled at
+    "config3s": dict(kind="hubbard", T=0.1, U=3.0, mu=None, filling=0.9, t1=1.0, t2=-0.2, L=4, nG=80, nK1=80,
+                     nK2=(40, 40), nK3=(20, 40), mPi_factor=32),
     "config5": dict(kind="hubbard", T=0.125, U=2.5, mu=0.0, t1=1.0, t2=0.0, L=24, nG=96, nK1=96, nK2=(48, 48),
                     nK3=(24, 48), mPi_factor=32),
 }
