@@ -56,6 +56,9 @@ __host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) {
 }
 __host__ __device__ __forceinline__ cplxf operator*(cplxf a, float s) { return cplxf{a.x * s, a.y * s}; }
 __host__ __device__ __forceinline__ cplxf& operator+=(cplxf& a, cplxf b) { a.x += b.x; a.y += b.y; return a; }
+__host__ __device__ __forceinline__ cplxf& operator-=(cplxf& a, cplxf b) { a.x -= b.x; a.y -= b.y; return a; }
+__host__ __device__ __forceinline__ cplxf operator-(cplxf a) { return cplxf{-a.x, -a.y}; }
+__host__ __device__ __forceinline__ cplxf conjg(cplxf a) { return cplxf{a.x, -a.y}; }
 // c + a·b with four fused multiply-adds (a complex product followed by an add costs six)
 __device__ __forceinline__ cplx cfma(cplx a, cplx b, cplx c) {
     return cplx{fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y))};
@@ -69,10 +72,13 @@ template <> __device__ __forceinline__ cplx to_c<cplx>(cplx v) { return v; }
 template <> __device__ __forceinline__ cplxf to_c<cplxf>(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
 __device__ __forceinline__ cplx to_d(cplx v) { return v; }
 __device__ __forceinline__ cplx to_d(cplxf v) { return cplx{(double)v.x, (double)v.y}; }
+__device__ __forceinline__ cplxf to_f32(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+__device__ __forceinline__ cplxf to_f32(cplxf v) { return v; }
 template <class C> __device__ __forceinline__ C czero() { return C{0, 0}; }
 
 // symmetry operation bits: 1 = negate, 2 = conjugate (MatsubaraFunctions Operation(sgn, con))
-__device__ __forceinline__ cplx apply_op(int op, cplx v) {
+template <class S>
+__device__ __forceinline__ S apply_op(int op, S v) {
     if (op & 2) v.y = -v.y;
     if (op & 1) { v.x = -v.x; v.y = -v.y; }
     return v;
@@ -97,23 +103,36 @@ struct Dims {
     double T, U;
 };
 
-// One channel's K1/K2/K3 and their momentum averages (A* alias K* for the local solver).
-struct ChanP {
-    const cplx* K1;
-    const cplx* K2;
-    const cplx* K3;
-    const cplx* A1;
-    const cplx* A2;
-    const cplx* A3;
+// One channel's K1/K2/K3 and their momentum averages (A* alias K* for the local solver), stored
+// as S (cplx; cplxf for the FP32 mirror of the mixed map).  Evaluators compute in S.
+template <class S>
+struct ChanPT {
+    const S* K1;
+    const S* K2;
+    const S* K3;
+    const S* A1;
+    const S* A2;
+    const S* A3;
 };
 // Target vertex F: RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x) + γp + γt + γa
-struct VertP {
-    ChanP g[3];
-    const cplx* Fp_p;
-    const cplx* Fp_x;
-    const cplx* Ft_p;
-    const cplx* Ft_x;
+template <class S>
+struct VertPT {
+    ChanPT<S> g[3];
+    const S* Fp_p;
+    const S* Fp_x;
+    const S* Ft_p;
+    const S* Ft_x;
 };
+using ChanP = ChanPT<cplx>;
+using VertP = VertPT<cplx>;
+using VertPF = VertPT<cplxf>;
+
+__device__ __forceinline__ cplx ldv(const cplx* p) { return ldg(p); }
+__device__ __forceinline__ cplxf ldv(const cplxf* p) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return cplxf{v.x, v.y};
+}
+template <class S> __device__ __forceinline__ S cre(double x) { return S{(decltype(S::x))x, 0}; }
 
 __device__ __forceinline__ size_t ix1(const Dims& d, int P, int m) { return (size_t)P * d.N1 + (m + d.n1 - 1); }
 __device__ __forceinline__ size_t ix2(const Dims& d, int P, int m, int n) {
@@ -127,19 +146,23 @@ __device__ __forceinline__ size_t ixPi(const Dims& d, int P, int m, int n) {
 }
 __device__ __forceinline__ size_t ixG(const Dims& d, int k, int n) { return (size_t)k * d.NG + (n + d.nG); }
 
-__device__ __forceinline__ cplx k1v(const ChanP& c, const Dims& d, int m, int P) {
-    return P == KAVG ? ldg(c.A1 + (m + d.n1 - 1)) : ldg(c.K1 + ix1(d, P, m));
+template <class S>
+__device__ __forceinline__ S k1v(const ChanPT<S>& c, const Dims& d, int m, int P) {
+    return P == KAVG ? ldv(c.A1 + (m + d.n1 - 1)) : ldv(c.K1 + ix1(d, P, m));
 }
-__device__ __forceinline__ cplx k2v(const ChanP& c, const Dims& d, int m, int n, int P) {
-    return P == KAVG ? ldg(c.A2 + ix2(d, 0, m, n)) : ldg(c.K2 + ix2(d, P, m, n));
+template <class S>
+__device__ __forceinline__ S k2v(const ChanPT<S>& c, const Dims& d, int m, int n, int P) {
+    return P == KAVG ? ldv(c.A2 + ix2(d, 0, m, n)) : ldv(c.K2 + ix2(d, P, m, n));
 }
-__device__ __forceinline__ cplx k3v(const ChanP& c, const Dims& d, int m, int n, int np, int P) {
-    return P == KAVG ? ldg(c.A3 + ix3(d, 0, m, n, np)) : ldg(c.K3 + ix3(d, P, m, n, np));
+template <class S>
+__device__ __forceinline__ S k3v(const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
+    return P == KAVG ? ldv(c.A3 + ix3(d, 0, m, n, np)) : ldv(c.K3 + ix3(d, P, m, n, np));
 }
 
 // Channel evaluator γ(Ω, ν, ν', P): src/channel.jl:220-339, src/nonlocal/channel.jl:246-382.
-__device__ __forceinline__ cplx chan_eval(const ChanP& c, const Dims& d, int m, int n, int np, int P) {
-    cplx v = mk(0, 0);
+template <class S>
+__device__ __forceinline__ S chan_eval(const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
+    S v{0, 0};
     const bool ninf = (n == FINF), npinf = (np == FINF);
     if (!bin(m, d.n1)) return v;
     v += k1v(c, d, m, P);
@@ -178,28 +201,33 @@ __device__ __forceinline__ void conv(int from, int to, int m, int n, int np, int
 }
 
 // RefVertex corrections: MeshFunction call, zero outside the box.
-__device__ __forceinline__ cplx ref_call(const cplx* f, const Dims& d, int m, int n, int np) {
-    if (!bin(m, d.nRO) || !fin(n, d.nRn) || !fin(np, d.nRn)) return mk(0, 0);
-    return ldg(f + (size_t)(m + d.nRO - 1) + (size_t)d.NRO * ((size_t)(n + d.nRn) + (size_t)d.NRn * (np + d.nRn)));
+template <class S>
+__device__ __forceinline__ S ref_call(const S* f, const Dims& d, int m, int n, int np) {
+    if (!bin(m, d.nRO) || !fin(n, d.nRn) || !fin(np, d.nRn)) return S{0, 0};
+    return ldv(f + (size_t)(m + d.nRO - 1) + (size_t)d.NRO * ((size_t)(n + d.nRn) + (size_t)d.NRn * (np + d.nRn)));
 }
 // RefVertex in the parallel spin component (src/refvertex.jl:90-125, 178-216).
-__device__ __forceinline__ cplx ref_pSp(const VertP& F, const Dims& d, int ch, int m, int n, int np) {
-    if (n == FINF || np == FINF) return mk(d.U, 0);
-    if (ch == CH_P) return ref_call(F.Fp_p, d, m, n, np) + mk(d.U, 0);
-    if (ch == CH_T) return ref_call(F.Ft_p, d, m, n, np) + mk(d.U, 0);
-    return mk(d.U, 0) - ref_call(F.Ft_x, d, m, np, n);
+template <class S>
+__device__ __forceinline__ S ref_pSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np) {
+    if (n == FINF || np == FINF) return cre<S>(d.U);
+    if (ch == CH_P) return ref_call(F.Fp_p, d, m, n, np) + cre<S>(d.U);
+    if (ch == CH_T) return ref_call(F.Ft_p, d, m, n, np) + cre<S>(d.U);
+    return cre<S>(d.U) - ref_call(F.Ft_x, d, m, np, n);
 }
 // RefVertex in the crossed spin component (src/refvertex.jl:127-164).
-__device__ __forceinline__ cplx ref_xSp(const VertP& F, const Dims& d, int ch, int m, int n, int np) {
-    if (n == FINF || np == FINF) return mk(-d.U, 0);
-    if (ch == CH_P) return ref_call(F.Fp_x, d, m, n, np) - mk(d.U, 0);
-    if (ch == CH_T) return ref_call(F.Ft_x, d, m, n, np) - mk(d.U, 0);
-    return -ref_call(F.Ft_p, d, m, np, n) - mk(d.U, 0);
+template <class S>
+__device__ __forceinline__ S ref_xSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np) {
+    if (n == FINF || np == FINF) return cre<S>(-d.U);
+    if (ch == CH_P) return ref_call(F.Fp_x, d, m, n, np) - cre<S>(d.U);
+    if (ch == CH_T) return ref_call(F.Ft_x, d, m, n, np) - cre<S>(d.U);
+    return -ref_call(F.Ft_p, d, m, np, n) - cre<S>(d.U);
 }
-__device__ __forceinline__ cplx ref_eval(const VertP& F, const Dims& d, int ch, int sp, int m, int n, int np) {
+template <class S>
+__device__ __forceinline__ S ref_eval(const VertPT<S>& F, const Dims& d, int ch, int sp, int m, int n, int np) {
+    using R = decltype(S::x);
     if (sp == SP_P) return ref_pSp(F, d, ch, m, n, np);
     if (sp == SP_X) return ref_xSp(F, d, ch, m, n, np);
-    return 2.0 * ref_pSp(F, d, ch, m, n, np) + ref_xSp(F, d, ch, m, n, np);
+    return ref_pSp(F, d, ch, m, n, np) * (R)2 + ref_xSp(F, d, ch, m, n, np);
 }
 
 // Flags of the vertex evaluator: bit 0 F0, bit 1 γp, bit 2 γt, bit 3 γa.
@@ -210,8 +238,9 @@ __device__ __forceinline__ int swap_ta(int fl) {
 
 // Vertex in the parallel spin component with momenta (P, kSW, kSW):
 // src/vertex.jl:209-284, src/nonlocal/vertex.jl:69-153, 216-379.
-__device__ __forceinline__ cplx vert_pSp(const VertP& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
-    cplx v = mk(0, 0);
+template <class S>
+__device__ __forceinline__ S vert_pSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
+    S v{0, 0};
     if (fl & FL_F0) v += ref_pSp(F, d, ch, m, n, np);
     if (n == FINF || np == FINF) {
         const int bit = (ch == CH_P) ? FL_GP : (ch == CH_T ? FL_GT : FL_GA);
@@ -225,29 +254,34 @@ __device__ __forceinline__ cplx vert_pSp(const VertP& F, const Dims& d, int ch, 
     return v;
 }
 // Crossed component via crossing symmetry (src/vertex.jl:288-313).
-__device__ __forceinline__ cplx vert_xSp(const VertP& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
+template <class S>
+__device__ __forceinline__ S vert_xSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
     const int sw = swap_ta(fl);
     if (ch == CH_P) return -vert_pSp(F, d, CH_P, m, n, (np == FINF) ? FINF : m - np - 1, P, sw);
     if (ch == CH_T) return -vert_pSp(F, d, CH_A, m, n, np, P, sw);
     return -vert_pSp(F, d, CH_T, m, n, np, P, sw);
 }
-__device__ __forceinline__ cplx vert_eval(const VertP& F, const Dims& d, int ch, int sp, int m, int n, int np, int P,
-                                          int fl = FL_ALL) {
+template <class S>
+__device__ __forceinline__ S vert_eval(const VertPT<S>& F, const Dims& d, int ch, int sp, int m, int n, int np, int P,
+                                       int fl = FL_ALL) {
+    using R = decltype(S::x);
     if (sp == SP_P) return vert_pSp(F, d, ch, m, n, np, P, fl);
     if (sp == SP_X) return vert_xSp(F, d, ch, m, n, np, P, fl);
-    cplx v = vert_pSp(F, d, ch, m, n, np, P, fl) * 2.0;
+    S v = vert_pSp(F, d, ch, m, n, np, P, fl) * (R)2;
     v += vert_xSp(F, d, ch, m, n, np, P, fl);
     return v;
 }
 
 // FL(Ω, ω, νInf, Ch, Sp): FL has F0 = RefVertex(0) and K1 = 0, so only its K2 survives.
-__device__ __forceinline__ cplx fl_right(const cplx* FLK2p, const cplx* FLK2t, const cplx* FLK2a, const Dims& d,
-                                         int ch, int m, int n, int P) {
-    if (!bin(m, d.n2O) || !fin(n, d.n2n)) return mk(0, 0);
+template <class S>
+__device__ __forceinline__ S fl_right(const S* FLK2p, const S* FLK2t, const S* FLK2a, const Dims& d, int ch, int m,
+                                      int n, int P) {
+    using R = decltype(S::x);
+    if (!bin(m, d.n2O) || !fin(n, d.n2n)) return S{0, 0};
     const size_t i = ix2(d, P, m, n);
-    if (ch == CH_P) return ldg(FLK2p + i);
-    if (ch == CH_A) return ldg(FLK2a + i);
-    return 2.0 * ldg(FLK2t + i) - ldg(FLK2a + i);  // dSp = 2 pSp + xSp, xSp(t) = -pSp(a)
+    if (ch == CH_P) return ldv(FLK2p + i);
+    if (ch == CH_A) return ldv(FLK2a + i);
+    return ldv(FLK2t + i) * (R)2 - ldv(FLK2a + i);  // dSp = 2 pSp + xSp, xSp(t) = -pSp(a)
 }
 
 __device__ __forceinline__ int cross(int ch, int m, int n) { return ch == CH_P ? m - n - 1 : n; }
@@ -288,6 +322,14 @@ struct Windows {
     }
 };
 
+__device__ __forceinline__ cplxf warp_sum(cplxf v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
 // warp reduction of a complex double
 __device__ __forceinline__ cplx warp_sum(cplx v) {
 #pragma unroll

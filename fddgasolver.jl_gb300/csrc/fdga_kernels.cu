@@ -345,7 +345,10 @@ __global__ void k_qavg(const ChanArrays in, ChanArraysW out, Dims d) {
 // symmetry-class representatives; all blocks without groups); "left" caches use (Ω, ω=a, ν'=b),
 // "right" caches (Ω, ν=a, ω=b).  Output order: Γpx F0p F0a F0t Γpp Γa Γt Fp Fa Ft.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_build_cache(VertP F, Caches C, const int* blocks, int nblocks, Dims d) {
+// S: vertex storage and arithmetic (cplx; cplxf reads the FP32 mirror of the mixed map).
+template <class S>
+__global__ void k_build_cache(VertPT<S> F, Caches C, const int* blocks, int nblocks, Dims d) {
+    using R = decltype(S::x);
     const size_t bs = (size_t)d.N3n * d.N3n;
     const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (t >= (size_t)nblocks * bs) return;
@@ -357,32 +360,32 @@ __global__ void k_build_cache(VertP F, Caches C, const int* blocks, int nblocks,
     const int m = bl % d.N3O - (d.n3O - 1);
     const int P = bl / d.N3O;
     // left
-    cplx v[10];
+    S v[10];
     v[0] = vert_eval(F, d, CH_P, SP_X, m, a, b, P, FL_GT | FL_GA);
     v[1] = ref_xSp(F, d, CH_P, m, a, b) - ref_xSp(F, d, CH_P, m, a, FINF);
-    const cplx f0a = ref_pSp(F, d, CH_A, m, a, b) - ref_pSp(F, d, CH_A, m, a, FINF);
-    const cplx f0t = ref_pSp(F, d, CH_T, m, a, b) - ref_pSp(F, d, CH_T, m, a, FINF);
+    const S f0a = ref_pSp(F, d, CH_A, m, a, b) - ref_pSp(F, d, CH_A, m, a, FINF);
+    const S f0t = ref_pSp(F, d, CH_T, m, a, b) - ref_pSp(F, d, CH_T, m, a, FINF);
     v[2] = f0a;
-    v[3] = 2.0 * f0t - f0a;
+    v[3] = f0t * (R)2 - f0a;
     // right
-    const cplx gpp = vert_pSp(F, d, CH_P, m, a, b, P, FL_GT | FL_GA);
-    const cplx ga = vert_pSp(F, d, CH_A, m, a, b, P, FL_GP | FL_GT);
-    const cplx gt = vert_pSp(F, d, CH_T, m, a, b, P, FL_GP | FL_GA);
-    const cplx fp = vert_pSp(F, d, CH_P, m, a, b, P, FL_F0 | FL_GP) - vert_pSp(F, d, CH_P, m, FINF, b, P, FL_F0 | FL_GP) + gpp;
-    const cplx fa = vert_pSp(F, d, CH_A, m, a, b, P, FL_F0 | FL_GA) - vert_pSp(F, d, CH_A, m, FINF, b, P, FL_F0 | FL_GA) + ga;
-    const cplx ft = vert_pSp(F, d, CH_T, m, a, b, P, FL_F0 | FL_GT) - vert_pSp(F, d, CH_T, m, FINF, b, P, FL_F0 | FL_GT) + gt;
+    const S gpp = vert_pSp(F, d, CH_P, m, a, b, P, FL_GT | FL_GA);
+    const S ga = vert_pSp(F, d, CH_A, m, a, b, P, FL_GP | FL_GT);
+    const S gt = vert_pSp(F, d, CH_T, m, a, b, P, FL_GP | FL_GA);
+    const S fp = vert_pSp(F, d, CH_P, m, a, b, P, FL_F0 | FL_GP) - vert_pSp(F, d, CH_P, m, FINF, b, P, FL_F0 | FL_GP) + gpp;
+    const S fa = vert_pSp(F, d, CH_A, m, a, b, P, FL_F0 | FL_GA) - vert_pSp(F, d, CH_A, m, FINF, b, P, FL_F0 | FL_GA) + ga;
+    const S ft = vert_pSp(F, d, CH_T, m, a, b, P, FL_F0 | FL_GT) - vert_pSp(F, d, CH_T, m, FINF, b, P, FL_F0 | FL_GT) + gt;
     v[4] = gpp;
     v[5] = ga;
-    v[6] = gt * 2.0 - ga;
+    v[6] = gt * (R)2 - ga;
     v[7] = fp;
     v[8] = fa;
-    v[9] = ft * 2.0 - fa;
+    v[9] = ft * (R)2 - fa;
     if (C.f[0]) {
 #pragma unroll
-        for (int k = 0; k < 10; ++k) C.f[k][i] = to_c<cplxf>(v[k]);
+        for (int k = 0; k < 10; ++k) C.f[k][i] = to_f32(v[k]);
     } else {
 #pragma unroll
-        for (int k = 0; k < 10; ++k) C.c[k][i] = v[k];
+        for (int k = 0; k < 10; ++k) C.c[k][i] = to_d(v[k]);
     }
 }
 
@@ -474,31 +477,32 @@ __global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const 
 // F(Ω,∞,ω) depends on ω only through the same channel's K2(Ω, ω) (ω in the K2 box), so the sum is
 // evaluated exactly as c·S_X + Σ_{ω ∈ K2 box} (F(Ω,∞,ω) - c) X(ω), c = F(Ω,∞,∞).
 // ---------------------------------------------------------------------------------------------
-template <int CH>
-__device__ __forceinline__ void bse_K1_body(const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+template <int CH, class S>
+__device__ __forceinline__ void bse_K1_body(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
                                             const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
+    using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
     const int m = idx % d.N1 - (d.n1 - 1), P = idx / d.N1;
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
-    const cplx c = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
-    cplx acc = mk(0, 0);
+    const S c = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    S acc{0, 0};
     if (bin(m, d.n2O)) {
         for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
             if (!fin(n, d.nPw)) continue;
             const int wt = cross(CH, m, n);
-            const cplx Fl = vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
-            const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
+            const S Fl = vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
+            const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
             const size_t ip = ixPi(d, P, m, n);
-            const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
-            acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * d.U), acc);
+            const S pi = to_c<S>(ldg(Pi + ip)), pi0 = to_c<S>(ldg(Pi0 + ip));
+            acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
         }
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-        const cplx sx = SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)];
-        out[idx] = (c * sx + acc) * (d.T * (CH == CH_T ? -1.0 : 1.0));
+        const S sx = to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]);
+        out[idx] = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
     }
 }
 
@@ -507,9 +511,10 @@ __device__ __forceinline__ void bse_K1_body(const VertP& F, const FLP& FL, const
 //   local (src/BSEa/BSEa_K2.jl:1-40):        Σ_{ω∈Π mesh} Γ_irr(Ω,ν,ω) Π0(Ω,ω) U
 //   nonlocal (src/nonlocal/BSEa/BSEa_K2.jl:1-39): Σ_{ω∈K2 mesh} Γ_irr(Ω,ν,ω̃) Π0(Ω,ω) U
 // ---------------------------------------------------------------------------------------------
-template <int CH>
-__device__ __forceinline__ void bse_L_K2_body(const VertP& F, const cplx* Pi0, cplx* out, const int* items, int nitems,
-                                              const Dims& d) {
+template <int CH, class S>
+__device__ __forceinline__ void bse_L_K2_body(const VertPT<S>& F, const cplx* Pi0, cplx* out, const int* items,
+                                              int nitems, const Dims& d) {
+    using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
@@ -518,20 +523,20 @@ __device__ __forceinline__ void bse_L_K2_body(const VertP& F, const cplx* Pi0, c
     const int P = idx / (d.N2n * d.N2O);
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     constexpr int IRR = (CH == CH_P) ? (FL_GT | FL_GA) : (CH == CH_T ? (FL_GP | FL_GA) : (FL_GP | FL_GT));
-    cplx acc = mk(0, 0);
+    S acc{0, 0};
     if (d.local) {
         for (int n = -d.nPw + lane; n < d.nPw; n += 32) {  // local solver: nPw = nPn
-            const cplx Gp = vert_eval(F, d, CH, SP, m, nu, n, P, IRR);
-            acc = cfma(Gp, ldg(Pi0 + ixPi(d, P, m, n)), acc);
+            const S Gp = vert_eval(F, d, CH, SP, m, nu, n, P, IRR);
+            acc = cfma(Gp, to_c<S>(ldg(Pi0 + ixPi(d, P, m, n))), acc);
         }
     } else {
         for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
-            const cplx Gl = vert_eval(F, d, CH, SP, m, nu, cross(CH, m, n), P, IRR);
-            acc = cfma(Gl, ldg(Pi0 + ixPi(d, P, m, n)), acc);
+            const S Gl = vert_eval(F, d, CH, SP, m, nu, cross(CH, m, n), P, IRR);
+            acc = cfma(Gl, to_c<S>(ldg(Pi0 + ixPi(d, P, m, n))), acc);
         }
     }
     acc = warp_sum(acc);
-    if (lane == 0) out[idx] = acc * (d.U * d.T * (CH == CH_T ? -1.0 : 1.0));
+    if (lane == 0) out[idx] = to_d(acc * (R)(d.U * d.T * (CH == CH_T ? -1.0 : 1.0)));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -543,9 +548,10 @@ __device__ __forceinline__ void bse_L_K2_body(const VertP& F, const cplx* Pi0, c
 // ω-independent value c = F(Ω,ν,∞) - F(Ω,∞,∞); the sum is evaluated exactly as
 // c·S_X + Σ_{ω ∈ union} (F(Ω,ν,ω) - F(Ω,∞,ω) - c) X(ω).
 // ---------------------------------------------------------------------------------------------
-template <int CH>
-__device__ __forceinline__ void bse_K2_body(const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0,
+template <int CH, class S>
+__device__ __forceinline__ void bse_K2_body(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
                                             const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
+    using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
@@ -554,8 +560,8 @@ __device__ __forceinline__ void bse_K2_body(const VertP& F, const FLP& FL, const
     const int P = idx / (d.N2n * d.N2O);
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     // F(Ω,∞,ω) equals F(Ω,∞,∞) (bit for bit) unless ω is in the K2 box
-    const cplx cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
-    const cplx c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
+    const S cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    const S c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
     Windows win;
     const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
     win.add(-d.n2n, d.n2n - 1, lo, hi);
@@ -564,21 +570,21 @@ __device__ __forceinline__ void bse_K2_body(const VertP& F, const FLP& FL, const
     win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
     if (CH == CH_P) win.add(m - nu - 1 - h1, m - nu - 1 + h1, lo, hi);
     win.merge();
-    cplx acc = mk(0, 0);
+    S acc{0, 0};
     for (int t = lane; t < win.total; t += 32) {
         const int n = win.at(t);
         const int wt = cross(CH, m, n);
-        const cplx Finf = fin(n, d.n2n) ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
-        const cplx Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
-        const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
+        const S Finf = fin(n, d.n2n) ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
+        const S Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
+        const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
-        const cplx pi = ldg(Pi + ip), pi0 = ldg(Pi0 + ip);
-        acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * d.U), acc);
+        const S pi = to_c<S>(ldg(Pi + ip)), pi0 = to_c<S>(ldg(Pi0 + ip));
+        acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-        const cplx sx = SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)];
-        out[idx] = (c * sx + acc) * (d.T * (CH == CH_T ? -1.0 : 1.0));
+        const S sx = to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]);
+        out[idx] = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
     }
 }
 
@@ -696,31 +702,33 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
 // box; elsewhere it equals c = γ(…, ν, ∞), so the vertex sum is c·SΠ + Σ_{window} Π (γ - c).
 // out = T [vertex part] + T ref_scale [RefVertex part].
 // ---------------------------------------------------------------------------------------------
-template <int WHICH>
-__device__ __forceinline__ void sde_L_body(const VertP& F, const cplx* Pi, const cplx* SPi, cplx* out, const int* items,
-                                           int nitems, int use_vertex, double ref_scale, const Dims& d) {
+template <int WHICH, class S>
+__device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, const cplx* SPi, cplx* out,
+                                           const int* items, int nitems, int use_vertex, double ref_scale,
+                                           const Dims& d) {
+    using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const int idx = items ? items[w] : w;
     const int nu = idx % d.N2n - d.n2n;
     const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
     const int P = idx / (d.N2n * d.N2O);
-    cplx acc = mk(0, 0), accr = mk(0, 0), c = mk(0, 0);
+    S acc{0, 0}, accr{0, 0}, c{0, 0};
     if (use_vertex) {
         if (WHICH == 0) {
             c = chan_eval(F.g[CH_P], d, m, FINF, nu, P);
             for (int t = lane; t < d.N2n; t += 32) {
                 const int n = m - (t - d.n2n) - 1;  // Ω-ω runs over the K2 box
                 if (!fin(n, d.nPw)) continue;
-                const cplx g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P) - c;
-                acc = cfma(ldg(Pi + ixPi(d, P, m, n)), g, acc);
+                const S g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P) - c;
+                acc = cfma(to_c<S>(ldg(Pi + ixPi(d, P, m, n))), g, acc);
             }
         } else {
             c = chan_eval(F.g[CH_T], d, m, nu, FINF, P) + chan_eval(F.g[CH_A], d, m, nu, FINF, P);
             for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
                 if (!fin(n, d.nPw)) continue;
-                const cplx g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P) - c;
-                acc = cfma(ldg(Pi + ixPi(d, P, m, n)), g, acc);
+                const S g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P) - c;
+                acc = cfma(to_c<S>(ldg(Pi + ixPi(d, P, m, n))), g, acc);
             }
         }
     }
@@ -729,45 +737,49 @@ __device__ __forceinline__ void sde_L_body(const VertP& F, const cplx* Pi, const
             const int r = t - d.nRn;
             const int n = (WHICH == 0) ? m - r - 1 : r;
             if (!fin(n, d.nPw)) continue;
-            cplx g;
-            if (WHICH == 0) g = ref_pSp(F, d, CH_P, m, m - n - 1, nu) - mk(d.U, 0);
-            else g = ref_pSp(F, d, CH_A, m, nu, n) + ref_pSp(F, d, CH_T, m, nu, n) - mk(d.U, 0) - mk(d.U, 0);
-            accr = cfma(ldg(Pi + ixPi(d, P, m, n)), g, accr);
+            S g;
+            if (WHICH == 0) g = ref_pSp(F, d, CH_P, m, m - n - 1, nu) - cre<S>(d.U);
+            else g = ref_pSp(F, d, CH_A, m, nu, n) + ref_pSp(F, d, CH_T, m, nu, n) - cre<S>(d.U) - cre<S>(d.U);
+            accr = cfma(to_c<S>(ldg(Pi + ixPi(d, P, m, n))), g, accr);
         }
     }
-    acc = warp_sum(acc) * d.U;
-    accr = warp_sum(accr) * d.U;
+    acc = warp_sum(acc) * (R)d.U;
+    accr = warp_sum(accr) * (R)d.U;
     if (lane == 0) {
-        if (use_vertex) acc += c * (ldg(SPi + (size_t)P * d.NPO + (m + d.nPO - 1)) * d.U);
-        out[idx] = acc * d.T + accr * (d.T * ref_scale);
+        if (use_vertex) acc += c * (to_c<S>(ldg(SPi + (size_t)P * d.NPO + (m + d.nPO - 1))) * (R)d.U);
+        out[idx] = to_d(acc * (R)d.T + accr * (R)(d.T * ref_scale));
     }
 }
 
 // ---------------------------------------------------------------------------------------------
 // All-channel launches: blockIdx.y selects the channel (0 = p, 1 = t, 2 = a; SDE: 0 = pp, 1 = ph).
 // ---------------------------------------------------------------------------------------------
-__global__ void k_bse_K1_all(VertP F, FLP FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
+template <class S>
+__global__ void k_bse_K1_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
     switch (blockIdx.y) {
         case CH_P: bse_K1_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
         case CH_T: bse_K1_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
         default:   bse_K1_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
-__global__ void k_bse_L_K2_all(VertP F, BubbleP B, ChanWork cw, Dims d) {
+template <class S>
+__global__ void k_bse_L_K2_all(VertPT<S> F, BubbleP B, ChanWork cw, Dims d) {
     switch (blockIdx.y) {
         case CH_P: bse_L_K2_body<CH_P>(F, B.pp0, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
         case CH_T: bse_L_K2_body<CH_T>(F, B.ph0, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
         default:   bse_L_K2_body<CH_A>(F, B.ph0, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
-__global__ void k_bse_K2_all(VertP F, FLP FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
+template <class S>
+__global__ void k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
     switch (blockIdx.y) {
         case CH_P: bse_K2_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
         case CH_T: bse_K2_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
         default:   bse_K2_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
-__global__ void k_sde_L_all(VertP F, BubbleP B, const cplx* SPpp, const cplx* SPph, ChanWork cw, int use_vertex,
+template <class S>
+__global__ void k_sde_L_all(VertPT<S> F, BubbleP B, const cplx* SPpp, const cplx* SPph, ChanWork cw, int use_vertex,
                             double ref_scale, Dims d) {
     if (blockIdx.y == 0) sde_L_body<0>(F, B.pp, SPpp, cw.out[0], cw.items[0], cw.nitems[0], use_vertex, ref_scale, d);
     else sde_L_body<1>(F, B.ph, SPph, cw.out[1], cw.items[1], cw.nitems[1], use_vertex, ref_scale, d);
@@ -1088,36 +1100,50 @@ cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW&
     k_qavg<<<grid, 256, 0, s>>>(in, out, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
+template <class S>
+static cudaError_t build_cache_t(cudaStream_t s, const VertPT<S>& F, const Caches& C, const int* blocks, int nblocks,
+                                 const Dims& d) {
+    const size_t n = (size_t)nblocks * d.N3n * d.N3n;
+    k_build_cache<S><<<blocks_for(n, 128), 128, 0, s>>>(F, C, blocks, nblocks, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d) {
-    const size_t n = (size_t)nblocks * d.N3n * d.N3n;
-    k_build_cache<<<blocks_for(n, 128), 128, 0, s>>>(F, C, blocks, nblocks, d);
-    LAUNCH_CHECK(); return cudaSuccess;
+    return build_cache_t(s, F, C, blocks, nblocks, d);
+}
+cudaError_t launch_build_cache(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
+                               const Dims& d) {
+    return build_cache_t(s, F, C, blocks, nblocks, d);
 }
 static unsigned warp_grid(const ChanWork& cw, int nch) {
     int mx = 0;
     for (int c = 0; c < nch; ++c) mx = std::max(mx, cw.nitems[c]);
     return blocks_for((size_t)mx * 32, 128);
 }
-cudaError_t launch_bse_K1_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
-                              const ChanWork& cw, const Dims& d) {
-    k_bse_K1_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VertP& F, const BubbleP& B, const ChanWork& cw, const Dims& d) {
-    k_bse_L_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, cw, d);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_bse_K2_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
-                              const ChanWork& cw, const Dims& d) {
-    k_bse_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
-cudaError_t launch_sde_L_all(cudaStream_t s, const VertP& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph,
-                             const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d) {
-    k_sde_L_all<<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d);
-    LAUNCH_CHECK(); return cudaSuccess;
-}
+#define FDGA_VERTEX_LAUNCHERS(VT, FT)                                                                              \
+    cudaError_t launch_bse_K1_all(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
+                                  const ChanWork& cw, const Dims& d) {                                             \
+        k_bse_K1_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);                               \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }                                                                                                               \
+    cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VT& F, const BubbleP& B, const ChanWork& cw,             \
+                                    const Dims& d) {                                                                \
+        k_bse_L_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, cw, d);                                     \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }                                                                                                               \
+    cudaError_t launch_bse_K2_all(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
+                                  const ChanWork& cw, const Dims& d) {                                             \
+        k_bse_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);                               \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }                                                                                                               \
+    cudaError_t launch_sde_L_all(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
+                                 const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d) {             \
+        k_sde_L_all<<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d);     \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }
+FDGA_VERTEX_LAUNCHERS(VertP, FLP)
+FDGA_VERTEX_LAUNCHERS(VertPF, FLPF)
+#undef FDGA_VERTEX_LAUNCHERS
 cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n) {
     k_finalize3<<<blocks_for(n, 256), 256, 0, s>>>(f, k2_epilogue, t_recombine, n);
     LAUNCH_CHECK(); return cudaSuccess;

@@ -22,9 +22,12 @@ struct Caches {  // Γpx F0p F0a F0t Γpp Γa Γt Fp Fa Ft
     cplx* c[10];
     cplxf* f[10];  // FP32 copies written instead of c in the mixed map (nullptr: FP64 map)
 };
-struct FLP {  // left vertex FL: only K2 enters the K1/K2 BSE through FL(Ω, ω, νInf)
-    const cplx* K2[3];
+template <class S>
+struct FLPT {  // left vertex FL: only K2 enters the K1/K2 BSE through FL(Ω, ω, νInf)
+    const S* K2[3];
 };
+using FLP = FLPT<cplx>;
+using FLPF = FLPT<cplxf>;
 struct K3Args {
     const cplx* A;    // cacheΓ (L_K3) or cacheF (K3)
     const cplx* B0;   // cacheF0
@@ -99,6 +102,7 @@ struct AAVecs32W {
 };
 
 cudaError_t set_fft_twiddles();
+// vertex-evaluating kernels: VertP/FLP (FP64 plain map) or VertPF/FLPF (FP32 mirror, mixed map)
 cudaError_t launch_bse_K1_all(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
                               const ChanWork& cw, const Dims& d);
 cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VertP& F, const BubbleP& B, const ChanWork& cw, const Dims& d);
@@ -106,6 +110,15 @@ cudaError_t launch_bse_K2_all(cudaStream_t s, const VertP& F, const FLP& FL, con
                               const ChanWork& cw, const Dims& d);
 cudaError_t launch_sde_L_all(cudaStream_t s, const VertP& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph,
                              const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d);
+cudaError_t launch_bse_K1_all(cudaStream_t s, const VertPF& F, const FLPF& FL, const BubbleP& B, const cplx* SX,
+                              const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VertPF& F, const BubbleP& B, const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_K2_all(cudaStream_t s, const VertPF& F, const FLPF& FL, const BubbleP& B, const cplx* SX,
+                              const ChanWork& cw, const Dims& d);
+cudaError_t launch_sde_L_all(cudaStream_t s, const VertPF& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph,
+                             const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d);
+cudaError_t launch_build_cache(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
+                               const Dims& d);
 cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n);
 cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
                           cplx* S0, cplx* S1, const Dims& d);

@@ -63,6 +63,9 @@ struct fdga_handle {
     cplx *xS = nullptr, *yS = nullptr, *tmpS = nullptr;
     cplx *avg = nullptr, *cache = nullptr, *FLK2 = nullptr, *FLK3 = nullptr;
     cplxf *cachef = nullptr, *FLK3f = nullptr;  // FP32 caches and FL.K3 of the mixed map
+    cplxf *xSf = nullptr, *ySf = nullptr, *avgf = nullptr, *FLK2f = nullptr;  // FP32 mirrors (mixed map)
+    cplxf* Freff[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
@@ -140,6 +143,11 @@ int ensure_mixed(fdga_handle* h) {
     if (h->cachef) return FDGA_OK;
     AL(h->cachef, 10 * h->n3);
     AL(h->FLK3f, 3 * h->n3);
+    AL(h->FLK2f, 3 * h->n2);
+    AL(h->xSf, 3 * h->nchan);
+    AL(h->ySf, 3 * h->nchan);
+    if (h->navg) AL(h->avgf, h->navg);
+    for (auto& f : h->Freff) AL(f, h->nRef);
     AL(h->d_err, 1);
     if (k3_tc_supported(h->d)) CK(prepare_bse_K3_tc(h->d));
     CK(cudaStreamSynchronize(h->st));
@@ -364,23 +372,28 @@ int upload_group(fdga_handle* h, Group& g, const HostGroup& hg) {
 // ---------------------------------------------------------------------------------------------
 // Launch sequence of one iteration: src/solve.jl:4-116
 // ---------------------------------------------------------------------------------------------
-VertP vertex_view(fdga_handle* h, cplx* S) {
-    VertP F;
+// vertex view of a state-layout array (the FP64 state or its FP32 mirror) with its momentum
+// averages and RefVertex corrections
+template <class S>
+VertPT<S> vertex_view_t(const fdga_handle* h, S* st, S* avg, S* const* fref) {
+    VertPT<S> F;
     for (int c = 0; c < 3; ++c) {
-        F.g[c].K1 = chanK(h, S, c, 1);
-        F.g[c].K2 = chanK(h, S, c, 2);
-        F.g[c].K3 = chanK(h, S, c, 3);
+        S* base = st + (size_t)c * h->nchan;
+        F.g[c].K1 = base;
+        F.g[c].K2 = base + h->n1;
+        F.g[c].K3 = base + h->n1 + h->n2;
         if (h->d.Nq == 1) {
             F.g[c].A1 = F.g[c].K1; F.g[c].A2 = F.g[c].K2; F.g[c].A3 = F.g[c].K3;
         } else {
             const size_t per1 = h->d.N1, per2 = (size_t)h->d.N2O * h->d.N2n, per3 = (size_t)h->d.N3O * h->d.N3n * h->d.N3n;
-            cplx* a = h->avg + (size_t)c * (per1 + per2 + per3);
+            S* a = avg + (size_t)c * (per1 + per2 + per3);
             F.g[c].A1 = a; F.g[c].A2 = a + per1; F.g[c].A3 = a + per1 + per2;
         }
     }
-    F.Fp_p = h->Fref[0]; F.Fp_x = h->Fref[1]; F.Ft_p = h->Fref[2]; F.Ft_x = h->Fref[3];
+    F.Fp_p = fref[0]; F.Fp_x = fref[1]; F.Ft_p = fref[2]; F.Ft_x = fref[3];
     return F;
 }
+VertP vertex_view(fdga_handle* h, cplx* S) { return vertex_view_t<cplx>(h, S, h->avg, h->Fref); }
 
 const Group& k2group(fdga_handle* h, int ch) { return ch == CH_P ? h->gK2pp : h->gK2ph; }
 
@@ -393,7 +406,8 @@ const Group& k2group(fdga_handle* h, int ch) { return ch == CH_P ? h->gK2pp : h-
 
 // L_pp and L_ph (vertex part and/or RefVertex part / 3) at the K2-group representatives, then the
 // SymmetryGroup broadcast into h->Lpp, h->Lph.
-cudaError_t sde_L_pair(fdga_handle* h, const VertP& F, const BubbleP& B, const cplx* SPi, int use_vertex, double rs,
+template <class V>
+cudaError_t sde_L_pair(fdga_handle* h, const V& F, const BubbleP& B, const cplx* SPi, int use_vertex, double rs,
                        int& nl) {
     const Dims& d = h->d;
     const size_t nS = (size_t)d.Nq * d.NPO;
@@ -443,15 +457,27 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
         stage("dyson_bubble");
     }
-    // the mixed map keeps the caches and FL.K3 in FP32: written once here, read by both K3 GEMMs
+    // The mixed map evaluates vertices from an FP32 mirror of the state (converted once per
+    // iteration) and keeps the caches, FL.K2 and FL.K3 in FP32: written once, read by the BSEs.
     const bool mixed = h->precision == FDGA_MIXED;
-    if (mixed && (!h->cachef || !h->FLK3f)) return fail(h, FDGA_ERR_STATE, "mixed-precision buffers missing");
+    if (mixed && (!h->cachef || !h->FLK3f || !h->xSf)) return fail(h, FDGA_ERR_STATE, "mixed-precision buffers missing");
+    VertPF Ff{}, Fnf{};
+    FLPF FLf{};
+    if (mixed) {
+        LC(launch_to_f32(s, h->xS, h->xSf, 3 * h->nchan));
+        if (d.Nq > 1) LC(launch_to_f32(s, h->avg, h->avgf, h->navg));
+        for (int i = 0; i < 4; ++i) LC(launch_to_f32(s, h->Fref[i], h->Freff[i], h->nRef));
+        Ff = vertex_view_t<cplxf>(h, h->xSf, h->avgf, h->Freff);
+        Fnf = vertex_view_t<cplxf>(h, h->ySf, h->avgf, h->Freff);
+        for (int c = 0; c < 3; ++c) FLf.K2[c] = h->FLK2f + (size_t)c * h->n2;
+    }
     Caches C{};
     for (int i = 0; i < 10; ++i) {
         C.c[i] = h->cache + (size_t)i * h->n3;
         C.f[i] = mixed ? h->cachef + (size_t)i * h->n3 : nullptr;
     }
-    LC(launch_build_cache(s, F, C, h->d_k3blocks, h->nk3blocks, d));
+    if (mixed) LC(launch_build_cache(s, Ff, C, h->d_k3blocks, h->nk3blocks, d));
+    else LC(launch_build_cache(s, F, C, h->d_k3blocks, h->nk3blocks, d));
     if (mixed && strategy != FDGA_FDPA) LC(launch_to_f32(s, h->FLK3, h->FLK3f, 3 * h->n3));
     stage("k3_cache");
     FLP FL;
@@ -486,10 +512,14 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     if (strategy == FDGA_FDPA) {
         {  // left K2 (FL.K2)
             ChanWork cw = work(2, h->raw2);
-            LC(launch_bse_L_K2_all(s, F, B, cw, d));
+            if (mixed) LC(launch_bse_L_K2_all(s, Ff, B, cw, d));
+            else LC(launch_bse_L_K2_all(s, F, B, cw, d));
             cplx* out[3] = {h->FLK2, h->FLK2 + h->n2, h->FLK2 + 2 * h->n2};
             const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
-            LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 0, 1, h->n2));
+            Finalize3 f2 = fin(2, h->raw2, out, grp);
+            if (mixed)
+                for (int c = 0; c < 3; ++c) f2.outf[c] = h->FLK2f + (size_t)c * h->n2;
+            LC(launch_finalize3(s, f2, 0, 1, h->n2));
         }
         stage("bse_L_K2");
         {  // left K3 (FL.K3)
@@ -526,7 +556,8 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FL, h->SX, d));
     {  // K1
         ChanWork cw = work(1, h->raw1);
-        LC(launch_bse_K1_all(s, F, FL, B, h->SX, cw, d));
+        if (mixed) LC(launch_bse_K1_all(s, Ff, FLf, B, h->SX, cw, d));
+        else LC(launch_bse_K1_all(s, F, FL, B, h->SX, cw, d));
         cplx* out[3] = {chanK(h, h->yS, CH_P, 1), chanK(h, h->yS, CH_T, 1), chanK(h, h->yS, CH_A, 1)};
         const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
         LC(launch_finalize3(s, fin(1, h->raw1, out, grp), 0, 1, h->n1));
@@ -534,7 +565,8 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     stage("bse_K1");
     {  // K2
         ChanWork cw = work(2, h->raw2);
-        LC(launch_bse_K2_all(s, F, FL, B, h->SX, cw, d));
+        if (mixed) LC(launch_bse_K2_all(s, Ff, FLf, B, h->SX, cw, d));
+        else LC(launch_bse_K2_all(s, F, FL, B, h->SX, cw, d));
         cplx* out[3] = {chanK(h, h->yS, CH_P, 2), chanK(h, h->yS, CH_T, 2), chanK(h, h->yS, CH_A, 2)};
         const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
         LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 1, 1, h->n2));
@@ -576,7 +608,12 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     cplx* SigOut = sigmaOf(h, h->yS);
     if (update_sigma) {
         const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
-        LC(sde_L_pair(h, Fn, B, h->SPi, 1, rs, nl));
+        if (mixed) {
+            LC(launch_to_f32(s, h->yS, h->ySf, 3 * h->nchan));
+            LC(sde_L_pair(h, Fnf, B, h->SPi, 1, rs, nl));
+        } else {
+            LC(sde_L_pair(h, Fn, B, h->SPi, 1, rs, nl));
+        }
         LC(launch_sde_sigma(s, h->GR, h->Lpp, h->Lph, h->LR, h->SigR, h->SigIn, h->twm, h->twp, d));
         nl += 3;
         LC(launch_u2(s, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
@@ -763,7 +800,10 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     ALC(h->Pi0pp, h->nPi); ALC(h->Pi0ph, h->nPi); ALC(h->Pipp, h->nPi); ALC(h->Piph, h->nPi);
     for (auto& f : h->Fref) ALC(f, h->nRef);
     ALC(h->xS, h->nstate); ALC(h->yS, h->nstate); ALC(h->tmpS, h->nstate);
-    if (d.Nq > 1) ALC(h->avg, 3 * ((size_t)d.N1 + (size_t)d.N2O * d.N2n + (size_t)d.N3O * d.N3n * d.N3n));
+    if (d.Nq > 1) {
+        h->navg = 3 * ((size_t)d.N1 + (size_t)d.N2O * d.N2n + (size_t)d.N3O * d.N3n * d.N3n);
+        ALC(h->avg, h->navg);
+    }
     ALC(h->cache, 10 * h->n3);
     ALC(h->FLK2, 3 * h->n2); ALC(h->FLK3, 3 * h->n3);
     ALC(h->Lpp, h->n2); ALC(h->Lph, h->n2); ALC(h->SigIn, h->nGk); ALC(h->SigU2, h->nGk); ALC(h->C0, h->nGk);
