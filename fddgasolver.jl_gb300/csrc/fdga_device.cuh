@@ -70,6 +70,7 @@ __device__ __forceinline__ cplxf cfma(cplxf a, cplxf b, cplxf c) {
 template <class C> __device__ __forceinline__ C to_c(cplx v);
 template <> __device__ __forceinline__ cplx to_c<cplx>(cplx v) { return v; }
 template <> __device__ __forceinline__ cplxf to_c<cplxf>(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+template <class C> __device__ __forceinline__ C to_c(cplxf v) { return C{v.x, v.y}; }
 __device__ __forceinline__ cplx to_d(cplx v) { return v; }
 __device__ __forceinline__ cplx to_d(cplxf v) { return cplx{(double)v.x, (double)v.y}; }
 __device__ __forceinline__ cplxf to_f32(cplx v) { return cplxf{(float)v.x, (float)v.y}; }

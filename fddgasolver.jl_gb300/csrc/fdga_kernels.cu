@@ -62,6 +62,13 @@ __device__ __forceinline__ cplx g_tail(const cplx* G, const Dims& d, int k, int 
     if (fin(n, d.nG)) return G[ixG(d, k, n)];
     return mk(1.0 / ((2.0 * n + 1.0) * M_PI * d.T), 0.0);
 }
+// the same in arithmetic type C from storage G (cplx or the mixed map's FP32 copy)
+template <class C, class G>
+__device__ __forceinline__ C g_tail_t(const G* Gp, const Dims& d, int k, int n) {
+    using R = decltype(C::x);
+    if (fin(n, d.nG)) return to_c<C>(Gp[ixG(d, k, n)]);
+    return C{(R)1 / (((R)2 * n + (R)1) * (R)M_PI * (R)d.T), (R)0};
+}
 
 __global__ void k_bubble_local(const cplx* G, cplx* pp, cplx* ph, Dims d) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -140,13 +147,18 @@ __host__ __device__ constexpr int bitrev(int i) {
     return r;
 }
 
+__constant__ cplxf c_twp32f[32];
+template <class C> __device__ __forceinline__ C twp32(int j);
+template <> __device__ __forceinline__ cplx twp32<cplx>(int j) { return c_twp32[j]; }
+template <> __device__ __forceinline__ cplxf twp32<cplxf>(int j) { return c_twp32f[j]; }
+
 // in-place backward DFT (e^{+2πi jk/L}) of v[0..L) held in registers
-template <int L>
-__device__ __forceinline__ void fft_bwd(cplx (&v)[L]) {
+template <int L, class C>
+__device__ __forceinline__ void fft_bwd(C (&v)[L]) {
 #pragma unroll
     for (int i = 0; i < L; ++i) {
         const int j = bitrev<L>(i);
-        if (j > i) { const cplx t = v[i]; v[i] = v[j]; v[j] = t; }
+        if (j > i) { const C t = v[i]; v[i] = v[j]; v[j] = t; }
     }
 #pragma unroll
     for (int len = 2; len <= L; len <<= 1) {
@@ -155,12 +167,12 @@ __device__ __forceinline__ void fft_bwd(cplx (&v)[L]) {
         for (int i = 0; i < L; i += len) {
 #pragma unroll
             for (int k = 0; k < half; ++k) {
-                const cplx b = v[i + k + half];
-                cplx t;
+                const C b = v[i + k + half];
+                C t;
                 if (k == 0) t = b;
-                else if (4 * k == len) t = mk(-b.y, b.x);  // multiply by i
-                else t = b * c_twp32[k * (32 / len)];
-                const cplx u = v[i + k];
+                else if (4 * k == len) t = C{-b.y, b.x};  // multiply by i
+                else t = b * twp32<C>(k * (32 / len));
+                const C u = v[i + k];
                 v[i + k] = u + t;
                 v[i + k + half] = u - t;
             }
@@ -168,9 +180,10 @@ __device__ __forceinline__ void fft_bwd(cplx (&v)[L]) {
     }
 }
 
-template <int L>
-__global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV) {
-    extern __shared__ cplx sh[];
+template <int L, class C, class G>
+__global__ void k_bubble_fft(const G* GR, cplx* pp, cplx* ph, Dims d, int TV) {
+    extern __shared__ __align__(16) unsigned char sh_raw[];
+    C* sh = reinterpret_cast<C*>(sh_raw);
     constexpr int NR = L * L, RS = L + 1, BS = L * (L + 1) + 1;
     const int m = blockIdx.y - (d.nPO - 1);
     const int n0 = blockIdx.x * TV - d.nPw;
@@ -178,16 +191,16 @@ __global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV)
         const int v = e / NR, R = e % NR;
         const int n = n0 + v;
         const int Rx = R % L, Ry = R / L;
-        cplx vpp = mk(0, 0), vph = mk(0, 0);
+        C vpp{0, 0}, vph{0, 0};
         if (n < d.nPw) {
             const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
             if (R == 0) {
-                vpp = g_tail(GR, d, 0, m - n - 1) * g_tail(GR, d, 0, n);
-                vph = g_tail(GR, d, 0, m + n) * g_tail(GR, d, 0, n);
+                vpp = g_tail_t<C>(GR, d, 0, m - n - 1) * g_tail_t<C>(GR, d, 0, n);
+                vph = g_tail_t<C>(GR, d, 0, m + n) * g_tail_t<C>(GR, d, 0, n);
             } else {
                 const int a = m - n - 1, b = m + n;
-                if (fin(a, d.nG) && fin(n, d.nG)) vpp = GR[ixG(d, R, a)] * GR[ixG(d, R, n)];
-                if (fin(b, d.nG) && fin(n, d.nG)) vph = GR[ixG(d, R, b)] * GR[ixG(d, mR, n)];
+                if (fin(a, d.nG) && fin(n, d.nG)) vpp = to_c<C>(GR[ixG(d, R, a)]) * to_c<C>(GR[ixG(d, R, n)]);
+                if (fin(b, d.nG) && fin(n, d.nG)) vph = to_c<C>(GR[ixG(d, R, b)]) * to_c<C>(GR[ixG(d, mR, n)]);
             }
         }
         sh[(size_t)v * BS + Ry * RS + Rx] = vpp;
@@ -195,8 +208,8 @@ __global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV)
     }
     __syncthreads();
     for (int r = threadIdx.x; r < 2 * TV * L; r += blockDim.x) {  // along x
-        cplx* row = sh + (size_t)(r / L) * BS + (r % L) * RS;
-        cplx v[L];
+        C* row = sh + (size_t)(r / L) * BS + (r % L) * RS;
+        C v[L];
 #pragma unroll
         for (int x = 0; x < L; ++x) v[x] = row[x];
         fft_bwd<L>(v);
@@ -205,8 +218,8 @@ __global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV)
     }
     __syncthreads();
     for (int c = threadIdx.x; c < 2 * TV * L; c += blockDim.x) {  // along y
-        cplx* col = sh + (size_t)(c / L) * BS + (c % L);
-        cplx v[L];
+        C* col = sh + (size_t)(c / L) * BS + (c % L);
+        C v[L];
 #pragma unroll
         for (int y = 0; y < L; ++y) v[y] = col[y * RS];
         fft_bwd<L>(v);
@@ -220,8 +233,8 @@ __global__ void k_bubble_fft(const cplx* GR, cplx* pp, cplx* ph, Dims d, int TV)
         const int P = rest % NR, which = rest / NR;
         const int n = n0 + v;
         if (n >= d.nPw) continue;
-        const cplx val = sh[(size_t)(which * TV + v) * BS + (P / L) * RS + (P % L)];
-        (which ? ph : pp)[ixPi(d, P, m, n)] = val;
+        const C val = sh[(size_t)(which * TV + v) * BS + (P / L) * RS + (P % L)];
+        (which ? ph : pp)[ixPi(d, P, m, n)] = to_d(val);
     }
 }
 
@@ -416,7 +429,8 @@ __global__ void k_rowsum(const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, int
 // Full-mesh bubble row sums in real space, for a stored window narrower than the mesh:
 //   SR[w][Ω][R] = Σ_{ν ∈ bubble mesh} Π_R^w(Ω, ν, R),   S^w(P, Ω) = Σ_R e^{+2πi P·R/L} SR[w][Ω][R],
 // with Π_R as in k_bubble_nl (R = 0 carries the 1/ν tail; R ≠ 0 needs both G in their box).
-__global__ void k_pisum_R(const cplx* GR, cplx* SR, Dims d) {
+template <class C, class G>
+__global__ void k_pisum_R(const G* GR, cplx* SR, Dims d) {
     const int NR = d.L * d.L;
     const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -426,24 +440,25 @@ __global__ void k_pisum_R(const cplx* GR, cplx* SR, Dims d) {
     const int R = rest / d.NPO, m = rest % d.NPO - (d.nPO - 1);  // SR[w][R][Ω]
     const int L = d.L, Rx = R % L, Ry = R / L;
     const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
-    cplx acc = mk(0, 0);
+    C acc{0, 0};
     if (R == 0) {
         for (int n = -d.nPn + lane; n < d.nPn; n += 32)
-            acc = cfma(which ? g_tail(GR, d, 0, m + n) : g_tail(GR, d, 0, m - n - 1), g_tail(GR, d, 0, n), acc);
+            acc = cfma(which ? g_tail_t<C>(GR, d, 0, m + n) : g_tail_t<C>(GR, d, 0, m - n - 1), g_tail_t<C>(GR, d, 0, n),
+                       acc);
     } else {
         for (int n = -d.nG + lane; n < d.nG; n += 32) {
             if (!fin(n, d.nPn)) continue;
             if (which) {
                 const int b = m + n;
-                if (fin(b, d.nG)) acc = cfma(GR[ixG(d, R, b)], GR[ixG(d, mR, n)], acc);
+                if (fin(b, d.nG)) acc = cfma(to_c<C>(GR[ixG(d, R, b)]), to_c<C>(GR[ixG(d, mR, n)]), acc);
             } else {
                 const int a = m - n - 1;
-                if (fin(a, d.nG)) acc = cfma(GR[ixG(d, R, a)], GR[ixG(d, R, n)], acc);
+                if (fin(a, d.nG)) acc = cfma(to_c<C>(GR[ixG(d, R, a)]), to_c<C>(GR[ixG(d, R, n)]), acc);
             }
         }
     }
     acc = warp_sum(acc);
-    if (lane == 0) SR[w] = acc;
+    if (lane == 0) SR[w] = to_d(acc);
 }
 // S_X(ch, P, Ω) = Σ_ω [(Π-Π0)(Ω,ω,P) U + Π(Ω,ω,P) FL(Ω,ω̃,∞)]: the ω-sum of the BSE's right factor
 // (src/BSEa/BSEa_K1.jl:43, BSEa_K2.jl:185), from the row sums and the K2 window of FL.
@@ -997,18 +1012,48 @@ static cudaError_t launch_bubble_fft(cudaStream_t s, const cplx* GR, cplx* pp, c
     const size_t shm = (size_t)2 * tv * BS * sizeof(cplx);
     static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
     if (shm > 48 * 1024 && shm > shm_set) {
-        cudaFuncSetAttribute(k_bubble_fft<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bubble_fft<L, cplx, cplx>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         shm_set = shm;
     }
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
-    k_bubble_fft<L><<<grid, 256, shm, s>>>(GR, pp, ph, d, tv);
+    k_bubble_fft<L, cplx, cplx><<<grid, 256, shm, s>>>(GR, pp, ph, d, tv);
     return cudaGetLastError();
+}
+// FP32 form (mixed map) from the FP32 copy of G(R); its tile fits the default 48 KB of shared memory
+template <int L>
+static cudaError_t launch_bubble_fft_f32(cudaStream_t s, const cplxf* GR, cplx* pp, cplx* ph, const Dims& d) {
+    constexpr int BS = L * (L + 1) + 1;
+    int tv = 32;
+    while (tv > 1 && (size_t)2 * tv * BS * sizeof(cplxf) > 48 * 1024) tv >>= 1;
+    const size_t shm = (size_t)2 * tv * BS * sizeof(cplxf);
+    dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
+    k_bubble_fft<L, cplxf, cplxf><<<grid, 256, shm, s>>>(GR, pp, ph, d, tv);
+    return cudaGetLastError();
+}
+bool bubble_f32_supported(const Dims& d) {
+    return !d.local && (d.L == 2 || d.L == 4 || d.L == 8 || d.L == 16 || d.L == 32);
+}
+cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const Dims& d) {
+    switch (d.L) {
+        case 2: return launch_bubble_fft_f32<2>(s, GRf, pp, ph, d);
+        case 4: return launch_bubble_fft_f32<4>(s, GRf, pp, ph, d);
+        case 8: return launch_bubble_fft_f32<8>(s, GRf, pp, ph, d);
+        case 16: return launch_bubble_fft_f32<16>(s, GRf, pp, ph, d);
+        case 32: return launch_bubble_fft_f32<32>(s, GRf, pp, ph, d);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t set_fft_twiddles() {
     cplx tw[32];
-    for (int j = 0; j < 32; ++j) tw[j] = mk(std::cos(2.0 * M_PI * j / 32.0), std::sin(2.0 * M_PI * j / 32.0));
-    return cudaMemcpyToSymbol(c_twp32, tw, sizeof(tw));
+    cplxf twf[32];
+    for (int j = 0; j < 32; ++j) {
+        tw[j] = mk(std::cos(2.0 * M_PI * j / 32.0), std::sin(2.0 * M_PI * j / 32.0));
+        twf[j] = cplxf{(float)tw[j].x, (float)tw[j].y};
+    }
+    cudaError_t e = cudaMemcpyToSymbol(c_twp32, tw, sizeof(tw));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_twp32f, twf, sizeof(twf));
+    return e;
 }
 
 cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
@@ -1071,14 +1116,15 @@ cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int
 }
 
 cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
-                          cplx* S0, cplx* S1, const Dims& d) {
+                          cplx* S0, cplx* S1, const Dims& d, const cplxf* GRf) {
     if (d.nPw == d.nPn) {  // the full mesh is stored: sum the rows
         dim3 grid((unsigned)(d.Nq * d.NPO), 2);
         k_rowsum<<<grid, 256, 0, s>>>(A0, A1, S0, S1, d.NPw);
         LAUNCH_CHECK(); return cudaSuccess;
     }
     const int NR = d.L * d.L;
-    k_pisum_R<<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GR, SRtmp, d);
+    if (GRf) k_pisum_R<cplxf, cplxf><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GRf, SRtmp, d);
+    else k_pisum_R<cplx, cplx><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GR, SRtmp, d);
     LAUNCH_CHECK();
     // S^w[P][Ω] = Σ_R e^{+2πi P·R/L} SR[w][R][Ω]
     cudaError_t e = launch_fft2(s, SRtmp, S0, d.NPO, +1, 1.0, twp, d);

@@ -120,8 +120,11 @@ cudaError_t launch_sde_L_all(cudaStream_t s, const VertPF& F, const BubbleP& B, 
 cudaError_t launch_build_cache(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
 cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n);
+// GRf (optional): FP32 copy of G(R) -> the real-space row sums run in FP32 (mixed map)
 cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
-                          cplx* S0, cplx* S1, const Dims& d);
+                          cplx* S0, cplx* S1, const Dims& d, const cplxf* GRf = nullptr);
+bool bubble_f32_supported(const Dims& d);
+cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const Dims& d);
 cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
                       const FLP& FL, cplx* SX, const Dims& d);
 cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n);

@@ -65,6 +65,7 @@ struct fdga_handle {
     cplxf *cachef = nullptr, *FLK3f = nullptr;  // FP32 caches and FL.K3 of the mixed map
     cplxf *xSf = nullptr, *ySf = nullptr, *avgf = nullptr, *FLK2f = nullptr;  // FP32 mirrors (mixed map)
     cplxf* Freff[4] = {nullptr, nullptr, nullptr, nullptr};
+    cplxf* GRf = nullptr;  // FP32 copy of G(R) (mixed map)
     size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
@@ -144,6 +145,7 @@ int ensure_mixed(fdga_handle* h) {
     AL(h->cachef, 10 * h->n3);
     AL(h->FLK3f, 3 * h->n3);
     AL(h->FLK2f, 3 * h->n2);
+    AL(h->GRf, h->nGk);
     AL(h->xSf, 3 * h->nchan);
     AL(h->ySf, 3 * h->nchan);
     if (h->navg) AL(h->avgf, h->navg);
@@ -453,8 +455,16 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     if (update_sigma) {
         LC(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
         LC(launch_g_realspace(s, h->G, h->GR, h->twm, d));
-        LC(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
-        LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
+        if (h->precision == FDGA_MIXED && bubble_f32_supported(d)) {
+            // mixed map: bubble and its full-mesh row sums in FP32 from an FP32 copy of G(R)
+            LC(launch_to_f32(s, h->GR, h->GRf, h->nGk));
+            LC(launch_bubble_f32(s, h->GRf, h->Pipp, h->Piph, d));
+            LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
+                             h->GRf));
+        } else {
+            LC(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
+            LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
+        }
         stage("dyson_bubble");
     }
     // The mixed map evaluates vertices from an FP32 mirror of the state (converted once per
