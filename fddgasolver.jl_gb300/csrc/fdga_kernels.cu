@@ -348,7 +348,13 @@ __global__ void k_qavg(const ChanArrays in, ChanArraysW out, Dims d) {
     const cplx* src = cl == 0 ? in.K1[ch] : (cl == 1 ? in.K2[ch] : in.K3[ch]);
     cplx* dst = cl == 0 ? out.K1[ch] : (cl == 1 ? out.K2[ch] : out.K3[ch]);
     cplx s = mk(0, 0);
-    for (int P = 0; P < d.Nq; ++P) s += src[(size_t)P * per + i];
+    int P = 0;
+    for (; P + 4 <= d.Nq; P += 4) {  // four independent loads in flight, summed in order
+        const cplx a0 = src[(size_t)P * per + i], a1 = src[(size_t)(P + 1) * per + i];
+        const cplx a2 = src[(size_t)(P + 2) * per + i], a3 = src[(size_t)(P + 3) * per + i];
+        s += a0; s += a1; s += a2; s += a3;
+    }
+    for (; P < d.Nq; ++P) s += src[(size_t)P * per + i];
     dst[i] = s * (1.0 / d.Nq);
 }
 
@@ -429,8 +435,24 @@ __global__ void k_rowsum(const cplx* A0, const cplx* A1, cplx* S0, cplx* S1, int
 // Full-mesh bubble row sums in real space, for a stored window narrower than the mesh:
 //   SR[w][Ω][R] = Σ_{ν ∈ bubble mesh} Π_R^w(Ω, ν, R),   S^w(P, Ω) = Σ_R e^{+2πi P·R/L} SR[w][Ω][R],
 // with Π_R as in k_bubble_nl (R = 0 carries the 1/ν tail; R ≠ 0 needs both G in their box).
+// T0[w][Ω] = Σ over the bubble mesh of the tail·tail products (both G outside their box); depends
+// only on T and the meshes.  One warp per (w, Ω).
+__global__ void k_tail_const(cplx* T0, Dims d) {
+    const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (size_t)2 * d.NPO) return;
+    const int which = (int)(w / d.NPO), m = (int)(w % d.NPO) - (d.nPO - 1);
+    cplx acc = mk(0, 0);
+    for (int n = -d.nPn + lane; n < d.nPn; n += 32) {
+        const int a = which ? m + n : m - n - 1;
+        if (fin(n, d.nG) || fin(a, d.nG)) continue;
+        acc = cfma(g_tail(nullptr, d, 0, a), g_tail(nullptr, d, 0, n), acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) T0[w] = acc;
+}
 template <class C, class G>
-__global__ void k_pisum_R(const G* GR, cplx* SR, Dims d) {
+__global__ void k_pisum_R(const G* GR, const cplx* T0, cplx* SR, Dims d) {
     const int NR = d.L * d.L;
     const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -442,9 +464,19 @@ __global__ void k_pisum_R(const G* GR, cplx* SR, Dims d) {
     const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
     C acc{0, 0};
     if (R == 0) {
-        for (int n = -d.nPn + lane; n < d.nPn; n += 32)
+        // terms with at least one factor inside the G box; the tail·tail remainder is the
+        // iteration-independent T0 (k_tail_const), added below
+        for (int n = -d.nG + lane; n < d.nG; n += 32) {  // n inside the box
+            if (!fin(n, d.nPn)) continue;
             acc = cfma(which ? g_tail_t<C>(GR, d, 0, m + n) : g_tail_t<C>(GR, d, 0, m - n - 1), g_tail_t<C>(GR, d, 0, n),
                        acc);
+        }
+        for (int a = -d.nG + lane; a < d.nG; a += 32) {  // partner inside the box, n outside
+            const int n = which ? a - m : m - 1 - a;
+            if (fin(n, d.nG) || !fin(n, d.nPn)) continue;
+            acc = cfma(g_tail_t<C>(GR, d, 0, a), g_tail_t<C>(GR, d, 0, n), acc);
+        }
+        if (lane == 0 && T0) acc += to_c<C>(T0[(size_t)which * d.NPO + (m + d.nPO - 1)]);
     } else {
         for (int n = -d.nG + lane; n < d.nG; n += 32) {
             if (!fin(n, d.nPn)) continue;
@@ -1085,11 +1117,13 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
 
 template <int L>
 static cudaError_t launch_fft2_tpl(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale) {
-    constexpr int BS = L * (L + 1) + 1;
-    int tr = 32;
-    while (tr > 1 && (size_t)tr * BS * sizeof(cplx) > 48 * 1024) tr >>= 1;
+    constexpr int BS = L * (L + 1) + 1, NR = L * L;
+    // rows per CTA: enough CTAs to cover the GPU (two per SM for 152 SMs), within 48 KB of tile
+    int tr = 1;
+    while (tr < 32 && (size_t)(2 * tr) * BS * sizeof(cplx) <= 48 * 1024 && (rows + 2 * tr - 1) / (2 * tr) >= 304) tr *= 2;
     const size_t shm = (size_t)tr * BS * sizeof(cplx);
-    k_fft2_rows<L><<<(unsigned)((rows + tr - 1) / tr), 256, shm, s>>>(in, out, rows, sign, scale, tr);
+    const int threads = std::min(256, std::max(32, ((tr * NR + 31) / 32) * 32));
+    k_fft2_rows<L><<<(unsigned)((rows + tr - 1) / tr), threads, shm, s>>>(in, out, rows, sign, scale, tr);
     return cudaGetLastError();
 }
 cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int sign, double scale,
@@ -1115,16 +1149,20 @@ cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int
     LAUNCH_CHECK(); return cudaSuccess;
 }
 
+cudaError_t launch_tail_const(cudaStream_t s, cplx* T0, const Dims& d) {
+    k_tail_const<<<blocks_for((size_t)2 * d.NPO * 32, 128), 128, 0, s>>>(T0, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
 cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
-                          cplx* S0, cplx* S1, const Dims& d, const cplxf* GRf) {
+                          cplx* S0, cplx* S1, const Dims& d, const cplx* T0, const cplxf* GRf) {
     if (d.nPw == d.nPn) {  // the full mesh is stored: sum the rows
         dim3 grid((unsigned)(d.Nq * d.NPO), 2);
         k_rowsum<<<grid, 256, 0, s>>>(A0, A1, S0, S1, d.NPw);
         LAUNCH_CHECK(); return cudaSuccess;
     }
     const int NR = d.L * d.L;
-    if (GRf) k_pisum_R<cplxf, cplxf><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GRf, SRtmp, d);
-    else k_pisum_R<cplx, cplx><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GR, SRtmp, d);
+    if (GRf) k_pisum_R<cplxf, cplxf><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GRf, T0, SRtmp, d);
+    else k_pisum_R<cplx, cplx><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GR, T0, SRtmp, d);
     LAUNCH_CHECK();
     // S^w[P][Ω] = Σ_R e^{+2πi P·R/L} SR[w][R][Ω]
     cudaError_t e = launch_fft2(s, SRtmp, S0, d.NPO, +1, 1.0, twp, d);

@@ -120,9 +120,11 @@ cudaError_t launch_sde_L_all(cudaStream_t s, const VertPF& F, const BubbleP& B, 
 cudaError_t launch_build_cache(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
 cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n);
+// T0: the tail·tail part of the R = 0 row sums (launch_tail_const, once per solver);
 // GRf (optional): FP32 copy of G(R) -> the real-space row sums run in FP32 (mixed map)
 cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const cplx* GR, cplx* SRtmp, const cplx* twp,
-                          cplx* S0, cplx* S1, const Dims& d, const cplxf* GRf = nullptr);
+                          cplx* S0, cplx* S1, const Dims& d, const cplx* T0, const cplxf* GRf = nullptr);
+cudaError_t launch_tail_const(cudaStream_t s, cplx* T0, const Dims& d);
 bool bubble_f32_supported(const Dims& d);
 cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const Dims& d);
 cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,

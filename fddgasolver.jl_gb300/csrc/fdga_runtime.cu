@@ -66,6 +66,7 @@ struct fdga_handle {
     cplxf *xSf = nullptr, *ySf = nullptr, *avgf = nullptr, *FLK2f = nullptr;  // FP32 mirrors (mixed map)
     cplxf* Freff[4] = {nullptr, nullptr, nullptr, nullptr};
     cplxf* GRf = nullptr;  // FP32 copy of G(R) (mixed map)
+    cplx* T0tail = nullptr;  // tail·tail part of the R = 0 bubble row sums [2][NΠΩ]
     size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
@@ -460,10 +461,11 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             LC(launch_to_f32(s, h->GR, h->GRf, h->nGk));
             LC(launch_bubble_f32(s, h->GRf, h->Pipp, h->Piph, d));
             LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
-                             h->GRf));
+                             h->T0tail, h->GRf));
         } else {
             LC(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
-            LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d));
+            LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
+                             h->T0tail));
         }
         stage("dyson_bubble");
     }
@@ -821,6 +823,7 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     ALC(h->twm, d.L); ALC(h->twp, d.L);
     ALC(h->SPi, 2 * (size_t)d.Nq * d.NPO); ALC(h->SPi0, 2 * (size_t)d.Nq * d.NPO); ALC(h->SX, 3 * (size_t)d.Nq * d.NPO);
     ALC(h->SRtmp, 2 * (size_t)d.NPO * d.Nq);
+    ALC(h->T0tail, 2 * (size_t)d.NPO);
     ALC(h->LR, 2 * h->n2); ALC(h->SigR, h->nGk);
     ALC(h->raw1, 3 * h->n1); ALC(h->raw2, 3 * h->n2); ALC(h->raw3, 3 * h->n3);
     h->nk3blocks = d.Nq * d.N3O;
@@ -908,7 +911,8 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_g_realspace(s, h->G0, h->GR, h->twm, d));
     CK(launch_bubble(s, h->G0, h->GR, h->Pi0pp, h->Pi0ph, h->twp, d));
     const size_t nS = (size_t)d.Nq * d.NPO;
-    CK(launch_rowsum(s, h->Pi0pp, h->Pi0ph, h->GR, h->SRtmp, h->twp, h->SPi0, h->SPi0 + nS, d));
+    CK(launch_tail_const(s, h->T0tail, d));
+    CK(launch_rowsum(s, h->Pi0pp, h->Pi0ph, h->GR, h->SRtmp, h->twp, h->SPi0, h->SPi0 + nS, d, h->T0tail));
     CK(cudaMemsetAsync(h->xS, 0, h->nstate * sizeof(cplx), s));
     CK(cudaMemsetAsync(h->yS, 0, h->nstate * sizeof(cplx), s));
     CK(cudaMemsetAsync(h->FLK2, 0, 3 * h->n2 * sizeof(cplx), s));
@@ -917,7 +921,7 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
     CK(launch_g_realspace(s, h->G, h->GR, h->twm, d));
     CK(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
-    CK(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + nS, d));
+    CK(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + nS, d, h->T0tail));
     CK(cudaStreamSynchronize(s));
     h->finalized = true;
     h->c0_dirty = true;
