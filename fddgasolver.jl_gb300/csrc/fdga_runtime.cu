@@ -90,6 +90,8 @@ struct fdga_handle {
     int k3_tile[2][2] = {{0, 0}, {0, 0}};  // [precision][mode]: K3 GEMM tile chosen by fdga_autotune (0: default)
     int last_launches = 0;
     cudaEvent_t ev[8] = {};
+    cudaStream_t st2 = nullptr, st3 = nullptr;                         // branch streams of the iteration
+    cudaEvent_t evfork = nullptr, evA = nullptr, evB = nullptr, evC = nullptr;
     // Anderson
     std::vector<cplx*> aa_buf;
     double* d_part = nullptr;
@@ -442,6 +444,15 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     nl = 0;
     VertP F = vertex_view(h, h->xS);
     VertP Fn = vertex_view(h, h->yS);  // Fbuff, i.e. the new F used by the SDE
+    // Independent parts run as concurrent branches (graph capture and batches; sequential when the
+    // stages are timed): B = Dyson + bubbles + row sums, C = left K2 BSE, main = momentum averages,
+    // caches and left K3 BSE; both branches join the main stream before the right BSEs.
+    const bool conc = !mark;
+    cudaStream_t sB = conc ? h->st2 : s, sC = conc ? h->st3 : s;
+    if (conc) {
+        CK(cudaEventRecord(h->evfork, s));
+        CK(cudaStreamWaitEvent(sB, h->evfork, 0));
+    }
     // momentum averages of F (kSW evaluation)
     if (d.Nq > 1) {
         ChanArrays in;
@@ -454,21 +465,22 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         stage("qavg");
     }
     if (update_sigma) {
-        LC(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
-        LC(launch_g_realspace(s, h->G, h->GR, h->twm, d));
+        LC(launch_dyson(sB, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
+        LC(launch_g_realspace(sB, h->G, h->GR, h->twm, d));
         if (h->precision == FDGA_MIXED && bubble_f32_supported(d)) {
             // mixed map: bubble and its full-mesh row sums in FP32 from an FP32 copy of G(R)
-            LC(launch_to_f32(s, h->GR, h->GRf, h->nGk));
-            LC(launch_bubble_f32(s, h->GRf, h->Pipp, h->Piph, d));
-            LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
+            LC(launch_to_f32(sB, h->GR, h->GRf, h->nGk));
+            LC(launch_bubble_f32(sB, h->GRf, h->Pipp, h->Piph, d));
+            LC(launch_rowsum(sB, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
                              h->T0tail, h->GRf));
         } else {
-            LC(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
-            LC(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
+            LC(launch_bubble(sB, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
+            LC(launch_rowsum(sB, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
                              h->T0tail));
         }
         stage("dyson_bubble");
     }
+    if (conc) CK(cudaEventRecord(h->evB, sB));
     // The mixed map evaluates vertices from an FP32 mirror of the state (converted once per
     // iteration) and keeps the caches, FL.K2 and FL.K3 in FP32: written once, read by the BSEs.
     const bool mixed = h->precision == FDGA_MIXED;
@@ -522,16 +534,21 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         return f;
     };
     if (strategy == FDGA_FDPA) {
-        {  // left K2 (FL.K2)
+        {  // left K2 (FL.K2): branch C
+            if (conc) {
+                CK(cudaEventRecord(h->evA, s));
+                CK(cudaStreamWaitEvent(sC, h->evA, 0));
+            }
             ChanWork cw = work(2, h->raw2);
-            if (mixed) LC(launch_bse_L_K2_all(s, Ff, B, cw, d));
-            else LC(launch_bse_L_K2_all(s, F, B, cw, d));
+            if (mixed) LC(launch_bse_L_K2_all(sC, Ff, B, cw, d));
+            else LC(launch_bse_L_K2_all(sC, F, B, cw, d));
             cplx* out[3] = {h->FLK2, h->FLK2 + h->n2, h->FLK2 + 2 * h->n2};
             const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
             Finalize3 f2 = fin(2, h->raw2, out, grp);
             if (mixed)
                 for (int c = 0; c < 3; ++c) f2.outf[c] = h->FLK2f + (size_t)c * h->n2;
-            LC(launch_finalize3(s, f2, 0, 1, h->n2));
+            LC(launch_finalize3(sC, f2, 0, 1, h->n2));
+            if (conc) CK(cudaEventRecord(h->evC, sC));
         }
         stage("bse_L_K2");
         {  // left K3 (FL.K3)
@@ -563,6 +580,10 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             LC(launch_finalize3(s, f3, 0, 1, h->n3));
         }
         stage("bse_L_K3_finalize");
+    }
+    if (conc) {  // join: bubbles (B) and FL.K2 (C)
+        CK(cudaStreamWaitEvent(s, h->evB, 0));
+        if (strategy == FDGA_FDPA) CK(cudaStreamWaitEvent(s, h->evC, 0));
     }
     // ω-sums of the right BSE factor (needs FL.K2 of this iteration)
     LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FL, h->SX, d));
@@ -807,6 +828,13 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
         return FDGA_ERR_CUDA;
     }
     for (auto& e : h->ev) cudaEventCreate(&e);
+    if (cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->st3, cudaStreamNonBlocking) != cudaSuccess) {
+        g_create_error = "cudaStreamCreate failed";
+        fdga_destroy(h);
+        return FDGA_ERR_CUDA;
+    }
+    for (cudaEvent_t* e : {&h->evfork, &h->evA, &h->evB, &h->evC}) cudaEventCreateWithFlags(e, cudaEventDisableTiming);
 #define ALC(ptr, n) do { r = dalloc(h, &(ptr), (n)); if (r) return fin_err(r); } while (0)
     ALC(h->Gbare, h->nGk); ALC(h->G0, h->nGk); ALC(h->Sig0, h->nGk); ALC(h->G, h->nGk);
     ALC(h->Pi0pp, h->nPi); ALC(h->Pi0ph, h->nPi); ALC(h->Pipp, h->nPi); ALC(h->Piph, h->nPi);
@@ -875,6 +903,8 @@ void fdga_destroy(fdga_handle* h) {
     if (h->flush_buf) cudaFree(h->flush_buf);
     for (void* p : h->allocs) cudaFree(p);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {h->evfork, h->evA, h->evB, h->evC}) if (e) cudaEventDestroy(e);
+    for (cudaStream_t t : {h->st2, h->st3}) if (t) { cudaStreamSynchronize(t); cudaStreamDestroy(t); }
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }
