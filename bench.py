@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge leg")
+    ap.add_argument("--U", type=float, default=None, help="override the configuration's U (differentiation runs)")
+    ap.add_argument("--restart", type=int, default=20, help="GMRES restart of the Newton solves (differentiation runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the oracle timing (for the large configurations, where one oracle iteration takes hours)")
     return ap.parse_args()
@@ -418,14 +420,18 @@ def run_differentiation(args, rank, world, dist):
     response (GMRES on (I − J) dx/dU = ∂Φ/∂U), checked against central differences h = 1e-4 of
     the converged χ_m at U ± h (same solver, re-solved from the fixed point)."""
     import numpy as np
-    cfg, S = build_problem(args.config, "ours")
+    from fdgasolver.workloads import CONFIGS, make_solver
+    cfg = dict(CONFIGS[args.config])
+    if args.U is not None:
+        cfg["U"] = args.U
+    S = make_solver(cfg, True)
     nO, L = 2 * cfg["nK1"] - 1, cfg["L"]
     iq = L // 2 + L * (L // 2)
     k0 = iq * nO + cfg["nK1"] - 1
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     t0 = time.perf_counter()
-    r = S.solve_newton("fdPA", maxiter=400, tol=1e-10, restart=20, jvp="mixed")
+    r = S.solve_newton("fdPA", maxiter=400, tol=1e-10, restart=args.restart, jvp="mixed")
     t_solve = time.perf_counter() - t0
     t0 = time.perf_counter()
     d, info = S.dchi_dU("m", hU=1e-4, restart=30, cycles=3, rtol=1e-7)
@@ -435,7 +441,7 @@ def run_differentiation(args, rank, world, dist):
     chi = {}
     for sgn in (+1, -1):
         S.set_U(U + sgn * h)
-        rs = S.solve_newton("fdPA", maxiter=400, tol=1e-11, restart=20, jvp="fp64")
+        rs = S.solve_newton("fdPA", maxiter=400, tol=1e-11, restart=args.restart, jvp="fp64")
         chi[sgn] = S.susceptibility("m")
         S.set_U(U)
     fd = (chi[+1] - chi[-1]) / (2 * h)
@@ -445,7 +451,8 @@ def run_differentiation(args, rank, world, dist):
         "value": t_lr, "unit": "s (linear response at the fixed point)", "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": t_lr * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 (FP64 complex)", "data": "synthetic (model inputs restated)",
-        "config": {"workload": WORKLOADS["config5"], "name": "config5", "parallelism": "single GPU"},
+        "config": {"workload": WORKLOADS["config5"] + ("" if args.U is None else f" (U overridden: {args.U})"),
+                   "name": "config5", "parallelism": "single GPU", "U": cfg["U"], "gmres_restart": args.restart},
         "solve": {"seconds": t_solve, "converged": r["converged"], "residual": r["residual"],
                   "newton_steps": r["newton"], "fp64_maps": r["evals_fp64"], "mixed_maps": r["evals_mixed"]},
         "dchi_m_dU": {"value": [d[k0].real, d[k0].imag], **info},
