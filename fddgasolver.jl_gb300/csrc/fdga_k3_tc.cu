@@ -45,11 +45,15 @@ __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo) {
     hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
     lo = v - hi;
 }
-__device__ __forceinline__ void st_pair(uint8_t* base, uint32_t off, float v, uint8_t* base_lo) {
-    float hi, lo;
-    split_tf32(v, hi, lo);
-    *reinterpret_cast<float*>(base + off) = hi;
-    *reinterpret_cast<float*>(base_lo + off) = lo;
+// four consecutive k of one row (16 bytes, 16-byte aligned): TF32 hi and lo parts
+__device__ __forceinline__ void st_quad(uint8_t* base_hi, uint8_t* base_lo, uint32_t off, float4 v) {
+    float4 hi, lo;
+    split_tf32(v.x, hi.x, lo.x);
+    split_tf32(v.y, hi.y, lo.y);
+    split_tf32(v.z, hi.z, lo.z);
+    split_tf32(v.w, hi.w, lo.w);
+    *reinterpret_cast<float4*>(base_hi + off) = hi;
+    *reinterpret_cast<float4*>(base_lo + off) = lo;
 }
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
@@ -127,53 +131,62 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
             for (int j = 0; j < 4; ++j) pis[tid][j] = v[j];
         }
         __syncthreads();
-        // A: (row ν, ω) items, 16 consecutive ω of one row per 16 threads (coalesced loads)
-        for (int e = tid; e < 128 * 16; e += TC_THREADS) {
-            const int nu = e >> 4, t = e & 15, w = w0 + t;
-            cplxf v{0.f, 0.f};
+        // A: (ω pair j, row ν) items, rows fastest so that a quarter warp's 16-byte stores fall in
+        // distinct banks; k = 4j..4j+3 holds [Re A(ω), Im A(ω), Re A(ω+1), Im A(ω+1)]
+        for (int e = tid; e < 128 * 8; e += TC_THREADS) {
+            const int nu = e & 127, j = e >> 7, w = w0 + 2 * j;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (nu < N && w < N) {
-                const float2 q = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w));
-                v = cplxf{q.x, q.y};
-            }
-            st_pair(Ahi, op_off(nu, 2 * t), v.x, Alo);
-            st_pair(Ahi, op_off(nu, 2 * t + 1), v.y, Alo);
-        }
-        // B: (t, ν') items of the chunk
-        for (int e = tid; e < 16 * N; e += TC_THREADS) {
-            const int t = e / N, col = e % N, w = w0 + t;
-            cplxf M{0.f, 0.f};
-            if (w < N) {
-                const cplxf pi0{pis[t][2], pis[t][3]};
-                const float2 q0 = __ldg(reinterpret_cast<const float2*>(a.B0 + base + (size_t)w * N + col));
-                const cplxf f0{q0.x, q0.y};
-                if (MODE == 0) {
-                    M = pi0 * f0;
-                } else {
-                    const cplxf pi{pis[t][0], pis[t][1]};
-                    const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
-                    const float2 qg = __ldg(reinterpret_cast<const float2*>(a.G + ig));
-                    const cplxf gs{qg.x, qg.y};
-                    M = ((pi - pi0) * f0 + pi * gs) * s1;
-                    const int ot = cross(CH, m, w - d.n3n);
-                    if (fin(ot, d.n3n)) {
-                        const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                        cplxf gl;
-                        if (CH == CH_T) {
-                            const float2 qt = __ldg(reinterpret_cast<const float2*>(a.FLt + il));
-                            const float2 qa = __ldg(reinterpret_cast<const float2*>(a.FLa + il));
-                            gl = cplxf{2.f * qt.x - qa.x, 2.f * qt.y - qa.y};
-                        } else {
-                            const float2 qc = __ldg(reinterpret_cast<const float2*>(a.FLc + il));
-                            gl = cplxf{qc.x, qc.y};
-                        }
-                        M += pi * gl * s2;
-                    }
+                const float2 q0 = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w));
+                v.x = q0.x; v.y = q0.y;
+                if (w + 1 < N) {
+                    const float2 q1 = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w + 1));
+                    v.z = q1.x; v.w = q1.y;
                 }
             }
-            st_pair(Bhi, op_off(2 * col, 2 * t), M.x, Blo);
-            st_pair(Bhi, op_off(2 * col + 1, 2 * t), M.y, Blo);
-            st_pair(Bhi, op_off(2 * col, 2 * t + 1), -M.y, Blo);
-            st_pair(Bhi, op_off(2 * col + 1, 2 * t + 1), M.x, Blo);
+            st_quad(Ahi, Alo, op_off(nu, 4 * j), v);
+        }
+        // B: (ω pair j, ν') items, ν' fastest (coalesced loads of the cache rows); rows 2ν' and
+        // 2ν'+1 of the real form, k = 4j..4j+3: [Re M(ω), −Im M(ω), Re M(ω+1), −Im M(ω+1)] and
+        // [Im M(ω), Re M(ω), Im M(ω+1), Re M(ω+1)]
+        for (int e = tid; e < 8 * N; e += TC_THREADS) {
+            const int j = e / N, col = e % N;
+            cplxf M2[2];
+            for (int h2 = 0; h2 < 2; ++h2) {
+                const int t = 2 * j + h2, w = w0 + t;
+                cplxf M{0.f, 0.f};
+                if (w < N) {
+                    const cplxf pi0{pis[t][2], pis[t][3]};
+                    const float2 q0 = __ldg(reinterpret_cast<const float2*>(a.B0 + base + (size_t)w * N + col));
+                    const cplxf f0{q0.x, q0.y};
+                    if (MODE == 0) {
+                        M = pi0 * f0;
+                    } else {
+                        const cplxf pi{pis[t][0], pis[t][1]};
+                        const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
+                        const float2 qg = __ldg(reinterpret_cast<const float2*>(a.G + ig));
+                        const cplxf gs{qg.x, qg.y};
+                        M = ((pi - pi0) * f0 + pi * gs) * s1;
+                        const int ot = cross(CH, m, w - d.n3n);
+                        if (fin(ot, d.n3n)) {
+                            const size_t il = base + (size_t)(ot + d.n3n) * N + col;
+                            cplxf gl;
+                            if (CH == CH_T) {
+                                const float2 qt = __ldg(reinterpret_cast<const float2*>(a.FLt + il));
+                                const float2 qa = __ldg(reinterpret_cast<const float2*>(a.FLa + il));
+                                gl = cplxf{2.f * qt.x - qa.x, 2.f * qt.y - qa.y};
+                            } else {
+                                const float2 qc = __ldg(reinterpret_cast<const float2*>(a.FLc + il));
+                                gl = cplxf{qc.x, qc.y};
+                            }
+                            M += pi * gl * s2;
+                        }
+                    }
+                }
+                M2[h2] = M;
+            }
+            st_quad(Bhi, Blo, op_off(2 * col, 4 * j), make_float4(M2[0].x, -M2[0].y, M2[1].x, -M2[1].y));
+            st_quad(Bhi, Blo, op_off(2 * col + 1, 4 * j), make_float4(M2[0].y, M2[0].x, M2[1].y, M2[1].x));
         }
         // generic-proxy writes -> visible to the tensor core (async proxy)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
