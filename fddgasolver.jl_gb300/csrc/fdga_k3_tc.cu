@@ -229,18 +229,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (nu < N) {
+                // epilogue in FP32 (one conversion per value at the store)
+                const float Tf = (float)T, sgn = (CH == CH_A) ? 1.f : -1.f;
                 for (int j = 0; j < 8; ++j) {
                     const int col = c0 / 2 + j;
                     if (col >= N) break;
-                    const cplx v = cplx{(double)__uint_as_float(r[2 * j]), (double)__uint_as_float(r[2 * j + 1])};
+                    const cplxf v{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
                     const size_t io = base + (size_t)nu * N + col;
                     if (MODE == 0) {
-                        a.out[io] = v * (T * ((CH == CH_A) ? 1.0 : -1.0));
+                        a.out[io] = to_d(v * (Tf * sgn));
                     } else {
-                        cplx gl;
-                        if (CH == CH_T) gl = 2.0 * to_d(cplxf{a.FLt[io].x, a.FLt[io].y}) - to_d(cplxf{a.FLa[io].x, a.FLa[io].y});
-                        else gl = to_d(cplxf{a.FLc[io].x, a.FLc[io].y});
-                        a.out[io] = v * T + gl;
+                        cplxf gl;
+                        if (CH == CH_T) gl = cplxf{2.f * a.FLt[io].x - a.FLa[io].x, 2.f * a.FLt[io].y - a.FLa[io].y};
+                        else gl = a.FLc[io];
+                        a.out[io] = to_d(v * Tf + gl);
                     }
                 }
             }

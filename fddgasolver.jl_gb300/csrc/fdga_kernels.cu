@@ -652,8 +652,6 @@ template <class C> __device__ __forceinline__ C ldk(const cplxf* p) {
     const float2 v = __ldg(reinterpret_cast<const float2*>(p));
     return C{v.x, v.y};
 }
-__device__ __forceinline__ cplx ldk_d(const cplx* p) { return ldg(p); }
-__device__ __forceinline__ cplx ldk_d(const cplxf* p) { return to_d(ldk<cplxf>(p)); }
 
 // ARGS = K3Args3 (FP64 operands) or K3Args3F (FP32 operands).  C = cplx: FP64 arithmetic (the plain
 // path).  C = cplxf: FP32 products and accumulation, FP64 epilogue (the mixed path; FP64 operands
@@ -729,12 +727,12 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
             const int row = row0 + ty + H * i, col = col0 + tx + H * j;
             if (row >= N || col >= N) continue;
             const size_t io = base + (size_t)row * N + col;
-            const cplx r = to_d(acc[i][j]);
+            // epilogue in the arithmetic type C (FP64 ops cost 64 FP32 ops on this part)
             if (MODE == 0) {
-                a.out[io] = r * (d.T * ((CH == CH_A) ? 1.0 : -1.0));
+                a.out[io] = to_d(acc[i][j] * (R)(d.T * ((CH == CH_A) ? 1.0 : -1.0)));
             } else {
-                const cplx gl = (CH == CH_T) ? 2.0 * ldk_d(a.FLt + io) - ldk_d(a.FLa + io) : ldk_d(a.FLc + io);
-                a.out[io] = r * d.T + gl;
+                const C gl = (CH == CH_T) ? ldk<C>(a.FLt + io) * (R)2 - ldk<C>(a.FLa + io) : ldk<C>(a.FLc + io);
+                a.out[io] = to_d(acc[i][j] * (R)d.T + gl);
             }
         }
 }
