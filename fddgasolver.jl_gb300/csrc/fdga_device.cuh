@@ -123,6 +123,7 @@ struct VertPT {
     const S* Fp_x;
     const S* Ft_p;
     const S* Ft_x;
+    int noref;  // 1: the RefVertex terms (U and its corrections) read as zero (a tangent vertex)
 };
 using ChanP = ChanPT<cplx>;
 using VertP = VertPT<cplx>;
@@ -210,6 +211,7 @@ __device__ __forceinline__ S ref_call(const S* f, const Dims& d, int m, int n, i
 // RefVertex in the parallel spin component (src/refvertex.jl:90-125, 178-216).
 template <class S>
 __device__ __forceinline__ S ref_pSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np) {
+    if (F.noref) return S{0, 0};
     if (n == FINF || np == FINF) return cre<S>(d.U);
     if (ch == CH_P) return ref_call(F.Fp_p, d, m, n, np) + cre<S>(d.U);
     if (ch == CH_T) return ref_call(F.Ft_p, d, m, n, np) + cre<S>(d.U);
@@ -218,6 +220,7 @@ __device__ __forceinline__ S ref_pSp(const VertPT<S>& F, const Dims& d, int ch, 
 // RefVertex in the crossed spin component (src/refvertex.jl:127-164).
 template <class S>
 __device__ __forceinline__ S ref_xSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np) {
+    if (F.noref) return S{0, 0};
     if (n == FINF || np == FINF) return cre<S>(-d.U);
     if (ch == CH_P) return ref_call(F.Fp_x, d, m, n, np) - cre<S>(d.U);
     if (ch == CH_T) return ref_call(F.Ft_x, d, m, n, np) - cre<S>(d.U);

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
             float v[4] = {0.f, 0.f, 0.f, 0.f};
             if (w < N) {
                 const size_t ip = ixPi(d, P, m, w - d.n3n);
-                const cplx p0 = ldg(a.Pi0 + ip);
+                const cplx p0 = a.Pi0 ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
                 v[2] = (float)p0.x; v[3] = (float)p0.y;
                 if (MODE == 1) { const cplx p = ldg(a.Pi + ip); v[0] = (float)p.x; v[1] = (float)p.y; }
             }
@@ -236,14 +236,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
                     if (col >= N) break;
                     const cplxf v{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
                     const size_t io = base + (size_t)nu * N + col;
+                    cplx o;
                     if (MODE == 0) {
-                        a.out[io] = to_d(v * (Tf * sgn));
+                        o = to_d(v * (Tf * sgn));
+                    } else if (a.flags & K3F_NOEPI) {
+                        o = to_d(v * Tf);
                     } else {
                         cplxf gl;
                         if (CH == CH_T) gl = cplxf{2.f * a.FLt[io].x - a.FLa[io].x, 2.f * a.FLt[io].y - a.FLa[io].y};
                         else gl = a.FLc[io];
-                        a.out[io] = to_d(v * Tf + gl);
+                        o = to_d(v * Tf + gl);
                     }
+                    a.out[io] = (a.flags & K3F_ACC) ? a.out[io] + o : o;
                 }
             }
         }

@@ -21,6 +21,14 @@ __global__ void k_dyson(cplx* G, const cplx* Sig, const cplx* Gb, size_t n) {
     G[i] = cdiv(one, cdiv(one, Gb[i]) + Sig[i]);
 }
 
+// Tangent of the Dyson update G = 1/(1/Gb + Σ) (in the stored iG, iΣ convention): dG = -G² dΣ.
+__global__ void k_dyson_tan(cplx* tG, const cplx* G, const cplx* tSig, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const cplx g = G[i];
+    tG[i] = (g * g) * (tSig[i] * -1.0);
+}
+
 // n = 1/2 + T Im(Σ G) / Nk  (src/dyson.jl:33-41); single block, deterministic order.
 __global__ void k_occupation(const cplx* G, size_t n, double T, int Nk, double* out) {
     __shared__ double red[1024];
@@ -70,13 +78,34 @@ __device__ __forceinline__ C g_tail_t(const G* Gp, const Dims& d, int k, int n) 
     return C{(R)1 / (((R)2 * n + (R)1) * (R)M_PI * (R)d.T), (R)0};
 }
 
-__global__ void k_bubble_local(const cplx* G, cplx* pp, cplx* ph, Dims d) {
+// tangent of g_tail_t: the 1/ν tail is constant, so the derivative is zero outside the box
+template <class C, class G>
+__device__ __forceinline__ C g_box_t(const G* Gp, const Dims& d, int k, int n) {
+    if (fin(n, d.nG)) return to_c<C>(Gp[ixG(d, k, n)]);
+    return C{0, 0};
+}
+// a·b, or for the tangent map (TAN) the product rule da·b + a·db
+template <bool TAN, class C>
+__device__ __forceinline__ C prod2(C a, C da, C b, C db) {
+    if (TAN) return cfma(da, b, a * db);
+    return a * b;
+}
+
+// TAN: the tangent bubbles dΠ from G and its tangent tG (product rule, the tails are constant)
+template <bool TAN>
+__global__ void k_bubble_local(const cplx* G, const cplx* tG, cplx* pp, cplx* ph, Dims d) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= (size_t)d.NPO * d.NPw) return;
     const int n = (int)(i % d.NPw) - d.nPw, m = (int)(i / d.NPw) - (d.nPO - 1);
     const cplx Gn = g_tail(G, d, 0, n);
-    pp[i] = Gn * g_tail(G, d, 0, m - n - 1);
-    ph[i] = Gn * g_tail(G, d, 0, m + n);
+    if (!TAN) {
+        pp[i] = Gn * g_tail(G, d, 0, m - n - 1);
+        ph[i] = Gn * g_tail(G, d, 0, m + n);
+        return;
+    }
+    const cplx tn = g_box_t<cplx>(tG, d, 0, n);
+    pp[i] = prod2<true>(Gn, tn, g_tail(G, d, 0, m - n - 1), g_box_t<cplx>(tG, d, 0, m - n - 1));
+    ph[i] = prod2<true>(Gn, tn, g_tail(G, d, 0, m + n), g_box_t<cplx>(tG, d, 0, m + n));
 }
 
 // Nonlocal bubbles in real space (src/nonlocal/bubble.jl:87-158) for L_G = L:
@@ -84,7 +113,8 @@ __global__ void k_bubble_local(const cplx* G, cplx* pp, cplx* ph, Dims d) {
 //   Π(P) = Σ_R Π(R) e^{+2πi P·R/L}  (bfft).  For L_G = L the ±L/2 half weights of the reference's
 //   R scan sum to one per lattice site, so the scan is one pass over the L x L sites.
 // One CTA = one Ω and a tile of TV fermionic frequencies; shared: Π(R) then the P transform.
-__global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp, Dims d, int TV) {
+template <bool TAN>
+__global__ void k_bubble_nl(const cplx* GR, const cplx* tGR, cplx* pp, cplx* ph, const cplx* twp, Dims d, int TV) {
     extern __shared__ cplx sh[];
     const int L = d.L, NR = L * L;
     cplx* A = sh;                     // [2][TV][NR]   (pp, ph) in R
@@ -99,12 +129,19 @@ __global__ void k_bubble_nl(const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
             const int Rx = R % L, Ry = R / L;
             const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
             if (R == 0) {
-                vpp = g_tail(GR, d, 0, m - n - 1) * g_tail(GR, d, 0, n);
-                vph = g_tail(GR, d, 0, m + n) * g_tail(GR, d, 0, n);
+                const cplx gn = g_tail(GR, d, 0, n), tn = TAN ? g_box_t<cplx>(tGR, d, 0, n) : gn;
+                vpp = prod2<TAN>(g_tail(GR, d, 0, m - n - 1), TAN ? g_box_t<cplx>(tGR, d, 0, m - n - 1) : gn, gn, tn);
+                vph = prod2<TAN>(g_tail(GR, d, 0, m + n), TAN ? g_box_t<cplx>(tGR, d, 0, m + n) : gn, gn, tn);
             } else {
                 const int a = m - n - 1, b = m + n;
-                if (fin(a, d.nG) && fin(n, d.nG)) vpp = GR[ixG(d, R, a)] * GR[ixG(d, R, n)];
-                if (fin(b, d.nG) && fin(n, d.nG)) vph = GR[ixG(d, R, b)] * GR[ixG(d, mR, n)];
+                if (fin(a, d.nG) && fin(n, d.nG)) {
+                    const size_t i1 = ixG(d, R, a), i2 = ixG(d, R, n);
+                    vpp = prod2<TAN>(GR[i1], TAN ? tGR[i1] : GR[i1], GR[i2], TAN ? tGR[i2] : GR[i2]);
+                }
+                if (fin(b, d.nG) && fin(n, d.nG)) {
+                    const size_t i1 = ixG(d, R, b), i2 = ixG(d, mR, n);
+                    vph = prod2<TAN>(GR[i1], TAN ? tGR[i1] : GR[i1], GR[i2], TAN ? tGR[i2] : GR[i2]);
+                }
             }
         }
         A[(size_t)v * NR + R] = vpp;
@@ -180,8 +217,8 @@ __device__ __forceinline__ void fft_bwd(C (&v)[L]) {
     }
 }
 
-template <int L, class C, class G>
-__global__ void k_bubble_fft(const G* GR, cplx* pp, cplx* ph, Dims d, int TV) {
+template <int L, class C, class G, bool TAN>
+__global__ void k_bubble_fft(const G* GR, const G* tGR, cplx* pp, cplx* ph, Dims d, int TV) {
     extern __shared__ __align__(16) unsigned char sh_raw[];
     C* sh = reinterpret_cast<C*>(sh_raw);
     constexpr int NR = L * L, RS = L + 1, BS = L * (L + 1) + 1;
@@ -195,12 +232,21 @@ __global__ void k_bubble_fft(const G* GR, cplx* pp, cplx* ph, Dims d, int TV) {
         if (n < d.nPw) {
             const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
             if (R == 0) {
-                vpp = g_tail_t<C>(GR, d, 0, m - n - 1) * g_tail_t<C>(GR, d, 0, n);
-                vph = g_tail_t<C>(GR, d, 0, m + n) * g_tail_t<C>(GR, d, 0, n);
+                const C gn = g_tail_t<C>(GR, d, 0, n), tn = TAN ? g_box_t<C>(tGR, d, 0, n) : gn;
+                vpp = prod2<TAN>(g_tail_t<C>(GR, d, 0, m - n - 1), TAN ? g_box_t<C>(tGR, d, 0, m - n - 1) : gn, gn, tn);
+                vph = prod2<TAN>(g_tail_t<C>(GR, d, 0, m + n), TAN ? g_box_t<C>(tGR, d, 0, m + n) : gn, gn, tn);
             } else {
                 const int a = m - n - 1, b = m + n;
-                if (fin(a, d.nG) && fin(n, d.nG)) vpp = to_c<C>(GR[ixG(d, R, a)]) * to_c<C>(GR[ixG(d, R, n)]);
-                if (fin(b, d.nG) && fin(n, d.nG)) vph = to_c<C>(GR[ixG(d, R, b)]) * to_c<C>(GR[ixG(d, mR, n)]);
+                if (fin(a, d.nG) && fin(n, d.nG)) {
+                    const size_t i1 = ixG(d, R, a), i2 = ixG(d, R, n);
+                    const C g1 = to_c<C>(GR[i1]), g2 = to_c<C>(GR[i2]);
+                    vpp = prod2<TAN>(g1, TAN ? to_c<C>(tGR[i1]) : g1, g2, TAN ? to_c<C>(tGR[i2]) : g2);
+                }
+                if (fin(b, d.nG) && fin(n, d.nG)) {
+                    const size_t i1 = ixG(d, R, b), i2 = ixG(d, mR, n);
+                    const C g1 = to_c<C>(GR[i1]), g2 = to_c<C>(GR[i2]);
+                    vph = prod2<TAN>(g1, TAN ? to_c<C>(tGR[i1]) : g1, g2, TAN ? to_c<C>(tGR[i2]) : g2);
+                }
             }
         }
         sh[(size_t)v * BS + Ry * RS + Rx] = vpp;
@@ -399,12 +445,15 @@ __global__ void k_build_cache(VertPT<S> F, Caches C, const int* blocks, int nblo
     v[7] = fp;
     v[8] = fa;
     v[9] = ft * (R)2 - fa;
+    // an absent cache (nullptr) is not written: the RefVertex caches of a tangent vertex are zero
     if (C.f[0]) {
 #pragma unroll
-        for (int k = 0; k < 10; ++k) C.f[k][i] = to_f32(v[k]);
+        for (int k = 0; k < 10; ++k)
+            if (C.f[k]) C.f[k][i] = to_f32(v[k]);
     } else {
 #pragma unroll
-        for (int k = 0; k < 10; ++k) C.c[k][i] = to_d(v[k]);
+        for (int k = 0; k < 10; ++k)
+            if (C.c[k]) C.c[k][i] = to_d(v[k]);
     }
 }
 
@@ -451,8 +500,9 @@ __global__ void k_tail_const(cplx* T0, Dims d) {
     acc = warp_sum(acc);
     if (lane == 0) T0[w] = acc;
 }
-template <class C, class G>
-__global__ void k_pisum_R(const G* GR, const cplx* T0, cplx* SR, Dims d) {
+// TAN: row sums of the tangent bubbles (product rule with tGR; the tails and T0 are constant)
+template <class C, class G, bool TAN>
+__global__ void k_pisum_R(const G* GR, const G* tGR, const cplx* T0, cplx* SR, Dims d) {
     const int NR = d.L * d.L;
     const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -468,25 +518,28 @@ __global__ void k_pisum_R(const G* GR, const cplx* T0, cplx* SR, Dims d) {
         // iteration-independent T0 (k_tail_const), added below
         for (int n = -d.nG + lane; n < d.nG; n += 32) {  // n inside the box
             if (!fin(n, d.nPn)) continue;
-            acc = cfma(which ? g_tail_t<C>(GR, d, 0, m + n) : g_tail_t<C>(GR, d, 0, m - n - 1), g_tail_t<C>(GR, d, 0, n),
-                       acc);
+            const int p = which ? m + n : m - n - 1;
+            if (TAN)
+                acc += prod2<true>(g_tail_t<C>(GR, d, 0, p), g_box_t<C>(tGR, d, 0, p), g_tail_t<C>(GR, d, 0, n),
+                                   g_box_t<C>(tGR, d, 0, n));
+            else
+                acc = cfma(g_tail_t<C>(GR, d, 0, p), g_tail_t<C>(GR, d, 0, n), acc);
         }
         for (int a = -d.nG + lane; a < d.nG; a += 32) {  // partner inside the box, n outside
             const int n = which ? a - m : m - 1 - a;
             if (fin(n, d.nG) || !fin(n, d.nPn)) continue;
-            acc = cfma(g_tail_t<C>(GR, d, 0, a), g_tail_t<C>(GR, d, 0, n), acc);
+            acc = cfma(TAN ? g_box_t<C>(tGR, d, 0, a) : g_tail_t<C>(GR, d, 0, a), g_tail_t<C>(GR, d, 0, n), acc);
         }
-        if (lane == 0 && T0) acc += to_c<C>(T0[(size_t)which * d.NPO + (m + d.nPO - 1)]);
+        if (lane == 0 && T0 && !TAN) acc += to_c<C>(T0[(size_t)which * d.NPO + (m + d.nPO - 1)]);
     } else {
         for (int n = -d.nG + lane; n < d.nG; n += 32) {
             if (!fin(n, d.nPn)) continue;
-            if (which) {
-                const int b = m + n;
-                if (fin(b, d.nG)) acc = cfma(to_c<C>(GR[ixG(d, R, b)]), to_c<C>(GR[ixG(d, mR, n)]), acc);
-            } else {
-                const int a = m - n - 1;
-                if (fin(a, d.nG)) acc = cfma(to_c<C>(GR[ixG(d, R, a)]), to_c<C>(GR[ixG(d, R, n)]), acc);
-            }
+            const int p = which ? m + n : m - n - 1;
+            if (!fin(p, d.nG)) continue;
+            const size_t i1 = ixG(d, R, p), i2 = ixG(d, which ? mR : R, n);
+            const C g1 = to_c<C>(GR[i1]), g2 = to_c<C>(GR[i2]);
+            if (TAN) acc += prod2<true>(g1, to_c<C>(tGR[i1]), g2, to_c<C>(tGR[i2]));
+            else acc = cfma(g1, g2, acc);
         }
     }
     acc = warp_sum(acc);
@@ -518,6 +571,34 @@ __global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const 
     if (lane == 0) SX[i] = (SPi[w * per + r] - SPi0[w * per + r]) * d.U + v;
 }
 
+// Tangent of S_X: dS_X = dSΠ U + Σ_ω [dΠ FL(Ω,ω̃,∞) + Π dFL(Ω,ω̃,∞)]  (SΠ0 is constant).
+__global__ void k_sx_tan(const cplx* Pipp, const cplx* Piph, const cplx* tPipp, const cplx* tPiph, const cplx* tSPi,
+                         FLP FL, FLP tFL, cplx* tSX, Dims d) {
+    const size_t per = (size_t)d.Nq * d.NPO;
+    const size_t i = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= 3 * per) return;
+    const int ch = (int)(i / per);
+    const size_t r = i % per;
+    const int m = (int)(r % d.NPO) - (d.nPO - 1), P = (int)(r / d.NPO);
+    const int w = (ch == CH_P) ? 0 : 1;
+    const cplx* Pi = w ? Piph : Pipp;
+    const cplx* tPi = w ? tPiph : tPipp;
+    cplx v = mk(0, 0);
+    if (bin(m, d.n2O)) {
+        for (int t = lane; t < d.N2n; t += 32) {
+            const int nt = t - d.n2n;
+            const int n = (ch == CH_P) ? m - nt - 1 : nt;
+            if (!fin(n, d.nPw)) continue;
+            const size_t ip = ixPi(d, P, m, n);
+            v += tPi[ip] * fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, ch, m, nt, P);
+            v += Pi[ip] * fl_right(tFL.K2[CH_P], tFL.K2[CH_T], tFL.K2[CH_A], d, ch, m, nt, P);
+        }
+    }
+    v = warp_sum(v);
+    if (lane == 0) tSX[i] = tSPi[w * per + r] * d.U + v;
+}
+
 // ---------------------------------------------------------------------------------------------
 // K1 BSE (src/BSEa/BSEa_K1.jl:2-54, src/nonlocal/BSEa/BSEa_K1.jl:2-57), warp per item:
 //   K1(Ω,P) = T s Σ_ω F(Ω,∞,ω) X(ω),  X(ω) = (Π-Π0)(Ω,ω) U + Π(Ω,ω) FL(Ω,ω̃,∞).
@@ -526,7 +607,8 @@ __global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const 
 // ---------------------------------------------------------------------------------------------
 template <int CH, class S>
 __device__ __forceinline__ void bse_K1_body(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
-                                            const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
+                                            const cplx* SX, cplx* out, const int* items, int nitems, int accum,
+                                            const Dims& d) {
     using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
@@ -542,14 +624,15 @@ __device__ __forceinline__ void bse_K1_body(const VertPT<S>& F, const FLPT<S>& F
             const S Fl = vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
             const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
             const size_t ip = ixPi(d, P, m, n);
-            const S pi = to_c<S>(ldg(Pi + ip)), pi0 = to_c<S>(ldg(Pi0 + ip));
+            const S pi = to_c<S>(ldg(Pi + ip)), pi0 = Pi0 ? to_c<S>(ldg(Pi0 + ip)) : S{0, 0};
             acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
         }
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-        const S sx = to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]);
-        out[idx] = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+        const S sx = SX ? to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]) : S{0, 0};
+        const cplx v = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+        out[idx] = accum ? out[idx] + v : v;
     }
 }
 
@@ -597,7 +680,8 @@ __device__ __forceinline__ void bse_L_K2_body(const VertPT<S>& F, const cplx* Pi
 // ---------------------------------------------------------------------------------------------
 template <int CH, class S>
 __device__ __forceinline__ void bse_K2_body(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
-                                            const cplx* SX, cplx* out, const int* items, int nitems, const Dims& d) {
+                                            const cplx* SX, cplx* out, const int* items, int nitems, int accum,
+                                            const Dims& d) {
     using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
@@ -625,13 +709,14 @@ __device__ __forceinline__ void bse_K2_body(const VertPT<S>& F, const FLPT<S>& F
         const S Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
         const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
-        const S pi = to_c<S>(ldg(Pi + ip)), pi0 = to_c<S>(ldg(Pi0 + ip));
+        const S pi = to_c<S>(ldg(Pi + ip)), pi0 = Pi0 ? to_c<S>(ldg(Pi0 + ip)) : S{0, 0};
         acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-        const S sx = to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]);
-        out[idx] = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+        const S sx = SX ? to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]) : S{0, 0};
+        const cplx v = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+        out[idx] = accum ? out[idx] + v : v;
     }
 }
 
@@ -688,7 +773,7 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
             if (k < N && col < N) {
                 const int o = k - d.n3n;  // ω as fermion index
                 const size_t ip = ixPi(d, P, m, o);
-                const C pi0 = to_c<C>(ldg(a.Pi0 + ip));
+                const C pi0 = a.Pi0 ? to_c<C>(ldg(a.Pi0 + ip)) : czero<C>();
                 const C f0 = ldk<C>(a.B0 + base + (size_t)k * N + col);
                 if (MODE == 0) {
                     v = pi0 * f0;
@@ -728,12 +813,16 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
             if (row >= N || col >= N) continue;
             const size_t io = base + (size_t)row * N + col;
             // epilogue in the arithmetic type C (FP64 ops cost 64 FP32 ops on this part)
+            cplx v;
             if (MODE == 0) {
-                a.out[io] = to_d(acc[i][j] * (R)(d.T * ((CH == CH_A) ? 1.0 : -1.0)));
+                v = to_d(acc[i][j] * (R)(d.T * ((CH == CH_A) ? 1.0 : -1.0)));
+            } else if (a.flags & K3F_NOEPI) {
+                v = to_d(acc[i][j] * (R)d.T);
             } else {
                 const C gl = (CH == CH_T) ? ldk<C>(a.FLt + io) * (R)2 - ldk<C>(a.FLa + io) : ldk<C>(a.FLc + io);
-                a.out[io] = to_d(acc[i][j] * (R)d.T + gl);
+                v = to_d(acc[i][j] * (R)d.T + gl);
             }
+            a.out[io] = (a.flags & K3F_ACC) ? a.out[io] + v : v;
         }
 }
 
@@ -749,7 +838,7 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
 // ---------------------------------------------------------------------------------------------
 template <int WHICH, class S>
 __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, const cplx* SPi, cplx* out,
-                                           const int* items, int nitems, int use_vertex, double ref_scale,
+                                           const int* items, int nitems, int use_vertex, double ref_scale, int accum,
                                            const Dims& d) {
     using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -792,7 +881,8 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
     accr = warp_sum(accr) * (R)d.U;
     if (lane == 0) {
         if (use_vertex) acc += c * (to_c<S>(ldg(SPi + (size_t)P * d.NPO + (m + d.nPO - 1))) * (R)d.U);
-        out[idx] = to_d(acc * (R)d.T + accr * (R)(d.T * ref_scale));
+        const cplx v = to_d(acc * (R)d.T + accr * (R)(d.T * ref_scale));
+        out[idx] = accum ? out[idx] + v : v;
     }
 }
 
@@ -802,9 +892,9 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
 template <class S>
 __global__ void k_bse_K1_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
     switch (blockIdx.y) {
-        case CH_P: bse_K1_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
-        case CH_T: bse_K1_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
-        default:   bse_K1_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+        case CH_P: bse_K1_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d); break;
+        case CH_T: bse_K1_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d); break;
+        default:   bse_K1_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d); break;
     }
 }
 template <class S>
@@ -818,16 +908,17 @@ __global__ void k_bse_L_K2_all(VertPT<S> F, BubbleP B, ChanWork cw, Dims d) {
 template <class S>
 __global__ void k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
     switch (blockIdx.y) {
-        case CH_P: bse_K2_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
-        case CH_T: bse_K2_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
-        default:   bse_K2_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+        case CH_P: bse_K2_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d); break;
+        case CH_T: bse_K2_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d); break;
+        default:   bse_K2_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d); break;
     }
 }
 template <class S>
 __global__ void k_sde_L_all(VertPT<S> F, BubbleP B, const cplx* SPpp, const cplx* SPph, ChanWork cw, int use_vertex,
                             double ref_scale, Dims d) {
-    if (blockIdx.y == 0) sde_L_body<0>(F, B.pp, SPpp, cw.out[0], cw.items[0], cw.nitems[0], use_vertex, ref_scale, d);
-    else sde_L_body<1>(F, B.ph, SPph, cw.out[1], cw.items[1], cw.nitems[1], use_vertex, ref_scale, d);
+    if (blockIdx.y == 0)
+        sde_L_body<0>(F, B.pp, SPpp, cw.out[0], cw.items[0], cw.nitems[0], use_vertex, ref_scale, cw.acc, d);
+    else sde_L_body<1>(F, B.ph, SPph, cw.out[1], cw.items[1], cw.nitems[1], use_vertex, ref_scale, cw.acc, d);
 }
 
 // Finalize of one vertex class for the three channels (out-of-place from the representative
@@ -867,7 +958,10 @@ __global__ void k_finalize3(Finalize3 f, int k2_epilogue, int t_recombine, size_
 //   Σ_R(ν, R) = Σ_Ω [G(-R, Ω-ν) Lpp(R, Ω, ν) + G(R, Ω+ν) Lph(-R, Ω, ν)],  L(R) = (1/N) Σ_P L(P) e^{-iP·R},
 //   Σ(ν, k) = T Σ_R e^{+ik·R} Σ_R(ν, R)   (the k transform is launch_fft2).  For L_G = L the ±L/2
 //   half weights of the reference's R scan sum to one per site.  Warp per (R, ν), lanes over Ω.
-__global__ void k_sde_sigma_R(const cplx* GR, const cplx* LppR, const cplx* LphR, cplx* SR, Dims d) {
+// TAN: the tangent dΣ_R = Σ_Ω [dG L + G dL] from tGR and the transformed tangent tLppR, tLphR.
+template <bool TAN>
+__global__ void k_sde_sigma_R(const cplx* GR, const cplx* LppR, const cplx* LphR, const cplx* tGR, const cplx* tLppR,
+                              const cplx* tLphR, cplx* SR, Dims d) {
     const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     const int NR = d.L * d.L;
@@ -880,8 +974,14 @@ __global__ void k_sde_sigma_R(const cplx* GR, const cplx* LppR, const cplx* LphR
         for (int t = lane; t < d.N2O; t += 32) {
             const int m = t - (d.n2O - 1);
             const int a = m - nu - 1, b = m + nu;
-            if (fin(a, d.nG)) acc = cfma(GR[ixG(d, mR, a)], LppR[ix2(d, R, m, nu)], acc);
-            if (fin(b, d.nG)) acc = cfma(GR[ixG(d, R, b)], LphR[ix2(d, mR, m, nu)], acc);
+            if (fin(a, d.nG)) {
+                const size_t ig = ixG(d, mR, a), il = ix2(d, R, m, nu);
+                acc = TAN ? cfma(tGR[ig], LppR[il], cfma(GR[ig], tLppR[il], acc)) : cfma(GR[ig], LppR[il], acc);
+            }
+            if (fin(b, d.nG)) {
+                const size_t ig = ixG(d, R, b), il = ix2(d, mR, m, nu);
+                acc = TAN ? cfma(tGR[ig], LphR[il], cfma(GR[ig], tLphR[il], acc)) : cfma(GR[ig], LphR[il], acc);
+            }
         }
     }
     acc = warp_sum(acc);
@@ -891,7 +991,9 @@ __global__ void k_sde_sigma_R(const cplx* GR, const cplx* LppR, const cplx* LphR
 // U² term (src/SDE.jl:328-364, src/nonlocal/SDE.jl:400-447), factorised:
 //   C_R(s) = Σ_{n1} G(-R, n1) G(R, n1 + s);   Σ_U²(ν, R) = U² T² Σ_{n2} G(R, n2) C_R(ν - n2)
 // GR layout [R][ν] (G(R)); s in [-(2nG-1), 2nG-1].
-__global__ void k_u2_corr(const cplx* GR, cplx* C, Dims d) {
+// TAN: tangents dC from tGR (product rule), then dΣ_U² = U² T² Σ [dG C + G dC].
+template <bool TAN>
+__global__ void k_u2_corr(const cplx* GR, const cplx* tGR, cplx* C, Dims d) {
     const int NS = 2 * d.NG - 1;
     const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -904,12 +1006,14 @@ __global__ void k_u2_corr(const cplx* GR, cplx* C, Dims d) {
     for (int n1 = -d.nG + lane; n1 < d.nG; n1 += 32) {
         const int n3 = n1 + s;
         if (!fin(n3, d.nG)) continue;
-        acc = cfma(GR[ixG(d, mR, n1)], GR[ixG(d, R, n3)], acc);
+        const size_t i1 = ixG(d, mR, n1), i3 = ixG(d, R, n3);
+        acc = TAN ? cfma(tGR[i1], GR[i3], cfma(GR[i1], tGR[i3], acc)) : cfma(GR[i1], GR[i3], acc);
     }
     acc = warp_sum(acc);
     if (lane == 0) C[w] = acc;
 }
-__global__ void k_u2_sum(const cplx* GR, const cplx* C, cplx* out, Dims d) {
+template <bool TAN>
+__global__ void k_u2_sum(const cplx* GR, const cplx* C, const cplx* tGR, const cplx* tC, cplx* out, Dims d) {
     const int NS = 2 * d.NG - 1;
     const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -919,7 +1023,8 @@ __global__ void k_u2_sum(const cplx* GR, const cplx* C, cplx* out, Dims d) {
     cplx acc = mk(0, 0);
     for (int n2 = -d.nG + lane; n2 < d.nG; n2 += 32) {
         const int s = nu - n2;  // in [-(2nG-1), 2nG-1]
-        acc = cfma(GR[ixG(d, R, n2)], C[(size_t)R * NS + (s + d.NG - 1)], acc);
+        const size_t ig = ixG(d, R, n2), ic = (size_t)R * NS + (s + d.NG - 1);
+        acc = TAN ? cfma(tGR[ig], C[ic], cfma(GR[ig], tC[ic], acc)) : cfma(GR[ig], C[ic], acc);
     }
     acc = warp_sum(acc);
     if (lane == 0) out[w] = acc * (d.U * d.U * d.T * d.T);
@@ -1034,44 +1139,55 @@ int bubble_tile(const Dims& d) {
     while (tv > 1 && (size_t)4 * tv * NR * sizeof(cplx) > 160 * 1024) tv >>= 1;
     return tv;
 }
-template <int L>
-static cudaError_t launch_bubble_fft(cudaStream_t s, const cplx* GR, cplx* pp, cplx* ph, const Dims& d) {
+template <int L, bool TAN>
+static cudaError_t launch_bubble_fft(cudaStream_t s, const cplx* GR, const cplx* tGR, cplx* pp, cplx* ph,
+                                     const Dims& d) {
     constexpr int BS = L * (L + 1) + 1;
     int tv = 32;
     while (tv > 1 && (size_t)2 * tv * BS * sizeof(cplx) > 80 * 1024) tv >>= 1;
     const size_t shm = (size_t)2 * tv * BS * sizeof(cplx);
     static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
     if (shm > 48 * 1024 && shm > shm_set) {
-        cudaFuncSetAttribute(k_bubble_fft<L, cplx, cplx>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bubble_fft<L, cplx, cplx, TAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         shm_set = shm;
     }
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
-    k_bubble_fft<L, cplx, cplx><<<grid, 256, shm, s>>>(GR, pp, ph, d, tv);
+    k_bubble_fft<L, cplx, cplx, TAN><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, d, tv);
     return cudaGetLastError();
 }
 // FP32 form (mixed map) from the FP32 copy of G(R); its tile fits the default 48 KB of shared memory
-template <int L>
-static cudaError_t launch_bubble_fft_f32(cudaStream_t s, const cplxf* GR, cplx* pp, cplx* ph, const Dims& d) {
+template <int L, bool TAN>
+static cudaError_t launch_bubble_fft_f32(cudaStream_t s, const cplxf* GR, const cplxf* tGR, cplx* pp, cplx* ph,
+                                         const Dims& d) {
     constexpr int BS = L * (L + 1) + 1;
     int tv = 32;
     while (tv > 1 && (size_t)2 * tv * BS * sizeof(cplxf) > 48 * 1024) tv >>= 1;
     const size_t shm = (size_t)2 * tv * BS * sizeof(cplxf);
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
-    k_bubble_fft<L, cplxf, cplxf><<<grid, 256, shm, s>>>(GR, pp, ph, d, tv);
+    k_bubble_fft<L, cplxf, cplxf, TAN><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, d, tv);
     return cudaGetLastError();
 }
 bool bubble_f32_supported(const Dims& d) {
     return !d.local && (d.L == 2 || d.L == 4 || d.L == 8 || d.L == 16 || d.L == 32);
 }
-cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const Dims& d) {
+template <bool TAN>
+static cudaError_t bubble_f32_t(cudaStream_t s, const cplxf* GRf, const cplxf* tGRf, cplx* pp, cplx* ph,
+                                const Dims& d) {
     switch (d.L) {
-        case 2: return launch_bubble_fft_f32<2>(s, GRf, pp, ph, d);
-        case 4: return launch_bubble_fft_f32<4>(s, GRf, pp, ph, d);
-        case 8: return launch_bubble_fft_f32<8>(s, GRf, pp, ph, d);
-        case 16: return launch_bubble_fft_f32<16>(s, GRf, pp, ph, d);
-        case 32: return launch_bubble_fft_f32<32>(s, GRf, pp, ph, d);
+        case 2: return launch_bubble_fft_f32<2, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 4: return launch_bubble_fft_f32<4, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 8: return launch_bubble_fft_f32<8, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 16: return launch_bubble_fft_f32<16, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 32: return launch_bubble_fft_f32<32, TAN>(s, GRf, tGRf, pp, ph, d);
         default: return cudaErrorInvalidValue;
     }
+}
+cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const Dims& d) {
+    return bubble_f32_t<false>(s, GRf, nullptr, pp, ph, d);
+}
+cudaError_t launch_bubble_f32_tan(cudaStream_t s, const cplxf* GRf, const cplxf* tGRf, cplx* tpp, cplx* tph,
+                                  const Dims& d) {
+    return bubble_f32_t<true>(s, GRf, tGRf, tpp, tph, d);
 }
 
 cudaError_t set_fft_twiddles() {
@@ -1086,31 +1202,40 @@ cudaError_t set_fft_twiddles() {
     return e;
 }
 
-cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
-                          const Dims& d) {
+template <bool TAN>
+static cudaError_t bubble_t(cudaStream_t s, const cplx* G, const cplx* tG, const cplx* GR, const cplx* tGR, cplx* pp,
+                            cplx* ph, const cplx* twp, const Dims& d) {
     if (d.local) {
         const size_t n = (size_t)d.NPO * d.NPw;
-        k_bubble_local<<<blocks_for(n, 256), 256, 0, s>>>(G, pp, ph, d);
+        k_bubble_local<TAN><<<blocks_for(n, 256), 256, 0, s>>>(G, tG, pp, ph, d);
         LAUNCH_CHECK(); return cudaSuccess;
     }
     switch (d.L) {
-        case 2: return launch_bubble_fft<2>(s, GR, pp, ph, d);
-        case 4: return launch_bubble_fft<4>(s, GR, pp, ph, d);
-        case 8: return launch_bubble_fft<8>(s, GR, pp, ph, d);
-        case 16: return launch_bubble_fft<16>(s, GR, pp, ph, d);
-        case 32: return launch_bubble_fft<32>(s, GR, pp, ph, d);
+        case 2: return launch_bubble_fft<2, TAN>(s, GR, tGR, pp, ph, d);
+        case 4: return launch_bubble_fft<4, TAN>(s, GR, tGR, pp, ph, d);
+        case 8: return launch_bubble_fft<8, TAN>(s, GR, tGR, pp, ph, d);
+        case 16: return launch_bubble_fft<16, TAN>(s, GR, tGR, pp, ph, d);
+        case 32: return launch_bubble_fft<32, TAN>(s, GR, tGR, pp, ph, d);
         default: break;
     }
     const int tv = bubble_tile(d);
     const size_t shm = (size_t)4 * tv * d.L * d.L * sizeof(cplx);
     static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
     if (shm > 48 * 1024 && shm > shm_set) {
-        cudaFuncSetAttribute(k_bubble_nl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bubble_nl<TAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         shm_set = shm;
     }
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
-    k_bubble_nl<<<grid, 256, shm, s>>>(GR, pp, ph, twp, d, tv);
+    k_bubble_nl<TAN><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, twp, d, tv);
     LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
+                          const Dims& d) {
+    return bubble_t<false>(s, G, nullptr, GR, nullptr, pp, ph, twp, d);
+}
+cudaError_t launch_bubble_tan(cudaStream_t s, const cplx* G, const cplx* tG, const cplx* GR, const cplx* tGR,
+                              cplx* tpp, cplx* tph, const cplx* twp, const Dims& d) {
+    return bubble_t<true>(s, G, tG, GR, tGR, tpp, tph, twp, d);
 }
 
 template <int L>
@@ -1159,8 +1284,9 @@ cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const 
         LAUNCH_CHECK(); return cudaSuccess;
     }
     const int NR = d.L * d.L;
-    if (GRf) k_pisum_R<cplxf, cplxf><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GRf, T0, SRtmp, d);
-    else k_pisum_R<cplx, cplx><<<blocks_for((size_t)2 * d.NPO * NR * 32, 128), 128, 0, s>>>(GR, T0, SRtmp, d);
+    const unsigned nb = blocks_for((size_t)2 * d.NPO * NR * 32, 128);
+    if (GRf) k_pisum_R<cplxf, cplxf, false><<<nb, 128, 0, s>>>(GRf, nullptr, T0, SRtmp, d);
+    else k_pisum_R<cplx, cplx, false><<<nb, 128, 0, s>>>(GR, nullptr, T0, SRtmp, d);
     LAUNCH_CHECK();
     // S^w[P][Ω] = Σ_R e^{+2πi P·R/L} SR[w][R][Ω]
     cudaError_t e = launch_fft2(s, SRtmp, S0, d.NPO, +1, 1.0, twp, d);
@@ -1272,17 +1398,67 @@ cudaError_t launch_sde_sigma(cudaStream_t s, const cplx* GR, const cplx* Lpp, co
     cudaError_t e = launch_fft2(s, Lpp, LR, rows, -1, invN, twm, d);
     if (e == cudaSuccess) e = launch_fft2(s, Lph, LR + (size_t)NR * rows, rows, -1, invN, twm, d);
     if (e != cudaSuccess) return e;
-    k_sde_sigma_R<<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(GR, LR, LR + (size_t)NR * rows, SR, d);
+    k_sde_sigma_R<false><<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(GR, LR, LR + (size_t)NR * rows, nullptr,
+                                                                                 nullptr, nullptr, SR, d);
     LAUNCH_CHECK();
     return launch_fft2(s, SR, S, d.NG, +1, d.T, twp, d);
 }
+cudaError_t launch_sde_sigma_tan(cudaStream_t s, const cplx* GR, const cplx* LR, const cplx* tGR, const cplx* tLpp,
+                                 const cplx* tLph, cplx* tLR, cplx* tSR, cplx* tS, const cplx* twm, const cplx* twp,
+                                 const Dims& d) {
+    const int rows = d.N2O * d.N2n, NR = d.L * d.L;
+    const double invN = 1.0 / NR;
+    cudaError_t e = launch_fft2(s, tLpp, tLR, rows, -1, invN, twm, d);
+    if (e == cudaSuccess) e = launch_fft2(s, tLph, tLR + (size_t)NR * rows, rows, -1, invN, twm, d);
+    if (e != cudaSuccess) return e;
+    k_sde_sigma_R<true><<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(
+        GR, LR, LR + (size_t)NR * rows, tGR, tLR, tLR + (size_t)NR * rows, tSR, d);
+    LAUNCH_CHECK();
+    return launch_fft2(s, tSR, tS, d.NG, +1, d.T, twp, d);
+}
 cudaError_t launch_u2(cudaStream_t s, const cplx* GR, cplx* C, cplx* SR, cplx* out, const cplx* twc, const Dims& d) {
     const int NR = d.L * d.L, NS = 2 * d.NG - 1;
-    k_u2_corr<<<blocks_for((size_t)NR * NS * 32, 128), 128, 0, s>>>(GR, C, d);
+    k_u2_corr<false><<<blocks_for((size_t)NR * NS * 32, 128), 128, 0, s>>>(GR, nullptr, C, d);
     LAUNCH_CHECK();
-    k_u2_sum<<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(GR, C, SR, d);
+    k_u2_sum<false><<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(GR, C, nullptr, nullptr, SR, d);
     LAUNCH_CHECK();
     return launch_fft2(s, SR, out, d.NG, +1, 1.0, twc, d);
+}
+cudaError_t launch_u2_tan(cudaStream_t s, const cplx* GR, const cplx* C, const cplx* tGR, cplx* tC, cplx* tSR,
+                          cplx* tout, const cplx* twc, const Dims& d) {
+    const int NR = d.L * d.L, NS = 2 * d.NG - 1;
+    k_u2_corr<true><<<blocks_for((size_t)NR * NS * 32, 128), 128, 0, s>>>(GR, tGR, tC, d);
+    LAUNCH_CHECK();
+    k_u2_sum<true><<<blocks_for((size_t)NR * d.NG * 32, 128), 128, 0, s>>>(GR, C, tGR, tC, tSR, d);
+    LAUNCH_CHECK();
+    return launch_fft2(s, tSR, tout, d.NG, +1, 1.0, twc, d);
+}
+cudaError_t launch_dyson_tan(cudaStream_t s, cplx* tG, const cplx* G, const cplx* tSig, size_t n) {
+    k_dyson_tan<<<blocks_for(n, 256), 256, 0, s>>>(tG, G, tSig, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_sx_tan(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* tPipp, const cplx* tPiph,
+                          const cplx* tSPi, const FLP& FL, const FLP& tFL, cplx* tSX, const Dims& d) {
+    const size_t n = (size_t)3 * d.Nq * d.NPO * 32;
+    k_sx_tan<<<blocks_for(n, 128), 128, 0, s>>>(Pipp, Piph, tPipp, tPiph, tSPi, FL, tFL, tSX, d);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_rowsum_tan(cudaStream_t s, const cplx* tA0, const cplx* tA1, const cplx* GR, const cplx* tGR,
+                              cplx* SRtmp, const cplx* twp, cplx* tS0, cplx* tS1, const Dims& d, const cplxf* GRf,
+                              const cplxf* tGRf) {
+    if (d.nPw == d.nPn) {  // the full mesh is stored: the row sums are linear in Π
+        dim3 grid((unsigned)(d.Nq * d.NPO), 2);
+        k_rowsum<<<grid, 256, 0, s>>>(tA0, tA1, tS0, tS1, d.NPw);
+        LAUNCH_CHECK(); return cudaSuccess;
+    }
+    const int NR = d.L * d.L;
+    const unsigned nb = blocks_for((size_t)2 * d.NPO * NR * 32, 128);
+    if (GRf) k_pisum_R<cplxf, cplxf, true><<<nb, 128, 0, s>>>(GRf, tGRf, nullptr, SRtmp, d);
+    else k_pisum_R<cplx, cplx, true><<<nb, 128, 0, s>>>(GR, tGR, nullptr, SRtmp, d);
+    LAUNCH_CHECK();
+    cudaError_t e = launch_fft2(s, SRtmp, tS0, d.NPO, +1, 1.0, twp, d);
+    if (e != cudaSuccess) return e;
+    return launch_fft2(s, SRtmp + (size_t)NR * d.NPO, tS1, d.NPO, +1, 1.0, twp, d);
 }
 cudaError_t launch_sigma_assemble(cudaStream_t s, const cplx* Sin, const cplx* SU2, const uint32_t* map,
                                   const double* occ, const cplx* C0, const cplx* Sig0, cplx* Sig, double U, int hartree,

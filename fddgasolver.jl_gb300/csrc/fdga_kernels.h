@@ -38,7 +38,10 @@ struct K3Args {
     const cplx* FLt;  // FL.γt.K3
     const cplx* FLa;  // FL.γa.K3
     cplx* out;
+    int flags;        // K3F_* (product-rule terms of the tangent map)
 };
+// K3Args flags: accumulate into out; leave the γL(ν,ν') epilogue term out; Pi0 == nullptr reads zero
+enum { K3F_ACC = 1, K3F_NOEPI = 2 };
 
 struct K3ArgsF {  // FP32 operands of the mixed map (the FP32 caches and FL.K3 copy)
     const cplxf* A;
@@ -50,6 +53,7 @@ struct K3ArgsF {  // FP32 operands of the mixed map (the FP32 caches and FL.K3 c
     const cplxf* FLt;
     const cplxf* FLa;
     cplx* out;
+    int flags;
 };
 struct K3Args3F {
     K3ArgsF a[3];
@@ -68,6 +72,7 @@ struct ChanWork {  // per-channel work of an all-channel launch, indexed by chan
     const int* items[3];  // representative device indices (nullptr: item = index)
     int nitems[3];
     cplx* out[3];
+    int acc;  // 1: out += value (product-rule terms of the tangent map)
 };
 struct BubbleP {
     const cplx* pp;
@@ -219,5 +224,22 @@ cudaError_t launch_kr_resid(cudaStream_t s, int nblk, const cplx* b, const cplxf
                             const cplx* yb, double beta, cplx* r, size_t n);
 cudaError_t launch_kr_axpby(cudaStream_t s, int nblk, cplx* out, const cplx* a, double lam, const cplx* b, size_t n);
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count);
+// tangent (forward-mode derivative) stages of the iteration map; the value intermediates (G, G(R),
+// Π, L(R), C of the U² term) of the same base point are inputs
+cudaError_t launch_dyson_tan(cudaStream_t s, cplx* tG, const cplx* G, const cplx* tSig, size_t n);
+cudaError_t launch_bubble_tan(cudaStream_t s, const cplx* G, const cplx* tG, const cplx* GR, const cplx* tGR,
+                              cplx* tpp, cplx* tph, const cplx* twp, const Dims& d);
+cudaError_t launch_bubble_f32_tan(cudaStream_t s, const cplxf* GRf, const cplxf* tGRf, cplx* tpp, cplx* tph,
+                                  const Dims& d);
+cudaError_t launch_rowsum_tan(cudaStream_t s, const cplx* tA0, const cplx* tA1, const cplx* GR, const cplx* tGR,
+                              cplx* SRtmp, const cplx* twp, cplx* tS0, cplx* tS1, const Dims& d,
+                              const cplxf* GRf = nullptr, const cplxf* tGRf = nullptr);
+cudaError_t launch_sx_tan(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* tPipp, const cplx* tPiph,
+                          const cplx* tSPi, const FLP& FL, const FLP& tFL, cplx* tSX, const Dims& d);
+cudaError_t launch_sde_sigma_tan(cudaStream_t s, const cplx* GR, const cplx* LR, const cplx* tGR, const cplx* tLpp,
+                                 const cplx* tLph, cplx* tLR, cplx* tSR, cplx* tS, const cplx* twm, const cplx* twp,
+                                 const Dims& d);
+cudaError_t launch_u2_tan(cudaStream_t s, const cplx* GR, const cplx* C, const cplx* tGR, cplx* tC, cplx* tSR,
+                          cplx* tout, const cplx* twc, const Dims& d);
 
 }  // namespace fdga

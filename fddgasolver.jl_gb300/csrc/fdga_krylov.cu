@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(RT) k_kc_point(const cplx* x, const cplxf* v, 
                                                  cplx* xp, size_t n) {
     for (size_t j = blockIdx.x * (size_t)RT + threadIdx.x; j < n; j += (size_t)gridDim.x * RT) {
         const uint32_t c = code[j];
-        xp[j] = x[j] + apply_op((int)(c & 3u), to_d(v[c >> 2])) * eps;
+        const cplx e = apply_op((int)(c & 3u), to_d(v[c >> 2])) * eps;
+        xp[j] = x ? x[j] + e : e;
     }
 }
 // out[j] = x[j] + λ op_j(d[code_j])   (d compact FP64)

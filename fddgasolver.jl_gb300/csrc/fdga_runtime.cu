@@ -108,6 +108,19 @@ struct fdga_handle {
     int groups_version = 0, kc_version = -1;
     std::vector<cplx*> ma_buf64;   // mixed solver: defect, g, g_old
     std::vector<cplxf*> ma_buf32;  // mixed solver: f, Δf, Q, Δg (FP32 history)
+    // Tangent map (forward-mode derivative of one iteration): direction x, result y (state layout)
+    // and the tangent intermediates; the value intermediates of the base point are the ones above.
+    struct Tangent {
+        cplx *x = nullptr, *y = nullptr, *avg = nullptr, *G = nullptr, *GR = nullptr;
+        cplx *Pipp = nullptr, *Piph = nullptr, *SPi = nullptr, *SX = nullptr;
+        cplx *cache = nullptr;  // 7 caches (Γpx Γpp Γa Γt Fp Fa Ft): the RefVertex caches have no tangent
+        cplx *FLK2 = nullptr, *FLK3 = nullptr, *Lpp = nullptr, *Lph = nullptr, *LR = nullptr, *SR = nullptr;
+        cplx *SigIn = nullptr, *u2C = nullptr, *u2R = nullptr, *SigU2 = nullptr;
+        double* occ = nullptr;
+        cplxf *cachef = nullptr, *FLK2f = nullptr, *FLK3f = nullptr, *xSf = nullptr, *ySf = nullptr;
+        cplxf *avgf = nullptr, *GRf = nullptr;  // FP32 forms (tangent of the mixed map)
+        Graph graphs[2][2][2][2];               // [precision][strategy][update_sigma][hartree]
+    } tan;
     std::vector<void*> allocs;
 };
 
@@ -381,7 +394,7 @@ int upload_group(fdga_handle* h, Group& g, const HostGroup& hg) {
 // averages and RefVertex corrections
 template <class S>
 VertPT<S> vertex_view_t(const fdga_handle* h, S* st, S* avg, S* const* fref) {
-    VertPT<S> F;
+    VertPT<S> F{};
     for (int c = 0; c < 3; ++c) {
         S* base = st + (size_t)c * h->nchan;
         F.g[c].K1 = base;
@@ -661,6 +674,321 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     return FDGA_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Tangent map (forward-mode derivative, the frule of one iteration): ty = Φ'(x) tx at the base
+// point x whose value intermediates (G, G(R), Π, SΠ, caches, FL, S_X, L(R), the U² correlator) the
+// last enqueue_iteration of the same precision left in the handle.  The map is a composition of
+// vertex-linear stages (momentum averages, caches, left BSEs, symmetrisation and recombination)
+// and of products (the bubble G·G, the BSEs F·Π·(F, FL), the SDE G·L and G·G·G); the tangent
+// applies the product rule stage by stage:
+//   * vertex-linear stages run on the tangent vertex with the RefVertex terms off (it is constant);
+//   * dG = -G² dΣ; dΠ and dSΠ from the product-rule bubble kernels (the 1/ν tails are constant);
+//   * each bilinear BSE runs once per factor with the other factors at their values (Π0 and the
+//     RefVertex caches are constant), accumulating: dK = K(dF, Π, FL) + K(F, dΠ, FL) + K(F, Π, dFL);
+//   * dΣ from dL = L(dF, Π) + L(F, dΠ), and the product-rule Σ_R and U² kernels.
+// ---------------------------------------------------------------------------------------------
+int ensure_tangent(fdga_handle* h) {
+    auto& t = h->tan;
+    const Dims& d = h->d;
+    const bool mixed = h->precision == FDGA_MIXED;
+    if (!t.x) {
+        AL(t.x, h->nstate); AL(t.y, h->nstate);
+        if (h->navg) AL(t.avg, h->navg);
+        AL(t.G, h->nGk); AL(t.GR, h->nGk);
+        AL(t.Pipp, h->nPi); AL(t.Piph, h->nPi);
+        AL(t.SPi, 2 * (size_t)d.Nq * d.NPO); AL(t.SX, 3 * (size_t)d.Nq * d.NPO);
+        AL(t.FLK2, 3 * h->n2); AL(t.FLK3, 3 * h->n3);
+        AL(t.Lpp, h->n2); AL(t.Lph, h->n2); AL(t.LR, 2 * h->n2); AL(t.SR, h->nGk);
+        AL(t.SigIn, h->nGk); AL(t.u2C, (size_t)d.Nq * (2 * d.NG - 1)); AL(t.u2R, h->nGk); AL(t.SigU2, h->nGk);
+        AL(t.occ, 1);
+    }
+    if (!mixed && !t.cache) AL(t.cache, 7 * h->n3);
+    if (mixed && !t.cachef) {
+        int r = ensure_mixed(h);
+        if (r) return r;
+        AL(t.cachef, 7 * h->n3);
+        AL(t.FLK2f, 3 * h->n2); AL(t.FLK3f, 3 * h->n3);
+        AL(t.xSf, 3 * h->nchan); AL(t.ySf, 3 * h->nchan);
+        if (h->navg) AL(t.avgf, h->navg);
+        AL(t.GRf, h->nGk);
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return FDGA_OK;
+}
+
+int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartree, int& nl) {
+    cudaStream_t s = h->st;
+    const Dims& d = h->d;
+    auto& t = h->tan;
+    nl = 0;
+    const bool mixed = h->precision == FDGA_MIXED;
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    VertP F = vertex_view(h, h->xS), Fn = vertex_view(h, h->yS);
+    VertP tF = vertex_view_t<cplx>(h, t.x, t.avg, h->Fref), tFn = vertex_view_t<cplx>(h, t.y, t.avg, h->Fref);
+    tF.noref = tFn.noref = 1;
+    if (d.Nq > 1) {
+        ChanArrays in;
+        ChanArraysW out;
+        for (int c = 0; c < 3; ++c) {
+            in.K1[c] = tF.g[c].K1; in.K2[c] = tF.g[c].K2; in.K3[c] = tF.g[c].K3;
+            out.K1[c] = (cplx*)tF.g[c].A1; out.K2[c] = (cplx*)tF.g[c].A2; out.K3[c] = (cplx*)tF.g[c].A3;
+        }
+        LC(launch_qavg(s, in, out, d));
+    }
+    if (update_sigma) {
+        LC(launch_dyson_tan(s, t.G, h->G, sigmaOf(h, t.x), h->nGk));
+        LC(launch_g_realspace(s, t.G, t.GR, h->twm, d));
+        if (mixed && bubble_f32_supported(d)) {
+            LC(launch_to_f32(s, t.GR, t.GRf, h->nGk));
+            LC(launch_bubble_f32_tan(s, h->GRf, t.GRf, t.Pipp, t.Piph, d));
+            LC(launch_rowsum_tan(s, t.Pipp, t.Piph, h->GR, t.GR, h->SRtmp, h->twp, t.SPi, t.SPi + nS, d, h->GRf,
+                                 t.GRf));
+        } else {
+            LC(launch_bubble_tan(s, h->G, t.G, h->GR, t.GR, t.Pipp, t.Piph, h->twp, d));
+            LC(launch_rowsum_tan(s, t.Pipp, t.Piph, h->GR, t.GR, h->SRtmp, h->twp, t.SPi, t.SPi + nS, d));
+        }
+    } else {  // G and Π are held fixed
+        LC(cudaMemsetAsync(t.Pipp, 0, h->nPi * sizeof(cplx), s));
+        LC(cudaMemsetAsync(t.Piph, 0, h->nPi * sizeof(cplx), s));
+        LC(cudaMemsetAsync(t.SPi, 0, 2 * nS * sizeof(cplx), s));
+    }
+    // FP32 mirrors of the tangent vertex (mixed map); the value mirrors are the value pass's
+    VertPF Ff{}, Fnf{}, tFf{}, tFnf{};
+    FLPF FLf{}, tFLf{};
+    if (mixed) {
+        LC(launch_to_f32(s, t.x, t.xSf, 3 * h->nchan));
+        if (d.Nq > 1) LC(launch_to_f32(s, t.avg, t.avgf, h->navg));
+        Ff = vertex_view_t<cplxf>(h, h->xSf, h->avgf, h->Freff);
+        Fnf = vertex_view_t<cplxf>(h, h->ySf, h->avgf, h->Freff);
+        tFf = vertex_view_t<cplxf>(h, t.xSf, t.avgf, h->Freff);
+        tFnf = vertex_view_t<cplxf>(h, t.ySf, t.avgf, h->Freff);
+        tFf.noref = tFnf.noref = 1;
+        for (int c = 0; c < 3; ++c) {
+            FLf.K2[c] = h->FLK2f + (size_t)c * h->n2;
+            tFLf.K2[c] = t.FLK2f + (size_t)c * h->n2;
+        }
+    }
+    // caches of the tangent vertex (slot -1: a RefVertex cache, constant)
+    static const int slot[10] = {0, -1, -1, -1, 1, 2, 3, 4, 5, 6};
+    Caches C{}, tC{};
+    for (int i = 0; i < 10; ++i) {
+        C.c[i] = h->cache + (size_t)i * h->n3;
+        C.f[i] = mixed ? h->cachef + (size_t)i * h->n3 : nullptr;
+        tC.c[i] = (slot[i] < 0 || mixed) ? nullptr : t.cache + (size_t)slot[i] * h->n3;
+        tC.f[i] = (slot[i] < 0 || !mixed) ? nullptr : t.cachef + (size_t)slot[i] * h->n3;
+    }
+    if (mixed) LC(launch_build_cache(s, tFf, tC, h->d_k3blocks, h->nk3blocks, d));
+    else LC(launch_build_cache(s, tF, tC, h->d_k3blocks, h->nk3blocks, d));
+    FLP FL, tFL;
+    for (int c = 0; c < 3; ++c) {
+        FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
+        tFL.K2[c] = t.FLK2 + (size_t)c * h->n2;
+    }
+    const int order[3] = {CH_P, CH_A, CH_T};
+    auto Pi = [&](int ch) -> const cplx* { return ch == CH_P ? h->Pipp : h->Piph; };
+    auto tPi = [&](int ch) -> const cplx* { return ch == CH_P ? t.Pipp : t.Piph; };
+    auto Pi0 = [&](int ch) -> const cplx* { return ch == CH_P ? h->Pi0pp : h->Pi0ph; };
+    const BubbleP B{h->Pipp, h->Piph, h->Pi0pp, h->Pi0ph};
+    const BubbleP tB{t.Pipp, t.Piph, nullptr, nullptr};   // dΠ, with Π0 read as zero
+    const BubbleP B0{h->Pipp, h->Piph, h->Pipp, h->Piph};  // Π with Π - Π0 read as zero
+    auto work = [&](int cls, cplx* raw, int acc) {
+        ChanWork cw{};
+        const size_t n = cls == 1 ? h->n1 : h->n2;
+        for (int ch = 0; ch < 3; ++ch) {
+            const Group& g = cls == 1 ? h->gK1 : k2group(h, ch);
+            cw.items[ch] = g.trivial ? nullptr : g.d_items;
+            cw.nitems[ch] = g.trivial ? (int)n : g.nitems;
+            cw.out[ch] = raw + (size_t)ch * n;
+        }
+        cw.acc = acc;
+        return cw;
+    };
+    auto fin = [&](int cls, cplx* raw, cplx* const out[3], const Group* const grp[3]) {
+        Finalize3 f{};
+        const size_t n = cls == 1 ? h->n1 : (cls == 2 ? h->n2 : h->n3);
+        for (int ch = 0; ch < 3; ++ch) {
+            f.raw[ch] = raw + (size_t)ch * n;
+            f.out[ch] = out[ch];
+            f.map[ch] = grp[ch]->trivial ? nullptr : grp[ch]->d_map;
+            f.FL[ch] = t.FLK2 + (size_t)ch * h->n2;
+        }
+        return f;
+    };
+    // K3 contraction launch in the precision of the map
+    auto k3 = [&](int mode, const K3Args3& a3, const K3Args3F& a3f) -> cudaError_t {
+        if (mixed && h->k3_tc && k3_tc_supported(d)) return launch_bse_K3_tc(s, mode, a3f, 3, d, h->d_err);
+        if (mixed) return launch_bse_K3_f32(s, mode, a3f, 3, d, h->k3_tile[FDGA_MIXED][mode]);
+        return launch_bse_K3(s, mode, a3, 3, d, 0, h->k3_tile[FDGA_FP64][mode]);
+    };
+    if (strategy == FDGA_FDPA) {
+        {  // dFL.K2 = L_K2(dF)  (Π0 constant)
+            ChanWork cw = work(2, h->raw2, 0);
+            if (mixed) LC(launch_bse_L_K2_all(s, tFf, B, cw, d));
+            else LC(launch_bse_L_K2_all(s, tF, B, cw, d));
+            cplx* out[3] = {t.FLK2, t.FLK2 + h->n2, t.FLK2 + 2 * h->n2};
+            const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
+            Finalize3 f2 = fin(2, h->raw2, out, grp);
+            if (mixed)
+                for (int c = 0; c < 3; ++c) f2.outf[c] = t.FLK2f + (size_t)c * h->n2;
+            LC(launch_finalize3(s, f2, 0, 1, h->n2));
+        }
+        {  // dFL.K3 = L_K3(dΓ)  (Π0 and the RefVertex caches constant)
+            K3Args3 a3{};
+            K3Args3F a3f{};
+            for (int i = 0; i < 3; ++i) {
+                const int ch = order[i];
+                const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+                K3Args& a = a3.a[i];
+                a.A = tC.c[cg]; a.B0 = C.c[cf0]; a.Pi0 = Pi0(ch);
+                a.out = h->raw3 + (size_t)ch * h->n3;
+                a3.ch[i] = a3f.ch[i] = ch;
+                K3ArgsF& af = a3f.a[i];
+                af.A = tC.f[cg]; af.B0 = C.f[cf0]; af.Pi0 = Pi0(ch);
+                af.out = a.out;
+            }
+            a3.blocks = a3f.blocks = h->d_k3blocks;
+            a3.nblocks = a3f.nblocks = h->nk3blocks;
+            LC(k3(0, a3, a3f));
+            cplx* out[3] = {t.FLK3, t.FLK3 + h->n3, t.FLK3 + 2 * h->n3};
+            const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
+            Finalize3 f3 = fin(3, h->raw3, out, grp);
+            if (mixed)
+                for (int c = 0; c < 3; ++c) f3.outf[c] = t.FLK3f + (size_t)c * h->n3;
+            LC(launch_finalize3(s, f3, 0, 1, h->n3));
+        }
+    } else {  // scPA: FL is not iterated
+        LC(cudaMemsetAsync(t.FLK2, 0, 3 * h->n2 * sizeof(cplx), s));
+        LC(cudaMemsetAsync(t.FLK3, 0, 3 * h->n3 * sizeof(cplx), s));
+        if (mixed) {
+            LC(cudaMemsetAsync(t.FLK2f, 0, 3 * h->n2 * sizeof(cplxf), s));
+            LC(cudaMemsetAsync(t.FLK3f, 0, 3 * h->n3 * sizeof(cplxf), s));
+        }
+    }
+    LC(launch_sx_tan(s, h->Pipp, h->Piph, t.Pipp, t.Piph, t.SPi, FL, tFL, t.SX, d));
+    {  // dK1 = K1(dF; Π, FL, S_X) + K1(F; dΠ, FL, dS_X) + K1(F; Π, dFL)
+        if (mixed) {
+            LC(launch_bse_K1_all(s, tFf, FLf, B, h->SX, work(1, h->raw1, 0), d));
+            LC(launch_bse_K1_all(s, Ff, FLf, tB, t.SX, work(1, h->raw1, 1), d));
+            LC(launch_bse_K1_all(s, Ff, tFLf, B0, nullptr, work(1, h->raw1, 1), d));
+        } else {
+            LC(launch_bse_K1_all(s, tF, FL, B, h->SX, work(1, h->raw1, 0), d));
+            LC(launch_bse_K1_all(s, F, FL, tB, t.SX, work(1, h->raw1, 1), d));
+            LC(launch_bse_K1_all(s, F, tFL, B0, nullptr, work(1, h->raw1, 1), d));
+        }
+        cplx* out[3] = {chanK(h, t.y, CH_P, 1), chanK(h, t.y, CH_T, 1), chanK(h, t.y, CH_A, 1)};
+        const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
+        LC(launch_finalize3(s, fin(1, h->raw1, out, grp), 0, 1, h->n1));
+    }
+    {  // dK2, the same three terms, then the FL epilogue with dFL.K2
+        if (mixed) {
+            LC(launch_bse_K2_all(s, tFf, FLf, B, h->SX, work(2, h->raw2, 0), d));
+            LC(launch_bse_K2_all(s, Ff, FLf, tB, t.SX, work(2, h->raw2, 1), d));
+            LC(launch_bse_K2_all(s, Ff, tFLf, B0, nullptr, work(2, h->raw2, 1), d));
+        } else {
+            LC(launch_bse_K2_all(s, tF, FL, B, h->SX, work(2, h->raw2, 0), d));
+            LC(launch_bse_K2_all(s, F, FL, tB, t.SX, work(2, h->raw2, 1), d));
+            LC(launch_bse_K2_all(s, F, tFL, B0, nullptr, work(2, h->raw2, 1), d));
+        }
+        cplx* out[3] = {chanK(h, t.y, CH_P, 2), chanK(h, t.y, CH_T, 2), chanK(h, t.y, CH_A, 2)};
+        const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
+        LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 1, 1, h->n2));
+    }
+    {  // dK3 = T dF·M + T F·M(dΠ) + T F·M(dΓ, dFL) + dγL
+        for (int term = 0; term < 3; ++term) {
+            K3Args3 a3{};
+            K3Args3F a3f{};
+            for (int i = 0; i < 3; ++i) {
+                const int ch = order[i];
+                const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
+                const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+                const cplx* fl = (term == 2 ? t.FLK3 : h->FLK3);
+                const cplxf* flf = (term == 2 ? t.FLK3f : h->FLK3f);
+                K3Args& a = a3.a[i];
+                K3ArgsF& af = a3f.a[i];
+                a.A = term == 0 ? tC.c[cf] : C.c[cf];
+                af.A = term == 0 ? tC.f[cf] : C.f[cf];
+                a.B0 = C.c[cf0]; af.B0 = C.f[cf0];
+                a.G = term == 2 ? tC.c[cg] : C.c[cg];
+                af.G = term == 2 ? tC.f[cg] : C.f[cg];
+                a.Pi = af.Pi = term == 1 ? tPi(ch) : Pi(ch);
+                a.Pi0 = af.Pi0 = term == 0 ? Pi0(ch) : (term == 1 ? nullptr : Pi(ch));
+                a.FLc = fl + (size_t)ch * h->n3; a.FLt = fl + (size_t)CH_T * h->n3; a.FLa = fl + (size_t)CH_A * h->n3;
+                if (mixed) {
+                    af.FLc = flf + (size_t)ch * h->n3; af.FLt = flf + (size_t)CH_T * h->n3;
+                    af.FLa = flf + (size_t)CH_A * h->n3;
+                }
+                a.out = af.out = h->raw3 + (size_t)ch * h->n3;
+                a.flags = af.flags = (term == 2 ? 0 : K3F_NOEPI) | (term > 0 ? K3F_ACC : 0);
+                a3.ch[i] = a3f.ch[i] = ch;
+            }
+            a3.blocks = a3f.blocks = h->d_k3blocks;
+            a3.nblocks = a3f.nblocks = h->nk3blocks;
+            LC(k3(1, a3, a3f));
+        }
+        cplx* out[3] = {chanK(h, t.y, CH_P, 3), chanK(h, t.y, CH_T, 3), chanK(h, t.y, CH_A, 3)};
+        const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
+        LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
+    }
+    cplx* tSig = sigmaOf(h, t.y);
+    if (update_sigma) {
+        const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
+        ChanWork cw{};
+        const Group* g[2] = {&h->gK2pp, &h->gK2ph};
+        for (int w = 0; w < 2; ++w) {
+            cw.items[w] = g[w]->trivial ? nullptr : g[w]->d_items;
+            cw.nitems[w] = g[w]->trivial ? (int)h->n2 : g[w]->nitems;
+            cw.out[w] = h->raw2 + (size_t)w * h->n2;
+        }
+        // dL = L(dF; Π, SΠ) + L(F; dΠ, dSΠ) (+ the RefVertex part with dΠ)
+        ChanWork cw1 = cw;
+        cw1.acc = 1;
+        if (mixed) {
+            LC(launch_to_f32(s, t.y, t.ySf, 3 * h->nchan));
+            LC(launch_sde_L_all(s, tFnf, B, h->SPi, h->SPi + nS, cw, 1, 0.0, d));
+            LC(launch_sde_L_all(s, Fnf, tB, t.SPi, t.SPi + nS, cw1, 1, rs, d));
+        } else {
+            LC(launch_sde_L_all(s, tFn, B, h->SPi, h->SPi + nS, cw, 1, 0.0, d));
+            LC(launch_sde_L_all(s, Fn, tB, t.SPi, t.SPi + nS, cw1, 1, rs, d));
+        }
+        Finalize3 f{};
+        f.raw[0] = h->raw2; f.out[0] = t.Lpp; f.map[0] = g[0]->trivial ? nullptr : g[0]->d_map;
+        f.raw[2] = h->raw2 + h->n2; f.out[2] = t.Lph; f.map[2] = g[1]->trivial ? nullptr : g[1]->d_map;
+        LC(launch_finalize3(s, f, 0, 0, h->n2));
+        LC(launch_sde_sigma_tan(s, h->GR, h->LR, t.GR, t.Lpp, t.Lph, t.LR, t.SR, t.SigIn, h->twm, h->twp, d));
+        nl += 3;
+        LC(launch_u2_tan(s, h->GR, h->u2C, t.GR, t.u2C, t.u2R, t.SigU2, h->twp, d));
+        nl += 2;
+        LC(launch_occupation(s, t.G, h->nGk, d.T, d.Nk, t.occ));  // 1/2 + dn: the Hartree term reads dn
+        LC(launch_sigma_assemble(s, t.SigIn, t.SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, t.occ, nullptr,
+                                 nullptr, tSig, d.U, hartree ? 1 : 0, 0, 0.0, h->nGk));
+    } else {
+        LC(cudaMemcpyAsync(tSig, sigmaOf(h, t.x), h->nGk * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    }
+    return FDGA_OK;
+}
+
+int run_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
+    int r = ensure_tangent(h);
+    if (r) return r;
+    Graph& g = h->tan.graphs[h->precision][strategy][update_sigma][hartree];
+    if (!g.exec) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        int nl = 0;
+        r = enqueue_tangent(h, strategy, update_sigma, hartree, nl);
+        cudaError_t ee = cudaStreamEndCapture(h->st, &graph);
+        if (r) return r;
+        if (ee != cudaSuccess) return cuda_fail(h, ee, "cudaStreamEndCapture");
+        ee = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ee != cudaSuccess) { g.exec = nullptr; return cuda_fail(h, ee, "cudaGraphInstantiate"); }
+        g.nodes = nl;
+    }
+    CK(cudaGraphLaunch(g.exec, h->st));
+    h->last_launches = g.nodes;
+    return FDGA_OK;
+}
+
 // Constant reference-system part of the fdPA SDE: C0 = SDE(F0, G0, Π0) without Hartree.
 int compute_C0(fdga_handle* h) {
     cudaStream_t s = h->st;
@@ -685,11 +1013,12 @@ int compute_C0(fdga_handle* h) {
 }
 
 void drop_graphs(fdga_handle* h) {
-    for (auto& p : h->graphs)
-        for (auto& a : p)
-            for (auto& b : a)
-                for (auto& g : b)
-                    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    for (auto* gs : {&h->graphs, &h->tan.graphs})
+        for (auto& p : *gs)
+            for (auto& a : p)
+                for (auto& b : a)
+                    for (auto& g : b)
+                        if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
 }
 
 int run_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
@@ -1563,6 +1892,31 @@ int fdga_jvp(fdga_handle* h, int strategy, const double* v, double* Jv, size_t n
     return FDGA_OK;
 }
 
+int fdga_frule(fdga_handle* h, int strategy, int update_sigma, int compute_hartree, const double* v, double* y,
+               double* Jv, size_t n) {
+    if (!h || !v || !Jv) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
+    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA) return fail(h, FDGA_ERR_ARG, "unknown strategy");
+    int r = ensure_tangent(h);
+    if (r) return r;
+    // value pass at x (leaves the intermediates of the base point in the handle), then the tangent
+    if ((r = run_iteration(h, strategy, update_sigma != 0, compute_hartree != 0))) return r;
+    CK(cudaMemcpyAsync(h->tmpS, v, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
+    CK(launch_scatter(h->st, h->tan.x, h->tmpS, h->perm, n));  // reference layout -> device layout
+    if ((r = run_tangent(h, strategy, update_sigma != 0, compute_hartree != 0))) return r;
+    if ((r = check_device_error(h))) return r;
+    CK(launch_gather(h->st, h->tmpS, h->tan.y, h->perm, n));
+    CK(cudaMemcpyAsync(Jv, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (y) {
+        CK(launch_gather(h->st, h->tmpS, h->yS, h->perm, n));
+        CK(cudaMemcpyAsync(y, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
+    return FDGA_OK;
+}
+
 int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int restart, int jvp_precision,
                       int* iters, double* res, double* trace, int* evals) {
     if (!h) return FDGA_ERR_ARG;
@@ -1896,6 +2250,16 @@ int fdga_map_repeat(fdga_handle* h, int strategy, int n) {
     if (!h || n < 0) return FDGA_ERR_ARG;
     for (int i = 0; i < n; ++i) {
         int r = run_iteration(h, strategy, true, true);
+        if (r) return r;
+    }
+    return FDGA_OK;
+}
+
+int fdga_tangent_repeat(fdga_handle* h, int strategy, int n) {
+    if (!h || n < 0) return FDGA_ERR_ARG;
+    if (!h->tan.x) return fail(h, FDGA_ERR_STATE, "fdga_frule has not been called");
+    for (int i = 0; i < n; ++i) {
+        int r = run_tangent(h, strategy, true, true);
         if (r) return r;
     }
     return FDGA_OK;

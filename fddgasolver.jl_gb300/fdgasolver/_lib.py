@@ -49,6 +49,8 @@ EXPORTS = {
                                          ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
                                          ctypes.c_void_p, ctypes.c_void_p]),
     "fdga_jvp": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "fdga_frule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_set_U": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdga_dchi_dU": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t,
@@ -71,6 +73,7 @@ EXPORTS = {
     "fdga_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
                                         ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "fdga_map_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "fdga_tangent_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "fdga_flush_l2": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "fdga_host_free": (ctypes.c_int, [ctypes.c_void_p]),

@@ -171,6 +171,17 @@ class _Solver:
         self._check(self._lib.fdga_jvp(self._h, STRATEGIES[strategy], v.ctypes.data, out.ctypes.data, v.size))
         return out
 
+    def frule(self, v, strategy="fdPA", update_sigma=True, compute_hartree=True):
+        """(Φ(x), Φ'(x)·v) at the current state x from the tangent kernels (forward mode, no finite
+        differences), the frule of one fixed_point! iteration; v in the flatten layout."""
+        v = np.ascontiguousarray(v, dtype=np.complex128)
+        y = np.empty_like(v)
+        jv = np.empty_like(v)
+        self._check(self._lib.fdga_frule(self._h, STRATEGIES[strategy], int(bool(update_sigma)),
+                                         int(bool(compute_hartree)), v.ctypes.data, y.ctypes.data,
+                                         jv.ctypes.data, v.size))
+        return y, jv
+
     def set_U(self, U):
         self._check(self._lib.fdga_set_U(self._h, float(U)))
 
@@ -251,6 +262,10 @@ class _Solver:
     def map_repeat(self, n, strategy="fdPA"):
         """Apply the iteration map n times to the unchanged device state (no host sync)."""
         self._check(self._lib.fdga_map_repeat(self._h, STRATEGIES[strategy], int(n)))
+
+    def tangent_repeat(self, n, strategy="fdPA"):
+        """Apply the tangent map n times at the base point and direction of the last frule call."""
+        self._check(self._lib.fdga_tangent_repeat(self._h, STRATEGIES[strategy], int(n)))
 
     def flush_l2(self, nbytes=256 << 20):
         """Overwrite the L2 with a device buffer write on the solver's stream."""

@@ -149,6 +149,16 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
  * host arrays in the flatten(S) layout; J is real-linear (v and i·v give unrelated products). */
 int fdga_jvp(fdga_handle* h, int strategy, const double* v, double* Jv, size_t n);
 
+/* Forward-mode derivative of one iteration (the frule of fixed_point!, src/solve.jl:4-116 and
+ * src/ParquetSolver.jl:277-306): at the current state S = x, y = Φ(x) and Jv = Φ'(x)·v, the
+ * derivative computed by the hand-written tangent kernels (product rule through Dyson, the
+ * bubbles, the caches, the K1/K2/K3 BSEs and the SDE; no finite differences), in the handle's
+ * precision.  update_sigma and compute_hartree select the map as in fdga_iterate.  v, y and Jv
+ * are host arrays in the flatten(S) layout (y may be NULL); S is left unchanged.  J is
+ * real-linear. */
+int fdga_frule(fdga_handle* h, int strategy, int update_sigma, int compute_hartree, const double* v, double* y,
+               double* Jv, size_t n);
+
 /* Bare interaction U of the handle (the RefVertex's bare part, the SDE and Hartree terms); the
  * reference builds a new solver for another U.  Drops the captured graphs. */
 int fdga_set_U(fdga_handle* h, double U);
@@ -220,6 +230,9 @@ int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t
 /* Applies the iteration map n times to the unchanged device state x (graph replays, no host
  * synchronisation): the device-resident timing loop of the benchmark. */
 int fdga_map_repeat(fdga_handle* h, int strategy, int n);
+/* Applies the tangent map n times (graph replays, no host synchronisation) at the base point and
+ * direction of the last fdga_frule call (full map): the timing loop of the derivative. */
+int fdga_tangent_repeat(fdga_handle* h, int strategy, int n);
 /* Writes `bytes` of a device buffer on the handle's stream, evicting the L2 between timed
  * iterations of a benchmark (the buffer is allocated on first use). */
 int fdga_flush_l2(fdga_handle* h, size_t bytes);
