@@ -11,6 +11,9 @@
 // FP32 caches); each is split into TF32 hi + lo and the product accumulates hi·hi + hi·lo + lo·hi
 // (kind::tf32, FP32 accumulation in tensor memory), which keeps FP32-level accuracy.
 //
+// Mode 2 (the tangent of the K3 BSE, dC = dA·M + A·dM) is one GEMM over the concatenated inner
+// index: the chunks first stage (dA, M), then (A, dM), into the same accumulator.
+//
 // One CTA of 512 threads per block: rows ν < N of the 128-lane accumulator, 2N ≤ 256 columns.
 // K runs in chunks of 16 ω (32 real k); two shared-memory stages; the threads stage chunk c+1
 // while the tensor core works on chunk c (tcgen05.commit -> mbarrier).  Shared-memory operands use
@@ -67,6 +70,16 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     }
     return false;
 }
+// γL at a K3 index: FL.γ_ch (a, p) or 2 FL.γt − FL.γa (t, density component)
+__device__ __forceinline__ cplxf fl_box(const cplxf* FLc, const cplxf* FLt, const cplxf* FLa, int ch, size_t i) {
+    if (ch == CH_T) {
+        const float2 qt = __ldg(reinterpret_cast<const float2*>(FLt + i));
+        const float2 qa = __ldg(reinterpret_cast<const float2*>(FLa + i));
+        return cplxf{2.f * qt.x - qa.x, 2.f * qt.y - qa.y};
+    }
+    const float2 qc = __ldg(reinterpret_cast<const float2*>(FLc + i));
+    return cplxf{qc.x, qc.y};
+}
 __device__ __forceinline__ void mma_tf32(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
@@ -80,10 +93,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
-    __shared__ float pis[16][4];  // Π(ω), Π0(ω) of the chunk (re, im, re, im)
+    __shared__ float pis[16][6];  // Π(ω), Π0(ω), dΠ(ω) of the chunk (re, im pairs)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = d.N3n, NN = 2 * N;
     const int nchunks = (N + 15) / 16;
+    const int nck = (MODE == 2 ? 2 : 1) * nchunks;  // mode 2: (dA, M) chunks, then (A, dM) chunks
     const int nb = args.nblocks;
     const int slot = blockIdx.x / nb;
     const int blk = args.blocks ? args.blocks[blockIdx.x % nb] : (int)(blockIdx.x % nb);
@@ -111,24 +125,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
     const uint32_t tmem = tmem_base;
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NN >> 3) << 17) | ((128u >> 4) << 24);
     bool ok = true;
-    for (int c = 0; c < nchunks; ++c) {
+    for (int c = 0; c < nck; ++c) {
         const int st = c & 1;
+        const bool tM = (MODE == 2 && c >= nchunks);
+        const cplxf* Ap = (MODE == 2 && !tM) ? a.tA : a.A;
         if (c >= 2 && !mbar_wait(smem_u32(&mbar[st]), ((c - 2) >> 1) & 1)) ok = false;
         uint8_t* Ahi = sm + (size_t)st * STAGE;
         uint8_t* Alo = Ahi + A_BYTES;
         uint8_t* Bhi = Alo + A_BYTES;
         uint8_t* Blo = Bhi + B_BYTES;
-        const int w0 = 16 * c;
+        const int w0 = 16 * (tM ? c - nchunks : c);
         if (tid < 16) {
             const int w = w0 + tid;
-            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (w < N) {
                 const size_t ip = ixPi(d, P, m, w - d.n3n);
                 const cplx p0 = a.Pi0 ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
                 v[2] = (float)p0.x; v[3] = (float)p0.y;
-                if (MODE == 1) { const cplx p = ldg(a.Pi + ip); v[0] = (float)p.x; v[1] = (float)p.y; }
+                if (MODE >= 1) { const cplx p = ldg(a.Pi + ip); v[0] = (float)p.x; v[1] = (float)p.y; }
+                if (tM) { const cplx p = ldg(a.tPi + ip); v[4] = (float)p.x; v[5] = (float)p.y; }
             }
-            for (int j = 0; j < 4; ++j) pis[tid][j] = v[j];
+            for (int j = 0; j < 6; ++j) pis[tid][j] = v[j];
         }
         __syncthreads();
         // A: (ω pair j, row ν) items, rows fastest so that a quarter warp's 16-byte stores fall in
@@ -137,10 +154,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
             const int nu = e & 127, j = e >> 7, w = w0 + 2 * j;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (nu < N && w < N) {
-                const float2 q0 = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w));
+                const float2 q0 = __ldg(reinterpret_cast<const float2*>(Ap + base + (size_t)nu * N + w));
                 v.x = q0.x; v.y = q0.y;
                 if (w + 1 < N) {
-                    const float2 q1 = __ldg(reinterpret_cast<const float2*>(a.A + base + (size_t)nu * N + w + 1));
+                    const float2 q1 = __ldg(reinterpret_cast<const float2*>(Ap + base + (size_t)nu * N + w + 1));
                     v.z = q1.x; v.w = q1.y;
                 }
             }
@@ -166,20 +183,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
                         const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
                         const float2 qg = __ldg(reinterpret_cast<const float2*>(a.G + ig));
                         const cplxf gs{qg.x, qg.y};
-                        M = ((pi - pi0) * f0 + pi * gs) * s1;
                         const int ot = cross(CH, m, w - d.n3n);
-                        if (fin(ot, d.n3n)) {
-                            const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                            cplxf gl;
-                            if (CH == CH_T) {
-                                const float2 qt = __ldg(reinterpret_cast<const float2*>(a.FLt + il));
-                                const float2 qa = __ldg(reinterpret_cast<const float2*>(a.FLa + il));
-                                gl = cplxf{2.f * qt.x - qa.x, 2.f * qt.y - qa.y};
-                            } else {
-                                const float2 qc = __ldg(reinterpret_cast<const float2*>(a.FLc + il));
-                                gl = cplxf{qc.x, qc.y};
-                            }
-                            M += pi * gl * s2;
+                        const size_t il = base + (size_t)(ot + d.n3n) * N + col;
+                        if (!tM) {
+                            M = ((pi - pi0) * f0 + pi * gs) * s1;
+                            if (fin(ot, d.n3n)) M += pi * fl_box(a.FLc, a.FLt, a.FLa, CH, il) * s2;
+                        } else {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL]
+                            const cplxf tpi{pis[t][4], pis[t][5]};
+                            const float2 qt = __ldg(reinterpret_cast<const float2*>(a.tG + ig));
+                            M = (tpi * (f0 + gs) + pi * cplxf{qt.x, qt.y}) * s1;
+                            if (fin(ot, d.n3n))
+                                M += (tpi * fl_box(a.FLc, a.FLt, a.FLa, CH, il) +
+                                      pi * fl_box(a.tFLc, a.tFLt, a.tFLa, CH, il)) * s2;
                         }
                     }
                 }
@@ -207,8 +222,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
         __syncthreads();
     }
     // the last chunk of each stage
-    if (nchunks >= 2 && !mbar_wait(smem_u32(&mbar[nchunks & 1]), ((nchunks - 2) >> 1) & 1)) ok = false;
-    if (!mbar_wait(smem_u32(&mbar[(nchunks - 1) & 1]), ((nchunks - 1) >> 1) & 1)) ok = false;
+    if (nck >= 2 && !mbar_wait(smem_u32(&mbar[nck & 1]), ((nck - 2) >> 1) & 1)) ok = false;
+    if (!mbar_wait(smem_u32(&mbar[(nck - 1) & 1]), ((nck - 1) >> 1) & 1)) ok = false;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
@@ -241,11 +256,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
                         o = to_d(v * (Tf * sgn));
                     } else if (a.flags & K3F_NOEPI) {
                         o = to_d(v * Tf);
+                    } else if (MODE == 1) {
+                        o = to_d(v * Tf + fl_box(a.FLc, a.FLt, a.FLa, CH, io));
                     } else {
-                        cplxf gl;
-                        if (CH == CH_T) gl = cplxf{2.f * a.FLt[io].x - a.FLa[io].x, 2.f * a.FLt[io].y - a.FLa[io].y};
-                        else gl = a.FLc[io];
-                        o = to_d(v * Tf + gl);
+                        o = to_d(v * Tf + fl_box(a.tFLc, a.tFLt, a.tFLa, CH, io));
                     }
                     a.out[io] = (a.flags & K3F_ACC) ? a.out[io] + o : o;
                 }
@@ -275,6 +289,8 @@ cudaError_t prepare_bse_K3_tc(const Dims& d) {
     cudaError_t e = cudaFuncSetAttribute(k_bse_K3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_bse_K3_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_bse_K3_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) smem_set = smem;
     return e;
 }
@@ -283,7 +299,8 @@ cudaError_t launch_bse_K3_tc(cudaStream_t s, int mode, const K3Args3F& a, int ns
     if (!k3_tc_supported(d)) return cudaErrorInvalidValue;
     const size_t smem = k3_tc_smem(d);
     const unsigned grid = (unsigned)(nslots * a.nblocks);
-    if (mode) k_bse_K3_tc<1><<<grid, TC_THREADS, smem, s>>>(a, d, err);
+    if (mode == 2) k_bse_K3_tc<2><<<grid, TC_THREADS, smem, s>>>(a, d, err);
+    else if (mode) k_bse_K3_tc<1><<<grid, TC_THREADS, smem, s>>>(a, d, err);
     else k_bse_K3_tc<0><<<grid, TC_THREADS, smem, s>>>(a, d, err);
     return cudaGetLastError();
 }

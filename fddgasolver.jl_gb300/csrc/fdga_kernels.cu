@@ -605,10 +605,12 @@ __global__ void k_sx_tan(const cplx* Pipp, const cplx* Piph, const cplx* tPipp, 
 // F(Ω,∞,ω) depends on ω only through the same channel's K2(Ω, ω) (ω in the K2 box), so the sum is
 // evaluated exactly as c·S_X + Σ_{ω ∈ K2 box} (F(Ω,∞,ω) - c) X(ω), c = F(Ω,∞,∞).
 // ---------------------------------------------------------------------------------------------
-template <int CH, class S>
+// TAN: the tangent dK1 = K1(dF; Π, FL, S_X) + K1(F; dΠ, dFL, dS_X) in one pass (T: the tangent
+// factors; dX = dΠ (FL + U) + Π dFL).
+template <int CH, class S, bool TAN>
 __device__ __forceinline__ void bse_K1_body(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
                                             const cplx* SX, cplx* out, const int* items, int nitems, int accum,
-                                            const Dims& d) {
+                                            const Dims& d, const TanArgsT<S>& T) {
     using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
@@ -616,6 +618,9 @@ __device__ __forceinline__ void bse_K1_body(const VertPT<S>& F, const FLPT<S>& F
     const int m = idx % d.N1 - (d.n1 - 1), P = idx / d.N1;
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     const S c = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    S tc{0, 0};
+    if constexpr (TAN) tc = vert_eval(T.F, d, CH, SP, m, FINF, FINF, P);
+    const cplx* tPi = (CH == CH_P) ? T.pp : T.ph;
     S acc{0, 0};
     if (bin(m, d.n2O)) {
         for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
@@ -625,13 +630,25 @@ __device__ __forceinline__ void bse_K1_body(const VertPT<S>& F, const FLPT<S>& F
             const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
             const size_t ip = ixPi(d, P, m, n);
             const S pi = to_c<S>(ldg(Pi + ip)), pi0 = Pi0 ? to_c<S>(ldg(Pi0 + ip)) : S{0, 0};
-            acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
+            if constexpr (!TAN) {
+                acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
+            } else {
+                const S X = cfma(pi, FLr, (pi - pi0) * (R)d.U);
+                const S tFl = vert_eval(T.F, d, CH, SP, m, FINF, n, P) - tc;
+                const S tFLr = fl_right(T.FL.K2[CH_P], T.FL.K2[CH_T], T.FL.K2[CH_A], d, CH, m, wt, P);
+                const S tpi = to_c<S>(ldg(tPi + ip));
+                const S tX = cfma(tpi, FLr + cre<S>(d.U), pi * tFLr);
+                acc = cfma(tFl, X, cfma(Fl, tX, acc));
+            }
         }
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-        const S sx = SX ? to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]) : S{0, 0};
-        const cplx v = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+        const size_t is = (size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1);
+        const S sx = SX ? to_c<S>(SX[is]) : S{0, 0};
+        S r = c * sx + acc;
+        if constexpr (TAN) r = cfma(tc, sx, c * to_c<S>(T.SX[is])) + acc;
+        const cplx v = to_d(r * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
         out[idx] = accum ? out[idx] + v : v;
     }
 }
@@ -678,10 +695,11 @@ __device__ __forceinline__ void bse_L_K2_body(const VertPT<S>& F, const cplx* Pi
 // ω-independent value c = F(Ω,ν,∞) - F(Ω,∞,∞); the sum is evaluated exactly as
 // c·S_X + Σ_{ω ∈ union} (F(Ω,ν,ω) - F(Ω,∞,ω) - c) X(ω).
 // ---------------------------------------------------------------------------------------------
-template <int CH, class S>
+// TAN: the tangent in one pass, as for K1.
+template <int CH, class S, bool TAN>
 __device__ __forceinline__ void bse_K2_body(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
                                             const cplx* SX, cplx* out, const int* items, int nitems, int accum,
-                                            const Dims& d) {
+                                            const Dims& d, const TanArgsT<S>& T) {
     using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
@@ -693,6 +711,12 @@ __device__ __forceinline__ void bse_K2_body(const VertPT<S>& F, const FLPT<S>& F
     // F(Ω,∞,ω) equals F(Ω,∞,∞) (bit for bit) unless ω is in the K2 box
     const S cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
     const S c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
+    S tcinf{0, 0}, tc{0, 0};
+    if constexpr (TAN) {
+        tcinf = vert_eval(T.F, d, CH, SP, m, FINF, FINF, P);
+        tc = vert_eval(T.F, d, CH, SP, m, nu, FINF, P) - tcinf;
+    }
+    const cplx* tPi = (CH == CH_P) ? T.pp : T.ph;
     Windows win;
     const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
     win.add(-d.n2n, d.n2n - 1, lo, hi);
@@ -710,12 +734,25 @@ __device__ __forceinline__ void bse_K2_body(const VertPT<S>& F, const FLPT<S>& F
         const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
         const S pi = to_c<S>(ldg(Pi + ip)), pi0 = Pi0 ? to_c<S>(ldg(Pi0 + ip)) : S{0, 0};
-        acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
+        if constexpr (!TAN) {
+            acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
+        } else {
+            const S X = cfma(pi, FLr, (pi - pi0) * (R)d.U);
+            const S tFinf = fin(n, d.n2n) ? vert_eval(T.F, d, CH, SP, m, FINF, n, P) : tcinf;
+            const S tFl = vert_eval(T.F, d, CH, SP, m, nu, n, P) - tFinf - tc;
+            const S tFLr = fl_right(T.FL.K2[CH_P], T.FL.K2[CH_T], T.FL.K2[CH_A], d, CH, m, wt, P);
+            const S tpi = to_c<S>(ldg(tPi + ip));
+            const S tX = cfma(tpi, FLr + cre<S>(d.U), pi * tFLr);
+            acc = cfma(tFl, X, cfma(Fl, tX, acc));
+        }
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-        const S sx = SX ? to_c<S>(SX[(size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1)]) : S{0, 0};
-        const cplx v = to_d((c * sx + acc) * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+        const size_t is = (size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1);
+        const S sx = SX ? to_c<S>(SX[is]) : S{0, 0};
+        S r = c * sx + acc;
+        if constexpr (TAN) r = cfma(tc, sx, c * to_c<S>(T.SX[is])) + acc;
+        const cplx v = to_d(r * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
         out[idx] = accum ? out[idx] + v : v;
     }
 }
@@ -760,50 +797,69 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
     const size_t base = (size_t)blk * N * N;
     const double s1 = (CH == CH_A) ? 1.0 : -1.0, s2 = (CH == CH_T) ? -1.0 : 1.0;
     C acc[2][2] = {{czero<C>(), czero<C>()}, {czero<C>(), czero<C>()}};
-    for (int k0 = 0; k0 < N; k0 += TK) {
-        for (int e = tid; e < TILE * TK; e += NT) {
-            const int r = e / TK, kk = e % TK;
-            const int row = row0 + r, k = k0 + kk;
-            As[r][kk] = (row < N && k < N) ? ldk<C>(a.A + base + (size_t)row * N + k) : czero<C>();
-        }
-        for (int e = tid; e < TK * TILE; e += NT) {
-            const int kk = e / TILE, c = e % TILE;
-            const int k = k0 + kk, col = col0 + c;
-            C v = czero<C>();
-            if (k < N && col < N) {
-                const int o = k - d.n3n;  // ω as fermion index
-                const size_t ip = ixPi(d, P, m, o);
-                const C pi0 = a.Pi0 ? to_c<C>(ldg(a.Pi0 + ip)) : czero<C>();
-                const C f0 = ldk<C>(a.B0 + base + (size_t)k * N + col);
-                if (MODE == 0) {
-                    v = pi0 * f0;
-                } else {
-                    const C pi = to_c<C>(ldg(a.Pi + ip));
-                    const C gs = (CH == CH_P) ? ldk<C>(a.G + base + (size_t)k * N + col)
-                                              : ldk<C>(a.G + base + (size_t)col * N + k);
-                    v = ((pi - pi0) * f0 + pi * gs) * (R)s1;
-                    const int ot = cross(CH, m, o);
-                    if (fin(ot, d.n3n)) {
+    // MODE 2 (tangent): the inner index runs twice, first over (dA, M), then over (A, dM)
+    constexpr int NH = (MODE == 2) ? 2 : 1;
+    for (int half = 0; half < NH; ++half) {
+        const auto* Ap = (MODE == 2 && half == 0) ? a.tA : a.A;
+        const bool tM = (MODE == 2 && half == 1);
+        for (int k0 = 0; k0 < N; k0 += TK) {
+            for (int e = tid; e < TILE * TK; e += NT) {
+                const int r = e / TK, kk = e % TK;
+                const int row = row0 + r, k = k0 + kk;
+                As[r][kk] = (row < N && k < N) ? ldk<C>(Ap + base + (size_t)row * N + k) : czero<C>();
+            }
+            for (int e = tid; e < TK * TILE; e += NT) {
+                const int kk = e / TILE, c = e % TILE;
+                const int k = k0 + kk, col = col0 + c;
+                C v = czero<C>();
+                if (k < N && col < N) {
+                    const int o = k - d.n3n;  // ω as fermion index
+                    const size_t ip = ixPi(d, P, m, o);
+                    const C pi0 = a.Pi0 ? to_c<C>(ldg(a.Pi0 + ip)) : czero<C>();
+                    const C f0 = ldk<C>(a.B0 + base + (size_t)k * N + col);
+                    if (MODE == 0) {
+                        v = pi0 * f0;
+                    } else {
+                        const C pi = to_c<C>(ldg(a.Pi + ip));
+                        const size_t ig = (CH == CH_P) ? base + (size_t)k * N + col : base + (size_t)col * N + k;
+                        const C gs = ldk<C>(a.G + ig);
+                        const int ot = cross(CH, m, o);
                         const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                        const C gl = (CH == CH_T) ? ldk<C>(a.FLt + il) * (R)2 - ldk<C>(a.FLa + il)
-                                                  : ldk<C>(a.FLc + il);
-                        v += pi * gl * (R)s2;
+                        if (!tM) {
+                            v = ((pi - pi0) * f0 + pi * gs) * (R)s1;
+                            if (fin(ot, d.n3n)) {
+                                const C gl = (CH == CH_T) ? ldk<C>(a.FLt + il) * (R)2 - ldk<C>(a.FLa + il)
+                                                          : ldk<C>(a.FLc + il);
+                                v += pi * gl * (R)s2;
+                            }
+                        } else {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL]
+                            const C tpi = to_c<C>(ldg(a.tPi + ip));
+                            const C tgs = ldk<C>(a.tG + ig);
+                            v = cfma(tpi, f0 + gs, pi * tgs) * (R)s1;
+                            if (fin(ot, d.n3n)) {
+                                const C gl = (CH == CH_T) ? ldk<C>(a.FLt + il) * (R)2 - ldk<C>(a.FLa + il)
+                                                          : ldk<C>(a.FLc + il);
+                                const C tgl = (CH == CH_T) ? ldk<C>(a.tFLt + il) * (R)2 - ldk<C>(a.tFLa + il)
+                                                           : ldk<C>(a.tFLc + il);
+                                v += cfma(tpi, gl, pi * tgl) * (R)s2;
+                            }
+                        }
                     }
                 }
+                Ms[kk][c] = v;
             }
-            Ms[kk][c] = v;
-        }
-        __syncthreads();
+            __syncthreads();
 #pragma unroll
-        for (int kk = 0; kk < TK; ++kk) {
-            const C a0 = As[ty][kk], a1 = As[ty + H][kk];
-            const C b0 = Ms[kk][tx], b1 = Ms[kk][tx + H];
-            acc[0][0] = cfma(a0, b0, acc[0][0]);
-            acc[0][1] = cfma(a0, b1, acc[0][1]);
-            acc[1][0] = cfma(a1, b0, acc[1][0]);
-            acc[1][1] = cfma(a1, b1, acc[1][1]);
+            for (int kk = 0; kk < TK; ++kk) {
+                const C a0 = As[ty][kk], a1 = As[ty + H][kk];
+                const C b0 = Ms[kk][tx], b1 = Ms[kk][tx + H];
+                acc[0][0] = cfma(a0, b0, acc[0][0]);
+                acc[0][1] = cfma(a0, b1, acc[0][1]);
+                acc[1][0] = cfma(a1, b0, acc[1][0]);
+                acc[1][1] = cfma(a1, b1, acc[1][1]);
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -818,9 +874,12 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
                 v = to_d(acc[i][j] * (R)(d.T * ((CH == CH_A) ? 1.0 : -1.0)));
             } else if (a.flags & K3F_NOEPI) {
                 v = to_d(acc[i][j] * (R)d.T);
-            } else {
+            } else if (MODE == 1) {
                 const C gl = (CH == CH_T) ? ldk<C>(a.FLt + io) * (R)2 - ldk<C>(a.FLa + io) : ldk<C>(a.FLc + io);
                 v = to_d(acc[i][j] * (R)d.T + gl);
+            } else {
+                const C tgl = (CH == CH_T) ? ldk<C>(a.tFLt + io) * (R)2 - ldk<C>(a.tFLa + io) : ldk<C>(a.tFLc + io);
+                v = to_d(acc[i][j] * (R)d.T + tgl);
             }
             a.out[io] = (a.flags & K3F_ACC) ? a.out[io] + v : v;
         }
@@ -836,10 +895,11 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
 // box; elsewhere it equals c = γ(…, ν, ∞), so the vertex sum is c·SΠ + Σ_{window} Π (γ - c).
 // out = T [vertex part] + T ref_scale [RefVertex part].
 // ---------------------------------------------------------------------------------------------
-template <int WHICH, class S>
+// TAN: dL = L(dF; Π, SΠ) + L(F; dΠ, dSΠ) + ref_scale·RefVertex part with dΠ, in one pass.
+template <int WHICH, class S, bool TAN>
 __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, const cplx* SPi, cplx* out,
                                            const int* items, int nitems, int use_vertex, double ref_scale, int accum,
-                                           const Dims& d) {
+                                           const Dims& d, const TanArgsT<S>& T) {
     using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
@@ -847,22 +907,37 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
     const int nu = idx % d.N2n - d.n2n;
     const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
     const int P = idx / (d.N2n * d.N2O);
-    S acc{0, 0}, accr{0, 0}, c{0, 0};
+    const cplx* tPi = WHICH == 0 ? T.pp : T.ph;
+    S acc{0, 0}, accr{0, 0}, c{0, 0}, tc{0, 0};
     if (use_vertex) {
         if (WHICH == 0) {
             c = chan_eval(F.g[CH_P], d, m, FINF, nu, P);
+            if constexpr (TAN) tc = chan_eval(T.F.g[CH_P], d, m, FINF, nu, P);
             for (int t = lane; t < d.N2n; t += 32) {
                 const int n = m - (t - d.n2n) - 1;  // Ω-ω runs over the K2 box
                 if (!fin(n, d.nPw)) continue;
                 const S g = chan_eval(F.g[CH_P], d, m, m - n - 1, nu, P) - c;
-                acc = cfma(to_c<S>(ldg(Pi + ixPi(d, P, m, n))), g, acc);
+                const size_t ip = ixPi(d, P, m, n);
+                if constexpr (!TAN) {
+                    acc = cfma(to_c<S>(ldg(Pi + ip)), g, acc);
+                } else {
+                    const S tg = chan_eval(T.F.g[CH_P], d, m, m - n - 1, nu, P) - tc;
+                    acc = cfma(to_c<S>(ldg(tPi + ip)), g, cfma(to_c<S>(ldg(Pi + ip)), tg, acc));
+                }
             }
         } else {
             c = chan_eval(F.g[CH_T], d, m, nu, FINF, P) + chan_eval(F.g[CH_A], d, m, nu, FINF, P);
+            if constexpr (TAN) tc = chan_eval(T.F.g[CH_T], d, m, nu, FINF, P) + chan_eval(T.F.g[CH_A], d, m, nu, FINF, P);
             for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
                 if (!fin(n, d.nPw)) continue;
                 const S g = chan_eval(F.g[CH_T], d, m, nu, n, P) + chan_eval(F.g[CH_A], d, m, nu, n, P) - c;
-                acc = cfma(to_c<S>(ldg(Pi + ixPi(d, P, m, n))), g, acc);
+                const size_t ip = ixPi(d, P, m, n);
+                if constexpr (!TAN) {
+                    acc = cfma(to_c<S>(ldg(Pi + ip)), g, acc);
+                } else {
+                    const S tg = chan_eval(T.F.g[CH_T], d, m, nu, n, P) + chan_eval(T.F.g[CH_A], d, m, nu, n, P) - tc;
+                    acc = cfma(to_c<S>(ldg(tPi + ip)), g, cfma(to_c<S>(ldg(Pi + ip)), tg, acc));
+                }
             }
         }
     }
@@ -874,13 +949,21 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
             S g;
             if (WHICH == 0) g = ref_pSp(F, d, CH_P, m, m - n - 1, nu) - cre<S>(d.U);
             else g = ref_pSp(F, d, CH_A, m, nu, n) + ref_pSp(F, d, CH_T, m, nu, n) - cre<S>(d.U) - cre<S>(d.U);
-            accr = cfma(to_c<S>(ldg(Pi + ixPi(d, P, m, n))), g, accr);
+            accr = cfma(to_c<S>(ldg((TAN ? tPi : Pi) + ixPi(d, P, m, n))), g, accr);
         }
     }
     acc = warp_sum(acc) * (R)d.U;
     accr = warp_sum(accr) * (R)d.U;
     if (lane == 0) {
-        if (use_vertex) acc += c * (to_c<S>(ldg(SPi + (size_t)P * d.NPO + (m + d.nPO - 1))) * (R)d.U);
+        const size_t is = (size_t)P * d.NPO + (m + d.nPO - 1);
+        if (use_vertex) {
+            if constexpr (!TAN) {
+                acc += c * (to_c<S>(ldg(SPi + is)) * (R)d.U);
+            } else {
+                const S tsp = to_c<S>(ldg((WHICH == 0 ? T.SPpp : T.SPph) + is));
+                acc += cfma(tc, to_c<S>(ldg(SPi + is)), c * tsp) * (R)d.U;
+            }
+        }
         const cplx v = to_d(acc * (R)d.T + accr * (R)(d.T * ref_scale));
         out[idx] = accum ? out[idx] + v : v;
     }
@@ -889,12 +972,13 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
 // ---------------------------------------------------------------------------------------------
 // All-channel launches: blockIdx.y selects the channel (0 = p, 1 = t, 2 = a; SDE: 0 = pp, 1 = ph).
 // ---------------------------------------------------------------------------------------------
-template <class S>
-__global__ void k_bse_K1_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
+template <class S, bool TAN>
+__global__ void k_bse_K1_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d,
+                             TanArgsT<S> T) {
     switch (blockIdx.y) {
-        case CH_P: bse_K1_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d); break;
-        case CH_T: bse_K1_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d); break;
-        default:   bse_K1_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d); break;
+        case CH_P: bse_K1_body<CH_P, S, TAN>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d, T); break;
+        case CH_T: bse_K1_body<CH_T, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d, T); break;
+        default:   bse_K1_body<CH_A, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d, T); break;
     }
 }
 template <class S>
@@ -905,20 +989,21 @@ __global__ void k_bse_L_K2_all(VertPT<S> F, BubbleP B, ChanWork cw, Dims d) {
         default:   bse_L_K2_body<CH_A>(F, B.ph0, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
-template <class S>
-__global__ void k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d) {
+template <class S, bool TAN>
+__global__ void k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d,
+                             TanArgsT<S> T) {
     switch (blockIdx.y) {
-        case CH_P: bse_K2_body<CH_P>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d); break;
-        case CH_T: bse_K2_body<CH_T>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d); break;
-        default:   bse_K2_body<CH_A>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d); break;
+        case CH_P: bse_K2_body<CH_P, S, TAN>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d, T); break;
+        case CH_T: bse_K2_body<CH_T, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d, T); break;
+        default:   bse_K2_body<CH_A, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d, T); break;
     }
 }
-template <class S>
+template <class S, bool TAN>
 __global__ void k_sde_L_all(VertPT<S> F, BubbleP B, const cplx* SPpp, const cplx* SPph, ChanWork cw, int use_vertex,
-                            double ref_scale, Dims d) {
+                            double ref_scale, Dims d, TanArgsT<S> T) {
     if (blockIdx.y == 0)
-        sde_L_body<0>(F, B.pp, SPpp, cw.out[0], cw.items[0], cw.nitems[0], use_vertex, ref_scale, cw.acc, d);
-    else sde_L_body<1>(F, B.ph, SPph, cw.out[1], cw.items[1], cw.nitems[1], use_vertex, ref_scale, cw.acc, d);
+        sde_L_body<0, S, TAN>(F, B.pp, SPpp, cw.out[0], cw.items[0], cw.nitems[0], use_vertex, ref_scale, cw.acc, d, T);
+    else sde_L_body<1, S, TAN>(F, B.ph, SPph, cw.out[1], cw.items[1], cw.nitems[1], use_vertex, ref_scale, cw.acc, d, T);
 }
 
 // Finalize of one vertex class for the three channels (out-of-place from the representative
@@ -1328,10 +1413,10 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
     for (int c = 0; c < nch; ++c) mx = std::max(mx, cw.nitems[c]);
     return blocks_for((size_t)mx * 32, 128);
 }
-#define FDGA_VERTEX_LAUNCHERS(VT, FT)                                                                              \
+#define FDGA_VERTEX_LAUNCHERS(VT, FT, TT, ST)                                                                       \
     cudaError_t launch_bse_K1_all(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const ChanWork& cw, const Dims& d) {                                             \
-        k_bse_K1_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);                               \
+        k_bse_K1_all<ST, false><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, TT{});                        \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VT& F, const BubbleP& B, const ChanWork& cw,             \
@@ -1341,16 +1426,31 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
     }                                                                                                               \
     cudaError_t launch_bse_K2_all(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const ChanWork& cw, const Dims& d) {                                             \
-        k_bse_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d);                               \
+        k_bse_K2_all<ST, false><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, TT{});                        \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_sde_L_all(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
                                  const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d) {             \
-        k_sde_L_all<<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d);     \
+        k_sde_L_all<ST, false><<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d, TT{}); \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }                                                                                                               \
+    cudaError_t launch_bse_K1_tan(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
+                                  const TT& T, const ChanWork& cw, const Dims& d) {                                \
+        k_bse_K1_all<ST, true><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, T);                           \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }                                                                                                               \
+    cudaError_t launch_bse_K2_tan(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
+                                  const TT& T, const ChanWork& cw, const Dims& d) {                                \
+        k_bse_K2_all<ST, true><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, T);                           \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }                                                                                                               \
+    cudaError_t launch_sde_L_tan(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
+                                 const TT& T, const ChanWork& cw, double ref_scale, const Dims& d) {                \
+        k_sde_L_all<ST, true><<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, 1, ref_scale, d, T);           \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }
-FDGA_VERTEX_LAUNCHERS(VertP, FLP)
-FDGA_VERTEX_LAUNCHERS(VertPF, FLPF)
+FDGA_VERTEX_LAUNCHERS(VertP, FLP, TanArgs, cplx)
+FDGA_VERTEX_LAUNCHERS(VertPF, FLPF, TanArgsF, cplxf)
 #undef FDGA_VERTEX_LAUNCHERS
 cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n) {
     k_finalize3<<<blocks_for(n, 256), 256, 0, s>>>(f, k2_epilogue, t_recombine, n);
@@ -1371,6 +1471,11 @@ static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const ARGS& a, int 
         if (tile == 16) return launch_k3_tile<0, 16, C>(s, a, nslots, d);
         if (tile == 24) return launch_k3_tile<0, 24, C>(s, a, nslots, d);
         return launch_k3_tile<0, 32, C>(s, a, nslots, d);
+    }
+    if (mode == 2) {
+        if (tile == 16) return launch_k3_tile<2, 16, C>(s, a, nslots, d);
+        if (tile == 24) return launch_k3_tile<2, 24, C>(s, a, nslots, d);
+        return launch_k3_tile<2, 32, C>(s, a, nslots, d);
     }
     if (tile == 16) return launch_k3_tile<1, 16, C>(s, a, nslots, d);
     if (tile == 24) return launch_k3_tile<1, 24, C>(s, a, nslots, d);

@@ -39,6 +39,13 @@ struct K3Args {
     const cplx* FLa;  // FL.γa.K3
     cplx* out;
     int flags;        // K3F_* (product-rule terms of the tangent map)
+    // tangent contraction (mode 2): dA, dΓ, dΠ and dFL beside the values above
+    const cplx* tA;
+    const cplx* tG;
+    const cplx* tPi;
+    const cplx* tFLc;
+    const cplx* tFLt;
+    const cplx* tFLa;
 };
 // K3Args flags: accumulate into out; leave the γL(ν,ν') epilogue term out; Pi0 == nullptr reads zero
 enum { K3F_ACC = 1, K3F_NOEPI = 2 };
@@ -54,6 +61,12 @@ struct K3ArgsF {  // FP32 operands of the mixed map (the FP32 caches and FL.K3 c
     const cplxf* FLa;
     cplx* out;
     int flags;
+    const cplxf* tA;
+    const cplxf* tG;
+    const cplx* tPi;
+    const cplxf* tFLc;
+    const cplxf* tFLt;
+    const cplxf* tFLa;
 };
 struct K3Args3F {
     K3ArgsF a[3];
@@ -80,6 +93,20 @@ struct BubbleP {
     const cplx* pp0;
     const cplx* ph0;
 };
+// Tangent factors of the K1/K2 BSE and SDE kernels (TAN form): the tangent vertex, dFL, dΠ, dS_X
+// and dSΠ, beside the value arguments.
+template <class S>
+struct TanArgsT {
+    VertPT<S> F;
+    FLPT<S> FL;
+    const cplx* pp;
+    const cplx* ph;
+    const cplx* SX;
+    const cplx* SPpp;
+    const cplx* SPph;
+};
+using TanArgs = TanArgsT<cplx>;
+using TanArgsF = TanArgsT<cplxf>;
 struct Finalize3 {  // indexed by channel (p, t, a)
     const cplx* raw[3];
     cplx* out[3];
@@ -124,6 +151,20 @@ cudaError_t launch_sde_L_all(cudaStream_t s, const VertPF& F, const BubbleP& B, 
                              const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d);
 cudaError_t launch_build_cache(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
+// tangent forms: dK = K(dF; Π, FL, S_X) + K(F; dΠ, dFL, dS_X) in one pass (the T factors), and
+// dL = L(dF; Π, SΠ) + L(F; dΠ, dSΠ) (+ the RefVertex part with dΠ)
+cudaError_t launch_bse_K1_tan(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                              const TanArgs& T, const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_K2_tan(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                              const TanArgs& T, const ChanWork& cw, const Dims& d);
+cudaError_t launch_sde_L_tan(cudaStream_t s, const VertP& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph,
+                             const TanArgs& T, const ChanWork& cw, double ref_scale, const Dims& d);
+cudaError_t launch_bse_K1_tan(cudaStream_t s, const VertPF& F, const FLPF& FL, const BubbleP& B, const cplx* SX,
+                              const TanArgsF& T, const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_K2_tan(cudaStream_t s, const VertPF& F, const FLPF& FL, const BubbleP& B, const cplx* SX,
+                              const TanArgsF& T, const ChanWork& cw, const Dims& d);
+cudaError_t launch_sde_L_tan(cudaStream_t s, const VertPF& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph,
+                             const TanArgsF& T, const ChanWork& cw, double ref_scale, const Dims& d);
 cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n);
 // T0: the tail·tail part of the R = 0 row sums (launch_tail_const, once per solver);
 // GRf (optional): FP32 copy of G(R) -> the real-space row sums run in FP32 (mixed map)
@@ -143,7 +184,9 @@ cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* p
 cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW& out, const Dims& d);
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
-// tile: 16, 24 or 32 (the output tile edge of the GEMM kernel); any other value picks the default for Nν3
+// mode 0 (left K3), 1 (K3), 2 (tangent of K3: dA·M + A·dM + dγL as one GEMM over the concatenated
+// inner index).  tile: 16, 24 or 32 (the output tile edge of the GEMM kernel); any other value picks
+// the default for Nν3
 cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed, int tile);
 int k3_default_tile(int N);
 cudaError_t launch_bse_K3_f32(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int tile);

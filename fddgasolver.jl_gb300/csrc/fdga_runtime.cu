@@ -70,6 +70,7 @@ struct fdga_handle {
     size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
+    int jvp_tangent = 1;                         // GMRES Jacobian products by the tangent kernels (else differences)
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
     cplx *GR = nullptr, *u2C = nullptr, *u2R = nullptr, *twm = nullptr, *twp = nullptr;
     cplx *SPi = nullptr, *SPi0 = nullptr, *SX = nullptr;  // bubble row sums [2][Nq][NΠΩ]; S_X [3][Nq][NΠΩ]
@@ -683,15 +684,16 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
 // applies the product rule stage by stage:
 //   * vertex-linear stages run on the tangent vertex with the RefVertex terms off (it is constant);
 //   * dG = -G² dΣ; dΠ and dSΠ from the product-rule bubble kernels (the 1/ν tails are constant);
-//   * each bilinear BSE runs once per factor with the other factors at their values (Π0 and the
-//     RefVertex caches are constant), accumulating: dK = K(dF, Π, FL) + K(F, dΠ, FL) + K(F, Π, dFL);
-//   * dΣ from dL = L(dF, Π) + L(F, dΠ), and the product-rule Σ_R and U² kernels.
+//   * each bilinear BSE runs as one fused tangent kernel, dK = K(dF; Π, FL) + K(F; dΠ, dFL) (Π0 and
+//     the RefVertex caches are constant): K1/K2 evaluate F and dF in the same pass, K3 is one GEMM
+//     over the concatenated inner index, [dA | A]·[M ; dM];
+//   * dΣ from dL = L(dF, Π) + L(F, dΠ) (one pass), and the product-rule Σ_R and U² kernels.
 // ---------------------------------------------------------------------------------------------
 int ensure_tangent(fdga_handle* h) {
     auto& t = h->tan;
     const Dims& d = h->d;
     const bool mixed = h->precision == FDGA_MIXED;
-    if (!t.x) {
+    if (!t.x) {  // (the zero-fills run on the solver stream, ahead of any use)
         AL(t.x, h->nstate); AL(t.y, h->nstate);
         if (h->navg) AL(t.avg, h->navg);
         AL(t.G, h->nGk); AL(t.GR, h->nGk);
@@ -712,20 +714,29 @@ int ensure_tangent(fdga_handle* h) {
         if (h->navg) AL(t.avgf, h->navg);
         AL(t.GRf, h->nGk);
     }
-    CK(cudaStreamSynchronize(h->st));
     return FDGA_OK;
 }
 
-int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartree, int& nl) {
+int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartree, int& nl,
+                    const StageHook& mark = StageHook()) {
     cudaStream_t s = h->st;
     const Dims& d = h->d;
     auto& t = h->tan;
+    auto stage = [&](const char* name) { if (mark) mark(name); };
     nl = 0;
     const bool mixed = h->precision == FDGA_MIXED;
     const size_t nS = (size_t)d.Nq * d.NPO;
     VertP F = vertex_view(h, h->xS), Fn = vertex_view(h, h->yS);
     VertP tF = vertex_view_t<cplx>(h, t.x, t.avg, h->Fref), tFn = vertex_view_t<cplx>(h, t.y, t.avg, h->Fref);
     tF.noref = tFn.noref = 1;
+    // as in the value map, the Dyson/bubble tangents (branch B) and the left K2 tangent (branch C)
+    // run concurrently with the main stream's caches and left K3 when captured into a graph
+    const bool conc = !mark;
+    cudaStream_t sB = conc ? h->st2 : s, sC = conc ? h->st3 : s;
+    if (conc) {
+        CK(cudaEventRecord(h->evfork, s));
+        CK(cudaStreamWaitEvent(sB, h->evfork, 0));
+    }
     if (d.Nq > 1) {
         ChanArrays in;
         ChanArraysW out;
@@ -734,24 +745,27 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
             out.K1[c] = (cplx*)tF.g[c].A1; out.K2[c] = (cplx*)tF.g[c].A2; out.K3[c] = (cplx*)tF.g[c].A3;
         }
         LC(launch_qavg(s, in, out, d));
+        stage("qavg");
     }
     if (update_sigma) {
-        LC(launch_dyson_tan(s, t.G, h->G, sigmaOf(h, t.x), h->nGk));
-        LC(launch_g_realspace(s, t.G, t.GR, h->twm, d));
+        LC(launch_dyson_tan(sB, t.G, h->G, sigmaOf(h, t.x), h->nGk));
+        LC(launch_g_realspace(sB, t.G, t.GR, h->twm, d));
         if (mixed && bubble_f32_supported(d)) {
-            LC(launch_to_f32(s, t.GR, t.GRf, h->nGk));
-            LC(launch_bubble_f32_tan(s, h->GRf, t.GRf, t.Pipp, t.Piph, d));
-            LC(launch_rowsum_tan(s, t.Pipp, t.Piph, h->GR, t.GR, h->SRtmp, h->twp, t.SPi, t.SPi + nS, d, h->GRf,
+            LC(launch_to_f32(sB, t.GR, t.GRf, h->nGk));
+            LC(launch_bubble_f32_tan(sB, h->GRf, t.GRf, t.Pipp, t.Piph, d));
+            LC(launch_rowsum_tan(sB, t.Pipp, t.Piph, h->GR, t.GR, h->SRtmp, h->twp, t.SPi, t.SPi + nS, d, h->GRf,
                                  t.GRf));
         } else {
-            LC(launch_bubble_tan(s, h->G, t.G, h->GR, t.GR, t.Pipp, t.Piph, h->twp, d));
-            LC(launch_rowsum_tan(s, t.Pipp, t.Piph, h->GR, t.GR, h->SRtmp, h->twp, t.SPi, t.SPi + nS, d));
+            LC(launch_bubble_tan(sB, h->G, t.G, h->GR, t.GR, t.Pipp, t.Piph, h->twp, d));
+            LC(launch_rowsum_tan(sB, t.Pipp, t.Piph, h->GR, t.GR, h->SRtmp, h->twp, t.SPi, t.SPi + nS, d));
         }
     } else {  // G and Π are held fixed
-        LC(cudaMemsetAsync(t.Pipp, 0, h->nPi * sizeof(cplx), s));
-        LC(cudaMemsetAsync(t.Piph, 0, h->nPi * sizeof(cplx), s));
-        LC(cudaMemsetAsync(t.SPi, 0, 2 * nS * sizeof(cplx), s));
+        LC(cudaMemsetAsync(t.Pipp, 0, h->nPi * sizeof(cplx), sB));
+        LC(cudaMemsetAsync(t.Piph, 0, h->nPi * sizeof(cplx), sB));
+        LC(cudaMemsetAsync(t.SPi, 0, 2 * nS * sizeof(cplx), sB));
     }
+    stage("dyson_bubble");
+    if (conc) CK(cudaEventRecord(h->evB, sB));
     // FP32 mirrors of the tangent vertex (mixed map); the value mirrors are the value pass's
     VertPF Ff{}, Fnf{}, tFf{}, tFnf{};
     FLPF FLf{}, tFLf{};
@@ -779,6 +793,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
     }
     if (mixed) LC(launch_build_cache(s, tFf, tC, h->d_k3blocks, h->nk3blocks, d));
     else LC(launch_build_cache(s, tF, tC, h->d_k3blocks, h->nk3blocks, d));
+    stage("k3_cache");
     FLP FL, tFL;
     for (int c = 0; c < 3; ++c) {
         FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
@@ -789,8 +804,6 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
     auto tPi = [&](int ch) -> const cplx* { return ch == CH_P ? t.Pipp : t.Piph; };
     auto Pi0 = [&](int ch) -> const cplx* { return ch == CH_P ? h->Pi0pp : h->Pi0ph; };
     const BubbleP B{h->Pipp, h->Piph, h->Pi0pp, h->Pi0ph};
-    const BubbleP tB{t.Pipp, t.Piph, nullptr, nullptr};   // dΠ, with Π0 read as zero
-    const BubbleP B0{h->Pipp, h->Piph, h->Pipp, h->Piph};  // Π with Π - Π0 read as zero
     auto work = [&](int cls, cplx* raw, int acc) {
         ChanWork cw{};
         const size_t n = cls == 1 ? h->n1 : h->n2;
@@ -821,17 +834,23 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         return launch_bse_K3(s, mode, a3, 3, d, 0, h->k3_tile[FDGA_FP64][mode]);
     };
     if (strategy == FDGA_FDPA) {
-        {  // dFL.K2 = L_K2(dF)  (Π0 constant)
+        {  // dFL.K2 = L_K2(dF)  (Π0 constant): branch C
+            if (conc) {
+                CK(cudaEventRecord(h->evA, s));
+                CK(cudaStreamWaitEvent(sC, h->evA, 0));
+            }
             ChanWork cw = work(2, h->raw2, 0);
-            if (mixed) LC(launch_bse_L_K2_all(s, tFf, B, cw, d));
-            else LC(launch_bse_L_K2_all(s, tF, B, cw, d));
+            if (mixed) LC(launch_bse_L_K2_all(sC, tFf, B, cw, d));
+            else LC(launch_bse_L_K2_all(sC, tF, B, cw, d));
             cplx* out[3] = {t.FLK2, t.FLK2 + h->n2, t.FLK2 + 2 * h->n2};
             const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
             Finalize3 f2 = fin(2, h->raw2, out, grp);
             if (mixed)
                 for (int c = 0; c < 3; ++c) f2.outf[c] = t.FLK2f + (size_t)c * h->n2;
-            LC(launch_finalize3(s, f2, 0, 1, h->n2));
+            LC(launch_finalize3(sC, f2, 0, 1, h->n2));
+            if (conc) CK(cudaEventRecord(h->evC, sC));
         }
+        stage("bse_L_K2");
         {  // dFL.K3 = L_K3(dΓ)  (Π0 and the RefVertex caches constant)
             K3Args3 a3{};
             K3Args3F a3f{};
@@ -856,6 +875,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
                 for (int c = 0; c < 3; ++c) f3.outf[c] = t.FLK3f + (size_t)c * h->n3;
             LC(launch_finalize3(s, f3, 0, 1, h->n3));
         }
+        stage("bse_L_K3");
     } else {  // scPA: FL is not iterated
         LC(cudaMemsetAsync(t.FLK2, 0, 3 * h->n2 * sizeof(cplx), s));
         LC(cudaMemsetAsync(t.FLK3, 0, 3 * h->n3 * sizeof(cplx), s));
@@ -864,71 +884,69 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
             LC(cudaMemsetAsync(t.FLK3f, 0, 3 * h->n3 * sizeof(cplxf), s));
         }
     }
+    if (conc) {  // join: dΠ, dSΠ (B) and dFL.K2 (C)
+        CK(cudaStreamWaitEvent(s, h->evB, 0));
+        if (strategy == FDGA_FDPA) CK(cudaStreamWaitEvent(s, h->evC, 0));
+    }
     LC(launch_sx_tan(s, h->Pipp, h->Piph, t.Pipp, t.Piph, t.SPi, FL, tFL, t.SX, d));
-    {  // dK1 = K1(dF; Π, FL, S_X) + K1(F; dΠ, FL, dS_X) + K1(F; Π, dFL)
-        if (mixed) {
-            LC(launch_bse_K1_all(s, tFf, FLf, B, h->SX, work(1, h->raw1, 0), d));
-            LC(launch_bse_K1_all(s, Ff, FLf, tB, t.SX, work(1, h->raw1, 1), d));
-            LC(launch_bse_K1_all(s, Ff, tFLf, B0, nullptr, work(1, h->raw1, 1), d));
-        } else {
-            LC(launch_bse_K1_all(s, tF, FL, B, h->SX, work(1, h->raw1, 0), d));
-            LC(launch_bse_K1_all(s, F, FL, tB, t.SX, work(1, h->raw1, 1), d));
-            LC(launch_bse_K1_all(s, F, tFL, B0, nullptr, work(1, h->raw1, 1), d));
-        }
+    stage("sx");
+    // tangent factors of the fused K1/K2/SDE kernels
+    const TanArgs T64{tF, tFL, t.Pipp, t.Piph, t.SX, t.SPi, t.SPi + nS};
+    const TanArgsF T32{tFf, tFLf, t.Pipp, t.Piph, t.SX, t.SPi, t.SPi + nS};
+    {  // dK1 = K1(dF; Π, FL, S_X) + K1(F; dΠ, dFL, dS_X), one pass
+        if (mixed) LC(launch_bse_K1_tan(s, Ff, FLf, B, h->SX, T32, work(1, h->raw1, 0), d));
+        else LC(launch_bse_K1_tan(s, F, FL, B, h->SX, T64, work(1, h->raw1, 0), d));
         cplx* out[3] = {chanK(h, t.y, CH_P, 1), chanK(h, t.y, CH_T, 1), chanK(h, t.y, CH_A, 1)};
         const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
         LC(launch_finalize3(s, fin(1, h->raw1, out, grp), 0, 1, h->n1));
     }
-    {  // dK2, the same three terms, then the FL epilogue with dFL.K2
-        if (mixed) {
-            LC(launch_bse_K2_all(s, tFf, FLf, B, h->SX, work(2, h->raw2, 0), d));
-            LC(launch_bse_K2_all(s, Ff, FLf, tB, t.SX, work(2, h->raw2, 1), d));
-            LC(launch_bse_K2_all(s, Ff, tFLf, B0, nullptr, work(2, h->raw2, 1), d));
-        } else {
-            LC(launch_bse_K2_all(s, tF, FL, B, h->SX, work(2, h->raw2, 0), d));
-            LC(launch_bse_K2_all(s, F, FL, tB, t.SX, work(2, h->raw2, 1), d));
-            LC(launch_bse_K2_all(s, F, tFL, B0, nullptr, work(2, h->raw2, 1), d));
-        }
+    stage("bse_K1");
+    {  // dK2 likewise, then the FL epilogue with dFL.K2
+        if (mixed) LC(launch_bse_K2_tan(s, Ff, FLf, B, h->SX, T32, work(2, h->raw2, 0), d));
+        else LC(launch_bse_K2_tan(s, F, FL, B, h->SX, T64, work(2, h->raw2, 0), d));
         cplx* out[3] = {chanK(h, t.y, CH_P, 2), chanK(h, t.y, CH_T, 2), chanK(h, t.y, CH_A, 2)};
         const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
         LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 1, 1, h->n2));
     }
-    {  // dK3 = T dF·M + T F·M(dΠ) + T F·M(dΓ, dFL) + dγL
-        for (int term = 0; term < 3; ++term) {
-            K3Args3 a3{};
-            K3Args3F a3f{};
-            for (int i = 0; i < 3; ++i) {
-                const int ch = order[i];
-                const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
-                const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
-                const cplx* fl = (term == 2 ? t.FLK3 : h->FLK3);
-                const cplxf* flf = (term == 2 ? t.FLK3f : h->FLK3f);
-                K3Args& a = a3.a[i];
-                K3ArgsF& af = a3f.a[i];
-                a.A = term == 0 ? tC.c[cf] : C.c[cf];
-                af.A = term == 0 ? tC.f[cf] : C.f[cf];
-                a.B0 = C.c[cf0]; af.B0 = C.f[cf0];
-                a.G = term == 2 ? tC.c[cg] : C.c[cg];
-                af.G = term == 2 ? tC.f[cg] : C.f[cg];
-                a.Pi = af.Pi = term == 1 ? tPi(ch) : Pi(ch);
-                a.Pi0 = af.Pi0 = term == 0 ? Pi0(ch) : (term == 1 ? nullptr : Pi(ch));
-                a.FLc = fl + (size_t)ch * h->n3; a.FLt = fl + (size_t)CH_T * h->n3; a.FLa = fl + (size_t)CH_A * h->n3;
-                if (mixed) {
-                    af.FLc = flf + (size_t)ch * h->n3; af.FLt = flf + (size_t)CH_T * h->n3;
-                    af.FLa = flf + (size_t)CH_A * h->n3;
-                }
-                a.out = af.out = h->raw3 + (size_t)ch * h->n3;
-                a.flags = af.flags = (term == 2 ? 0 : K3F_NOEPI) | (term > 0 ? K3F_ACC : 0);
-                a3.ch[i] = a3f.ch[i] = ch;
+    stage("bse_K2");
+    {  // dK3 = T (dF·M + F·dM) + dγL: one GEMM over the concatenated inner index (mode 2)
+        K3Args3 a3{};
+        K3Args3F a3f{};
+        for (int i = 0; i < 3; ++i) {
+            const int ch = order[i];
+            const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
+            const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+            K3Args& a = a3.a[i];
+            K3ArgsF& af = a3f.a[i];
+            a.A = C.c[cf]; af.A = C.f[cf];
+            a.tA = tC.c[cf]; af.tA = tC.f[cf];
+            a.B0 = C.c[cf0]; af.B0 = C.f[cf0];
+            a.G = C.c[cg]; af.G = C.f[cg];
+            a.tG = tC.c[cg]; af.tG = tC.f[cg];
+            a.Pi = af.Pi = Pi(ch);
+            a.tPi = af.tPi = tPi(ch);
+            a.Pi0 = af.Pi0 = Pi0(ch);
+            a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3;
+            a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
+            a.tFLc = t.FLK3 + (size_t)ch * h->n3; a.tFLt = t.FLK3 + (size_t)CH_T * h->n3;
+            a.tFLa = t.FLK3 + (size_t)CH_A * h->n3;
+            if (mixed) {
+                af.FLc = h->FLK3f + (size_t)ch * h->n3; af.FLt = h->FLK3f + (size_t)CH_T * h->n3;
+                af.FLa = h->FLK3f + (size_t)CH_A * h->n3;
+                af.tFLc = t.FLK3f + (size_t)ch * h->n3; af.tFLt = t.FLK3f + (size_t)CH_T * h->n3;
+                af.tFLa = t.FLK3f + (size_t)CH_A * h->n3;
             }
-            a3.blocks = a3f.blocks = h->d_k3blocks;
-            a3.nblocks = a3f.nblocks = h->nk3blocks;
-            LC(k3(1, a3, a3f));
+            a.out = af.out = h->raw3 + (size_t)ch * h->n3;
+            a3.ch[i] = a3f.ch[i] = ch;
         }
+        a3.blocks = a3f.blocks = h->d_k3blocks;
+        a3.nblocks = a3f.nblocks = h->nk3blocks;
+        LC(k3(2, a3, a3f));
         cplx* out[3] = {chanK(h, t.y, CH_P, 3), chanK(h, t.y, CH_T, 3), chanK(h, t.y, CH_A, 3)};
         const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
         LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
     }
+    stage("bse_K3");
     cplx* tSig = sigmaOf(h, t.y);
     if (update_sigma) {
         const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
@@ -939,16 +957,16 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
             cw.nitems[w] = g[w]->trivial ? (int)h->n2 : g[w]->nitems;
             cw.out[w] = h->raw2 + (size_t)w * h->n2;
         }
-        // dL = L(dF; Π, SΠ) + L(F; dΠ, dSΠ) (+ the RefVertex part with dΠ)
-        ChanWork cw1 = cw;
-        cw1.acc = 1;
+        // dL = L(dF; Π, SΠ) + L(F; dΠ, dSΠ) (+ the RefVertex part with dΠ), one pass
         if (mixed) {
             LC(launch_to_f32(s, t.y, t.ySf, 3 * h->nchan));
-            LC(launch_sde_L_all(s, tFnf, B, h->SPi, h->SPi + nS, cw, 1, 0.0, d));
-            LC(launch_sde_L_all(s, Fnf, tB, t.SPi, t.SPi + nS, cw1, 1, rs, d));
+            TanArgsF Tn = T32;
+            Tn.F = tFnf;
+            LC(launch_sde_L_tan(s, Fnf, B, h->SPi, h->SPi + nS, Tn, cw, rs, d));
         } else {
-            LC(launch_sde_L_all(s, tFn, B, h->SPi, h->SPi + nS, cw, 1, 0.0, d));
-            LC(launch_sde_L_all(s, Fn, tB, t.SPi, t.SPi + nS, cw1, 1, rs, d));
+            TanArgs Tn = T64;
+            Tn.F = tFn;
+            LC(launch_sde_L_tan(s, Fn, B, h->SPi, h->SPi + nS, Tn, cw, rs, d));
         }
         Finalize3 f{};
         f.raw[0] = h->raw2; f.out[0] = t.Lpp; f.map[0] = g[0]->trivial ? nullptr : g[0]->d_map;
@@ -964,6 +982,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
     } else {
         LC(cudaMemcpyAsync(tSig, sigmaOf(h, t.x), h->nGk * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
     }
+    stage("sde");
     return FDGA_OK;
 }
 
@@ -1706,10 +1725,20 @@ int cmax(fdga_handle* h, const cplx* a, double& out) {
 }
 
 // A v = v − J v at the base point xb (full) for the unit compact FP32 direction v, into w.
-// Forward: J v = (Φ(xb + εv) − yb)/ε (yb compact).  Central: (Φ(xb + εv) − Φ(xb − εv))/(2ε).
+// Tangent kernels (jvp_tangent): J v = Φ'(xb) v; the value intermediates of xb (the last map at xb,
+// in the current precision) are in the handle and the state xS is xb.
+// Forward difference: J v = (Φ(xb + εv) − yb)/ε (yb compact).  Central: (Φ(xb + εv) − Φ(xb − εv))/(2ε).
 int apply_A(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplxf* v, double eps, bool central,
             cplxf* w, int& nmaps) {
     const size_t n = h->nstate, nc = h->nc;
+    if (h->jvp_tangent) {
+        CK(launch_kc_point(h->st, NBLK_RED, nullptr, v, h->kc_code, 1.0, h->tan.x, n));
+        int r = run_tangent(h, strategy, true, true);
+        if (r) return r;
+        ++nmaps;
+        CK(launch_kc_apply(h->st, NBLK_RED, h->tan.y, nullptr, h->kc_pos, v, 1.0, -1.0, w, nc));
+        return FDGA_OK;
+    }
     CK(launch_kc_point(h->st, NBLK_RED, xb, v, h->kc_code, eps, h->xS, n));
     int r = run_iteration(h, strategy, true, true);
     if (r) return r;
@@ -1765,7 +1794,7 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
             double dn = 0.0;
             if ((r = cnorm(h, dx, sc, dn))) return r;
             if (dn == 0.0) break;
-            if (nmaps + (central ? 2 : 1) > max_maps) break;
+            if (nmaps + (central && !h->jvp_tangent ? 2 : 1) > max_maps) break;
             CK(launch_kr_load(h->st, NBLK_RED, dx, W, sc, h->kr_part, nc));
             CK(launch_kr_scale(h->st, NBLK_RED, sc, dn, sc, nc));
             if ((r = apply_A(h, strategy, xb, yb, sc, eps, central, w, nmaps))) return r;
@@ -1781,7 +1810,7 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
         int k = 0;
         double est = beta;
         for (int j = 0; j < m; ++j) {
-            if (nmaps + (central ? 2 : 1) > max_maps) break;
+            if (nmaps + (central && !h->jvp_tangent ? 2 : 1) > max_maps) break;
             if ((r = apply_A(h, strategy, xb, yb, V.v[j], eps, central, w, nmaps))) return r;
             // classical Gram-Schmidt, twice (weighted inner products)
             CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, W, h->kr_part, -1, nc));
@@ -1929,6 +1958,15 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
     const size_t nc = h->nc;
     if (jvp_precision == FDGA_MIXED && (r = ensure_mixed(h))) return r;
     const int prec0 = h->precision;
+    if (h->jvp_tangent) {  // tangent buffers of both precisions used below
+        for (int p : {(int)FDGA_FP64, jvp_precision}) {
+            const int keep = h->precision;
+            h->precision = p;
+            r = ensure_tangent(h);
+            h->precision = keep;
+            if (r) return r;
+        }
+    }
     struct Restore {
         fdga_handle* h; int p;
         ~Restore() { h->precision = p; }
@@ -1977,7 +2015,10 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
         if (jvp_prec == FDGA_MIXED && nouter > 3 && !(resid < 0.5 * prev)) jvp_prec = FDGA_FP64;
         // forcing term (Eisenstat–Walker choice 2, bounded); the mixed map's rounding floor bounds it below
         double eta = nouter <= 2 ? 0.1 : std::min(0.1, 0.9 * (resid / prev) * (resid / prev));
-        eta = std::max(eta, jvp_prec == FDGA_MIXED ? 1e-3 : 1e-6);
+        // (tangent JVPs of the mixed map carry FP32 rounding, ~1e-6; differences of it ~1e-4)
+        eta = std::max(eta, jvp_prec == FDGA_MIXED ? (h->jvp_tangent ? 1e-5 : 1e-3) : 1e-6);
+        // no linear solve beyond what the tolerance asks of this step
+        eta = std::min(0.1, std::max(eta, 0.1 * tol / resid));
         if (jvp_prec == FDGA_MIXED) {
             h->precision = FDGA_MIXED;
             CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
@@ -2062,7 +2103,12 @@ int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int resta
     CK(launch_kc_gather(h->st, NBLK_RED, h->yS, nullptr, h->kc_pos, 1.0, b, nc));
     CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, b, 0.5 / hU, b, nc));  // b = (y+ − y−)/(2h)
     if ((r = fdga_set_U(h, U))) return r;
-    // (I − J) dx = ∂Φ/∂U, central-difference Jacobian
+    if (h->jvp_tangent) {  // value intermediates at the fixed point for the tangent kernels
+        if ((r = ensure_tangent(h))) return r;
+        CK(cudaMemcpyAsync(h->xS, xs, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        if ((r = run_iteration(h, strategy, true, true))) return r;
+    }
+    // (I − J) dx = ∂Φ/∂U (Jacobian by the tangent kernels, or central differences)
     int nmaps = 0, its = 0;
     double relres = 1.0;
     r = gmres_solve(h, strategy, xs, nullptr, b, dx, restart, cycles, rtol, 1e-5, true, 1 << 30, nmaps, its, relres);
@@ -2162,6 +2208,10 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
         drop_graphs(h);
         return FDGA_OK;
     }
+    if (k == "jvp_tangent") {
+        h->jvp_tangent = value ? 1 : 0;
+        return FDGA_OK;
+    }
     return fail(h, FDGA_ERR_ARG, "unknown option " + k);
 }
 
@@ -2196,10 +2246,15 @@ int fdga_synchronize(fdga_handle* h) {
     CK(cudaStreamSynchronize(h->st));
     return FDGA_OK;
 }
-int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms, int max_stages,
-                     int* nstages) {
+}  // extern "C"
+
+namespace {
+// per-stage device times of an eager launch sequence (the iteration or its tangent)
+int stage_times_impl(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms,
+                     int max_stages, int* nstages, bool tangent) {
     if (!h || !ms || !nstages || nrep < 1) return FDGA_ERR_ARG;
     if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (tangent && !h->tan.x) return fail(h, FDGA_ERR_STATE, "fdga_frule has not been called");
     if (h->c0_dirty) { int r = compute_C0(h); if (r) return r; }
     std::vector<std::string> nm;
     std::vector<double> acc;
@@ -2218,7 +2273,8 @@ int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t
             evs.push_back(e);
             cur.push_back(name);
         };
-        int r = enqueue_iteration(h, strategy, true, true, nl, hook);
+        int r = tangent ? enqueue_tangent(h, strategy, true, true, nl, hook)
+                        : enqueue_iteration(h, strategy, true, true, nl, hook);
         if (r) return r;
         CK(cudaStreamSynchronize(h->st));
         if (rep == 0) { nm = cur; acc.assign(cur.size(), 0.0); }
@@ -2228,7 +2284,7 @@ int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t
             acc[i] += t;
         }
         for (auto e : evs) cudaEventDestroy(e);
-        CK(cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        if (!tangent) CK(cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
     }
     CK(cudaStreamSynchronize(h->st));
     const int n = (int)std::min<size_t>(nm.size(), (size_t)max_stages);
@@ -2244,6 +2300,18 @@ int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t
     }
     *nstages = n;
     return FDGA_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms, int max_stages,
+                     int* nstages) {
+    return stage_times_impl(h, strategy, nrep, names, names_cap, ms, max_stages, nstages, false);
+}
+int fdga_tangent_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms,
+                             int max_stages, int* nstages) {
+    return stage_times_impl(h, strategy, nrep, names, names_cap, ms, max_stages, nstages, true);
 }
 
 int fdga_map_repeat(fdga_handle* h, int strategy, int n) {

@@ -72,6 +72,8 @@ EXPORTS = {
     "fdga_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "fdga_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
                                         ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "fdga_tangent_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
+                                        ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "fdga_map_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "fdga_tangent_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "fdga_flush_l2": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t]),

@@ -249,13 +249,14 @@ class _Solver:
     def synchronize(self):
         self._check(self._lib.fdga_synchronize(self._h))
 
-    def stage_times(self, strategy="fdPA", nrep=3):
-        """Per-stage device milliseconds of an eager iteration (CUDA events on the solver stream)."""
+    def stage_times(self, strategy="fdPA", nrep=3, tangent=False):
+        """Per-stage device milliseconds of an eager iteration (CUDA events on the solver stream);
+        tangent=True: of the tangent map at the last frule's base point and direction."""
         names = ctypes.create_string_buffer(1024)
         ms = np.zeros(32, dtype=np.float64)
         n = ctypes.c_int()
-        self._check(self._lib.fdga_stage_times(self._h, STRATEGIES[strategy], int(nrep), names, 1024, ms.ctypes.data,
-                                               32, ctypes.byref(n)))
+        fn = self._lib.fdga_tangent_stage_times if tangent else self._lib.fdga_stage_times
+        self._check(fn(self._h, STRATEGIES[strategy], int(nrep), names, 1024, ms.ctypes.data, 32, ctypes.byref(n)))
         keys = names.value.decode().split(",") if n.value else []
         return dict(zip(keys, ms[: n.value].tolist()))
 

@@ -104,7 +104,9 @@ int fdga_set_precision(fdga_handle* h, int precision);
 
 /* Integer options: "k3_tensor_cores" (default 1): the mixed map's K3 contractions run on the
  * tensor cores (tcgen05, TF32 hi/lo split, FP32 accumulation) when 2·Nν3 ≤ 256 and Nν3 is a
- * multiple of 8, else as FP32 CUDA-core GEMMs. */
+ * multiple of 8, else as FP32 CUDA-core GEMMs.  "jvp_tangent" (default 1): the GMRES solves of
+ * fdga_solve_newton and fdga_dchi_dU apply the Jacobian through the tangent kernels (as
+ * fdga_frule); 0: by finite differences of the map. */
 int fdga_set_option(fdga_handle* h, const char* key, int value);
 
 /* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.
@@ -227,6 +229,9 @@ int fdga_synchronize(fdga_handle* h);
  * advances by nrep iterations.  names receives a comma-separated stage list. */
 int fdga_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms,
                      int max_stages, int* nstages);
+/* The same for the tangent map at the base point and direction of the last fdga_frule call. */
+int fdga_tangent_stage_times(fdga_handle* h, int strategy, int nrep, char* names, size_t names_cap, double* ms,
+                             int max_stages, int* nstages);
 /* Applies the iteration map n times to the unchanged device state x (graph replays, no host
  * synchronisation): the device-resident timing loop of the benchmark. */
 int fdga_map_repeat(fdga_handle* h, int strategy, int n);

@@ -1,8 +1,9 @@
 """Newton–Krylov solve, Jacobian-vector products and the linear response dχ/dU.
 
 (1) fdga_jvp agrees with central differences of the oracle's map (step 1e-6) to 1e-6 relative.
-(2) fdga_solve_newton reaches the FP64 fixed point (FP64 and mixed JVPs): converged at 1e-10 on
-    the FP64 residual, state within 1e-8 of the oracle's Anderson solution.
+(2) fdga_solve_newton reaches the FP64 fixed point (FP64 and mixed JVPs, by the tangent kernels
+    and by differences): converged at 1e-10 on the FP64 residual, state within 1e-8 of the
+    oracle's Anderson solution.
 (3) dχ_m/dU and dχ_d/dU at the fixed point (GMRES on (I − J) dx/dU = ∂Φ/∂U) agree with central
     differences h = 1e-4 of the oracle's converged χ at U ± h to 1e-6 relative.  The RefVertex
     is the bare U here, so that the reference vertex depends on U only through U itself.
@@ -37,11 +38,13 @@ def test_jvp_matches_oracle_differences(cfg):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tangent", [1, 0], ids=["tangent", "differences"])
 @pytest.mark.parametrize("jvp", ["fp64", "mixed"])
 @pytest.mark.parametrize("cfg", [NL4_NOISE, LOCAL], ids=["nl4", "local"])
-def test_newton_reaches_fixed_point(cfg, jvp):
+def test_newton_reaches_fixed_point(cfg, jvp, tangent):
     orc = make_oracle(cfg, True)
     gpu = make_gpu(cfg, True)
+    gpu.set_option("jvp_tangent", tangent)
     r_o = orc.solve("fdPA", maxiter=300, tol=1e-11, beta=0.5, mem=8)
     r_g = gpu.solve_newton("fdPA", maxiter=400, tol=1e-10, restart=30, jvp=jvp)
     assert r_o["converged"] and r_g["converged"], (r_g["trace"], r_g["evals_fp64"], r_g["evals_mixed"])
@@ -49,8 +52,9 @@ def test_newton_reaches_fixed_point(cfg, jvp):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tangent", [1, 0], ids=["tangent", "differences"])
 @pytest.mark.parametrize("cfg", [NL4, LOCAL], ids=["nl4", "local"])
-def test_dchi_dU_matches_oracle_differences(cfg):
+def test_dchi_dU_matches_oracle_differences(cfg, tangent):
     h = 1e-4
     chi = {}
     for sgn in (+1, -1):
@@ -61,6 +65,7 @@ def test_dchi_dU_matches_oracle_differences(cfg):
         K1a, K1t = o.get("F.a.K1"), o.get("F.t.K1")
         chi[sgn] = {"m": K1a / c["U"] ** 2, "d": (K1a - 2 * K1t) / c["U"] ** 2}
     gpu = make_gpu(cfg, True)
+    gpu.set_option("jvp_tangent", tangent)
     r = gpu.solve("fdPA", maxiter=400, tol=1e-13, delta=0.5, mem=8)
     assert r["converged"]
     for ch in ("m", "d"):
