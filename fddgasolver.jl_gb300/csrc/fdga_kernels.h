@@ -107,6 +107,27 @@ struct TanArgsT {
 };
 using TanArgs = TanArgsT<cplx>;
 using TanArgsF = TanArgsT<cplxf>;
+// cotangent (adjoint) views: writable K arrays and momentum averages of the three channels
+struct ChanBar {
+    cplx *K1, *K2, *K3, *A1, *A2, *A3;
+};
+struct VertBar {
+    ChanBar g[3];
+};
+struct FLBar {
+    cplx* K2[3];
+};
+struct ChanBarArrays {  // averages' cotangents (read) and the K arrays' cotangents (accumulated)
+    const cplx* A1[3];
+    const cplx* A2[3];
+    const cplx* A3[3];
+    cplx* K1[3];
+    cplx* K2[3];
+    cplx* K3[3];
+};
+struct Ptr3 {
+    cplx* p[3];
+};
 struct Finalize3 {  // indexed by channel (p, t, a)
     const cplx* raw[3];
     cplx* out[3];
@@ -282,6 +303,38 @@ cudaError_t launch_sx_tan(cudaStream_t s, const cplx* Pipp, const cplx* Piph, co
 cudaError_t launch_sde_sigma_tan(cudaStream_t s, const cplx* GR, const cplx* LR, const cplx* tGR, const cplx* tLpp,
                                  const cplx* tLph, cplx* tLR, cplx* tSR, cplx* tS, const cplx* twm, const cplx* twp,
                                  const Dims& d);
+// reverse-mode (adjoint) stages of the iteration map (fdga_adjoint.cu)
+cudaError_t launch_adj_assemble(cudaStream_t s, const cplx* Sbar, const uint32_t* map, cplx* Sin_bar, cplx* SU2_bar,
+                                size_t n, int hartree, double U, double* nbar);
+cudaError_t launch_adj_occupation(cudaStream_t s, cplx* Gbar, const double* nbar, double T, int Nk, size_t n);
+cudaError_t launch_adj_dyson(cudaStream_t s, const cplx* G, const cplx* Gbar, cplx* Sbar, size_t n);
+cudaError_t launch_adj_u2(cudaStream_t s, const cplx* GR, const cplx* C, cplx* obar_k, cplx* obar_R, cplx* Cbar,
+                          cplx* GRbar, const cplx* twm, const Dims& d);
+cudaError_t launch_adj_sigma(cudaStream_t s, const cplx* GR, const cplx* LR, const cplx* Sinbar, cplx* SRbar,
+                             cplx* LRbar, cplx* Lbar, cplx* GRbar, const cplx* twm, const cplx* twp, const Dims& d);
+cudaError_t launch_adj_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue, int t_recombine, size_t n,
+                                 cplx* const FLbar[3]);
+cudaError_t launch_adj_sde_L(cudaStream_t s, const VertP& F, const VertBar& Fb, const BubbleP& B, const cplx* SPpp,
+                             const cplx* SPph, cplx* Pbpp, cplx* Pbph, cplx* SPbpp, cplx* SPbph, const cplx* rawbar,
+                             const ChanWork& cw, size_t n2, double rs, const Dims& d);
+cudaError_t launch_adj_K1(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                          const VertBar& Fb, const FLBar& FLb, cplx* Pbpp, cplx* Pbph, cplx* SXbar, const cplx* rawbar,
+                          const ChanWork& cw, size_t n1, const Dims& d);
+cudaError_t launch_adj_K2(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,
+                          const VertBar& Fb, const FLBar& FLb, cplx* Pbpp, cplx* Pbph, cplx* SXbar, const cplx* rawbar,
+                          const ChanWork& cw, size_t n2, const Dims& d);
+cudaError_t launch_adj_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const FLP& FL, const cplx* SXbar,
+                          cplx* Pbpp, cplx* Pbph, cplx* SPibar, const FLBar& FLb, const Dims& d);
+cudaError_t launch_adj_L_K2(cudaStream_t s, const BubbleP& B, const VertBar& Fb, const cplx* rawbar, const ChanWork& cw,
+                            size_t n2, const Dims& d);
+cudaError_t launch_adj_cache(cudaStream_t s, const VertBar& Fb, const Caches& Cb, const int* blocks, int nblocks,
+                             const Dims& d);
+cudaError_t launch_adj_K3(cudaStream_t s, int mode, const K3Args3& a, const cplx* const Obar[3], cplx* const Abar[3],
+                          cplx* const Gbar[3], cplx* const Mbuf[3], cplx* const Mbar[3], cplx* Pbpp, cplx* Pbph,
+                          cplx* const FLbar[3], const Dims& d);
+cudaError_t launch_adj_bubble(cudaStream_t s, const cplx* GR, cplx* Pbpp, cplx* Pbph, cplx* PbRpp, cplx* PbRph,
+                              const cplx* SPibar, cplx* SRbar, cplx* GRbar, const cplx* twm, const Dims& d);
+cudaError_t launch_adj_qavg(cudaStream_t s, const ChanBarArrays& bar, const Dims& d);
 cudaError_t launch_u2_tan(cudaStream_t s, const cplx* GR, const cplx* C, const cplx* tGR, cplx* tC, cplx* tSR,
                           cplx* tout, const cplx* twc, const Dims& d);
 

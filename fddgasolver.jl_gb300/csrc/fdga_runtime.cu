@@ -122,6 +122,17 @@ struct fdga_handle {
         cplxf *avgf = nullptr, *GRf = nullptr;  // FP32 forms (tangent of the mixed map)
         Graph graphs[2][2][2][2];               // [precision][strategy][update_sigma][hartree]
     } tan;
+    // Adjoint map (reverse-mode derivative of one FP64 iteration): cotangents x̄ (result) and ȳ (input,
+    // plus the SDE's contributions to the new vertex), and the cotangent intermediates
+    struct Adjoint {
+        cplx *xb = nullptr, *yb = nullptr, *avgb = nullptr, *Gb = nullptr, *GRb = nullptr;
+        cplx *Pbpp = nullptr, *Pbph = nullptr, *PbRpp = nullptr, *PbRph = nullptr, *SPib = nullptr, *SRb = nullptr;
+        cplx *SXb = nullptr, *cacheb = nullptr, *FLK2b = nullptr, *FLK3b = nullptr;
+        cplx *raw1 = nullptr, *raw2 = nullptr, *raw3 = nullptr, *M = nullptr, *Mb = nullptr;
+        cplx *SigInb = nullptr, *SU2b = nullptr, *SigRb = nullptr, *u2Rb = nullptr, *u2Cb = nullptr;
+        cplx *LRb = nullptr, *Lb = nullptr;
+        double* nbar = nullptr;
+    } adj;
     std::vector<void*> allocs;
 };
 
@@ -1005,6 +1016,228 @@ int run_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
     }
     CK(cudaGraphLaunch(g.exec, h->st));
     h->last_launches = g.nodes;
+    return FDGA_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Adjoint map (reverse mode, the rrule of one FP64 iteration): x̄ = Φ'(x)ᵀ ȳ for the real inner
+// product, at the base point whose value intermediates the last FP64 enqueue_iteration left in the
+// handle.  The stages of enqueue_iteration run backwards: Σ assembly, U² and Σ_R terms, L (SDE),
+// the K1/K2/K3 outputs (symmetrisation, FL epilogue, recombination), the K3 GEMMs, K2, K1, S_X, the
+// left BSEs, the caches, the bubbles and row sums, G(R), Dyson and the momentum averages.  The
+// kernels are in fdga_adjoint.cu.
+// ---------------------------------------------------------------------------------------------
+int ensure_adjoint(fdga_handle* h) {
+    auto& a = h->adj;
+    if (a.xb) return FDGA_OK;
+    const Dims& d = h->d;
+    const size_t NR = (size_t)d.L * d.L, nS = (size_t)d.Nq * d.NPO;
+    AL(a.xb, h->nstate); AL(a.yb, h->nstate);
+    if (h->navg) AL(a.avgb, h->navg);
+    AL(a.Gb, h->nGk); AL(a.GRb, h->nGk);
+    AL(a.Pbpp, h->nPi); AL(a.Pbph, h->nPi); AL(a.PbRpp, h->nPi); AL(a.PbRph, h->nPi);
+    AL(a.SPib, 2 * nS); AL(a.SRb, 2 * NR * d.NPO); AL(a.SXb, 3 * nS);
+    AL(a.cacheb, 10 * h->n3); AL(a.FLK2b, 3 * h->n2); AL(a.FLK3b, 3 * h->n3);
+    AL(a.raw1, 3 * h->n1); AL(a.raw2, 3 * h->n2); AL(a.raw3, 3 * h->n3);
+    AL(a.M, 3 * h->n3); AL(a.Mb, 3 * h->n3);
+    AL(a.SigInb, h->nGk); AL(a.SU2b, h->nGk); AL(a.SigRb, h->nGk); AL(a.u2Rb, h->nGk);
+    AL(a.u2Cb, (size_t)d.Nq * (2 * d.NG - 1));
+    AL(a.LRb, 2 * h->n2); AL(a.Lb, 2 * h->n2);
+    AL(a.nbar, 1);
+    return FDGA_OK;
+}
+
+int enqueue_adjoint(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
+    cudaStream_t s = h->st;
+    const Dims& d = h->d;
+    auto& a = h->adj;
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    auto Z = [&](void* p, size_t bytes) { return cudaMemsetAsync(p, 0, bytes, s); };
+    CK(Z(a.xb, h->nstate * sizeof(cplx)));
+    if (h->navg) CK(Z(a.avgb, h->navg * sizeof(cplx)));
+    CK(Z(a.GRb, h->nGk * sizeof(cplx)));
+    CK(Z(a.Pbpp, h->nPi * sizeof(cplx))); CK(Z(a.Pbph, h->nPi * sizeof(cplx)));
+    CK(Z(a.SPib, 2 * nS * sizeof(cplx))); CK(Z(a.SXb, 3 * nS * sizeof(cplx)));
+    CK(Z(a.cacheb, 10 * h->n3 * sizeof(cplx)));
+    CK(Z(a.FLK2b, 3 * h->n2 * sizeof(cplx))); CK(Z(a.FLK3b, 3 * h->n3 * sizeof(cplx)));
+    CK(Z(a.SigInb, h->nGk * sizeof(cplx))); CK(Z(a.SU2b, h->nGk * sizeof(cplx)));
+    CK(Z(a.nbar, sizeof(double)));
+    VertP F = vertex_view(h, h->xS), Fn = vertex_view(h, h->yS);
+    // cotangent views: x̄ (with the averages' cotangents) and ȳ (SDE contributions to the new vertex)
+    auto bar_view = [&](cplx* st, cplx* avg) {
+        VertBar B{};
+        for (int c = 0; c < 3; ++c) {
+            cplx* base = st + (size_t)c * h->nchan;
+            B.g[c].K1 = base; B.g[c].K2 = base + h->n1; B.g[c].K3 = base + h->n1 + h->n2;
+            if (d.Nq == 1 || !avg) {
+                B.g[c].A1 = B.g[c].K1; B.g[c].A2 = B.g[c].K2; B.g[c].A3 = B.g[c].K3;
+            } else {
+                const size_t per1 = d.N1, per2 = (size_t)d.N2O * d.N2n, per3 = (size_t)d.N3O * d.N3n * d.N3n;
+                cplx* av = avg + (size_t)c * (per1 + per2 + per3);
+                B.g[c].A1 = av; B.g[c].A2 = av + per1; B.g[c].A3 = av + per1 + per2;
+            }
+        }
+        return B;
+    };
+    const VertBar Xb = bar_view(a.xb, a.avgb), Yb = bar_view(a.yb, nullptr);
+    FLP FL;
+    FLBar FLb;
+    for (int c = 0; c < 3; ++c) {
+        FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
+        FLb.K2[c] = a.FLK2b + (size_t)c * h->n2;
+    }
+    const BubbleP B{h->Pipp, h->Piph, h->Pi0pp, h->Pi0ph};
+    auto work = [&](int cls) {
+        ChanWork cw{};
+        const size_t n = cls == 1 ? h->n1 : h->n2;
+        for (int ch = 0; ch < 3; ++ch) {
+            const Group& g = cls == 1 ? h->gK1 : k2group(h, ch);
+            cw.items[ch] = g.trivial ? nullptr : g.d_items;
+            cw.nitems[ch] = g.trivial ? (int)n : g.nitems;
+        }
+        return cw;
+    };
+    // finalize transposed: output cotangents ō (f.raw) -> representative cotangents (f.out)
+    auto fin_adj = [&](const cplx* const ob[3], cplx* rb, size_t n, const Group* const grp[3], int k2e, int trec,
+                       cplx* const FLbar[3]) -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(rb, 0, 3 * n * sizeof(cplx), s);
+        if (e != cudaSuccess) return e;
+        Finalize3 f{};
+        for (int ch = 0; ch < 3; ++ch) {
+            f.raw[ch] = ob[ch];
+            f.out[ch] = ob[ch] ? rb + (size_t)ch * n : nullptr;
+            f.map[ch] = grp[ch]->trivial ? nullptr : grp[ch]->d_map;
+        }
+        return launch_adj_finalize3(s, f, k2e, trec, n, FLbar);
+    };
+    cplx* Sbar_in = sigmaOf(h, a.xb);
+    if (update_sigma) {
+        // Σ_out = op(Σin + Σ_U²)[rep] + i (n - 1/2) U
+        CK(launch_adj_assemble(s, sigmaOf(h, a.yb), h->gSig.trivial ? nullptr : h->gSig.d_map, a.SigInb, a.SU2b,
+                               h->nGk, hartree ? 1 : 0, d.U, a.nbar));
+        CK(launch_adj_u2(s, h->GR, h->u2C, a.SU2b, a.u2Rb, a.u2Cb, a.GRb, h->twm, d));
+        CK(launch_adj_sigma(s, h->GR, h->LR, a.SigInb, a.SigRb, a.LRb, a.Lb, a.GRb, h->twm, h->twp, d));
+        // L = symmetrised representatives (K2 groups; slots 0 = pp, 2 = ph)
+        {
+            const cplx* ob[3] = {a.Lb, nullptr, a.Lb + h->n2};
+            const Group* grp[3] = {&h->gK2pp, &h->gK2pp, &h->gK2ph};
+            CK(cudaMemsetAsync(a.raw2, 0, 3 * h->n2 * sizeof(cplx), s));
+            Finalize3 f{};
+            f.raw[0] = ob[0]; f.out[0] = a.raw2; f.map[0] = grp[0]->trivial ? nullptr : grp[0]->d_map;
+            f.raw[2] = ob[2]; f.out[2] = a.raw2 + h->n2; f.map[2] = grp[2]->trivial ? nullptr : grp[2]->d_map;
+            CK(launch_adj_finalize3(s, f, 0, 0, h->n2, nullptr));
+            ChanWork cw{};
+            const Group* g2[2] = {&h->gK2pp, &h->gK2ph};
+            for (int w = 0; w < 2; ++w) {
+                cw.items[w] = g2[w]->trivial ? nullptr : g2[w]->d_items;
+                cw.nitems[w] = g2[w]->trivial ? (int)h->n2 : g2[w]->nitems;
+            }
+            const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
+            CK(launch_adj_sde_L(s, Fn, Yb, B, h->SPi, h->SPi + nS, a.Pbpp, a.Pbph, a.SPib, a.SPib + nS, a.raw2, cw,
+                                h->n2, rs, d));
+        }
+    } else {
+        CK(cudaMemcpyAsync(Sbar_in, sigmaOf(h, a.yb), h->nGk * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    }
+    const int order[3] = {CH_P, CH_A, CH_T};
+    auto Pi = [&](int ch) -> const cplx* { return ch == CH_P ? h->Pipp : h->Piph; };
+    auto Pi0 = [&](int ch) -> const cplx* { return ch == CH_P ? h->Pi0pp : h->Pi0ph; };
+    cplx* cb[10];
+    for (int i = 0; i < 10; ++i) cb[i] = a.cacheb + (size_t)i * h->n3;
+    Caches C{};
+    for (int i = 0; i < 10; ++i) C.c[i] = h->cache + (size_t)i * h->n3;
+    cplx* FL3b[3] = {a.FLK3b, a.FLK3b + h->n3, a.FLK3b + 2 * h->n3};
+    cplx* FL2b[3] = {a.FLK2b, a.FLK2b + h->n2, a.FLK2b + 2 * h->n2};
+    {  // K3 outputs -> representatives -> the K3 GEMM transposed (caches F and Γ, Π, FL.K3)
+        const cplx* ob[3] = {chanK(h, a.yb, CH_P, 3), chanK(h, a.yb, CH_T, 3), chanK(h, a.yb, CH_A, 3)};
+        const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
+        CK(fin_adj(ob, a.raw3, h->n3, grp, 0, 1, nullptr));
+        K3Args3 a3{};
+        const cplx* Ob[3];
+        cplx *Ab[3], *Gb[3], *Mb[3], *Mbb[3];
+        for (int i = 0; i < 3; ++i) {
+            const int ch = order[i];
+            const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
+            const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+            K3Args& k = a3.a[i];
+            k.A = C.c[cf]; k.B0 = C.c[cf0]; k.G = C.c[cg]; k.Pi = Pi(ch); k.Pi0 = Pi0(ch);
+            k.FLc = h->FLK3 + (size_t)ch * h->n3; k.FLt = h->FLK3 + (size_t)CH_T * h->n3;
+            k.FLa = h->FLK3 + (size_t)CH_A * h->n3;
+            a3.ch[i] = ch;
+            Ob[i] = a.raw3 + (size_t)ch * h->n3;
+            Ab[i] = cb[cf];
+            Gb[i] = cb[cg];
+            Mb[i] = a.M + (size_t)i * h->n3;
+            Mbb[i] = a.Mb + (size_t)i * h->n3;
+        }
+        a3.blocks = h->d_k3blocks;
+        a3.nblocks = h->nk3blocks;
+        CK(launch_adj_K3(s, 1, a3, Ob, Ab, Gb, Mb, Mbb, a.Pbpp, a.Pbph, FL3b, d));
+    }
+    {  // K2 outputs (with the FL epilogue) and K2 BSE transposed
+        const cplx* ob[3] = {chanK(h, a.yb, CH_P, 2), chanK(h, a.yb, CH_T, 2), chanK(h, a.yb, CH_A, 2)};
+        const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
+        CK(fin_adj(ob, a.raw2, h->n2, grp, 1, 1, FL2b));
+        CK(launch_adj_K2(s, F, FL, B, h->SX, Xb, FLb, a.Pbpp, a.Pbph, a.SXb, a.raw2, work(2), h->n2, d));
+    }
+    {  // K1
+        const cplx* ob[3] = {chanK(h, a.yb, CH_P, 1), chanK(h, a.yb, CH_T, 1), chanK(h, a.yb, CH_A, 1)};
+        const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
+        CK(fin_adj(ob, a.raw1, h->n1, grp, 0, 1, nullptr));
+        CK(launch_adj_K1(s, F, FL, B, h->SX, Xb, FLb, a.Pbpp, a.Pbph, a.SXb, a.raw1, work(1), h->n1, d));
+    }
+    CK(launch_adj_sx(s, h->Pipp, h->Piph, FL, a.SXb, a.Pbpp, a.Pbph, a.SPib, FLb, d));
+    if (strategy == FDGA_FDPA) {  // FL is iterated only in fdPA
+        {  // FL.K3 = L_K3(Γ caches)
+            const cplx* ob[3] = {FL3b[CH_P], FL3b[CH_T], FL3b[CH_A]};
+            const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
+            CK(fin_adj(ob, a.raw3, h->n3, grp, 0, 1, nullptr));
+            K3Args3 a3{};
+            const cplx* Ob[3];
+            cplx *Ab[3], *Mb[3], *Mbb[3];
+            for (int i = 0; i < 3; ++i) {
+                const int ch = order[i];
+                const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+                K3Args& k = a3.a[i];
+                k.A = C.c[cg]; k.B0 = C.c[cf0]; k.Pi0 = Pi0(ch);
+                a3.ch[i] = ch;
+                Ob[i] = a.raw3 + (size_t)ch * h->n3;
+                Ab[i] = cb[cg];
+                Mb[i] = a.M + (size_t)i * h->n3;
+                Mbb[i] = a.Mb + (size_t)i * h->n3;
+            }
+            a3.blocks = h->d_k3blocks;
+            a3.nblocks = h->nk3blocks;
+            CK(launch_adj_K3(s, 0, a3, Ob, Ab, nullptr, Mb, Mbb, nullptr, nullptr, nullptr, d));
+        }
+        {  // FL.K2 = L_K2(F)
+            const cplx* ob[3] = {FL2b[CH_P], FL2b[CH_T], FL2b[CH_A]};
+            const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
+            CK(fin_adj(ob, a.raw2, h->n2, grp, 0, 1, nullptr));
+            CK(launch_adj_L_K2(s, B, Xb, a.raw2, work(2), h->n2, d));
+        }
+    }
+    {  // caches
+        Caches Cb{};
+        for (int i = 0; i < 10; ++i) Cb.c[i] = cb[i];
+        CK(launch_adj_cache(s, Xb, Cb, h->d_k3blocks, h->nk3blocks, d));
+    }
+    if (update_sigma) {  // bubbles and row sums -> Ḡ(R) -> Ḡ -> Σ̄ (Dyson)
+        CK(launch_adj_bubble(s, h->GR, a.Pbpp, a.Pbph, a.PbRpp, a.PbRph, a.SPib, a.SRb, a.GRb, h->twm, d));
+        CK(launch_fft2(s, a.GRb, a.Gb, d.NG, +1, 1.0 / ((double)d.L * d.L), h->twp, d));
+        if (hartree) CK(launch_adj_occupation(s, a.Gb, a.nbar, d.T, d.Nk, h->nGk));
+        CK(launch_adj_dyson(s, h->G, a.Gb, Sbar_in, h->nGk));
+    }
+    if (d.Nq > 1) {  // momentum averages
+        ChanBarArrays bar{};
+        const size_t per1 = d.N1, per2 = (size_t)d.N2O * d.N2n, per3 = (size_t)d.N3O * d.N3n * d.N3n;
+        for (int c = 0; c < 3; ++c) {
+            const cplx* av = a.avgb + (size_t)c * (per1 + per2 + per3);
+            bar.A1[c] = av; bar.A2[c] = av + per1; bar.A3[c] = av + per1 + per2;
+            bar.K1[c] = Xb.g[c].K1; bar.K2[c] = Xb.g[c].K2; bar.K3[c] = Xb.g[c].K3;
+        }
+        CK(launch_adj_qavg(s, bar, d));
+    }
     return FDGA_OK;
 }
 
@@ -1937,6 +2170,33 @@ int fdga_frule(fdga_handle* h, int strategy, int update_sigma, int compute_hartr
     if ((r = check_device_error(h))) return r;
     CK(launch_gather(h->st, h->tmpS, h->tan.y, h->perm, n));
     CK(cudaMemcpyAsync(Jv, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (y) {
+        CK(launch_gather(h->st, h->tmpS, h->yS, h->perm, n));
+        CK(cudaMemcpyAsync(y, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
+    return FDGA_OK;
+}
+
+int fdga_rrule(fdga_handle* h, int strategy, int update_sigma, int compute_hartree, const double* ybar, double* y,
+               double* xbar, size_t n) {
+    if (!h || !ybar || !xbar) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
+    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA) return fail(h, FDGA_ERR_ARG, "unknown strategy");
+    int r = ensure_adjoint(h);
+    if (r) return r;
+    const int prec0 = h->precision;
+    h->precision = FDGA_FP64;  // the adjoint runs on the FP64 intermediates
+    r = run_iteration(h, strategy, update_sigma != 0, compute_hartree != 0);
+    h->precision = prec0;
+    if (r) return r;
+    CK(cudaMemcpyAsync(h->tmpS, ybar, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
+    CK(launch_scatter(h->st, h->adj.yb, h->tmpS, h->perm, n));  // reference layout -> device layout
+    if ((r = enqueue_adjoint(h, strategy, update_sigma != 0, compute_hartree != 0))) return r;
+    CK(launch_gather(h->st, h->tmpS, h->adj.xb, h->perm, n));
+    CK(cudaMemcpyAsync(xbar, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     if (y) {
         CK(launch_gather(h->st, h->tmpS, h->yS, h->perm, n));

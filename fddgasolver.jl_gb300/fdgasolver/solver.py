@@ -182,6 +182,17 @@ class _Solver:
                                          jv.ctypes.data, v.size))
         return y, jv
 
+    def rrule(self, ybar, strategy="fdPA", update_sigma=True, compute_hartree=True):
+        """(Φ(x), Φ'(x)ᵀ·ȳ) at the current state x from the adjoint kernels (reverse mode), the rrule
+        of one fixed_point! iteration; the transpose is for the real inner product Re Σ conj(a) b."""
+        ybar = np.ascontiguousarray(ybar, dtype=np.complex128)
+        y = np.empty_like(ybar)
+        xbar = np.empty_like(ybar)
+        self._check(self._lib.fdga_rrule(self._h, STRATEGIES[strategy], int(bool(update_sigma)),
+                                         int(bool(compute_hartree)), ybar.ctypes.data, y.ctypes.data,
+                                         xbar.ctypes.data, ybar.size))
+        return y, xbar
+
     def set_U(self, U):
         self._check(self._lib.fdga_set_U(self._h, float(U)))
 

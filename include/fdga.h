@@ -161,6 +161,14 @@ int fdga_jvp(fdga_handle* h, int strategy, const double* v, double* Jv, size_t n
 int fdga_frule(fdga_handle* h, int strategy, int update_sigma, int compute_hartree, const double* v, double* y,
                double* Jv, size_t n);
 
+/* Reverse-mode derivative of one iteration (the rrule): at the current state S = x, y = Φ(x) and
+ * x̄ = Φ'(x)ᵀ ȳ, the transpose for the real inner product <a, b> = Re Σ conj(a) b, so that
+ * <ȳ, Φ'(x) v> = <x̄, v> for every v.  Computed by the hand-written adjoint kernels in FP64 (the
+ * vertex gathers transposed into scatter-adds, the K3 BSE into two batched GEMMs, the bubbles from
+ * G(R) recomputed by the value pass).  Arrays as in fdga_frule (y may be NULL). */
+int fdga_rrule(fdga_handle* h, int strategy, int update_sigma, int compute_hartree, const double* ybar, double* y,
+               double* xbar, size_t n);
+
 /* Bare interaction U of the handle (the RefVertex's bare part, the SDE and Hartree terms); the
  * reference builds a new solver for another U.  Drops the captured graphs. */
 int fdga_set_U(fdga_handle* h, double U);
