@@ -289,7 +289,7 @@ def run_ours(args, rank, world, dist):
     if not args.no_converge:
         conv = {}
         res = {}
-        for mode in ("plain", "mixed", "newton", "newton_mixed"):
+        for mode in ("plain", "mixed", "newton", "newton_mixed", "newton_mixed_differences"):
             cfg2, S2 = build_problem(args.config, "ours")
             x0 = S2.flatten()
             S2.iterate_solver("fdPA")  # captures the iteration graphs outside the timed solves
@@ -301,12 +301,17 @@ def run_ours(args, rank, world, dist):
                 r = S2.solve("fdPA", maxiter=300, tol=1e-8, delta=0.85, mem=8)
                 info = {"iterations": r["iterations"],
                         "method": "Anderson m=8, beta=0.85 (NLsolve restated, device-resident QR), FP64 map"}
-            elif mode in ("newton", "newton_mixed"):
+            elif mode.startswith("newton"):
                 jvp = "fp64" if mode == "newton" else "mixed"
+                tangent = 0 if mode.endswith("differences") else 1
+                S2.set_option("jvp_tangent", tangent)
                 r = S2.solve_newton("fdPA", maxiter=600, tol=1e-8, restart=30, jvp=jvp)
-                info = {"newton_steps": r["newton"], "fp64_maps": r["evals_fp64"], "mixed_maps": r["evals_mixed"],
-                        "method": f"Newton-Krylov: GMRES(30) on (I-J)dx = R with forward-difference JVPs of the "
-                                  f"{jvp} map, Eisenstat-Walker forcing, backtracking on the FP64 residual"}
+                how = ("the hand-written tangent kernels (fdga_frule) of the " if tangent else
+                       "forward differences of the ")
+                info = {"newton_steps": r["newton"], "fp64_maps": r["evals_fp64"],
+                        "mixed_maps_or_tangents": r["evals_mixed"],
+                        "method": f"Newton-Krylov: GMRES(30) on (I-J)dx = R with JVPs from {how}{jvp} map, "
+                                  f"Eisenstat-Walker forcing, backtracking on the FP64 residual"}
             else:
                 r = S2.solve_mixed("fdPA", maxiter=600, tol=1e-8, delta=0.85, mem=8)
                 info = {"fp64_maps": r["evals_fp64"], "mixed_maps": r["evals_mixed"],
@@ -319,7 +324,7 @@ def run_ours(args, rank, world, dist):
             res[mode]["Sigma"] = S2.get("Sigma")
             S2.close()
         import numpy as np
-        for mode in ("mixed", "newton", "newton_mixed"):
+        for mode in ("mixed", "newton", "newton_mixed", "newton_mixed_differences"):
             conv[f"speedup_{mode}_vs_plain"] = conv["plain"]["seconds"] / conv[mode]["seconds"]
             conv[f"{mode}_vs_plain_solution_rel_err"] = {
                 k: float(np.abs(res[mode][k] - res["plain"][k]).max() / np.abs(res["plain"][k]).max())
@@ -335,9 +340,11 @@ def run_ours(args, rank, world, dist):
         iq = (L // 2 + L * (L // 2)) if cfg2["kind"] != "siam" else 0
         v = d[iq * nO + cfg2["nK1"] - 1]
         conv["dchi_m_dU"] = {"value_Omega0_q_pipi": [v.real, v.imag], "seconds": t, **info,
-                             "method": "GMRES(40) on (I-J) dx/dU = dPhi/dU at the converged state, central-difference "
-                                       "JVPs and dPhi/dU (h = 1e-4)"}
+                             "method": "GMRES(40) on (I-J) dx/dU = dPhi/dU at the converged state, JVPs by the "
+                                       "tangent kernels, dPhi/dU by central differences (h = 1e-4)"}
         S2.close()
+    # ---- derivatives of one iteration at this workload: tangent (frule) and adjoint (rrule) ----
+    diff = derivative_report(S, x)
     nstate = S.state_len
     out = {
         "metric": METRIC, "value": ms_dev * 1e-3, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -352,9 +359,52 @@ def run_ours(args, rank, world, dist):
         "time_to_converge": conv,
         "roofline": roofline,
         "precision_mixed_map_vs_fp64": precision,
+        "derivatives": diff,
         "clocks": clk,
     }
     S.close()
+    return out
+
+
+def derivative_report(S, x):
+    """Tangent (fdga_frule) and adjoint (fdga_rrule) of one iteration at x: device time per application
+    of the tangent map (CUDA graph replays) next to the map, the transpose identity <ȳ, J v> = <Jᵀ ȳ, v>,
+    and the tangent against central differences of the FP64 map."""
+    import numpy as np
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size)
+    yb = rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        S.set_precision(prec)
+        S.unflatten(x)
+        _, jv = S.frule(v)
+        S.synchronize()
+        ms = {}
+        for what, f in (("map", S.map_repeat), ("tangent", S.tangent_repeat)):
+            f(3)
+            S.synchronize()
+            S.event_record(0)
+            f(20)
+            S.event_record(1)
+            S.synchronize()
+            ms[what] = S.event_elapsed_ms(0, 1) / 20
+        out[f"{prec}_ms"] = ms
+        if prec == "fp64":
+            j64 = jv
+        else:
+            out["mixed_tangent_rel_err_vs_fp64"] = float(np.abs(jv - j64).max() / np.abs(j64).max())
+    S.set_precision("fp64")
+    S.unflatten(x)
+    t0 = time.perf_counter()
+    _, xb = S.rrule(yb)
+    out["adjoint_host_ms_incl_value_pass_and_copies"] = (time.perf_counter() - t0) * 1e3
+    lhs, rhs = float(np.real(np.vdot(yb, j64))), float(np.real(np.vdot(xb, v)))
+    out["transpose_identity_rel"] = abs(lhs - rhs) / (np.linalg.norm(yb) * np.linalg.norm(j64))
+    h = 1e-6 * max(1.0, float(np.abs(x).max()))
+    d = (S.fixed_point(x + h * v) - S.fixed_point(x - h * v)) / (2 * h) + v
+    out["tangent_vs_central_difference_rel"] = float(np.abs(j64 - d).max() / np.abs(d).max())
+    S.unflatten(x)
     return out
 
 
