@@ -181,11 +181,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
                     } else {
                         const cplxf pi{pis[t][0], pis[t][1]};
                         const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
-                        const float2 qg = __ldg(reinterpret_cast<const float2*>(a.G + ig));
-                        const cplxf gs{qg.x, qg.y};
                         const int ot = cross(CH, m, w - d.n3n);
                         const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                        if (!tM) {
+                        cplxf gs{0.f, 0.f};
+                        if (!(a.flags & K3F_1LOOP)) {
+                            const float2 qg = __ldg(reinterpret_cast<const float2*>(a.G + ig));
+                            gs = cplxf{qg.x, qg.y};
+                        }
+                        if (a.flags & K3F_1LOOP) {
+                            M = ((pi - pi0) * f0) * s1;
+                        } else if (!tM) {
                             M = ((pi - pi0) * f0 + pi * gs) * s1;
                             if (fin(ot, d.n3n)) M += pi * fl_box(a.FLc, a.FLt, a.FLa, CH, il) * s2;
                         } else {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL]

@@ -822,10 +822,12 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
                     } else {
                         const C pi = to_c<C>(ldg(a.Pi + ip));
                         const size_t ig = (CH == CH_P) ? base + (size_t)k * N + col : base + (size_t)col * N + k;
-                        const C gs = ldk<C>(a.G + ig);
+                        const C gs = (a.flags & K3F_1LOOP) ? czero<C>() : ldk<C>(a.G + ig);
                         const int ot = cross(CH, m, o);
                         const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                        if (!tM) {
+                        if (a.flags & K3F_1LOOP) {
+                            v = ((pi - pi0) * f0) * (R)s1;
+                        } else if (!tM) {
                             v = ((pi - pi0) * f0 + pi * gs) * (R)s1;
                             if (fin(ot, d.n3n)) {
                                 const C gl = (CH == CH_T) ? ldk<C>(a.FLt + il) * (R)2 - ldk<C>(a.FLa + il)
@@ -966,6 +968,98 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
         }
         const cplx v = to_d(acc * (R)d.T + accr * (R)(d.T * ref_scale));
         out[idx] = accum ? out[idx] + v : v;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// K1 and K2 of the :fdPA_new / :scPA_new strategies, local solver (src/BSEa/BSEa_K1.jl:57-100,
+// src/BSEa/BSEa_K2.jl:104-150), warp per item:
+//   K1(Ω)   = T s U Σ_ω [F(Ω,∞,ω) Π(Ω,ω) - F0(Ω,∞,ω) Π0(Ω,ω)]
+//   K2(Ω,ν) = T s U Σ_ω [(F(Ω,ν,ω) - F(Ω,∞,ω)) Π - (F0(Ω,ν,ω) - F0(Ω,∞,ω)) Π0],  ω over the bubble mesh.
+// F0(Ω,∞,ω) is U_sp for every ω.  For K1, F(Ω,∞,ω) = F(Ω,∞,∞) = c outside the K2 box, so the sum is
+// c SΠ + Σ_{K2 box} (F - c) Π - U_sp SΠ0.  For K2 the F difference is ω-independent outside the
+// windows of bse_K2_body and the F0 difference vanishes outside the RefVertex box.
+// ---------------------------------------------------------------------------------------------
+template <int CH, class S>
+__device__ __forceinline__ void bse_K1_new_body(const VertPT<S>& F, const cplx* Pi, const cplx* SPi,
+                                                const cplx* SPi0, cplx* out, const int* items, int nitems,
+                                                const Dims& d) {
+    using R = decltype(S::x);
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nitems) return;
+    const int idx = items ? items[w] : w;
+    const int m = idx % d.N1 - (d.n1 - 1), P = idx / d.N1;
+    constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
+    const S c = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    S acc{0, 0};
+    if (bin(m, d.n2O)) {
+        for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
+            if (!fin(n, d.nPw)) continue;
+            acc = cfma(vert_eval(F, d, CH, SP, m, FINF, n, P) - c, to_c<S>(ldg(Pi + ixPi(d, P, m, n))), acc);
+        }
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+        const size_t is = (size_t)P * d.NPO + (m + d.nPO - 1);
+        const S u0 = ref_eval(F, d, CH, SP, m, FINF, FINF);
+        const S v = cfma(c, to_c<S>(SPi[is]), acc) - u0 * to_c<S>(SPi0[is]);
+        out[idx] = to_d(v * (R)(d.U * d.T * (CH == CH_T ? -1.0 : 1.0)));
+    }
+}
+template <int CH, class S>
+__device__ __forceinline__ void bse_K2_new_body(const VertPT<S>& F, const cplx* Pi, const cplx* Pi0, const cplx* SPi,
+                                                cplx* out, const int* items, int nitems, const Dims& d) {
+    using R = decltype(S::x);
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nitems) return;
+    const int idx = items ? items[w] : w;
+    const int nu = idx % d.N2n - d.n2n;
+    const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
+    const int P = idx / (d.N2n * d.N2O);
+    constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
+    const S cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    const S c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
+    const S u0 = ref_eval(F, d, CH, SP, m, FINF, FINF);
+    Windows win;
+    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
+    win.add(-d.n2n, d.n2n - 1, lo, hi);
+    win.add(-d.nRn, d.nRn - 1, lo, hi);
+    win.add(nu - h1, nu + h1, lo, hi);
+    win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
+    if (CH == CH_P) win.add(m - nu - 1 - h1, m - nu - 1 + h1, lo, hi);
+    win.merge();
+    S acc{0, 0};
+    for (int t = lane; t < win.total; t += 32) {
+        const int n = win.at(t);
+        const S Finf = fin(n, d.n2n) ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
+        const S Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
+        const S F0l = ref_eval(F, d, CH, SP, m, nu, n) - u0;
+        const size_t ip = ixPi(d, P, m, n);
+        acc = cfma(Fl, to_c<S>(ldg(Pi + ip)), acc);
+        acc = acc - F0l * to_c<S>(ldg(Pi0 + ip));
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+        const S v = cfma(c, to_c<S>(SPi[(size_t)P * d.NPO + (m + d.nPO - 1)]), acc);
+        out[idx] = to_d(v * (R)(d.U * d.T * (CH == CH_T ? -1.0 : 1.0)));
+    }
+}
+template <class S>
+__global__ void k_bse_K1_new_all(VertPT<S> F, BubbleP B, const cplx* SPi, const cplx* SPi0, ChanWork cw, Dims d) {
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    switch (blockIdx.y) {
+        case CH_P: bse_K1_new_body<CH_P>(F, B.pp, SPi, SPi0, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
+        case CH_T: bse_K1_new_body<CH_T>(F, B.ph, SPi + nS, SPi0 + nS, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
+        default:   bse_K1_new_body<CH_A>(F, B.ph, SPi + nS, SPi0 + nS, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+    }
+}
+template <class S>
+__global__ void k_bse_K2_new_all(VertPT<S> F, BubbleP B, const cplx* SPi, ChanWork cw, Dims d) {
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    switch (blockIdx.y) {
+        case CH_P: bse_K2_new_body<CH_P>(F, B.pp, B.pp0, SPi, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
+        case CH_T: bse_K2_new_body<CH_T>(F, B.ph, B.ph0, SPi + nS, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
+        default:   bse_K2_new_body<CH_A>(F, B.ph, B.ph0, SPi + nS, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
 
@@ -1449,6 +1543,21 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
         k_sde_L_all<ST, true><<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, 1, ref_scale, d, T);           \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }
+#define FDGA_NEW_LAUNCHERS(VT, ST)                                                                                 \
+    cudaError_t launch_bse_K1_new(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,  \
+                                  const ChanWork& cw, const Dims& d) {                                             \
+        k_bse_K1_new_all<ST><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, SPi, SPi0, cw, d);                    \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }                                                                                                               \
+    cudaError_t launch_bse_K2_new(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,  \
+                                  const ChanWork& cw, const Dims& d) {                                             \
+        (void)SPi0;                                                                                                 \
+        k_bse_K2_new_all<ST><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, SPi, cw, d);                          \
+        LAUNCH_CHECK(); return cudaSuccess;                                                                         \
+    }
+FDGA_NEW_LAUNCHERS(VertP, cplx)
+FDGA_NEW_LAUNCHERS(VertPF, cplxf)
+#undef FDGA_NEW_LAUNCHERS
 FDGA_VERTEX_LAUNCHERS(VertP, FLP, TanArgs, cplx)
 FDGA_VERTEX_LAUNCHERS(VertPF, FLPF, TanArgsF, cplxf)
 #undef FDGA_VERTEX_LAUNCHERS

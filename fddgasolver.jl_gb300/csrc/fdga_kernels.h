@@ -48,7 +48,8 @@ struct K3Args {
     const cplx* tFLa;
 };
 // K3Args flags: accumulate into out; leave the γL(ν,ν') epilogue term out; Pi0 == nullptr reads zero
-enum { K3F_ACC = 1, K3F_NOEPI = 2 };
+// K3F_1LOOP: the one-loop form of :fdPA_1loop, M = s1 (Π - Π0) F0 (no Γ and no FL terms)
+enum { K3F_ACC = 1, K3F_NOEPI = 2, K3F_1LOOP = 4 };
 
 struct K3ArgsF {  // FP32 operands of the mixed map (the FP32 caches and FL.K3 copy)
     const cplxf* A;
@@ -172,6 +173,15 @@ cudaError_t launch_sde_L_all(cudaStream_t s, const VertPF& F, const BubbleP& B, 
                              const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d);
 cudaError_t launch_build_cache(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
+// K1 and K2 of the :fdPA_new / :scPA_new strategies (local solver); SPi, SPi0: full-mesh row sums [2][Nq][NΠΩ]
+cudaError_t launch_bse_K1_new(cudaStream_t s, const VertP& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,
+                              const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_K2_new(cudaStream_t s, const VertP& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,
+                              const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_K1_new(cudaStream_t s, const VertPF& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,
+                              const ChanWork& cw, const Dims& d);
+cudaError_t launch_bse_K2_new(cudaStream_t s, const VertPF& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,
+                              const ChanWork& cw, const Dims& d);
 // tangent forms: dK = K(dF; Π, FL, S_X) + K(F; dΠ, dFL, dS_X) in one pass (the T factors), and
 // dL = L(dF; Π, SΠ) + L(F; dΠ, dSΠ) (+ the RefVertex part with dΠ)
 cudaError_t launch_bse_K1_tan(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const cplx* SX,

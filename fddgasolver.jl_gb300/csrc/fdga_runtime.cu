@@ -71,6 +71,7 @@ struct fdga_handle {
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
     int jvp_tangent = 1;                         // GMRES Jacobian products by the tangent kernels (else differences)
+    int newton_cycles = 1;                       // GMRES restart cycles per Newton step
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
     cplx *GR = nullptr, *u2C = nullptr, *u2R = nullptr, *twm = nullptr, *twp = nullptr;
     cplx *SPi = nullptr, *SPi0 = nullptr, *SX = nullptr;  // bubble row sums [2][Nq][NΠΩ]; S_X [3][Nq][NΠΩ]
@@ -86,7 +87,9 @@ struct fdga_handle {
     double n0 = 0.5;
     uint32_t* perm = nullptr;  // reference flatten index -> device index
     Group gSig, gK1, gK2pp, gK2ph, gK3pp, gK3ph, gK3ppL, gK3phL;
-    Graph graphs[2][2][2][2];  // [precision][strategy][update_sigma][hartree]
+    Graph graphs[2][5][2][2];  // [precision][strategy][update_sigma][hartree]
+    cplx* FLzero = nullptr;    // zero FL.K2 (the one-loop BSEs of :fdPA_1loop have no FL factor)
+    cplxf* FLzerof = nullptr;
     int precision = FDGA_FP64;
     int k3_tile[2][2] = {{0, 0}, {0, 0}};  // [precision][mode]: K3 GEMM tile chosen by fdga_autotune (0: default)
     int last_launches = 0;
@@ -202,6 +205,10 @@ cplx* chanK(const fdga_handle* h, cplx* S, int ch, int cls) {
     return cls == 1 ? base : (cls == 2 ? base + h->n1 : base + h->n1 + h->n2);
 }
 cplx* sigmaOf(const fdga_handle* h, cplx* S) { return S + 3 * h->nchan; }
+// the SDE of :fdPA_new and :fdPA_1loop is the fdPA one (src/SDE.jl:3-33)
+bool strategy_fdpa_sde(int strategy) {
+    return strategy == FDGA_FDPA || strategy == FDGA_FDPA_NEW || strategy == FDGA_FDPA_1LOOP;
+}
 
 // ---- reference column-major index <-> device index ----
 size_t dev_index(const Dims& d, int kind, size_t j) {
@@ -527,7 +534,11 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     }
     if (mixed) LC(launch_build_cache(s, Ff, C, h->d_k3blocks, h->nk3blocks, d));
     else LC(launch_build_cache(s, F, C, h->d_k3blocks, h->nk3blocks, d));
-    if (mixed && strategy != FDGA_FDPA) LC(launch_to_f32(s, h->FLK3, h->FLK3f, 3 * h->n3));
+    // strategies that compute FL.K3 (:fdPA, :fdPA_new) write its FP32 copy in the finalize
+    const bool left_K3 = strategy == FDGA_FDPA || strategy == FDGA_FDPA_NEW;
+    const bool is_new = strategy == FDGA_FDPA_NEW || strategy == FDGA_SCPA_NEW;
+    const bool oneloop = strategy == FDGA_FDPA_1LOOP;
+    if (mixed && !left_K3) LC(launch_to_f32(s, h->FLK3, h->FLK3f, 3 * h->n3));
     stage("k3_cache");
     FLP FL;
     for (int c = 0; c < 3; ++c) FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
@@ -558,6 +569,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         }
         return f;
     };
+    // src/solve.jl:26-82: :fdPA computes FL.K2 and FL.K3, :fdPA_new FL.K3 only
     if (strategy == FDGA_FDPA) {
         {  // left K2 (FL.K2): branch C
             if (conc) {
@@ -576,6 +588,8 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             if (conc) CK(cudaEventRecord(h->evC, sC));
         }
         stage("bse_L_K2");
+    }
+    if (left_K3) {
         {  // left K3 (FL.K3)
             K3Args3 a3{};
             K3Args3F a3f{};
@@ -610,24 +624,37 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         CK(cudaStreamWaitEvent(s, h->evB, 0));
         if (strategy == FDGA_FDPA) CK(cudaStreamWaitEvent(s, h->evC, 0));
     }
+    // the one-loop BSEs (:fdPA_1loop) are the fdPA ones without their FL factor
+    FLP FLz = FL;
+    FLPF FLzf = FLf;
+    if (oneloop) {
+        for (int c = 0; c < 3; ++c) {
+            FLz.K2[c] = h->FLzero + (size_t)c * h->n2;
+            FLzf.K2[c] = h->FLzerof + (size_t)c * h->n2;
+        }
+    }
     // ω-sums of the right BSE factor (needs FL.K2 of this iteration)
-    LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FL, h->SX, d));
+    if (!is_new) LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FLz, h->SX, d));
     {  // K1
         ChanWork cw = work(1, h->raw1);
-        if (mixed) LC(launch_bse_K1_all(s, Ff, FLf, B, h->SX, cw, d));
-        else LC(launch_bse_K1_all(s, F, FL, B, h->SX, cw, d));
+        if (is_new && mixed) LC(launch_bse_K1_new(s, Ff, B, h->SPi, h->SPi0, cw, d));
+        else if (is_new) LC(launch_bse_K1_new(s, F, B, h->SPi, h->SPi0, cw, d));
+        else if (mixed) LC(launch_bse_K1_all(s, Ff, FLzf, B, h->SX, cw, d));
+        else LC(launch_bse_K1_all(s, F, FLz, B, h->SX, cw, d));
         cplx* out[3] = {chanK(h, h->yS, CH_P, 1), chanK(h, h->yS, CH_T, 1), chanK(h, h->yS, CH_A, 1)};
         const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
         LC(launch_finalize3(s, fin(1, h->raw1, out, grp), 0, 1, h->n1));
     }
     stage("bse_K1");
-    {  // K2
+    {  // K2 (the _new form has no FL epilogue)
         ChanWork cw = work(2, h->raw2);
-        if (mixed) LC(launch_bse_K2_all(s, Ff, FLf, B, h->SX, cw, d));
-        else LC(launch_bse_K2_all(s, F, FL, B, h->SX, cw, d));
+        if (is_new && mixed) LC(launch_bse_K2_new(s, Ff, B, h->SPi, h->SPi0, cw, d));
+        else if (is_new) LC(launch_bse_K2_new(s, F, B, h->SPi, h->SPi0, cw, d));
+        else if (mixed) LC(launch_bse_K2_all(s, Ff, FLzf, B, h->SX, cw, d));
+        else LC(launch_bse_K2_all(s, F, FLz, B, h->SX, cw, d));
         cplx* out[3] = {chanK(h, h->yS, CH_P, 2), chanK(h, h->yS, CH_T, 2), chanK(h, h->yS, CH_A, 2)};
         const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
-        LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 1, 1, h->n2));
+        LC(launch_finalize3(s, fin(2, h->raw2, out, grp), is_new ? 0 : 1, 1, h->n2));
     }
     stage("bse_K2");
     {  // K3
@@ -641,6 +668,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             a.A = C.c[cf]; a.B0 = C.c[cf0]; a.G = C.c[cg]; a.Pi = Pi(ch); a.Pi0 = Pi0(ch);
             a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3; a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
             a.out = h->raw3 + (size_t)ch * h->n3;
+            a.flags = oneloop ? (K3F_1LOOP | K3F_NOEPI) : 0;  // :fdPA_1loop: T F (Π - Π0) F0 only
             a3.ch[i] = ch;
             if (mixed) {
                 K3ArgsF& af = a3f.a[i];
@@ -648,6 +676,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
                 af.FLc = h->FLK3f + (size_t)ch * h->n3; af.FLt = h->FLK3f + (size_t)CH_T * h->n3;
                 af.FLa = h->FLK3f + (size_t)CH_A * h->n3;
                 af.out = a.out;
+                af.flags = a.flags;
                 a3f.ch[i] = ch;
             }
         }
@@ -678,7 +707,8 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         nl += 2;
         LC(launch_occupation(s, h->G, h->nGk, d.T, d.Nk, h->occ));
         LC(launch_sigma_assemble(s, h->SigIn, h->SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, h->occ, h->C0,
-                                 h->Sig0, SigOut, d.U, hartree ? 1 : 0, strategy == FDGA_FDPA ? 1 : 0, h->n0, h->nGk));
+                                 h->Sig0, SigOut, d.U, hartree ? 1 : 0, strategy_fdpa_sde(strategy) ? 1 : 0, h->n0,
+                                 h->nGk));
     } else {
         LC(cudaMemcpyAsync(SigOut, sigmaOf(h, h->xS), h->nGk * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
     }
@@ -1241,6 +1271,23 @@ int enqueue_adjoint(fdga_handle* h, int strategy, bool update_sigma, bool hartre
     return FDGA_OK;
 }
 
+// Strategies of iterate_solver! (src/solve.jl:10): the _new forms exist for the local solver
+// (src/BSEa/BSEa_K1.jl:57, BSEa_K2.jl:108), the one-loop form for the nonlocal one
+// (src/nonlocal/BSEa/BSE_1loop.jl); elsewhere the reference has no method for them.
+// (also allocates the zero FL of the one-loop form, outside any graph capture)
+int check_strategy(fdga_handle* h, int strategy) {
+    if (strategy < FDGA_FDPA || strategy > FDGA_FDPA_1LOOP) return fail(h, FDGA_ERR_ARG, "unknown strategy");
+    if ((strategy == FDGA_FDPA_NEW || strategy == FDGA_SCPA_NEW) && !h->d.local)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the :fdPA_new / :scPA_new BSEs exist for the local solver only");
+    if (strategy == FDGA_FDPA_1LOOP && h->d.local)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the :fdPA_1loop BSEs exist for the nonlocal solver only");
+    if (strategy == FDGA_FDPA_1LOOP && !h->FLzero) {
+        AL(h->FLzero, 3 * h->n2);
+        AL(h->FLzerof, 3 * h->n2);
+    }
+    return FDGA_OK;
+}
+
 // Constant reference-system part of the fdPA SDE: C0 = SDE(F0, G0, Π0) without Hartree.
 int compute_C0(fdga_handle* h) {
     cudaStream_t s = h->st;
@@ -1264,18 +1311,23 @@ int compute_C0(fdga_handle* h) {
     return FDGA_OK;
 }
 
+template <class A>
+void drop_graph_array(A& gs) {
+    for (auto& p : gs)
+        for (auto& a : p)
+            for (auto& b : a)
+                for (auto& g : b)
+                    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+}
 void drop_graphs(fdga_handle* h) {
-    for (auto* gs : {&h->graphs, &h->tan.graphs})
-        for (auto& p : *gs)
-            for (auto& a : p)
-                for (auto& b : a)
-                    for (auto& g : b)
-                        if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    drop_graph_array(h->graphs);
+    drop_graph_array(h->tan.graphs);
 }
 
 int run_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
     if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
-    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA) return fail(h, FDGA_ERR_ARG, "unknown strategy");
+    int r0 = check_strategy(h, strategy);
+    if (r0) return r0;
     if (h->c0_dirty) {
         int r = compute_C0(h);
         if (r) return r;
@@ -1957,6 +2009,11 @@ int cmax(fdga_handle* h, const cplx* a, double& out) {
     return status;
 }
 
+// tangent-kernel JVPs: on request, for the strategies the tangent map covers
+bool use_tangent(const fdga_handle* h, int strategy) {
+    return h->jvp_tangent && (strategy == FDGA_FDPA || strategy == FDGA_SCPA);
+}
+
 // A v = v − J v at the base point xb (full) for the unit compact FP32 direction v, into w.
 // Tangent kernels (jvp_tangent): J v = Φ'(xb) v; the value intermediates of xb (the last map at xb,
 // in the current precision) are in the handle and the state xS is xb.
@@ -1964,7 +2021,7 @@ int cmax(fdga_handle* h, const cplx* a, double& out) {
 int apply_A(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplxf* v, double eps, bool central,
             cplxf* w, int& nmaps) {
     const size_t n = h->nstate, nc = h->nc;
-    if (h->jvp_tangent) {
+    if (use_tangent(h, strategy)) {
         CK(launch_kc_point(h->st, NBLK_RED, nullptr, v, h->kc_code, 1.0, h->tan.x, n));
         int r = run_tangent(h, strategy, true, true);
         if (r) return r;
@@ -2027,7 +2084,7 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
             double dn = 0.0;
             if ((r = cnorm(h, dx, sc, dn))) return r;
             if (dn == 0.0) break;
-            if (nmaps + (central && !h->jvp_tangent ? 2 : 1) > max_maps) break;
+            if (nmaps + (central && !use_tangent(h, strategy) ? 2 : 1) > max_maps) break;
             CK(launch_kr_load(h->st, NBLK_RED, dx, W, sc, h->kr_part, nc));
             CK(launch_kr_scale(h->st, NBLK_RED, sc, dn, sc, nc));
             if ((r = apply_A(h, strategy, xb, yb, sc, eps, central, w, nmaps))) return r;
@@ -2043,7 +2100,7 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
         int k = 0;
         double est = beta;
         for (int j = 0; j < m; ++j) {
-            if (nmaps + (central && !h->jvp_tangent ? 2 : 1) > max_maps) break;
+            if (nmaps + (central && !use_tangent(h, strategy) ? 2 : 1) > max_maps) break;
             if ((r = apply_A(h, strategy, xb, yb, V.v[j], eps, central, w, nmaps))) return r;
             // classical Gram-Schmidt, twice (weighted inner products)
             CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, W, h->kr_part, -1, nc));
@@ -2159,7 +2216,8 @@ int fdga_frule(fdga_handle* h, int strategy, int update_sigma, int compute_hartr
     if (!h || !v || !Jv) return fail(h, FDGA_ERR_ARG, "null argument");
     if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
     if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
-    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA) return fail(h, FDGA_ERR_ARG, "unknown strategy");
+    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the tangent map covers the fdPA and scPA strategies");
     int r = ensure_tangent(h);
     if (r) return r;
     // value pass at x (leaves the intermediates of the base point in the handle), then the tangent
@@ -2184,7 +2242,8 @@ int fdga_rrule(fdga_handle* h, int strategy, int update_sigma, int compute_hartr
     if (!h || !ybar || !xbar) return fail(h, FDGA_ERR_ARG, "null argument");
     if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
     if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
-    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA) return fail(h, FDGA_ERR_ARG, "unknown strategy");
+    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the adjoint map covers the fdPA and scPA strategies");
     int r = ensure_adjoint(h);
     if (r) return r;
     const int prec0 = h->precision;
@@ -2218,7 +2277,7 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
     const size_t nc = h->nc;
     if (jvp_precision == FDGA_MIXED && (r = ensure_mixed(h))) return r;
     const int prec0 = h->precision;
-    if (h->jvp_tangent) {  // tangent buffers of both precisions used below
+    if (use_tangent(h, strategy)) {  // tangent buffers of both precisions used below
         for (int p : {(int)FDGA_FP64, jvp_precision}) {
             const int keep = h->precision;
             h->precision = p;
@@ -2271,12 +2330,14 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
         ++nouter;
         if (resid < tol) { converged = true; break; }
         if (n64 + nmix + 3 > maxiter) break;
-        // the mixed JVPs' rounding floor stalls Newton on ill-conditioned Jacobians: switch to FP64
-        if (jvp_prec == FDGA_MIXED && nouter > 3 && !(resid < 0.5 * prev)) jvp_prec = FDGA_FP64;
+        // the rounding floor of mixed JVPs by differences stalls Newton on ill-conditioned Jacobians:
+        // switch to FP64 (mixed tangent JVPs carry FP32 rounding only and keep the mixed map)
+        if (!use_tangent(h, strategy) && jvp_prec == FDGA_MIXED && nouter > 3 && !(resid < 0.5 * prev))
+            jvp_prec = FDGA_FP64;
         // forcing term (Eisenstat–Walker choice 2, bounded); the mixed map's rounding floor bounds it below
         double eta = nouter <= 2 ? 0.1 : std::min(0.1, 0.9 * (resid / prev) * (resid / prev));
         // (tangent JVPs of the mixed map carry FP32 rounding, ~1e-6; differences of it ~1e-4)
-        eta = std::max(eta, jvp_prec == FDGA_MIXED ? (h->jvp_tangent ? 1e-5 : 1e-3) : 1e-6);
+        eta = std::max(eta, jvp_prec == FDGA_MIXED ? (use_tangent(h, strategy) ? 1e-5 : 1e-3) : 1e-6);
         // no linear solve beyond what the tolerance asks of this step
         eta = std::min(0.1, std::max(eta, 0.1 * tol / resid));
         if (jvp_prec == FDGA_MIXED) {
@@ -2291,7 +2352,8 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
         const int left = maxiter - n64 - nmix - 1;
         const double eps_rel = jvp_prec == FDGA_MIXED ? 3e-4 : 1e-7;
         // (I − J) dx = F
-        r = gmres_solve(h, strategy, x, yb, F, dx, restart, 1, eta, eps_rel, false, left, nmaps, its, relres);
+        r = gmres_solve(h, strategy, x, yb, F, dx, restart, h->newton_cycles, eta, eps_rel, false, left, nmaps, its,
+                        relres);
         if (r) return r;
         if (h->precision == FDGA_FP64) n64 += nmaps; else nmix += nmaps;
         // backtracking on the FP64 residual
@@ -2363,7 +2425,7 @@ int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int resta
     CK(launch_kc_gather(h->st, NBLK_RED, h->yS, nullptr, h->kc_pos, 1.0, b, nc));
     CK(launch_kr_resid(h->st, NBLK_RED, nullptr, nullptr, 0.0, yp, b, 0.5 / hU, b, nc));  // b = (y+ − y−)/(2h)
     if ((r = fdga_set_U(h, U))) return r;
-    if (h->jvp_tangent) {  // value intermediates at the fixed point for the tangent kernels
+    if (use_tangent(h, strategy)) {  // value intermediates at the fixed point for the tangent kernels
         if ((r = ensure_tangent(h))) return r;
         CK(cudaMemcpyAsync(h->xS, xs, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
         if ((r = run_iteration(h, strategy, true, true))) return r;
@@ -2472,6 +2534,11 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
         h->jvp_tangent = value ? 1 : 0;
         return FDGA_OK;
     }
+    if (k == "newton_gmres_cycles") {
+        if (value < 1 || value > 64) return fail(h, FDGA_ERR_ARG, "newton_gmres_cycles must be in [1, 64]");
+        h->newton_cycles = value;
+        return FDGA_OK;
+    }
     return fail(h, FDGA_ERR_ARG, "unknown option " + k);
 }
 
@@ -2515,6 +2582,12 @@ int stage_times_impl(fdga_handle* h, int strategy, int nrep, char* names, size_t
     if (!h || !ms || !nstages || nrep < 1) return FDGA_ERR_ARG;
     if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
     if (tangent && !h->tan.x) return fail(h, FDGA_ERR_STATE, "fdga_frule has not been called");
+    if (tangent && strategy != FDGA_FDPA && strategy != FDGA_SCPA)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the tangent map covers the fdPA and scPA strategies");
+    {
+        int r = check_strategy(h, strategy);
+        if (r) return r;
+    }
     if (h->c0_dirty) { int r = compute_C0(h); if (r) return r; }
     std::vector<std::string> nm;
     std::vector<double> acc;
@@ -2639,6 +2712,7 @@ int fdga_query(fdga_handle* h, const char* key, double* value) {
 int fdga_autotune(fdga_handle* h, int strategy, int* tiles) {
     if (!h) return FDGA_ERR_ARG;
     if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (int r = check_strategy(h, strategy)) return r;
     if (h->c0_dirty) { int r = compute_C0(h); if (r) return r; }
     if (int r = ensure_mixed(h)) return r;
     // size classes shared by all handles of the process: (Nν3, local, precision) -> (tile L_K3, tile K3)

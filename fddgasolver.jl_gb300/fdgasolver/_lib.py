@@ -87,7 +87,7 @@ EXPORTS = {
     "fdga_launches_per_iteration": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
 }
 
-FDGA_FDPA, FDGA_SCPA = 0, 1
+FDGA_FDPA, FDGA_SCPA, FDGA_FDPA_NEW, FDGA_SCPA_NEW, FDGA_FDPA_1LOOP = 0, 1, 2, 3, 4
 FDGA_FP64, FDGA_MIXED = 0, 1
 IN_GBARE, IN_G0, IN_SIGMA0, IN_FP_P, IN_FP_X, IN_FT_P, IN_FT_X = range(7)
 

@@ -20,7 +20,8 @@ import numpy as np
 from . import _lib
 from .models import hubbard_bare_Green, siam_bare_Green
 
-STRATEGIES = {"fdPA": _lib.FDGA_FDPA, "scPA": _lib.FDGA_SCPA}
+STRATEGIES = {"fdPA": _lib.FDGA_FDPA, "scPA": _lib.FDGA_SCPA, "fdPA_new": _lib.FDGA_FDPA_NEW,
+              "scPA_new": _lib.FDGA_SCPA_NEW, "fdPA_1loop": _lib.FDGA_FDPA_1LOOP}
 
 
 class RefVertex:

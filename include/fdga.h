@@ -30,7 +30,11 @@ enum {
     FDGA_ERR_STATE = 6       /* call order violated (e.g. iterate before finalize) */
 };
 
-enum { FDGA_FDPA = 0, FDGA_SCPA = 1 };          /* iterate_solver! strategy (src/solve.jl:10) */
+/* iterate_solver! strategy (src/solve.jl:10-82): fdPA, scPA; the alternative K1/K2 form
+ * (K = (F Π - F0 Π0) U) of :fdPA_new / :scPA_new, local solver only; the one-loop BSEs of
+ * :fdPA_1loop, nonlocal solver only (FDGA_ERR_UNSUPPORTED elsewhere, where the reference has no
+ * method).  The tangent and adjoint maps cover FDGA_FDPA and FDGA_SCPA. */
+enum { FDGA_FDPA = 0, FDGA_SCPA = 1, FDGA_FDPA_NEW = 2, FDGA_SCPA_NEW = 3, FDGA_FDPA_1LOOP = 4 };
 /* Arithmetic of the iteration map.  FDGA_FP64: every kernel in FP64 (the plain path, parity
  * with the reference).  FDGA_MIXED: the K3 Bethe-Salpeter contractions (the bulk of the work at
  * large boxes) in FP32 arithmetic with FP32 accumulation; storage, Dyson, bubbles, SDE, residual
@@ -106,7 +110,8 @@ int fdga_set_precision(fdga_handle* h, int precision);
  * tensor cores (tcgen05, TF32 hi/lo split, FP32 accumulation) when 2·Nν3 ≤ 256 and Nν3 is a
  * multiple of 8, else as FP32 CUDA-core GEMMs.  "jvp_tangent" (default 1): the GMRES solves of
  * fdga_solve_newton and fdga_dchi_dU apply the Jacobian through the tangent kernels (as
- * fdga_frule); 0: by finite differences of the map. */
+ * fdga_frule); 0: by finite differences of the map.  "newton_gmres_cycles" (default 1): GMRES
+ * restart cycles per Newton step of fdga_solve_newton (more for ill-conditioned fixed points). */
 int fdga_set_option(fdga_handle* h, const char* key, int value);
 
 /* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.

@@ -731,6 +731,134 @@ static void bse_K3(Solver& s, int ch) {
 }
 
 // --------------------------------------------------------------------------------------------
+// Strategy variants.  :fdPA_new / :scPA_new (local solver): the K1 and K2 classes in the form
+// K = (F Π - F0 Π0) U (src/BSEa/BSEa_K1.jl:57-100, src/BSEa/BSEa_K2.jl:104-150, wrappers and the
+// t-channel recombination src/BSE_templates.jl:185-250).  :fdPA_1loop (nonlocal solver): the
+// one-loop BSEs with F0 on the right, K = F (Π - Π0) F0 (src/nonlocal/BSEa/BSE_1loop.jl:1-180,
+// wrappers src/BSE_templates.jl:252-360).  U = bare_vertex(F, Sp) is U for pSp and dSp.
+// --------------------------------------------------------------------------------------------
+static void bse_K1_new(Solver& s, int ch) {
+    const int sp = spin_of(ch);
+    const double sgn = sign_of(ch), T = s.d.T, U = s.d.U;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[0] : s.sgph[0];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    const std::vector<cd>& Pi = (ch == CH_P) ? s.Pipp : s.Piph;
+    sg_eval(G, s.shK1, out.K1.data(), [&](const int* w) -> cd {
+        const int m = w[0], P = (s.Nq == 1) ? 0 : w[1];
+        cd val = 0.0;
+        for (int n = -s.nPn; n < s.nPn; ++n) {
+            const size_t ip = s.iPi(m, n, P);
+            const cd Fl = s.F.eval(ch, sp, m, FINF, n, P);
+            const cd F0l = any_eval(s.F0, ch, sp, m, FINF, n, P);
+            val += (Fl * Pi[ip] - F0l * Pi0[ip]) * U;
+        }
+        return T * val * sgn;
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K1.size(); ++i) out.K1[i] = (out.K1[i] + s.Fbuff.g[CH_A].K1[i]) / 2.0;
+    }
+}
+
+static void bse_K2_new(Solver& s, int ch) {
+    const int sp = spin_of(ch);
+    const double sgn = sign_of(ch), T = s.d.T, U = s.d.U;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[1] : s.sgph[1];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    const std::vector<cd>& Pi = (ch == CH_P) ? s.Pipp : s.Piph;
+    sg_eval(G, s.shK2, out.K2.data(), [&](const int* w) -> cd {
+        const int m = w[0], nu = w[1], P = (s.Nq == 1) ? 0 : w[2];
+        cd val = 0.0;
+        for (int n = -s.nPn; n < s.nPn; ++n) {
+            const size_t ip = s.iPi(m, n, P);
+            const cd Fl = s.F.eval(ch, sp, m, nu, n, P) - s.F.eval(ch, sp, m, FINF, n, P);
+            const cd F0l = any_eval(s.F0, ch, sp, m, nu, n, P) - any_eval(s.F0, ch, sp, m, FINF, n, P);
+            val += (Fl * Pi[ip] - F0l * Pi0[ip]) * U;
+        }
+        return T * val * sgn;
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K2.size(); ++i) out.K2[i] = (out.K2[i] + s.Fbuff.g[CH_A].K2[i]) / 2.0;
+    }
+}
+
+static void bse_K1_1loop(Solver& s, int ch) {
+    const int sp = spin_of(ch);
+    const double sgn = sign_of(ch), T = s.d.T;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[0] : s.sgph[0];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    const std::vector<cd>& Pi = (ch == CH_P) ? s.Pipp : s.Piph;
+    sg_eval(G, s.shK1, out.K1.data(), [&](const int* w) -> cd {
+        const int m = w[0], P = (s.Nq == 1) ? 0 : w[1];
+        cd val = 0.0;
+        for (int n = -s.nPn; n < s.nPn; ++n) {
+            const size_t ip = s.iPi(m, n, P);
+            const cd Fl = s.F.eval(ch, sp, m, FINF, n, P);
+            const cd F0r = any_eval(s.F0, ch, sp, m, cross(ch, m, n), FINF, P);
+            val += Fl * (Pi[ip] - Pi0[ip]) * F0r;
+        }
+        return T * val * sgn;
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K1.size(); ++i) out.K1[i] = (out.K1[i] + s.Fbuff.g[CH_A].K1[i]) / 2.0;
+    }
+}
+
+static void bse_K2_1loop(Solver& s, int ch) {
+    const int sp = spin_of(ch);
+    const double sgn = sign_of(ch), T = s.d.T;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[1] : s.sgph[1];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    const std::vector<cd>& Pi = (ch == CH_P) ? s.Pipp : s.Piph;
+    sg_eval(G, s.shK2, out.K2.data(), [&](const int* w) -> cd {
+        const int m = w[0], nu = w[1], P = (s.Nq == 1) ? 0 : w[2];
+        cd val = 0.0;
+        for (int n = -s.nPn; n < s.nPn; ++n) {
+            const size_t ip = s.iPi(m, n, P);
+            const cd Fl = s.F.eval(ch, sp, m, nu, n, P) - s.F.eval(ch, sp, m, FINF, n, P);
+            const cd F0r = any_eval(s.F0, ch, sp, m, cross(ch, m, n), FINF, P);
+            val += Fl * (Pi[ip] - Pi0[ip]) * F0r;
+        }
+        return T * val * sgn;
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K2.size(); ++i) {
+            out.K2[i] += s.FL.g[CH_T].K2[i] * 2.0;
+            out.K2[i] += s.FL.g[CH_A].K2[i] * -1.0;
+        }
+        for (size_t i = 0; i < out.K2.size(); ++i) out.K2[i] = (out.K2[i] + s.Fbuff.g[CH_A].K2[i]) / 2.0;
+    } else {
+        for (size_t i = 0; i < out.K2.size(); ++i) out.K2[i] += s.FL.g[ch].K2[i];
+    }
+}
+
+static void bse_K3_1loop(Solver& s, int ch) {
+    const double s1 = (ch == CH_A) ? 1.0 : -1.0, T = s.d.T;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[2] : s.sgph[2];
+    const std::vector<cd>& cF = s.cache[ch == CH_P ? C_FP : (ch == CH_A ? C_FA : C_FT)];
+    const std::vector<cd>& cF0 = s.cache[ch == CH_P ? C_F0P : (ch == CH_A ? C_F0A : C_F0T)];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    const std::vector<cd>& Pi = (ch == CH_P) ? s.Pipp : s.Piph;
+    const Chan& K = s.F.g[0];
+    sg_eval(G, s.shK3, out.K3.data(), [&](const int* w) -> cd {
+        const int m = w[0], nu = w[1], nup = w[2], P = (s.Nq == 1) ? 0 : w[3];
+        cd val = 0.0;
+        for (int o = -K.n3n; o < K.n3n; ++o) {
+            const size_t ip = s.iPi(m, o, P);
+            val += cF[K.i3(m, nu, o, P)] * (Pi[ip] - Pi0[ip]) * cF0[K.i3(m, o, nup, P)] * s1;
+        }
+        return T * val;
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K3.size(); ++i) out.K3[i] = (out.K3[i] + s.Fbuff.g[CH_A].K3[i]) / 2.0;
+    }
+}
+
+// --------------------------------------------------------------------------------------------
 // SDE: src/SDE.jl:3-364, src/nonlocal/SDE.jl:3-447
 // --------------------------------------------------------------------------------------------
 // L_pp, L_ph for a vertex (γ contributions only) or for a RefVertex (F - U).
@@ -924,7 +1052,7 @@ static void sde_solver(Solver& s, bool fdpa, bool incH) {
 // --------------------------------------------------------------------------------------------
 // One parquet iteration: src/solve.jl:4-116
 // --------------------------------------------------------------------------------------------
-enum { STRAT_FDPA = 0, STRAT_SCPA = 1 };
+enum { STRAT_FDPA = 0, STRAT_SCPA = 1, STRAT_FDPA_NEW = 2, STRAT_SCPA_NEW = 3, STRAT_FDPA_1LOOP = 4 };
 
 static void iterate(Solver& s, int strategy, bool update_sigma, bool incH) {
     s.F.update_avg();
@@ -933,13 +1061,25 @@ static void iterate(Solver& s, int strategy, bool update_sigma, bool incH) {
         bubbles(s, s.Pipp, s.Piph, s.G);
     }
     build_K3_cache(s);
-    if (strategy == STRAT_FDPA) {
-        bse_L_K2(s, CH_P); bse_L_K2(s, CH_A); bse_L_K2(s, CH_T);
-        bse_L_K3(s, CH_P); bse_L_K3(s, CH_A); bse_L_K3(s, CH_T);
+    // src/solve.jl:26-82
+    if (strategy == STRAT_FDPA_NEW || strategy == STRAT_SCPA_NEW) {
+        if (strategy == STRAT_FDPA_NEW) { bse_L_K3(s, CH_P); bse_L_K3(s, CH_A); bse_L_K3(s, CH_T); }
+        bse_K3(s, CH_P); bse_K3(s, CH_A); bse_K3(s, CH_T);
+        bse_K1_new(s, CH_P); bse_K1_new(s, CH_A); bse_K1_new(s, CH_T);
+        bse_K2_new(s, CH_P); bse_K2_new(s, CH_A); bse_K2_new(s, CH_T);
+    } else if (strategy == STRAT_FDPA_1LOOP) {
+        bse_K3_1loop(s, CH_P); bse_K3_1loop(s, CH_A); bse_K3_1loop(s, CH_T);
+        bse_K1_1loop(s, CH_P); bse_K1_1loop(s, CH_A); bse_K1_1loop(s, CH_T);
+        bse_K2_1loop(s, CH_P); bse_K2_1loop(s, CH_A); bse_K2_1loop(s, CH_T);
+    } else {
+        if (strategy == STRAT_FDPA) {
+            bse_L_K2(s, CH_P); bse_L_K2(s, CH_A); bse_L_K2(s, CH_T);
+            bse_L_K3(s, CH_P); bse_L_K3(s, CH_A); bse_L_K3(s, CH_T);
+        }
+        bse_K1(s, CH_P); bse_K1(s, CH_A); bse_K1(s, CH_T);
+        bse_K2(s, CH_P); bse_K2(s, CH_A); bse_K2(s, CH_T);
+        bse_K3(s, CH_P); bse_K3(s, CH_A); bse_K3(s, CH_T);
     }
-    bse_K1(s, CH_P); bse_K1(s, CH_A); bse_K1(s, CH_T);
-    bse_K2(s, CH_P); bse_K2(s, CH_A); bse_K2(s, CH_T);
-    bse_K3(s, CH_P); bse_K3(s, CH_A); bse_K3(s, CH_T);
     for (int c = 0; c < 3; ++c) {
         s.F.g[c].K1 = s.Fbuff.g[c].K1;
         s.F.g[c].K2 = s.Fbuff.g[c].K2;
@@ -947,7 +1087,8 @@ static void iterate(Solver& s, int strategy, bool update_sigma, bool incH) {
     }
     if (update_sigma) {
         s.F.update_avg();
-        sde_solver(s, strategy == STRAT_FDPA, incH);
+        // src/SDE.jl:3-33: the _new and _1loop variants take the SDE of their base strategy
+        sde_solver(s, strategy == STRAT_FDPA || strategy == STRAT_FDPA_NEW || strategy == STRAT_FDPA_1LOOP, incH);
     }
 }
 

@@ -71,7 +71,7 @@ def max_threads() -> int:
     return int(lib().orc_max_threads())
 
 
-STRATEGIES = {"fdPA": 0, "scPA": 1}
+STRATEGIES = {"fdPA": 0, "scPA": 1, "fdPA_new": 2, "scPA_new": 3, "fdPA_1loop": 4}
 
 
 def _dp(a):
