@@ -313,6 +313,9 @@ cudaError_t launch_sx_tan(cudaStream_t s, const cplx* Pipp, const cplx* Piph, co
 cudaError_t launch_sde_sigma_tan(cudaStream_t s, const cplx* GR, const cplx* LR, const cplx* tGR, const cplx* tLpp,
                                  const cplx* tLph, cplx* tLR, cplx* tSR, cplx* tS, const cplx* twm, const cplx* twp,
                                  const Dims& d);
+// Fourier interpolation between lattice sizes (fdga_interp.cu): kind 0 Σ [k][ν] (frequencies
+// clamped to the source mesh), 1..3 K1, K2, K3 of one channel [P][frequencies] (zero outside it)
+cudaError_t launch_fourier_interp(cudaStream_t s, int kind, const cplx* in, cplx* out, const Dims& o, const Dims& i);
 // reverse-mode (adjoint) stages of the iteration map (fdga_adjoint.cu)
 cudaError_t launch_adj_assemble(cudaStream_t s, const cplx* Sbar, const uint32_t* map, cplx* Sin_bar, cplx* SU2_bar,
                                 size_t n, int hartree, double U, double* nbar);

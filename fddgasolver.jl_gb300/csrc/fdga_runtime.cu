@@ -1591,6 +1591,75 @@ int fdga_finalize(fdga_handle* h) {
     return FDGA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Dyson! and bubbles! (with the full-mesh row sums) of the current state's Σ
+int dyson_bubbles(fdga_handle* h) {
+    const Dims& d = h->d;
+    cudaStream_t s = h->st;
+    const size_t nS = (size_t)d.Nq * d.NPO;
+    CK(launch_dyson(s, h->G, sigmaOf(h, h->xS), h->Gbare, h->nGk));
+    CK(launch_g_realspace(s, h->G, h->GR, h->twm, d));
+    CK(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
+    CK(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + nS, d, h->T0tail));
+    CK(cudaStreamSynchronize(s));
+    return FDGA_OK;
+}
+// symmetrize_solver! (src/ParquetSolver.jl:246-259): every element of a class takes its
+// representative's value under the class operation (Σ and the K1/K2/K3 of the three channels)
+int symmetrize_state(fdga_handle* h) {
+    cudaStream_t s = h->st;
+    CK(cudaMemcpyAsync(h->tmpS, h->xS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    auto sym = [&](const Group& g, size_t off, size_t n) -> cudaError_t {
+        if (g.trivial) return cudaSuccess;
+        Finalize3 f{};
+        f.raw[0] = h->tmpS + off;
+        f.out[0] = h->xS + off;
+        f.map[0] = g.d_map;
+        return launch_finalize3(s, f, 0, 0, n);
+    };
+    CK(sym(h->gSig, 3 * h->nchan, h->nGk));
+    for (int ch = 0; ch < 3; ++ch) {
+        const size_t o = (size_t)ch * h->nchan;
+        CK(sym(h->gK1, o, h->n1));
+        CK(sym(ch == CH_P ? h->gK2pp : h->gK2ph, o + h->n1, h->n2));
+        CK(sym(ch == CH_P ? h->gK3pp : h->gK3ph, o + h->n1 + h->n2, h->n3));
+    }
+    CK(cudaStreamSynchronize(s));
+    return FDGA_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int fdga_dyson_bubbles(fdga_handle* h) {
+    if (!h) return FDGA_ERR_ARG;
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    return dyson_bubbles(h);
+}
+
+int fdga_interpolate_solver(fdga_handle* ho, fdga_handle* hi) {
+    if (!ho || !hi) return fail(ho, FDGA_ERR_ARG, "null handle");
+    if (!ho->finalized || !hi->finalized) return fail(ho, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (ho->d.local || hi->d.local)
+        return fail(ho, FDGA_ERR_UNSUPPORTED, "interpolate_solver! is defined for the nonlocal solver");
+    if (ho->d.T != hi->d.T) return fail(ho, FDGA_ERR_ARG, "the two solvers must share the temperature");
+    if (ho->d.L * ho->d.L != ho->d.Nk || hi->d.L * hi->d.L != hi->d.Nk)
+        return fail(ho, FDGA_ERR_UNSUPPORTED, "Fourier interpolation needs L_G = L");
+    const Dims &o = ho->d, &i = hi->d;
+    fdga_handle* h = ho;  // errors are reported on the target
+    CK(cudaStreamSynchronize(hi->st));
+    cudaStream_t s = ho->st;
+    // src/interpolate.jl:147-191: Σ, then Dyson and bubbles, then the vertex, then symmetrize
+    CK(launch_fourier_interp(s, 0, sigmaOf(hi, hi->xS), sigmaOf(ho, ho->xS), o, i));
+    if (int r = dyson_bubbles(ho)) return r;
+    for (int ch = 0; ch < 3; ++ch)
+        for (int cls = 1; cls <= 3; ++cls)
+            CK(launch_fourier_interp(s, cls, chanK(hi, hi->xS, ch, cls), chanK(ho, ho->xS, ch, cls), o, i));
+    return symmetrize_state(ho);
+}
+
 int fdga_init_sym_grp(fdga_handle* h) {
     if (!h) return FDGA_ERR_ARG;
     std::vector<HostGroup> hg;

@@ -54,6 +54,8 @@ EXPORTS = {
     "fdga_rrule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_set_U": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "fdga_dyson_bubbles": (ctypes.c_int, [ctypes.c_void_p]),
+    "fdga_interpolate_solver": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdga_dchi_dU": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t,
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),

@@ -369,6 +369,28 @@ def unflatten(S, x):
     S.unflatten(x)
 
 
+def dyson_bubbles(S):
+    """Dyson!(S); bubbles!(S) of the current state (src/dyson.jl:5-31, src/bubble.jl)."""
+    S._check(S._lib.fdga_dyson_bubbles(S._h))
+
+
+def interpolate_solver(So, Si, occ_target=None, hubbard_params=None):
+    """interpolate_solver!(So, Si; occ_target, hubbard_params) (src/interpolate.jl:147-191): Σ and
+    the vertex of Si Fourier-interpolated to So's lattice, So's G and bubbles updated and So
+    symmetrized.  With occ_target, μ is then fixed to the occupation (src/dyson.jl:45-58) and Gbare,
+    G and the bubbles follow."""
+    So._check(So._lib.fdga_interpolate_solver(So._h, Si._h))
+    if occ_target is not None:
+        from .models import compute_hubbard_chemical_potential, hubbard_bare_Green
+        hp = dict(hubbard_params or {})
+        sig = So.get("Sigma").reshape(2 * So.nG, So.L * So.L, order="F")
+        mu = compute_hubbard_chemical_potential(occ_target, sig, So.T, So.nG, So.L, **hp)
+        So._set(_lib.IN_GBARE, hubbard_bare_Green(So.T, So.nG, So.L, mu=mu, **hp))
+        dyson_bubbles(So)
+        return mu
+    return None
+
+
 class Batch:
     """Independent solvers iterated together: one CUDA graph launch performs one iterate_solver! of
     every member, the members' kernels running as concurrent graph branches."""

@@ -174,6 +174,17 @@ int fdga_frule(fdga_handle* h, int strategy, int update_sigma, int compute_hartr
 int fdga_rrule(fdga_handle* h, int strategy, int update_sigma, int compute_hartree, const double* ybar, double* y,
                double* xbar, size_t n);
 
+/* Dyson!(S) and bubbles!(S) (src/dyson.jl:5-31, src/bubble.jl) of the current state: G from Σ
+ * and Gbare, then the bubbles and their row sums. */
+int fdga_dyson_bubbles(fdga_handle* h);
+
+/* interpolate_solver!(So, Si) (src/interpolate.jl:147-191) for two nonlocal solvers of equal
+ * temperature: Σ of Si Fourier-interpolated to So's lattice (frequencies clamped to Si's mesh),
+ * Dyson and bubbles of So, K1/K2/K3 of the three channels interpolated per frequency point (zero
+ * outside Si's boxes), then symmetrize_solver!(So).  The occ_target / μ update of the reference
+ * is the caller's: set Gbare and call fdga_dyson_bubbles. */
+int fdga_interpolate_solver(fdga_handle* so, fdga_handle* si);
+
 /* Bare interaction U of the handle (the RefVertex's bare part, the SDE and Hartree terms); the
  * reference builds a new solver for another U.  Drops the captured graphs. */
 int fdga_set_U(fdga_handle* h, double U);
