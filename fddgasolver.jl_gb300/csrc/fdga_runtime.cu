@@ -510,6 +510,10 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             LC(launch_rowsum(sB, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
                              h->T0tail));
         }
+        // the SDE's U² term and the occupation need only G: also on branch B
+        LC(launch_u2(sB, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
+        nl += 2;
+        LC(launch_occupation(sB, h->G, h->nGk, d.T, d.Nk, h->occ));
         stage("dyson_bubble");
     }
     if (conc) CK(cudaEventRecord(h->evB, sB));
@@ -703,9 +707,6 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         }
         LC(launch_sde_sigma(s, h->GR, h->Lpp, h->Lph, h->LR, h->SigR, h->SigIn, h->twm, h->twp, d));
         nl += 3;
-        LC(launch_u2(s, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
-        nl += 2;
-        LC(launch_occupation(s, h->G, h->nGk, d.T, d.Nk, h->occ));
         LC(launch_sigma_assemble(s, h->SigIn, h->SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, h->occ, h->C0,
                                  h->Sig0, SigOut, d.U, hartree ? 1 : 0, strategy_fdpa_sde(strategy) ? 1 : 0, h->n0,
                                  h->nGk));
@@ -804,6 +805,11 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         LC(cudaMemsetAsync(t.Pipp, 0, h->nPi * sizeof(cplx), sB));
         LC(cudaMemsetAsync(t.Piph, 0, h->nPi * sizeof(cplx), sB));
         LC(cudaMemsetAsync(t.SPi, 0, 2 * nS * sizeof(cplx), sB));
+    }
+    if (update_sigma) {  // the U² and occupation tangents need only dG: also on branch B
+        LC(launch_u2_tan(sB, h->GR, h->u2C, t.GR, t.u2C, t.u2R, t.SigU2, h->twp, d));
+        nl += 2;
+        LC(launch_occupation(sB, t.G, h->nGk, d.T, d.Nk, t.occ));  // 1/2 + dn: the Hartree term reads dn
     }
     stage("dyson_bubble");
     if (conc) CK(cudaEventRecord(h->evB, sB));
@@ -1015,9 +1021,6 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         LC(launch_finalize3(s, f, 0, 0, h->n2));
         LC(launch_sde_sigma_tan(s, h->GR, h->LR, t.GR, t.Lpp, t.Lph, t.LR, t.SR, t.SigIn, h->twm, h->twp, d));
         nl += 3;
-        LC(launch_u2_tan(s, h->GR, h->u2C, t.GR, t.u2C, t.u2R, t.SigU2, h->twp, d));
-        nl += 2;
-        LC(launch_occupation(s, t.G, h->nGk, d.T, d.Nk, t.occ));  // 1/2 + dn: the Hartree term reads dn
         LC(launch_sigma_assemble(s, t.SigIn, t.SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, t.occ, nullptr,
                                  nullptr, tSig, d.U, hartree ? 1 : 0, 0, 0.0, h->nGk));
     } else {
