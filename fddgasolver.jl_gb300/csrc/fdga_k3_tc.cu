@@ -15,10 +15,10 @@
 // index: the chunks first stage (dA, M), then (A, dM), into the same accumulator.
 //
 // One CTA of 512 threads per block: rows ν < N of the 128-lane accumulator, 2N ≤ 256 columns.
-// K runs in chunks of 16 ω (32 real k); two shared-memory stages; the threads stage chunk c+1
+// K runs in chunks of CW ω (2·CW real k); two shared-memory stages; the threads stage chunk c+1
 // while the tensor core works on chunk c (tcgen05.commit -> mbarrier).  Shared-memory operands use
 // the no-swizzle K-major canonical layout: 8-row x 16-byte core matrices, K-adjacent core
-// matrices 128 B apart (LBO), 8-row groups 1024 B apart (SBO).  Every wait is bounded; a timeout
+// matrices 128 B apart (LBO), 8-row groups KC·32 = 512 B apart (SBO).  Every wait is bounded; a timeout
 // sets *err and the kernel still releases its tensor memory.
 #include "fdga_kernels.h"
 
@@ -27,8 +27,11 @@ namespace fdga {
 namespace {
 
 constexpr int TC_THREADS = 512;  // 16 warps stage the operands; warps 4q..4q+3 read TMEM lanes 32q..
-constexpr int KC = 32;                      // real K per chunk (16 ω)
-constexpr int A_BYTES = 128 * KC * 4;       // one A operand (hi or lo) of a chunk: 16 KB
+constexpr int KC = 16;                      // real K per chunk
+constexpr int CW = KC / 2;                  // ω per chunk
+constexpr int A_BYTES = 128 * KC * 4;       // one A operand (hi or lo) of a chunk: 8 KB
+// (a chunk of 8 ω keeps a CTA under 113 KB of shared memory, so two CTAs share an SM and hide
+// each other's operand-staging latency; two CTAs use all 512 TMEM columns)
 constexpr uint32_t SPIN_LIMIT = 1u << 22;   // bounded mbarrier polling
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -38,10 +41,10 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 __device__ __forceinline__ uint32_t op_off(int r, int k) {
     return (uint32_t)((((r >> 3) * (KC / 4) + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
 }
-// shared-memory matrix descriptor: start, LBO = 128 B, SBO = 1024 B, fixed 0b001 at bits 46-48,
+// shared-memory matrix descriptor: start, LBO = 128 B, SBO = KC·32 B, fixed 0b001 at bits 46-48,
 // no swizzle
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((KC * 32) >> 4) << 32) |
            (1ull << 46);
 }
 __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo) {
@@ -89,14 +92,14 @@ __device__ __forceinline__ void mma_tf32(uint32_t dt, uint64_t a, uint64_t b, ui
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims d, int* err) {
+__global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims d, int* err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
-    __shared__ float pis[16][6];  // Π(ω), Π0(ω), dΠ(ω) of the chunk (re, im pairs)
+    __shared__ float pis[CW][6];  // Π(ω), Π0(ω), dΠ(ω) of the chunk (re, im pairs)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = d.N3n, NN = 2 * N;
-    const int nchunks = (N + 15) / 16;
+    const int nchunks = (N + CW - 1) / CW;
     const int nck = (MODE == 2 ? 2 : 1) * nchunks;  // mode 2: (dA, M) chunks, then (A, dM) chunks
     const int nb = args.nblocks;
     const int slot = blockIdx.x / nb;
@@ -134,8 +137,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
         uint8_t* Alo = Ahi + A_BYTES;
         uint8_t* Bhi = Alo + A_BYTES;
         uint8_t* Blo = Bhi + B_BYTES;
-        const int w0 = 16 * (tM ? c - nchunks : c);
-        if (tid < 16) {
+        const int w0 = CW * (tM ? c - nchunks : c);
+        if (tid < CW) {
             const int w = w0 + tid;
             float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (w < N) {
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
         __syncthreads();
         // A: (ω pair j, row ν) items, rows fastest so that a quarter warp's 16-byte stores fall in
         // distinct banks; k = 4j..4j+3 holds [Re A(ω), Im A(ω), Re A(ω+1), Im A(ω+1)]
-        for (int e = tid; e < 128 * 8; e += TC_THREADS) {
+        for (int e = tid; e < 128 * (KC / 4); e += TC_THREADS) {
             const int nu = e & 127, j = e >> 7, w = w0 + 2 * j;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (nu < N && w < N) {
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_bse_K3_tc(K3Args3F args, Dims
         // B: (ω pair j, ν') items, ν' fastest (coalesced loads of the cache rows); rows 2ν' and
         // 2ν'+1 of the real form, k = 4j..4j+3: [Re M(ω), −Im M(ω), Re M(ω+1), −Im M(ω+1)] and
         // [Im M(ω), Re M(ω), Im M(ω+1), Re M(ω+1)]
-        for (int e = tid; e < 8 * N; e += TC_THREADS) {
+        for (int e = tid; e < (KC / 4) * N; e += TC_THREADS) {
             const int j = e / N, col = e % N;
             cplxf M2[2];
             for (int h2 = 0; h2 < 2; ++h2) {
