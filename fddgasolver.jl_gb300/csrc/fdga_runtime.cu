@@ -95,7 +95,7 @@ struct fdga_handle {
     int last_launches = 0;
     cudaEvent_t ev[8] = {};
     cudaStream_t st2 = nullptr, st3 = nullptr;                         // branch streams of the iteration
-    cudaEvent_t evfork = nullptr, evA = nullptr, evB = nullptr, evC = nullptr;
+    cudaEvent_t evfork = nullptr, evA = nullptr, evB = nullptr, evC = nullptr, evD = nullptr, evE = nullptr;
     // Anderson
     std::vector<cplx*> aa_buf;
     double* d_part = nullptr;
@@ -637,30 +637,37 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             FLzf.K2[c] = h->FLzerof + (size_t)c * h->n2;
         }
     }
+    // K1 and K2 (branch D) run concurrently with the K3 contraction (main stream); the SDE joins
+    cudaStream_t sD = conc ? h->st3 : s;
+    if (conc) {
+        CK(cudaEventRecord(h->evD, s));
+        CK(cudaStreamWaitEvent(sD, h->evD, 0));
+    }
     // ω-sums of the right BSE factor (needs FL.K2 of this iteration)
-    if (!is_new) LC(launch_sx(s, h->Pipp, h->Piph, h->SPi, h->SPi0, FLz, h->SX, d));
+    if (!is_new) LC(launch_sx(sD, h->Pipp, h->Piph, h->SPi, h->SPi0, FLz, h->SX, d));
     {  // K1
         ChanWork cw = work(1, h->raw1);
-        if (is_new && mixed) LC(launch_bse_K1_new(s, Ff, B, h->SPi, h->SPi0, cw, d));
-        else if (is_new) LC(launch_bse_K1_new(s, F, B, h->SPi, h->SPi0, cw, d));
-        else if (mixed) LC(launch_bse_K1_all(s, Ff, FLzf, B, h->SX, cw, d));
-        else LC(launch_bse_K1_all(s, F, FLz, B, h->SX, cw, d));
+        if (is_new && mixed) LC(launch_bse_K1_new(sD, Ff, B, h->SPi, h->SPi0, cw, d));
+        else if (is_new) LC(launch_bse_K1_new(sD, F, B, h->SPi, h->SPi0, cw, d));
+        else if (mixed) LC(launch_bse_K1_all(sD, Ff, FLzf, B, h->SX, cw, d));
+        else LC(launch_bse_K1_all(sD, F, FLz, B, h->SX, cw, d));
         cplx* out[3] = {chanK(h, h->yS, CH_P, 1), chanK(h, h->yS, CH_T, 1), chanK(h, h->yS, CH_A, 1)};
         const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
-        LC(launch_finalize3(s, fin(1, h->raw1, out, grp), 0, 1, h->n1));
+        LC(launch_finalize3(sD, fin(1, h->raw1, out, grp), 0, 1, h->n1));
     }
     stage("bse_K1");
     {  // K2 (the _new form has no FL epilogue)
         ChanWork cw = work(2, h->raw2);
-        if (is_new && mixed) LC(launch_bse_K2_new(s, Ff, B, h->SPi, h->SPi0, cw, d));
-        else if (is_new) LC(launch_bse_K2_new(s, F, B, h->SPi, h->SPi0, cw, d));
-        else if (mixed) LC(launch_bse_K2_all(s, Ff, FLzf, B, h->SX, cw, d));
-        else LC(launch_bse_K2_all(s, F, FLz, B, h->SX, cw, d));
+        if (is_new && mixed) LC(launch_bse_K2_new(sD, Ff, B, h->SPi, h->SPi0, cw, d));
+        else if (is_new) LC(launch_bse_K2_new(sD, F, B, h->SPi, h->SPi0, cw, d));
+        else if (mixed) LC(launch_bse_K2_all(sD, Ff, FLzf, B, h->SX, cw, d));
+        else LC(launch_bse_K2_all(sD, F, FLz, B, h->SX, cw, d));
         cplx* out[3] = {chanK(h, h->yS, CH_P, 2), chanK(h, h->yS, CH_T, 2), chanK(h, h->yS, CH_A, 2)};
         const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
-        LC(launch_finalize3(s, fin(2, h->raw2, out, grp), is_new ? 0 : 1, 1, h->n2));
+        LC(launch_finalize3(sD, fin(2, h->raw2, out, grp), is_new ? 0 : 1, 1, h->n2));
     }
     stage("bse_K2");
+    if (conc) CK(cudaEventRecord(h->evE, sD));
     {  // K3
         K3Args3 a3{};
         K3Args3F a3f{};
@@ -695,6 +702,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
     }
     stage("bse_K3_finalize");
+    if (conc) CK(cudaStreamWaitEvent(s, h->evE, 0));  // join: K1, K2 (D)
     // SDE (src/SDE.jl:3-33) with the new F
     cplx* SigOut = sigmaOf(h, h->yS);
     if (update_sigma) {
@@ -935,27 +943,34 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         CK(cudaStreamWaitEvent(s, h->evB, 0));
         if (strategy == FDGA_FDPA) CK(cudaStreamWaitEvent(s, h->evC, 0));
     }
-    LC(launch_sx_tan(s, h->Pipp, h->Piph, t.Pipp, t.Piph, t.SPi, FL, tFL, t.SX, d));
+    // dK1 and dK2 (branch D) run concurrently with the K3 tangent (main stream)
+    cudaStream_t sD = conc ? h->st3 : s;
+    if (conc) {
+        CK(cudaEventRecord(h->evD, s));
+        CK(cudaStreamWaitEvent(sD, h->evD, 0));
+    }
+    LC(launch_sx_tan(sD, h->Pipp, h->Piph, t.Pipp, t.Piph, t.SPi, FL, tFL, t.SX, d));
     stage("sx");
     // tangent factors of the fused K1/K2/SDE kernels
     const TanArgs T64{tF, tFL, t.Pipp, t.Piph, t.SX, t.SPi, t.SPi + nS};
     const TanArgsF T32{tFf, tFLf, t.Pipp, t.Piph, t.SX, t.SPi, t.SPi + nS};
     {  // dK1 = K1(dF; Π, FL, S_X) + K1(F; dΠ, dFL, dS_X), one pass
-        if (mixed) LC(launch_bse_K1_tan(s, Ff, FLf, B, h->SX, T32, work(1, h->raw1, 0), d));
-        else LC(launch_bse_K1_tan(s, F, FL, B, h->SX, T64, work(1, h->raw1, 0), d));
+        if (mixed) LC(launch_bse_K1_tan(sD, Ff, FLf, B, h->SX, T32, work(1, h->raw1, 0), d));
+        else LC(launch_bse_K1_tan(sD, F, FL, B, h->SX, T64, work(1, h->raw1, 0), d));
         cplx* out[3] = {chanK(h, t.y, CH_P, 1), chanK(h, t.y, CH_T, 1), chanK(h, t.y, CH_A, 1)};
         const Group* grp[3] = {&h->gK1, &h->gK1, &h->gK1};
-        LC(launch_finalize3(s, fin(1, h->raw1, out, grp), 0, 1, h->n1));
+        LC(launch_finalize3(sD, fin(1, h->raw1, out, grp), 0, 1, h->n1));
     }
     stage("bse_K1");
     {  // dK2 likewise, then the FL epilogue with dFL.K2
-        if (mixed) LC(launch_bse_K2_tan(s, Ff, FLf, B, h->SX, T32, work(2, h->raw2, 0), d));
-        else LC(launch_bse_K2_tan(s, F, FL, B, h->SX, T64, work(2, h->raw2, 0), d));
+        if (mixed) LC(launch_bse_K2_tan(sD, Ff, FLf, B, h->SX, T32, work(2, h->raw2, 0), d));
+        else LC(launch_bse_K2_tan(sD, F, FL, B, h->SX, T64, work(2, h->raw2, 0), d));
         cplx* out[3] = {chanK(h, t.y, CH_P, 2), chanK(h, t.y, CH_T, 2), chanK(h, t.y, CH_A, 2)};
         const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
-        LC(launch_finalize3(s, fin(2, h->raw2, out, grp), 1, 1, h->n2));
+        LC(launch_finalize3(sD, fin(2, h->raw2, out, grp), 1, 1, h->n2));
     }
     stage("bse_K2");
+    if (conc) CK(cudaEventRecord(h->evE, sD));
     {  // dK3 = T (dF·M + F·dM) + dγL: one GEMM over the concatenated inner index (mode 2)
         K3Args3 a3{};
         K3Args3F a3f{};
@@ -994,6 +1009,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
     }
     stage("bse_K3");
+    if (conc) CK(cudaStreamWaitEvent(s, h->evE, 0));  // join: dK1, dK2 (D)
     cplx* tSig = sigmaOf(h, t.y);
     if (update_sigma) {
         const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
@@ -1470,7 +1486,8 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
         fdga_destroy(h);
         return FDGA_ERR_CUDA;
     }
-    for (cudaEvent_t* e : {&h->evfork, &h->evA, &h->evB, &h->evC}) cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+    for (cudaEvent_t* e : {&h->evfork, &h->evA, &h->evB, &h->evC, &h->evD, &h->evE})
+        cudaEventCreateWithFlags(e, cudaEventDisableTiming);
 #define ALC(ptr, n) do { r = dalloc(h, &(ptr), (n)); if (r) return fin_err(r); } while (0)
     ALC(h->Gbare, h->nGk); ALC(h->G0, h->nGk); ALC(h->Sig0, h->nGk); ALC(h->G, h->nGk);
     ALC(h->Pi0pp, h->nPi); ALC(h->Pi0ph, h->nPi); ALC(h->Pipp, h->nPi); ALC(h->Piph, h->nPi);
@@ -1539,7 +1556,7 @@ void fdga_destroy(fdga_handle* h) {
     if (h->flush_buf) cudaFree(h->flush_buf);
     for (void* p : h->allocs) cudaFree(p);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {h->evfork, h->evA, h->evB, h->evC}) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {h->evfork, h->evA, h->evB, h->evC, h->evD, h->evE}) if (e) cudaEventDestroy(e);
     for (cudaStream_t t : {h->st2, h->st3}) if (t) { cudaStreamSynchronize(t); cudaStreamDestroy(t); }
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
