@@ -121,3 +121,31 @@ def test_solve_matches_oracle_trajectory():
     assert r_o["converged"] and r_g["converged"]
     assert r_o["iterations"] == r_g["iterations"]
     assert blockwise_rel_err(cfg, gpu.flatten(), orc.flatten()) < 1e-9
+
+
+@pytest.mark.parametrize("case,e,nK2", [("half_filling", 0.0, (6, 6)), ("doped", 0.5, (7, 6))])
+def test_siam_scpa_reference_golden_on_gpu(case, e, nK2):
+    """The reference's own golden values (test/test_siam_scPA.jl, bubble mesh factor 1) from the
+    device solve! (Anderson m = 8, β = 0.85, tol 1e-4 as the reference), to the 5e-4 that the
+    stopping tolerance allows."""
+    import json
+    import os
+
+    from fdgasolver.solver import parquet_solver_siam_parquet_approximation
+    from test_oracle_golden import _c, _k1_at
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_golden.json")))
+    g = gold[f"siam_scPA_{case}"]
+    T, U, nG, nK1 = 0.1, 1.0, 36, 24
+    S = parquet_solver_siam_parquet_approximation(nG, nK1, nK2, nK2, e=e, Delta=np.pi / 5, D=10.0, T=T, U=U,
+                                                  mPi_factor=1)
+    S.init_sym_grp()
+    r = S.solve("scPA", maxiter=100, tol=1e-4, delta=0.85, mem=8)
+    assert r["converged"]
+    sig = S.get("Sigma")[np.array([-2, -1, 0, 1]) + nG]
+    assert np.max(np.abs(sig - _c(g["Sigma"])) / np.abs(_c(g["Sigma"]))) < 5e-4
+    xs = 2 * np.pi * T * -2 + np.arange(4) * 1.0
+    for ch in "apt":
+        k1 = S.get(f"F.{ch}.K1")
+        v = np.array([_k1_at(k1, x, T, nK1) for x in xs])
+        assert np.max(np.abs(v - _c(g[ch])) / np.abs(_c(g[ch]))) < 5e-4, ch
+    S.close()
