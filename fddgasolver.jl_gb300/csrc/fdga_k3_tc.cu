@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
-    __shared__ float pis[CW][6];  // Π(ω), Π0(ω), dΠ(ω) of the chunk (re, im pairs)
+    __shared__ float pis[128][6];  // Π(ω), Π0(ω), dΠ(ω) of the block (re, im pairs), loaded once
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = d.N3n, NN = 2 * N;
     const int nchunks = (N + CW - 1) / CW;
@@ -116,6 +116,15 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_base))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid < N) {
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const size_t ip = ixPi(d, P, m, tid - d.n3n);
+        const cplx p0 = a.Pi0 ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
+        v[2] = (float)p0.x; v[3] = (float)p0.y;
+        if (MODE >= 1) { const cplx p = ldg(a.Pi + ip); v[0] = (float)p.x; v[1] = (float)p.y; }
+        if (MODE == 2) { const cplx p = ldg(a.tPi + ip); v[4] = (float)p.x; v[5] = (float)p.y; }
+        for (int j = 0; j < 6; ++j) pis[tid][j] = v[j];
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
@@ -138,19 +147,6 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
         uint8_t* Bhi = Alo + A_BYTES;
         uint8_t* Blo = Bhi + B_BYTES;
         const int w0 = CW * (tM ? c - nchunks : c);
-        if (tid < CW) {
-            const int w = w0 + tid;
-            float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (w < N) {
-                const size_t ip = ixPi(d, P, m, w - d.n3n);
-                const cplx p0 = a.Pi0 ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
-                v[2] = (float)p0.x; v[3] = (float)p0.y;
-                if (MODE >= 1) { const cplx p = ldg(a.Pi + ip); v[0] = (float)p.x; v[1] = (float)p.y; }
-                if (tM) { const cplx p = ldg(a.tPi + ip); v[4] = (float)p.x; v[5] = (float)p.y; }
-            }
-            for (int j = 0; j < 6; ++j) pis[tid][j] = v[j];
-        }
-        __syncthreads();
         // A: (ω pair j, row ν) items, rows fastest so that a quarter warp's 16-byte stores fall in
         // distinct banks; k = 4j..4j+3 holds [Re A(ω), Im A(ω), Re A(ω+1), Im A(ω+1)]
         for (int e = tid; e < 128 * (KC / 4); e += TC_THREADS) {
@@ -176,13 +172,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
                 const int t = 2 * j + h2, w = w0 + t;
                 cplxf M{0.f, 0.f};
                 if (w < N) {
-                    const cplxf pi0{pis[t][2], pis[t][3]};
+                    const cplxf pi0{pis[w][2], pis[w][3]};
                     const float2 q0 = __ldg(reinterpret_cast<const float2*>(a.B0 + base + (size_t)w * N + col));
                     const cplxf f0{q0.x, q0.y};
                     if (MODE == 0) {
                         M = pi0 * f0;
                     } else {
-                        const cplxf pi{pis[t][0], pis[t][1]};
+                        const cplxf pi{pis[w][0], pis[w][1]};
                         const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
                         const int ot = cross(CH, m, w - d.n3n);
                         const size_t il = base + (size_t)(ot + d.n3n) * N + col;
@@ -197,7 +193,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
                             M = ((pi - pi0) * f0 + pi * gs) * s1;
                             if (fin(ot, d.n3n)) M += pi * fl_box(a.FLc, a.FLt, a.FLa, CH, il) * s2;
                         } else {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL]
-                            const cplxf tpi{pis[t][4], pis[t][5]};
+                            const cplxf tpi{pis[w][4], pis[w][5]};
                             const float2 qt = __ldg(reinterpret_cast<const float2*>(a.tG + ig));
                             M = (tpi * (f0 + gs) + pi * cplxf{qt.x, qt.y}) * s1;
                             if (fin(ot, d.n3n))
@@ -227,7 +223,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
                              smem_u32(&mbar[st]))
                          : "memory");
         }
-        __syncthreads();
+        // no barrier here: the next chunk writes the other stage, and a stage is rewritten only after
+        // the mbarrier reports the MMAs that read it complete
     }
     // the last chunk of each stage
     if (nck >= 2 && !mbar_wait(smem_u32(&mbar[nck & 1]), ((nck - 2) >> 1) & 1)) ok = false;
