@@ -395,15 +395,18 @@ def derivative_report(S, x):
         else:
             out["mixed_tangent_rel_err_vs_fp64"] = float(np.abs(jv - j64).max() / np.abs(j64).max())
     S.set_precision("fp64")
+    h = 1e-6 * max(1.0, float(np.abs(x).max()))
+    d = (S.fixed_point(x + h * v) - S.fixed_point(x - h * v)) / (2 * h) + v
+    out["tangent_vs_central_difference_rel"] = float(np.abs(j64 - d).max() / np.abs(d).max())
     S.unflatten(x)
+    if x.size > 50_000_000:  # the adjoint's cotangent buffers would not fit beside the state
+        out["adjoint"] = "skipped: its buffers (about 9 state-sized K3 arrays) exceed the HBM left at this size"
+        return out
     t0 = time.perf_counter()
     _, xb = S.rrule(yb)
     out["adjoint_host_ms_incl_value_pass_and_copies"] = (time.perf_counter() - t0) * 1e3
     lhs, rhs = float(np.real(np.vdot(yb, j64))), float(np.real(np.vdot(xb, v)))
     out["transpose_identity_rel"] = abs(lhs - rhs) / (np.linalg.norm(yb) * np.linalg.norm(j64))
-    h = 1e-6 * max(1.0, float(np.abs(x).max()))
-    d = (S.fixed_point(x + h * v) - S.fixed_point(x - h * v)) / (2 * h) + v
-    out["tangent_vs_central_difference_rel"] = float(np.abs(j64 - d).max() / np.abs(d).max())
     S.unflatten(x)
     return out
 

@@ -113,34 +113,40 @@ __global__ void k_bubble_local(const cplx* G, const cplx* tG, cplx* pp, cplx* ph
 //   Π(P) = Σ_R Π(R) e^{+2πi P·R/L}  (bfft).  For L_G = L the ±L/2 half weights of the reference's
 //   R scan sum to one per lattice site, so the scan is one pass over the L x L sites.
 // One CTA = one Ω and a tile of TV fermionic frequencies; shared: Π(R) then the P transform.
-template <bool TAN>
-__global__ void k_bubble_nl(const cplx* GR, const cplx* tGR, cplx* pp, cplx* ph, const cplx* twp, Dims d, int TV) {
-    extern __shared__ cplx sh[];
+// C: arithmetic type (FP64, or FP32 for the mixed map's bubble from the FP32 copy of G(R)); G:
+// storage of G(R).  The twiddles are staged in shared memory in C.
+template <bool TAN, class C, class G>
+__global__ void k_bubble_nl(const G* GR, const G* tGR, cplx* pp, cplx* ph, const cplx* twp, Dims d, int TV) {
+    extern __shared__ __align__(16) unsigned char sh_raw[];
     const int L = d.L, NR = L * L;
-    cplx* A = sh;                     // [2][TV][NR]   (pp, ph) in R
-    cplx* B = sh + 2 * (size_t)TV * NR;  // [2][TV][NR]  after the x transform
+    C* A = reinterpret_cast<C*>(sh_raw);  // [2][TV][NR]   (pp, ph) in R
+    C* B = A + 2 * (size_t)TV * NR;       // [2][TV][NR]  after the x transform
+    C* tw = B + 2 * (size_t)TV * NR;      // [L]
+    for (int j = threadIdx.x; j < L; j += blockDim.x) tw[j] = to_c<C>(twp[j]);
     const int m = blockIdx.y - (d.nPO - 1);
     const int n0 = blockIdx.x * TV - d.nPw;
     for (int e = threadIdx.x; e < TV * NR; e += blockDim.x) {
         const int v = e / NR, R = e % NR;
         const int n = n0 + v;
-        cplx vpp = mk(0, 0), vph = mk(0, 0);
+        C vpp{0, 0}, vph{0, 0};
         if (n < d.nPw) {
             const int Rx = R % L, Ry = R / L;
             const int mR = ((L - Rx) % L) + L * ((L - Ry) % L);
             if (R == 0) {
-                const cplx gn = g_tail(GR, d, 0, n), tn = TAN ? g_box_t<cplx>(tGR, d, 0, n) : gn;
-                vpp = prod2<TAN>(g_tail(GR, d, 0, m - n - 1), TAN ? g_box_t<cplx>(tGR, d, 0, m - n - 1) : gn, gn, tn);
-                vph = prod2<TAN>(g_tail(GR, d, 0, m + n), TAN ? g_box_t<cplx>(tGR, d, 0, m + n) : gn, gn, tn);
+                const C gn = g_tail_t<C>(GR, d, 0, n), tn = TAN ? g_box_t<C>(tGR, d, 0, n) : gn;
+                vpp = prod2<TAN>(g_tail_t<C>(GR, d, 0, m - n - 1), TAN ? g_box_t<C>(tGR, d, 0, m - n - 1) : gn, gn, tn);
+                vph = prod2<TAN>(g_tail_t<C>(GR, d, 0, m + n), TAN ? g_box_t<C>(tGR, d, 0, m + n) : gn, gn, tn);
             } else {
                 const int a = m - n - 1, b = m + n;
                 if (fin(a, d.nG) && fin(n, d.nG)) {
                     const size_t i1 = ixG(d, R, a), i2 = ixG(d, R, n);
-                    vpp = prod2<TAN>(GR[i1], TAN ? tGR[i1] : GR[i1], GR[i2], TAN ? tGR[i2] : GR[i2]);
+                    const C g1 = to_c<C>(GR[i1]), g2 = to_c<C>(GR[i2]);
+                    vpp = prod2<TAN>(g1, TAN ? to_c<C>(tGR[i1]) : g1, g2, TAN ? to_c<C>(tGR[i2]) : g2);
                 }
                 if (fin(b, d.nG) && fin(n, d.nG)) {
                     const size_t i1 = ixG(d, R, b), i2 = ixG(d, mR, n);
-                    vph = prod2<TAN>(GR[i1], TAN ? tGR[i1] : GR[i1], GR[i2], TAN ? tGR[i2] : GR[i2]);
+                    const C g1 = to_c<C>(GR[i1]), g2 = to_c<C>(GR[i2]);
+                    vph = prod2<TAN>(g1, TAN ? to_c<C>(tGR[i1]) : g1, g2, TAN ? to_c<C>(tGR[i2]) : g2);
                 }
             }
         }
@@ -152,9 +158,9 @@ __global__ void k_bubble_nl(const cplx* GR, const cplx* tGR, cplx* pp, cplx* ph,
     for (int e = threadIdx.x; e < 2 * TV * NR; e += blockDim.x) {
         const int row = e / NR, r = e % NR;
         const int Px = r % L, y = r / L;
-        const cplx* a = A + (size_t)row * NR + (size_t)y * L;
-        cplx s = mk(0, 0);
-        for (int x = 0; x < L; ++x) s = cfma(a[x], twp[(Px * x) % L], s);
+        const C* a = A + (size_t)row * NR + (size_t)y * L;
+        C s{0, 0};
+        for (int x = 0; x < L; ++x) s = cfma(a[x], tw[(Px * x) % L], s);
         B[(size_t)row * NR + r] = s;
     }
     __syncthreads();
@@ -166,10 +172,10 @@ __global__ void k_bubble_nl(const cplx* GR, const cplx* tGR, cplx* pp, cplx* ph,
         const int Px = P % L, Py = P / L;
         const int n = n0 + v;
         if (n >= d.nPw) continue;
-        const cplx* b = B + (size_t)(which * TV + v) * NR;
-        cplx s = mk(0, 0);
-        for (int y = 0; y < L; ++y) s = cfma(b[(size_t)y * L + Px], twp[(Py * y) % L], s);
-        (which ? ph : pp)[ixPi(d, P, m, n)] = s;
+        const C* b = B + (size_t)(which * TV + v) * NR;
+        C s{0, 0};
+        for (int y = 0; y < L; ++y) s = cfma(b[(size_t)y * L + Px], tw[(Py * y) % L], s);
+        (which ? ph : pp)[ixPi(d, P, m, n)] = to_d(s);
     }
 }
 
@@ -1312,6 +1318,24 @@ cudaError_t launch_occupation(cudaStream_t s, const cplx* G, size_t n, double T,
 cudaError_t launch_g_realspace(cudaStream_t s, const cplx* G, cplx* GR, const cplx* tw, const Dims& d) {
     return launch_fft2(s, G, GR, d.NG, -1, 1.0 / (d.L * d.L), tw, d);
 }
+// DFT bubble (any L): TV fermion frequencies per CTA, (4 TV L² + L) values of shared memory
+template <bool TAN, class C, class G>
+static cudaError_t launch_bubble_dft(cudaStream_t s, const G* GR, const G* tGR, cplx* pp, cplx* ph, const cplx* twp,
+                                     const Dims& d) {
+    const int NR = d.L * d.L;
+    int tv = 32;
+    while (tv > 1 && (size_t)(4 * tv * NR + d.L) * sizeof(C) > 160 * 1024) tv >>= 1;
+    const size_t shm = (size_t)(4 * tv * NR + d.L) * sizeof(C);
+    static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
+    if (shm > 48 * 1024 && shm > shm_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_bubble_nl<TAN, C, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        if (e != cudaSuccess) return e;
+        shm_set = shm;
+    }
+    dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
+    k_bubble_nl<TAN, C, G><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, twp, d, tv);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
 int bubble_tile(const Dims& d) {
     const int NR = d.L * d.L;
     int tv = 32;
@@ -1346,27 +1370,25 @@ static cudaError_t launch_bubble_fft_f32(cudaStream_t s, const cplxf* GR, const 
     k_bubble_fft<L, cplxf, cplxf, TAN><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, d, tv);
     return cudaGetLastError();
 }
-bool bubble_f32_supported(const Dims& d) {
-    return !d.local && (d.L == 2 || d.L == 4 || d.L == 8 || d.L == 16 || d.L == 32);
-}
+bool bubble_f32_supported(const Dims& d) { return !d.local; }
 template <bool TAN>
 static cudaError_t bubble_f32_t(cudaStream_t s, const cplxf* GRf, const cplxf* tGRf, cplx* pp, cplx* ph,
-                                const Dims& d) {
+                                const cplx* twp, const Dims& d) {
     switch (d.L) {
         case 2: return launch_bubble_fft_f32<2, TAN>(s, GRf, tGRf, pp, ph, d);
         case 4: return launch_bubble_fft_f32<4, TAN>(s, GRf, tGRf, pp, ph, d);
         case 8: return launch_bubble_fft_f32<8, TAN>(s, GRf, tGRf, pp, ph, d);
         case 16: return launch_bubble_fft_f32<16, TAN>(s, GRf, tGRf, pp, ph, d);
         case 32: return launch_bubble_fft_f32<32, TAN>(s, GRf, tGRf, pp, ph, d);
-        default: return cudaErrorInvalidValue;
+        default: return launch_bubble_dft<TAN, cplxf, cplxf>(s, GRf, tGRf, pp, ph, twp, d);
     }
 }
-cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const Dims& d) {
-    return bubble_f32_t<false>(s, GRf, nullptr, pp, ph, d);
+cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const cplx* twp, const Dims& d) {
+    return bubble_f32_t<false>(s, GRf, nullptr, pp, ph, twp, d);
 }
 cudaError_t launch_bubble_f32_tan(cudaStream_t s, const cplxf* GRf, const cplxf* tGRf, cplx* tpp, cplx* tph,
-                                  const Dims& d) {
-    return bubble_f32_t<true>(s, GRf, tGRf, tpp, tph, d);
+                                  const cplx* twp, const Dims& d) {
+    return bubble_f32_t<true>(s, GRf, tGRf, tpp, tph, twp, d);
 }
 
 cudaError_t set_fft_twiddles() {
@@ -1397,16 +1419,7 @@ static cudaError_t bubble_t(cudaStream_t s, const cplx* G, const cplx* tG, const
         case 32: return launch_bubble_fft<32, TAN>(s, GR, tGR, pp, ph, d);
         default: break;
     }
-    const int tv = bubble_tile(d);
-    const size_t shm = (size_t)4 * tv * d.L * d.L * sizeof(cplx);
-    static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
-    if (shm > 48 * 1024 && shm > shm_set) {
-        cudaFuncSetAttribute(k_bubble_nl<TAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        shm_set = shm;
-    }
-    dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
-    k_bubble_nl<TAN><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, twp, d, tv);
-    LAUNCH_CHECK(); return cudaSuccess;
+    return launch_bubble_dft<TAN, cplx, cplx>(s, GR, tGR, pp, ph, twp, d);
 }
 cudaError_t launch_bubble(cudaStream_t s, const cplx* G, const cplx* GR, cplx* pp, cplx* ph, const cplx* twp,
                           const Dims& d) {

@@ -203,7 +203,7 @@ cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const 
                           cplx* S0, cplx* S1, const Dims& d, const cplx* T0, const cplxf* GRf = nullptr);
 cudaError_t launch_tail_const(cudaStream_t s, cplx* T0, const Dims& d);
 bool bubble_f32_supported(const Dims& d);
-cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const Dims& d);
+cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const cplx* twp, const Dims& d);
 cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
                       const FLP& FL, cplx* SX, const Dims& d);
 cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n);
@@ -304,7 +304,7 @@ cudaError_t launch_dyson_tan(cudaStream_t s, cplx* tG, const cplx* G, const cplx
 cudaError_t launch_bubble_tan(cudaStream_t s, const cplx* G, const cplx* tG, const cplx* GR, const cplx* tGR,
                               cplx* tpp, cplx* tph, const cplx* twp, const Dims& d);
 cudaError_t launch_bubble_f32_tan(cudaStream_t s, const cplxf* GRf, const cplxf* tGRf, cplx* tpp, cplx* tph,
-                                  const Dims& d);
+                                  const cplx* twp, const Dims& d);
 cudaError_t launch_rowsum_tan(cudaStream_t s, const cplx* tA0, const cplx* tA1, const cplx* GR, const cplx* tGR,
                               cplx* SRtmp, const cplx* twp, cplx* tS0, cplx* tS1, const Dims& d,
                               const cplxf* GRf = nullptr, const cplxf* tGRf = nullptr);

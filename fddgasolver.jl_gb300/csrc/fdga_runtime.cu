@@ -502,7 +502,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         if (h->precision == FDGA_MIXED && bubble_f32_supported(d)) {
             // mixed map: bubble and its full-mesh row sums in FP32 from an FP32 copy of G(R)
             LC(launch_to_f32(sB, h->GR, h->GRf, h->nGk));
-            LC(launch_bubble_f32(sB, h->GRf, h->Pipp, h->Piph, d));
+            LC(launch_bubble_f32(sB, h->GRf, h->Pipp, h->Piph, h->twp, d));
             LC(launch_rowsum(sB, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + (size_t)d.Nq * d.NPO, d,
                              h->T0tail, h->GRf));
         } else {
@@ -802,7 +802,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         LC(launch_g_realspace(sB, t.G, t.GR, h->twm, d));
         if (mixed && bubble_f32_supported(d)) {
             LC(launch_to_f32(sB, t.GR, t.GRf, h->nGk));
-            LC(launch_bubble_f32_tan(sB, h->GRf, t.GRf, t.Pipp, t.Piph, d));
+            LC(launch_bubble_f32_tan(sB, h->GRf, t.GRf, t.Pipp, t.Piph, h->twp, d));
             LC(launch_rowsum_tan(sB, t.Pipp, t.Piph, h->GR, t.GR, h->SRtmp, h->twp, t.SPi, t.SPi + nS, d, h->GRf,
                                  t.GRf));
         } else {

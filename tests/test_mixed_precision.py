@@ -15,10 +15,13 @@ SMALL_LOCAL = dict(kind="siam", T=0.1, U=1.0, e=0.2, Delta=0.5, D=10.0, nG=16, n
                    mPi_factor=6)
 SMALL_NL = dict(kind="hubbard", T=0.5, U=2.0, mu=0.3, t1=1.0, t2=-0.2, L=4, nG=8, nK1=8, nK2=(3, 3), nK3=(2, 3),
                 mPi_factor=4, refvertex_noise=0.05, seed=7)
+# an odd lattice: the mixed map's FP32 bubble takes the DFT path
+ODD_NL = dict(kind="hubbard", T=0.4, U=1.5, mu=0.1, t1=1.0, L=3, nG=6, nK1=6, nK2=(3, 2), nK3=(2, 2), mPi_factor=3,
+              refvertex_noise=0.05, seed=3)
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("cfg", [SMALL_LOCAL, SMALL_NL], ids=["local", "nl4"])
+@pytest.mark.parametrize("cfg", [SMALL_LOCAL, SMALL_NL, ODD_NL], ids=["local", "nl4", "nl3odd"])
 def test_mixed_map_close_to_fp64(cfg):
     rng = np.random.default_rng(4)
     gpu = make_gpu(cfg, True)

@@ -88,7 +88,7 @@ def test_frule_full_map(cfg, sym, strategy):
     assert np.abs(gpu.flatten() - x).max() == 0.0
 
 
-@pytest.mark.parametrize("cfg", [LOCAL, NL4], ids=["local", "nl4"])
+@pytest.mark.parametrize("cfg", [LOCAL, NL4, NL3], ids=["local", "nl4", "nl3odd"])
 def test_frule_mixed_precision(cfg):
     rng = np.random.default_rng(9)
     orc = make_oracle(cfg, True)
