@@ -1264,6 +1264,14 @@ __global__ void k_residual(const cplx* y, const cplx* x, cplx* fx, cplx* g, doub
     }
     if (threadIdx.x == 0) pmax[blockIdx.x] = red[0];
 }
+// out[i] = y[perm[i]] - x[perm[i]]: the residual of the device-layout states in reference order
+__global__ void k_gather_sub(cplx* out, const cplx* y, const cplx* x, const uint32_t* perm, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) {
+        const uint32_t j = perm[i];
+        out[i] = y[j] - x[j];
+    }
+}
 __global__ void k_sub(cplx* out, const cplx* a, const cplx* b, size_t n) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = a[i] - b[i];
@@ -1704,6 +1712,10 @@ cudaError_t launch_scatter(cudaStream_t s, cplx* dst, const cplx* src, const uin
 cudaError_t launch_residual(cudaStream_t s, const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax,
                             int nblk, size_t n) {
     k_residual<<<nblk, 256, 0, s>>>(y, x, fx, g, beta, pmax, n);
+    LAUNCH_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_gather_sub(cudaStream_t s, cplx* out, const cplx* y, const cplx* x, const uint32_t* perm, size_t n) {
+    k_gather_sub<<<blocks_for(n, 256), 256, 0, s>>>(out, y, x, perm, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_sub(cudaStream_t s, cplx* out, const cplx* a, const cplx* b, size_t n) {

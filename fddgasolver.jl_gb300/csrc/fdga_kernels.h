@@ -239,6 +239,7 @@ cudaError_t launch_scatter(cudaStream_t s, cplx* dst, const cplx* src, const uin
 cudaError_t launch_residual(cudaStream_t s, const cplx* y, const cplx* x, cplx* fx, cplx* g, double beta, double* pmax,
                             int nblk, size_t n);
 cudaError_t launch_sub(cudaStream_t s, cplx* out, const cplx* a, const cplx* b, size_t n);
+cudaError_t launch_gather_sub(cudaStream_t s, cplx* out, const cplx* y, const cplx* x, const uint32_t* perm, size_t n);
 cudaError_t launch_aa_diff(cudaStream_t s, int nblk, cplx* dg, const cplx* g, const cplx* gold, cplx* df,
                            const cplx* fx, const cplx* Qb, cplx* part_out, size_t n);
 cudaError_t launch_aa_mgs(cudaStream_t s, int nblk, cplx* df, const cplx* Qa, const cplx* part_in, cplx* Rentry,

@@ -88,14 +88,23 @@ struct fdga_handle {
     uint32_t* perm = nullptr;  // reference flatten index -> device index
     Group gSig, gK1, gK2pp, gK2ph, gK3pp, gK3ph, gK3ppL, gK3phL;
     Graph graphs[2][5][2][2];  // [precision][strategy][update_sigma][hartree]
+    // fdga_residual on page-locked host buffers: one graph with the copies inside (see residual_graph)
+    struct {
+        Graph g;
+        const void* x = nullptr;
+        void* R = nullptr;
+        int precision = -1, strategy = -1;
+    } rg;
     cplx* FLzero = nullptr;    // zero FL.K2 (the one-loop BSEs of :fdPA_1loop have no FL factor)
     cplxf* FLzerof = nullptr;
     int precision = FDGA_FP64;
+    int fused_residual = 1;  // option "fused_residual": fdga_residual on page-locked buffers as one graph
     int k3_tile[2][2] = {{0, 0}, {0, 0}};  // [precision][mode]: K3 GEMM tile chosen by fdga_autotune (0: default)
     int last_launches = 0;
     cudaEvent_t ev[8] = {};
     cudaStream_t st2 = nullptr, st3 = nullptr;                         // branch streams of the iteration
-    cudaEvent_t evfork = nullptr, evA = nullptr, evB = nullptr, evC = nullptr, evD = nullptr, evE = nullptr;
+    cudaEvent_t evfork = nullptr, evA = nullptr, evB = nullptr, evC = nullptr, evD = nullptr, evE = nullptr,
+                evR = nullptr;
     // Anderson
     std::vector<cplx*> aa_buf;
     double* d_part = nullptr;
@@ -467,9 +476,14 @@ cudaError_t sde_L_pair(fdga_handle* h, const V& F, const BubbleP& B, const cplx*
 }
 
 using StageHook = std::function<void(const char*)>;
+// enqueued on the main stream of a captured iteration: right after branch B (which needs only Σ)
+// has forked, and right after the new vertex is complete (before the SDE)
+struct IterHooks {
+    std::function<int()> after_fork, vertex_done;
+};
 
 int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree, int& nl,
-                      const StageHook& mark = StageHook()) {
+                      const StageHook& mark = StageHook(), const IterHooks* hooks = nullptr) {
     cudaStream_t s = h->st;
     auto stage = [&](const char* name) { if (mark) mark(name); };
     const Dims& d = h->d;
@@ -484,6 +498,10 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     if (conc) {
         CK(cudaEventRecord(h->evfork, s));
         CK(cudaStreamWaitEvent(sB, h->evfork, 0));
+    }
+    if (hooks && hooks->after_fork) {
+        int r = hooks->after_fork();
+        if (r) return r;
     }
     // momentum averages of F (kSW evaluation)
     if (d.Nq > 1) {
@@ -703,6 +721,10 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
     }
     stage("bse_K3_finalize");
     if (conc) CK(cudaStreamWaitEvent(s, h->evE, 0));  // join: K1, K2 (D)
+    if (hooks && hooks->vertex_done) {
+        int r = hooks->vertex_done();
+        if (r) return r;
+    }
     // SDE (src/SDE.jl:3-33) with the new F
     cplx* SigOut = sigmaOf(h, h->yS);
     if (update_sigma) {
@@ -1341,6 +1363,10 @@ void drop_graph_array(A& gs) {
 void drop_graphs(fdga_handle* h) {
     drop_graph_array(h->graphs);
     drop_graph_array(h->tan.graphs);
+    if (h->rg.g.exec) cudaGraphExecDestroy(h->rg.g.exec);
+    h->rg.g = Graph();
+    h->rg.x = nullptr;
+    h->rg.R = nullptr;
 }
 
 int run_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
@@ -1486,7 +1512,7 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
         fdga_destroy(h);
         return FDGA_ERR_CUDA;
     }
-    for (cudaEvent_t* e : {&h->evfork, &h->evA, &h->evB, &h->evC, &h->evD, &h->evE})
+    for (cudaEvent_t* e : {&h->evfork, &h->evA, &h->evB, &h->evC, &h->evD, &h->evE, &h->evR})
         cudaEventCreateWithFlags(e, cudaEventDisableTiming);
 #define ALC(ptr, n) do { r = dalloc(h, &(ptr), (n)); if (r) return fin_err(r); } while (0)
     ALC(h->Gbare, h->nGk); ALC(h->G0, h->nGk); ALC(h->Sig0, h->nGk); ALC(h->G, h->nGk);
@@ -1556,7 +1582,7 @@ void fdga_destroy(fdga_handle* h) {
     if (h->flush_buf) cudaFree(h->flush_buf);
     for (void* p : h->allocs) cudaFree(p);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {h->evfork, h->evA, h->evB, h->evC, h->evD, h->evE}) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {h->evfork, h->evA, h->evB, h->evC, h->evD, h->evE, h->evR}) if (e) cudaEventDestroy(e);
     for (cudaStream_t t : {h->st2, h->st3}) if (t) { cudaStreamSynchronize(t); cudaStreamDestroy(t); }
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
@@ -1758,9 +1784,89 @@ int fdga_iterate(fdga_handle* h, int strategy, int update_sigma, int compute_har
     return check_device_error(h);
 }
 
+bool page_locked(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// fdga_residual as one graph when x and R are page-locked: the host copies become graph nodes that
+// overlap the iteration.  Σ (the last flatten block, stored unpermuted at the end of the device
+// state) is copied first, straight into place, so the Dyson/bubble branch starts while the vertex
+// is still in flight; the vertex part of R = Φ(x) - x is formed and copied back on a side stream
+// while the SDE computes the new Σ.  The state is left at Φ(x), as in the unfused path.
+int residual_graph(fdga_handle* h, int strategy, const double* x, double* R) {
+    int r0 = check_strategy(h, strategy);
+    if (r0) return r0;
+    if (h->c0_dirty) {
+        int r = compute_C0(h);
+        if (r) return r;
+    }
+    auto& rg = h->rg;
+    if (rg.g.exec && (rg.x != x || rg.R != R || rg.precision != h->precision || rg.strategy != strategy)) {
+        cudaGraphExecDestroy(rg.g.exec);
+        rg.g = Graph();
+    }
+    if (!rg.g.exec) {
+        cudaStream_t s = h->st, sE = h->st2;
+        const size_t nv = 3 * h->nchan, nS = h->nGk;
+        const cplx* xh = reinterpret_cast<const cplx*>(x);
+        cplx* Rh = reinterpret_cast<cplx*>(R);
+        IterHooks hk;
+        hk.after_fork = [&]() -> int {
+            CK(cudaMemcpyAsync(h->tmpS, xh, nv * sizeof(cplx), cudaMemcpyHostToDevice, s));
+            CK(launch_scatter(s, h->xS, h->tmpS, h->perm, nv));
+            return FDGA_OK;
+        };
+        hk.vertex_done = [&]() -> int {
+            CK(cudaEventRecord(h->evR, s));
+            CK(cudaStreamWaitEvent(sE, h->evR, 0));
+            CK(launch_gather_sub(sE, h->tmpS, h->yS, h->xS, h->perm, nv));
+            CK(cudaMemcpyAsync(Rh, h->tmpS, nv * sizeof(cplx), cudaMemcpyDeviceToHost, sE));
+            CK(cudaEventRecord(h->evR, sE));
+            return FDGA_OK;
+        };
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int nl = 0, r = FDGA_OK;
+        cudaError_t ee = cudaMemcpyAsync(sigmaOf(h, h->xS), xh + nv, nS * sizeof(cplx), cudaMemcpyHostToDevice, s);
+        if (ee == cudaSuccess) r = enqueue_iteration(h, strategy, true, true, nl, StageHook(), &hk);
+        if (ee == cudaSuccess && !r) ee = launch_sub(s, h->tmpS + nv, sigmaOf(h, h->yS), sigmaOf(h, h->xS), nS);
+        if (ee == cudaSuccess && !r)
+            ee = cudaMemcpyAsync(Rh + nv, h->tmpS + nv, nS * sizeof(cplx), cudaMemcpyDeviceToHost, s);
+        if (ee == cudaSuccess && !r) ee = cudaStreamWaitEvent(s, h->evR, 0);
+        if (ee == cudaSuccess && !r)
+            ee = cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, s);
+        cudaError_t ec = cudaStreamEndCapture(s, &graph);
+        if (r) return r;
+        if (ee != cudaSuccess) {
+            if (ec == cudaSuccess) cudaGraphDestroy(graph);
+            return cuda_fail(h, ee, "residual graph capture");
+        }
+        if (ec != cudaSuccess) return cuda_fail(h, ec, "cudaStreamEndCapture");
+        ee = cudaGraphInstantiate(&rg.g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ee != cudaSuccess) { rg.g.exec = nullptr; return cuda_fail(h, ee, "cudaGraphInstantiate"); }
+        rg.g.nodes = nl + 3;  // + scatter, gather-sub, sub
+        rg.x = x;
+        rg.R = R;
+        rg.precision = h->precision;
+        rg.strategy = strategy;
+    }
+    CK(cudaGraphLaunch(rg.g.exec, h->st));
+    h->last_launches = rg.g.nodes;
+    CK(cudaStreamSynchronize(h->st));
+    return check_device_error(h);
+}
+
 int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size_t n) {
     if (!h || !x || !R) return fail(h, FDGA_ERR_ARG, "null argument");
     if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (h->fused_residual && page_locked(x) && page_locked(R)) return residual_graph(h, strategy, x, R);
     CK(cudaMemcpyAsync(h->tmpS, x, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
     CK(launch_scatter(h->st, h->xS, h->tmpS, h->perm, n));
     int r = run_iteration(h, strategy, true, true);
@@ -2621,6 +2727,10 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
     }
     if (k == "jvp_tangent") {
         h->jvp_tangent = value ? 1 : 0;
+        return FDGA_OK;
+    }
+    if (k == "fused_residual") {
+        h->fused_residual = value ? 1 : 0;
         return FDGA_OK;
     }
     if (k == "newton_gmres_cycles") {

@@ -111,11 +111,15 @@ int fdga_set_precision(fdga_handle* h, int precision);
  * multiple of 8, else as FP32 CUDA-core GEMMs.  "jvp_tangent" (default 1): the GMRES solves of
  * fdga_solve_newton and fdga_dchi_dU apply the Jacobian through the tangent kernels (as
  * fdga_frule); 0: by finite differences of the map.  "newton_gmres_cycles" (default 1): GMRES
- * restart cycles per Newton step of fdga_solve_newton (more for ill-conditioned fixed points). */
+ * restart cycles per Newton step of fdga_solve_newton (more for ill-conditioned fixed points).
+ * "fused_residual" (default 1): fdga_residual on page-locked x and R runs as one CUDA graph whose
+ * host copies overlap the iteration; 0: copy, iterate and copy back in sequence. */
 int fdga_set_option(fdga_handle* h, const char* key, int value);
 
 /* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.
- * x and R are host arrays of fdga_state_len elements. */
+ * x and R are host arrays of fdga_state_len elements.  When both are page-locked (cudaHostAlloc,
+ * cudaHostRegister) the copies run inside the iteration's graph, overlapped with it; the graph is
+ * kept for the last (x, R, precision, strategy) seen. */
 int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size_t n);
 
 /* solve!(S; maxiter, tol, δ, mem) (src/solve.jl:160-196): Anderson acceleration (NLsolve
