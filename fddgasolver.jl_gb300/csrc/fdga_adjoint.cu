@@ -327,7 +327,7 @@ __global__ void k_adj_sde_L(VertP F, VertBar Fb, BubbleP B, const cplx* SPpp, co
     else adj_sde_L_body<1>(F, Fb, B.ph, SPph, Pbph, SPbph, rawbar + cw.nitems[2], cw.items[1], cw.nitems[1], rs, d);
 }
 
-// ---- K1 / K2 BSE (bse_K1_body, bse_K2_body), transposed ----
+// ---- K1 / K2 BSE (bse_K1_body, bse_K2_row), transposed ----
 template <int CH>
 __device__ void adj_K1_body(const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0, const cplx* SX,
                             const VertBar& Fb, const FLBar& FLb, cplx* Pibar, cplx* SXbar, const cplx* rawbar,

@@ -162,29 +162,36 @@ __device__ __forceinline__ S k3v(const ChanPT<S>& c, const Dims& d, int m, int n
 }
 
 // Channel evaluator γ(Ω, ν, ν', P): src/channel.jl:220-339, src/nonlocal/channel.jl:246-382.
+// chan_val writes the value into t and returns true, or returns false (t untouched) where the
+// channel vanishes (Ω outside the K1 box).  The sums start from their first term: GB300's FP64
+// pipe is the bound of every evaluator-heavy kernel, and an addition of zero costs as much as any.
 template <class S>
-__device__ __forceinline__ S chan_eval(const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
-    S v{0, 0};
+__device__ __forceinline__ bool chan_val(S& t, const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
+    if (!bin(m, d.n1)) return false;
+    t = k1v(c, d, m, P);
+    if (!bin(m, d.n2O)) return true;
     const bool ninf = (n == FINF), npinf = (np == FINF);
-    if (!bin(m, d.n1)) return v;
-    v += k1v(c, d, m, P);
-    if (!bin(m, d.n2O)) return v;
     if (!ninf && !npinf) {
         const bool a = fin(n, d.n2n), b = fin(np, d.n2n);
         if (a && b) {
-            v += k2v(c, d, m, n, P) + k2v(c, d, m, np, P);
-            if (bin(m, d.n3O) && fin(n, d.n3n) && fin(np, d.n3n)) v += k3v(c, d, m, n, np, P);
+            t += k2v(c, d, m, n, P) + k2v(c, d, m, np, P);
+            if (bin(m, d.n3O) && fin(n, d.n3n) && fin(np, d.n3n)) t += k3v(c, d, m, n, np, P);
         } else if (a) {
-            v += k2v(c, d, m, n, P);
+            t += k2v(c, d, m, n, P);
         } else if (b) {
-            v += k2v(c, d, m, np, P);
+            t += k2v(c, d, m, np, P);
         }
     } else if (ninf && !npinf) {
-        if (fin(np, d.n2n)) v += k2v(c, d, m, np, P);
+        if (fin(np, d.n2n)) t += k2v(c, d, m, np, P);
     } else if (!ninf && npinf) {
-        if (fin(n, d.n2n)) v += k2v(c, d, m, n, P);
+        if (fin(n, d.n2n)) t += k2v(c, d, m, n, P);
     }
-    return v;
+    return true;
+}
+template <class S>
+__device__ __forceinline__ S chan_eval(const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
+    S t;
+    return chan_val(t, c, d, m, n, np, P) ? t : S{0, 0};
 }
 
 // Frequency conversion between channel representations (src/convention.jl:4-36).
@@ -202,36 +209,48 @@ __device__ __forceinline__ void conv(int from, int to, int m, int n, int np, int
     }
 }
 
-// RefVertex corrections: MeshFunction call, zero outside the box.
+// RefVertex corrections: MeshFunction call; false (r untouched) outside the box, where they vanish.
+template <class S>
+__device__ __forceinline__ bool ref_val(S& r, const S* f, const Dims& d, int m, int n, int np) {
+    if (!bin(m, d.nRO) || !fin(n, d.nRn) || !fin(np, d.nRn)) return false;
+    r = ldv(f + (size_t)(m + d.nRO - 1) + (size_t)d.NRO * ((size_t)(n + d.nRn) + (size_t)d.NRn * (np + d.nRn)));
+    return true;
+}
 template <class S>
 __device__ __forceinline__ S ref_call(const S* f, const Dims& d, int m, int n, int np) {
-    if (!bin(m, d.nRO) || !fin(n, d.nRn) || !fin(np, d.nRn)) return S{0, 0};
-    return ldv(f + (size_t)(m + d.nRO - 1) + (size_t)d.NRO * ((size_t)(n + d.nRn) + (size_t)d.NRn * (np + d.nRn)));
+    S r;
+    return ref_val(r, f, d, m, n, np) ? r : S{0, 0};
 }
-// RefVertex in the parallel spin component (src/refvertex.jl:90-125, 178-216).
+// RefVertex in the parallel spin component (src/refvertex.jl:90-125, 178-216): U + correction
+// (only the real part carries U).
 template <class S>
 __device__ __forceinline__ S ref_pSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np) {
+    using R = decltype(S::x);
     if (F.noref) return S{0, 0};
-    if (n == FINF || np == FINF) return cre<S>(d.U);
-    if (ch == CH_P) return ref_call(F.Fp_p, d, m, n, np) + cre<S>(d.U);
-    if (ch == CH_T) return ref_call(F.Ft_p, d, m, n, np) + cre<S>(d.U);
-    return cre<S>(d.U) - ref_call(F.Ft_x, d, m, np, n);
+    const R U = (R)d.U;
+    if (n == FINF || np == FINF) return S{U, 0};
+    S r;
+    if (ch == CH_A) return ref_val(r, F.Ft_x, d, m, np, n) ? S{U - r.x, -r.y} : S{U, 0};
+    return ref_val(r, ch == CH_P ? F.Fp_p : F.Ft_p, d, m, n, np) ? S{r.x + U, r.y} : S{U, 0};
 }
-// RefVertex in the crossed spin component (src/refvertex.jl:127-164).
+// RefVertex in the crossed spin component (src/refvertex.jl:127-164): -U + correction.
 template <class S>
 __device__ __forceinline__ S ref_xSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np) {
+    using R = decltype(S::x);
     if (F.noref) return S{0, 0};
-    if (n == FINF || np == FINF) return cre<S>(-d.U);
-    if (ch == CH_P) return ref_call(F.Fp_x, d, m, n, np) - cre<S>(d.U);
-    if (ch == CH_T) return ref_call(F.Ft_x, d, m, n, np) - cre<S>(d.U);
-    return -ref_call(F.Ft_p, d, m, np, n) - cre<S>(d.U);
+    const R U = (R)d.U;
+    if (n == FINF || np == FINF) return S{-U, 0};
+    S r;
+    if (ch == CH_A) return ref_val(r, F.Ft_p, d, m, np, n) ? S{-r.x - U, -r.y} : S{-U, 0};
+    return ref_val(r, ch == CH_P ? F.Fp_x : F.Ft_x, d, m, n, np) ? S{r.x - U, r.y} : S{-U, 0};
 }
 template <class S>
 __device__ __forceinline__ S ref_eval(const VertPT<S>& F, const Dims& d, int ch, int sp, int m, int n, int np) {
     using R = decltype(S::x);
     if (sp == SP_P) return ref_pSp(F, d, ch, m, n, np);
     if (sp == SP_X) return ref_xSp(F, d, ch, m, n, np);
-    return ref_pSp(F, d, ch, m, n, np) * (R)2 + ref_xSp(F, d, ch, m, n, np);
+    const S p = ref_pSp(F, d, ch, m, n, np), x = ref_xSp(F, d, ch, m, n, np);
+    return S{fma(p.x, (R)2, x.x), fma(p.y, (R)2, x.y)};  // 2p is exact: one rounding, as 2p + x
 }
 
 // Flags of the vertex evaluator: bit 0 F0, bit 1 γp, bit 2 γt, bit 3 γa.
@@ -241,29 +260,42 @@ __device__ __forceinline__ int swap_ta(int fl) {
 }
 
 // Vertex in the parallel spin component with momenta (P, kSW, kSW):
-// src/vertex.jl:209-284, src/nonlocal/vertex.jl:69-153, 216-379.
+// src/vertex.jl:209-284, src/nonlocal/vertex.jl:69-153, 216-379.  Terms are summed in the order
+// F0, γp, γt, γa; the first present term is assigned, not added to zero.
 template <class S>
 __device__ __forceinline__ S vert_pSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
-    S v{0, 0};
-    if (fl & FL_F0) v += ref_pSp(F, d, ch, m, n, np);
+    S v{0, 0}, t;
+    bool has = false;
+    auto put = [&](const S& x) {
+        if (has) v += x;
+        else { v = x; has = true; }
+    };
+    if (fl & FL_F0) {  // (zero for a tangent vertex; kept so that `has` is known at compile time)
+        v = ref_pSp(F, d, ch, m, n, np);
+        has = true;
+    }
     if (n == FINF || np == FINF) {
         const int bit = (ch == CH_P) ? FL_GP : (ch == CH_T ? FL_GT : FL_GA);
-        if (fl & bit) v += chan_eval(F.g[ch], d, m, n, np, P);
+        if ((fl & bit) && chan_val(t, F.g[ch], d, m, n, np, P)) put(t);
         return v;
     }
     const int Pc = (d.Nq == 1) ? 0 : KAVG;
-    if (fl & FL_GP) { int a, b, c; conv(ch, CH_P, m, n, np, a, b, c); v += chan_eval(F.g[CH_P], d, a, b, c, ch == CH_P ? P : Pc); }
-    if (fl & FL_GT) { int a, b, c; conv(ch, CH_T, m, n, np, a, b, c); v += chan_eval(F.g[CH_T], d, a, b, c, ch == CH_T ? P : Pc); }
-    if (fl & FL_GA) { int a, b, c; conv(ch, CH_A, m, n, np, a, b, c); v += chan_eval(F.g[CH_A], d, a, b, c, ch == CH_A ? P : Pc); }
+    if (fl & FL_GP) { int a, b, c; conv(ch, CH_P, m, n, np, a, b, c); if (chan_val(t, F.g[CH_P], d, a, b, c, ch == CH_P ? P : Pc)) put(t); }
+    if (fl & FL_GT) { int a, b, c; conv(ch, CH_T, m, n, np, a, b, c); if (chan_val(t, F.g[CH_T], d, a, b, c, ch == CH_T ? P : Pc)) put(t); }
+    if (fl & FL_GA) { int a, b, c; conv(ch, CH_A, m, n, np, a, b, c); if (chan_val(t, F.g[CH_A], d, a, b, c, ch == CH_A ? P : Pc)) put(t); }
     return v;
 }
-// Crossed component via crossing symmetry (src/vertex.jl:288-313).
+// Crossed component via crossing symmetry (src/vertex.jl:288-313): xSp = -xneg.
+template <class S>
+__device__ __forceinline__ S vert_xneg(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
+    const int sw = swap_ta(fl);
+    if (ch == CH_P) return vert_pSp(F, d, CH_P, m, n, (np == FINF) ? FINF : m - np - 1, P, sw);
+    if (ch == CH_T) return vert_pSp(F, d, CH_A, m, n, np, P, sw);
+    return vert_pSp(F, d, CH_T, m, n, np, P, sw);
+}
 template <class S>
 __device__ __forceinline__ S vert_xSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P, int fl) {
-    const int sw = swap_ta(fl);
-    if (ch == CH_P) return -vert_pSp(F, d, CH_P, m, n, (np == FINF) ? FINF : m - np - 1, P, sw);
-    if (ch == CH_T) return -vert_pSp(F, d, CH_A, m, n, np, P, sw);
-    return -vert_pSp(F, d, CH_T, m, n, np, P, sw);
+    return -vert_xneg(F, d, ch, m, n, np, P, fl);
 }
 template <class S>
 __device__ __forceinline__ S vert_eval(const VertPT<S>& F, const Dims& d, int ch, int sp, int m, int n, int np, int P,
@@ -271,8 +303,38 @@ __device__ __forceinline__ S vert_eval(const VertPT<S>& F, const Dims& d, int ch
     using R = decltype(S::x);
     if (sp == SP_P) return vert_pSp(F, d, ch, m, n, np, P, fl);
     if (sp == SP_X) return vert_xSp(F, d, ch, m, n, np, P, fl);
-    S v = vert_pSp(F, d, ch, m, n, np, P, fl) * (R)2;
-    v += vert_xSp(F, d, ch, m, n, np, P, fl);
+    const S p = vert_pSp(F, d, ch, m, n, np, P, fl), x = vert_xneg(F, d, ch, m, n, np, P, fl);
+    return S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};  // 2 pSp + xSp, 2p exact: one rounding
+}
+
+// F(Ω,ν,ω) - F(Ω,∞,ω) - F(Ω,ν,∞) + F(Ω,∞,∞) of the spin-parallel vertex in representation ch
+// (the vertex factor of the K2 BSE, src/BSEa/BSEa_K2.jl:43-103).  With ν or ω at infinity only the
+// RefVertex's U and the own channel's K1 and K2 terms survive, and those cancel in the difference,
+// which is therefore [F0(Ω,ν,ω) - U] + K3_ch(Ω,ν,ω) + Σ_{c ≠ ch} γ_c(conv(Ω,ν,ω)): the
+// RefVertex correction, the own channel's K3 and the other two channels, each added only inside
+// its box.  Same value as the four evaluations up to rounding, at a fraction of the FP64 work.
+template <class S>
+__device__ __forceinline__ S pSp_k2diff(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P) {
+    S v{0, 0}, t;
+    bool has = false;
+    auto put = [&](const S& x) {
+        if (has) v += x;
+        else { v = x; has = true; }
+    };
+    if (!F.noref) {
+        if (ch == CH_A) {
+            if (ref_val(t, F.Ft_x, d, m, np, n)) put(-t);
+        } else if (ref_val(t, ch == CH_P ? F.Fp_p : F.Ft_p, d, m, n, np)) {
+            put(t);
+        }
+    }
+    if (bin(m, d.n1) && bin(m, d.n2O) && fin(n, d.n2n) && fin(np, d.n2n) && bin(m, d.n3O) && fin(n, d.n3n) &&
+        fin(np, d.n3n))
+        put(k3v(F.g[ch], d, m, n, np, P));
+    const int Pc = (d.Nq == 1) ? 0 : KAVG;
+    if (ch != CH_P) { int a, b, c; conv(ch, CH_P, m, n, np, a, b, c); if (chan_val(t, F.g[CH_P], d, a, b, c, Pc)) put(t); }
+    if (ch != CH_T) { int a, b, c; conv(ch, CH_T, m, n, np, a, b, c); if (chan_val(t, F.g[CH_T], d, a, b, c, Pc)) put(t); }
+    if (ch != CH_A) { int a, b, c; conv(ch, CH_A, m, n, np, a, b, c); if (chan_val(t, F.g[CH_A], d, a, b, c, Pc)) put(t); }
     return v;
 }
 

@@ -701,65 +701,111 @@ __device__ __forceinline__ void bse_L_K2_body(const VertPT<S>& F, const cplx* Pi
 // ω-independent value c = F(Ω,ν,∞) - F(Ω,∞,∞); the sum is evaluated exactly as
 // c·S_X + Σ_{ω ∈ union} (F(Ω,ν,ω) - F(Ω,∞,ω) - c) X(ω).
 // ---------------------------------------------------------------------------------------------
-// TAN: the tangent in one pass, as for K1.
-template <int CH, class S, bool TAN>
-__device__ __forceinline__ void bse_K2_body(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
-                                            const cplx* SX, cplx* out, const int* items, int nitems, int accum,
-                                            const Dims& d, const TanArgsT<S>& T) {
+// One CTA per (channel, P, Ω) row of representatives (the items of a row differ only in ν).  The
+// ν-independent factor of the ω-sum, X(ω) = Π(ω) FL(Ω,ω,∞) + (Π - Π0)(ω) U, is tabulated once per
+// row in shared memory over the ω range any window can reach, [-W, W) with
+// W = n2O + n2n + n1 + nRn + 2 (clipped to the stored bubble window); each warp then sums one
+// item's window terms.  The vertex factor F(Ω,ν,ω) - F(Ω,∞,ω) - c is evaluated in its reduced form
+// (pSp_k2diff; the t channel's 2 pSp + xSp by crossing, xSp = -pSp in the a representation).
+// GB300's FP64 pipe bounds this kernel: both take FP64 work out of the per-term loop.
+// TAN: the tangent in one pass, as for K1 (tables X and dX).
+__host__ __device__ __forceinline__ int k2_table_half(const Dims& d) {
+    const int W = d.n2O + d.n2n + d.n1 + d.nRn + 2;
+    return W < d.nPw ? W : d.nPw;
+}
+// F(Ω,ν,ω) - F(Ω,∞,ω) - F(Ω,ν,∞) + F(Ω,∞,∞) in the spin combination of the K2 BSE of channel CH
+template <int CH, class S>
+__device__ __forceinline__ S k2_vertex_diff(const VertPT<S>& F, const Dims& d, int m, int nu, int n, int P) {
     using R = decltype(S::x);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= nitems) return;
-    const int idx = items ? items[w] : w;
-    const int nu = idx % d.N2n - d.n2n;
-    const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
-    const int P = idx / (d.N2n * d.N2O);
-    constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
-    // F(Ω,∞,ω) equals F(Ω,∞,∞) (bit for bit) unless ω is in the K2 box
-    const S cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
-    const S c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
-    S tcinf{0, 0}, tc{0, 0};
-    if constexpr (TAN) {
-        tcinf = vert_eval(T.F, d, CH, SP, m, FINF, FINF, P);
-        tc = vert_eval(T.F, d, CH, SP, m, nu, FINF, P) - tcinf;
+    if constexpr (CH != CH_T) {
+        return pSp_k2diff(F, d, CH, m, nu, n, P);
+    } else {  // density: 2 pSp + xSp, xSp(t) = -pSp(a); 2p exact, one rounding
+        const S p = pSp_k2diff(F, d, CH_T, m, nu, n, P), x = pSp_k2diff(F, d, CH_A, m, nu, n, P);
+        return S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};
     }
+}
+// c = F(Ω,ν,∞) - F(Ω,∞,∞) in the same spin combination: only the own channel's K2(Ω,ν) survives
+// (the t channel's crossed part is the a channel's, by crossing)
+template <class S>
+__device__ __forceinline__ S k2_own(const VertPT<S>& F, const Dims& d, int ch, int m, int nu, int P) {
+    if (!bin(m, d.n1) || !bin(m, d.n2O) || !fin(nu, d.n2n)) return S{0, 0};
+    return k2v(F.g[ch], d, m, nu, P);
+}
+template <int CH, class S>
+__device__ __forceinline__ S k2_c(const VertPT<S>& F, const Dims& d, int m, int nu, int P) {
+    using R = decltype(S::x);
+    if constexpr (CH != CH_T) {
+        return k2_own(F, d, CH, m, nu, P);
+    } else {
+        const S p = k2_own(F, d, CH_T, m, nu, P), x = k2_own(F, d, CH_A, m, nu, P);
+        return S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};
+    }
+}
+template <int CH, class S, bool TAN>
+__device__ __forceinline__ void bse_K2_row(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
+                                           const cplx* SX, cplx* out, const int* items, const int* gstart,
+                                           int ngroups, int accum, const Dims& d, const TanArgsT<S>& T, S* tab) {
+    using R = decltype(S::x);
+    const int g = blockIdx.x;
+    if (g >= ngroups) return;
+    const int i0 = gstart ? gstart[g] : g * d.N2n, i1 = gstart ? gstart[g + 1] : (g + 1) * d.N2n;
+    const int first = items ? items[i0] : i0;
+    const int m = (first / d.N2n) % d.N2O - (d.n2O - 1);
+    const int P = first / (d.N2n * d.N2O);
+    const int half = k2_table_half(d), NT = 2 * half;
+    S* Xt = tab;
+    S* tXt = tab + NT;
     const cplx* tPi = (CH == CH_P) ? T.pp : T.ph;
-    Windows win;
-    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
-    win.add(-d.n2n, d.n2n - 1, lo, hi);
-    win.add(-d.nRn, d.nRn - 1, lo, hi);
-    win.add(nu - h1, nu + h1, lo, hi);
-    win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
-    if (CH == CH_P) win.add(m - nu - 1 - h1, m - nu - 1 + h1, lo, hi);
-    win.merge();
-    S acc{0, 0};
-    for (int t = lane; t < win.total; t += 32) {
-        const int n = win.at(t);
+    for (int j = threadIdx.x; j < NT; j += blockDim.x) {
+        const int n = j - half;
         const int wt = cross(CH, m, n);
-        const S Finf = fin(n, d.n2n) ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
-        const S Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
         const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
         const S pi = to_c<S>(ldg(Pi + ip)), pi0 = Pi0 ? to_c<S>(ldg(Pi0 + ip)) : S{0, 0};
-        if constexpr (!TAN) {
-            acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
-        } else {
-            const S X = cfma(pi, FLr, (pi - pi0) * (R)d.U);
-            const S tFinf = fin(n, d.n2n) ? vert_eval(T.F, d, CH, SP, m, FINF, n, P) : tcinf;
-            const S tFl = vert_eval(T.F, d, CH, SP, m, nu, n, P) - tFinf - tc;
+        Xt[j] = cfma(pi, FLr, (pi - pi0) * (R)d.U);
+        if constexpr (TAN) {
             const S tFLr = fl_right(T.FL.K2[CH_P], T.FL.K2[CH_T], T.FL.K2[CH_A], d, CH, m, wt, P);
             const S tpi = to_c<S>(ldg(tPi + ip));
-            const S tX = cfma(tpi, FLr + cre<S>(d.U), pi * tFLr);
-            acc = cfma(tFl, X, cfma(Fl, tX, acc));
+            tXt[j] = cfma(tpi, FLr + cre<S>(d.U), pi * tFLr);
         }
     }
-    acc = warp_sum(acc);
-    if (lane == 0) {
-        const size_t is = (size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1);
-        const S sx = SX ? to_c<S>(SX[is]) : S{0, 0};
-        S r = c * sx + acc;
-        if constexpr (TAN) r = cfma(tc, sx, c * to_c<S>(T.SX[is])) + acc;
-        const cplx v = to_d(r * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
-        out[idx] = accum ? out[idx] + v : v;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
+    const size_t is = (size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1);
+    for (int it = i0 + warp; it < i1; it += nwarps) {
+        const int idx = items ? items[it] : it;
+        const int nu = idx % d.N2n - d.n2n;
+        const S c = k2_c<CH>(F, d, m, nu, P);
+        S tc{0, 0};
+        if constexpr (TAN) tc = k2_c<CH>(T.F, d, m, nu, P);
+        Windows win;
+        win.add(-d.n2n, d.n2n - 1, lo, hi);
+        win.add(-d.nRn, d.nRn - 1, lo, hi);
+        win.add(nu - h1, nu + h1, lo, hi);
+        win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
+        if (CH == CH_P) win.add(m - nu - 1 - h1, m - nu - 1 + h1, lo, hi);
+        win.merge();
+        S acc{0, 0};
+        for (int t = lane; t < win.total; t += 32) {
+            const int n = win.at(t);
+            const int j = n + half;
+            const S Fl = k2_vertex_diff<CH>(F, d, m, nu, n, P);
+            if constexpr (!TAN) {
+                acc = cfma(Fl, Xt[j], acc);
+            } else {
+                const S tFl = k2_vertex_diff<CH>(T.F, d, m, nu, n, P);
+                acc = cfma(tFl, Xt[j], cfma(Fl, tXt[j], acc));
+            }
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            const S sx = SX ? to_c<S>(SX[is]) : S{0, 0};
+            S r = c * sx + acc;
+            if constexpr (TAN) r = cfma(tc, sx, c * to_c<S>(T.SX[is])) + acc;
+            const cplx v = to_d(r * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+            out[idx] = accum ? out[idx] + v : v;
+        }
     }
 }
 
@@ -984,7 +1030,7 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
 //   K2(Ω,ν) = T s U Σ_ω [(F(Ω,ν,ω) - F(Ω,∞,ω)) Π - (F0(Ω,ν,ω) - F0(Ω,∞,ω)) Π0],  ω over the bubble mesh.
 // F0(Ω,∞,ω) is U_sp for every ω.  For K1, F(Ω,∞,ω) = F(Ω,∞,∞) = c outside the K2 box, so the sum is
 // c SΠ + Σ_{K2 box} (F - c) Π - U_sp SΠ0.  For K2 the F difference is ω-independent outside the
-// windows of bse_K2_body and the F0 difference vanishes outside the RefVertex box.
+// windows of bse_K2_row and the F0 difference vanishes outside the RefVertex box.
 // ---------------------------------------------------------------------------------------------
 template <int CH, class S>
 __device__ __forceinline__ void bse_K1_new_body(const VertPT<S>& F, const cplx* Pi, const cplx* SPi,
@@ -1090,12 +1136,14 @@ __global__ void k_bse_L_K2_all(VertPT<S> F, BubbleP B, ChanWork cw, Dims d) {
     }
 }
 template <class S, bool TAN>
-__global__ void k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d,
-                             TanArgsT<S> T) {
+__global__ void __launch_bounds__(128) k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw,
+                                                    Dims d, TanArgsT<S> T) {
+    extern __shared__ __align__(16) unsigned char k2_smem[];
+    S* tab = reinterpret_cast<S*>(k2_smem);
     switch (blockIdx.y) {
-        case CH_P: bse_K2_body<CH_P, S, TAN>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d, T); break;
-        case CH_T: bse_K2_body<CH_T, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d, T); break;
-        default:   bse_K2_body<CH_A, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d, T); break;
+        case CH_P: bse_K2_row<CH_P, S, TAN>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.gstart[CH_P], cw.ngroups[CH_P], cw.acc, d, T, tab); break;
+        case CH_T: bse_K2_row<CH_T, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.gstart[CH_T], cw.ngroups[CH_T], cw.acc, d, T, tab); break;
+        default:   bse_K2_row<CH_A, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.gstart[CH_A], cw.ngroups[CH_A], cw.acc, d, T, tab); break;
     }
 }
 template <class S, bool TAN>
@@ -1523,6 +1571,22 @@ cudaError_t launch_build_cache(cudaStream_t s, const VertPF& F, const Caches& C,
                                const Dims& d) {
     return build_cache_t(s, F, C, blocks, nblocks, d);
 }
+// K2 rows: one CTA per (channel, P, Ω) row of representatives
+static unsigned row_grid(const ChanWork& cw, int nch) {
+    int mx = 0;
+    for (int c = 0; c < nch; ++c) mx = std::max(mx, cw.ngroups[c]);
+    return (unsigned)std::max(mx, 1);
+}
+template <class S, bool TAN>
+static size_t k2_row_smem(const Dims& d) {
+    return (size_t)(TAN ? 2 : 1) * 2 * k2_table_half(d) * sizeof(S);
+}
+template <class K>
+static cudaError_t k2_smem_attr(K kernel, size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
 static unsigned warp_grid(const ChanWork& cw, int nch) {
     int mx = 0;
     for (int c = 0; c < nch; ++c) mx = std::max(mx, cw.nitems[c]);
@@ -1541,7 +1605,10 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
     }                                                                                                               \
     cudaError_t launch_bse_K2_all(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const ChanWork& cw, const Dims& d) {                                             \
-        k_bse_K2_all<ST, false><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, TT{});                        \
+        const size_t smem = k2_row_smem<ST, false>(d);                                                             \
+        cudaError_t e = k2_smem_attr(k_bse_K2_all<ST, false>, smem);                                                \
+        if (e != cudaSuccess) return e;                                                                             \
+        k_bse_K2_all<ST, false><<<dim3(row_grid(cw, 3), 3), 128, smem, s>>>(F, FL, B, SX, cw, d, TT{});              \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_sde_L_all(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
@@ -1556,7 +1623,10 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
     }                                                                                                               \
     cudaError_t launch_bse_K2_tan(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const TT& T, const ChanWork& cw, const Dims& d) {                                \
-        k_bse_K2_all<ST, true><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, T);                           \
+        const size_t smem = k2_row_smem<ST, true>(d);                                                              \
+        cudaError_t e = k2_smem_attr(k_bse_K2_all<ST, true>, smem);                                                 \
+        if (e != cudaSuccess) return e;                                                                             \
+        k_bse_K2_all<ST, true><<<dim3(row_grid(cw, 3), 3), 128, smem, s>>>(F, FL, B, SX, cw, d, T);                  \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_sde_L_tan(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \

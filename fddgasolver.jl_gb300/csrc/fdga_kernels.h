@@ -83,8 +83,12 @@ struct K3Args3 {  // the three channels of one K3 launch over a list of (P, Ω) 
 };
 
 struct ChanWork {  // per-channel work of an all-channel launch, indexed by channel (p, t, a) or (pp, ph)
-    const int* items[3];  // representative device indices (nullptr: item = index)
+    const int* items[3];  // representative device indices, ascending (nullptr: item = index)
     int nitems[3];
+    // K2: rows of items that share (P, Ω); row r = items[gstart[r] .. gstart[r+1]) (nullptr: the
+    // N2n consecutive indices of row r)
+    const int* gstart[3];
+    int ngroups[3];
     cplx* out[3];
     int acc;  // 1: out += value (product-rule terms of the tangent map)
 };

@@ -30,8 +30,10 @@ enum ArrKind { AK_G = 0, AK_K1, AK_K2, AK_K3, AK_PI };
 
 struct Group {
     bool trivial = true;
-    int* d_items = nullptr;       // representative device indices
+    int* d_items = nullptr;       // representative device indices, ascending
     int nitems = 0;
+    int* d_gstart = nullptr;      // K2 groups: start of each (P, Ω) row of items, plus the end
+    int ngroups = 0;
     uint32_t* d_map = nullptr;    // per device index: rep*4 + op
     size_t n = 0;
 };
@@ -402,12 +404,22 @@ void compute_all_groups(const Dims& d, std::vector<HostGroup>& out) {
     for (auto& t : th) t.join();
 }
 
-int upload_group(fdga_handle* h, Group& g, const HostGroup& hg) {
+// row: items with equal index / row form one row (the K2 groups' (P, Ω) rows); 0: no rows
+int upload_group(fdga_handle* h, Group& g, const HostGroup& hg, int row = 0) {
     const size_t n = hg.map.size();
     if (!g.d_map) AL(g.d_map, n);
     if (!g.d_items) AL(g.d_items, n);
     CK(cudaMemcpyAsync(g.d_map, hg.map.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync(g.d_items, hg.items.data(), hg.items.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    std::vector<int> starts;
+    if (row > 0) {
+        for (size_t i = 0; i < hg.items.size(); ++i)
+            if (i == 0 || hg.items[i] / row != hg.items[i - 1] / row) starts.push_back((int)i);
+        starts.push_back((int)hg.items.size());
+        if (!g.d_gstart) AL(g.d_gstart, n / row + 1);
+        CK(cudaMemcpyAsync(g.d_gstart, starts.data(), starts.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        g.ngroups = (int)starts.size() - 1;
+    }
     CK(cudaStreamSynchronize(h->st));
     g.trivial = false;
     g.nitems = (int)hg.items.size();
@@ -442,6 +454,11 @@ VertPT<S> vertex_view_t(const fdga_handle* h, S* st, S* avg, S* const* fref) {
 VertP vertex_view(fdga_handle* h, cplx* S) { return vertex_view_t<cplx>(h, S, h->avg, h->Fref); }
 
 const Group& k2group(fdga_handle* h, int ch) { return ch == CH_P ? h->gK2pp : h->gK2ph; }
+// the (P, Ω) rows of the K2 work of channel ch (the K2 BSE kernel runs one CTA per row)
+void k2_rows(const fdga_handle* h, const Group& g, ChanWork& cw, int ch) {
+    cw.gstart[ch] = g.trivial ? nullptr : g.d_gstart;
+    cw.ngroups[ch] = g.trivial ? h->d.Nq * h->d.N2O : g.ngroups;
+}
 
 #define LC(call)                                                     \
     do {                                                             \
@@ -577,6 +594,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             cw.items[ch] = g.trivial ? nullptr : g.d_items;
             cw.nitems[ch] = g.trivial ? (int)n : g.nitems;
             cw.out[ch] = raw + (size_t)ch * n;
+            if (cls == 2) k2_rows(h, g, cw, ch);
         }
         return cw;
     };
@@ -889,6 +907,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
             cw.items[ch] = g.trivial ? nullptr : g.d_items;
             cw.nitems[ch] = g.trivial ? (int)n : g.nitems;
             cw.out[ch] = raw + (size_t)ch * n;
+            if (cls == 2) k2_rows(h, g, cw, ch);
         }
         cw.acc = acc;
         return cw;
@@ -1713,7 +1732,7 @@ int fdga_init_sym_grp(fdga_handle* h) {
     ++h->groups_version;
     Group* dst[8] = {&h->gSig, &h->gK1, &h->gK2pp, &h->gK2ph, &h->gK3pp, &h->gK3ph, &h->gK3ppL, &h->gK3phL};
     for (int i = 0; i < 8; ++i) {
-        int r = upload_group(h, *dst[i], hg[i]);
+        int r = upload_group(h, *dst[i], hg[i], i == 2 || i == 3 ? h->d.N2n : 0);
         if (r) return r;
     }
     // (P, Ω) blocks of the K3 mesh that hold a representative of any K3 group: only these blocks
