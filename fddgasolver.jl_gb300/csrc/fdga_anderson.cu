@@ -16,6 +16,17 @@ namespace {
 
 constexpr int RT = 256;  // threads of every reduction block
 
+// The long-vector passes are bound by GB300's FP64 pipe: complex products are written as FMAs.
+// conj(a) b + c
+__device__ __forceinline__ cplx cfma_conj(cplx a, cplx b, cplx c) {
+    return mk(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+// c - a b
+__device__ __forceinline__ cplx cfnma(cplx a, cplx b, cplx c) {
+    return mk(fma(-a.x, b.x, fma(a.y, b.y, c.x)), fma(-a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+__device__ __forceinline__ double norm2_acc(cplx v, double s) { return fma(v.x, v.x, fma(v.y, v.y, s)); }
+
 // Sum of part[0..np) in a fixed order, identical in every block; the result is valid in all threads.
 __device__ __forceinline__ cplx block_reduce_parts(const cplx* part, int np, cplx* sh) {
     cplx s = mk(0.0, 0.0);
@@ -51,8 +62,8 @@ __global__ void __launch_bounds__(RT) k_aa_diff(cplx* dg, const cplx* g, const c
         dg[i] = g[i] - gold[i];
         const cplx v = fx[i] - df[i];
         df[i] = v;
-        if (Qb) s += conjg(Qb[i]) * v;
-        else s.x += v.x * v.x + v.y * v.y;
+        if (Qb) s = cfma_conj(Qb[i], v, s);
+        else s.x = norm2_acc(v, s.x);
     }
     block_store_partial(s, sh, part_out);
 }
@@ -66,10 +77,10 @@ __global__ void __launch_bounds__(RT) k_aa_mgs(cplx* df, const cplx* Qa, const c
     if (blockIdx.x == 0 && threadIdx.x == 0) *Rentry = r;
     cplx s = mk(0.0, 0.0);
     for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
-        const cplx v = df[i] - r * Qa[i];
+        const cplx v = cfnma(r, Qa[i], df[i]);
         df[i] = v;
-        if (Qb) s += conjg(Qb[i]) * v;
-        else s.x += v.x * v.x + v.y * v.y;
+        if (Qb) s = cfma_conj(Qb[i], v, s);
+        else s.x = norm2_acc(v, s.x);
     }
     block_store_partial(s, sh, part_out);
 }
@@ -80,9 +91,10 @@ __global__ void __launch_bounds__(RT) k_aa_qnew(cplx* Qk, const cplx* df, const 
     __shared__ cplx sh[RT];
     const double nr = sqrt(fmax(0.0, block_reduce_parts(part_in, np, sh).x));
     if (blockIdx.x == 0 && threadIdx.x == 0) *Rkk = mk(nr, 0.0);
+    const double inv = 1.0 / nr;  // one division per block, not two per element
     for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
         const cplx v = df[i];
-        Qk[i] = mk(v.x / nr, v.y / nr);
+        Qk[i] = mk(v.x * inv, v.y * inv);
     }
 }
 
@@ -99,7 +111,7 @@ __global__ void __launch_bounds__(RT) k_aa_multidot(AAVecs Q, int nv, const cplx
         const cplx f = fx[i];
 #pragma unroll
         for (int j = 0; j < AA_CHUNK; ++j)
-            if (j < cnt) s[j] += conjg(Q.v[i0 + j][i]) * f;
+            if (j < cnt) s[j] = cfma_conj(Q.v[i0 + j][i], f, s[j]);
     }
     for (int j = 0; j < cnt; ++j) block_store_partial(s[j], sh, part + (size_t)(i0 + j) * np);
 }
@@ -133,7 +145,7 @@ __global__ void __launch_bounds__(RT) k_aa_update(cplx* x, const cplx* g, AAVecs
     for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
         const cplx gi = g[i];
         cplx v = gi;
-        for (int j = 0; j < meff; ++j) v -= gs[j] * dG.v[j][i];
+        for (int j = 0; j < meff; ++j) v = cfnma(gs[j], dG.v[j][i], v);
         x[i] = v;
         fxold[i] = fx[i];
         gold[i] = gi;
@@ -184,8 +196,9 @@ __global__ void __launch_bounds__(RT) k_aa_qrot(AAVecsW Q, int m, const cplx* ro
             const double c = rs[2 * (i - 1)].x;
             const cplx sn = rs[2 * (i - 1) + 1];
             const cplx b = Q.v[i][t];
-            Q.v[i - 1][t] = a * c + conjg(sn) * b;
-            a = (-sn) * a + b * c;
+            // Q_{i-1} = c a + conj(s) b ; a = -s a + c b
+            Q.v[i - 1][t] = mk(fma(a.x, c, fma(sn.x, b.x, sn.y * b.y)), fma(a.y, c, fma(sn.x, b.y, -sn.y * b.x)));
+            a = mk(fma(b.x, c, fma(-sn.x, a.x, sn.y * a.y)), fma(b.y, c, fma(-sn.x, a.y, -sn.y * a.x)));
         }
         Q.v[m - 1][t] = a;
     }
