@@ -83,20 +83,15 @@ __global__ void __launch_bounds__(RT) k_kr_dots(KrVecs V, int nv, const cplxf* w
     if (with_norm) store_partial(an.total(), sh, part + (size_t)norm_slot * np);
 }
 
-// coef[i] = Σ_blocks part[i], i < ncoef (one block, fixed order)
+// coef[i] = Σ_blocks part[i], i < ncoef (one block; a warp per coefficient, lanes over the
+// partials in a fixed order, then a fixed shuffle tree: no block barriers)
 __global__ void __launch_bounds__(RT) k_kr_reduce(const double* part, int np, int ncoef, double* coef) {
-    __shared__ double sh[RT];
-    for (int i = 0; i < ncoef; ++i) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = warp; i < ncoef; i += RT / 32) {
         double s = 0.0;
-        for (int b = threadIdx.x; b < np; b += RT) s += part[(size_t)i * np + b];
-        sh[threadIdx.x] = s;
-        __syncthreads();
-        for (int o = RT / 2; o > 0; o >>= 1) {
-            if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) coef[i] = sh[0];
-        __syncthreads();
+        for (int b = lane; b < np; b += 32) s += part[(size_t)i * np + b];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) coef[i] = s;
     }
 }
 
