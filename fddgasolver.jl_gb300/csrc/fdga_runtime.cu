@@ -2090,12 +2090,21 @@ int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, doub
     // residual, or when they stagnate at the mixed map's rounding floor.  Phase 2 starts when an
     // outer step reduced the FP64 residual by less than 10x (the floor is reached): the same
     // Anderson iteration then runs on the FP64 map to tol.
-    const double eta = 1e-3;
+    // The inner residual cannot go below the mixed map's rounding floor, about the FP32 unit
+    // roundoff times the size of the state; the inner tolerance stops there instead of leaving
+    // the inner solve to stagnate.
+    const double eta = 1e-3, u32 = 5.96e-8;
+    double floor32 = 0.0;
     for (;;) {
         h->precision = FDGA_FP64;
         int r = run_iteration(h, strategy, true, true);
         if (r) return r;
         ++n64;
+        if (floor32 == 0.0) {  // max|Φ(x)| at the first outer iterate
+            CK(launch_residual(h->st, h->yS, nullptr, nullptr, nullptr, 0.0, h->d_part, NBLK_RED, n));
+            floor32 = 2.0 * u32 * reduce_max(h, NBLK_RED, status);
+            if (status) return status;
+        }
         CK(launch_residual(h->st, h->yS, h->xS, c, nullptr, 0.0, h->d_part, NBLK_RED, n));
         const double rk = reduce_max(h, NBLK_RED, status);
         if (status) return status;
@@ -2120,7 +2129,7 @@ int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, doub
         if (r) return r;
         ++nmix;
         CK(launch_sub(h->st, c, c, h->yS, n));
-        r = inner(c, std::max(eta * rk, 0.25 * tol), 8, false);
+        r = inner(c, std::max({eta * rk, 0.25 * tol, floor32}), 8, false);
         if (r) return r;
     }
     // S holds Φ64(x) of the last outer evaluation, as after the reference's solve!
