@@ -830,15 +830,18 @@ template <class C> __device__ __forceinline__ C ldk(const cplxf* p) {
 // ARGS = K3Args3 (FP64 operands) or K3Args3F (FP32 operands).  C = cplx: FP64 arithmetic (the plain
 // path).  C = cplxf: FP32 products and accumulation, FP64 epilogue (the mixed path; FP64 operands
 // are converted when they are staged into shared memory).
-template <int MODE, int TILE, class C, class ARGS>
-__global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS args, Dims d) {
+template <int MODE, int TILE, int TCOL, class C, class ARGS>
+__global__ void __launch_bounds__((TILE / 2) * (TCOL / 2)) k_bse_K3_gemm(ARGS args, Dims d) {
     using R = decltype(C::x);
-    constexpr int TK = 8, H = TILE / 2, NT = H * H;
+    constexpr int TK = 8, H = TILE / 2, HC = TCOL / 2, NT = H * HC;
     __shared__ C As[TILE][TK + 1];
-    __shared__ C Ms[TK][TILE + 1];
+    __shared__ C Ms[TK][TCOL + 1];
+    // the ω-only factors of M, signs folded in, for the current and the next K chunk:
+    // [0] s1(Π-Π0) (mode 0: Π0)  [1] s1 Π  [2] s2 Π  [3] s1 dΠ  [4] s2 dΠ
+    __shared__ C Pk[2][TK][5];
     const int tid = threadIdx.x;
-    const int tx = tid % H, ty = tid / H;
-    const int col0 = blockIdx.z * TILE, row0 = blockIdx.y * TILE;
+    const int tx = tid % HC, ty = tid / HC;
+    const int col0 = blockIdx.z * TCOL, row0 = blockIdx.y * TILE;
     const int nb = args.nblocks;
     const int slot = blockIdx.x / nb;
     const int blk = args.blocks ? args.blocks[blockIdx.x % nb] : (int)(blockIdx.x % nb);
@@ -847,8 +850,44 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
     const int m = blk % d.N3O - (d.n3O - 1), P = blk / d.N3O;
     const int N = d.N3n;
     const size_t base = (size_t)blk * N * N;
-    const double s1 = (CH == CH_A) ? 1.0 : -1.0, s2 = (CH == CH_T) ? -1.0 : 1.0;
+    const R s1 = (CH == CH_A) ? (R)1 : (R)-1, s2 = (CH == CH_T) ? (R)-1 : (R)1;
+    const bool oneloop = (a.flags & K3F_1LOOP) != 0;
+    auto fill_pk = [&](int buf, int k0) {
+        if (tid < TK) {
+            C* q = Pk[buf][tid];
+            const int k = k0 + tid;
+            for (int j = 0; j < 5; ++j) q[j] = czero<C>();
+            if (k < N) {
+                const size_t ip = ixPi(d, P, m, k - d.n3n);
+                const C pi0 = a.Pi0 ? to_c<C>(ldg(a.Pi0 + ip)) : czero<C>();
+                if (MODE == 0) {
+                    q[0] = pi0;
+                } else {
+                    const C pi = to_c<C>(ldg(a.Pi + ip));
+                    q[0] = (pi - pi0) * s1;
+                    q[1] = pi * s1;
+                    q[2] = pi * s2;
+                    if (MODE == 2) {
+                        const C tpi = to_c<C>(ldg(a.tPi + ip));
+                        q[3] = tpi * s1;
+                        q[4] = tpi * s2;
+                    }
+                }
+            }
+        }
+    };
+    // γL at a K3 index in the channel's spin combination (t: 2 FL.γt - FL.γa)
+    auto gl_at = [&](const auto* FLc, const auto* FLt, const auto* FLa, size_t i) -> C {
+        if (CH == CH_T) {
+            const C t = ldk<C>(FLt + i), u = ldk<C>(FLa + i);
+            return C{fma(t.x, (R)2, -u.x), fma(t.y, (R)2, -u.y)};
+        }
+        return ldk<C>(FLc + i);
+    };
     C acc[2][2] = {{czero<C>(), czero<C>()}, {czero<C>(), czero<C>()}};
+    fill_pk(0, 0);
+    __syncthreads();
+    int cur = 0;
     // MODE 2 (tangent): the inner index runs twice, first over (dA, M), then over (A, dM)
     constexpr int NH = (MODE == 2) ? 2 : 1;
     for (int half = 0; half < NH; ++half) {
@@ -860,80 +899,70 @@ __global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_bse_K3_gemm(ARGS ar
                 const int row = row0 + r, k = k0 + kk;
                 As[r][kk] = (row < N && k < N) ? ldk<C>(Ap + base + (size_t)row * N + k) : czero<C>();
             }
-            for (int e = tid; e < TK * TILE; e += NT) {
-                const int kk = e / TILE, c = e % TILE;
+            for (int e = tid; e < TK * TCOL; e += NT) {
+                const int kk = e / TCOL, c = e % TCOL;
                 const int k = k0 + kk, col = col0 + c;
+                const C* q = Pk[cur][kk];
                 C v = czero<C>();
                 if (k < N && col < N) {
-                    const int o = k - d.n3n;  // ω as fermion index
-                    const size_t ip = ixPi(d, P, m, o);
-                    const C pi0 = a.Pi0 ? to_c<C>(ldg(a.Pi0 + ip)) : czero<C>();
                     const C f0 = ldk<C>(a.B0 + base + (size_t)k * N + col);
                     if (MODE == 0) {
-                        v = pi0 * f0;
+                        v = q[0] * f0;
+                    } else if (oneloop) {
+                        v = q[0] * f0;
                     } else {
-                        const C pi = to_c<C>(ldg(a.Pi + ip));
                         const size_t ig = (CH == CH_P) ? base + (size_t)k * N + col : base + (size_t)col * N + k;
-                        const C gs = (a.flags & K3F_1LOOP) ? czero<C>() : ldk<C>(a.G + ig);
-                        const int ot = cross(CH, m, o);
+                        const C gs = ldk<C>(a.G + ig);
+                        const int ot = cross(CH, m, k - d.n3n);
                         const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                        if (a.flags & K3F_1LOOP) {
-                            v = ((pi - pi0) * f0) * (R)s1;
-                        } else if (!tM) {
-                            v = ((pi - pi0) * f0 + pi * gs) * (R)s1;
-                            if (fin(ot, d.n3n)) {
-                                const C gl = (CH == CH_T) ? ldk<C>(a.FLt + il) * (R)2 - ldk<C>(a.FLa + il)
-                                                          : ldk<C>(a.FLc + il);
-                                v += pi * gl * (R)s2;
-                            }
+                        if (!tM) {  // s1 [(Π-Π0) F0 + Π Γ] + s2 Π γL
+                            v = cfma(q[0], f0, q[1] * gs);
+                            if (fin(ot, d.n3n)) v = cfma(q[2], gl_at(a.FLc, a.FLt, a.FLa, il), v);
                         } else {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL]
-                            const C tpi = to_c<C>(ldg(a.tPi + ip));
-                            const C tgs = ldk<C>(a.tG + ig);
-                            v = cfma(tpi, f0 + gs, pi * tgs) * (R)s1;
-                            if (fin(ot, d.n3n)) {
-                                const C gl = (CH == CH_T) ? ldk<C>(a.FLt + il) * (R)2 - ldk<C>(a.FLa + il)
-                                                          : ldk<C>(a.FLc + il);
-                                const C tgl = (CH == CH_T) ? ldk<C>(a.tFLt + il) * (R)2 - ldk<C>(a.tFLa + il)
-                                                           : ldk<C>(a.tFLc + il);
-                                v += cfma(tpi, gl, pi * tgl) * (R)s2;
-                            }
+                            v = cfma(q[3], f0 + gs, q[1] * ldk<C>(a.tG + ig));
+                            if (fin(ot, d.n3n))
+                                v = cfma(q[4], gl_at(a.FLc, a.FLt, a.FLa, il),
+                                         cfma(q[2], gl_at(a.tFLc, a.tFLt, a.tFLa, il), v));
                         }
                     }
                 }
                 Ms[kk][c] = v;
             }
+            // the next chunk's factors (the next K chunk, or the first chunk of the next half)
+            const int nk0 = (k0 + TK < N) ? k0 + TK : 0;
+            if (k0 + TK < N || half + 1 < NH) fill_pk(cur ^ 1, nk0);
             __syncthreads();
 #pragma unroll
             for (int kk = 0; kk < TK; ++kk) {
                 const C a0 = As[ty][kk], a1 = As[ty + H][kk];
-                const C b0 = Ms[kk][tx], b1 = Ms[kk][tx + H];
+                const C b0 = Ms[kk][tx], b1 = Ms[kk][tx + HC];
                 acc[0][0] = cfma(a0, b0, acc[0][0]);
                 acc[0][1] = cfma(a0, b1, acc[0][1]);
                 acc[1][0] = cfma(a1, b0, acc[1][0]);
                 acc[1][1] = cfma(a1, b1, acc[1][1]);
             }
             __syncthreads();
+            cur ^= 1;
         }
     }
+    const R Tr = (R)d.T;
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const int row = row0 + ty + H * i, col = col0 + tx + H * j;
+            const int row = row0 + ty + H * i, col = col0 + tx + HC * j;
             if (row >= N || col >= N) continue;
             const size_t io = base + (size_t)row * N + col;
             // epilogue in the arithmetic type C (FP64 ops cost 64 FP32 ops on this part)
+            const C c = acc[i][j];
             cplx v;
             if (MODE == 0) {
-                v = to_d(acc[i][j] * (R)(d.T * ((CH == CH_A) ? 1.0 : -1.0)));
+                v = to_d(c * (R)(d.T * ((CH == CH_A) ? 1.0 : -1.0)));
             } else if (a.flags & K3F_NOEPI) {
-                v = to_d(acc[i][j] * (R)d.T);
-            } else if (MODE == 1) {
-                const C gl = (CH == CH_T) ? ldk<C>(a.FLt + io) * (R)2 - ldk<C>(a.FLa + io) : ldk<C>(a.FLc + io);
-                v = to_d(acc[i][j] * (R)d.T + gl);
+                v = to_d(c * Tr);
             } else {
-                const C tgl = (CH == CH_T) ? ldk<C>(a.tFLt + io) * (R)2 - ldk<C>(a.tFLa + io) : ldk<C>(a.tFLc + io);
-                v = to_d(acc[i][j] * (R)d.T + tgl);
+                const C g = (MODE == 1) ? gl_at(a.FLc, a.FLt, a.FLa, io) : gl_at(a.tFLc, a.tFLt, a.tFLa, io);
+                v = to_d(C{fma(c.x, Tr, g.x), fma(c.y, Tr, g.y)});
             }
             a.out[io] = (a.flags & K3F_ACC) ? a.out[io] + v : v;
         }
@@ -1656,30 +1685,36 @@ cudaError_t launch_finalize3(cudaStream_t s, const Finalize3& f, int k2_epilogue
     k_finalize3<<<blocks_for(n, 256), 256, 0, s>>>(f, k2_epilogue, t_recombine, n);
     LAUNCH_CHECK(); return cudaSuccess;
 }
-template <int MODE, int TILE, class C, class ARGS>
+template <int MODE, int TILE, int TCOL, class C, class ARGS>
 static cudaError_t launch_k3_tile(cudaStream_t s, const ARGS& a, int nslots, const Dims& d) {
-    const unsigned tiles = (unsigned)((d.N3n + TILE - 1) / TILE);
-    dim3 grid((unsigned)(nslots * a.nblocks), tiles, tiles);
-    k_bse_K3_gemm<MODE, TILE, C, ARGS><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(a, d);
+    const unsigned rt = (unsigned)((d.N3n + TILE - 1) / TILE), ct = (unsigned)((d.N3n + TCOL - 1) / TCOL);
+    dim3 grid((unsigned)(nslots * a.nblocks), rt, ct);
+    k_bse_K3_gemm<MODE, TILE, TCOL, C, ARGS><<<grid, (TILE / 2) * (TCOL / 2), 0, s>>>(a, d);
     return cudaGetLastError();
 }
-int k3_default_tile(int N) { return N <= 16 ? 16 : (N <= 24 ? 24 : 32); }
+// Tile codes: 16, 24, 32 = square TILE x TILE output tiles; 100 + TILE = TILE rows x TILE/2
+// columns (twice the CTAs, each forming only its own columns of M: better balance over the SMs
+// for launches with few CTAs per SM, at twice the operand staging per flop; the autotuner decides,
+// the default is square: measured on GB300 at Nν3 = 24, 675 blocks, the split is 7 % slower).
+bool k3_tile_valid(int tile) { return tile == 16 || tile == 24 || tile == 32 || tile == 116 || tile == 124 || tile == 132; }
+static int k3_default_tile(int N) { return N <= 16 ? 16 : (N <= 24 ? 24 : 32); }
+template <int MODE, class C, class ARGS>
+static cudaError_t launch_k3_mode(cudaStream_t s, const ARGS& a, int nslots, const Dims& d, int tile) {
+    switch (tile) {
+        case 16: return launch_k3_tile<MODE, 16, 16, C>(s, a, nslots, d);
+        case 24: return launch_k3_tile<MODE, 24, 24, C>(s, a, nslots, d);
+        case 116: return launch_k3_tile<MODE, 16, 8, C>(s, a, nslots, d);
+        case 124: return launch_k3_tile<MODE, 24, 12, C>(s, a, nslots, d);
+        case 132: return launch_k3_tile<MODE, 32, 16, C>(s, a, nslots, d);
+        default: return launch_k3_tile<MODE, 32, 32, C>(s, a, nslots, d);
+    }
+}
 template <class C, class ARGS>
 static cudaError_t launch_bse_K3_t(cudaStream_t s, int mode, const ARGS& a, int nslots, const Dims& d, int tile) {
-    if (tile != 16 && tile != 24 && tile != 32) tile = k3_default_tile(d.N3n);
-    if (mode == 0) {
-        if (tile == 16) return launch_k3_tile<0, 16, C>(s, a, nslots, d);
-        if (tile == 24) return launch_k3_tile<0, 24, C>(s, a, nslots, d);
-        return launch_k3_tile<0, 32, C>(s, a, nslots, d);
-    }
-    if (mode == 2) {
-        if (tile == 16) return launch_k3_tile<2, 16, C>(s, a, nslots, d);
-        if (tile == 24) return launch_k3_tile<2, 24, C>(s, a, nslots, d);
-        return launch_k3_tile<2, 32, C>(s, a, nslots, d);
-    }
-    if (tile == 16) return launch_k3_tile<1, 16, C>(s, a, nslots, d);
-    if (tile == 24) return launch_k3_tile<1, 24, C>(s, a, nslots, d);
-    return launch_k3_tile<1, 32, C>(s, a, nslots, d);
+    if (!k3_tile_valid(tile)) tile = k3_default_tile(d.N3n);
+    if (mode == 0) return launch_k3_mode<0, C>(s, a, nslots, d, tile);
+    if (mode == 2) return launch_k3_mode<2, C>(s, a, nslots, d, tile);
+    return launch_k3_mode<1, C>(s, a, nslots, d, tile);
 }
 cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed, int tile) {
     return mixed ? launch_bse_K3_t<cplxf>(s, mode, a, nslots, d, tile)

@@ -220,10 +220,10 @@ cudaError_t launch_qavg(cudaStream_t s, const ChanArrays& in, const ChanArraysW&
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
                                const Dims& d);
 // mode 0 (left K3), 1 (K3), 2 (tangent of K3: dA·M + A·dM + dγL as one GEMM over the concatenated
-// inner index).  tile: 16, 24 or 32 (the output tile edge of the GEMM kernel); any other value picks
-// the default for Nν3
+// inner index).  tile: 16, 24 or 32 (square output tiles of the GEMM kernel) or 116, 124, 132 (TILE
+// rows x TILE/2 columns); any other value picks the default for Nν3 and the launch's CTA count
 cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int mixed, int tile);
-int k3_default_tile(int N);
+bool k3_tile_valid(int tile);
 cudaError_t launch_bse_K3_f32(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int tile);
 cudaError_t launch_to_f32(cudaStream_t s, const cplx* in, cplxf* out, size_t n);
 // tcgen05 form of the mixed K3 contractions (2Nν3 ≤ 256 MMA columns); *err set on a wait timeout

@@ -2946,7 +2946,7 @@ int fdga_autotune(fdga_handle* h, int strategy, int* tiles) {
     static std::mutex mu;
     static std::map<std::tuple<int, int, int>, std::pair<int, int>> cache;
     const int prec0 = h->precision;
-    const int cand[3] = {16, 24, 32};
+    const int cand[6] = {16, 24, 32, 116, 124, 132};
     for (int prec = FDGA_FP64; prec <= FDGA_MIXED; ++prec) {
         const auto key = std::make_tuple(h->d.N3n, h->d.local, prec);
         {

@@ -200,7 +200,8 @@ int fdga_set_U(fdga_handle* h, double U);
 int fdga_dchi_dU(fdga_handle* h, int strategy, int channel, double hU, int restart, int cycles, double rtol,
                  double* out, size_t n_out, int* gmres_iters, double* relres);
 
-/* K3 GEMM tile autotuner: times the 16/24/32 output-tile variants of both K3 contractions on
+/* K3 GEMM tile autotuner: times the output-tile variants of both K3 contractions (16/24/32
+ * square tiles, and the same row heights with half-width column tiles: codes 116/124/132) on
  * this handle's data, in FP64 and mixed precision, and keeps the fastest.  Size classes
  * (Nν3, local/nonlocal, precision) are tuned once per process and shared by all handles.
  * tiles (4 ints, may be NULL) = {FP64 L_K3, FP64 K3, mixed L_K3, mixed K3}. */
