@@ -1165,7 +1165,7 @@ __global__ void k_bse_L_K2_all(VertPT<S> F, BubbleP B, ChanWork cw, Dims d) {
     }
 }
 template <class S, bool TAN>
-__global__ void __launch_bounds__(128) k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw,
+__global__ void __launch_bounds__(512) k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw,
                                                     Dims d, TanArgsT<S> T) {
     extern __shared__ __align__(16) unsigned char k2_smem[];
     S* tab = reinterpret_cast<S*>(k2_smem);
@@ -1606,6 +1606,9 @@ static unsigned row_grid(const ChanWork& cw, int nch) {
     for (int c = 0; c < nch; ++c) mx = std::max(mx, cw.ngroups[c]);
     return (unsigned)std::max(mx, 1);
 }
+// 4 warps per row; 16 when the launch has fewer than four rows per SM of GB300 (the local solver,
+// whose rows are only the NΩ2 bosonic frequencies)
+static unsigned row_threads(const ChanWork& cw, int nch) { return row_grid(cw, nch) * nch < 4 * 152 ? 512 : 128; }
 template <class S, bool TAN>
 static size_t k2_row_smem(const Dims& d) {
     return (size_t)(TAN ? 2 : 1) * 2 * k2_table_half(d) * sizeof(S);
@@ -1637,7 +1640,7 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
         const size_t smem = k2_row_smem<ST, false>(d);                                                             \
         cudaError_t e = k2_smem_attr(k_bse_K2_all<ST, false>, smem);                                                \
         if (e != cudaSuccess) return e;                                                                             \
-        k_bse_K2_all<ST, false><<<dim3(row_grid(cw, 3), 3), 128, smem, s>>>(F, FL, B, SX, cw, d, TT{});              \
+        k_bse_K2_all<ST, false><<<dim3(row_grid(cw, 3), 3), row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, TT{}); \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_sde_L_all(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
@@ -1655,7 +1658,7 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
         const size_t smem = k2_row_smem<ST, true>(d);                                                              \
         cudaError_t e = k2_smem_attr(k_bse_K2_all<ST, true>, smem);                                                 \
         if (e != cudaSuccess) return e;                                                                             \
-        k_bse_K2_all<ST, true><<<dim3(row_grid(cw, 3), 3), 128, smem, s>>>(F, FL, B, SX, cw, d, T);                  \
+        k_bse_K2_all<ST, true><<<dim3(row_grid(cw, 3), 3), row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, T);     \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_sde_L_tan(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
