@@ -338,6 +338,59 @@ __device__ __forceinline__ S pSp_k2diff(const VertPT<S>& F, const Dims& d, int c
     return v;
 }
 
+// pSp_k2diff of a vertex F and of a tangent vertex dF (RefVertex terms off) in one pass: the
+// frequency conversions, box tests and offsets are shared, only the loads are doubled.
+template <class S>
+__device__ __forceinline__ bool chan_val2(S& t, S& u, const ChanPT<S>& c, const ChanPT<S>& e, const Dims& d, int m,
+                                          int n, int np, int P) {
+    if (!bin(m, d.n1)) return false;
+    t = k1v(c, d, m, P);
+    u = k1v(e, d, m, P);
+    if (!bin(m, d.n2O)) return true;
+    const bool a = fin(n, d.n2n), b = fin(np, d.n2n);  // n, np finite here
+    if (a && b) {
+        t += k2v(c, d, m, n, P) + k2v(c, d, m, np, P);
+        u += k2v(e, d, m, n, P) + k2v(e, d, m, np, P);
+        if (bin(m, d.n3O) && fin(n, d.n3n) && fin(np, d.n3n)) {
+            t += k3v(c, d, m, n, np, P);
+            u += k3v(e, d, m, n, np, P);
+        }
+    } else if (a) {
+        t += k2v(c, d, m, n, P);
+        u += k2v(e, d, m, n, P);
+    } else if (b) {
+        t += k2v(c, d, m, np, P);
+        u += k2v(e, d, m, np, P);
+    }
+    return true;
+}
+template <class S>
+__device__ __forceinline__ void pSp_k2diff2(const VertPT<S>& F, const VertPT<S>& E, const Dims& d, int ch, int m, int n,
+                                            int np, int P, S& v, S& w) {
+    S t, u;
+    bool has = false;
+    auto put = [&](const S& x, const S& y) {
+        if (has) { v += x; w += y; }
+        else { v = x; w = y; has = true; }
+    };
+    v = S{0, 0};
+    w = S{0, 0};
+    if (!F.noref) {  // (the tangent vertex has no RefVertex terms)
+        if (ch == CH_A) {
+            if (ref_val(t, F.Ft_x, d, m, np, n)) put(-t, S{0, 0});
+        } else if (ref_val(t, ch == CH_P ? F.Fp_p : F.Ft_p, d, m, n, np)) {
+            put(t, S{0, 0});
+        }
+    }
+    if (bin(m, d.n1) && bin(m, d.n2O) && fin(n, d.n2n) && fin(np, d.n2n) && bin(m, d.n3O) && fin(n, d.n3n) &&
+        fin(np, d.n3n))
+        put(k3v(F.g[ch], d, m, n, np, P), k3v(E.g[ch], d, m, n, np, P));
+    const int Pc = (d.Nq == 1) ? 0 : KAVG;
+    if (ch != CH_P) { int a, b, c; conv(ch, CH_P, m, n, np, a, b, c); if (chan_val2(t, u, F.g[CH_P], E.g[CH_P], d, a, b, c, Pc)) put(t, u); }
+    if (ch != CH_T) { int a, b, c; conv(ch, CH_T, m, n, np, a, b, c); if (chan_val2(t, u, F.g[CH_T], E.g[CH_T], d, a, b, c, Pc)) put(t, u); }
+    if (ch != CH_A) { int a, b, c; conv(ch, CH_A, m, n, np, a, b, c); if (chan_val2(t, u, F.g[CH_A], E.g[CH_A], d, a, b, c, Pc)) put(t, u); }
+}
+
 // FL(Ω, ω, νInf, Ch, Sp): FL has F0 = RefVertex(0) and K1 = 0, so only its K2 survives.
 template <class S>
 __device__ __forceinline__ S fl_right(const S* FLK2p, const S* FLK2t, const S* FLK2a, const Dims& d, int ch, int m,

@@ -724,6 +724,21 @@ __device__ __forceinline__ S k2_vertex_diff(const VertPT<S>& F, const Dims& d, i
         return S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};
     }
 }
+// the same for F and a tangent vertex dF in one pass
+template <int CH, class S>
+__device__ __forceinline__ void k2_vertex_diff2(const VertPT<S>& F, const VertPT<S>& E, const Dims& d, int m, int nu,
+                                                int n, int P, S& v, S& w) {
+    using R = decltype(S::x);
+    if constexpr (CH != CH_T) {
+        pSp_k2diff2(F, E, d, CH, m, nu, n, P, v, w);
+    } else {
+        S p, q, x, y;
+        pSp_k2diff2(F, E, d, CH_T, m, nu, n, P, p, q);
+        pSp_k2diff2(F, E, d, CH_A, m, nu, n, P, x, y);
+        v = S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};
+        w = S{fma(q.x, (R)2, -y.x), fma(q.y, (R)2, -y.y)};
+    }
+}
 // c = F(Ω,ν,∞) - F(Ω,∞,∞) in the same spin combination: only the own channel's K2(Ω,ν) survives
 // (the t channel's crossed part is the a channel's, by crossing)
 template <class S>
@@ -790,11 +805,12 @@ __device__ __forceinline__ void bse_K2_row(const VertPT<S>& F, const FLPT<S>& FL
         for (int t = lane; t < win.total; t += 32) {
             const int n = win.at(t);
             const int j = n + half;
-            const S Fl = k2_vertex_diff<CH>(F, d, m, nu, n, P);
             if constexpr (!TAN) {
+                const S Fl = k2_vertex_diff<CH>(F, d, m, nu, n, P);
                 acc = cfma(Fl, Xt[j], acc);
             } else {
-                const S tFl = k2_vertex_diff<CH>(T.F, d, m, nu, n, P);
+                S Fl, tFl;
+                k2_vertex_diff2<CH>(F, T.F, d, m, nu, n, P, Fl, tFl);
                 acc = cfma(tFl, Xt[j], cfma(Fl, tXt[j], acc));
             }
         }
