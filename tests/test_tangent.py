@@ -102,3 +102,33 @@ def test_frule_mixed_precision(cfg):
     gpu.set_precision("fp64")
     err = blockwise_rel_err(cfg, j32, j64)
     assert 0 < err < 2e-5
+
+
+def test_frule_config2_shapes():
+    """Full config-2 shapes (Hubbard 8x8, sym groups): enough (P, Ω) rows that the K2 kernels run
+    their 4-warp CTAs.  FP64 tangent vs Richardson central differences of the oracle (1e-8); the
+    mixed tangent vs the FP64 tangent (2e-5)."""
+    from fdgasolver.workloads import CONFIGS
+    cfg = dict(CONFIGS["config2"])
+    rng = np.random.default_rng(13)
+    orc = make_oracle(cfg, True)
+    gpu = make_gpu(cfg, True)
+    x = orc.flatten()
+    x = x + 0.5 * orc.residual(x, "fdPA")
+    v = _dir(rng, x.size)
+    h = 2e-3
+
+    def phi(z):
+        return orc.residual(z, "fdPA") + z
+
+    d1 = (phi(x + h * v) - phi(x - h * v)) / (2 * h)
+    d2 = (phi(x + 0.5 * h * v) - phi(x - 0.5 * h * v)) / h
+    ref = (4 * d2 - d1) / 3
+    gpu.unflatten(x)
+    _, j64 = gpu.frule(v)
+    assert blockwise_rel_err(cfg, j64, ref) < 1e-8
+    gpu.set_precision("mixed")
+    gpu.unflatten(x)
+    _, j32 = gpu.frule(v)
+    assert 0 < blockwise_rel_err(cfg, j32, j64) < 2e-5
+    gpu.close()
