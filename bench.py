@@ -48,7 +48,9 @@ UNIT = "s/iteration"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 for config1/config2, enough to span several clock samples; "
+                         "fewer for the larger configurations)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config2")
@@ -57,7 +59,13 @@ def parse():
     ap.add_argument("--restart", type=int, default=20, help="GMRES restart of the Newton solves (differentiation runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the oracle timing (for the large configurations, where one oracle iteration takes hours)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:  # the whole default run stays within a few minutes
+        if args.impl == "reference":
+            args.steps = 5
+        else:
+            args.steps = {"config1": 200, "config2": 200, "config3": 10, "config4": 10}.get(args.config, 3)
+    return args
 
 
 def dist_env():
@@ -110,6 +118,12 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+
+    def has_sample(self):
+        try:
+            return self.path is not None and os.path.getsize(self.path) > 0
+        except OSError:
+            return False
 
     def stop(self):
         if not self.proc:
@@ -253,6 +267,12 @@ def run_ours(args, rank, world, dist):
     # ---- device-resident timed region ----
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
+    # keep the GPU loaded (untimed iterations) until the sampler's first line, so that every clock
+    # sample is taken under load (nvidia-smi needs a few hundred ms to start)
+    t_wait = time.perf_counter()
+    while clocks.proc and not clocks.has_sample() and time.perf_counter() - t_wait < 3.0:
+        S.map_repeat(20)
+        S.synchronize()
     dist.barrier()
     S.synchronize()
     ms_dev = 0.0
@@ -279,6 +299,10 @@ def run_ours(args, rank, world, dist):
         S.fixed_point_ptr(xb.ptr, Rb.ptr)
         t_e2e += time.perf_counter() - t0
     t_e2e /= args.steps
+    # kernels launched in the two timed regions: the iteration graph's per device-resident step, the
+    # fused residual graph's per e2e step (the L2 flushes are memsets, outside the timed spans)
+    e2e_launches = S.launches_per_iteration()
+    gpu_launches = args.steps * launches + args.steps * e2e_launches
     dist.barrier()
     clk = clocks.stop()
     xb.free()
@@ -360,8 +384,9 @@ def run_ours(args, rank, world, dist):
                    "name": args.config, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "L2 flushed (256 MB device write) before every timed iteration; flush not timed"},
         "e2e": {"value": t_e2e, "unit": UNIT, "h2d_bytes_per_step": nstate * 16, "d2h_bytes_per_step": nstate * 16},
-        "gpu_launches": launches * args.steps,
+        "gpu_launches": gpu_launches,
         "launches_per_iteration": launches,
+        "e2e_launches_per_call": e2e_launches,
         "time_to_converge": conv,
         "roofline": roofline,
         "precision_mixed_map_vs_fp64": precision,
