@@ -923,11 +923,13 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         }
         return f;
     };
-    // K3 contraction launch in the precision of the map
+    // K3 contraction launch in the precision of the map; the tangent (mode 2) takes the tile tuned
+    // for the K3 contraction (mode 1), whose operands it shares
     auto k3 = [&](int mode, const K3Args3& a3, const K3Args3F& a3f) -> cudaError_t {
+        const int tm = mode == 0 ? 0 : 1;
         if (mixed && h->k3_tc && k3_tc_supported(d)) return launch_bse_K3_tc(s, mode, a3f, 3, d, h->d_err);
-        if (mixed) return launch_bse_K3_f32(s, mode, a3f, 3, d, h->k3_tile[FDGA_MIXED][mode]);
-        return launch_bse_K3(s, mode, a3, 3, d, 0, h->k3_tile[FDGA_FP64][mode]);
+        if (mixed) return launch_bse_K3_f32(s, mode, a3f, 3, d, h->k3_tile[FDGA_MIXED][tm]);
+        return launch_bse_K3(s, mode, a3, 3, d, 0, h->k3_tile[FDGA_FP64][tm]);
     };
     if (strategy == FDGA_FDPA) {
         {  // dFL.K2 = L_K2(dF)  (Π0 constant): branch C
