@@ -1413,7 +1413,7 @@ long orc_len(void* h, const char* name) {
 int orc_set(void* h, const char* name, const double* re_im, long n) {
     auto* v = named((Solver*)h, name);
     if (!v || (long)v->size() != n) return 1;
-    std::memcpy(v->data(), re_im, sizeof(cd) * n);
+    std::memcpy(static_cast<void*>(v->data()), re_im, sizeof(cd) * n);  // std::complex<double>: (re, im) pairs
     return 0;
 }
 int orc_get(void* h, const char* name, double* re_im, long n) {
