@@ -1099,7 +1099,10 @@ int run_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
         int nl = 0;
         r = enqueue_tangent(h, strategy, update_sigma, hartree, nl);
         cudaError_t ee = cudaStreamEndCapture(h->st, &graph);
-        if (r) return r;
+        if (r) {
+            if (ee == cudaSuccess) cudaGraphDestroy(graph);
+            return r;
+        }
         if (ee != cudaSuccess) return cuda_fail(h, ee, "cudaStreamEndCapture");
         ee = cudaGraphInstantiate(&g.exec, graph, 0);
         cudaGraphDestroy(graph);
@@ -1405,7 +1408,10 @@ int run_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hartree)
         int nl = 0;
         int r = enqueue_iteration(h, strategy, update_sigma, hartree, nl);
         cudaError_t ee = cudaStreamEndCapture(h->st, &graph);
-        if (r) return r;
+        if (r) {
+            if (ee == cudaSuccess) cudaGraphDestroy(graph);
+            return r;
+        }
         if (ee != cudaSuccess) return cuda_fail(h, ee, "cudaStreamEndCapture");
         ee = cudaGraphInstantiate(&g.exec, graph, 0);
         cudaGraphDestroy(graph);
@@ -1862,7 +1868,10 @@ int residual_graph(fdga_handle* h, int strategy, const double* x, double* R) {
         if (ee == cudaSuccess && !r)
             ee = cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, s);
         cudaError_t ec = cudaStreamEndCapture(s, &graph);
-        if (r) return r;
+        if (r) {
+            if (ec == cudaSuccess) cudaGraphDestroy(graph);
+            return r;
+        }
         if (ee != cudaSuccess) {
             if (ec == cudaSuccess) cudaGraphDestroy(graph);
             return cuda_fail(h, ee, "residual graph capture");
@@ -3097,8 +3106,9 @@ int fdga_batch_iterate(fdga_batch* b, int strategy, int precision) {
             total += nl;
         }
         const cudaError_t ee = cudaStreamEndCapture(b->st, &graph);
-        if (r) return r;
-        if (e != cudaSuccess || ee != cudaSuccess) {
+        if (r || e != cudaSuccess || ee != cudaSuccess) {
+            if (ee == cudaSuccess) cudaGraphDestroy(graph);
+            if (r) return r;
             b->err = std::string("batch capture: ") + cudaGetErrorString(e != cudaSuccess ? e : ee);
             return FDGA_ERR_CUDA;
         }
