@@ -2281,6 +2281,24 @@ int apply_A(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const 
     return FDGA_OK;
 }
 
+// The FP32 operands that the tangent of the mixed map reads at its base point (G(R), the mirrors of
+// x, Φ(x) and the momentum averages, FL.K2, FL.K3, the ten K3 caches), converted from the FP64
+// map's intermediates at the same point: the mixed tangent then linearises at the FP64 value
+// pass, and no mixed map is needed to set its base up.  Every other intermediate the tangent reads
+// is FP64 and shared by the two precisions.
+int mixed_tangent_base_from_fp64(fdga_handle* h) {
+    if (int r = ensure_mixed(h)) return r;
+    cudaStream_t s = h->st;
+    CK(launch_to_f32(s, h->GR, h->GRf, h->nGk));
+    CK(launch_to_f32(s, h->xS, h->xSf, 3 * h->nchan));
+    CK(launch_to_f32(s, h->yS, h->ySf, 3 * h->nchan));
+    if (h->navg) CK(launch_to_f32(s, h->avg, h->avgf, h->navg));
+    CK(launch_to_f32(s, h->FLK2, h->FLK2f, 3 * h->n2));
+    CK(launch_to_f32(s, h->FLK3, h->FLK3f, 3 * h->n3));
+    CK(launch_to_f32(s, h->cache, h->cachef, 10 * h->n3));
+    return FDGA_OK;
+}
+
 // Restarted GMRES(m) for A dx = b (compact vectors), dx starting at 0.  Cycles after the first
 // restart from the true residual b − A dx.  relres = final ‖b − A dx‖/‖b‖ estimate.
 int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplx* b, cplx* dx, int m,
@@ -2574,7 +2592,11 @@ int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int
         eta = std::max(eta, jvp_prec == FDGA_MIXED ? (use_tangent(h, strategy) ? 1e-5 : 1e-3) : 1e-6);
         // no linear solve beyond what the tolerance asks of this step
         eta = std::min(0.1, std::max(eta, 0.1 * tol / resid));
-        if (jvp_prec == FDGA_MIXED) {
+        if (jvp_prec == FDGA_MIXED && use_tangent(h, strategy)) {
+            // the base of the mixed tangent from the FP64 map just run at x (xS = x, yS = Φ64(x))
+            if ((r = mixed_tangent_base_from_fp64(h))) return r;
+            h->precision = FDGA_MIXED;
+        } else if (jvp_prec == FDGA_MIXED) {
             h->precision = FDGA_MIXED;
             CK(cudaMemcpyAsync(h->xS, x, n * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
             if ((r = run_iteration(h, strategy, true, true))) return r;
