@@ -288,15 +288,11 @@ static size_t k3_tc_smem(const Dims& d) { return 2 * ((size_t)2 * A_BYTES + (siz
 
 cudaError_t prepare_bse_K3_tc(const Dims& d) {
     // the dynamic shared-memory limit is raised once per size, before any graph capture
-    static size_t smem_set = 0;
+    static size_t set0 = 0, set1 = 0, set2 = 0;
     const size_t smem = k3_tc_smem(d);
-    if (smem <= smem_set) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_bse_K3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_bse_K3_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_bse_K3_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) smem_set = smem;
+    cudaError_t e = raise_smem_limit(k_bse_K3_tc<0>, set0, smem);
+    if (e == cudaSuccess) e = raise_smem_limit(k_bse_K3_tc<1>, set1, smem);
+    if (e == cudaSuccess) e = raise_smem_limit(k_bse_K3_tc<2>, set2, smem);
     return e;
 }
 

@@ -1428,11 +1428,8 @@ static cudaError_t launch_bubble_dft(cudaStream_t s, const G* GR, const G* tGR, 
     while (tv > 1 && (size_t)(4 * tv * NR + d.L) * sizeof(C) > 160 * 1024) tv >>= 1;
     const size_t shm = (size_t)(4 * tv * NR + d.L) * sizeof(C);
     static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
-    if (shm > 48 * 1024 && shm > shm_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_bubble_nl<TAN, C, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        if (e != cudaSuccess) return e;
-        shm_set = shm;
-    }
+    cudaError_t e = raise_smem_limit(k_bubble_nl<TAN, C, G>, shm_set, shm);
+    if (e != cudaSuccess) return e;
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
     k_bubble_nl<TAN, C, G><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, twp, d, tv);
     LAUNCH_CHECK(); return cudaSuccess;
@@ -1451,10 +1448,8 @@ static cudaError_t launch_bubble_fft(cudaStream_t s, const cplx* GR, const cplx*
     while (tv > 1 && (size_t)2 * tv * BS * sizeof(cplx) > 80 * 1024) tv >>= 1;
     const size_t shm = (size_t)2 * tv * BS * sizeof(cplx);
     static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
-    if (shm > 48 * 1024 && shm > shm_set) {
-        cudaFuncSetAttribute(k_bubble_fft<L, cplx, cplx, TAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        shm_set = shm;
-    }
+    cudaError_t e = raise_smem_limit(k_bubble_fft<L, cplx, cplx, TAN>, shm_set, shm);
+    if (e != cudaSuccess) return e;
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
     k_bubble_fft<L, cplx, cplx, TAN><<<grid, 256, shm, s>>>(GR, tGR, pp, ph, d, tv);
     return cudaGetLastError();
@@ -1631,9 +1626,9 @@ static size_t k2_row_smem(const Dims& d) {
 }
 template <class K>
 static cudaError_t k2_smem_attr(K kernel, size_t smem) {
-    if (smem <= 48 * 1024) return cudaSuccess;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static size_t raised = 0;  // one record per kernel instantiation
+    return raise_smem_limit(kernel, raised, smem);
 }
 static unsigned warp_grid(const ChanWork& cw, int nch) {
     int mx = 0;

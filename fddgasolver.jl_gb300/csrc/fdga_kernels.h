@@ -4,9 +4,25 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "fdga_device.cuh"
 
 namespace fdga {
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`; `raised` is the caller's record
+// of the largest limit set for that kernel.  One process-wide lock serialises the check and the
+// update, so concurrent launchers never lower a limit another thread raised.
+template <class K>
+inline cudaError_t raise_smem_limit(K kernel, size_t& raised, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (bytes <= raised) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) raised = bytes;
+    return e;
+}
 
 struct ChanArrays {  // read-only K arrays of the three channels
     const cplx* K1[3];

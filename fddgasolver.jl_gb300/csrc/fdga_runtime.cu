@@ -84,6 +84,7 @@ struct fdga_handle {
     int* d_k3blocks = nullptr;                             // (P, Ω) blocks holding K3 class representatives
     void* flush_buf = nullptr;                             // L2 flush buffer (benchmarks)
     size_t flush_bytes = 0;
+    unsigned char flush_val = 0;
     int nk3blocks = 0;
     double* occ = nullptr;
     double n0 = 0.5;
@@ -2946,8 +2947,7 @@ int fdga_flush_l2(fdga_handle* h, size_t bytes) {
         if (e != cudaSuccess) return fail(h, FDGA_ERR_OOM, std::string("flush buffer: ") + cudaGetErrorString(e));
         h->flush_bytes = bytes;
     }
-    static unsigned char v = 0;
-    CK(cudaMemsetAsync(h->flush_buf, ++v, bytes, h->st));
+    CK(cudaMemsetAsync(h->flush_buf, ++h->flush_val, bytes, h->st));  // a new value each time
     return FDGA_OK;
 }
 
