@@ -4,7 +4,7 @@ The golden values were produced by the reference's `solve!` with its default fto
 stopping point depends on the NLsolve Anderson trajectory; the oracle restates that trajectory
 (m = 8, beta = 0.85) and agreement is bounded by the stopping tolerance, not by round-off.
 
-Two facts the pins establish (both recorded in the design doc):
+Two facts the pins establish:
 * test/test_siam_scPA.jl was generated with a bubble frequency mesh of nK1 fermions
   (mΠν_factor = 1); with the current default factor 6 the values move by 2-18 %.
 * test/test_siam_fdPA.jl:179 matches the fdPA SDE with the reference Hartree term subtracted once;
