@@ -32,14 +32,14 @@ for _p in (ROOT, PKG):
 
 METRIC = "s per parquet iteration (plain FP64, fdPA, Hubbard 8x8 config)"
 WORKLOADS = {
-    "config1": "SIAM local fdPA: beta=10 U=1 Gamma=0.5 flat band nK1=64 nK2=(32,32) nK3=(16,16) nG=64 mPi=6, init_sym_grp",
-    "config2": "Hubbard 8x8 NL fdPA: t=1 t'=0 mu=0 U=2 beta=5 nK1=32 nK2=(16,16) nK3=(8,12) nG=32 mPi=32, "
+    "siam_b10_nk3_16": "SIAM local fdPA: beta=10 U=1 Gamma=0.5 flat band nK1=64 nK2=(32,32) nK3=(16,16) nG=64 mPi=6, init_sym_grp",
+    "hubbard8x8_b5_nk3_8x12": "Hubbard 8x8 NL fdPA: t=1 t'=0 mu=0 U=2 beta=5 nK1=32 nK2=(16,16) nK3=(8,12) nG=32 mPi=32, "
                "synthetic RefVertex, init_sym_grp",
-    "config3": "Hubbard 16x16 NL fdPA: t=1 t'=-0.2 n=0.9 U=3 beta=10 nK1=80 nK2=(40,40) nK3=(20,40) nG=80 mPi=32, "
+    "hubbard16x16_n09_nk3_20x40": "Hubbard 16x16 NL fdPA: t=1 t'=-0.2 n=0.9 U=3 beta=10 nK1=80 nK2=(40,40) nK3=(20,40) nG=80 mPi=32, "
                "init_sym_grp",
-    "config3s": "Hubbard 4x4 NL fdPA with config 3's boxes: t=1 t'=-0.2 n=0.9 U=3 beta=10 nK1=80 nK2=(40,40) "
+    "hubbard4x4_n09_nk3_20x40": "Hubbard 4x4 NL fdPA with the 16x16 workload's boxes: t=1 t'=-0.2 n=0.9 U=3 beta=10 nK1=80 nK2=(40,40) "
                 "nK3=(20,40) nG=80 mPi=32, init_sym_grp (profiling size)",
-    "config5": "Hubbard 24x24 NL fdPA: t=1 t'=0 mu=0 U=2.5 beta=8 nK1=96 nK2=(48,48) nK3=(24,48) nG=96 mPi=32, "
+    "hubbard24x24_b8_nk3_24x48": "Hubbard 24x24 NL fdPA: t=1 t'=0 mu=0 U=2.5 beta=8 nK1=96 nK2=(48,48) nK3=(24,48) nG=96 mPi=32, "
                "init_sym_grp",
 }
 UNIT = "s/iteration"
@@ -49,11 +49,11 @@ def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default: 200 for config1/config2, enough to span several clock samples; "
+                    help="timed steps (default: 200 for siam_b10_nk3_16/hubbard8x8_b5_nk3_8x12, enough to span several clock samples; "
                          "fewer for the larger configurations)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="config2")
+    ap.add_argument("--config", default="hubbard8x8_b5_nk3_8x12")
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge leg")
     ap.add_argument("--U", type=float, default=None, help="override the configuration's U (differentiation runs)")
     ap.add_argument("--restart", type=int, default=20, help="GMRES restart of the Newton solves (differentiation runs)")
@@ -64,7 +64,7 @@ def parse():
         if args.impl == "reference":
             args.steps = 5
         else:
-            args.steps = {"config1": 200, "config2": 200, "config3": 10, "config4": 10}.get(args.config, 3)
+            args.steps = {"siam_b10_nk3_16": 200, "hubbard8x8_b5_nk3_8x12": 200, "hubbard16x16_n09_nk3_20x40": 10, "siam_batch48": 10}.get(args.config, 3)
     return args
 
 
@@ -488,7 +488,7 @@ def run_batch(args, rank, world, dist):
         "dtype": "c128 (FP64 complex)", "data": "synthetic (seeded instance parameters)",
         "config": {"workload": "48 SIAM local fdPA instances: U~U[0.5,3], beta in {5,10,20,40}, Gamma~U[0.3,1], "
                                "nK3=(nu/2,nu), nu=16/32/48/64 by beta, nK2=(nu,nu), nK1=nG=2nu, mPi=6",
-                   "name": "config4", "parallelism": "single GPU, one graph with 48 branches"},
+                   "name": "siam_batch48", "parallelism": "single GPU, one graph with 48 branches"},
         "mixed_s_per_batch_iteration": ms32 / args.steps * 1e-3,
         "sequential_s_per_round": t_seq,
         "speedup_batch_vs_sequential": t_seq / t64,
@@ -535,8 +535,8 @@ def run_differentiation(args, rank, world, dist):
         "value": t_lr, "unit": "s (linear response at the fixed point)", "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": t_lr * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 (FP64 complex)", "data": "synthetic (model inputs restated)",
-        "config": {"workload": WORKLOADS["config5"] + ("" if args.U is None else f" (U overridden: {args.U})"),
-                   "name": "config5", "parallelism": "single GPU", "U": cfg["U"], "gmres_restart": args.restart},
+        "config": {"workload": WORKLOADS["hubbard24x24_b8_nk3_24x48"] + ("" if args.U is None else f" (U overridden: {args.U})"),
+                   "name": "hubbard24x24_b8_nk3_24x48", "parallelism": "single GPU", "U": cfg["U"], "gmres_restart": args.restart},
         "solve": {"seconds": t_solve, "converged": r["converged"], "residual": r["residual"],
                   "newton_steps": r["newton"], "fp64_maps": r["evals_fp64"], "mixed_maps": r["evals_mixed"]},
         "dchi_m_dU": {"value": [d[k0].real, d[k0].imag], **info},
@@ -598,9 +598,9 @@ def main():
     if world > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     dist = Dist(world)
-    if args.config in ("config4", "config5-diff"):
-        if args.config == "config5-diff":
-            args.config = "config5"
+    if args.config in ("siam_batch48", "hubbard24x24_b8_newton"):
+        if args.config == "hubbard24x24_b8_newton":
+            args.config = "hubbard24x24_b8_nk3_24x48"
             out = run_differentiation(args, rank, world, dist)
         else:
             out = run_batch(args, rank, world, dist)

@@ -4,17 +4,17 @@ The reference names no dataset; these reproduce the configuration text: model, p
 sizes (read as the reference constructor arguments) and, for the nonlocal plain-method case, a
 seeded synthetic RefVertex.
 
-config1: SIAM, local fdPA, β=10, U=1, flat band Δ(iν) = -iΓ sign ν, Γ = 0.5 (D = ∞), e = 0,
+siam_b10_nk3_16: SIAM, local fdPA, β=10, U=1, flat band Δ(iν) = -iΓ sign ν, Γ = 0.5 (D = ∞), e = 0,
          nK1=64, nK2=(32,32), nK3=(16,16), nG=64, mΠν_factor=6.
-config2: Hubbard 8x8, nonlocal fdPA, t=1, t'=0, μ=0, U=2, β=5, nK1=32, nK2=(16,16), nK3=(8,12),
+hubbard8x8_b5_nk3_8x12: Hubbard 8x8, nonlocal fdPA, t=1, t'=0, μ=0, U=2, β=5, nK1=32, nK2=(16,16), nK3=(8,12),
          nG=32, mΠν_factor=32; F0 = RefVertex(U) with corrections on the K3 box drawn as
          complex Gaussian noise σ = 0.05 U, symmetrised ν<->ν', scaled 1/sqrt((1+|ν|)(1+|ν'|)).
-config3: Hubbard 16x16, nonlocal fdPA, t=1, t'=-0.2, U=3, β=10, nK1=80, nK2=(40,40), nK3=(20,40), nG=80,
+hubbard16x16_n09_nk3_20x40: Hubbard 16x16, nonlocal fdPA, t=1, t'=-0.2, U=3, β=10, nK1=80, nK2=(40,40), nK3=(20,40), nG=80,
          mΠν_factor=32; μ tuned once on Gbare (Σ = 0) to density n = 0.9 (per-spin occupation 0.45).
-config4: 48 SIAM instances, local fdPA, flat band (D = ∞), e = 0, seeded U ~ U[0.5, 3], β ∈ {5, 10, 20, 40},
+siam_batch48: 48 SIAM instances, local fdPA, flat band (D = ∞), e = 0, seeded U ~ U[0.5, 3], β ∈ {5, 10, 20, 40},
          Γ ~ U[0.3, 1]; boxes scale with β: nK3 = (nν/2, nν) with nν = 16, 32, 48, 64 for β = 5, 10, 20,
          40, nK2 = (nν, nν), nK1 = nG = 2nν, mΠν_factor = 6 (batch_instances).
-config5: Hubbard 24x24, nonlocal fdPA, t=1, t'=0, μ=0, U=2.5, β=8, nK1=96, nK2=(48,48), nK3=(24,48), nG=96,
+hubbard24x24_b8_nk3_24x48: Hubbard 24x24, nonlocal fdPA, t=1, t'=0, μ=0, U=2.5, β=8, nK1=96, nK2=(48,48), nK3=(24,48), nG=96,
          mΠν_factor=32.
 """
 import numpy as np
@@ -23,16 +23,16 @@ from .models import fermionic_values
 from .solver import RefVertex
 
 CONFIGS = {
-    "config1": dict(kind="siam", T=0.1, U=1.0, e=0.0, Delta=0.5, D=float("inf"), nG=64, nK1=64, nK2=(32, 32),
+    "siam_b10_nk3_16": dict(kind="siam", T=0.1, U=1.0, e=0.0, Delta=0.5, D=float("inf"), nG=64, nK1=64, nK2=(32, 32),
                     nK3=(16, 16), mPi_factor=6),
-    "config2": dict(kind="hubbard", T=0.2, U=2.0, mu=0.0, t1=1.0, t2=0.0, L=8, nG=32, nK1=32, nK2=(16, 16),
+    "hubbard8x8_b5_nk3_8x12": dict(kind="hubbard", T=0.2, U=2.0, mu=0.0, t1=1.0, t2=0.0, L=8, nG=32, nK1=32, nK2=(16, 16),
                     nK3=(8, 12), mPi_factor=32, refvertex_noise=0.05, seed=20261203),
-    "config3": dict(kind="hubbard", T=0.1, U=3.0, mu=None, filling=0.9, t1=1.0, t2=-0.2, L=16, nG=80, nK1=80,
+    "hubbard16x16_n09_nk3_20x40": dict(kind="hubbard", T=0.1, U=3.0, mu=None, filling=0.9, t1=1.0, t2=-0.2, L=16, nG=80, nK1=80,
                     nK2=(40, 40), nK3=(20, 40), mPi_factor=32),
-    # config 3's frequency boxes on a 4x4 lattice: the size the K3 tensor-core kernel is profiled at
-    "config3s": dict(kind="hubbard", T=0.1, U=3.0, mu=None, filling=0.9, t1=1.0, t2=-0.2, L=4, nG=80, nK1=80,
+    # the 16x16 workload's frequency boxes on a 4x4 lattice: the size the K3 tensor-core kernel is profiled at
+    "hubbard4x4_n09_nk3_20x40": dict(kind="hubbard", T=0.1, U=3.0, mu=None, filling=0.9, t1=1.0, t2=-0.2, L=4, nG=80, nK1=80,
                      nK2=(40, 40), nK3=(20, 40), mPi_factor=32),
-    "config5": dict(kind="hubbard", T=0.125, U=2.5, mu=0.0, t1=1.0, t2=0.0, L=24, nG=96, nK1=96, nK2=(48, 48),
+    "hubbard24x24_b8_nk3_24x48": dict(kind="hubbard", T=0.125, U=2.5, mu=0.0, t1=1.0, t2=0.0, L=24, nG=96, nK1=96, nK2=(48, 48),
                     nK3=(24, 48), mPi_factor=32),
 }
 

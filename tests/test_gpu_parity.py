@@ -98,10 +98,10 @@ def test_flatten_roundtrip_and_layout():
     assert np.array_equal(gpu.get("F.p.K1"), x[:n1])
 
 
-def test_config2_map_parity():
+def test_hubbard8x8_map_parity():
     """Full config-2 shapes (Hubbard 8x8, nK3=(8,12), mΠν_factor=32, synthetic RefVertex), sym groups."""
     from fdgasolver.workloads import CONFIGS
-    cfg = dict(CONFIGS["config2"])
+    cfg = dict(CONFIGS["hubbard8x8_b5_nk3_8x12"])
     orc = make_oracle(cfg, True)
     gpu = make_gpu(cfg, True)
     rng = np.random.default_rng(3)

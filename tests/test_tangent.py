@@ -104,12 +104,12 @@ def test_frule_mixed_precision(cfg):
     assert 0 < err < 2e-5
 
 
-def test_frule_config2_shapes():
+def test_frule_hubbard8x8_shapes():
     """Full config-2 shapes (Hubbard 8x8, sym groups): enough (P, Ω) rows that the K2 kernels run
     their 4-warp CTAs.  FP64 tangent vs Richardson central differences of the oracle (1e-8); the
     mixed tangent vs the FP64 tangent (2e-5)."""
     from fdgasolver.workloads import CONFIGS
-    cfg = dict(CONFIGS["config2"])
+    cfg = dict(CONFIGS["hubbard8x8_b5_nk3_8x12"])
     rng = np.random.default_rng(13)
     orc = make_oracle(cfg, True)
     gpu = make_gpu(cfg, True)
