@@ -12,10 +12,10 @@ namespace fdga {
 
 // Raises a kernel's dynamic shared-memory limit to at least `bytes`; `raised` is the caller's record
 // of the largest limit set for that kernel.  One process-wide lock serialises the check and the
-// update, so concurrent launchers never lower a limit another thread raised.
+// update, so concurrent launchers never lower a limit another thread raised.  (No shortcut below
+// 48 KB: the default limit also counts the kernel's static shared memory.)
 template <class K>
 inline cudaError_t raise_smem_limit(K kernel, size_t& raised, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
     static std::mutex mu;
     std::lock_guard<std::mutex> lk(mu);
     if (bytes <= raised) return cudaSuccess;
