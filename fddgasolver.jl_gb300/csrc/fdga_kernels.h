@@ -12,10 +12,12 @@ namespace fdga {
 
 // Raises a kernel's dynamic shared-memory limit to at least `bytes`; `raised` is the caller's record
 // of the largest limit set for that kernel.  One process-wide lock serialises the check and the
-// update, so concurrent launchers never lower a limit another thread raised.  (No shortcut below
-// 48 KB: the default limit also counts the kernel's static shared memory.)
+// update, so concurrent launchers never lower a limit another thread raised.  Sizes up to `floor`
+// need no raise (48 KB for a kernel without static shared memory; the default limit counts both
+// kinds, so a kernel with static shared memory passes 0 and raises before any graph capture).
 template <class K>
-inline cudaError_t raise_smem_limit(K kernel, size_t& raised, size_t bytes) {
+inline cudaError_t raise_smem_limit(K kernel, size_t& raised, size_t bytes, size_t floor = 48 * 1024) {
+    if (bytes <= floor) return cudaSuccess;
     static std::mutex mu;
     std::lock_guard<std::mutex> lk(mu);
     if (bytes <= raised) return cudaSuccess;
