@@ -564,7 +564,8 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": dt, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128 (FP64 complex)", "data": "synthetic (seeded)",
-        "config": {"workload": "Hubbard 8x8 NL fdPA (same as ours)", "name": args.config},
+        "config": {"workload": WORKLOADS.get(args.config, args.config), "name": args.config,
+                   "parallelism": "host cores (OpenMP), rank 0 only"},
         "cpu_baseline": {"value": dt, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full iterations of the workload (C++ restatement of the reference "
                                    f"algorithm; Julia reference not runnable here)"},
