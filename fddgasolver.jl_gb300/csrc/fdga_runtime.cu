@@ -1091,6 +1091,8 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
 }
 
 int run_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
+    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA)  // (the graph table holds these two)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the tangent map covers the fdPA and scPA strategies");
     int r = ensure_tangent(h);
     if (r) return r;
     Graph& g = h->tan.graphs[h->precision][strategy][update_sigma][hartree];

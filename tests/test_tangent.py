@@ -132,3 +132,16 @@ def test_frule_hubbard8x8_shapes():
     _, j32 = gpu.frule(v)
     assert 0 < blockwise_rel_err(cfg, j32, j64) < 2e-5
     gpu.close()
+
+
+def test_tangent_refuses_strategies_without_a_tangent_map():
+    """The tangent graphs exist for :fdPA and :scPA; other strategies are refused, not indexed."""
+    from fdgasolver import _lib
+    gpu = make_gpu(NL4, True)
+    x = gpu.flatten()
+    gpu.frule(_dir(np.random.default_rng(1), x.size))
+    with pytest.raises(_lib.FdgaError) as e:
+        gpu.tangent_repeat(1, "fdPA_1loop")
+    assert e.value.code == 2  # FDGA_ERR_UNSUPPORTED
+    gpu.tangent_repeat(1, "fdPA")  # still usable
+    gpu.close()
