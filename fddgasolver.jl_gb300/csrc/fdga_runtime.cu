@@ -1717,6 +1717,7 @@ int fdga_dyson_bubbles(fdga_handle* h) {
 
 int fdga_interpolate_solver(fdga_handle* ho, fdga_handle* hi) {
     if (!ho || !hi) return fail(ho, FDGA_ERR_ARG, "null handle");
+    if (ho == hi) return fail(ho, FDGA_ERR_ARG, "source and target must be different solvers");
     if (!ho->finalized || !hi->finalized) return fail(ho, FDGA_ERR_STATE, "fdga_finalize has not been called");
     if (ho->d.local || hi->d.local)
         return fail(ho, FDGA_ERR_UNSUPPORTED, "interpolate_solver! is defined for the nonlocal solver");
@@ -3064,13 +3065,21 @@ int fdga_batch_create(fdga_handle* const* hs, int n, fdga_batch** out) {
     if (!hs || n < 1 || !out) { g_create_error = "invalid batch arguments"; return FDGA_ERR_ARG; }
     for (int i = 0; i < n; ++i)
         if (!hs[i] || !hs[i]->finalized) { g_create_error = "every batch member must be a finalized handle"; return FDGA_ERR_STATE; }
+    {  // each member's state is written by its own branch of the batch graph: no handle twice
+        std::vector<const fdga_handle*> v(hs, hs + n);
+        std::sort(v.begin(), v.end());
+        if (std::adjacent_find(v.begin(), v.end()) != v.end()) {
+            g_create_error = "a handle appears twice in the batch";
+            return FDGA_ERR_ARG;
+        }
+    }
     fdga_batch* b = new fdga_batch();
     b->hs.assign(hs, hs + n);
     if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&b->ev[0]) != cudaSuccess || cudaEventCreate(&b->ev[1]) != cudaSuccess) {
         g_create_error = "batch stream/event creation failed";
-        delete b;
+        fdga_batch_destroy(b);  // releases what was created
         return FDGA_ERR_CUDA;
     }
     b->join.resize(n);

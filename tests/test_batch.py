@@ -70,3 +70,15 @@ def test_batch_rejects_bad_arguments():
     out = ctypes.c_void_p()
     assert lib.fdga_batch_create(None, 0, ctypes.byref(out)) != 0
     assert lib.fdga_batch_iterate(None, 0, 0) != 0
+
+
+@pytest.mark.gpu
+def test_batch_rejects_a_handle_twice():
+    """Each member's state is written by its own branch of the batch graph."""
+    from fdgasolver import _lib
+    from fdgasolver.solver import Batch
+    a = make_gpu(MEMBERS[0], True)
+    with pytest.raises(_lib.FdgaError) as e:
+        Batch([a, a])
+    assert e.value.code == 1  # FDGA_ERR_ARG
+    a.close()

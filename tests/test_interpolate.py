@@ -155,3 +155,14 @@ def test_interpolate_solver(ci, co, sym):
     assert _rel(So.get("G"), G) < 1e-13
     Si.close()
     So.close()
+
+
+def test_interpolate_solver_refuses_in_place():
+    """Source and target must be different solvers (the kernels read one and write the other)."""
+    from fdgasolver import _lib
+    from fdgasolver.solver import interpolate_solver
+    S = make_gpu(dict(BASE, L=4), False)
+    with pytest.raises(_lib.FdgaError) as e:
+        interpolate_solver(S, S)
+    assert e.value.code == 1  # FDGA_ERR_ARG
+    S.close()
