@@ -129,7 +129,7 @@ cudaError_t launch_fourier_interp(cudaStream_t s, int kind, const cplx* in, cplx
         default: rows_o = o.N3O * o.N3n * o.N3n; rows_i = i.N3O * i.N3n * i.N3n; break;
     }
     const size_t smem = fourier_interp_smem(o, i);
-    static size_t raised = 0;
+    static SmemRecord raised;
     cudaError_t e = raise_smem_limit(k_fourier_interp, raised, smem);
     if (e != cudaSuccess) return e;
     const int threads = std::min(256, std::max(32, ((std::max(i.L * i.L, o.L * o.L) + 31) / 32) * 32));

@@ -288,7 +288,7 @@ static size_t k3_tc_smem(const Dims& d) { return 2 * ((size_t)2 * A_BYTES + (siz
 
 cudaError_t prepare_bse_K3_tc(const Dims& d) {
     // the dynamic shared-memory limit is raised once per size, before any graph capture
-    static size_t set0 = 0, set1 = 0, set2 = 0;
+    static SmemRecord set0, set1, set2;
     const size_t smem = k3_tc_smem(d);
     cudaError_t e = raise_smem_limit(k_bse_K3_tc<0>, set0, smem, 0);  // (static shared memory too)
     if (e == cudaSuccess) e = raise_smem_limit(k_bse_K3_tc<1>, set1, smem, 0);

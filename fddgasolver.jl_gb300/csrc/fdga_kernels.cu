@@ -1427,7 +1427,7 @@ static cudaError_t launch_bubble_dft(cudaStream_t s, const G* GR, const G* tGR, 
     int tv = 32;
     while (tv > 1 && (size_t)(4 * tv * NR + d.L) * sizeof(C) > 160 * 1024) tv >>= 1;
     const size_t shm = (size_t)(4 * tv * NR + d.L) * sizeof(C);
-    static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
+    static SmemRecord shm_set;  // raised once, outside graph capture (first call is from fdga_finalize)
     cudaError_t e = raise_smem_limit(k_bubble_nl<TAN, C, G>, shm_set, shm);
     if (e != cudaSuccess) return e;
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
@@ -1447,7 +1447,7 @@ static cudaError_t launch_bubble_fft(cudaStream_t s, const cplx* GR, const cplx*
     int tv = 32;
     while (tv > 1 && (size_t)2 * tv * BS * sizeof(cplx) > 80 * 1024) tv >>= 1;
     const size_t shm = (size_t)2 * tv * BS * sizeof(cplx);
-    static size_t shm_set = 0;  // raised once, outside graph capture (first call is from fdga_finalize)
+    static SmemRecord shm_set;  // raised once, outside graph capture (first call is from fdga_finalize)
     cudaError_t e = raise_smem_limit(k_bubble_fft<L, cplx, cplx, TAN>, shm_set, shm);
     if (e != cudaSuccess) return e;
     dim3 grid((d.NPw + tv - 1) / tv, d.NPO);
@@ -1627,7 +1627,7 @@ static size_t k2_row_smem(const Dims& d) {
 template <class K>
 static cudaError_t k2_smem_attr(K kernel, size_t smem) {
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
-    static size_t raised = 0;  // one record per kernel instantiation
+    static SmemRecord raised;  // one record per kernel instantiation
     return raise_smem_limit(kernel, raised, smem);
 }
 static unsigned warp_grid(const ChanWork& cw, int nch) {

@@ -10,19 +10,28 @@
 
 namespace fdga {
 
-// Raises a kernel's dynamic shared-memory limit to at least `bytes`; `raised` is the caller's record
-// of the largest limit set for that kernel.  One process-wide lock serialises the check and the
-// update, so concurrent launchers never lower a limit another thread raised.  Sizes up to `floor`
-// need no raise (48 KB for a kernel without static shared memory; the default limit counts both
-// kinds, so a kernel with static shared memory passes 0 and raises before any graph capture).
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the current device; `raised`
+// is the caller's record of the largest limit set for that kernel, one entry per device ordinal
+// (cudaFuncSetAttribute acts on the current device only).  One process-wide lock serialises the check
+// and the update, so concurrent launchers never lower a limit another thread raised.  Sizes up to
+// `floor` need no raise (48 KB for a kernel without static shared memory; the default limit counts
+// both kinds, so a kernel with static shared memory passes 0 and raises before any graph capture).
+struct SmemRecord {
+    static constexpr int kMaxDevices = 64;
+    size_t bytes[kMaxDevices] = {};
+};
 template <class K>
-inline cudaError_t raise_smem_limit(K kernel, size_t& raised, size_t bytes, size_t floor = 48 * 1024) {
+inline cudaError_t raise_smem_limit(K kernel, SmemRecord& raised, size_t bytes, size_t floor = 48 * 1024) {
     if (bytes <= floor) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= SmemRecord::kMaxDevices) return cudaErrorInvalidDevice;
     static std::mutex mu;
     std::lock_guard<std::mutex> lk(mu);
-    if (bytes <= raised) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) raised = bytes;
+    if (bytes <= raised.bytes[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) raised.bytes[dev] = bytes;
     return e;
 }
 

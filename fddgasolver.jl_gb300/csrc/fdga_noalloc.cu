@@ -19,7 +19,7 @@
 #include <string>
 
 #include "../../include/fdga.h"
-#include "fdga_device.cuh"
+#include "fdga_kernels.h"
 
 namespace fdga_internal {
 void set_create_error(const std::string& msg);  // fdga_create_error() text, fdga_runtime.cu
@@ -32,10 +32,11 @@ using fdga::Dims;
 using fdga::fin;
 using fdga::mk;
 
-// The shared work array: every call on a device uses (and overwrites) this one buffer.
+// The shared work array: one instance per device; every call on that device uses (and overwrites) it.
 __device__ __align__(256) cplx g_bubble_scratch[FDGA_BUBBLE_NOALLOC_MAX_ELEMS];
 
-constexpr int kMaxL = 64;
+constexpr int kMaxL = 64;        // twiddle table size
+constexpr int kMaxLattice = 56;  // largest L whose bubble tile (one frequency) fits the shared memory
 struct Twiddles {
     cplx m[kMaxL];  // e^{-2πi j/L}
     cplx p[kMaxL];  // e^{+2πi j/L}
@@ -150,7 +151,7 @@ extern "C" int fdga_bubble_noalloc(const fdga_config* c, const double* G, double
     if (c->nG < 1 || c->nK1 < 1 || c->mPi_factor < 1 || c->L < 1 || !(c->T > 0)) return bad(FDGA_ERR_ARG, "invalid sizes");
     if (c->LG != c->L) return bad(FDGA_ERR_UNSUPPORTED, "L_G != L");
     if (c->local && c->L != 1) return bad(FDGA_ERR_ARG, "the local solver has L = 1");
-    if (c->L > kMaxL) return bad(FDGA_ERR_ARG, "L larger than 64");
+    if (c->L > kMaxLattice) return bad(FDGA_ERR_ARG, "L = " + std::to_string(c->L) + " exceeds the maximum lattice size 56");
     const size_t NG = 2 * (size_t)c->nG, NR = (size_t)c->L * c->L;
     if (NG * NR > (size_t)FDGA_BUBBLE_NOALLOC_MAX_ELEMS)
         return bad(FDGA_ERR_ARG, "2nG*L*L = " + std::to_string(NG * NR) + " exceeds the work-array maximum of " +
@@ -162,7 +163,7 @@ extern "C" int fdga_bubble_noalloc(const fdga_config* c, const double* G, double
     int tv = 32;
     while (tv > 1 && (size_t)4 * tv * NR * sizeof(cplx) > 160 * 1024) tv >>= 1;
     const size_t shm = (size_t)4 * tv * NR * sizeof(cplx);
-    if (shm > 200 * 1024) return bad(FDGA_ERR_ARG, "momentum mesh too large for the shared-memory tile");
+    if (shm > 200 * 1024) return bad(FDGA_ERR_ARG, "momentum mesh too large for the shared-memory tile");  // (L <= 56 fits)
     cplx* GR = nullptr;
     int r = scratch_address(&GR);
     if (r) return r;
@@ -173,7 +174,8 @@ extern "C" int fdga_bubble_noalloc(const fdga_config* c, const double* G, double
         tw.p[j] = mk(std::cos(a), std::sin(a));
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaFuncSetAttribute(k_noalloc_bubble, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    static fdga::SmemRecord smem_raised;  // per device, under the library's shared-memory lock
+    cudaError_t e = fdga::raise_smem_limit(k_noalloc_bubble, smem_raised, shm);
     if (e != cudaSuccess) return bad(FDGA_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
     const size_t ng = NR * NG;
     k_noalloc_greal<<<(unsigned)((ng + 127) / 128), 128, 0, s>>>(reinterpret_cast<const cplx*>(G), GR, tw, d);

@@ -3082,8 +3082,15 @@ int fdga_batch_create(fdga_handle* const* hs, int n, fdga_batch** out) {
         fdga_batch_destroy(b);  // releases what was created
         return FDGA_ERR_CUDA;
     }
-    b->join.resize(n);
-    for (auto& e : b->join) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    b->join.assign(n, nullptr);
+    for (auto& e : b->join) {
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            e = nullptr;
+            g_create_error = "batch join event creation failed";
+            fdga_batch_destroy(b);
+            return FDGA_ERR_CUDA;
+        }
+    }
     *out = b;
     return FDGA_OK;
 }
@@ -3093,7 +3100,7 @@ void fdga_batch_destroy(fdga_batch* b) {
     for (auto& a : b->exec)
         for (auto& g : a)
             if (g) cudaGraphExecDestroy(g);
-    for (auto e : b->join) cudaEventDestroy(e);
+    for (auto e : b->join) if (e) cudaEventDestroy(e);
     if (b->fork) cudaEventDestroy(b->fork);
     for (auto e : b->ev) if (e) cudaEventDestroy(e);
     if (b->st) cudaStreamDestroy(b->st);

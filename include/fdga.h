@@ -286,14 +286,17 @@ int fdga_launches_per_iteration(const fdga_handle* h, int* n);
  * fdga_finalize computes for G0 (src/nonlocal/bubble.jl:87-158, src/bubble.jl:9-36).
  * No device or host memory is allocated: the work array G(R) lives in one file-scope __device__
  * buffer of FDGA_BUBBLE_NOALLOC_MAX_ELEMS complex values (2 MiB), which every GPU that loads the
- * library holds until the process exits.  Larger problems (2nG*L*L above the maximum, or L > 64)
- * are rejected with FDGA_ERR_ARG and a message in fdga_last_error(NULL).
+ * library holds until the process exits.  Larger problems (2nG*L*L above the maximum, or L > 56,
+ * the largest lattice whose bubble tile fits the shared memory) are rejected with FDGA_ERR_ARG and
+ * a message in fdga_last_error(NULL), before any device work.
  * The first call on a device looks up the buffer's device address (cudaGetSymbolAddress with that
- * device current); make that first call before any stream capture.
+ * device current) and raises the kernel's shared-memory limit there; make that first call before
+ * any stream capture.
  * Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and the call returns
- * without synchronising.  All calls share the one buffer and it keeps the last call's contents,
- * so calls whose kernels overlap on the GPU (different streams or threads without ordering)
- * race on it: serialise them. */
+ * without synchronising.  The buffer is per device: all calls on one device share it and it keeps
+ * the last call's contents, so calls on the same device whose kernels overlap on the GPU (different
+ * streams or threads without ordering) race on it: serialise them.  Calls on different devices do
+ * not share it. */
 #define FDGA_BUBBLE_NOALLOC_MAX_ELEMS 131072
 int fdga_bubble_noalloc(const fdga_config* cfg, const double* G, double* Pipp, double* Piph, void* stream);
 

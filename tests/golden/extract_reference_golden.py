@@ -7,7 +7,7 @@ that pin the parquet-iteration path:
 * test/test_siam_fdPA.jl:179            -- Σ(πT) of the fdPA solve from a Vertex-valued reference
 * test/test_hubbard.jl:84-88            -- Hubbard occupations
 
-Usage: python tests/golden/extract_reference_golden.py [reference_root]
+Usage: python tests/golden/extract_reference_golden.py <reference_root>
 The reference checkout is read only here; tests use the committed JSON.
 """
 import json
@@ -67,8 +67,9 @@ def main(root: str) -> dict:
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    data = main(root)
+    if len(sys.argv) != 2:
+        sys.exit("usage: extract_reference_golden.py <path of the fdDGAsolver.jl checkout>")
+    data = main(sys.argv[1])
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "reference_golden.json"), "w") as f:
         json.dump(data, f, indent=1)

@@ -80,18 +80,59 @@ def test_noalloc_bubble_matches_finalize_two_calls():
         assert np.abs(ph - ph_ref).max() <= TOL * np.abs(ph_ref).max()
 
 
-def test_noalloc_rejects_sizes_beyond_the_work_array():
-    """Size validation happens before any device work; checked where no CUDA device exists."""
-    try:
-        import torch
-        if torch.cuda.is_available():
-            pytest.skip("validation-only check runs on hosts without a GPU")
-    except ImportError:
-        pass
+def _oracle_bubbles(local, G, nK1, L, f, T):
+    """Π0 of G0 = G from the CPU oracle (the restatement of src/nonlocal/bubble.jl / src/bubble.jl)."""
+    from oracle import oracle as O
+    orc = O.OracleSolver(nG=G.shape[0] // 2, nK1=nK1, nK2=(2, 2), nK3=(1, 2), T=T, U=1.0, L=L, local=bool(local),
+                         mPi_factor=f)
+    orc.set("Gbare", G)
+    orc.set("G0", G)
+    orc.finalize()
+    return orc.get("Pi0pp"), orc.get("Pi0ph")
+
+
+@pytest.mark.gpu
+def test_noalloc_bubble_matches_oracle():
+    """The same two calls against the oracle's bubbles directly."""
+    import fdgasolver as F
     from fdgasolver import _lib
     lib = _lib.load()
-    cfg = _config(False, 2048, 8, 8, 4, 0.5)  # 2nG*L*L = 262144 > 131072
+    cases = [
+        dict(local=False, nG=8, nK1=8, L=4, f=4, T=0.5,
+             G=lambda: F.hubbard_bare_Green(0.5, 8, 4, mu=0.3, t1=1.0, t2=-0.2)),
+        dict(local=True, nG=16, nK1=12, L=1, f=3, T=0.1,
+             G=lambda: F.siam_bare_Green(0.1, 16, Delta=0.5, e=0.2, D=10.0)),
+    ]
+    for case in cases:
+        G = case["G"]()
+        cfg = _config(case["local"], case["nG"], case["nK1"], case["L"], case["f"], case["T"])
+        pp_ref, ph_ref = _oracle_bubbles(case["local"], G, case["nK1"], case["L"], case["f"], case["T"])
+        pp, ph = _noalloc(lib, cfg, G)
+        assert np.abs(pp - pp_ref).max() <= TOL * np.abs(pp_ref).max()
+        assert np.abs(ph - ph_ref).max() <= TOL * np.abs(ph_ref).max()
+
+
+def _check_rejections():
+    """Both limits are checked on the host before any device work, so host buffers are safe here."""
+    from fdgasolver import _lib
+    lib = _lib.load()
     buf = (ctypes.c_double * 2)()
+    cfg = _config(False, 2048, 8, 8, 4, 0.5)  # 2nG*L*L = 262144 > 131072
     rc = lib.fdga_bubble_noalloc(ctypes.byref(cfg), buf, buf, buf, None)
     assert rc == 1  # FDGA_ERR_ARG
     assert b"exceeds the work-array maximum" in lib.fdga_last_error(None)
+    cfg = _config(False, 2, 8, 57, 4, 0.5)  # 2nG*L*L = 12996 fits, but L = 57 > 56
+    rc = lib.fdga_bubble_noalloc(ctypes.byref(cfg), buf, buf, buf, None)
+    assert rc == 1
+    assert b"exceeds the maximum lattice size 56" in lib.fdga_last_error(None)
+
+
+def test_noalloc_rejects_sizes_beyond_the_work_array():
+    """Size validation on a host without a GPU (the library loads without one)."""
+    _check_rejections()
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_sizes_beyond_the_work_array_gpu():
+    """The same rejections in the GPU process that uses the entry point."""
+    _check_rejections()
