@@ -102,6 +102,15 @@ struct Dims {
     int nRO, NRO, nRn, NRn;
     int local;
     double T, U;
+    // extents of the union of the vertex boxes of F and of a Vertex-valued reference vertex F0 (equal
+    // to n1, n2O, n2n, n3n when F0 is a RefVertex): the ω windows of the BSE and SDE sums use them
+    int xn1, xn2O, xn2n, xn3n;
+};
+
+// Box of a channel's K1/K2/K3 (the member names of Dims, so that the channel evaluators take either):
+// the reference vertex F0 of fdDΓA is a Vertex with boxes of its own (src/ParquetSolver.jl:5,88).
+struct Box {
+    int n1, N1, n2O, N2O, n2n, N2n, n3O, N3O, n3n, N3n;
 };
 
 // One channel's K1/K2/K3 and their momentum averages (A* alias K* for the local solver), stored
@@ -115,7 +124,9 @@ struct ChanPT {
     const S* A2;
     const S* A3;
 };
-// Target vertex F: RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x) + γp + γt + γa
+// Target vertex F = F0 + γp + γt + γa.  The reference vertex F0 is RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x),
+// or (has0) a Vertex F0 = RefVertex + γ0p + γ0t + γ0a whose channels g0 have their own box b0
+// (fdDΓA from a solved vertex: ParquetSolver{Q, VT, RefVT} with RefVT a Vertex, src/ParquetSolver.jl:5-88).
 template <class S>
 struct VertPT {
     ChanPT<S> g[3];
@@ -123,7 +134,10 @@ struct VertPT {
     const S* Fp_x;
     const S* Ft_p;
     const S* Ft_x;
-    int noref;  // 1: the RefVertex terms (U and its corrections) read as zero (a tangent vertex)
+    int noref;  // 1: the reference-vertex terms (U, its corrections and F0's channels) read as zero (a tangent vertex)
+    int has0;   // 1: F0 is a Vertex with the channels g0 (box b0) on top of the RefVertex terms
+    ChanPT<S> g0[3];
+    Box b0;
 };
 using ChanP = ChanPT<cplx>;
 using VertP = VertPT<cplx>;
@@ -136,11 +150,15 @@ __device__ __forceinline__ cplxf ldv(const cplxf* p) {
 }
 template <class S> __device__ __forceinline__ S cre(double x) { return S{(decltype(S::x))x, 0}; }
 
-__device__ __forceinline__ size_t ix1(const Dims& d, int P, int m) { return (size_t)P * d.N1 + (m + d.n1 - 1); }
-__device__ __forceinline__ size_t ix2(const Dims& d, int P, int m, int n) {
+// index of a channel element in its box; D = Dims (the solver's own boxes) or Box (the boxes of F0)
+template <class D>
+__host__ __device__ __forceinline__ size_t ix1(const D& d, int P, int m) { return (size_t)P * d.N1 + (m + d.n1 - 1); }
+template <class D>
+__host__ __device__ __forceinline__ size_t ix2(const D& d, int P, int m, int n) {
     return ((size_t)P * d.N2O + (m + d.n2O - 1)) * d.N2n + (n + d.n2n);
 }
-__device__ __forceinline__ size_t ix3(const Dims& d, int P, int m, int n, int np) {
+template <class D>
+__host__ __device__ __forceinline__ size_t ix3(const D& d, int P, int m, int n, int np) {
     return (((size_t)P * d.N3O + (m + d.n3O - 1)) * d.N3n + (n + d.n3n)) * d.N3n + (np + d.n3n);
 }
 __device__ __forceinline__ size_t ixPi(const Dims& d, int P, int m, int n) {
@@ -148,16 +166,16 @@ __device__ __forceinline__ size_t ixPi(const Dims& d, int P, int m, int n) {
 }
 __device__ __forceinline__ size_t ixG(const Dims& d, int k, int n) { return (size_t)k * d.NG + (n + d.nG); }
 
-template <class S>
-__device__ __forceinline__ S k1v(const ChanPT<S>& c, const Dims& d, int m, int P) {
+template <class S, class D>
+__device__ __forceinline__ S k1v(const ChanPT<S>& c, const D& d, int m, int P) {
     return P == KAVG ? ldv(c.A1 + (m + d.n1 - 1)) : ldv(c.K1 + ix1(d, P, m));
 }
-template <class S>
-__device__ __forceinline__ S k2v(const ChanPT<S>& c, const Dims& d, int m, int n, int P) {
+template <class S, class D>
+__device__ __forceinline__ S k2v(const ChanPT<S>& c, const D& d, int m, int n, int P) {
     return P == KAVG ? ldv(c.A2 + ix2(d, 0, m, n)) : ldv(c.K2 + ix2(d, P, m, n));
 }
-template <class S>
-__device__ __forceinline__ S k3v(const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
+template <class S, class D>
+__device__ __forceinline__ S k3v(const ChanPT<S>& c, const D& d, int m, int n, int np, int P) {
     return P == KAVG ? ldv(c.A3 + ix3(d, 0, m, n, np)) : ldv(c.K3 + ix3(d, P, m, n, np));
 }
 
@@ -165,8 +183,8 @@ __device__ __forceinline__ S k3v(const ChanPT<S>& c, const Dims& d, int m, int n
 // chan_val writes the value into t and returns true, or returns false (t untouched) where the
 // channel vanishes (Ω outside the K1 box).  The sums start from their first term: GB300's FP64
 // pipe is the bound of every evaluator-heavy kernel, and an addition of zero costs as much as any.
-template <class S>
-__device__ __forceinline__ bool chan_val(S& t, const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
+template <class S, class D>
+__device__ __forceinline__ bool chan_val(S& t, const ChanPT<S>& c, const D& d, int m, int n, int np, int P) {
     if (!bin(m, d.n1)) return false;
     t = k1v(c, d, m, P);
     if (!bin(m, d.n2O)) return true;
@@ -188,8 +206,8 @@ __device__ __forceinline__ bool chan_val(S& t, const ChanPT<S>& c, const Dims& d
     }
     return true;
 }
-template <class S>
-__device__ __forceinline__ S chan_eval(const ChanPT<S>& c, const Dims& d, int m, int n, int np, int P) {
+template <class S, class D>
+__device__ __forceinline__ S chan_eval(const ChanPT<S>& c, const D& d, int m, int n, int np, int P) {
     S t;
     return chan_val(t, c, d, m, n, np, P) ? t : S{0, 0};
 }
@@ -253,6 +271,70 @@ __device__ __forceinline__ S ref_eval(const VertPT<S>& F, const Dims& d, int ch,
     return S{fma(p.x, (R)2, x.x), fma(p.y, (R)2, x.y)};  // 2p is exact: one rounding, as 2p + x
 }
 
+// Channels of a Vertex-valued reference vertex F0 in representation ch, parallel spin, at (Ω,ν,ν')
+// with momentum P: the own channel at P, the other two (frequencies converted) at their momentum
+// average; with ν or ν' at infinity only the own channel (src/vertex.jl:209-284 and
+// src/nonlocal/vertex.jl:69-153, 216-379 applied to F0).  False (t untouched): no channel term.
+template <class S>
+__device__ __forceinline__ bool f0chan_val(S& t, const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np,
+                                           int P) {
+    if (n == FINF || np == FINF) return chan_val(t, F.g0[ch], F.b0, m, n, np, P);
+    const int Pc = (d.Nq == 1) ? 0 : KAVG;
+    bool has = false;
+    S u;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        int a, b, c;
+        conv(ch, r, m, n, np, a, b, c);
+        if (chan_val(u, F.g0[r], F.b0, a, b, c, r == ch ? P : Pc)) {
+            if (has) t += u;
+            else { t = u; has = true; }
+        }
+    }
+    return has;
+}
+// The reference vertex F0 in the parallel spin component: the RefVertex, plus its channels when F0
+// is a Vertex (the RefVertex terms come first, as in the reference's recursion F.F0.F0).
+template <class S>
+__device__ __forceinline__ S f0_pSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P) {
+    S v = ref_pSp(F, d, ch, m, n, np);
+    if (F.has0 && !F.noref) {
+        S t;
+        if (f0chan_val(t, F, d, ch, m, n, np, P)) v += t;
+    }
+    return v;
+}
+// F0 in the crossed spin component.  A RefVertex stores it (Fp_x, Ft_x); a Vertex F0 has it by
+// crossing symmetry, xSp = -pSp at the crossed arguments, for its RefVertex part too
+// (src/vertex.jl:288-313).
+template <class S>
+__device__ __forceinline__ S f0_xSp(const VertPT<S>& F, const Dims& d, int ch, int m, int n, int np, int P) {
+    if (!F.has0) return ref_xSp(F, d, ch, m, n, np);
+    if (ch == CH_P) return -f0_pSp(F, d, CH_P, m, n, (np == FINF) ? FINF : m - np - 1, P);
+    if (ch == CH_T) return -f0_pSp(F, d, CH_A, m, n, np, P);
+    return -f0_pSp(F, d, CH_T, m, n, np, P);
+}
+template <class S>
+__device__ __forceinline__ S f0_eval(const VertPT<S>& F, const Dims& d, int ch, int sp, int m, int n, int np, int P) {
+    using R = decltype(S::x);
+    if (!F.has0) return ref_eval(F, d, ch, sp, m, n, np);
+    if (sp == SP_P) return f0_pSp(F, d, ch, m, n, np, P);
+    if (sp == SP_X) return f0_xSp(F, d, ch, m, n, np, P);
+    const S p = f0_pSp(F, d, ch, m, n, np, P), x = f0_xSp(F, d, ch, m, n, np, P);
+    return S{fma(p.x, (R)2, x.x), fma(p.y, (R)2, x.y)};
+}
+// F0(Ω, ω, ∞) - U in the spin combination of channel ch's BSE (pSp for p and a, dSp = 2 pSp + xSp for
+// t): zero for a RefVertex; for a Vertex F0 its own channel's K1 + K2(ω) (t: 2 γ0t - γ0a, since
+// xSp(t) = -pSp(a) at these arguments).  The factor F0r of the K1/K2 BSEs is U_sp plus this.
+template <class S>
+__device__ __forceinline__ S f0_right(const VertPT<S>& F, int ch, int m, int n, int P) {
+    using R = decltype(S::x);
+    if (!F.has0) return S{0, 0};
+    if (ch != CH_T) return chan_eval(F.g0[ch], F.b0, m, n, FINF, P);
+    const S t = chan_eval(F.g0[CH_T], F.b0, m, n, FINF, P), a = chan_eval(F.g0[CH_A], F.b0, m, n, FINF, P);
+    return S{fma(t.x, (R)2, -a.x), fma(t.y, (R)2, -a.y)};
+}
+
 // Flags of the vertex evaluator: bit 0 F0, bit 1 γp, bit 2 γt, bit 3 γa.
 enum { FL_F0 = 1, FL_GP = 2, FL_GT = 4, FL_GA = 8, FL_ALL = 15 };
 __device__ __forceinline__ int swap_ta(int fl) {
@@ -271,7 +353,7 @@ __device__ __forceinline__ S vert_pSp(const VertPT<S>& F, const Dims& d, int ch,
         else { v = x; has = true; }
     };
     if (fl & FL_F0) {  // (zero for a tangent vertex; kept so that `has` is known at compile time)
-        v = ref_pSp(F, d, ch, m, n, np);
+        v = f0_pSp(F, d, ch, m, n, np, P);
         has = true;
     }
     if (n == FINF || np == FINF) {
@@ -328,6 +410,20 @@ __device__ __forceinline__ S pSp_k2diff(const VertPT<S>& F, const Dims& d, int c
             put(t);
         }
     }
+    if (F.has0 && !F.noref) {  // a Vertex F0 reduces the same way: its own K3 and its other two channels
+        const Box& b = F.b0;
+        if (bin(m, b.n1) && bin(m, b.n2O) && fin(n, b.n2n) && fin(np, b.n2n) && bin(m, b.n3O) && fin(n, b.n3n) &&
+            fin(np, b.n3n))
+            put(k3v(F.g0[ch], b, m, n, np, P));
+        const int Pc0 = (d.Nq == 1) ? 0 : KAVG;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            if (r == ch) continue;
+            int a, bb, c;
+            conv(ch, r, m, n, np, a, bb, c);
+            if (chan_val(t, F.g0[r], b, a, bb, c, Pc0)) put(t);
+        }
+    }
     if (bin(m, d.n1) && bin(m, d.n2O) && fin(n, d.n2n) && fin(np, d.n2n) && bin(m, d.n3O) && fin(n, d.n3n) &&
         fin(np, d.n3n))
         put(k3v(F.g[ch], d, m, n, np, P));
@@ -380,6 +476,20 @@ __device__ __forceinline__ void pSp_k2diff2(const VertPT<S>& F, const VertPT<S>&
             if (ref_val(t, F.Ft_x, d, m, np, n)) put(-t, S{0, 0});
         } else if (ref_val(t, ch == CH_P ? F.Fp_p : F.Ft_p, d, m, n, np)) {
             put(t, S{0, 0});
+        }
+        if (F.has0) {  // the reduced difference of a Vertex F0 (constant: no tangent part)
+            const Box& b = F.b0;
+            if (bin(m, b.n1) && bin(m, b.n2O) && fin(n, b.n2n) && fin(np, b.n2n) && bin(m, b.n3O) && fin(n, b.n3n) &&
+                fin(np, b.n3n))
+                put(k3v(F.g0[ch], b, m, n, np, P), S{0, 0});
+            const int Pc0 = (d.Nq == 1) ? 0 : KAVG;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                if (r == ch) continue;
+                int a, bb, c;
+                conv(ch, r, m, n, np, a, bb, c);
+                if (chan_val(t, F.g0[r], b, a, bb, c, Pc0)) put(t, S{0, 0});
+            }
         }
     }
     if (bin(m, d.n1) && bin(m, d.n2O) && fin(n, d.n2n) && fin(np, d.n2n) && bin(m, d.n3O) && fin(n, d.n3n) &&

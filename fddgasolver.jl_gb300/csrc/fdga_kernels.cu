@@ -416,9 +416,25 @@ __global__ void k_qavg(const ChanArrays in, ChanArraysW out, Dims d) {
 // symmetry-class representatives; all blocks without groups); "left" caches use (Ω, ω=a, ν'=b),
 // "right" caches (Ω, ν=a, ω=b).  Output order: Γpx F0p F0a F0t Γpp Γa Γt Fp Fa Ft.
 // ---------------------------------------------------------------------------------------------
+// V0 (every vertex-evaluating kernel): compiled with the evaluation of a Vertex-valued reference
+// vertex F0.  The plain instantiation clears has0 in a local copy of the view, so the compiler drops
+// those paths and the RefVertex kernels keep their registers.
+template <bool V0, class S>
+__device__ __forceinline__ VertPT<S> vert_spec(const VertPT<S>& F) {
+    VertPT<S> G = F;
+    if constexpr (!V0) G.has0 = 0;
+    return G;
+}
+template <bool V0, class S>
+__device__ __forceinline__ TanArgsT<S> tan_spec(const TanArgsT<S>& T) {
+    TanArgsT<S> U = T;
+    if constexpr (!V0) U.F.has0 = 0;
+    return U;
+}
 // S: vertex storage and arithmetic (cplx; cplxf reads the FP32 mirror of the mixed map).
-template <class S>
-__global__ void k_build_cache(VertPT<S> F, Caches C, const int* blocks, int nblocks, Dims d) {
+template <class S, bool V0>
+__global__ void k_build_cache(VertPT<S> Fin, Caches C, const int* blocks, int nblocks, Dims d) {
+    const VertPT<S> F = vert_spec<V0>(Fin);
     using R = decltype(S::x);
     const size_t bs = (size_t)d.N3n * d.N3n;
     const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -433,9 +449,9 @@ __global__ void k_build_cache(VertPT<S> F, Caches C, const int* blocks, int nblo
     // left
     S v[10];
     v[0] = vert_eval(F, d, CH_P, SP_X, m, a, b, P, FL_GT | FL_GA);
-    v[1] = ref_xSp(F, d, CH_P, m, a, b) - ref_xSp(F, d, CH_P, m, a, FINF);
-    const S f0a = ref_pSp(F, d, CH_A, m, a, b) - ref_pSp(F, d, CH_A, m, a, FINF);
-    const S f0t = ref_pSp(F, d, CH_T, m, a, b) - ref_pSp(F, d, CH_T, m, a, FINF);
+    v[1] = f0_xSp(F, d, CH_P, m, a, b, P) - f0_xSp(F, d, CH_P, m, a, FINF, P);
+    const S f0a = f0_pSp(F, d, CH_A, m, a, b, P) - f0_pSp(F, d, CH_A, m, a, FINF, P);
+    const S f0t = f0_pSp(F, d, CH_T, m, a, b, P) - f0_pSp(F, d, CH_T, m, a, FINF, P);
     v[2] = f0a;
     v[3] = f0t * (R)2 - f0a;
     // right
@@ -554,7 +570,10 @@ __global__ void k_pisum_R(const G* GR, const G* tGR, const cplx* T0, cplx* SR, D
 // S_X(ch, P, Ω) = Σ_ω [(Π-Π0)(Ω,ω,P) U + Π(Ω,ω,P) FL(Ω,ω̃,∞)]: the ω-sum of the BSE's right factor
 // (src/BSEa/BSEa_K1.jl:43, BSEa_K2.jl:185), from the row sums and the K2 window of FL.
 // Layout SX[ch][P][Ω] with Ω over the K1 box; SPi/SPi0 [w][P][Ω] with w = 0 pp, 1 ph.
-__global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0, FLP FL, cplx* SX, Dims d) {
+// A Vertex-valued F0 adds (Π-Π0)(Ω,ω) [F0(Ω,ω̃,∞) - U] = (SΠ - SΠ0) k0 + Σ_{ω̃ ∈ F0's K2 box}
+// (Π-Π0)(ω) [f0_right(ω̃) - k0], k0 = its own channel's K1 (f0_right at ω̃ = ∞).
+__global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* Pi0pp, const cplx* Pi0ph, const cplx* SPi,
+                     const cplx* SPi0, FLP FL, VertP F0v, cplx* SX, Dims d) {
     const size_t per = (size_t)d.Nq * d.NPO;
     const size_t i = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;  // warp per output
     const int lane = threadIdx.x & 31;
@@ -573,13 +592,30 @@ __global__ void k_sx(const cplx* Pipp, const cplx* Piph, const cplx* SPi, const 
             v += Pi[ixPi(d, P, m, n)] * fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, ch, m, nt, P);
         }
     }
+    cplx k0 = mk(0, 0);
+    if (F0v.has0 && bin(m, F0v.b0.n1)) {
+        const cplx* Pi0 = w ? Pi0ph : Pi0pp;
+        k0 = f0_right(F0v, ch, m, FINF, P);
+        if (bin(m, F0v.b0.n2O)) {
+            for (int t = lane; t < F0v.b0.N2n; t += 32) {
+                const int nt = t - F0v.b0.n2n;
+                const int n = (ch == CH_P) ? m - nt - 1 : nt;
+                if (!fin(n, d.nPw)) continue;
+                const size_t ip = ixPi(d, P, m, n);
+                v += (Pi[ip] - Pi0[ip]) * (f0_right(F0v, ch, m, nt, P) - k0);
+            }
+        }
+    }
     v = warp_sum(v);
-    if (lane == 0) SX[i] = (SPi[w * per + r] - SPi0[w * per + r]) * d.U + v;
+    if (lane == 0) {
+        const cplx ds = SPi[w * per + r] - SPi0[w * per + r];
+        SX[i] = F0v.has0 ? ds * (mk(d.U, 0) + k0) + v : ds * d.U + v;
+    }
 }
 
 // Tangent of S_X: dS_X = dSΠ U + Σ_ω [dΠ FL(Ω,ω̃,∞) + Π dFL(Ω,ω̃,∞)]  (SΠ0 is constant).
 __global__ void k_sx_tan(const cplx* Pipp, const cplx* Piph, const cplx* tPipp, const cplx* tPiph, const cplx* tSPi,
-                         FLP FL, FLP tFL, cplx* tSX, Dims d) {
+                         FLP FL, FLP tFL, VertP F0v, cplx* tSX, Dims d) {
     const size_t per = (size_t)d.Nq * d.NPO;
     const size_t i = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -601,8 +637,20 @@ __global__ void k_sx_tan(const cplx* Pipp, const cplx* Piph, const cplx* tPipp, 
             v += Pi[ip] * fl_right(tFL.K2[CH_P], tFL.K2[CH_T], tFL.K2[CH_A], d, ch, m, nt, P);
         }
     }
+    cplx k0 = mk(0, 0);  // a Vertex-valued F0 (constant): dΠ times its F0(Ω,ω̃,∞) - U, as in k_sx
+    if (F0v.has0 && bin(m, F0v.b0.n1)) {
+        k0 = f0_right(F0v, ch, m, FINF, P);
+        if (bin(m, F0v.b0.n2O)) {
+            for (int t = lane; t < F0v.b0.N2n; t += 32) {
+                const int nt = t - F0v.b0.n2n;
+                const int n = (ch == CH_P) ? m - nt - 1 : nt;
+                if (!fin(n, d.nPw)) continue;
+                v += tPi[ixPi(d, P, m, n)] * (f0_right(F0v, ch, m, nt, P) - k0);
+            }
+        }
+    }
     v = warp_sum(v);
-    if (lane == 0) tSX[i] = tSPi[w * per + r] * d.U + v;
+    if (lane == 0) tSX[i] = F0v.has0 ? tSPi[w * per + r] * (mk(d.U, 0) + k0) + v : tSPi[w * per + r] * d.U + v;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -628,22 +676,26 @@ __device__ __forceinline__ void bse_K1_body(const VertPT<S>& F, const FLPT<S>& F
     if constexpr (TAN) tc = vert_eval(T.F, d, CH, SP, m, FINF, FINF, P);
     const cplx* tPi = (CH == CH_P) ? T.pp : T.ph;
     S acc{0, 0};
-    if (bin(m, d.n2O)) {
-        for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
+    // F(Ω,∞,ω) varies in the K2 boxes of F and (a Vertex-valued) F0: the extents xn2O, xn2n
+    if (bin(m, d.xn2O)) {
+        for (int n = -d.xn2n + lane; n < d.xn2n; n += 32) {
             if (!fin(n, d.nPw)) continue;
             const int wt = cross(CH, m, n);
             const S Fl = vert_eval(F, d, CH, SP, m, FINF, n, P) - c;
             const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
             const size_t ip = ixPi(d, P, m, n);
             const S pi = to_c<S>(ldg(Pi + ip)), pi0 = Pi0 ? to_c<S>(ldg(Pi0 + ip)) : S{0, 0};
+            // F0r = F0(Ω, ω̃, ∞) = U_sp (RefVertex), plus the own channel of a Vertex-valued F0
+            const S U0 = F.has0 ? cre<S>(d.U) + f0_right(F, CH, m, wt, P) : cre<S>(d.U);
             if constexpr (!TAN) {
-                acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
+                if (F.has0) acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * U0), acc);
+                else acc = cfma(Fl, cfma(pi, FLr, (pi - pi0) * (R)d.U), acc);
             } else {
-                const S X = cfma(pi, FLr, (pi - pi0) * (R)d.U);
+                const S X = F.has0 ? cfma(pi, FLr, (pi - pi0) * U0) : cfma(pi, FLr, (pi - pi0) * (R)d.U);
                 const S tFl = vert_eval(T.F, d, CH, SP, m, FINF, n, P) - tc;
                 const S tFLr = fl_right(T.FL.K2[CH_P], T.FL.K2[CH_T], T.FL.K2[CH_A], d, CH, m, wt, P);
                 const S tpi = to_c<S>(ldg(tPi + ip));
-                const S tX = cfma(tpi, FLr + cre<S>(d.U), pi * tFLr);
+                const S tX = cfma(tpi, FLr + U0, pi * tFLr);
                 acc = cfma(tFl, X, cfma(Fl, tX, acc));
             }
         }
@@ -677,6 +729,25 @@ __device__ __forceinline__ void bse_L_K2_body(const VertPT<S>& F, const cplx* Pi
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     constexpr int IRR = (CH == CH_P) ? (FL_GT | FL_GA) : (CH == CH_T ? (FL_GP | FL_GA) : (FL_GP | FL_GT));
     S acc{0, 0};
+    if (F.has0) {
+        // a Vertex-valued F0: the factor F0r = F0(Ω, ω̃, ∞) (local) or F0(Ω, ω, ∞) (nonlocal) depends on ω
+        if (d.local) {
+            for (int n = -d.nPw + lane; n < d.nPw; n += 32) {
+                const S Gp = vert_eval(F, d, CH, SP, m, nu, n, P, IRR);
+                const S f0r = cre<S>(d.U) + f0_right(F, CH, m, cross(CH, m, n), P);
+                acc = cfma(Gp, to_c<S>(ldg(Pi0 + ixPi(d, P, m, n))) * f0r, acc);
+            }
+        } else {
+            for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
+                const S Gl = vert_eval(F, d, CH, SP, m, nu, cross(CH, m, n), P, IRR);
+                const S f0r = cre<S>(d.U) + f0_right(F, CH, m, n, P);
+                acc = cfma(Gl, to_c<S>(ldg(Pi0 + ixPi(d, P, m, n))) * f0r, acc);
+            }
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) out[idx] = to_d(acc * (R)(d.T * (CH == CH_T ? -1.0 : 1.0)));
+        return;
+    }
     if (d.local) {
         for (int n = -d.nPw + lane; n < d.nPw; n += 32) {  // local solver: nPw = nPn
             const S Gp = vert_eval(F, d, CH, SP, m, nu, n, P, IRR);
@@ -710,7 +781,7 @@ __device__ __forceinline__ void bse_L_K2_body(const VertPT<S>& F, const cplx* Pi
 // GB300's FP64 pipe bounds this kernel: both take FP64 work out of the per-term loop.
 // TAN: the tangent in one pass, as for K1 (tables X and dX).
 __host__ __device__ __forceinline__ int k2_table_half(const Dims& d) {
-    const int W = d.n2O + d.n2n + d.n1 + d.nRn + 2;
+    const int W = d.xn2O + d.xn2n + d.xn1 + d.nRn + 2;  // (extents over F and a Vertex-valued F0)
     return W < d.nPw ? W : d.nPw;
 }
 // F(Ω,ν,ω) - F(Ω,∞,ω) - F(Ω,ν,∞) + F(Ω,∞,∞) in the spin combination of the K2 BSE of channel CH
@@ -743,8 +814,13 @@ __device__ __forceinline__ void k2_vertex_diff2(const VertPT<S>& F, const VertPT
 // (the t channel's crossed part is the a channel's, by crossing)
 template <class S>
 __device__ __forceinline__ S k2_own(const VertPT<S>& F, const Dims& d, int ch, int m, int nu, int P) {
-    if (!bin(m, d.n1) || !bin(m, d.n2O) || !fin(nu, d.n2n)) return S{0, 0};
-    return k2v(F.g[ch], d, m, nu, P);
+    S v{0, 0};
+    if (bin(m, d.n1) && bin(m, d.n2O) && fin(nu, d.n2n)) v = k2v(F.g[ch], d, m, nu, P);
+    if (F.has0 && !F.noref) {  // the own channel of a Vertex-valued F0 contributes its K2(Ω, ν) too
+        const Box& b = F.b0;
+        if (bin(m, b.n1) && bin(m, b.n2O) && fin(nu, b.n2n)) v += k2v(F.g0[ch], b, m, nu, P);
+    }
+    return v;
 }
 template <int CH, class S>
 __device__ __forceinline__ S k2_c(const VertPT<S>& F, const Dims& d, int m, int nu, int P) {
@@ -777,16 +853,18 @@ __device__ __forceinline__ void bse_K2_row(const VertPT<S>& F, const FLPT<S>& FL
         const S FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
         const S pi = to_c<S>(ldg(Pi + ip)), pi0 = Pi0 ? to_c<S>(ldg(Pi0 + ip)) : S{0, 0};
-        Xt[j] = cfma(pi, FLr, (pi - pi0) * (R)d.U);
+        // F0r = U_sp, plus the own channel of a Vertex-valued F0 (f0_right)
+        const S U0 = F.has0 ? cre<S>(d.U) + f0_right(F, CH, m, wt, P) : cre<S>(d.U);
+        Xt[j] = F.has0 ? cfma(pi, FLr, (pi - pi0) * U0) : cfma(pi, FLr, (pi - pi0) * (R)d.U);
         if constexpr (TAN) {
             const S tFLr = fl_right(T.FL.K2[CH_P], T.FL.K2[CH_T], T.FL.K2[CH_A], d, CH, m, wt, P);
             const S tpi = to_c<S>(ldg(tPi + ip));
-            tXt[j] = cfma(tpi, FLr + cre<S>(d.U), pi * tFLr);
+            tXt[j] = cfma(tpi, FLr + U0, pi * tFLr);
         }
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
+    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.xn1 - 1;
     const size_t is = (size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1);
     for (int it = i0 + warp; it < i1; it += nwarps) {
         const int idx = items ? items[it] : it;
@@ -795,7 +873,7 @@ __device__ __forceinline__ void bse_K2_row(const VertPT<S>& F, const FLPT<S>& FL
         S tc{0, 0};
         if constexpr (TAN) tc = k2_c<CH>(T.F, d, m, nu, P);
         Windows win;
-        win.add(-d.n2n, d.n2n - 1, lo, hi);
+        win.add(-d.xn2n, d.xn2n - 1, lo, hi);
         win.add(-d.nRn, d.nRn - 1, lo, hi);
         win.add(nu - h1, nu + h1, lo, hi);
         win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
@@ -1008,7 +1086,7 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
     const int P = idx / (d.N2n * d.N2O);
     const cplx* tPi = WHICH == 0 ? T.pp : T.ph;
     S acc{0, 0}, accr{0, 0}, c{0, 0}, tc{0, 0};
-    if (use_vertex) {
+    if (use_vertex & 1) {
         if (WHICH == 0) {
             c = chan_eval(F.g[CH_P], d, m, FINF, nu, P);
             if constexpr (TAN) tc = chan_eval(T.F.g[CH_P], d, m, FINF, nu, P);
@@ -1040,6 +1118,28 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
             }
         }
     }
+    // the Vertex level of a Vertex-valued F0 (use_vertex bit 2): the same sums over its channels g0
+    // (box b0), SDE!(Σ, …, F.F0, …) of the reference's recursion; constant in the tangent map
+    S acc0{0, 0}, c0{0, 0};
+    if ((use_vertex & 2) && F.has0) {
+        const Box& b = F.b0;
+        if (WHICH == 0) {
+            c0 = chan_eval(F.g0[CH_P], b, m, FINF, nu, P);
+            for (int t = lane; t < b.N2n; t += 32) {
+                const int n = m - (t - b.n2n) - 1;
+                if (!fin(n, d.nPw)) continue;
+                const S g = chan_eval(F.g0[CH_P], b, m, m - n - 1, nu, P) - c0;
+                acc0 = cfma(to_c<S>(ldg((TAN ? tPi : Pi) + ixPi(d, P, m, n))), g, acc0);
+            }
+        } else {
+            c0 = chan_eval(F.g0[CH_T], b, m, nu, FINF, P) + chan_eval(F.g0[CH_A], b, m, nu, FINF, P);
+            for (int n = -b.n2n + lane; n < b.n2n; n += 32) {
+                if (!fin(n, d.nPw)) continue;
+                const S g = chan_eval(F.g0[CH_T], b, m, nu, n, P) + chan_eval(F.g0[CH_A], b, m, nu, n, P) - c0;
+                acc0 = cfma(to_c<S>(ldg((TAN ? tPi : Pi) + ixPi(d, P, m, n))), g, acc0);
+            }
+        }
+    }
     if (ref_scale != 0.0) {
         for (int t = lane; t < d.NRn; t += 32) {
             const int r = t - d.nRn;
@@ -1053,9 +1153,17 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
     }
     acc = warp_sum(acc) * (R)d.U;
     accr = warp_sum(accr) * (R)d.U;
+    if ((use_vertex & 2) && F.has0) {
+        acc0 = warp_sum(acc0);
+        if (lane == 0) {
+            const size_t is0 = (size_t)P * d.NPO + (m + d.nPO - 1);
+            const cplx* sp0 = TAN ? (WHICH == 0 ? T.SPpp : T.SPph) : SPi;
+            acc += cfma(c0, to_c<S>(ldg(sp0 + is0)), acc0) * (R)d.U;
+        }
+    }
     if (lane == 0) {
         const size_t is = (size_t)P * d.NPO + (m + d.nPO - 1);
-        if (use_vertex) {
+        if (use_vertex & 1) {
             if constexpr (!TAN) {
                 acc += c * (to_c<S>(ldg(SPi + is)) * (R)d.U);
             } else {
@@ -1077,8 +1185,11 @@ __device__ __forceinline__ void sde_L_body(const VertPT<S>& F, const cplx* Pi, c
 // c SΠ + Σ_{K2 box} (F - c) Π - U_sp SΠ0.  For K2 the F difference is ω-independent outside the
 // windows of bse_K2_row and the F0 difference vanishes outside the RefVertex box.
 // ---------------------------------------------------------------------------------------------
+// A Vertex-valued F0 varies in its own K2 box: F0(Ω,∞,ω) = u0 + (F0(Ω,∞,ω) - u0) there, and its
+// difference F0(Ω,ν,ω) - F0(Ω,∞,ω) has the ω-independent part c0 = F0(Ω,ν,∞) - F0(Ω,∞,∞) (its K2(ν))
+// outside the windows, which enlarge to the boxes of F0 (the extents xn1, xn2O, xn2n).
 template <int CH, class S>
-__device__ __forceinline__ void bse_K1_new_body(const VertPT<S>& F, const cplx* Pi, const cplx* SPi,
+__device__ __forceinline__ void bse_K1_new_body(const VertPT<S>& F, const cplx* Pi, const cplx* Pi0, const cplx* SPi,
                                                 const cplx* SPi0, cplx* out, const int* items, int nitems,
                                                 const Dims& d) {
     using R = decltype(S::x);
@@ -1088,24 +1199,27 @@ __device__ __forceinline__ void bse_K1_new_body(const VertPT<S>& F, const cplx* 
     const int m = idx % d.N1 - (d.n1 - 1), P = idx / d.N1;
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     const S c = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
+    const S u0 = f0_eval(F, d, CH, SP, m, FINF, FINF, P);
     S acc{0, 0};
-    if (bin(m, d.n2O)) {
-        for (int n = -d.n2n + lane; n < d.n2n; n += 32) {
+    if (bin(m, d.xn2O)) {
+        for (int n = -d.xn2n + lane; n < d.xn2n; n += 32) {
             if (!fin(n, d.nPw)) continue;
-            acc = cfma(vert_eval(F, d, CH, SP, m, FINF, n, P) - c, to_c<S>(ldg(Pi + ixPi(d, P, m, n))), acc);
+            const size_t ip = ixPi(d, P, m, n);
+            acc = cfma(vert_eval(F, d, CH, SP, m, FINF, n, P) - c, to_c<S>(ldg(Pi + ip)), acc);
+            if (F.has0) acc = acc - (f0_eval(F, d, CH, SP, m, FINF, n, P) - u0) * to_c<S>(ldg(Pi0 + ip));
         }
     }
     acc = warp_sum(acc);
     if (lane == 0) {
         const size_t is = (size_t)P * d.NPO + (m + d.nPO - 1);
-        const S u0 = ref_eval(F, d, CH, SP, m, FINF, FINF);
         const S v = cfma(c, to_c<S>(SPi[is]), acc) - u0 * to_c<S>(SPi0[is]);
         out[idx] = to_d(v * (R)(d.U * d.T * (CH == CH_T ? -1.0 : 1.0)));
     }
 }
 template <int CH, class S>
 __device__ __forceinline__ void bse_K2_new_body(const VertPT<S>& F, const cplx* Pi, const cplx* Pi0, const cplx* SPi,
-                                                cplx* out, const int* items, int nitems, const Dims& d) {
+                                                const cplx* SPi0, cplx* out, const int* items, int nitems,
+                                                const Dims& d) {
     using R = decltype(S::x);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nitems) return;
@@ -1116,10 +1230,11 @@ __device__ __forceinline__ void bse_K2_new_body(const VertPT<S>& F, const cplx* 
     constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     const S cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
     const S c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
-    const S u0 = ref_eval(F, d, CH, SP, m, FINF, FINF);
+    const S u0 = f0_eval(F, d, CH, SP, m, FINF, FINF, P);
+    const S c0 = F.has0 ? f0_eval(F, d, CH, SP, m, nu, FINF, P) - u0 : S{0, 0};  // (zero for a RefVertex)
     Windows win;
-    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
-    win.add(-d.n2n, d.n2n - 1, lo, hi);
+    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.xn1 - 1;
+    win.add(-d.xn2n, d.xn2n - 1, lo, hi);
     win.add(-d.nRn, d.nRn - 1, lo, hi);
     win.add(nu - h1, nu + h1, lo, hi);
     win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
@@ -1128,61 +1243,71 @@ __device__ __forceinline__ void bse_K2_new_body(const VertPT<S>& F, const cplx* 
     S acc{0, 0};
     for (int t = lane; t < win.total; t += 32) {
         const int n = win.at(t);
-        const S Finf = fin(n, d.n2n) ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
+        const S Finf = fin(n, d.xn2n) ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
         const S Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
-        const S F0l = ref_eval(F, d, CH, SP, m, nu, n) - u0;
+        const S F0l = F.has0 ? f0_eval(F, d, CH, SP, m, nu, n, P) - f0_eval(F, d, CH, SP, m, FINF, n, P) - c0
+                             : ref_eval(F, d, CH, SP, m, nu, n) - u0;
         const size_t ip = ixPi(d, P, m, n);
         acc = cfma(Fl, to_c<S>(ldg(Pi + ip)), acc);
         acc = acc - F0l * to_c<S>(ldg(Pi0 + ip));
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-        const S v = cfma(c, to_c<S>(SPi[(size_t)P * d.NPO + (m + d.nPO - 1)]), acc);
+        const size_t is = (size_t)P * d.NPO + (m + d.nPO - 1);
+        S v = cfma(c, to_c<S>(SPi[is]), acc);
+        if (F.has0) v = v - c0 * to_c<S>(SPi0[is]);
         out[idx] = to_d(v * (R)(d.U * d.T * (CH == CH_T ? -1.0 : 1.0)));
     }
 }
-template <class S>
-__global__ void k_bse_K1_new_all(VertPT<S> F, BubbleP B, const cplx* SPi, const cplx* SPi0, ChanWork cw, Dims d) {
+template <class S, bool V0>
+__global__ void k_bse_K1_new_all(VertPT<S> Fin, BubbleP B, const cplx* SPi, const cplx* SPi0, ChanWork cw, Dims d) {
+    const VertPT<S> F = vert_spec<V0>(Fin);
     const size_t nS = (size_t)d.Nq * d.NPO;
     switch (blockIdx.y) {
-        case CH_P: bse_K1_new_body<CH_P>(F, B.pp, SPi, SPi0, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
-        case CH_T: bse_K1_new_body<CH_T>(F, B.ph, SPi + nS, SPi0 + nS, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
-        default:   bse_K1_new_body<CH_A>(F, B.ph, SPi + nS, SPi0 + nS, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+        case CH_P: bse_K1_new_body<CH_P>(F, B.pp, B.pp0, SPi, SPi0, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
+        case CH_T: bse_K1_new_body<CH_T>(F, B.ph, B.ph0, SPi + nS, SPi0 + nS, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
+        default:   bse_K1_new_body<CH_A>(F, B.ph, B.ph0, SPi + nS, SPi0 + nS, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
-template <class S>
-__global__ void k_bse_K2_new_all(VertPT<S> F, BubbleP B, const cplx* SPi, ChanWork cw, Dims d) {
+template <class S, bool V0>
+__global__ void k_bse_K2_new_all(VertPT<S> Fin, BubbleP B, const cplx* SPi, const cplx* SPi0, ChanWork cw, Dims d) {
+    const VertPT<S> F = vert_spec<V0>(Fin);
     const size_t nS = (size_t)d.Nq * d.NPO;
     switch (blockIdx.y) {
-        case CH_P: bse_K2_new_body<CH_P>(F, B.pp, B.pp0, SPi, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
-        case CH_T: bse_K2_new_body<CH_T>(F, B.ph, B.ph0, SPi + nS, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
-        default:   bse_K2_new_body<CH_A>(F, B.ph, B.ph0, SPi + nS, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
+        case CH_P: bse_K2_new_body<CH_P>(F, B.pp, B.pp0, SPi, SPi0, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
+        case CH_T: bse_K2_new_body<CH_T>(F, B.ph, B.ph0, SPi + nS, SPi0 + nS, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
+        default:   bse_K2_new_body<CH_A>(F, B.ph, B.ph0, SPi + nS, SPi0 + nS, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
 
 // ---------------------------------------------------------------------------------------------
 // All-channel launches: blockIdx.y selects the channel (0 = p, 1 = t, 2 = a; SDE: 0 = pp, 1 = ph).
 // ---------------------------------------------------------------------------------------------
-template <class S, bool TAN>
-__global__ void k_bse_K1_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d,
-                             TanArgsT<S> T) {
+template <class S, bool TAN, bool V0>
+__global__ void k_bse_K1_all(VertPT<S> Fin, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw, Dims d,
+                             TanArgsT<S> Tin) {
+    const VertPT<S> F = vert_spec<V0>(Fin);
+    const TanArgsT<S> T = tan_spec<V0>(Tin);
     switch (blockIdx.y) {
         case CH_P: bse_K1_body<CH_P, S, TAN>(F, FL, B.pp, B.pp0, SX, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], cw.acc, d, T); break;
         case CH_T: bse_K1_body<CH_T, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], cw.acc, d, T); break;
         default:   bse_K1_body<CH_A, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], cw.acc, d, T); break;
     }
 }
-template <class S>
-__global__ void k_bse_L_K2_all(VertPT<S> F, BubbleP B, ChanWork cw, Dims d) {
+template <class S, bool V0>
+__global__ void k_bse_L_K2_all(VertPT<S> Fin, BubbleP B, ChanWork cw, Dims d) {
+    const VertPT<S> F = vert_spec<V0>(Fin);
     switch (blockIdx.y) {
         case CH_P: bse_L_K2_body<CH_P>(F, B.pp0, cw.out[CH_P], cw.items[CH_P], cw.nitems[CH_P], d); break;
         case CH_T: bse_L_K2_body<CH_T>(F, B.ph0, cw.out[CH_T], cw.items[CH_T], cw.nitems[CH_T], d); break;
         default:   bse_L_K2_body<CH_A>(F, B.ph0, cw.out[CH_A], cw.items[CH_A], cw.nitems[CH_A], d); break;
     }
 }
-template <class S, bool TAN>
-__global__ void __launch_bounds__(512) k_bse_K2_all(VertPT<S> F, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw,
-                                                    Dims d, TanArgsT<S> T) {
+template <class S, bool TAN, bool V0>
+__global__ void __launch_bounds__(512) k_bse_K2_all(VertPT<S> Fin, FLPT<S> FL, BubbleP B, const cplx* SX, ChanWork cw,
+                                                    Dims d, TanArgsT<S> Tin) {
+    const VertPT<S> F = vert_spec<V0>(Fin);
+    const TanArgsT<S> T = tan_spec<V0>(Tin);
     extern __shared__ __align__(16) unsigned char k2_smem[];
     S* tab = reinterpret_cast<S*>(k2_smem);
     switch (blockIdx.y) {
@@ -1191,9 +1316,11 @@ __global__ void __launch_bounds__(512) k_bse_K2_all(VertPT<S> F, FLPT<S> FL, Bub
         default:   bse_K2_row<CH_A, S, TAN>(F, FL, B.ph, B.ph0, SX, cw.out[CH_A], cw.items[CH_A], cw.gstart[CH_A], cw.ngroups[CH_A], cw.acc, d, T, tab); break;
     }
 }
-template <class S, bool TAN>
-__global__ void k_sde_L_all(VertPT<S> F, BubbleP B, const cplx* SPpp, const cplx* SPph, ChanWork cw, int use_vertex,
-                            double ref_scale, Dims d, TanArgsT<S> T) {
+template <class S, bool TAN, bool V0>
+__global__ void k_sde_L_all(VertPT<S> Fin, BubbleP B, const cplx* SPpp, const cplx* SPph, ChanWork cw, int use_vertex,
+                            double ref_scale, Dims d, TanArgsT<S> Tin) {
+    const VertPT<S> F = vert_spec<V0>(Fin);
+    const TanArgsT<S> T = tan_spec<V0>(Tin);
     if (blockIdx.y == 0)
         sde_L_body<0, S, TAN>(F, B.pp, SPpp, cw.out[0], cw.items[0], cw.nitems[0], use_vertex, ref_scale, cw.acc, d, T);
     else sde_L_body<1, S, TAN>(F, B.ph, SPph, cw.out[1], cw.items[1], cw.nitems[1], use_vertex, ref_scale, cw.acc, d, T);
@@ -1318,10 +1445,13 @@ __global__ void k_sigma_assemble(const cplx* Sin, const cplx* SU2, const uint32_
     if (map) { const uint32_t e = map[i]; r = e >> 2; op = (int)(e & 3u); }
     cplx v = apply_op(op, Sin[r] + SU2[r]);
     if (hartree) v += mk(0.0, (*occ - 0.5) * U);
-    if (fdpa) {
+    if (fdpa) {  // 1: the reference system's Hartree term subtracted twice (src/SDE.jl:9-24); 2: once
         v = v + (C0[i] * -1.0);
         v += Sig0[i];
-        if (hartree) v = v + mk(0.0, -(n0 - 0.5) * U) + mk(0.0, -(n0 - 0.5) * U);
+        if (hartree) {
+            v = v + mk(0.0, -(n0 - 0.5) * U);
+            if (fdpa == 1) v = v + mk(0.0, -(n0 - 0.5) * U);
+        }
     }
     Sig[i] = v;
 }
@@ -1583,10 +1713,10 @@ cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const 
     if (e != cudaSuccess) return e;
     return cudaSuccess;
 }
-cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
-                      const FLP& FL, cplx* SX, const Dims& d) {
+cudaError_t launch_sx(cudaStream_t s, const BubbleP& B, const cplx* SPi, const cplx* SPi0, const FLP& FL,
+                      const VertP& F0v, cplx* SX, const Dims& d) {
     const size_t n = (size_t)3 * d.Nq * d.NPO * 32;
-    k_sx<<<blocks_for(n, 128), 128, 0, s>>>(Pipp, Piph, SPi, SPi0, FL, SX, d);
+    k_sx<<<blocks_for(n, 128), 128, 0, s>>>(B.pp, B.ph, B.pp0, B.ph0, SPi, SPi0, FL, F0v, SX, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 
@@ -1600,7 +1730,8 @@ template <class S>
 static cudaError_t build_cache_t(cudaStream_t s, const VertPT<S>& F, const Caches& C, const int* blocks, int nblocks,
                                  const Dims& d) {
     const size_t n = (size_t)nblocks * d.N3n * d.N3n;
-    k_build_cache<S><<<blocks_for(n, 128), 128, 0, s>>>(F, C, blocks, nblocks, d);
+    if (F.has0) k_build_cache<S, true><<<blocks_for(n, 128), 128, 0, s>>>(F, C, blocks, nblocks, d);
+    else k_build_cache<S, false><<<blocks_for(n, 128), 128, 0, s>>>(F, C, blocks, nblocks, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_build_cache(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
@@ -1635,58 +1766,80 @@ static unsigned warp_grid(const ChanWork& cw, int nch) {
     for (int c = 0; c < nch; ++c) mx = std::max(mx, cw.nitems[c]);
     return blocks_for((size_t)mx * 32, 128);
 }
+// each vertex-evaluating kernel is launched in its V0 = F.has0 instantiation (see vert_spec)
+template <class K>
+static cudaError_t k2_launch_attr(K k_plain, K k_v0, bool v0, size_t smem) {
+    return k2_smem_attr(v0 ? k_v0 : k_plain, smem);
+}
 #define FDGA_VERTEX_LAUNCHERS(VT, FT, TT, ST)                                                                       \
     cudaError_t launch_bse_K1_all(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const ChanWork& cw, const Dims& d) {                                             \
-        k_bse_K1_all<ST, false><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, TT{});                        \
+        const dim3 g(warp_grid(cw, 3), 3);                                                                          \
+        if (F.has0) k_bse_K1_all<ST, false, true><<<g, 128, 0, s>>>(F, FL, B, SX, cw, d, TT{});                     \
+        else k_bse_K1_all<ST, false, false><<<g, 128, 0, s>>>(F, FL, B, SX, cw, d, TT{});                           \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_bse_L_K2_all(cudaStream_t s, const VT& F, const BubbleP& B, const ChanWork& cw,             \
                                     const Dims& d) {                                                                \
-        k_bse_L_K2_all<<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, cw, d);                                     \
+        const dim3 g(warp_grid(cw, 3), 3);                                                                          \
+        if (F.has0) k_bse_L_K2_all<ST, true><<<g, 128, 0, s>>>(F, B, cw, d);                                        \
+        else k_bse_L_K2_all<ST, false><<<g, 128, 0, s>>>(F, B, cw, d);                                              \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_bse_K2_all(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const ChanWork& cw, const Dims& d) {                                             \
         const size_t smem = k2_row_smem<ST, false>(d);                                                             \
-        cudaError_t e = k2_smem_attr(k_bse_K2_all<ST, false>, smem);                                                \
+        cudaError_t e = k2_launch_attr(k_bse_K2_all<ST, false, false>, k_bse_K2_all<ST, false, true>, F.has0, smem); \
         if (e != cudaSuccess) return e;                                                                             \
-        k_bse_K2_all<ST, false><<<dim3(row_grid(cw, 3), 3), row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, TT{}); \
+        const dim3 g(row_grid(cw, 3), 3);                                                                           \
+        if (F.has0) k_bse_K2_all<ST, false, true><<<g, row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, TT{});   \
+        else k_bse_K2_all<ST, false, false><<<g, row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, TT{});         \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_sde_L_all(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
                                  const ChanWork& cw, int use_vertex, double ref_scale, const Dims& d) {             \
-        k_sde_L_all<ST, false><<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d, TT{}); \
+        const dim3 g(warp_grid(cw, 2), 2);                                                                          \
+        if (F.has0) k_sde_L_all<ST, false, true><<<g, 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d, TT{}); \
+        else k_sde_L_all<ST, false, false><<<g, 128, 0, s>>>(F, B, SPpp, SPph, cw, use_vertex, ref_scale, d, TT{});  \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_bse_K1_tan(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const TT& T, const ChanWork& cw, const Dims& d) {                                \
-        k_bse_K1_all<ST, true><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, FL, B, SX, cw, d, T);                           \
+        const dim3 g(warp_grid(cw, 3), 3);                                                                          \
+        if (F.has0) k_bse_K1_all<ST, true, true><<<g, 128, 0, s>>>(F, FL, B, SX, cw, d, T);                         \
+        else k_bse_K1_all<ST, true, false><<<g, 128, 0, s>>>(F, FL, B, SX, cw, d, T);                               \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_bse_K2_tan(cudaStream_t s, const VT& F, const FT& FL, const BubbleP& B, const cplx* SX,    \
                                   const TT& T, const ChanWork& cw, const Dims& d) {                                \
         const size_t smem = k2_row_smem<ST, true>(d);                                                              \
-        cudaError_t e = k2_smem_attr(k_bse_K2_all<ST, true>, smem);                                                 \
+        cudaError_t e = k2_launch_attr(k_bse_K2_all<ST, true, false>, k_bse_K2_all<ST, true, true>, F.has0, smem);  \
         if (e != cudaSuccess) return e;                                                                             \
-        k_bse_K2_all<ST, true><<<dim3(row_grid(cw, 3), 3), row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, T);     \
+        const dim3 g(row_grid(cw, 3), 3);                                                                           \
+        if (F.has0) k_bse_K2_all<ST, true, true><<<g, row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, T);       \
+        else k_bse_K2_all<ST, true, false><<<g, row_threads(cw, 3), smem, s>>>(F, FL, B, SX, cw, d, T);             \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_sde_L_tan(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPpp, const cplx* SPph, \
                                  const TT& T, const ChanWork& cw, double ref_scale, const Dims& d) {                \
-        k_sde_L_all<ST, true><<<dim3(warp_grid(cw, 2), 2), 128, 0, s>>>(F, B, SPpp, SPph, cw, 1, ref_scale, d, T);           \
+        const dim3 g(warp_grid(cw, 2), 2);                                                                          \
+        if (F.has0) k_sde_L_all<ST, true, true><<<g, 128, 0, s>>>(F, B, SPpp, SPph, cw, 3, ref_scale, d, T);       \
+        else k_sde_L_all<ST, true, false><<<g, 128, 0, s>>>(F, B, SPpp, SPph, cw, 1, ref_scale, d, T);             \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }
 #define FDGA_NEW_LAUNCHERS(VT, ST)                                                                                 \
     cudaError_t launch_bse_K1_new(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,  \
                                   const ChanWork& cw, const Dims& d) {                                             \
-        k_bse_K1_new_all<ST><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, SPi, SPi0, cw, d);                    \
+        const dim3 g(warp_grid(cw, 3), 3);                                                                          \
+        if (F.has0) k_bse_K1_new_all<ST, true><<<g, 128, 0, s>>>(F, B, SPi, SPi0, cw, d);                           \
+        else k_bse_K1_new_all<ST, false><<<g, 128, 0, s>>>(F, B, SPi, SPi0, cw, d);                                 \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }                                                                                                               \
     cudaError_t launch_bse_K2_new(cudaStream_t s, const VT& F, const BubbleP& B, const cplx* SPi, const cplx* SPi0,  \
                                   const ChanWork& cw, const Dims& d) {                                             \
-        (void)SPi0;                                                                                                 \
-        k_bse_K2_new_all<ST><<<dim3(warp_grid(cw, 3), 3), 128, 0, s>>>(F, B, SPi, cw, d);                          \
+        const dim3 g(warp_grid(cw, 3), 3);                                                                          \
+        if (F.has0) k_bse_K2_new_all<ST, true><<<g, 128, 0, s>>>(F, B, SPi, SPi0, cw, d);                           \
+        else k_bse_K2_new_all<ST, false><<<g, 128, 0, s>>>(F, B, SPi, SPi0, cw, d);                                 \
         LAUNCH_CHECK(); return cudaSuccess;                                                                         \
     }
 FDGA_NEW_LAUNCHERS(VertP, cplx)
@@ -1792,9 +1945,10 @@ cudaError_t launch_dyson_tan(cudaStream_t s, cplx* tG, const cplx* G, const cplx
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_sx_tan(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* tPipp, const cplx* tPiph,
-                          const cplx* tSPi, const FLP& FL, const FLP& tFL, cplx* tSX, const Dims& d) {
+                          const cplx* tSPi, const FLP& FL, const FLP& tFL, const VertP& F0v, cplx* tSX,
+                          const Dims& d) {
     const size_t n = (size_t)3 * d.Nq * d.NPO * 32;
-    k_sx_tan<<<blocks_for(n, 128), 128, 0, s>>>(Pipp, Piph, tPipp, tPiph, tSPi, FL, tFL, tSX, d);
+    k_sx_tan<<<blocks_for(n, 128), 128, 0, s>>>(Pipp, Piph, tPipp, tPiph, tSPi, FL, tFL, F0v, tSX, d);
     LAUNCH_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_rowsum_tan(cudaStream_t s, const cplx* tA0, const cplx* tA1, const cplx* GR, const cplx* tGR,

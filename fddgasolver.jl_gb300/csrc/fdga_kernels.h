@@ -235,8 +235,9 @@ cudaError_t launch_rowsum(cudaStream_t s, const cplx* A0, const cplx* A1, const 
 cudaError_t launch_tail_const(cudaStream_t s, cplx* T0, const Dims& d);
 bool bubble_f32_supported(const Dims& d);
 cudaError_t launch_bubble_f32(cudaStream_t s, const cplxf* GRf, cplx* pp, cplx* ph, const cplx* twp, const Dims& d);
-cudaError_t launch_sx(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* SPi, const cplx* SPi0,
-                      const FLP& FL, cplx* SX, const Dims& d);
+// F0v: the FP64 vertex view whose reference vertex enters F0(Ω, ω̃, ∞) (only has0/g0/b0 are read)
+cudaError_t launch_sx(cudaStream_t s, const BubbleP& B, const cplx* SPi, const cplx* SPi0, const FLP& FL,
+                      const VertP& F0v, cplx* SX, const Dims& d);
 cudaError_t launch_dyson(cudaStream_t s, cplx* G, const cplx* Sig, const cplx* Gb, size_t n);
 cudaError_t launch_occupation(cudaStream_t s, const cplx* G, size_t n, double T, int Nk, double* out);
 cudaError_t launch_g_realspace(cudaStream_t s, const cplx* G, cplx* GR, const cplx* tw, const Dims& d);
@@ -341,7 +342,8 @@ cudaError_t launch_rowsum_tan(cudaStream_t s, const cplx* tA0, const cplx* tA1, 
                               cplx* SRtmp, const cplx* twp, cplx* tS0, cplx* tS1, const Dims& d,
                               const cplxf* GRf = nullptr, const cplxf* tGRf = nullptr);
 cudaError_t launch_sx_tan(cudaStream_t s, const cplx* Pipp, const cplx* Piph, const cplx* tPipp, const cplx* tPiph,
-                          const cplx* tSPi, const FLP& FL, const FLP& tFL, cplx* tSX, const Dims& d);
+                          const cplx* tSPi, const FLP& FL, const FLP& tFL, const VertP& F0v, cplx* tSX,
+                          const Dims& d);
 cudaError_t launch_sde_sigma_tan(cudaStream_t s, const cplx* GR, const cplx* LR, const cplx* tGR, const cplx* tLpp,
                                  const cplx* tLph, cplx* tLR, cplx* tSR, cplx* tS, const cplx* twm, const cplx* twp,
                                  const Dims& d);

@@ -15,6 +15,7 @@
 #include <string>
 #include <thread>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/fdga.h"
@@ -69,6 +70,14 @@ struct fdga_handle {
     cplxf* Freff[4] = {nullptr, nullptr, nullptr, nullptr};
     cplxf* GRf = nullptr;  // FP32 copy of G(R) (mixed map)
     cplx* T0tail = nullptr;  // tail·tail part of the R = 0 bubble row sums [2][NΠΩ]
+    // Vertex-valued reference vertex F0 (cfg.f0_vertex): its channels [p|t|a] x [K1|K2|K3] in the
+    // device layout of its own boxes b0, their momentum averages, and FP32 copies for the mixed map
+    bool has0 = false;
+    Box b0{};
+    size_t n0_1 = 0, n0_2 = 0, n0_3 = 0, n0chan = 0, n0avg = 0;
+    cplx *F0v = nullptr, *F0avg = nullptr;
+    cplxf *F0vf = nullptr, *F0avgf = nullptr;
+    int fdpa_single_hartree = 0;  // option: subtract the reference system's Hartree term once
     size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
@@ -193,6 +202,12 @@ int ensure_mixed(fdga_handle* h) {
     AL(h->ySf, 3 * h->nchan);
     if (h->navg) AL(h->avgf, h->navg);
     for (auto& f : h->Freff) AL(f, h->nRef);
+    if (h->has0) {
+        AL(h->F0vf, 3 * h->n0chan);
+        if (h->n0avg) AL(h->F0avgf, h->n0avg);
+        CK(launch_to_f32(h->st, h->F0v, h->F0vf, 3 * h->n0chan));
+        if (h->n0avg) CK(launch_to_f32(h->st, h->F0avg, h->F0avgf, h->n0avg));
+    }
     AL(h->d_err, 1);
     if (k3_tc_supported(h->d)) CK(prepare_bse_K3_tc(h->d));
     CK(cudaStreamSynchronize(h->st));
@@ -257,11 +272,26 @@ int make_dims(const fdga_config* c, Dims& d) {
     // Stored bubble window.  Every bubble frequency read by the nonlocal iteration satisfies
     // |ω| <= nK2Ω + nK2ν + nK1 (K2 windows around -(Ω+ν+1) and Ω-ν-1), <= nK2Ω + nRν (SDE RefVertex
     // window) or <= nK1 + nK2ν (S_X); the local solver's left K2 BSE sums the whole mesh.
-    d.nPw = c->local ? d.nPn : std::min(d.nPn, c->nK2[0] + c->nK2[1] + c->nK1 + c->nR[1] + 2);
+    // A Vertex-valued F0 widens every window to the union of its boxes and the solver's.
+    d.xn1 = d.n1; d.xn2O = d.n2O; d.xn2n = d.n2n; d.xn3n = d.n3n;
+    if (c->f0_vertex) {
+        d.xn1 = std::max(d.n1, c->nF0K1);
+        d.xn2O = std::max(d.n2O, c->nF0K2[0]);
+        d.xn2n = std::max(d.n2n, c->nF0K2[1]);
+        d.xn3n = std::max(d.n3n, c->nF0K3[1]);
+    }
+    d.nPw = c->local ? d.nPn : std::min(d.nPn, d.xn2O + d.xn2n + d.xn1 + c->nR[1] + 2);
     d.NPw = 2 * d.nPw;
     d.local = c->local ? 1 : 0;
     d.T = c->T; d.U = c->U;
     return FDGA_OK;
+}
+// The solver's dims with the channel boxes of a Vertex-valued F0 (for its index maps and averages).
+Dims f0_dims(const Dims& d, const Box& b) {
+    Dims e = d;
+    e.n1 = b.n1; e.N1 = b.N1; e.n2O = b.n2O; e.N2O = b.N2O; e.n2n = b.n2n; e.N2n = b.N2n;
+    e.n3O = b.n3O; e.N3O = b.N3O; e.n3n = b.n3n; e.N3n = b.N3n;
+    return e;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -450,6 +480,28 @@ VertPT<S> vertex_view_t(const fdga_handle* h, S* st, S* avg, S* const* fref) {
         }
     }
     F.Fp_p = fref[0]; F.Fp_x = fref[1]; F.Ft_p = fref[2]; F.Ft_x = fref[3];
+    if (h->has0) {  // the channels of a Vertex-valued F0 (FP64, or their FP32 copies in the mixed map)
+        S* f0 = nullptr;
+        S* a0 = nullptr;
+        if constexpr (std::is_same<S, cplx>::value) { f0 = h->F0v; a0 = h->F0avg; }
+        else { f0 = h->F0vf; a0 = h->F0avgf; }
+        const Box& b = h->b0;
+        for (int c = 0; c < 3; ++c) {
+            S* base = f0 + (size_t)c * h->n0chan;
+            F.g0[c].K1 = base;
+            F.g0[c].K2 = base + h->n0_1;
+            F.g0[c].K3 = base + h->n0_1 + h->n0_2;
+            if (h->d.Nq == 1) {
+                F.g0[c].A1 = F.g0[c].K1; F.g0[c].A2 = F.g0[c].K2; F.g0[c].A3 = F.g0[c].K3;
+            } else {
+                const size_t per1 = b.N1, per2 = (size_t)b.N2O * b.N2n, per3 = (size_t)b.N3O * b.N3n * b.N3n;
+                S* a = a0 + (size_t)c * (per1 + per2 + per3);
+                F.g0[c].A1 = a; F.g0[c].A2 = a + per1; F.g0[c].A3 = a + per1 + per2;
+            }
+        }
+        F.b0 = b;
+        F.has0 = 1;
+    }
     return F;
 }
 VertP vertex_view(fdga_handle* h, cplx* S) { return vertex_view_t<cplx>(h, S, h->avg, h->Fref); }
@@ -681,7 +733,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         CK(cudaStreamWaitEvent(sD, h->evD, 0));
     }
     // ω-sums of the right BSE factor (needs FL.K2 of this iteration)
-    if (!is_new) LC(launch_sx(sD, h->Pipp, h->Piph, h->SPi, h->SPi0, FLz, h->SX, d));
+    if (!is_new) LC(launch_sx(sD, B, h->SPi, h->SPi0, FLz, F, h->SX, d));
     {  // K1
         ChanWork cw = work(1, h->raw1);
         if (is_new && mixed) LC(launch_bse_K1_new(sD, Ff, B, h->SPi, h->SPi0, cw, d));
@@ -750,15 +802,15 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         const double rs = h->ref_nonzero ? 1.0 / 3.0 : 0.0;
         if (mixed) {
             LC(launch_to_f32(s, h->yS, h->ySf, 3 * h->nchan));
-            LC(sde_L_pair(h, Fnf, B, h->SPi, 1, rs, nl));
+            LC(sde_L_pair(h, Fnf, B, h->SPi, h->has0 ? 3 : 1, rs, nl));
         } else {
-            LC(sde_L_pair(h, Fn, B, h->SPi, 1, rs, nl));
+            LC(sde_L_pair(h, Fn, B, h->SPi, h->has0 ? 3 : 1, rs, nl));
         }
         LC(launch_sde_sigma(s, h->GR, h->Lpp, h->Lph, h->LR, h->SigR, h->SigIn, h->twm, h->twp, d));
         nl += 3;
         LC(launch_sigma_assemble(s, h->SigIn, h->SigU2, h->gSig.trivial ? nullptr : h->gSig.d_map, h->occ, h->C0,
-                                 h->Sig0, SigOut, d.U, hartree ? 1 : 0, strategy_fdpa_sde(strategy) ? 1 : 0, h->n0,
-                                 h->nGk));
+                                 h->Sig0, SigOut, d.U, hartree ? 1 : 0,
+                                 strategy_fdpa_sde(strategy) ? (h->fdpa_single_hartree ? 2 : 1) : 0, h->n0, h->nGk));
     } else {
         LC(cudaMemcpyAsync(SigOut, sigmaOf(h, h->xS), h->nGk * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
     }
@@ -993,7 +1045,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         CK(cudaEventRecord(h->evD, s));
         CK(cudaStreamWaitEvent(sD, h->evD, 0));
     }
-    LC(launch_sx_tan(sD, h->Pipp, h->Piph, t.Pipp, t.Piph, t.SPi, FL, tFL, t.SX, d));
+    LC(launch_sx_tan(sD, h->Pipp, h->Piph, t.Pipp, t.Piph, t.SPi, FL, tFL, F, t.SX, d));
     stage("sx");
     // tangent factors of the fused K1/K2/SDE kernels
     const TanArgs T64{tF, tFL, t.Pipp, t.Piph, t.SX, t.SPi, t.SPi + nS};
@@ -1361,9 +1413,11 @@ int compute_C0(fdga_handle* h) {
     cudaStream_t s = h->st;
     const Dims& d = h->d;
     int nl = 0;
-    VertP F0 = vertex_view(h, h->yS);  // only the RefVertex fields are read by the REF kernels
+    // only the reference-vertex fields are read: the RefVertex part (/3) and, for a Vertex F0, its
+    // channels (use_vertex bit 2: the Vertex level of the recursion SDE!(Σ, G0, …, F0, …), src/SDE.jl:35-48)
+    VertP F0 = vertex_view(h, h->yS);
     BubbleP B0{h->Pi0pp, h->Pi0ph, h->Pi0pp, h->Pi0ph};
-    LC(sde_L_pair(h, F0, B0, h->SPi0, 0, 1.0 / 3.0, nl));
+    LC(sde_L_pair(h, F0, B0, h->SPi0, h->has0 ? 2 : 0, 1.0 / 3.0, nl));
     LC(launch_g_realspace(s, h->G0, h->GR, h->twm, d));
     LC(launch_sde_sigma(s, h->GR, h->Lpp, h->Lph, h->LR, h->SigR, h->SigIn, h->twm, h->twp, d));
     LC(launch_u2(s, h->GR, h->u2C, h->u2R, h->SigU2, h->twp, d));
@@ -1482,6 +1536,52 @@ bool lookup(fdga_handle* h, const std::string& n, cplx*& p, int& kind, size_t& l
     return true;
 }
 
+
+// FDGA_IN_F0_VERTEX: flatten(F0) of a Vertex-valued reference vertex (reference column-major layout,
+// src/vertex.jl:152-165) permuted into the device layout of its boxes; then its momentum averages
+// (kSW) and, when the mixed map's buffers exist, its FP32 copies.  F0 is constant over the solve.
+int set_f0_vertex(fdga_handle* h, const double* re_im, size_t n) {
+    if (!h->has0) return fail(h, FDGA_ERR_ARG, "the handle's reference vertex is a RefVertex (f0_vertex = 0)");
+    if (n != 3 * h->n0chan)
+        return fail(h, FDGA_ERR_ARG, "F0 vertex size mismatch: got " + std::to_string(n) + ", expected " +
+                                         std::to_string(3 * h->n0chan));
+    for (size_t i = 0; i < 2 * n; ++i)
+        if (!std::isfinite(re_im[i])) return fail(h, FDGA_ERR_NONFINITE, "non-finite value in the F0 vertex");
+    const Dims d0 = f0_dims(h->d, h->b0);
+    const cplx* in = reinterpret_cast<const cplx*>(re_im);
+    std::vector<cplx> dev(n);
+    size_t j = 0;
+    for (int c = 0; c < 3; ++c) {  // γp, γt, γa
+        const size_t off = (size_t)c * h->n0chan;
+        for (size_t i = 0; i < h->n0_1; ++i) dev[off + dev_index(d0, AK_K1, i)] = in[j++];
+        for (size_t i = 0; i < h->n0_2; ++i) dev[off + h->n0_1 + dev_index(d0, AK_K2, i)] = in[j++];
+        for (size_t i = 0; i < h->n0_3; ++i) dev[off + h->n0_1 + h->n0_2 + dev_index(d0, AK_K3, i)] = in[j++];
+    }
+    cudaStream_t s = h->st;
+    CK(cudaMemcpyAsync(h->F0v, dev.data(), n * sizeof(cplx), cudaMemcpyHostToDevice, s));
+    if (h->d.Nq > 1) {
+        ChanArrays a;
+        ChanArraysW o;
+        const size_t per1 = h->b0.N1, per2 = (size_t)h->b0.N2O * h->b0.N2n;
+        const size_t per3 = (size_t)h->b0.N3O * h->b0.N3n * h->b0.N3n;
+        for (int c = 0; c < 3; ++c) {
+            cplx* base = h->F0v + (size_t)c * h->n0chan;
+            a.K1[c] = base; a.K2[c] = base + h->n0_1; a.K3[c] = base + h->n0_1 + h->n0_2;
+            cplx* av = h->F0avg + (size_t)c * (per1 + per2 + per3);
+            o.K1[c] = av; o.K2[c] = av + per1; o.K3[c] = av + per1 + per2;
+        }
+        CK(launch_qavg(s, a, o, d0));
+    }
+    if (h->F0vf) {
+        CK(launch_to_f32(s, h->F0v, h->F0vf, 3 * h->n0chan));
+        if (h->n0avg) CK(launch_to_f32(s, h->F0avg, h->F0avgf, h->n0avg));
+    }
+    CK(cudaStreamSynchronize(s));
+    h->c0_dirty = true;
+    drop_graphs(h);
+    return FDGA_OK;
+}
+
 }  // namespace
 
 // =============================================================================================
@@ -1510,6 +1610,15 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
         return FDGA_ERR_ARG;
     }
     if (c->nR[0] < 1 || c->nR[1] < 1) return bad("RefVertex box must be >= 1");
+    if (c->f0_vertex != 0 && c->f0_vertex != 1) return bad("f0_vertex must be 0 or 1");
+    if (c->f0_vertex) {
+        if (c->nF0K1 < 1 || c->nF0K2[0] < 1 || c->nF0K2[1] < 1 || c->nF0K3[0] < 1 || c->nF0K3[1] < 1)
+            return bad("the boxes of the Vertex F0 must be >= 1");
+        if (c->nF0K1 < c->nF0K2[0] || c->nF0K1 < c->nF0K2[1])
+            return bad("F0: No. bosonic frequencies in K1 must be larger than the K2 box (src/channel.jl:33-34)");
+        if (c->nF0K2[0] < c->nF0K3[0] || c->nF0K2[1] < c->nF0K3[1])
+            return bad("F0: Number of frequencies in K2 must be larger than in K3 (src/channel.jl:40)");
+    }
     fdga_handle* h = new fdga_handle();
     h->cfg = *c;
     h->precision = FDGA_FP64;  // the config's precision is applied once the buffers exist (below)
@@ -1523,6 +1632,18 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     h->nRef = (size_t)d.NRO * d.NRn * d.NRn;
     h->nchan = h->n1 + h->n2 + h->n3;
     h->nstate = 3 * h->nchan + h->nGk;
+    if (c->f0_vertex) {
+        Box& b = h->b0;
+        b.n1 = c->nF0K1; b.N1 = 2 * c->nF0K1 - 1;
+        b.n2O = c->nF0K2[0]; b.N2O = 2 * c->nF0K2[0] - 1; b.n2n = c->nF0K2[1]; b.N2n = 2 * c->nF0K2[1];
+        b.n3O = c->nF0K3[0]; b.N3O = 2 * c->nF0K3[0] - 1; b.n3n = c->nF0K3[1]; b.N3n = 2 * c->nF0K3[1];
+        h->has0 = true;
+        h->n0_1 = (size_t)b.N1 * d.Nq;
+        h->n0_2 = (size_t)b.N2O * b.N2n * d.Nq;
+        h->n0_3 = (size_t)b.N3O * b.N3n * b.N3n * d.Nq;
+        h->n0chan = h->n0_1 + h->n0_2 + h->n0_3;
+        if (d.Nq > 1) h->n0avg = 3 * ((size_t)b.N1 + (size_t)b.N2O * b.N2n + (size_t)b.N3O * b.N3n * b.N3n);
+    }
     if (h->nstate >= ((size_t)1 << 32) || h->n3 >= ((size_t)1 << 30)) {
         delete h;
         g_create_error = "problem too large for 32-bit index maps";
@@ -1552,6 +1673,10 @@ int fdga_create(const fdga_config* c, fdga_handle** out) {
     if (d.Nq > 1) {
         h->navg = 3 * ((size_t)d.N1 + (size_t)d.N2O * d.N2n + (size_t)d.N3O * d.N3n * d.N3n);
         ALC(h->avg, h->navg);
+    }
+    if (h->has0) {
+        ALC(h->F0v, 3 * h->n0chan);
+        if (h->n0avg) ALC(h->F0avg, h->n0avg);
     }
     ALC(h->cache, 10 * h->n3);
     ALC(h->FLK2, 3 * h->n2); ALC(h->FLK3, 3 * h->n3);
@@ -1620,6 +1745,7 @@ void fdga_destroy(fdga_handle* h) {
 
 int fdga_set_input(fdga_handle* h, int which, const double* re_im, size_t n) {
     if (!h || !re_im) return fail(h, FDGA_ERR_ARG, "null argument");
+    if (which == FDGA_IN_F0_VERTEX) return set_f0_vertex(h, re_im, n);
     cplx* dst = nullptr;
     size_t len = 0;
     switch (which) {
@@ -2500,6 +2626,8 @@ int fdga_rrule(fdga_handle* h, int strategy, int update_sigma, int compute_hartr
     if (n != h->nstate) return fail(h, FDGA_ERR_ARG, "state length mismatch");
     if (strategy != FDGA_FDPA && strategy != FDGA_SCPA)
         return fail(h, FDGA_ERR_UNSUPPORTED, "the adjoint map covers the fdPA and scPA strategies");
+    if (h->has0)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the adjoint map covers a RefVertex reference vertex only (use fdga_frule)");
     int r = ensure_adjoint(h);
     if (r) return r;
     const int prec0 = h->precision;
@@ -2801,6 +2929,11 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
     if (k == "newton_gmres_cycles") {
         if (value < 1 || value > 64) return fail(h, FDGA_ERR_ARG, "newton_gmres_cycles must be in [1, 64]");
         h->newton_cycles = value;
+        return FDGA_OK;
+    }
+    if (k == "fdpa_single_hartree") {
+        h->fdpa_single_hartree = value ? 1 : 0;
+        drop_graphs(h);
         return FDGA_OK;
     }
     return fail(h, FDGA_ERR_ARG, "unknown option " + k);

@@ -19,6 +19,8 @@ class fdga_config(ctypes.Structure):
         ("nG", ctypes.c_int32), ("nK1", ctypes.c_int32), ("nK2", ctypes.c_int32 * 2), ("nK3", ctypes.c_int32 * 2),
         ("L", ctypes.c_int32), ("LG", ctypes.c_int32), ("mPi_factor", ctypes.c_int32), ("local", ctypes.c_int32),
         ("T", ctypes.c_double), ("U", ctypes.c_double), ("nR", ctypes.c_int32 * 2), ("precision", ctypes.c_int32),
+        ("f0_vertex", ctypes.c_int32), ("nF0K1", ctypes.c_int32), ("nF0K2", ctypes.c_int32 * 2),
+        ("nF0K3", ctypes.c_int32 * 2),
     ]
 
 
@@ -91,7 +93,7 @@ EXPORTS = {
 
 FDGA_FDPA, FDGA_SCPA, FDGA_FDPA_NEW, FDGA_SCPA_NEW, FDGA_FDPA_1LOOP = 0, 1, 2, 3, 4
 FDGA_FP64, FDGA_MIXED = 0, 1
-IN_GBARE, IN_G0, IN_SIGMA0, IN_FP_P, IN_FP_X, IN_FT_P, IN_FT_X = range(7)
+IN_GBARE, IN_G0, IN_SIGMA0, IN_FP_P, IN_FP_X, IN_FT_P, IN_FT_X, IN_F0_VERTEX = range(8)
 
 _LIB = None
 

@@ -47,6 +47,36 @@ class RefVertex:
                 raise ValueError("all RefVertex corrections must share one shape")
 
 
+class Vertex:
+    """Vertex(F0, γp, γt, γa) (src/vertex.jl:7-35): a channel-decomposed vertex whose own reference
+    vertex F0 is a RefVertex.  As the reference vertex of a solver it makes the fdDΓA solve of
+    ParquetSolver(nK1, nK2, nK3, Gbare, S0.G, S0.Σ, S0.F) (test/test_siam_fdPA.jl:79-84).
+
+    flat = flatten(F) = [γp(K1,K2,K3), γt, γa] in the reference's column-major layout of its boxes
+    nK1, nK2, nK3 (src/vertex.jl:152-165); L is the momentum mesh (1 for a local vertex)."""
+
+    def __init__(self, F0, nK1, nK2, nK3, flat, L=1):
+        if not isinstance(F0, RefVertex):
+            raise TypeError("the reference vertex of a Vertex is a RefVertex")
+        self.F0 = F0
+        self.T, self.U = F0.T, F0.U
+        self.nK1, self.nK2, self.nK3, self.L = int(nK1), tuple(nK2), tuple(nK3), int(L)
+        self.flat = np.ascontiguousarray(np.asarray(flat, dtype=np.complex128).reshape(-1))
+        Nq = self.L * self.L
+        n = 3 * Nq * ((2 * self.nK1 - 1) + (2 * self.nK2[0] - 1) * 2 * self.nK2[1] +
+                      (2 * self.nK3[0] - 1) * (2 * self.nK3[1]) ** 2)
+        if self.flat.size != n:
+            raise ValueError(f"flatten(F) has {self.flat.size} values, the boxes need {n}")
+
+    @property
+    def nR(self):
+        return self.F0.nR
+
+    @property
+    def arrays(self):
+        return self.F0.arrays
+
+
 def _as_f(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.complex128).reshape(-1, order="F"))
 
@@ -55,8 +85,10 @@ class _Solver:
     local = True
 
     def __init__(self, nK1, nK2, nK3, L, Gbare, G0, Sigma0, F0, *, mPi_factor, precision=0):
-        if not isinstance(F0, RefVertex):
-            raise NotImplementedError("this build takes a RefVertex reference vertex")
+        if not isinstance(F0, (RefVertex, Vertex)):
+            raise TypeError("the reference vertex F0 is a RefVertex or a Vertex")
+        if isinstance(F0, Vertex) and F0.L != int(L):
+            raise ValueError("a Vertex reference vertex has the solver's momentum mesh")
         lib = _lib.load()
         Gbare = np.asarray(Gbare, dtype=np.complex128)
         nG = Gbare.shape[0] // 2
@@ -70,6 +102,11 @@ class _Solver:
         c.T, c.U = F0.T, F0.U
         c.nR[0], c.nR[1] = F0.nR
         c.precision = int(precision)
+        if isinstance(F0, Vertex):
+            c.f0_vertex = 1
+            c.nF0K1 = F0.nK1
+            c.nF0K2[0], c.nF0K2[1] = F0.nK2
+            c.nF0K3[0], c.nF0K3[1] = F0.nK3
         h = ctypes.c_void_p()
         _lib.check(lib.fdga_create(ctypes.byref(c), ctypes.byref(h)))
         self._h = h
@@ -82,6 +119,8 @@ class _Solver:
         self._set(_lib.IN_SIGMA0, Sigma0)
         for k, a in enumerate(F0.arrays):
             self._set(_lib.IN_FP_P + k, a)
+        if isinstance(F0, Vertex):
+            self._check(lib.fdga_set_input(h, _lib.IN_F0_VERTEX, F0.flat.ctypes.data, F0.flat.size))
         self._check(lib.fdga_finalize(h))
         n = ctypes.c_size_t()
         self._check(lib.fdga_state_len(h, ctypes.byref(n)))
@@ -109,6 +148,15 @@ class _Solver:
     # -- reference API --
     def init_sym_grp(self):
         self._check(self._lib.fdga_init_sym_grp(self._h))
+
+    @property
+    def F(self):
+        """S.F: the current vertex as a host Vertex (its reference vertex is this solver's RefVertex),
+        to become the reference vertex F0 of another solver."""
+        if isinstance(self.F0, Vertex):
+            raise NotImplementedError("S.F of a solver whose own F0 is a Vertex (a reference chain of depth > 2)")
+        nS = 2 * self.nG * self.L * self.L
+        return Vertex(self.F0, self.nK1, self.nK2, self.nK3, self.flatten()[:-nS], L=self.L)
 
     def flatten(self):
         x = np.empty(self.state_len, dtype=np.complex128)

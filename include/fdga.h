@@ -43,9 +43,14 @@ enum { FDGA_FDPA = 0, FDGA_SCPA = 1, FDGA_FDPA_NEW = 2, FDGA_SCPA_NEW = 3, FDGA_
 enum { FDGA_FP64 = 0, FDGA_MIXED = 1 };
 
 /* Solver dimensions: the reference constructor arguments
- * ParquetSolver(nK1, nK2, nK3, Gbare, G0, Σ0, F0; mΠν_factor)         (src/ParquetSolver.jl:277-352)
+ * ParquetSolver(nK1, nK2, nK3, Gbare, G0, Σ0, F0; mΠν_factor)         (src/ParquetSolver.jl:88-157)
  * NL_ParquetSolver(nK1, nK2, nK3, mK_Γ, Gbare, G0, Σ0, F0; mΠν_factor) (src/nonlocal/ParquetSolver.jl:77-152)
- * with the RefVertex reference vertex F0 = RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x)  (src/refvertex.jl:1-35). */
+ * with the reference vertex F0 either the RefVertex F0 = RefVertex(U, Fp_p, Fp_x, Ft_p, Ft_x)
+ * (src/refvertex.jl:1-35), or (f0_vertex = 1) a Vertex F0 = RefVertex + γp + γt + γa with its own
+ * boxes nF0K1, nF0K2, nF0K3 (ParquetSolver{Q, VT, RefVT} with RefVT a Vertex: fdDΓA from a solved
+ * vertex, e.g. ParquetSolver(nK1, nK2, nK3, Gbare, S0.G, S0.Σ, S0.F), test/test_siam_fdPA.jl:79-84).
+ * The Vertex F0's own reference vertex is the RefVertex of U and nR above; its channels are uploaded
+ * with FDGA_IN_F0_VERTEX.  A nonlocal solver's Vertex F0 has the solver's momentum mesh. */
 typedef struct fdga_config {
     int32_t nG;          /* Green-function mesh: 2nG fermionic frequencies */
     int32_t nK1;         /* K1 box: 2nK1-1 bosonic frequencies */
@@ -59,6 +64,10 @@ typedef struct fdga_config {
     double U;            /* bare interaction of the RefVertex */
     int32_t nR[2];       /* box of the RefVertex corrections Fp_p .. Ft_x; (1,1) = bare U */
     int32_t precision;   /* FDGA_FP64 or FDGA_MIXED: initial arithmetic of fdga_iterate / fdga_residual */
+    int32_t f0_vertex;   /* 0: F0 is the RefVertex; 1: F0 is a Vertex with the boxes below */
+    int32_t nF0K1;       /* K1 box of the Vertex F0 */
+    int32_t nF0K2[2];    /* K2 box of the Vertex F0 (bosonic, fermionic) */
+    int32_t nF0K3[2];    /* K3 box of the Vertex F0 (bosonic, fermionic) */
 } fdga_config;
 
 /* Inputs uploaded with fdga_set_input (reference column-major layout). */
@@ -69,7 +78,9 @@ enum {
     FDGA_IN_FP_P = 3,    /* [2nR0-1, 2nR1, 2nR1] RefVertex corrections                    */
     FDGA_IN_FP_X = 4,
     FDGA_IN_FT_P = 5,
-    FDGA_IN_FT_X = 6
+    FDGA_IN_FT_X = 6,
+    FDGA_IN_F0_VERTEX = 7 /* flatten(F0) = [γp(K1,K2,K3), γt, γa] of a Vertex F0 in its own boxes
+                           * (flatten of a Vertex, src/vertex.jl:152-165)                      */
 };
 
 /* Creates a handle (replaces the reference constructors above; allocates all device state). */
