@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 namespace fdga {
 
@@ -924,12 +925,19 @@ template <class C> __device__ __forceinline__ C ldk(const cplxf* p) {
 // ARGS = K3Args3 (FP64 operands) or K3Args3F (FP32 operands).  C = cplx: FP64 arithmetic (the plain
 // path).  C = cplxf: FP32 products and accumulation, FP64 epilogue (the mixed path; FP64 operands
 // are converted when they are staged into shared memory).
+// FP64 arithmetic (the plain path, bound by GB300's FP64 pipe) forms each complex product with three
+// real multiplications (Gauss): t1 = Σ ar br, t2 = Σ ai bi, t3 = Σ (ar + ai)(br + bi), then
+// C = (t1 - t2) + i (t3 - t1 - t2).  The sums ar + ai and br + bi are formed once, when an element
+// is staged, so the inner loop issues 3 FMAs per complex multiply-add instead of 4.
 template <int MODE, int TILE, int TCOL, class C, class ARGS>
 __global__ void __launch_bounds__((TILE / 2) * (TCOL / 2)) k_bse_K3_gemm(ARGS args, Dims d) {
     using R = decltype(C::x);
     constexpr int TK = 8, H = TILE / 2, HC = TCOL / 2, NT = H * HC;
+    constexpr bool G3 = std::is_same<C, cplx>::value;  // three-multiplication form in FP64
     __shared__ C As[TILE][TK + 1];
     __shared__ C Ms[TK][TCOL + 1];
+    __shared__ R Asum[G3 ? TILE : 1][TK + 1];  // ar + ai of the staged A (FP64 form)
+    __shared__ R Msum[G3 ? TK : 1][TCOL + 1];  // br + bi of the staged M
     // the ω-only factors of M, signs folded in, for the current and the next K chunk:
     // [0] s1(Π-Π0) (mode 0: Π0)  [1] s1 Π  [2] s2 Π  [3] s1 dΠ  [4] s2 dΠ
     __shared__ C Pk[2][TK][5];
@@ -978,7 +986,8 @@ __global__ void __launch_bounds__((TILE / 2) * (TCOL / 2)) k_bse_K3_gemm(ARGS ar
         }
         return ldk<C>(FLc + i);
     };
-    C acc[2][2] = {{czero<C>(), czero<C>()}, {czero<C>(), czero<C>()}};
+    C acc[2][2] = {{czero<C>(), czero<C>()}, {czero<C>(), czero<C>()}};  // G3: (t1, t2)
+    R acc3[2][2] = {{(R)0, (R)0}, {(R)0, (R)0}};                           // G3: t3
     fill_pk(0, 0);
     __syncthreads();
     int cur = 0;
@@ -991,7 +1000,9 @@ __global__ void __launch_bounds__((TILE / 2) * (TCOL / 2)) k_bse_K3_gemm(ARGS ar
             for (int e = tid; e < TILE * TK; e += NT) {
                 const int r = e / TK, kk = e % TK;
                 const int row = row0 + r, k = k0 + kk;
-                As[r][kk] = (row < N && k < N) ? ldk<C>(Ap + base + (size_t)row * N + k) : czero<C>();
+                const C v = (row < N && k < N) ? ldk<C>(Ap + base + (size_t)row * N + k) : czero<C>();
+                As[r][kk] = v;
+                if constexpr (G3) Asum[r][kk] = v.x + v.y;
             }
             for (int e = tid; e < TK * TCOL; e += NT) {
                 const int kk = e / TCOL, c = e % TCOL;
@@ -1021,6 +1032,7 @@ __global__ void __launch_bounds__((TILE / 2) * (TCOL / 2)) k_bse_K3_gemm(ARGS ar
                     }
                 }
                 Ms[kk][c] = v;
+                if constexpr (G3) Msum[kk][c] = v.x + v.y;
             }
             // the next chunk's factors (the next K chunk, or the first chunk of the next half)
             const int nk0 = (k0 + TK < N) ? k0 + TK : 0;
@@ -1030,10 +1042,23 @@ __global__ void __launch_bounds__((TILE / 2) * (TCOL / 2)) k_bse_K3_gemm(ARGS ar
             for (int kk = 0; kk < TK; ++kk) {
                 const C a0 = As[ty][kk], a1 = As[ty + H][kk];
                 const C b0 = Ms[kk][tx], b1 = Ms[kk][tx + HC];
-                acc[0][0] = cfma(a0, b0, acc[0][0]);
-                acc[0][1] = cfma(a0, b1, acc[0][1]);
-                acc[1][0] = cfma(a1, b0, acc[1][0]);
-                acc[1][1] = cfma(a1, b1, acc[1][1]);
+                if constexpr (G3) {
+                    const R sa[2] = {Asum[ty][kk], Asum[ty + H][kk]}, sb[2] = {Msum[kk][tx], Msum[kk][tx + HC]};
+                    const C aa[2] = {a0, a1}, bb[2] = {b0, b1};
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            acc[i][j].x = fma(aa[i].x, bb[j].x, acc[i][j].x);
+                            acc[i][j].y = fma(aa[i].y, bb[j].y, acc[i][j].y);
+                            acc3[i][j] = fma(sa[i], sb[j], acc3[i][j]);
+                        }
+                } else {
+                    acc[0][0] = cfma(a0, b0, acc[0][0]);
+                    acc[0][1] = cfma(a0, b1, acc[0][1]);
+                    acc[1][0] = cfma(a1, b0, acc[1][0]);
+                    acc[1][1] = cfma(a1, b1, acc[1][1]);
+                }
             }
             __syncthreads();
             cur ^= 1;
@@ -1048,7 +1073,8 @@ __global__ void __launch_bounds__((TILE / 2) * (TCOL / 2)) k_bse_K3_gemm(ARGS ar
             if (row >= N || col >= N) continue;
             const size_t io = base + (size_t)row * N + col;
             // epilogue in the arithmetic type C (FP64 ops cost 64 FP32 ops on this part)
-            const C c = acc[i][j];
+            C c = acc[i][j];
+            if constexpr (G3) c = C{acc[i][j].x - acc[i][j].y, acc3[i][j] - (acc[i][j].x + acc[i][j].y)};
             cplx v;
             if (MODE == 0) {
                 v = to_d(c * (R)(d.T * ((CH == CH_A) ? 1.0 : -1.0)));
