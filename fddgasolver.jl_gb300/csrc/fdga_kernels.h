@@ -254,6 +254,17 @@ cudaError_t launch_bse_K3(cudaStream_t s, int mode, const K3Args3& a, int nslots
 bool k3_tile_valid(int tile);
 cudaError_t launch_bse_K3_f32(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int tile);
 cudaError_t launch_to_f32(cudaStream_t s, const cplx* in, cplxf* out, size_t n);
+// TMA-fed, warp-specialised tcgen05 form (fdga_k3_tma.cu): the FP32 operand arrays live in up to four
+// buffers (the caches, FL.K3, the tangent caches, the tangent FL.K3; base == nullptr: absent) over
+// which the TMA tensor maps are built; every K3ArgsF operand pointer must lie in one of them
+struct TmaBuffers {
+    const void* base[4];
+    size_t ncplx[4];
+};
+bool k3_tma_supported(const Dims& d, int mode);
+cudaError_t prepare_bse_K3_tma(const Dims& d);
+cudaError_t launch_bse_K3_tma(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int* err,
+                              const TmaBuffers& bufs);
 // tcgen05 form of the mixed K3 contractions (2Nν3 ≤ 256 MMA columns); *err set on a wait timeout
 bool k3_tc_supported(const Dims& d);
 cudaError_t prepare_bse_K3_tc(const Dims& d);

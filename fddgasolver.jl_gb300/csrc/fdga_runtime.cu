@@ -81,6 +81,7 @@ struct fdga_handle {
     size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
+    int k3_tma = 1;                              // ... in the TMA-fed warp-specialised kernel when it fits
     int jvp_tangent = 1;                         // GMRES Jacobian products by the tangent kernels (else differences)
     int newton_cycles = 1;                       // GMRES restart cycles per Newton step
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
@@ -210,6 +211,7 @@ int ensure_mixed(fdga_handle* h) {
     }
     AL(h->d_err, 1);
     if (k3_tc_supported(h->d)) CK(prepare_bse_K3_tc(h->d));
+    CK(prepare_bse_K3_tma(h->d));
     CK(cudaStreamSynchronize(h->st));
     return FDGA_OK;
 }
@@ -545,6 +547,23 @@ cudaError_t sde_L_pair(fdga_handle* h, const V& F, const BubbleP& B, const cplx*
     return e;
 }
 
+// The mixed map's K3 contraction on the tensor cores: the TMA-fed kernel when it fits the mode and
+// the box, else the staging kernel of fdga_k3_tc.cu.  False: neither applies (FP32 CUDA-core GEMM).
+bool k3_tensor_cores(const fdga_handle* h, int mode) {
+    return h->k3_tc && ((h->k3_tma && k3_tma_supported(h->d, mode)) || k3_tc_supported(h->d));
+}
+cudaError_t launch_k3_tensor_cores(fdga_handle* h, cudaStream_t s, int mode, const K3Args3F& a3f) {
+    if (h->k3_tma && k3_tma_supported(h->d, mode)) {
+        TmaBuffers b{};
+        b.base[0] = h->cachef; b.ncplx[0] = 10 * h->n3;
+        b.base[1] = h->FLK3f; b.ncplx[1] = 3 * h->n3;
+        b.base[2] = h->tan.cachef; b.ncplx[2] = h->tan.cachef ? 7 * h->n3 : 0;
+        b.base[3] = h->tan.FLK3f; b.ncplx[3] = h->tan.FLK3f ? 3 * h->n3 : 0;
+        return launch_bse_K3_tma(s, mode, a3f, 3, h->d, h->d_err, b);
+    }
+    return launch_bse_K3_tc(s, mode, a3f, 3, h->d, h->d_err);
+}
+
 using StageHook = std::function<void(const char*)>;
 // enqueued on the main stream of a captured iteration: right after branch B (which needs only Σ)
 // has forked, and right after the new vertex is complete (before the SDE)
@@ -700,7 +719,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             }
             a3.blocks = a3f.blocks = h->d_k3blocks;
             a3.nblocks = a3f.nblocks = h->nk3blocks;
-            if (mixed && h->k3_tc && k3_tc_supported(d)) LC(launch_bse_K3_tc(s, 0, a3f, 3, d, h->d_err));
+            if (mixed && k3_tensor_cores(h, 0)) LC(launch_k3_tensor_cores(h, s, 0, a3f));
             else if (mixed) LC(launch_bse_K3_f32(s, 0, a3f, 3, d, h->k3_tile[FDGA_MIXED][0]));
             else LC(launch_bse_K3(s, 0, a3, 3, d, 0, h->k3_tile[FDGA_FP64][0]));
             stage("bse_L_K3_gemm");
@@ -782,7 +801,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         }
         a3.blocks = a3f.blocks = h->d_k3blocks;
         a3.nblocks = a3f.nblocks = h->nk3blocks;
-        if (mixed && h->k3_tc && k3_tc_supported(d)) LC(launch_bse_K3_tc(s, 1, a3f, 3, d, h->d_err));
+        if (mixed && k3_tensor_cores(h, 1)) LC(launch_k3_tensor_cores(h, s, 1, a3f));
         else if (mixed) LC(launch_bse_K3_f32(s, 1, a3f, 3, d, h->k3_tile[FDGA_MIXED][1]));
         else LC(launch_bse_K3(s, 1, a3, 3, d, 0, h->k3_tile[FDGA_FP64][1]));
         stage("bse_K3_gemm");
@@ -980,7 +999,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
     // for the K3 contraction (mode 1), whose operands it shares
     auto k3 = [&](int mode, const K3Args3& a3, const K3Args3F& a3f) -> cudaError_t {
         const int tm = mode == 0 ? 0 : 1;
-        if (mixed && h->k3_tc && k3_tc_supported(d)) return launch_bse_K3_tc(s, mode, a3f, 3, d, h->d_err);
+        if (mixed && k3_tensor_cores(h, mode)) return launch_k3_tensor_cores(h, s, mode, a3f);
         if (mixed) return launch_bse_K3_f32(s, mode, a3f, 3, d, h->k3_tile[FDGA_MIXED][tm]);
         return launch_bse_K3(s, mode, a3, 3, d, 0, h->k3_tile[FDGA_FP64][tm]);
     };
@@ -2915,6 +2934,11 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
     const std::string k(key);
     if (k == "k3_tensor_cores") {
         h->k3_tc = value ? 1 : 0;
+        drop_graphs(h);
+        return FDGA_OK;
+    }
+    if (k == "k3_tma") {
+        h->k3_tma = value ? 1 : 0;
         drop_graphs(h);
         return FDGA_OK;
     }
