@@ -7,18 +7,21 @@
 // product in 2x2 real form (k = 2ω + q, n = 2ν' + p) and TF32 hi/lo operands accumulated as
 // hi·hi + hi·lo + lo·hi in FP32 tensor memory.
 //
-// Structure: a persistent CTA (one per SM) loops over the (channel, block) work items, 14 warps:
+// Structure: a persistent CTA (one per SM) loops over the (channel, block) work items; warp roles:
 //   warp 0        producer: per chunk of CW = 8 ω, 2-8 TMA tile loads (A columns, the rows of cacheF0,
 //                 the Γ cache in rows (p) or columns (a, t), FL rows and the tangent operands) and 1D
-//                 bulk copies of the chunk's Π, Π0, dΠ into one of two input stages, signalled on the
+//                 bulk copies of the chunk's Π, Π0, dΠ into one of 2-8 input stages, signalled on the
 //                 stage's mbarrier by the transaction count;
-//   warps 2..9    formers: split A into TF32 hi/lo and form M (and dM) from the staged tiles into one of
-//                 two operand buffers in the no-swizzle K-major canonical layout;
+//   last warp     converter: the chunk's Π, Π0, dΠ to FP32 once per stage use (the conversion runs on
+//                 GB300's FP64 pipe, so it is not repeated per operand element);
+//   formers       (8 or 16 warps from warp 2) split A into TF32 hi/lo and form M (and dM) from the
+//                 staged tiles into one of two operand buffers in the no-swizzle K-major canonical layout;
 //   warp 1        allocates the tensor memory and issues the MMAs (one thread), 6 per chunk, then
 //                 tcgen05.commit frees the operand buffer; the last commit of an item hands its
 //                 accumulator (one of two TMEM buffers of 256 columns) to the epilogue;
-//   warps 10..13  epilogue: tcgen05.ld of the accumulator (one 32-lane quadrant each), T·D plus the
-//                 γL(ν,ν') term, FP64 stores, then the TMEM buffer is released.
+//   epilogue      (8 or 12 warps, two or three per 32-lane TMEM quadrant) tcgen05.ld of the accumulator,
+//                 transposed through shared memory, T·D plus the γL(ν,ν') term, widened to FP64 by bit
+//                 operations (exact) and stored as contiguous row segments; then the TMEM buffer is freed.
 // The loads of the next chunks, the forming, the MMAs and the previous item's epilogue overlap.
 // Every mbarrier wait is bounded: a timeout sets *err and the shared abort flag, every role leaves its
 // loop, outstanding TMA loads and MMAs are waited for (bounded), and the tensor memory is released.
@@ -37,14 +40,28 @@ namespace {
 
 constexpr int KC = 16;          // real K per chunk (CW complex ω)
 constexpr int CW = KC / 2;      // ω per chunk
-constexpr int NS_IN = 2;        // input stages (TMA destinations)
+constexpr int MAX_IN = 8;       // input stages (TMA destinations): as many as the shared memory holds, 2..8
 constexpr int NS_OP = 2;        // operand buffers (MMA sources)
-constexpr int THREADS = 448;    // 14 warps
-constexpr int W_PROD = 0, W_MMA = 1, W_FORM0 = 2, N_FORM = 8, W_EPI0 = 10;
-constexpr int FORMERS = 32 * N_FORM;
+constexpr int W_PROD = 0, W_MMA = 1, W_FORM0 = 2;
+// role split per mode (measured): the left contraction (mode 0, no γL epilogue term) is bound by the
+// forming and takes 16 former and 8 epilogue warps; the others, whose epilogue reads γL, 8 and 12
+template <int MODE>
+struct Roles {
+    static constexpr int N_FORM = MODE == 0 ? 16 : 8;
+    static constexpr int N_EPI = MODE == 0 ? 8 : 12;
+    static constexpr int W_EPI0 = W_FORM0 + N_FORM;
+    static constexpr int W_CONV = W_EPI0 + N_EPI;
+    static constexpr int THREADS = 32 * (W_CONV + 1);
+    static constexpr int EPI_PER_Q = N_EPI / 4;  // epilogue warps per TMEM lane quadrant
+    static constexpr int FORMERS = 32 * N_FORM;
+};
+constexpr int MAX_EPI = 12;
+constexpr int TP = 18;                      // row pitch (floats) of an epilogue warp's transpose tile
+
 constexpr int A_OP = 128 * KC * 4;           // one A operand (hi or lo) of a chunk: 8 KB
 constexpr uint32_t SPIN_LIMIT = 1u << 22;    // bounded mbarrier polling
 constexpr size_t MIN_SMEM = 116 * 1024;      // one CTA per SM: it owns all 512 TMEM columns
+constexpr size_t SMEM_BUDGET = 192 * 1024;   // dynamic shared memory for the stages and operand buffers
 
 // input tile slots of a stage (each 64·N bytes: an N x KC column box or a CW x 2N row box)
 enum { T_A = 0, T_B0 = 1, T_G = 2, T_TG = 3, T_FL0 = 4, T_FL1 = 5, T_TFL0 = 6, T_TFL1 = 7 };
@@ -127,6 +144,18 @@ __device__ __forceinline__ cplxf ld2(const uint8_t* p) {
     const float2 v = *reinterpret_cast<const float2*>(p);
     return cplxf{v.x, v.y};
 }
+// FP32 -> FP64 by bit operations (exact; FP32 subnormals become signed zeros): the conversion
+// instruction runs on GB300's FP64 pipe at 1/64 of the FP32 rate, integer operations do not
+__device__ __forceinline__ double f2d_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint64_t sgn = (uint64_t)(u & 0x80000000u) << 32;
+    const uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    uint64_t r = sgn;
+    if (e == 255u) r |= (0x7FFull << 52) | ((uint64_t)m << 29);
+    else if (e != 0u) r |= ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+    return __longlong_as_double((long long)r);
+}
+__device__ __forceinline__ cplx c2d_bits(cplxf v) { return cplx{f2d_bits(v.x), f2d_bits(v.y)}; }
 // γL at a K3 index in the channel's spin combination (t: 2 FL.γt - FL.γa), FP32 copies
 __device__ __forceinline__ cplxf fl_box(const cplxf* FLc, const cplxf* FLt, const cplxf* FLa, int ch, size_t i) {
     if (ch == CH_T) {
@@ -167,27 +196,35 @@ struct TmaParams {
     const int* blocks;
     int nblocks;
     int nslots;
+    int nsin;  // input stages
 };
 
 namespace {
 
 __host__ __device__ inline int stage_tiles(int mode) { return mode == 0 ? 2 : (mode == 1 ? 6 : 8); }
-// a stage: the tiles, then the chunk's Π, Π0, dΠ (CW FP64 complex each, 128 B apart; 512 B reserved)
-__host__ __device__ inline size_t stage_bytes(int mode, int N) { return (size_t)stage_tiles(mode) * 64 * N + 512; }
+// a stage: the tiles, then the chunk's Π, Π0, dΠ (CW FP64 complex each, 128 B apart), then their FP32
+// forms written by the converter warp (3 CW FP32 complex); 640 B reserved
+constexpr int PI_F32 = 3 * CW * 16;  // offset of the FP32 forms in the Π area
+__host__ __device__ inline size_t stage_bytes(int mode, int N) { return (size_t)stage_tiles(mode) * 64 * N + 640; }
 __host__ __device__ inline size_t opbuf_bytes(int N) { return 2 * (size_t)A_OP + 2 * (size_t)(2 * N) * KC * 4; }
 
 template <int MODE>
-__global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant__ TmaParams p, Dims d, int* err) {
+__global__ void __launch_bounds__(Roles<MODE>::THREADS, 1) k_bse_K3_tma(const __grid_constant__ TmaParams p, Dims d, int* err) {
+    constexpr int N_FORM = Roles<MODE>::N_FORM, N_EPI = Roles<MODE>::N_EPI, W_EPI0 = Roles<MODE>::W_EPI0;
+    constexpr int W_CONV = Roles<MODE>::W_CONV, EPI_PER_Q = Roles<MODE>::EPI_PER_Q, FORMERS = Roles<MODE>::FORMERS;
     extern __shared__ __align__(1024) uint8_t sm[];
-    __shared__ __align__(8) uint64_t full[NS_IN], empty[NS_IN], opready[NS_OP], opfree[NS_OP], tfull[2], tfree[2], finbar;
+    __shared__ __align__(8) uint64_t full[MAX_IN], empty[MAX_IN], ready[MAX_IN], opready[NS_OP], opfree[NS_OP], tfull[2],
+        tfree[2], finbar;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
+    __shared__ __align__(16) float epi_tile[MAX_EPI * 32 * TP];  // the epilogue warps' transpose tiles
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = d.N3n, NN = 2 * N;
     const int nchunks = N / CW;
     const int nck = (MODE == 2 ? 2 : 1) * nchunks;
     const int TILE = 64 * N;
     const size_t STG = stage_bytes(MODE, N);
+    const int NS_IN = p.nsin;
     uint8_t* in_base = sm;
     uint8_t* op_base = sm + NS_IN * STG;
     const int OPB = 2 * N * KC * 4;
@@ -195,9 +232,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant
 
     if (tid == 0) {
         abort_flag = 0;
-        for (int i = 0; i < NS_IN; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], N_FORM); }
+        for (int i = 0; i < NS_IN; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], N_FORM); mbar_init(&ready[i], 1); }
         for (int i = 0; i < NS_OP; ++i) { mbar_init(&opready[i], N_FORM); mbar_init(&opfree[i], 1); }
-        for (int i = 0; i < 2; ++i) { mbar_init(&tfull[i], 1); mbar_init(&tfree[i], 4); }
+        for (int i = 0; i < 2; ++i) { mbar_init(&tfull[i], 1); mbar_init(&tfree[i], N_EPI); }
         mbar_init(&finbar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -221,7 +258,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant
         // ---------------- producer ----------------
         if (lane == 0) {
             uint32_t g = 0;
-            int last_parity[NS_IN] = {-1, -1};
+            int last_parity[MAX_IN];
+            for (int s = 0; s < MAX_IN; ++s) last_parity[s] = -1;
             for (int item = blockIdx.x; item < nitems && !abort_flag; item += gridDim.x) {
                 const TmaSlot& sl = p.slot[item / p.nblocks];
                 const int bi = item % p.nblocks;
@@ -337,35 +375,36 @@ __global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant
                 const int w0 = CW * (h1 ? ck - nchunks : ck);
                 const int s = g % NS_IN, o = g % NS_OP;
                 if (!mbar_wait(&full[s], (g / NS_IN) & 1, &abort_flag)) { ok = false; break; }
+                if (!mbar_wait(&ready[s], (g / NS_IN) & 1, &abort_flag)) { ok = false; break; }
                 if (g >= NS_OP && !mbar_wait(&opfree[o], ((g / NS_OP) - 1) & 1, &abort_flag)) { ok = false; break; }
                 const uint8_t* st = in_base + (size_t)s * STG;
-                const cplx* pa = reinterpret_cast<const cplx*>(st + (size_t)stage_tiles(MODE) * TILE);
+                const cplxf* pf = reinterpret_cast<const cplxf*>(st + (size_t)stage_tiles(MODE) * TILE + PI_F32);
                 uint8_t* ob = op_base + (size_t)o * opbuf_bytes(N);
                 uint8_t* Ahi = ob;
                 uint8_t* Alo = ob + A_OP;
                 uint8_t* Bhi = ob + 2 * A_OP;
                 uint8_t* Blo = Bhi + OPB;
                 // A: rows ν < N (rows ≥ N of the 128-lane operand are never read back), K = [Re, Im] pairs
-                for (int e = ft; e < N * (KC / 4); e += FORMERS) {
+                for (int e = ft; e < 4 * N; e += FORMERS) {  // A items (row r, K quad j), rows fastest
                     const int r = e % N, j = e / N;
                     const float4 v = *reinterpret_cast<const float4*>(st + T_A * TILE + (size_t)(r * KC + 4 * j) * 4);
                     st_quad(Ahi, Alo, op_off(r, 4 * j), v);
                 }
                 // B: (ω pair j, ν') items, ν' fastest; rows 2ν' and 2ν'+1 of the real form, k = 4j..4j+3:
                 // [Re M(ω), −Im M(ω), Re M(ω+1), −Im M(ω+1)] and [Im M(ω), Re M(ω), Im M(ω+1), Re M(ω+1)]
-                for (int e = ft; e < (KC / 4) * N; e += FORMERS) {
+                for (int e = ft; e < 4 * N; e += FORMERS) {  // B items (column ν', ω pair j), columns fastest
                     const int col = e % N, j = e / N;
                     cplxf M2[2];
 #pragma unroll
                     for (int h2 = 0; h2 < 2; ++h2) {
                         const int wl = 2 * j + h2, w = w0 + wl;
-                        const cplxf pi0 = has_pi0 ? to_f32(pa[CW + wl]) : cplxf{0.f, 0.f};
+                        const cplxf pi0 = has_pi0 ? pf[CW + wl] : cplxf{0.f, 0.f};
                         const cplxf f0 = ld2(st + T_B0 * TILE + (size_t)(wl * NN + 2 * col) * 4);
                         cplxf M{0.f, 0.f};
                         if (MODE == 0) {
                             M = pi0 * f0;
                         } else {
-                            const cplxf pi = to_f32(pa[wl]);
+                            const cplxf pi = pf[wl];
                             if (oneloop) {
                                 M = ((pi - pi0) * f0) * s1;
                             } else {
@@ -389,7 +428,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant
                                     M = ((pi - pi0) * f0 + pi * gs) * s1;
                                     if (inb) M += pi * fl * s2;
                                 } else {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL]
-                                    const cplxf tpi = to_f32(pa[2 * CW + wl]);
+                                    const cplxf tpi = pf[2 * CW + wl];
                                     const cplxf tg = ld2(st + T_TG * TILE + og);
                                     M = (tpi * (f0 + gs) + pi * tg) * s1;
                                     if (inb) {
@@ -421,10 +460,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant
             }
             if (!ok) { fail(); break; }
         }
-    } else {
+    } else if (warp < W_CONV) {
         // ---------------- epilogue ----------------
-        const int q = warp & 3;  // TMEM lane quadrant this warp may read
-        const int nu = 32 * q + lane;
+        // TMEM lane quadrant q holds rows 32q..32q+31; its EPI_PER_Q warps take alternate groups of 16
+        // accumulator columns (8 complex outputs).  Each group is transposed through the warp's tile so
+        // that a warp reads FL and writes the FP64 outputs as 4 contiguous row segments per instruction.
+        const int q = warp & 3, sub = (warp - W_EPI0) >> 2;
+        float* tile = epi_tile + (warp - W_EPI0) * 32 * TP;
         const float Tf = (float)d.T;
         int li = 0;
         for (int item = blockIdx.x; item < nitems; item += gridDim.x, ++li) {
@@ -435,39 +477,97 @@ __global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant
             const size_t base = (size_t)blk * N * N;
             const int ch = sl.ch;
             const float sgn = (ch == CH_A) ? 1.f : -1.f;
+            const bool epi = MODE >= 1 && !(sl.flags & K3F_NOEPI);
+            const bool acc = (sl.flags & K3F_ACC) != 0;
             const int t = li & 1;
             if (!mbar_wait(&tfull[t], (li >> 1) & 1, &abort_flag)) { fail(); break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int c0 = 0; c0 < NN; c0 += 16) {
-                uint32_t r[16];
-                const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(t * 256 + c0);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                      "=r"(r[15])
-                    : "r"(taddr)
-                    : "memory");
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (nu < N) {
+            if (32 * q < N) {  // (a quadrant beyond the block's rows has nothing to store)
+                for (int c0 = 16 * sub; c0 < NN; c0 += 16 * EPI_PER_Q) {
+                    uint32_t r[16];
+                    const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(t * 256 + c0);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                        "[%16];"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                          "=r"(r[14]), "=r"(r[15])
+                        : "r"(taddr)
+                        : "memory");
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const int col = c0 / 2 + j;
-                        const cplxf v{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
-                        const size_t io = base + (size_t)nu * N + col;
-                        cplx o;
-                        if (MODE == 0) o = to_d(v * (Tf * sgn));
-                        else if (sl.flags & K3F_NOEPI) o = to_d(v * Tf);
-                        else if (MODE == 1) o = to_d(v * Tf + fl_box(sl.FLc, sl.FLt, sl.FLa, ch, io));
-                        else o = to_d(v * Tf + fl_box(sl.tFLc, sl.tFLt, sl.tFLa, ch, io));
-                        sl.out[io] = (sl.flags & K3F_ACC) ? sl.out[io] + o : o;
+                    for (int k = 0; k < 16; ++k) tile[lane * TP + k] = __uint_as_float(r[k]);
+                    __syncwarp();
+                    const int cc = lane & 7;  // complex column within the group
+                    // the γL terms of all 8 passes are loaded before any is used (one load latency per group)
+                    cplxf gl[8];
+#pragma unroll
+                    for (int pass = 0; pass < 8; ++pass) {
+                        const int row = 32 * q + pass * 4 + (lane >> 3);
+                        const size_t io = base + (size_t)row * N + c0 / 2 + cc;
+                        gl[pass] = cplxf{0.f, 0.f};
+                        if (epi && row < N)
+                            gl[pass] = MODE == 1 ? fl_box(sl.FLc, sl.FLt, sl.FLa, ch, io)
+                                                 : fl_box(sl.tFLc, sl.tFLt, sl.tFLa, ch, io);
                     }
+                    // the accumulating form (an FP64 read-modify-write) is a separate loop, so that the
+                    // plain stores carry no FP64 add the compiler might evaluate ahead of the select
+                    if (!acc) {
+                        // independent batches (tile loads, arithmetic, stores) keep the 8 passes in flight together
+                        float2 dv[8];
+#pragma unroll
+                        for (int pass = 0; pass < 8; ++pass)
+                            dv[pass] = *reinterpret_cast<const float2*>(tile + (pass * 4 + (lane >> 3)) * TP + 2 * cc);
+                        double2 o[8];
+#pragma unroll
+                        for (int pass = 0; pass < 8; ++pass) {
+                            const cplxf v{dv[pass].x, dv[pass].y};
+                            const cplxf f = (MODE == 0) ? v * (Tf * sgn) : v * Tf + gl[pass];
+                            o[pass] = make_double2(f2d_bits(f.x), f2d_bits(f.y));
+                        }
+                        double2* dst = reinterpret_cast<double2*>(sl.out + base) + (size_t)(32 * q + (lane >> 3)) * N + c0 / 2 + cc;
+#pragma unroll
+                        for (int pass = 0; pass < 8; ++pass)
+                            if (32 * q + pass * 4 + (lane >> 3) < N) dst[(size_t)pass * 4 * N] = o[pass];
+                    } else {
+                        for (int pass = 0; pass < 8; ++pass) {
+                            const int rr = pass * 4 + (lane >> 3);
+                            const int row = 32 * q + rr;
+                            if (row < N) {
+                                const float2 dv = *reinterpret_cast<const float2*>(tile + rr * TP + 2 * cc);
+                                const cplxf v{dv.x, dv.y};
+                                const cplxf f = (MODE == 0) ? v * (Tf * sgn) : v * Tf + gl[pass];
+                                const size_t io = base + (size_t)row * N + c0 / 2 + cc;
+                                sl.out[io] = sl.out[io] + c2d_bits(f);
+                            }
+                        }
+                    }
+                    __syncwarp();
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(&tfree[t]);
+        }
+    } else {
+        // ---------------- converter: the chunk's Π, Π0, dΠ to FP32, once per stage use ----------------
+        uint32_t g = 0;
+        for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+            if (abort_flag) break;
+            bool ok = true;
+            for (int ck = 0; ck < nck; ++ck) {
+                const int s = g % NS_IN;
+                if (!mbar_wait(&full[s], (g / NS_IN) & 1, &abort_flag)) { ok = false; break; }
+                uint8_t* pbase = in_base + (size_t)s * STG + (size_t)stage_tiles(MODE) * TILE;
+                if (lane < 3 * CW) {
+                    const cplx v = reinterpret_cast<const cplx*>(pbase)[lane];
+                    reinterpret_cast<cplxf*>(pbase + PI_F32)[lane] = to_f32(v);
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&ready[s]);
+                ++g;
+            }
+            if (!ok) { fail(); break; }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -480,8 +580,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_bse_K3_tma(const __grid_constant
 // shared-memory limit records of the three instantiations (per device)
 SmemRecord g_raised[3];
 
+// input stages that fit beside the operand buffers (0: the box does not fit)
+int tma_stages(int mode, int N) {
+    const size_t ops = NS_OP * opbuf_bytes(N);
+    if (ops >= SMEM_BUDGET) return 0;
+    size_t n = (SMEM_BUDGET - ops) / stage_bytes(mode, N);
+    if (n > (size_t)MAX_IN) n = MAX_IN;
+    return n >= 2 ? (int)n : 0;
+}
 size_t tma_smem(int mode, int N) {
-    const size_t need = NS_IN * stage_bytes(mode, N) + NS_OP * opbuf_bytes(N);
+    const size_t need = tma_stages(mode, N) * stage_bytes(mode, N) + NS_OP * opbuf_bytes(N);
     return need < MIN_SMEM ? MIN_SMEM : need;
 }
 
@@ -523,7 +631,7 @@ bool encode_pair(CUtensorMap* m, const void* base, size_t ncplx, int N) {
 bool k3_tma_supported(const Dims& d, int mode) {
     if (!(d.N3n >= 32 && d.N3n <= 128 && (d.N3n % 8) == 0)) return false;
     if (!encode_fn()) return false;
-    return NS_IN * stage_bytes(mode, d.N3n) + NS_OP * opbuf_bytes(d.N3n) + 8 * 1024 <= 227 * 1024;
+    return tma_stages(mode, d.N3n) >= 2;
 }
 
 cudaError_t launch_bse_K3_tma(cudaStream_t s, int mode, const K3Args3F& a, int nslots, const Dims& d, int* err,
@@ -580,6 +688,7 @@ cudaError_t launch_bse_K3_tma(cudaStream_t s, int mode, const K3Args3F& a, int n
     p.blocks = a.blocks;
     p.nblocks = a.nblocks;
     p.nslots = nslots;
+    p.nsin = tma_stages(mode, N);
     int dev = 0, nsm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -591,9 +700,9 @@ cudaError_t launch_bse_K3_tma(cudaStream_t s, int mode, const K3Args3F& a, int n
     if (e != cudaSuccess) return e;
     const int nitems = nslots * a.nblocks;
     const unsigned grid = (unsigned)(nitems < nsm ? nitems : nsm);
-    if (mode == 0) k_bse_K3_tma<0><<<grid, THREADS, smem, s>>>(p, d, err);
-    else if (mode == 1) k_bse_K3_tma<1><<<grid, THREADS, smem, s>>>(p, d, err);
-    else k_bse_K3_tma<2><<<grid, THREADS, smem, s>>>(p, d, err);
+    if (mode == 0) k_bse_K3_tma<0><<<grid, Roles<0>::THREADS, smem, s>>>(p, d, err);
+    else if (mode == 1) k_bse_K3_tma<1><<<grid, Roles<1>::THREADS, smem, s>>>(p, d, err);
+    else k_bse_K3_tma<2><<<grid, Roles<2>::THREADS, smem, s>>>(p, d, err);
     return cudaGetLastError();
 }
 
