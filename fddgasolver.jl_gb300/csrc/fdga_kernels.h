@@ -313,6 +313,17 @@ cudaError_t launch_ma_qrot(cudaStream_t s, int nblk, const AAVecs32W& Q, int m, 
 cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double U,
                        int NO, int Nq, int local, cplx* out);
 cudaError_t measure_fp64_rate(float* ms, double* gflops);
+// mfRG linear map (fdga_mfrg.cu): part 0 the irreducible caches of the state vertex, part 1 the
+// F0-only caches; the K1/K2 BSEs of the map (FP64, F0 and FL.K2 only)
+cudaError_t launch_build_cache_mfrg(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,
+                                    const Dims& d, int part);
+cudaError_t launch_build_cache_mfrg(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
+                                    const Dims& d, int part);
+cudaError_t launch_bse_K1_mfrg(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const ChanWork& cw,
+                               const Dims& d);
+cudaError_t launch_bse_K2_mfrg(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const ChanWork& cw,
+                               const Dims& d);
+cudaError_t launch_scale(cudaStream_t s, cplx* out, const cplx* in, double sc, size_t n);
 // GMRES building blocks (real inner products on the FP32 Krylov basis)
 cudaError_t launch_kr_point(cudaStream_t s, int nblk, const cplx* x, const cplxf* v, double eps, cplx* xp, size_t n);
 cudaError_t launch_kr_apply(cudaStream_t s, int nblk, const cplx* y, const cplx* y0, const cplxf* v, double a,

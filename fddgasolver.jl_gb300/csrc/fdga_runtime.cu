@@ -158,6 +158,13 @@ struct fdga_handle {
         cplx *LRb = nullptr, *Lb = nullptr;
         double* nbar = nullptr;
     } adj;
+    // mfRG linear map (src/mfRG.jl:20-89): its scaled input vertex x·factor, its output Φ_mfRG and a
+    // work vector (state layout; the Σ parts stay zero), one captured graph per precision
+    struct Mfrg {
+        cplx *x = nullptr, *y = nullptr, *u = nullptr;
+        Graph graphs[2];
+    } mf;
+    size_t nc_sig = 0;  // offset of Σ's classes in the compact (one value per class) state
     std::vector<void*> allocs;
 };
 
@@ -1463,6 +1470,8 @@ void drop_graph_array(A& gs) {
 void drop_graphs(fdga_handle* h) {
     drop_graph_array(h->graphs);
     drop_graph_array(h->tan.graphs);
+    for (auto& g : h->mf.graphs)
+        if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
     if (h->rg.g.exec) cudaGraphExecDestroy(h->rg.g.exec);
     h->rg.g = Graph();
     h->rg.x = nullptr;
@@ -2059,8 +2068,18 @@ int fdga_residual(fdga_handle* h, int strategy, const double* x, double* R, size
     return check_device_error(h);
 }
 
-int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int* iters, double* res,
-               double* trace) {
+}  // extern "C"
+
+namespace {
+
+// Anderson solve hooks: before() runs ahead of each map evaluation, after() between the map and the
+// residual (it may replace the new state y, e.g. by x + a preconditioned residual)
+struct SolveHooks {
+    std::function<int()> before, after;
+};
+
+int solve_anderson(fdga_handle* h, int strategy, bool update_sigma, int maxiter, double tol, double beta, int mem,
+                   int* iters, double* res, double* trace, const SolveHooks* hk) {
     if (!h) return FDGA_ERR_ARG;
     if (maxiter < 1 || mem < 0 || !(tol >= 0)) return fail(h, FDGA_ERR_ARG, "invalid solver parameters");
     const size_t n = h->nstate;
@@ -2095,8 +2114,11 @@ int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double bet
     double resid = 0.0;
     bool converged = false;
     for (it = 1; it <= maxiter; ++it) {
-        int r = run_iteration(h, strategy, true, true);
+        int r = hk && hk->before ? hk->before() : FDGA_OK;
         if (r) return r;
+        r = run_iteration(h, strategy, update_sigma, true);
+        if (r) return r;
+        if (hk && hk->after && (r = hk->after())) return r;
         CK(launch_residual(h->st, h->yS, h->xS, fx, g, beta, h->d_part, NBLK_RED, n));
         resid = reduce_max(h, NBLK_RED, status);
         if (status) return status;
@@ -2140,6 +2162,15 @@ int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double bet
     if (iters) *iters = converged ? it : -it;
     if (res) *res = resid;
     return FDGA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdga_solve(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int* iters, double* res,
+               double* trace) {
+    return solve_anderson(h, strategy, true, maxiter, tol, beta, mem, iters, res, trace, nullptr);
 }
 
 int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int* iters, double* res,
@@ -2331,6 +2362,7 @@ int ensure_compact(fdga_handle* h) {
     blk.push_back({&h->gSig, 3 * h->nchan, h->nGk});
     uint32_t off = 0;
     for (const auto& b : blk) {
+        if (b.g == &h->gSig) h->nc_sig = off;
         const bool triv = b.g->trivial;
         CK(launch_kc_codes(h->st, triv ? nullptr : b.g->d_map, triv ? nullptr : b.g->d_items,
                            triv ? (int)b.len : b.g->nitems, b.len, b.base, off, h->kc_code, h->kc_pos));
@@ -2448,11 +2480,18 @@ int mixed_tangent_base_from_fp64(fdga_handle* h) {
     return FDGA_OK;
 }
 
+// The operator of a GMRES solve: w = A v for a unit compact FP32 direction v.  apply() adds the map
+// evaluations it made to the solve's count; cost is that number, for the budget check.
+struct KrylovOp {
+    std::function<int(const cplxf* v, cplxf* w)> apply;
+    int cost = 1;
+};
+
 // Restarted GMRES(m) for A dx = b (compact vectors), dx starting at 0.  Cycles after the first
-// restart from the true residual b − A dx.  relres = final ‖b − A dx‖/‖b‖ estimate.
-int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplx* b, cplx* dx, int m,
-                int cycles, double rtol, double eps_rel, bool central, int max_maps, int& nmaps, int& iters,
-                double& relres) {
+// restart from the true residual b − A dx.  Stops at ‖b − A dx‖ <= atol + rtol ‖b‖ (estimate);
+// relres = final ‖b − A dx‖/‖b‖ estimate.
+int gmres_core(fdga_handle* h, const KrylovOp& op, const cplx* b, cplx* dx, int m, int cycles, double rtol,
+               double atol, int max_maps, int& nmaps, int& iters, double& relres) {
     const size_t nc = h->nc;
     KrVecs V{};
     for (int i = 0; i <= m; ++i) V.v[i] = h->kr32[i];
@@ -2460,13 +2499,11 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
     cplxf* w = h->kr32[m + 1];
     cplxf* sc = h->kr32[m + 2];
     cplx* rr = h->kr64[3];
-    cplx* xc = h->kr64[5];
     const float* W = h->kc_w;
     int r;
-    double xnorm = 0.0, bnorm = 0.0;
-    CK(launch_kc_gather(h->st, NBLK_RED, xb, nullptr, h->kc_pos, 1.0, xc, nc));
-    if ((r = cnorm(h, xc, sc, xnorm)) || (r = cnorm(h, b, sc, bnorm))) return r;
-    const double eps = eps_rel * (1.0 + xnorm);
+    double bnorm = 0.0;
+    if ((r = cnorm(h, b, sc, bnorm))) return r;
+    const double thr = atol + rtol * bnorm;
     CK(cudaMemsetAsync(dx, 0, nc * sizeof(cplx), h->st));
     relres = 1.0;
     if (bnorm == 0.0) { relres = 0.0; return FDGA_OK; }
@@ -2485,14 +2522,14 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
             double dn = 0.0;
             if ((r = cnorm(h, dx, sc, dn))) return r;
             if (dn == 0.0) break;
-            if (nmaps + (central && !use_tangent(h, strategy) ? 2 : 1) > max_maps) break;
+            if (nmaps + op.cost > max_maps) break;
             CK(launch_kr_load(h->st, NBLK_RED, dx, W, sc, h->kr_part, nc));
             CK(launch_kr_scale(h->st, NBLK_RED, sc, dn, sc, nc));
-            if ((r = apply_A(h, strategy, xb, yb, sc, eps, central, w, nmaps))) return r;
+            if ((r = op.apply(sc, w))) return r;
             CK(launch_kr_resid(h->st, NBLK_RED, b, w, -dn, nullptr, nullptr, 0.0, rr, nc));
             if ((r = cnorm(h, rr, sc, beta))) return r;
             relres = beta / bnorm;
-            if (relres <= rtol) break;
+            if (beta <= thr) break;
             CK(launch_kr_load(h->st, NBLK_RED, rr, W, sc, h->kr_part, nc));
             CK(launch_kr_scale(h->st, NBLK_RED, sc, beta, Vw[0], nc));
         }
@@ -2501,8 +2538,8 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
         int k = 0;
         double est = beta;
         for (int j = 0; j < m; ++j) {
-            if (nmaps + (central && !use_tangent(h, strategy) ? 2 : 1) > max_maps) break;
-            if ((r = apply_A(h, strategy, xb, yb, V.v[j], eps, central, w, nmaps))) return r;
+            if (nmaps + op.cost > max_maps) break;
+            if ((r = op.apply(V.v[j], w))) return r;
             // classical Gram-Schmidt, twice (weighted inner products)
             CK(launch_kr_dots(h->st, NBLK_RED, V, j + 1, w, W, h->kr_part, -1, nc));
             CK(launch_kr_reduce(h->st, h->kr_part, NBLK_RED, j + 1, c1));
@@ -2534,7 +2571,7 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
             ++iters;
             k = j + 1;
             est = std::fabs(g[j + 1]);
-            if (est <= rtol * bnorm || hn == 0.0) break;
+            if (est <= thr || hn == 0.0) break;
         }
         if (k == 0) break;
         for (int i = k - 1; i >= 0; --i) {
@@ -2545,10 +2582,276 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
         CK(cudaMemcpyAsync(cy, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, h->st));
         CK(launch_kr_update(h->st, NBLK_RED, dx, V, k, cy, 1.0, nc));
         relres = est / bnorm;
-        if (relres <= rtol) break;
+        if (est <= thr) break;
     }
     CK(cudaStreamSynchronize(h->st));
     return FDGA_OK;
+}
+
+// GMRES for the Newton step: A v = v − J v at the base point xb (apply_A); the difference step is
+// ε = eps_rel (1 + ‖xb‖).
+int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, const cplx* b, cplx* dx, int m,
+                int cycles, double rtol, double eps_rel, bool central, int max_maps, int& nmaps, int& iters,
+                double& relres) {
+    cplx* xc = h->kr64[5];
+    double xnorm = 0.0;
+    CK(launch_kc_gather(h->st, NBLK_RED, xb, nullptr, h->kc_pos, 1.0, xc, h->nc));
+    int r = cnorm(h, xc, h->kr32[m + 2], xnorm);
+    if (r) return r;
+    const double eps = eps_rel * (1.0 + xnorm);
+    KrylovOp op;
+    op.cost = central && !use_tangent(h, strategy) ? 2 : 1;
+    op.apply = [&](const cplxf* v, cplxf* w) { return apply_A(h, strategy, xb, yb, v, eps, central, w, nmaps); };
+    return gmres_core(h, op, b, dx, m, cycles, rtol, 0.0, max_maps, nmaps, iters, relres);
+}
+
+// ---------------------------------------------------------------------------------------------
+// mfRG linear map (src/mfRG.jl:20-89): y = x − Φ_mfRG(x·f)/f, f = 1e-2, on the vertex part of the
+// state.  Φ_mfRG runs the iteration's BSE sequence on the vertex x·f with the reference system's
+// bubble Π0 in every BSE and F0 in the right factors (the is_mfRG branches):
+//   caches (fdga_mfrg.cu) → L_K2 (FL.K2) → K1, K2 of the map → L_K3 (FL.K3) → K3 with Π = Π0.
+// The map depends on the state only through x (Π0, F0, G0 are the reference system's): it is the
+// same linear operator for every application within a solve.  Nonlocal solver; :fdPA and
+// :fdPA_1loop run the same map, :fdPA_new (the _new BSEs) is a local-solver strategy here.
+// ---------------------------------------------------------------------------------------------
+constexpr double kMfrgFactor = 1e-2;
+
+int check_mfrg(fdga_handle* h, int strategy) {
+    if (!h->finalized) return fail(h, FDGA_ERR_STATE, "fdga_finalize has not been called");
+    if (strategy != FDGA_FDPA && strategy != FDGA_FDPA_NEW && strategy != FDGA_FDPA_1LOOP)
+        return fail(h, FDGA_ERR_ARG, "the mfRG map takes the strategies fdPA, fdPA_new and fdPA_1loop");
+    if (h->d.local) return fail(h, FDGA_ERR_UNSUPPORTED, "the mfRG map is defined for the nonlocal solver");
+    if (strategy == FDGA_FDPA_NEW)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the :fdPA_new BSEs exist for the local solver only");
+    if (h->precision == FDGA_MIXED) {
+        int r = ensure_mixed(h);
+        if (r) return r;
+    }
+    if (!h->mf.x) {
+        AL(h->mf.x, h->nstate);
+        AL(h->mf.y, h->nstate);
+        AL(h->mf.u, h->nstate);
+    }
+    return FDGA_OK;
+}
+
+// the F0-only caches of the map (once per solve; the iteration overwrites the right ones)
+int mfrg_prepare(fdga_handle* h) {
+    Caches C{};
+    const bool mixed = h->precision == FDGA_MIXED;
+    for (int i = 0; i < 10; ++i) {
+        C.c[i] = h->cache + (size_t)i * h->n3;
+        C.f[i] = mixed ? h->cachef + (size_t)i * h->n3 : nullptr;
+    }
+    if (mixed) {
+        for (int i = 0; i < 4; ++i) CK(launch_to_f32(h->st, h->Fref[i], h->Freff[i], h->nRef));
+        VertPF Ff = vertex_view_t<cplxf>(h, h->xSf, h->avgf, h->Freff);
+        CK(launch_build_cache_mfrg(h->st, Ff, C, h->d_k3blocks, h->nk3blocks, h->d, 1));
+    } else {
+        CK(launch_build_cache_mfrg(h->st, vertex_view(h, h->mf.x), C, h->d_k3blocks, h->nk3blocks, h->d, 1));
+    }
+    return FDGA_OK;
+}
+
+// Φ_mfRG(mf.x) into mf.y.  Branch C: L_K2 → K1, K2 of the map; main: caches → L_K3 → K3.
+int enqueue_mfrg(fdga_handle* h, int& nl) {
+    cudaStream_t s = h->st, sC = h->st3;
+    const Dims& d = h->d;
+    nl = 0;
+    const bool mixed = h->precision == FDGA_MIXED;
+    VertP F = vertex_view(h, h->mf.x);
+    if (d.Nq > 1) {
+        ChanArrays in;
+        ChanArraysW out;
+        for (int c = 0; c < 3; ++c) {
+            in.K1[c] = F.g[c].K1; in.K2[c] = F.g[c].K2; in.K3[c] = F.g[c].K3;
+            out.K1[c] = (cplx*)F.g[c].A1; out.K2[c] = (cplx*)F.g[c].A2; out.K3[c] = (cplx*)F.g[c].A3;
+        }
+        LC(launch_qavg(s, in, out, d));
+    }
+    VertPF Ff{};
+    if (mixed) {
+        LC(launch_to_f32(s, h->mf.x, h->xSf, 3 * h->nchan));
+        if (d.Nq > 1) LC(launch_to_f32(s, h->avg, h->avgf, h->navg));
+        Ff = vertex_view_t<cplxf>(h, h->xSf, h->avgf, h->Freff);
+    }
+    CK(cudaEventRecord(h->evA, s));
+    CK(cudaStreamWaitEvent(sC, h->evA, 0));
+    Caches C{};
+    for (int i = 0; i < 10; ++i) {
+        C.c[i] = h->cache + (size_t)i * h->n3;
+        C.f[i] = mixed ? h->cachef + (size_t)i * h->n3 : nullptr;
+    }
+    if (mixed) LC(launch_build_cache_mfrg(s, Ff, C, h->d_k3blocks, h->nk3blocks, d, 0));
+    else LC(launch_build_cache_mfrg(s, F, C, h->d_k3blocks, h->nk3blocks, d, 0));
+    BubbleP B{h->Pipp, h->Piph, h->Pi0pp, h->Pi0ph};
+    auto Pi0 = [&](int ch) { return ch == CH_P ? h->Pi0pp : h->Pi0ph; };
+    auto work = [&](int cls, cplx* raw) {
+        ChanWork cw{};
+        const size_t n = cls == 1 ? h->n1 : h->n2;
+        for (int ch = 0; ch < 3; ++ch) {
+            const Group& g = cls == 1 ? h->gK1 : k2group(h, ch);
+            cw.items[ch] = g.trivial ? nullptr : g.d_items;
+            cw.nitems[ch] = g.trivial ? (int)n : g.nitems;
+            cw.out[ch] = raw + (size_t)ch * n;
+        }
+        return cw;
+    };
+    auto fin = [&](int cls, cplx* raw, cplx* const out[3], const Group* const grp[3]) {
+        Finalize3 f{};
+        const size_t n = cls == 1 ? h->n1 : (cls == 2 ? h->n2 : h->n3);
+        for (int ch = 0; ch < 3; ++ch) {
+            f.raw[ch] = raw + (size_t)ch * n;
+            f.out[ch] = out[ch];
+            f.map[ch] = grp[ch]->trivial ? nullptr : grp[ch]->d_map;
+            f.FL[ch] = h->FLK2 + (size_t)ch * h->n2;
+        }
+        return f;
+    };
+    {  // branch C: FL.K2, then the K1 and K2 of the map (they need FL.K2 only)
+        ChanWork cw = work(2, h->raw2);
+        if (mixed) LC(launch_bse_L_K2_all(sC, Ff, B, cw, d));
+        else LC(launch_bse_L_K2_all(sC, F, B, cw, d));
+        cplx* out[3] = {h->FLK2, h->FLK2 + h->n2, h->FLK2 + 2 * h->n2};
+        const Group* grp[3] = {&h->gK2pp, &h->gK2ph, &h->gK2ph};
+        Finalize3 f2 = fin(2, h->raw2, out, grp);
+        if (mixed)
+            for (int c = 0; c < 3; ++c) f2.outf[c] = h->FLK2f + (size_t)c * h->n2;
+        LC(launch_finalize3(sC, f2, 0, 1, h->n2));
+        FLP FL;
+        for (int c = 0; c < 3; ++c) FL.K2[c] = h->FLK2 + (size_t)c * h->n2;
+        ChanWork c1 = work(1, h->raw1);
+        LC(launch_bse_K1_mfrg(sC, F, FL, B, c1, d));
+        cplx* o1[3] = {chanK(h, h->mf.y, CH_P, 1), chanK(h, h->mf.y, CH_T, 1), chanK(h, h->mf.y, CH_A, 1)};
+        const Group* g1[3] = {&h->gK1, &h->gK1, &h->gK1};
+        LC(launch_finalize3(sC, fin(1, h->raw1, o1, g1), 0, 1, h->n1));
+        ChanWork c2 = work(2, h->raw2);
+        LC(launch_bse_K2_mfrg(sC, F, FL, B, c2, d));
+        cplx* o2[3] = {chanK(h, h->mf.y, CH_P, 2), chanK(h, h->mf.y, CH_T, 2), chanK(h, h->mf.y, CH_A, 2)};
+        LC(launch_finalize3(sC, fin(2, h->raw2, o2, grp), 1, 1, h->n2));
+        CK(cudaEventRecord(h->evC, sC));
+    }
+    const int order[3] = {CH_P, CH_A, CH_T};
+    {  // FL.K3 (BSE_L_K3!, unchanged by the mfRG flag)
+        K3Args3 a3{};
+        K3Args3F a3f{};
+        for (int i = 0; i < 3; ++i) {
+            const int ch = order[i];
+            const int cg = ch == CH_P ? 4 : (ch == CH_A ? 5 : 6), cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+            K3Args& a = a3.a[i];
+            a.A = C.c[cg]; a.B0 = C.c[cf0]; a.Pi0 = Pi0(ch);
+            a.out = h->raw3 + (size_t)ch * h->n3;
+            a3.ch[i] = ch;
+            K3ArgsF& af = a3f.a[i];
+            af.A = C.f[cg]; af.B0 = C.f[cf0]; af.Pi0 = Pi0(ch);
+            af.out = a.out;
+            a3f.ch[i] = ch;
+        }
+        a3.blocks = a3f.blocks = h->d_k3blocks;
+        a3.nblocks = a3f.nblocks = h->nk3blocks;
+        if (mixed && k3_tensor_cores(h, 0)) LC(launch_k3_tensor_cores(h, s, 0, a3f));
+        else if (mixed) LC(launch_bse_K3_f32(s, 0, a3f, 3, d, h->k3_tile[FDGA_MIXED][0]));
+        else LC(launch_bse_K3(s, 0, a3, 3, d, 0, h->k3_tile[FDGA_FP64][0]));
+        cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
+        const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
+        Finalize3 f3 = fin(3, h->raw3, out, grp);
+        if (mixed)
+            for (int c = 0; c < 3; ++c) f3.outf[c] = h->FLK3f + (size_t)c * h->n3;
+        LC(launch_finalize3(s, f3, 0, 1, h->n3));
+    }
+    {  // K3 of the map: the plain contraction with Π = Π0 (its (Π - Π0) cacheF0 term vanishes)
+        K3Args3 a3{};
+        K3Args3F a3f{};
+        for (int i = 0; i < 3; ++i) {
+            const int ch = order[i];
+            const int cg = ch == CH_P ? 0 : (ch == CH_A ? 5 : 6), cf = ch == CH_P ? 7 : (ch == CH_A ? 8 : 9);
+            const int cf0 = ch == CH_P ? 1 : (ch == CH_A ? 2 : 3);
+            K3Args& a = a3.a[i];
+            a.A = C.c[cf]; a.B0 = C.c[cf0]; a.G = C.c[cg]; a.Pi = Pi0(ch); a.Pi0 = Pi0(ch);
+            a.FLc = h->FLK3 + (size_t)ch * h->n3; a.FLt = h->FLK3 + (size_t)CH_T * h->n3;
+            a.FLa = h->FLK3 + (size_t)CH_A * h->n3;
+            a.out = h->raw3 + (size_t)ch * h->n3;
+            a.flags = 0;
+            a3.ch[i] = ch;
+            if (mixed) {
+                K3ArgsF& af = a3f.a[i];
+                af.A = C.f[cf]; af.B0 = C.f[cf0]; af.G = C.f[cg]; af.Pi = a.Pi; af.Pi0 = a.Pi0;
+                af.FLc = h->FLK3f + (size_t)ch * h->n3; af.FLt = h->FLK3f + (size_t)CH_T * h->n3;
+                af.FLa = h->FLK3f + (size_t)CH_A * h->n3;
+                af.out = a.out;
+                af.flags = 0;
+                a3f.ch[i] = ch;
+            }
+        }
+        a3.blocks = a3f.blocks = h->d_k3blocks;
+        a3.nblocks = a3f.nblocks = h->nk3blocks;
+        if (mixed && k3_tensor_cores(h, 1)) LC(launch_k3_tensor_cores(h, s, 1, a3f));
+        else if (mixed) LC(launch_bse_K3_f32(s, 1, a3f, 3, d, h->k3_tile[FDGA_MIXED][1]));
+        else LC(launch_bse_K3(s, 1, a3, 3, d, 0, h->k3_tile[FDGA_FP64][1]));
+        cplx* out[3] = {chanK(h, h->mf.y, CH_P, 3), chanK(h, h->mf.y, CH_T, 3), chanK(h, h->mf.y, CH_A, 3)};
+        const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
+        LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
+    }
+    CK(cudaStreamWaitEvent(s, h->evC, 0));
+    return FDGA_OK;
+}
+
+// one application of Φ_mfRG (mf.x → mf.y) as a captured graph per precision
+int run_mfrg(fdga_handle* h) {
+    Graph& g = h->mf.graphs[h->precision];
+    if (!g.exec) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        int nl = 0;
+        int r = enqueue_mfrg(h, nl);
+        cudaError_t ee = cudaStreamEndCapture(h->st, &graph);
+        if (r) {
+            if (ee == cudaSuccess) cudaGraphDestroy(graph);
+            return r;
+        }
+        if (ee != cudaSuccess) return cuda_fail(h, ee, "cudaStreamEndCapture");
+        ee = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ee != cudaSuccess) { g.exec = nullptr; return cuda_fail(h, ee, "cudaGraphInstantiate"); }
+        g.nodes = nl;
+    }
+    CK(cudaGraphLaunch(g.exec, h->st));
+    h->last_launches = g.nodes;
+    return FDGA_OK;
+}
+
+// The mfRG operator on compact vectors for GMRES: w = v − Φ_mfRG(f·v)/f (the Σ classes pass through)
+KrylovOp mfrg_operator(fdga_handle* h, int& nmaps) {
+    KrylovOp op;
+    op.cost = 1;
+    op.apply = [h, &nmaps](const cplxf* v, cplxf* w) -> int {
+        CK(launch_kc_point(h->st, NBLK_RED, nullptr, v, h->kc_code, kMfrgFactor, h->mf.x, 3 * h->nchan));
+        int r = run_mfrg(h);
+        if (r) return r;
+        ++nmaps;
+        CK(launch_kc_apply(h->st, NBLK_RED, h->mf.y, nullptr, h->kc_pos, v, 1.0, -1.0 / kMfrgFactor, w, h->nc));
+        return FDGA_OK;
+    };
+    return op;
+}
+
+// Krylov solve of the preconditioner, M z = R_F (src/mfRG.jl:145-155), on the compact state: b is the
+// vertex part of (y − x) at the class representatives (Σ's classes zero), z (compact FP64) in
+// h->kr64[2].  Restarted GMRES(min(64, maxiter)), at most maxiter map applications, stopping at
+// ‖r‖ <= atol + rtol ‖b‖.
+int mfrg_krylov(fdga_handle* h, const cplx* y, const cplx* x, int maxiter, double rtol, double atol, int& nmaps,
+                int& iters, double& relres) {
+    const int m = std::max(1, std::min(KR_MAX - 1, maxiter));
+    int r = ensure_krylov(h, m);
+    if (r) return r;
+    cplx* b = h->kr64[1];
+    cplx* z = h->kr64[2];
+    CK(launch_kc_gather(h->st, NBLK_RED, y, x, h->kc_pos, 1.0, b, h->nc));
+    if (h->nc > h->nc_sig) CK(cudaMemsetAsync(b + h->nc_sig, 0, (h->nc - h->nc_sig) * sizeof(cplx), h->st));
+    if ((r = mfrg_prepare(h))) return r;
+    const int cycles = (maxiter + m - 1) / m;
+    KrylovOp op = mfrg_operator(h, nmaps);
+    return gmres_core(h, op, b, z, m, cycles, rtol, atol, maxiter, nmaps, iters, relres);
 }
 
 }  // namespace
@@ -3348,6 +3651,105 @@ int fdga_launches_per_iteration(const fdga_handle* h, int* n) {
     if (!h || !n) return FDGA_ERR_ARG;
     *n = h->last_launches;
     return FDGA_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// mfRG / Krylov-preconditioned solver: src/mfRG.jl:20-89 (the map), :93-173 (the preconditioned
+// fixed point) and the nlsolve(anderson) driver around it.
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+int fdga_mfrg_apply(fdga_handle* h, int strategy, const double* x, double* y, size_t n) {
+    if (!h || !x || !y) return fail(h, FDGA_ERR_ARG, "null argument");
+    int r = check_mfrg(h, strategy);
+    if (r) return r;
+    const size_t nv = 3 * h->nchan;
+    if (n != nv) return fail(h, FDGA_ERR_ARG, "the mfRG map acts on the vertex part of the state (length(S.F))");
+    cudaStream_t s = h->st;
+    CK(cudaMemcpyAsync(h->tmpS, x, nv * sizeof(cplx), cudaMemcpyHostToDevice, s));
+    CK(launch_scatter(s, h->mf.u, h->tmpS, h->perm, nv));
+    CK(launch_scale(s, h->mf.x, h->mf.u, kMfrgFactor, nv));
+    if ((r = mfrg_prepare(h))) return r;
+    if ((r = run_mfrg(h))) return r;
+    CK(launch_kr_axpby(s, NBLK_RED, h->mf.u, h->mf.u, -1.0 / kMfrgFactor, h->mf.y, nv));
+    CK(launch_gather(s, h->tmpS, h->mf.u, h->perm, nv));
+    CK(cudaMemcpyAsync(y, h->tmpS, nv * sizeof(cplx), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return check_device_error(h);
+}
+
+int fdga_residual_mfrg(fdga_handle* h, int strategy, const double* x, double* R, size_t n, int update_sigma,
+                       int krylov_maxiter, double krylov_rtol, double krylov_atol, int* krylov_iters,
+                       double* krylov_res) {
+    if (!h || !x || !R) return fail(h, FDGA_ERR_ARG, "null argument");
+    int r = check_mfrg(h, strategy);
+    if (r) return r;
+    if (krylov_maxiter < 1 || !(krylov_rtol >= 0) || !(krylov_atol >= 0))
+        return fail(h, FDGA_ERR_ARG, "invalid Krylov parameters");
+    const size_t nv = 3 * h->nchan, nS = h->nGk;
+    if (n != (update_sigma ? h->nstate : nv))
+        return fail(h, FDGA_ERR_ARG, update_sigma ? "state length mismatch" : "vertex length mismatch");
+    if (h->c0_dirty && (r = compute_C0(h))) return r;
+    cudaStream_t s = h->st;
+    // x (unsymmetrised) in mf.u; the solver symmetrised from it in xS
+    CK(cudaMemcpyAsync(h->tmpS, x, n * sizeof(cplx), cudaMemcpyHostToDevice, s));
+    if (!update_sigma) CK(cudaMemcpyAsync(h->mf.u + nv, sigmaOf(h, h->xS), nS * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    CK(launch_scatter(s, h->mf.u, h->tmpS, h->perm, n));
+    CK(cudaMemcpyAsync(h->xS, h->mf.u, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    if ((r = symmetrize_state(h))) return r;
+    if ((r = run_iteration(h, strategy, update_sigma != 0, true))) return r;
+    int nmaps = 0, iters = 0;
+    double relres = 0.0;
+    if ((r = mfrg_krylov(h, h->yS, h->mf.u, krylov_maxiter, krylov_rtol, krylov_atol, nmaps, iters, relres))) return r;
+    // R = [z ; Σ(x) - x_Σ]
+    CK(cudaMemsetAsync(h->mf.x, 0, nv * sizeof(cplx), s));
+    CK(launch_kc_axpy(s, NBLK_RED, h->mf.x, h->kr64[2], h->kc_code, 1.0, h->mf.x, nv));
+    if (update_sigma) CK(launch_sub(s, h->mf.x + nv, sigmaOf(h, h->yS), h->mf.u + nv, nS));
+    CK(launch_gather(s, h->tmpS, h->mf.x, h->perm, n));
+    CK(cudaMemcpyAsync(R, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->xS, h->yS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    if (krylov_iters) *krylov_iters = iters;
+    if (krylov_res) *krylov_res = relres;
+    return check_device_error(h);
+}
+
+int fdga_solve_mfrg(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int update_sigma,
+                    int krylov_maxiter, double krylov_rtol, double krylov_atol, int* iters, double* res,
+                    double* trace, int* krylov_total) {
+    if (!h) return FDGA_ERR_ARG;
+    int r = check_mfrg(h, strategy);
+    if (r) return r;
+    if (krylov_maxiter < 1 || !(krylov_rtol >= 0) || !(krylov_atol >= 0))
+        return fail(h, FDGA_ERR_ARG, "invalid Krylov parameters");
+    const size_t nv = 3 * h->nchan, nS = h->nGk;
+    int total = 0;
+    SolveHooks hk;
+    hk.before = [&]() -> int {  // keep x, iterate from its symmetrised copy (symmetrize_solver!)
+        CK(cudaMemcpyAsync(h->mf.u, h->xS, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        return symmetrize_state(h);
+    };
+    hk.after = [&]() -> int {  // y ← x + [M⁻¹ R_F ; R_Σ]
+        int nmaps = 0, it = 0;
+        double relres = 0.0;
+        int rr = mfrg_krylov(h, h->yS, h->mf.u, krylov_maxiter, krylov_rtol, krylov_atol, nmaps, it, relres);
+        if (rr) return rr;
+        total += it;
+        CK(launch_kc_axpy(h->st, NBLK_RED, h->mf.u, h->kr64[2], h->kc_code, 1.0, h->yS, nv));
+        if (!update_sigma)
+            CK(cudaMemcpyAsync(sigmaOf(h, h->yS), h->mf.u + nv, nS * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        CK(cudaMemcpyAsync(h->xS, h->mf.u, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+        return FDGA_OK;
+    };
+    r = solve_anderson(h, strategy, update_sigma != 0, maxiter, tol, beta, mem, iters, res, trace, &hk);
+    if (krylov_total) *krylov_total = total;
+    if (r) return r;
+    // unflatten!(S, res.zero); symmetrize_solver!(S): the last evaluated x
+    CK(cudaMemcpyAsync(h->xS, h->mf.u, h->nstate * sizeof(cplx), cudaMemcpyDeviceToDevice, h->st));
+    if ((r = symmetrize_state(h))) return r;
+    return check_device_error(h);
 }
 
 }  // extern "C"

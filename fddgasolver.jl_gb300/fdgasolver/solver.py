@@ -213,6 +213,46 @@ class _Solver:
         return {"converged": it.value > 0, "newton": n, "residual": res.value, "trace": trace[:n],
                 "evals_fp64": int(ev[0]), "evals_mixed": int(ev[1])}
 
+    def mfrg_apply(self, x, strategy="fdPA"):
+        """mfRGLinearMap(S, strategy) * x (src/mfRG.jl:20-89): x - Φ_mfRG(x·1e-2)/1e-2 on a vertex
+        vector of length(S.F) (the vertex part of flatten(S)); nonlocal solver."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.empty_like(x)
+        self._check(self._lib.fdga_mfrg_apply(self._h, STRATEGIES[strategy], x.ctypes.data, y.ctypes.data, x.size))
+        return y
+
+    def fixed_point_preconditioned(self, x, strategy="fdPA", update_sigma=False, krylov_maxiter=400,
+                                   krylov_rtol=1e-6, krylov_atol=1e-6):
+        """fixed_point_preconditioned!(R, x, S; strategy, update_Σ) (src/mfRG.jl:93-173): the residual
+        of one iteration with its vertex part solved against the mfRG map (GMRES on the device).
+        x is flatten(S) when update_sigma, else the vertex part flatten(S.F).  Returns
+        (R, info) with info = {"krylov_iterations", "krylov_residual"}."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        R = np.empty_like(x)
+        it = ctypes.c_int()
+        rel = ctypes.c_double()
+        self._check(self._lib.fdga_residual_mfrg(self._h, STRATEGIES[strategy], x.ctypes.data, R.ctypes.data, x.size,
+                                                 int(bool(update_sigma)), int(krylov_maxiter), float(krylov_rtol),
+                                                 float(krylov_atol), ctypes.byref(it), ctypes.byref(rel)))
+        return R, {"krylov_iterations": it.value, "krylov_residual": rel.value}
+
+    def solve_mfrg(self, strategy="fdPA", maxiter=40, tol=1e-4, delta=0.85, mem=50, update_sigma=False,
+                   krylov_maxiter=400, krylov_rtol=1e-6, krylov_atol=1e-6):
+        """solve_using_mfRG_without_mixing!(S; tol, strategy, update_Σ, maxiter, memory, mixing)
+        (src/mfRG.jl:686-776): nlsolve(anderson) over fixed_point_preconditioned!, on the device from the
+        current state; S ends at the last evaluated x, symmetrized."""
+        trace = np.zeros(maxiter, dtype=np.float64)
+        it = ctypes.c_int()
+        res = ctypes.c_double()
+        kt = ctypes.c_int()
+        self._check(self._lib.fdga_solve_mfrg(self._h, STRATEGIES[strategy], int(maxiter), float(tol), float(delta),
+                                              int(mem), int(bool(update_sigma)), int(krylov_maxiter),
+                                              float(krylov_rtol), float(krylov_atol), ctypes.byref(it),
+                                              ctypes.byref(res), trace.ctypes.data, ctypes.byref(kt)))
+        n = abs(it.value)
+        return {"converged": it.value > 0, "iterations": n, "residual": res.value, "trace": trace[:n],
+                "krylov_iterations": kt.value}
+
     def jvp(self, v, strategy="fdPA"):
         """dΦ/dx · v at the current state (flatten layout)."""
         v = np.ascontiguousarray(v, dtype=np.complex128)
@@ -403,6 +443,34 @@ def iterate_solver(S, strategy="fdPA", update_Sigma=True, compute_Hartree=True):
 
 def fixed_point(S, x, strategy="fdPA"):
     return S.fixed_point(x, strategy)
+
+
+class mfRGLinearMap:
+    """mfRGLinearMap(S, strategy) (src/mfRG.jl:20-32): a linear map on length(S.F) vectors;
+    A * x and A @ x apply it on the device."""
+
+    def __init__(self, S, strategy="fdPA"):
+        if strategy not in ("fdPA", "fdPA_new", "fdPA_1loop"):
+            raise ValueError(f"Invalid strategy {strategy}. Must be fdPA or fdPA_new or fdPA_1loop.")
+        self.S, self.strategy = S, strategy
+        n = S.state_len - 2 * S.nG * S.L * S.L  # length(S.F): flatten(S) without Σ
+        self.shape = (n, n)
+
+    def __mul__(self, x):
+        return self.S.mfrg_apply(x, self.strategy)
+
+    __matmul__ = __mul__
+
+
+def fixed_point_preconditioned(S, x, strategy="fdPA", update_sigma=False, krylov_maxiter=400):
+    """fixed_point_preconditioned!(R, x, S; strategy, update_Σ, krylov_maxiter) (src/mfRG.jl:93-173)."""
+    return S.fixed_point_preconditioned(x, strategy, update_sigma, krylov_maxiter)[0]
+
+
+def solve_using_mfRG_without_mixing(S, strategy="fdPA", tol=1e-4, update_sigma=False, maxiter=100, memory=50,
+                                    mixing=0.85, krylov_maxiter=400):
+    """solve_using_mfRG_without_mixing!(S; ...) (src/mfRG.jl:686-776) on the device."""
+    return S.solve_mfrg(strategy, maxiter, tol, mixing, memory, update_sigma, krylov_maxiter)
 
 
 def solve(S, strategy="fdPA", maxiter=100, tol=1e-4, delta=0.85, mem=8):

@@ -166,6 +166,39 @@ int fdga_solve_mixed(fdga_handle* h, int strategy, int maxiter, double tol, doub
 int fdga_solve_newton(fdga_handle* h, int strategy, int maxiter, double tol, int restart, int jvp_precision,
                       int* iters, double* res, double* trace, int* evals);
 
+/* mfRGLinearMap(S, strategy) * x (src/mfRG.jl:20-89), nonlocal solver: y = x - Φ_mfRG(x f)/f with
+ * f = 1e-2, where Φ_mfRG is the BSE sequence of the iteration on the vertex x f with the
+ * reference system's bubble Π0 in every BSE and F0 in the right factors (the is_mfRG branches;
+ * the caches of the two-argument build_K3_cache_mfRG!, src/nonlocal_2/build_K3_cache.jl:97-165).
+ * x and y are host arrays of length(S.F) = the vertex part of flatten(S).  Strategies :fdPA and
+ * :fdPA_1loop (the same map); :fdPA_new and the local solver return FDGA_ERR_UNSUPPORTED.  The
+ * map depends on F0, Π0 and x only; it overwrites the handle's caches and FL (the next iteration
+ * recomputes them) and leaves the state S unchanged. */
+int fdga_mfrg_apply(fdga_handle* h, int strategy, const double* x, double* y, size_t n);
+
+/* fixed_point_preconditioned!(R, x, S; strategy, update_Σ) (src/mfRG.jl:93-173): unflatten x
+ * (flatten(S) when update_sigma, else flatten(S.F) with Σ kept), symmetrize, iterate, then
+ * R_F = flatten(S.F) - x[1:length(S.F)] preconditioned by the mfRG map: R[1:length(S.F)] = z with
+ * M z = R_F solved by restarted GMRES(min(64, krylov_maxiter)) on the device, real arithmetic on
+ * the symmetry-class representatives, stopping at ‖M z - R_F‖ <= krylov_atol + krylov_rtol ‖R_F‖
+ * or after krylov_maxiter map applications (the reference: Krylov.dqgmres with atol = rtol = 1e-6,
+ * itmax = 400); R[length(S.F)+1:end] = flatten(S.Σ) - x_Σ when update_sigma.  *krylov_iters and
+ * *krylov_res (may be NULL) receive the GMRES iterations and its final relative residual
+ * estimate.  On return S holds Φ(x). */
+int fdga_residual_mfrg(fdga_handle* h, int strategy, const double* x, double* R, size_t n, int update_sigma,
+                       int krylov_maxiter, double krylov_rtol, double krylov_atol, int* krylov_iters,
+                       double* krylov_res);
+
+/* solve_using_mfRG_without_mixing!(S; tol, strategy, update_Σ, maxiter, memory, mixing,
+ * krylov_maxiter) (src/mfRG.jl:686-776): nlsolve(fixed_point_preconditioned!, x0; method = :anderson,
+ * beta = mixing, m = memory, ftol = tol) on the device: Anderson acceleration of
+ * the preconditioned residual, starting from the current state S.  Outputs as fdga_solve;
+ * *krylov_total (may be NULL) = GMRES iterations over the solve.  On return S holds the last
+ * evaluated x, symmetrized (unflatten!(S, res.zero); symmetrize_solver!(S), src/mfRG.jl:764-771). */
+int fdga_solve_mfrg(fdga_handle* h, int strategy, int maxiter, double tol, double beta, int mem, int update_sigma,
+                    int krylov_maxiter, double krylov_rtol, double krylov_atol, int* iters, double* res,
+                    double* trace, int* krylov_total);
+
 /* Jacobian-vector product of the iteration map at the current state S: Jv = dΦ/dx · v, central
  * differences with step 1e-5 (1 + ‖x‖₂) along v/‖v‖₂, in the handle's precision.  v and Jv are
  * host arrays in the flatten(S) layout; J is real-linear (v and i·v give unrelated products). */

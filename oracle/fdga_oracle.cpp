@@ -1092,6 +1092,182 @@ static void iterate(Solver& s, int strategy, bool update_sigma, bool incH) {
     }
 }
 
+// --------------------------------------------------------------------------------------------
+// mfRG linear map of the Krylov-preconditioned solver (nonlocal solver): src/mfRG.jl:20-89.  The
+// map calls the two-argument cache builder, whose method for the nonlocal solvers lives in
+// src/nonlocal_2/build_K3_cache.jl:97-165: the Γ caches are F(γr = false) - F.F0(γr = false)
+// (for a Vertex-valued F0 this keeps F0's own γr) and the right F caches come from F0 alone, each
+// evaluated on the class representatives of the K3 symmetry group.  The BSEs are the is_mfRG
+// branches of src/nonlocal/BSEa/BSEa_K1.jl:29-37, BSEa_K2.jl:70-77 and BSEa_K3.jl:83-97.
+// --------------------------------------------------------------------------------------------
+static cd f0_eval_flags(const AnyV& F0, int ch, int sp, int m, int n, int np, int P, Flags fl) {
+    if (F0.ref) return F0.ref->eval(ch, sp, m, n, np);  // RefVertex ignores the channel flags
+    return F0.vert->eval(ch, sp, m, n, np, P, fl);
+}
+
+static void build_K3_cache_mfrg(Solver& s) {
+    build_K3_cache(s);  // the left F0 caches (F0 alone, unchanged by the map)
+    const Shape& sh = s.shK3;
+    const Vert& F = s.F;
+    const AnyV& F0 = s.F0;
+    auto Pof = [&](const int* w) { return (s.Nq == 1) ? 0 : w[3]; };
+    Flags np_; np_.gp = false;
+    Flags na_; na_.ga = false;
+    Flags nt_; nt_.gt = false;
+    sg_eval(s.sgpp[2], sh, s.cache[C_GPX].data(), [&](const int* w) -> cd {
+        const int P = Pof(w);
+        return F.eval(CH_P, SP_X, w[0], w[1], w[2], P, np_) - f0_eval_flags(F0, CH_P, SP_X, w[0], w[1], w[2], P, np_);
+    });
+    sg_eval(s.sgpp[2], sh, s.cache[C_GPP].data(), [&](const int* w) -> cd {
+        const int P = Pof(w);
+        return F.eval(CH_P, SP_P, w[0], w[1], w[2], P, np_) - f0_eval_flags(F0, CH_P, SP_P, w[0], w[1], w[2], P, np_);
+    });
+    sg_eval(s.sgph[2], sh, s.cache[C_GA].data(), [&](const int* w) -> cd {
+        const int P = Pof(w);
+        return F.eval(CH_A, SP_P, w[0], w[1], w[2], P, na_) - f0_eval_flags(F0, CH_A, SP_P, w[0], w[1], w[2], P, na_);
+    });
+    sg_eval(s.sgph[2], sh, s.cache[C_GT].data(), [&](const int* w) -> cd {
+        const int P = Pof(w);
+        return F.eval(CH_T, SP_P, w[0], w[1], w[2], P, nt_) - f0_eval_flags(F0, CH_T, SP_P, w[0], w[1], w[2], P, nt_);
+    });
+    sg_eval(s.sgpp[2], sh, s.cache[C_FP].data(), [&](const int* w) -> cd {
+        const int P = Pof(w);
+        return any_eval(F0, CH_P, SP_P, w[0], w[1], w[2], P) - any_eval(F0, CH_P, SP_P, w[0], FINF, w[2], P);
+    });
+    sg_eval(s.sgph[2], sh, s.cache[C_FA].data(), [&](const int* w) -> cd {
+        const int P = Pof(w);
+        return any_eval(F0, CH_A, SP_P, w[0], w[1], w[2], P) - any_eval(F0, CH_A, SP_P, w[0], FINF, w[2], P);
+    });
+    sg_eval(s.sgph[2], sh, s.cache[C_FT].data(), [&](const int* w) -> cd {
+        const int P = Pof(w);
+        return any_eval(F0, CH_T, SP_P, w[0], w[1], w[2], P) - any_eval(F0, CH_T, SP_P, w[0], FINF, w[2], P);
+    });
+    const size_t n = sh.size();
+    for (size_t i = 0; i < n; ++i) {
+        s.cache[C_GT][i] = s.cache[C_GT][i] * 2.0 - s.cache[C_GA][i];
+        s.cache[C_FT][i] = s.cache[C_FT][i] * 2.0 - s.cache[C_FA][i];
+    }
+}
+
+// K1 = T s Σ_ω F0(Ω,∞,ω) Π0(Ω,ω) FL(Ω,ω̃,∞)
+static void bse_K1_mfrg(Solver& s, int ch) {
+    const int sp = spin_of(ch);
+    const double sgn = sign_of(ch), T = s.d.T;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[0] : s.sgph[0];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    sg_eval(G, s.shK1, out.K1.data(), [&](const int* w) -> cd {
+        const int m = w[0], P = (s.Nq == 1) ? 0 : w[1];
+        cd val = 0.0;
+        for (int n = -s.nPn; n < s.nPn; ++n) {
+            const int wt = cross(ch, m, n);
+            cd F0l = any_eval(s.F0, ch, sp, m, FINF, n, P);
+            cd FLr = s.FL.eval(ch, sp, m, wt, FINF, P);
+            val += F0l * Pi0[s.iPi(m, n, P)] * FLr;
+        }
+        return T * val * sgn;
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K1.size(); ++i) out.K1[i] = (out.K1[i] + s.Fbuff.g[CH_A].K1[i]) / 2.0;
+    }
+}
+
+// K2 = T s Σ_ω [F0(Ω,ν,ω̃) - F0(Ω,∞,ω̃)] Π0(Ω,ω) FL(Ω,ω,∞) + the FL.K2 epilogue
+static void bse_K2_mfrg(Solver& s, int ch) {
+    const int sp = spin_of(ch);
+    const double sgn = sign_of(ch), T = s.d.T;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[1] : s.sgph[1];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    sg_eval(G, s.shK2, out.K2.data(), [&](const int* w) -> cd {
+        const int m = w[0], nu = w[1], P = (s.Nq == 1) ? 0 : w[2];
+        cd val = 0.0;
+        for (int n = -s.nPn; n < s.nPn; ++n) {
+            const int wt = cross(ch, m, n);
+            cd F0l = any_eval(s.F0, ch, sp, m, nu, wt, P) - any_eval(s.F0, ch, sp, m, FINF, wt, P);
+            cd FLr = s.FL.eval(ch, sp, m, n, FINF, P);
+            val += F0l * Pi0[s.iPi(m, n, P)] * FLr;
+        }
+        return T * val * sgn;
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K2.size(); ++i) {
+            out.K2[i] += s.FL.g[CH_T].K2[i] * 2.0;
+            out.K2[i] += s.FL.g[CH_A].K2[i] * -1.0;
+        }
+        for (size_t i = 0; i < out.K2.size(); ++i) out.K2[i] = (out.K2[i] + s.Fbuff.g[CH_A].K2[i]) / 2.0;
+    } else {
+        for (size_t i = 0; i < out.K2.size(); ++i) out.K2[i] += s.FL.g[ch].K2[i];
+    }
+}
+
+// K3 = T Σ_ω cacheF(ν,ω) Π0(ω) [s1 Γ(ω,ν') + s2 γL(ω̃,ν') (ω̃ in the box)] + γL(ν,ν')
+static void bse_K3_mfrg(Solver& s, int ch) {
+    const double s1 = (ch == CH_A) ? 1.0 : -1.0, s2 = (ch == CH_T) ? -1.0 : 1.0, T = s.d.T;
+    Chan& out = s.Fbuff.g[ch];
+    const SymGroup& G = (ch == CH_P) ? s.sgpp[2] : s.sgph[2];
+    const std::vector<cd>& cG = s.cache[ch == CH_P ? C_GPX : (ch == CH_A ? C_GA : C_GT)];
+    const std::vector<cd>& cF = s.cache[ch == CH_P ? C_FP : (ch == CH_A ? C_FA : C_FT)];
+    const std::vector<cd>& Pi0 = (ch == CH_P) ? s.Pi0pp : s.Pi0ph;
+    const Chan& K = s.F.g[0];
+    const Chan& gL = s.FL.g[ch];
+    const Chan& gLt = s.FL.g[CH_T];
+    const Chan& gLa = s.FL.g[CH_A];
+    sg_eval(G, s.shK3, out.K3.data(), [&](const int* w) -> cd {
+        const int m = w[0], nu = w[1], nup = w[2], P = (s.Nq == 1) ? 0 : w[3];
+        cd val = 0.0;
+        for (int o = -K.n3n; o < K.n3n; ++o) {
+            cd pi0 = Pi0[s.iPi(m, o, P)];
+            cd Fs = cF[K.i3(m, nu, o, P)];
+            cd Gs = (ch == CH_P) ? cG[K.i3(m, o, nup, P)] : cG[K.i3(m, nup, o, P)];
+            val += Fs * pi0 * Gs * s1;
+            const int ot = cross(ch, m, o);
+            if (fin(ot, K.n3n)) {
+                if (ch == CH_T)
+                    val += Fs * pi0 * (2.0 * gLt.K3[K.i3(m, ot, nup, P)] - gLa.K3[K.i3(m, ot, nup, P)]) * s2;
+                else
+                    val += Fs * pi0 * gL.K3[K.i3(m, ot, nup, P)] * s2;
+            }
+        }
+        if (ch == CH_T) return T * val + 2.0 * gLt.K3[K.i3(m, nu, nup, P)] - gLa.K3[K.i3(m, nu, nup, P)];
+        return T * val + gL.K3[K.i3(m, nu, nup, P)];
+    });
+    if (ch == CH_T) {
+        for (size_t i = 0; i < out.K3.size(); ++i) out.K3[i] = (out.K3[i] + s.Fbuff.g[CH_A].K3[i]) / 2.0;
+    }
+}
+
+// y = x - Φ_mfRG(x f)/f with f = 1e-2 (vertex part of the state only; the map is linear in x)
+static void mfrg_apply(Solver& s, const cd* x, cd* y) {
+    const double factor = 1e-2;
+    size_t o = 0;
+    for (int c : {CH_P, CH_T, CH_A}) {
+        Chan& g = s.F.g[c];
+        for (auto& v : g.K1) v = x[o++] * factor;
+        for (auto& v : g.K2) v = x[o++] * factor;
+        for (auto& v : g.K3) v = x[o++] * factor;
+    }
+    s.F.update_avg();
+    build_K3_cache_mfrg(s);
+    bse_L_K2(s, CH_P); bse_L_K2(s, CH_A); bse_L_K2(s, CH_T);
+    bse_K1_mfrg(s, CH_P); bse_K1_mfrg(s, CH_A); bse_K1_mfrg(s, CH_T);
+    bse_K2_mfrg(s, CH_P); bse_K2_mfrg(s, CH_A); bse_K2_mfrg(s, CH_T);
+    bse_L_K3(s, CH_P); bse_L_K3(s, CH_A); bse_L_K3(s, CH_T);
+    bse_K3_mfrg(s, CH_P); bse_K3_mfrg(s, CH_A); bse_K3_mfrg(s, CH_T);
+    o = 0;
+    for (int c : {CH_P, CH_T, CH_A}) {
+        const Chan& g = s.Fbuff.g[c];
+        for (const auto& v : g.K1) { y[o] = x[o] - v / factor; ++o; }
+        for (const auto& v : g.K2) { y[o] = x[o] - v / factor; ++o; }
+        for (const auto& v : g.K3) { y[o] = x[o] - v / factor; ++o; }
+    }
+    for (int c = 0; c < 3; ++c) {  // set!(S.F, S.Fbuff)
+        s.F.g[c].K1 = s.Fbuff.g[c].K1;
+        s.F.g[c].K2 = s.Fbuff.g[c].K2;
+        s.F.g[c].K3 = s.Fbuff.g[c].K3;
+    }
+}
+
 static size_t state_len(const Solver& s) { return s.F.length() + s.Sig.size(); }
 
 static void flatten(const Solver& s, cd* x) {
@@ -1430,6 +1606,24 @@ void orc_flatten(void* h, double* x) { flatten(*(Solver*)h, (cd*)x); }
 void orc_unflatten(void* h, const double* x) { unflatten(*(Solver*)h, (const cd*)x); }
 void orc_iterate(void* h, int strategy, int update_sigma, int compute_hartree) {
     iterate(*(Solver*)h, strategy, update_sigma != 0, compute_hartree != 0);
+}
+// symmetrize_solver!(S) (src/ParquetSolver.jl:246-259): every class takes its representative's value
+void orc_symmetrize(void* h) {
+    Solver& s = *(Solver*)h;
+    sg_symmetrize(s.sgSig, s.Sig.data());
+    for (int c : {CH_A, CH_P, CH_T}) {
+        const SymGroup* G = (c == CH_P) ? s.sgpp : s.sgph;
+        sg_symmetrize(G[0], s.F.g[c].K1.data());
+        sg_symmetrize(G[1], s.F.g[c].K2.data());
+        sg_symmetrize(G[2], s.F.g[c].K3.data());
+    }
+}
+// mfRG linear map: y = x - Φ_mfRG(x f)/f on the vertex part (length F.length()); nonlocal solver only
+int orc_mfrg_apply(void* h, const double* x, double* y) {
+    Solver& s = *(Solver*)h;
+    if (s.d.local) return 1;
+    mfrg_apply(s, (const cd*)x, (cd*)y);
+    return 0;
 }
 void orc_dyson(void* h) { Solver& s = *(Solver*)h; dyson(s.G, s.Sig, s.Gbare); }
 void orc_bubbles(void* h) { Solver& s = *(Solver*)h; bubbles(s, s.Pipp, s.Piph, s.G); }

@@ -57,6 +57,9 @@ def lib():
         L.orc_group_info.restype = ctypes.c_long
         L.orc_group_info.argtypes = [vp, cp, ip, ip, ip, ctypes.c_long]
         L.orc_set_variant_single_hartree.argtypes = [vp, ctypes.c_int]
+        L.orc_symmetrize.argtypes = [vp]
+        L.orc_mfrg_apply.restype = ctypes.c_int
+        L.orc_mfrg_apply.argtypes = [vp, dp, dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
         _LIB = L
@@ -151,6 +154,54 @@ class OracleSolver:
         x = np.ascontiguousarray(x, dtype=np.complex128)
         assert x.size == lib().orc_state_len(self.h)
         lib().orc_unflatten(self.h, _dp(x.view(np.float64)))
+
+    def mfrg_apply(self, x):
+        """mfRGLinearMap(S) * x (src/mfRG.jl:36-89): the vertex part of the state; nonlocal solver."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.zeros_like(x)
+        if lib().orc_mfrg_apply(self.h, _dp(x.view(np.float64)), _dp(y.view(np.float64))) != 0:
+            raise ValueError("the mfRG linear map is defined for the nonlocal solver")
+        return y
+
+    def symmetrize(self):
+        """symmetrize_solver!(S) (src/ParquetSolver.jl:246-259)."""
+        lib().orc_symmetrize(self.h)
+
+    def fixed_point_preconditioned(self, x, strategy="fdPA", update_sigma=False, rtol=1e-12, maxiter=2000):
+        """fixed_point_preconditioned!(R, x, S; strategy, update_Σ) (src/mfRG.jl:93-173) with the Krylov
+        solve M z = R_F done to rtol by real GMRES (scipy) on the real-linear map: the map conjugates
+        under the symmetry operations, so it acts on (Re, Im) pairs.  Test-only restatement."""
+        import scipy.sparse.linalg as sla
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        full = self.flatten()
+        nS = full.size - self.vertex_len()
+        if update_sigma:
+            self.unflatten(x)
+        else:
+            full[: x.size] = x
+            self.unflatten(full)
+        self.symmetrize()
+        self.iterate(strategy, update_sigma=update_sigma)
+        y = self.flatten()
+        nF = y.size - nS
+        RF = y[:nF] - x[:nF]
+        RS = y[nF:] - x[nF:] if update_sigma else None
+        n = nF
+
+        def mv(v):
+            z = self.mfrg_apply(v[:n] + 1j * v[n:])
+            return np.concatenate([z.real, z.imag])
+
+        A = sla.LinearOperator((2 * n, 2 * n), matvec=mv, dtype=np.float64)
+        b = np.concatenate([RF.real, RF.imag])
+        sol, info = sla.gmres(A, b, rtol=rtol, atol=0.0, restart=200, maxiter=maxiter)
+        if info != 0:
+            raise RuntimeError(f"oracle GMRES did not converge (info={info})")
+        z = sol[:n] + 1j * sol[n:]
+        return np.concatenate([z, RS]) if update_sigma else z
+
+    def vertex_len(self):
+        return lib().orc_state_len(self.h) - self.length("Sigma")
 
     def iterate(self, strategy="fdPA", update_sigma=True, compute_hartree=True):
         lib().orc_iterate(self.h, STRATEGIES[strategy], int(update_sigma), int(compute_hartree))
