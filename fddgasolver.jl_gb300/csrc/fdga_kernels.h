@@ -324,6 +324,8 @@ cudaError_t launch_bse_K1_mfrg(cudaStream_t s, const VertP& F, const FLP& FL, co
 cudaError_t launch_bse_K2_mfrg(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const ChanWork& cw,
                                const Dims& d);
 cudaError_t launch_scale(cudaStream_t s, cplx* out, const cplx* in, double sc, size_t n);
+cudaError_t launch_cache_broadcast(cudaStream_t s, cplx* c0, cplx* c1, cplx* c2, const uint32_t* map, size_t n);
+cudaError_t launch_cache_broadcast(cudaStream_t s, cplxf* c0, cplxf* c1, cplxf* c2, const uint32_t* map, size_t n);
 // GMRES building blocks (real inner products on the FP32 Krylov basis)
 cudaError_t launch_kr_point(cudaStream_t s, int nblk, const cplx* x, const cplxf* v, double eps, cplx* xp, size_t n);
 cudaError_t launch_kr_apply(cudaStream_t s, int nblk, const cplx* y, const cplx* y0, const cplxf* v, double a,

@@ -10,7 +10,11 @@
 //     RefVertex F0, the RefVertex terms -F0p(Ω, ω, Ω-ν') - F0x(Ω, ω, ν') (zero for a RefVertex whose
 //     crossed component obeys crossing symmetry, as the bare U does);
 //   * the right "total vertex" caches come from F0 alone, F0(Ω, ν, ω) - F0(Ω, ∞, ω): constant over
-//     the applications of one map, so they are written by a separate launch (part 1) once per solve.
+//     the applications of one map, so they are written by a separate launch (part 1) once per solve;
+//   * all seven are evaluated through the K3 symmetry groups (SG(cache, InitFunction(diagram))): the
+//     representatives' values are broadcast to their classes.  F0(Ω, ν, ω) - F0(Ω, ∞, ω) is not
+//     invariant under ν <-> ω, so the broadcast changes it; the launch after each cache stage
+//     (launch_cache_broadcast) reproduces that.
 #include "fdga_kernels.h"
 
 namespace fdga {
@@ -163,6 +167,22 @@ unsigned warp_blocks(const ChanWork& cw) {
     return blocks_of((size_t)(mx > 0 ? mx : 1) * 32, 128);
 }
 
+// SymmetryGroup broadcast of up to three K3-shaped caches in place: c[i] = op_i(c[rep_i]).  A
+// representative's own operation is the identity, so it is never rewritten and the in-place update
+// has no read-after-write hazard.
+template <class S>
+__global__ void k_cache_broadcast(S* c0, S* c1, S* c2, const uint32_t* map, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t v = map[i];
+        const size_t r = v >> 2;
+        if (r == i) continue;
+        const int op = (int)(v & 3u);
+        c0[i] = apply_op(op, c0[r]);
+        if (c1) c1[i] = apply_op(op, c1[r]);
+        if (c2) c2[i] = apply_op(op, c2[r]);
+    }
+}
+
 template <class S>
 cudaError_t cache_mfrg_t(cudaStream_t s, const VertPT<S>& F, const Caches& C, const int* blocks, int nblocks,
                          const Dims& d, int part) {
@@ -183,6 +203,18 @@ cudaError_t launch_build_cache_mfrg(cudaStream_t s, const VertP& F, const Caches
 cudaError_t launch_build_cache_mfrg(cudaStream_t s, const VertPF& F, const Caches& C, const int* blocks, int nblocks,
                                     const Dims& d, int part) {
     return cache_mfrg_t(s, F, C, blocks, nblocks, d, part);
+}
+cudaError_t launch_cache_broadcast(cudaStream_t s, cplx* c0, cplx* c1, cplx* c2, const uint32_t* map, size_t n) {
+    const unsigned g = blocks_of(n, 256) < 8192u ? blocks_of(n, 256) : 8192u;
+    k_cache_broadcast<cplx><<<g, 256, 0, s>>>(c0, c1, c2, map, n);
+    MF_CHECK();
+    return cudaSuccess;
+}
+cudaError_t launch_cache_broadcast(cudaStream_t s, cplxf* c0, cplxf* c1, cplxf* c2, const uint32_t* map, size_t n) {
+    const unsigned g = blocks_of(n, 256) < 8192u ? blocks_of(n, 256) : 8192u;
+    k_cache_broadcast<cplxf><<<g, 256, 0, s>>>(c0, c1, c2, map, n);
+    MF_CHECK();
+    return cudaSuccess;
 }
 cudaError_t launch_bse_K1_mfrg(cudaStream_t s, const VertP& F, const FLP& FL, const BubbleP& B, const ChanWork& cw,
                                const Dims& d) {

@@ -2635,6 +2635,22 @@ int check_mfrg(fdga_handle* h, int strategy) {
     return FDGA_OK;
 }
 
+// SG(cache, InitFunction(diagram)) of the map's caches: the class broadcast through the K3 groups,
+// part 0 the Γ caches (Γpx, Γpp: pp group; Γa, Γt: ph group), part 1 Fp (pp), Fa, Ft (ph)
+int mfrg_broadcast(fdga_handle* h, cudaStream_t s, const Caches& C, int part, int& nl) {
+    const bool mixed = h->precision == FDGA_MIXED;
+    const int pp[2][2] = {{0, 4}, {7, -1}}, ph[2][2] = {{5, 6}, {8, 9}};
+    auto run = [&](const Group& g, const int* k) -> int {
+        if (g.trivial) return FDGA_OK;
+        if (mixed) LC(launch_cache_broadcast(s, C.f[k[0]], k[1] >= 0 ? C.f[k[1]] : nullptr, nullptr, g.d_map, h->n3));
+        else LC(launch_cache_broadcast(s, C.c[k[0]], k[1] >= 0 ? C.c[k[1]] : nullptr, nullptr, g.d_map, h->n3));
+        return FDGA_OK;
+    };
+    int r = run(h->gK3pp, pp[part]);
+    if (!r) r = run(h->gK3ph, ph[part]);
+    return r;
+}
+
 // the F0-only caches of the map (once per solve; the iteration overwrites the right ones)
 int mfrg_prepare(fdga_handle* h) {
     Caches C{};
@@ -2650,7 +2666,8 @@ int mfrg_prepare(fdga_handle* h) {
     } else {
         CK(launch_build_cache_mfrg(h->st, vertex_view(h, h->mf.x), C, h->d_k3blocks, h->nk3blocks, h->d, 1));
     }
-    return FDGA_OK;
+    int nl = 0;
+    return mfrg_broadcast(h, h->st, C, 1, nl);
 }
 
 // Φ_mfRG(mf.x) into mf.y.  Branch C: L_K2 → K1, K2 of the map; main: caches → L_K3 → K3.
@@ -2684,6 +2701,7 @@ int enqueue_mfrg(fdga_handle* h, int& nl) {
     }
     if (mixed) LC(launch_build_cache_mfrg(s, Ff, C, h->d_k3blocks, h->nk3blocks, d, 0));
     else LC(launch_build_cache_mfrg(s, F, C, h->d_k3blocks, h->nk3blocks, d, 0));
+    if (int r = mfrg_broadcast(h, s, C, 0, nl)) return r;
     BubbleP B{h->Pipp, h->Piph, h->Pi0pp, h->Pi0ph};
     auto Pi0 = [&](int ch) { return ch == CH_P ? h->Pi0pp : h->Pi0ph; };
     auto work = [&](int cls, cplx* raw) {
