@@ -179,6 +179,23 @@ constexpr int KR_MAX = 64;  // largest Krylov basis of the GMRES solves
 struct KrVecs {
     const cplxf* v[KR_MAX];
 };
+// Device-resident Arnoldi cycle (a GMRES restart cycle replayed as one graph with a WHILE node):
+// the loop counters, the stopping data and the Hessenberg matrix with its Givens rotations.
+struct KrDevState {
+    int j;         // column being built
+    int k;         // columns completed
+    int done;      // converged (|g_{j+1}| <= thr) or breakdown (H(j+1, j) = 0)
+    int nmaps;     // operator applications in this cycle
+    int budget;    // applications allowed in this cycle
+    int cost;      // applications per column
+    int m;         // restart length
+    int pad;
+    double thr;    // absolute stopping threshold on the residual estimate
+    double est;    // |g_{j+1}| after the last column
+    double hn;     // H(j+1, j) of the last column
+    double H[(KR_MAX + 1) * KR_MAX];  // column-major, leading dimension KR_MAX + 1
+    double cs[KR_MAX], sn[KR_MAX], g[KR_MAX + 1];
+};
 struct AAVecs32 {
     const cplxf* v[AA_MAX];
 };
@@ -354,6 +371,18 @@ cudaError_t launch_kc_codes(cudaStream_t s, const uint32_t* map, const int* item
 cudaError_t launch_kr_resid(cudaStream_t s, int nblk, const cplx* b, const cplxf* v, double alpha, const cplx* y,
                             const cplx* yb, double beta, cplx* r, size_t n);
 cudaError_t launch_kr_axpby(cudaStream_t s, int nblk, cplx* out, const cplx* a, double lam, const cplx* b, size_t n);
+// the Arnoldi column j = st->j of the device-resident cycle (fdga_krylov.cu): the operator input
+// V[j] expanded into xp (x + eps op(V[j])), its output gathered into w, the two classical
+// Gram-Schmidt passes (the second with |w|²), the Hessenberg/Givens update, V[j+1] and the advance
+// that sets the WHILE node's condition
+cudaError_t launch_kr_init(cudaStream_t s, KrDevState* st, int m, int budget, int cost, double thr, double beta);
+cudaError_t launch_kc_point_j(cudaStream_t s, int nblk, const cplx* x, const KrVecs& V, const KrDevState* st,
+                              const uint32_t* code, double eps, cplx* xp, size_t n);
+cudaError_t launch_kc_apply_j(cudaStream_t s, int nblk, const cplx* y, const uint32_t* pos, const KrVecs& V,
+                              const KrDevState* st, double a, double b, cplxf* w, size_t nc);
+cudaError_t launch_kr_cgs_j(cudaStream_t s, int nblk, const KrVecs& V, KrDevState* st, cplxf* w, const float* wgt,
+                            double* part, double* c1, double* c2, size_t n);
+cudaError_t launch_kr_advance(cudaStream_t s, KrDevState* st, cudaGraphConditionalHandle cond);
 cudaError_t launch_nonfinite(cudaStream_t s, const cplx* a, size_t n, unsigned int* count);
 // tangent (forward-mode derivative) stages of the iteration map; the value intermediates (G, G(R),
 // Π, L(R), C of the U² term) of the same base point are inputs

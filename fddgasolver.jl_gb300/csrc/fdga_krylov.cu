@@ -228,6 +228,130 @@ __global__ void __launch_bounds__(RT) k_kr_axpby(cplx* out, const cplx* a, doubl
     for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) out[i] = a[i] + b[i] * lam;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Device-resident Arnoldi column (the body of the WHILE node of a GMRES cycle).  j is read from
+// the cycle state by every kernel; the basis pointers are the fixed V[0..m].
+// ---------------------------------------------------------------------------------------------
+__global__ void k_kr_init(KrDevState* st, int m, int budget, int cost, double thr, double beta) {
+    if (threadIdx.x != 0) return;
+    st->j = 0; st->k = 0; st->done = 0; st->nmaps = 0;
+    st->budget = budget; st->cost = cost; st->m = m;
+    st->thr = thr; st->est = beta; st->hn = 0.0;
+    for (int i = 0; i <= KR_MAX; ++i) st->g[i] = 0.0;
+    st->g[0] = beta;
+}
+__global__ void __launch_bounds__(RT) k_kc_point_j(const cplx* x, KrVecs V, const KrDevState* st,
+                                                   const uint32_t* code, double eps, cplx* xp, size_t n) {
+    const cplxf* v = V.v[st->j];
+    for (size_t j = blockIdx.x * (size_t)RT + threadIdx.x; j < n; j += (size_t)gridDim.x * RT) {
+        const uint32_t c = code[j];
+        const cplx e = apply_op((int)(c & 3u), to_d(v[c >> 2])) * eps;
+        xp[j] = x ? x[j] + e : e;
+    }
+}
+__global__ void __launch_bounds__(RT) k_kc_apply_j(const cplx* y, const uint32_t* pos, KrVecs V, const KrDevState* st,
+                                                   double a, double b, cplxf* w, size_t nc) {
+    const cplxf* v = V.v[st->j];
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < nc; i += (size_t)gridDim.x * RT)
+        w[i] = tof(y[pos[i]] * b + to_d(v[i]) * a);
+}
+// partials of Re<V_i, w>, i <= j, for the chunk of blockIdx.y (blocks past j only add the norm)
+__global__ void __launch_bounds__(RT) k_kr_dots_j(KrVecs V, const KrDevState* st, const cplxf* w, const float* wgt,
+                                                  double* part, int np, int norm_slot, size_t n) {
+    __shared__ double sh[RT];
+    const int nv = st->j + 1;
+    const int i0 = blockIdx.y * CHUNK;
+    const int cnt = max(0, min(CHUNK, nv - i0));
+    const bool with_norm = norm_slot >= 0 && blockIdx.y == 0;
+    if (cnt == 0 && !with_norm) return;
+    RAcc a[CHUNK], an;
+    for (size_t i = blockIdx.x * (size_t)RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) {
+        cplxf wi = w[i];
+        const cplxf wraw = wi;
+        if (wgt) wi = wi * wgt[i];
+#pragma unroll
+        for (int j = 0; j < CHUNK; ++j)
+            if (j < cnt) a[j].add(rdot(V.v[i0 + j][i], wi));
+        if (with_norm) an.add(rdot(wraw, wi));
+    }
+    for (int j = 0; j < cnt; ++j) store_partial(a[j].total(), sh, part + (size_t)(i0 + j) * np);
+    if (with_norm) store_partial(an.total(), sh, part + (size_t)norm_slot * np);
+}
+// coef[i] = Σ part[i], i <= j; and coef[KR_MAX + 1] = Σ part[norm_slot] when norm_slot >= 0
+__global__ void __launch_bounds__(RT) k_kr_reduce_j(const double* part, int np, const KrDevState* st, int norm_slot,
+                                                    double* coef) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nrow = st->j + 1 + (norm_slot >= 0 ? 1 : 0);
+    for (int r = warp; r < nrow; r += RT / 32) {
+        const int i = r <= st->j ? r : norm_slot;
+        double s = 0.0;
+        for (int b = lane; b < np; b += 32) s += part[(size_t)i * np + b];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) coef[r <= st->j ? r : KR_MAX + 1] = s;
+    }
+}
+// w -= Σ_{i<=j} c_i V_i; with hn (second pass): V[j+1] = w / H(j+1, j)
+__global__ void __launch_bounds__(RT) k_kr_sub_j(KrVecs V, const KrDevState* st, const double* c, cplxf* w,
+                                                 int scale_out, size_t n) {
+    __shared__ float cs[KR_MAX];
+    const int nv = st->j + 1;
+    for (int i = threadIdx.x; i < nv; i += RT) cs[i] = (float)c[i];
+    __syncthreads();
+    const double hn = st->hn;
+    cplxf* out = scale_out ? const_cast<cplxf*>(V.v[nv]) : w;
+    const float inv = (scale_out && hn > 0.0) ? (float)(1.0 / hn) : 1.0f;
+    for (size_t t = blockIdx.x * (size_t)RT + threadIdx.x; t < n; t += (size_t)gridDim.x * RT) {
+        cplxf s = w[t];
+        for (int i = 0; i < nv; ++i) {
+            const cplxf v = V.v[i][t];
+            s.x -= cs[i] * v.x;
+            s.y -= cs[i] * v.y;
+        }
+        out[t] = s * inv;
+    }
+}
+// Hessenberg column j from the two passes (h_ij = c1_i + c2_i; H(j+1, j)² = |w1|² - Σ c2_i², the
+// norm after the second pass for the orthonormal basis), the previous rotations, the new one, and
+// the residual estimate |g_{j+1}|.  One thread.
+__global__ void k_kr_givens(KrDevState* st, const double* c1, const double* c2) {
+    if (threadIdx.x != 0) return;
+    const int j = st->j;
+    constexpr int LD = KR_MAX + 1;
+    double* Hj = st->H + (size_t)LD * j;
+    double q = 0.0;
+    for (int i = 0; i <= j; ++i) {
+        Hj[i] = c1[i] + c2[i];
+        q += c2[i] * c2[i];
+    }
+    const double hn = sqrt(fmax(0.0, c2[KR_MAX + 1] - q));
+    Hj[j + 1] = hn;
+    st->hn = hn;
+    for (int i = 0; i < j; ++i) {
+        const double a = Hj[i], b = Hj[i + 1];
+        Hj[i] = st->cs[i] * a + st->sn[i] * b;
+        Hj[i + 1] = -st->sn[i] * a + st->cs[i] * b;
+    }
+    const double a = Hj[j], b = Hj[j + 1], rho = hypot(a, b);
+    st->cs[j] = rho > 0 ? a / rho : 1.0;
+    st->sn[j] = rho > 0 ? b / rho : 0.0;
+    Hj[j] = rho;
+    Hj[j + 1] = 0.0;
+    st->g[j + 1] = -st->sn[j] * st->g[j];
+    st->g[j] = st->cs[j] * st->g[j];
+    st->est = fabs(st->g[j + 1]);
+    st->done = (st->est <= st->thr || hn == 0.0) ? 1 : 0;
+}
+// column j complete: advance, and continue the WHILE node while not done, j < m and the budget
+// allows one more application (j grows by one per pass, so the loop ends after at most m passes)
+__global__ void k_kr_advance(KrDevState* st, cudaGraphConditionalHandle cond) {
+    if (threadIdx.x != 0) return;
+    st->nmaps += st->cost;
+    st->k = st->j + 1;
+    st->j = st->j + 1;
+    const bool more = !st->done && st->j < st->m && st->nmaps + st->cost <= st->budget;
+    cudaGraphSetConditional(cond, more ? 1u : 0u);
+}
+
 }  // namespace
 
 #define KR_CHECK()                                   \
@@ -313,6 +437,39 @@ namespace fdga {
 cudaError_t launch_kr_resid(cudaStream_t s, int nblk, const cplx* b, const cplxf* v, double alpha, const cplx* y,
                             const cplx* yb, double beta, cplx* r, size_t n) {
     k_kr_resid<<<nblk, RT, 0, s>>>(b, v, alpha, y, yb, beta, r, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_init(cudaStream_t s, KrDevState* st, int m, int budget, int cost, double thr, double beta) {
+    if (m < 1 || m >= KR_MAX) return cudaErrorInvalidValue;
+    k_kr_init<<<1, 32, 0, s>>>(st, m, budget, cost, thr, beta);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_point_j(cudaStream_t s, int nblk, const cplx* x, const KrVecs& V, const KrDevState* st,
+                              const uint32_t* code, double eps, cplx* xp, size_t n) {
+    k_kc_point_j<<<nblk, RT, 0, s>>>(x, V, st, code, eps, xp, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kc_apply_j(cudaStream_t s, int nblk, const cplx* y, const uint32_t* pos, const KrVecs& V,
+                              const KrDevState* st, double a, double b, cplxf* w, size_t nc) {
+    k_kc_apply_j<<<nblk, RT, 0, s>>>(y, pos, V, st, a, b, w, nc);
+    KR_CHECK(); return cudaSuccess;
+}
+// both classical Gram-Schmidt passes of column j and its Hessenberg update (fixed grids: the
+// launches are captured once and replayed for every j <= m - 1 of the cycle)
+cudaError_t launch_kr_cgs_j(cudaStream_t s, int nblk, const KrVecs& V, KrDevState* st, cplxf* w, const float* wgt,
+                            double* part, double* c1, double* c2, size_t n) {
+    const int chunks = (KR_MAX + CHUNK - 1) / CHUNK;
+    k_kr_dots_j<<<dim3(nblk, chunks), RT, 0, s>>>(V, st, w, wgt, part, nblk, -1, n);
+    k_kr_reduce_j<<<1, RT, 0, s>>>(part, nblk, st, -1, c1);
+    k_kr_sub_j<<<nblk, RT, 0, s>>>(V, st, c1, w, 0, n);
+    k_kr_dots_j<<<dim3(nblk, chunks), RT, 0, s>>>(V, st, w, wgt, part, nblk, KR_MAX + 1, n);
+    k_kr_reduce_j<<<1, RT, 0, s>>>(part, nblk, st, KR_MAX + 1, c2);
+    k_kr_givens<<<1, 32, 0, s>>>(st, c1, c2);
+    k_kr_sub_j<<<nblk, RT, 0, s>>>(V, st, c2, w, 1, n);
+    KR_CHECK(); return cudaSuccess;
+}
+cudaError_t launch_kr_advance(cudaStream_t s, KrDevState* st, cudaGraphConditionalHandle cond) {
+    k_kr_advance<<<1, 32, 0, s>>>(st, cond);
     KR_CHECK(); return cudaSuccess;
 }
 cudaError_t launch_kr_axpby(cudaStream_t s, int nblk, cplx* out, const cplx* a, double lam, const cplx* b, size_t n) {

@@ -128,6 +128,12 @@ struct fdga_handle {
     cplx* kr_x = nullptr;          // full FP64 Newton iterate / fixed point
     std::vector<cplx*> jv;         // fdga_jvp work vectors (full FP64)
     double *kr_part = nullptr, *kr_coef = nullptr;
+    // device-resident GMRES cycles: the cycle state (device, and a page-locked host copy read once per
+    // cycle) and one instantiated WHILE-node graph per (operator, restart length)
+    KrDevState* kr_st = nullptr;
+    KrDevState* kr_st_host = nullptr;
+    std::map<std::pair<int, int>, Graph> kr_graphs;
+    int kr_device_loop = 1;  // option "gmres_device_loop"
     uint32_t *kc_code = nullptr, *kc_pos = nullptr;  // compact index of the state (symmetry classes)
     float* kc_w = nullptr;                           // class sizes
     size_t nc = 0;
@@ -1472,6 +1478,9 @@ void drop_graphs(fdga_handle* h) {
     drop_graph_array(h->tan.graphs);
     for (auto& g : h->mf.graphs)
         if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    for (auto& kv : h->kr_graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    h->kr_graphs.clear();
     if (h->rg.g.exec) cudaGraphExecDestroy(h->rg.g.exec);
     h->rg.g = Graph();
     h->rg.x = nullptr;
@@ -1763,6 +1772,7 @@ void fdga_destroy(fdga_handle* h) {
     if (h->st) cudaStreamSynchronize(h->st);
     drop_graphs(h);
     if (h->flush_buf) cudaFree(h->flush_buf);
+    if (h->kr_st_host) cudaFreeHost(h->kr_st_host);
     for (void* p : h->allocs) cudaFree(p);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : {h->evfork, h->evA, h->evB, h->evC, h->evD, h->evE, h->evR}) if (e) cudaEventDestroy(e);
@@ -2384,6 +2394,9 @@ int ensure_krylov(fdga_handle* h, int m) {
     if (h->kr_nc != nc) {  // compact length changed (symmetry groups set): drop the compact buffers
         h->kr64.clear();
         h->kr32.clear();
+        for (auto& kv : h->kr_graphs)  // (their captured basis pointers)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        h->kr_graphs.clear();
         h->kr_nc = nc;
     }
     while (h->kr64.size() < 6) {
@@ -2401,6 +2414,10 @@ int ensure_krylov(fdga_handle* h, int m) {
         r = dalloc(h, &h->kr_part, (size_t)(KR_MAX + 2) * NBLK_RED);
         if (!r) r = dalloc(h, &h->kr_coef, 4 * (size_t)(KR_MAX + 2));
         if (r) return r;
+    }
+    if (!h->kr_st) {
+        AL(h->kr_st, 1);
+        CK(cudaHostAlloc((void**)&h->kr_st_host, sizeof(KrDevState), cudaHostAllocDefault));
     }
     return FDGA_OK;
 }
@@ -2485,7 +2502,49 @@ int mixed_tangent_base_from_fp64(fdga_handle* h) {
 struct KrylovOp {
     std::function<int(const cplxf* v, cplxf* w)> apply;
     int cost = 1;
+    // capture-safe form for the device-resident cycle: enqueue w = A V[st->j] on h->st; key names the
+    // operator for the cycle-graph cache (-1: host-driven Arnoldi only)
+    std::function<int(const KrVecs& V, const KrDevState* st, cplxf* w)> enqueue_j;
+    int key = -1;
 };
+
+// The Arnoldi loop of one GMRES cycle as one graph: a WHILE node whose body is the column j = st->j
+// (operator, two Gram-Schmidt passes, Hessenberg/Givens update, V[j+1]) and the advance kernel that
+// sets its condition.  j grows by one per pass and the condition requires j < m, so the loop ends
+// after at most m passes.  Built once per (operator, m) and replayed every cycle.
+int kr_cycle_graph(fdga_handle* h, const KrylovOp& op, const KrVecs& V, cplxf* w, int m, Graph*& out) {
+    Graph& slot = h->kr_graphs[std::make_pair(op.key, m)];
+    out = &slot;
+    if (slot.exec) return FDGA_OK;
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    struct Del { cudaGraph_t g; ~Del() { if (g) cudaGraphDestroy(g); } } del{g};
+    cudaGraphConditionalHandle cond;
+    CK(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = cond;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int r = op.enqueue_j(V, h->kr_st, w);
+    cudaError_t e = cudaSuccess;
+    if (!r)
+        e = launch_kr_cgs_j(h->st, NBLK_RED, V, h->kr_st, w, h->kc_w, h->kr_part, h->kr_coef,
+                            h->kr_coef + (KR_MAX + 2), h->nc);
+    if (!r && e == cudaSuccess) e = launch_kr_advance(h->st, h->kr_st, cond);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(h->st, &captured);
+    if (r) return r;
+    if (e != cudaSuccess) return cuda_fail(h, e, "GMRES cycle capture");
+    if (ee != cudaSuccess) return cuda_fail(h, ee, "cudaStreamEndCapture (GMRES cycle)");
+    e = cudaGraphInstantiate(&slot.exec, g, 0);
+    if (e != cudaSuccess) { slot.exec = nullptr; return cuda_fail(h, e, "cudaGraphInstantiate (GMRES cycle)"); }
+    return FDGA_OK;
+}
 
 // Restarted GMRES(m) for A dx = b (compact vectors), dx starting at 0.  Cycles after the first
 // restart from the true residual b − A dx.  Stops at ‖b − A dx‖ <= atol + rtol ‖b‖ (estimate);
@@ -2537,7 +2596,26 @@ int gmres_core(fdga_handle* h, const KrylovOp& op, const cplx* b, cplx* dx, int 
         g[0] = beta;
         int k = 0;
         double est = beta;
-        for (int j = 0; j < m; ++j) {
+        const bool dev = op.enqueue_j && op.key >= 0 && h->kr_device_loop;
+        if (dev) {
+            // device-resident Arnoldi: one graph launch and one state read per cycle
+            if (nmaps + op.cost > max_maps) break;
+            Graph* cg = nullptr;
+            if ((r = kr_cycle_graph(h, op, V, w, m, cg))) return r;
+            CK(launch_kr_init(h->st, h->kr_st, m, max_maps - nmaps, op.cost, thr, beta));
+            CK(cudaGraphLaunch(cg->exec, h->st));
+            CK(cudaMemcpyAsync(h->kr_st_host, h->kr_st, sizeof(KrDevState), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
+            const KrDevState& S = *h->kr_st_host;
+            k = S.k;
+            iters += k;
+            nmaps += S.nmaps;
+            est = S.est;
+            for (int jj = 0; jj < k; ++jj)
+                for (int i = 0; i <= jj; ++i) Hij(i, jj) = S.H[(size_t)i + (size_t)(KR_MAX + 1) * jj];
+            for (int i = 0; i <= k; ++i) g[i] = S.g[i];
+        }
+        for (int j = 0; j < m && !dev; ++j) {
             if (nmaps + op.cost > max_maps) break;
             if ((r = op.apply(V.v[j], w))) return r;
             // classical Gram-Schmidt, twice (weighted inner products)
@@ -2602,6 +2680,18 @@ int gmres_solve(fdga_handle* h, int strategy, const cplx* xb, const cplx* yb, co
     KrylovOp op;
     op.cost = central && !use_tangent(h, strategy) ? 2 : 1;
     op.apply = [&](const cplxf* v, cplxf* w) { return apply_A(h, strategy, xb, yb, v, eps, central, w, nmaps); };
+    if (use_tangent(h, strategy)) {  // v − J v by the tangent kernels: capturable into the cycle graph
+        if ((r = ensure_tangent(h))) return r;
+        op.key = 10 * h->precision + strategy;
+        op.enqueue_j = [h, strategy](const KrVecs& V, const KrDevState* st, cplxf* w) -> int {
+            CK(launch_kc_point_j(h->st, NBLK_RED, nullptr, V, st, h->kc_code, 1.0, h->tan.x, h->nstate));
+            int nl = 0;
+            int rr = enqueue_tangent(h, strategy, true, true, nl);
+            if (rr) return rr;
+            CK(launch_kc_apply_j(h->st, NBLK_RED, h->tan.y, h->kc_pos, V, st, 1.0, -1.0, w, h->nc));
+            return FDGA_OK;
+        };
+    }
     return gmres_core(h, op, b, dx, m, cycles, rtol, 0.0, max_maps, nmaps, iters, relres);
 }
 
@@ -2848,6 +2938,15 @@ KrylovOp mfrg_operator(fdga_handle* h, int& nmaps) {
         if (r) return r;
         ++nmaps;
         CK(launch_kc_apply(h->st, NBLK_RED, h->mf.y, nullptr, h->kc_pos, v, 1.0, -1.0 / kMfrgFactor, w, h->nc));
+        return FDGA_OK;
+    };
+    op.key = 100 + h->precision;
+    op.enqueue_j = [h](const KrVecs& V, const KrDevState* st, cplxf* w) -> int {
+        CK(launch_kc_point_j(h->st, NBLK_RED, nullptr, V, st, h->kc_code, kMfrgFactor, h->mf.x, 3 * h->nchan));
+        int nl = 0;
+        int rr = enqueue_mfrg(h, nl);
+        if (rr) return rr;
+        CK(launch_kc_apply_j(h->st, NBLK_RED, h->mf.y, h->kc_pos, V, st, 1.0, -1.0 / kMfrgFactor, w, h->nc));
         return FDGA_OK;
     };
     return op;
@@ -3251,6 +3350,10 @@ int fdga_set_precision(fdga_handle* h, int precision) {
 }
 
 int fdga_set_option(fdga_handle* h, const char* key, int value) {
+    if (h && key && std::string(key) == "gmres_device_loop") {
+        h->kr_device_loop = value ? 1 : 0;
+        return FDGA_OK;
+    }
     if (!h || !key) return FDGA_ERR_ARG;
     const std::string k(key);
     if (k == "k3_tensor_cores") {
