@@ -18,7 +18,7 @@ namespace {
 constexpr int RT = 256;
 constexpr int FLUSH = 64;  // FP32 products summed per FP64 accumulation
 
-__device__ __forceinline__ cplxf tof(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+__device__ __forceinline__ cplxf tof(cplx v) { return to_f32(v); }
 __device__ __forceinline__ cplxf conjf_(cplxf a) { return cplxf{a.x, -a.y}; }
 
 __device__ __forceinline__ cplx block_reduce_parts(const cplx* part, int np, cplx* sh) {

@@ -69,11 +69,31 @@ __device__ __forceinline__ cplxf cfma(cplxf a, cplxf b, cplxf c) {
 // conversions between the storage type and the arithmetic type C of a templated kernel
 template <class C> __device__ __forceinline__ C to_c(cplx v);
 template <> __device__ __forceinline__ cplx to_c<cplx>(cplx v) { return v; }
-template <> __device__ __forceinline__ cplxf to_c<cplxf>(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+// FP64 -> FP32 with IEEE 754 round-to-nearest-even, done on the integer pipes: GB300 issues the
+// F2F conversion on its FP64 pipe (1/64 rate), where it costs as much as the FP64 arithmetic the
+// mixed map removes.  The 52-bit significand is rounded to 23 bits on the 29 dropped bits (ties
+// to even); a carry out of the significand steps the exponent, up to infinity.  FP64 zeros and
+// subnormals give a signed zero (exact: they lie below half the smallest FP32 subnormal); results
+// that would be FP32 subnormal, and infinities and NaNs, take the hardware conversion (same value).
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int hi = (unsigned int)(b >> 32);
+    const unsigned int sign = hi & 0x80000000u;
+    const int ef = (int)((hi >> 20) & 0x7ffu);
+    if (ef == 0) return __uint_as_float(sign);
+    const int e = ef - 1023 + 127;
+    if (e <= 0 || e >= 255) return __double2float_rn(x);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    unsigned int r = (unsigned int)(m >> 29);
+    const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull);
+    if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) r += 1u;
+    return __uint_as_float((sign | ((unsigned int)e << 23)) + r);
+}
+template <> __device__ __forceinline__ cplxf to_c<cplxf>(cplx v) { return cplxf{d2f_rn(v.x), d2f_rn(v.y)}; }
 template <class C> __device__ __forceinline__ C to_c(cplxf v) { return C{v.x, v.y}; }
 __device__ __forceinline__ cplx to_d(cplx v) { return v; }
 __device__ __forceinline__ cplx to_d(cplxf v) { return cplx{(double)v.x, (double)v.y}; }
-__device__ __forceinline__ cplxf to_f32(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+__device__ __forceinline__ cplxf to_f32(cplx v) { return cplxf{d2f_rn(v.x), d2f_rn(v.y)}; }
 __device__ __forceinline__ cplxf to_f32(cplxf v) { return v; }
 template <class C> __device__ __forceinline__ C czero() { return C{0, 0}; }
 

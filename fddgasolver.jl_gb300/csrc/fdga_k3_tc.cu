@@ -121,9 +121,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const size_t ip = ixPi(d, P, m, tid - d.n3n);
         const cplx p0 = a.Pi0 ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
-        v[2] = (float)p0.x; v[3] = (float)p0.y;
-        if (MODE >= 1) { const cplx p = ldg(a.Pi + ip); v[0] = (float)p.x; v[1] = (float)p.y; }
-        if (MODE == 2) { const cplx p = ldg(a.tPi + ip); v[4] = (float)p.x; v[5] = (float)p.y; }
+        v[2] = d2f_rn(p0.x); v[3] = d2f_rn(p0.y);
+        if (MODE >= 1) { const cplx p = ldg(a.Pi + ip); v[0] = d2f_rn(p.x); v[1] = d2f_rn(p.y); }
+        if (MODE == 2) { const cplx p = ldg(a.tPi + ip); v[4] = d2f_rn(p.x); v[5] = d2f_rn(p.y); }
         for (int j = 0; j < 6; ++j) pis[tid][j] = v[j];
     }
     if (tid == 0) {

@@ -2027,6 +2027,44 @@ cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const c
     k_chi<<<blocks_for(n, 256), 256, 0, s>>>(K1p, K1t, K1a, which, 1.0 / (U * U), NO, Nq, local, out);
     LAUNCH_CHECK(); return cudaSuccess;
 }
+// Self-check of d2f_rn against the hardware conversion: n inputs from a hash of the index --
+// random bit patterns over all exponents, exact ties (the 29 dropped bits 1000...0) of both
+// parities, values just below and above a tie, and the zero/subnormal/overflow/infinity/NaN edges.
+__global__ void k_selftest_d2f(unsigned long long seed, size_t n, unsigned int* mismatches) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        unsigned long long z = (i + 1) * 0x9E3779B97F4A7C15ull + seed;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        unsigned long long b = z;
+        switch (i % 8) {
+            case 1: b = (z & ~0x1FFFFFFFull) | 0x10000000ull; break;          // tie
+            case 2: b = (z & ~0x1FFFFFFFull) | 0x0FFFFFFFull; break;          // just below a tie
+            case 3: b = (z & ~0x1FFFFFFFull) | 0x10000001ull; break;          // just above a tie
+            case 4: b = (z & 0x800FFFFFFFFFFFFFull) | ((unsigned long long)(870 + (z >> 52) % 291) << 52); break;  // FP32 range edges
+            case 5: b = (z & 0x800FFFFFFFFFFFFFull) | (((z >> 40) % 3 == 0 ? 0x7ffull : (z >> 40) % 3 == 1 ? 0ull : 0x47full) << 52); break;
+            default: break;
+        }
+        const double x = __longlong_as_double((long long)b);
+        const unsigned int a = __float_as_uint(d2f_rn(x)), h = __float_as_uint(__double2float_rn(x));
+        const bool both_nan = isnan(x);
+        if (a != h && !both_nan) atomicAdd(mismatches, 1u);
+    }
+}
+cudaError_t selftest_d2f(size_t n, unsigned int* mismatches_host) {
+    unsigned int* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(unsigned int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(d, 0, sizeof(unsigned int));
+    if (e == cudaSuccess) {
+        k_selftest_d2f<<<1024, 256>>>(0x5DEECE66Dull, n, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches_host, d, sizeof(unsigned int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e;
+}
+
 cudaError_t measure_fp64_rate(float* ms, double* gflops) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -330,6 +330,8 @@ cudaError_t launch_ma_qrot(cudaStream_t s, int nblk, const AAVecs32W& Q, int m, 
 cudaError_t launch_chi(cudaStream_t s, const cplx* K1p, const cplx* K1t, const cplx* K1a, int which, double U,
                        int NO, int Nq, int local, cplx* out);
 cudaError_t measure_fp64_rate(float* ms, double* gflops);
+// number of mismatches between d2f_rn and the hardware FP64 -> FP32 conversion over n hashed inputs
+cudaError_t selftest_d2f(size_t n, unsigned int* mismatches_host);
 // mfRG linear map (fdga_mfrg.cu): part 0 the irreducible caches of the state vertex, part 1 the
 // F0-only caches; the K1/K2 BSEs of the map (FP64, F0 and FL.K2 only)
 cudaError_t launch_build_cache_mfrg(cudaStream_t s, const VertP& F, const Caches& C, const int* blocks, int nblocks,

@@ -20,7 +20,7 @@ constexpr int RT = 256;
 constexpr int FLUSH = 64;
 constexpr int CHUNK = 8;
 
-__device__ __forceinline__ cplxf tof(cplx v) { return cplxf{(float)v.x, (float)v.y}; }
+__device__ __forceinline__ cplxf tof(cplx v) { return to_f32(v); }
 
 struct RAcc {  // real accumulator: FP32 runs flushed into FP64
     float s32 = 0.f;

@@ -163,6 +163,7 @@ struct fdga_handle {
         cplx *SigInb = nullptr, *SU2b = nullptr, *SigRb = nullptr, *u2Rb = nullptr, *u2Cb = nullptr;
         cplx *LRb = nullptr, *Lb = nullptr;
         double* nbar = nullptr;
+        Graph graphs[2][2][2];  // [strategy][update_sigma][hartree] (FP64)
     } adj;
     // mfRG linear map (src/mfRG.jl:20-89): its scaled input vertex x·factor, its output Φ_mfRG and a
     // work vector (state layout; the Σ parts stay zero), one captured graph per precision
@@ -1423,6 +1424,28 @@ int enqueue_adjoint(fdga_handle* h, int strategy, bool update_sigma, bool hartre
     return FDGA_OK;
 }
 
+// the adjoint map as one CUDA graph per (strategy, flags), replayed at the base point the last FP64
+// map left in the handle, on the cotangent in adj.yb
+int run_adjoint(fdga_handle* h, int strategy, bool update_sigma, bool hartree) {
+    Graph& g = h->adj.graphs[strategy][update_sigma][hartree];
+    if (!g.exec) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        int r = enqueue_adjoint(h, strategy, update_sigma, hartree);
+        cudaError_t ee = cudaStreamEndCapture(h->st, &graph);
+        if (r) {
+            if (ee == cudaSuccess) cudaGraphDestroy(graph);
+            return r;
+        }
+        if (ee != cudaSuccess) return cuda_fail(h, ee, "cudaStreamEndCapture (adjoint)");
+        ee = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ee != cudaSuccess) { g.exec = nullptr; return cuda_fail(h, ee, "cudaGraphInstantiate (adjoint)"); }
+    }
+    CK(cudaGraphLaunch(g.exec, h->st));
+    return FDGA_OK;
+}
+
 // Strategies of iterate_solver! (src/solve.jl:10): the _new forms exist for the local solver
 // (src/BSEa/BSEa_K1.jl:57, BSEa_K2.jl:108), the one-loop form for the nonlocal one
 // (src/nonlocal/BSEa/BSE_1loop.jl); elsewhere the reference has no method for them.
@@ -1476,6 +1499,10 @@ void drop_graph_array(A& gs) {
 void drop_graphs(fdga_handle* h) {
     drop_graph_array(h->graphs);
     drop_graph_array(h->tan.graphs);
+    for (auto& a : h->adj.graphs)
+        for (auto& b : a)
+            for (auto& g : b)
+                if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
     for (auto& g : h->mf.graphs)
         if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
     for (auto& kv : h->kr_graphs)
@@ -3076,7 +3103,7 @@ int fdga_rrule(fdga_handle* h, int strategy, int update_sigma, int compute_hartr
     if (r) return r;
     CK(cudaMemcpyAsync(h->tmpS, ybar, n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
     CK(launch_scatter(h->st, h->adj.yb, h->tmpS, h->perm, n));  // reference layout -> device layout
-    if ((r = enqueue_adjoint(h, strategy, update_sigma != 0, compute_hartree != 0))) return r;
+    if ((r = run_adjoint(h, strategy, update_sigma != 0, compute_hartree != 0))) return r;
     CK(launch_gather(h->st, h->tmpS, h->adj.xb, h->perm, n));
     CK(cudaMemcpyAsync(xbar, h->tmpS, n * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -3511,6 +3538,20 @@ int fdga_tangent_repeat(fdga_handle* h, int strategy, int n) {
     return FDGA_OK;
 }
 
+// benchmark helper: replay the adjoint graph n times at the base point and cotangent of the last
+// fdga_rrule (no host sync)
+int fdga_adjoint_repeat(fdga_handle* h, int strategy, int n) {
+    if (!h || n < 0) return FDGA_ERR_ARG;
+    if (strategy != FDGA_FDPA && strategy != FDGA_SCPA)
+        return fail(h, FDGA_ERR_UNSUPPORTED, "the adjoint map covers the fdPA and scPA strategies");
+    if (!h->adj.graphs[strategy][1][1].exec) return fail(h, FDGA_ERR_STATE, "fdga_rrule has not been called");
+    for (int i = 0; i < n; ++i) {
+        int r = run_adjoint(h, strategy, true, true);
+        if (r) return r;
+    }
+    return FDGA_OK;
+}
+
 int fdga_host_alloc(size_t bytes, void** p) {
     if (!p) return FDGA_ERR_ARG;
     cudaError_t e = cudaHostAlloc(p, bytes ? bytes : 1, cudaHostAllocDefault);
@@ -3542,6 +3583,13 @@ int fdga_query(fdga_handle* h, const char* key, double* value) {
         float ms = 0.f;
         const cudaError_t e = measure_fp64_rate(&ms, value);
         if (e != cudaSuccess) return cuda_fail(h, e, "fp64 calibration");
+        return FDGA_OK;
+    }
+    if (k == "selftest_d2f") {  // mismatches of the integer-path FP64 -> FP32 rounding over 2^26 inputs
+        unsigned int mm = 0;
+        const cudaError_t e = selftest_d2f((size_t)1 << 26, &mm);
+        if (e != cudaSuccess) return cuda_fail(h, e, "d2f self-check");
+        *value = mm;
         return FDGA_OK;
     }
     if (!h) return FDGA_ERR_ARG;

@@ -92,6 +92,7 @@ EXPORTS = {
                                         ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "fdga_map_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "fdga_tangent_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "fdga_adjoint_repeat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "fdga_flush_l2": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t]),
     "fdga_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "fdga_host_free": (ctypes.c_int, [ctypes.c_void_p]),

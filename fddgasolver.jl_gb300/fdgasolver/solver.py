@@ -364,6 +364,10 @@ class _Solver:
         """Apply the iteration map n times to the unchanged device state (no host sync)."""
         self._check(self._lib.fdga_map_repeat(self._h, STRATEGIES[strategy], int(n)))
 
+    def adjoint_repeat(self, n, strategy="fdPA"):
+        """Replay the adjoint map n times at the base point and cotangent of the last rrule call."""
+        self._check(self._lib.fdga_adjoint_repeat(self._h, STRATEGIES[strategy], int(n)))
+
     def tangent_repeat(self, n, strategy="fdPA"):
         """Apply the tangent map n times at the base point and direction of the last frule call."""
         self._check(self._lib.fdga_tangent_repeat(self._h, STRATEGIES[strategy], int(n)))
@@ -439,6 +443,17 @@ def init_sym_grp(S):
 
 def iterate_solver(S, strategy="fdPA", update_Sigma=True, compute_Hartree=True):
     S.iterate_solver(strategy, update_Sigma, compute_Hartree)
+
+
+def _lib_query(key):
+    """fdga_query without a handle (device-level keys: fp64_gflops, selftest_d2f)."""
+    from ._lib import load
+    lib = load()
+    v = ctypes.c_double()
+    rc = lib.fdga_query(None, key.encode(), ctypes.byref(v))
+    if rc != 0:
+        raise RuntimeError(f"fdga_query({key}) failed with status {rc}")
+    return v.value
 
 
 def fixed_point(S, x, strategy="fdPA"):

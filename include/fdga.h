@@ -311,6 +311,9 @@ int fdga_map_repeat(fdga_handle* h, int strategy, int n);
 /* Applies the tangent map n times (graph replays, no host synchronisation) at the base point and
  * direction of the last fdga_frule call (full map): the timing loop of the derivative. */
 int fdga_tangent_repeat(fdga_handle* h, int strategy, int n);
+/* Benchmark helper: replays the adjoint map's graph n times at the base point and cotangent of the
+ * last fdga_rrule (update_sigma = compute_hartree = 1), without a host sync. */
+int fdga_adjoint_repeat(fdga_handle* h, int strategy, int n);
 /* Writes `bytes` of a device buffer on the handle's stream, evicting the L2 between timed
  * iterations of a benchmark (the buffer is allocated on first use). */
 int fdga_flush_l2(fdga_handle* h, size_t bytes);

@@ -78,3 +78,11 @@ def test_tensor_core_k3_tangent(cfg):
     assert blockwise_rel_err(cfg, j_tma, j64) < 2e-5
     assert blockwise_rel_err(cfg, j_tma, j_tc) < 1e-6
     gpu.close()
+
+
+def test_fp64_to_fp32_rounding_matches_hardware():
+    """The integer-path FP64 -> FP32 rounding used by every narrowing of the mixed map (d2f_rn)
+    gives the hardware conversion's bits on 2^26 hashed inputs (ties of both parities, values next
+    to ties, the FP32 range edges, zeros, subnormals, infinities, NaNs)."""
+    from fdgasolver.solver import _lib_query
+    assert _lib_query("selftest_d2f") == 0
