@@ -104,6 +104,28 @@ __device__ __forceinline__ S apply_op(int op, S v) {
     if (op & 1) { v.x = -v.x; v.y = -v.y; }
     return v;
 }
+// Exact FP64 sign flips and power-of-two scalings on the integer pipes (GB300's FP64 pipe is the
+// bound of the class expansions): -x flips the sign bit; x/2 and 2x step the exponent field when x
+// and the result are normal, and take the FP64 multiply otherwise (same value in every case).
+__device__ __forceinline__ double neg_exact(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ double half_exact(double x) {
+    const long long b = __double_as_longlong(x);
+    const unsigned int ef = (unsigned int)((unsigned long long)b >> 52) & 0x7ffu;
+    return (ef >= 2u && ef < 0x7ffu) ? __longlong_as_double(b - (1ll << 52)) : x * 0.5;
+}
+__device__ __forceinline__ double twice_exact(double x) {
+    const long long b = __double_as_longlong(x);
+    const unsigned int ef = (unsigned int)((unsigned long long)b >> 52) & 0x7ffu;
+    return (ef >= 1u && ef < 0x7feu) ? __longlong_as_double(b + (1ll << 52)) : x * 2.0;
+}
+template <>
+__device__ __forceinline__ cplx apply_op<cplx>(int op, cplx v) {
+    if (op & 2) v.y = neg_exact(v.y);
+    if (op & 1) { v.x = neg_exact(v.x); v.y = neg_exact(v.y); }
+    return v;
+}
 
 static constexpr int FINF = -(1 << 30);  // νInf
 static constexpr int KAVG = -1;          // kSW: momentum average

@@ -1372,12 +1372,16 @@ __global__ void k_finalize3(Finalize3 f, int k2_epilogue, int t_recombine, size_
         }
     }
     if (k2_epilogue) {
+        const cplx flt = f.FL[CH_T][i], fla = f.FL[CH_A][i];
         v[CH_P] += f.FL[CH_P][i];
-        v[CH_A] += f.FL[CH_A][i];
-        v[CH_T] += f.FL[CH_T][i] * 2.0;
-        v[CH_T] += f.FL[CH_A][i] * -1.0;
+        v[CH_A] += fla;
+        v[CH_T] += cplx{twice_exact(flt.x), twice_exact(flt.y)};
+        v[CH_T] -= fla;
     }
-    if (t_recombine) v[CH_T] = (v[CH_T] + v[CH_A]) * 0.5;
+    if (t_recombine) {  // (γtd + γa)/2
+        const cplx s = v[CH_T] + v[CH_A];
+        v[CH_T] = cplx{half_exact(s.x), half_exact(s.y)};
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         if (f.out[c]) f.out[c][i] = v[c];
