@@ -92,6 +92,21 @@ __device__ void vert_adj(const VertBar& B, const Dims& d, int ch, int sp, int m,
     pSp_adj(B, d, ch, m, n, np, P, fl, g * 2.0);
     xSp_adj(B, d, ch, m, n, np, P, fl, g);
 }
+// transpose of pSp_k2diff (fdga_device.cuh), the reduced K2 vertex difference: the own channel's
+// K3 and the two other channels (the RefVertex correction is constant)
+__device__ void pSp_k2diff_adj(const VertBar& B, const Dims& d, int ch, int m, int n, int np, int P, cplx g) {
+    if (bin(m, d.n1) && bin(m, d.n2O) && fin(n, d.n2n) && fin(np, d.n2n) && bin(m, d.n3O) && fin(n, d.n3n) &&
+        fin(np, d.n3n))
+        k3a(B.g[ch], d, m, n, np, P, g);
+    const int Pc = (d.Nq == 1) ? 0 : KAVG;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        if (r == ch) continue;
+        int a, b, c;
+        conv(ch, r, m, n, np, a, b, c);
+        chan_adj(B.g[r], d, a, b, c, Pc, g);
+    }
+}
 // transpose of fl_right
 __device__ __forceinline__ void fl_right_adj(const FLBar& FL, const Dims& d, int ch, int m, int n, int P, cplx g) {
     if (!bin(m, d.n2O) || !fin(n, d.n2n)) return;
@@ -365,6 +380,11 @@ __device__ void adj_K1_body(const VertP& F, const FLP& FL, const cplx* Pi, const
         vert_adj(Fb, d, CH, SP, m, FINF, FINF, P, FL_ALL, cbar);
     }
 }
+// K2 BSE, transposed in the form the forward kernel computes (bse_K2_row):
+//   out = T s [c S_X + Σ_{ω ∈ window} D(ω) X(ω)],  c = own K2(Ω, ν) (t: 2 γt - γa),
+//   D = the reduced vertex difference (k2_vertex_diff), X = Π FL(Ω, ω̃, ∞) + (Π - Π0) U.
+// The own channel's K1 and K2 terms of F(Ω,ν,ω) - F(Ω,∞,ω) cancel exactly, so they receive no
+// scatter; only the own K3, the other two channels, Π̄, FL̄ and S̄_X do.
 template <int CH>
 __device__ void adj_K2_body(const VertP& F, const FLP& FL, const cplx* Pi, const cplx* Pi0, const cplx* SX,
                             const VertBar& Fb, const FLBar& FLb, cplx* Pibar, cplx* SXbar, const cplx* rawbar,
@@ -375,46 +395,47 @@ __device__ void adj_K2_body(const VertP& F, const FLP& FL, const cplx* Pi, const
     const int nu = idx % d.N2n - d.n2n;
     const int m = (idx / d.N2n) % d.N2O - (d.n2O - 1);
     const int P = idx / (d.N2n * d.N2O);
-    constexpr int SP = (CH == CH_T) ? SP_D : SP_P;
     const cplx s = rawbar[idx] * (d.T * (CH == CH_T ? -1.0 : 1.0));
-    const cplx cinf = vert_eval(F, d, CH, SP, m, FINF, FINF, P);
-    const cplx c = vert_eval(F, d, CH, SP, m, nu, FINF, P) - cinf;
     Windows win;
-    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.n1 - 1;
-    win.add(-d.n2n, d.n2n - 1, lo, hi);
+    const int lo = -d.nPw, hi = d.nPw - 1, h1 = d.xn1 - 1;
+    win.add(-d.xn2n, d.xn2n - 1, lo, hi);
     win.add(-d.nRn, d.nRn - 1, lo, hi);
     win.add(nu - h1, nu + h1, lo, hi);
     win.add(-(m + nu + 1) - h1, -(m + nu + 1) + h1, lo, hi);
     if (CH == CH_P) win.add(m - nu - 1 - h1, m - nu - 1 + h1, lo, hi);
     win.merge();
-    cplx cbar = mk(0, 0), cinfbar = mk(0, 0);
     for (int t = lane; t < win.total; t += 32) {
         const int n = win.at(t);
         const int wt = cross(CH, m, n);
-        const bool inb = fin(n, d.n2n);
-        const cplx Finf = inb ? vert_eval(F, d, CH, SP, m, FINF, n, P) : cinf;
-        const cplx Fl = vert_eval(F, d, CH, SP, m, nu, n, P) - Finf - c;
+        const cplx D = k2_vertex_diff<CH>(F, d, m, nu, n, P);
         const cplx FLr = fl_right(FL.K2[CH_P], FL.K2[CH_T], FL.K2[CH_A], d, CH, m, wt, P);
         const size_t ip = ixPi(d, P, m, n);
         const cplx pi = Pi[ip], pi0 = Pi0[ip];
         const cplx X = cfma(pi, FLr, (pi - pi0) * d.U);
-        const cplx Flb = cmulc(X, s);
-        vert_adj(Fb, d, CH, SP, m, nu, n, P, FL_ALL, Flb);
-        if (inb) vert_adj(Fb, d, CH, SP, m, FINF, n, P, FL_ALL, Flb * -1.0);
-        else cinfbar = cinfbar - Flb;
-        cbar = cbar - Flb;
-        const cplx Xb = cmulc(Fl, s);
+        const cplx Db = cmulc(X, s);
+        if (CH != CH_T) {
+            pSp_k2diff_adj(Fb, d, CH, m, nu, n, P, Db);
+        } else {
+            pSp_k2diff_adj(Fb, d, CH_T, m, nu, n, P, Db * 2.0);
+            pSp_k2diff_adj(Fb, d, CH_A, m, nu, n, P, Db * -1.0);
+        }
+        const cplx Xb = cmulc(D, s);
         aadd(Pibar + ip, cmulc(FLr + mk(d.U, 0), Xb));
         fl_right_adj(FLb, d, CH, m, wt, P, cmulc(pi, Xb));
     }
-    cbar = warp_sum(cbar);
-    cinfbar = warp_sum(cinfbar);
     if (lane == 0) {
         const size_t is = (size_t)CH * d.Nq * d.NPO + (size_t)P * d.NPO + (m + d.nPO - 1);
-        cbar += cmulc(SX[is], s);
+        const cplx c = k2_c<CH>(F, d, m, nu, P);
         aadd(SXbar + is, cmulc(c, s));
-        vert_adj(Fb, d, CH, SP, m, nu, FINF, P, FL_ALL, cbar);
-        vert_adj(Fb, d, CH, SP, m, FINF, FINF, P, FL_ALL, cinfbar - cbar);
+        const cplx cb = cmulc(SX[is], s);
+        if (bin(m, d.n1) && bin(m, d.n2O) && fin(nu, d.n2n)) {
+            if (CH != CH_T) {
+                k2a(Fb.g[CH], d, m, nu, P, cb);
+            } else {
+                k2a(Fb.g[CH_T], d, m, nu, P, cb * 2.0);
+                k2a(Fb.g[CH_A], d, m, nu, P, cb * -1.0);
+            }
+        }
     }
 }
 __global__ void k_adj_K1(VertP F, FLP FL, BubbleP B, const cplx* SX, VertBar Fb, FLBar FLb, cplx* Pbpp, cplx* Pbph,

@@ -785,54 +785,6 @@ __host__ __device__ __forceinline__ int k2_table_half(const Dims& d) {
     const int W = d.xn2O + d.xn2n + d.xn1 + d.nRn + 2;  // (extents over F and a Vertex-valued F0)
     return W < d.nPw ? W : d.nPw;
 }
-// F(Ω,ν,ω) - F(Ω,∞,ω) - F(Ω,ν,∞) + F(Ω,∞,∞) in the spin combination of the K2 BSE of channel CH
-template <int CH, class S>
-__device__ __forceinline__ S k2_vertex_diff(const VertPT<S>& F, const Dims& d, int m, int nu, int n, int P) {
-    using R = decltype(S::x);
-    if constexpr (CH != CH_T) {
-        return pSp_k2diff(F, d, CH, m, nu, n, P);
-    } else {  // density: 2 pSp + xSp, xSp(t) = -pSp(a); 2p exact, one rounding
-        const S p = pSp_k2diff(F, d, CH_T, m, nu, n, P), x = pSp_k2diff(F, d, CH_A, m, nu, n, P);
-        return S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};
-    }
-}
-// the same for F and a tangent vertex dF in one pass
-template <int CH, class S>
-__device__ __forceinline__ void k2_vertex_diff2(const VertPT<S>& F, const VertPT<S>& E, const Dims& d, int m, int nu,
-                                                int n, int P, S& v, S& w) {
-    using R = decltype(S::x);
-    if constexpr (CH != CH_T) {
-        pSp_k2diff2(F, E, d, CH, m, nu, n, P, v, w);
-    } else {
-        S p, q, x, y;
-        pSp_k2diff2(F, E, d, CH_T, m, nu, n, P, p, q);
-        pSp_k2diff2(F, E, d, CH_A, m, nu, n, P, x, y);
-        v = S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};
-        w = S{fma(q.x, (R)2, -y.x), fma(q.y, (R)2, -y.y)};
-    }
-}
-// c = F(Ω,ν,∞) - F(Ω,∞,∞) in the same spin combination: only the own channel's K2(Ω,ν) survives
-// (the t channel's crossed part is the a channel's, by crossing)
-template <class S>
-__device__ __forceinline__ S k2_own(const VertPT<S>& F, const Dims& d, int ch, int m, int nu, int P) {
-    S v{0, 0};
-    if (bin(m, d.n1) && bin(m, d.n2O) && fin(nu, d.n2n)) v = k2v(F.g[ch], d, m, nu, P);
-    if (F.has0 && !F.noref) {  // the own channel of a Vertex-valued F0 contributes its K2(Ω, ν) too
-        const Box& b = F.b0;
-        if (bin(m, b.n1) && bin(m, b.n2O) && fin(nu, b.n2n)) v += k2v(F.g0[ch], b, m, nu, P);
-    }
-    return v;
-}
-template <int CH, class S>
-__device__ __forceinline__ S k2_c(const VertPT<S>& F, const Dims& d, int m, int nu, int P) {
-    using R = decltype(S::x);
-    if constexpr (CH != CH_T) {
-        return k2_own(F, d, CH, m, nu, P);
-    } else {
-        const S p = k2_own(F, d, CH_T, m, nu, P), x = k2_own(F, d, CH_A, m, nu, P);
-        return S{fma(p.x, (R)2, -x.x), fma(p.y, (R)2, -x.y)};
-    }
-}
 template <int CH, class S, bool TAN>
 __device__ __forceinline__ void bse_K2_row(const VertPT<S>& F, const FLPT<S>& FL, const cplx* Pi, const cplx* Pi0,
                                            const cplx* SX, cplx* out, const int* items, const int* gstart,
