@@ -195,6 +195,12 @@ __constant__ cplxf c_twp32f[32];
 template <class C> __device__ __forceinline__ C twp32(int j);
 template <> __device__ __forceinline__ cplx twp32<cplx>(int j) { return c_twp32[j]; }
 template <> __device__ __forceinline__ cplxf twp32<cplxf>(int j) { return c_twp32f[j]; }
+// e^{+2πi j/96}: the twiddles of the lattices L = 3·2^a (3 ≤ L ≤ 96)
+__constant__ cplx c_twp96[96];
+__constant__ cplxf c_twp96f[96];
+template <class C> __device__ __forceinline__ C twp96(int j);
+template <> __device__ __forceinline__ cplx twp96<cplx>(int j) { return c_twp96[j]; }
+template <> __device__ __forceinline__ cplxf twp96<cplxf>(int j) { return c_twp96f[j]; }
 
 // in-place backward DFT (e^{+2πi jk/L}) of v[0..L) held in registers
 template <int L, class C>
@@ -222,6 +228,44 @@ __device__ __forceinline__ void fft_bwd(C (&v)[L]) {
             }
         }
     }
+}
+
+// in-place backward DFT of length L = 3M (M a power of two), by one mixed-radix step
+// (Cooley–Tukey, n = 3 n1 + n2, k = k1 + M k2): three length-M transforms of the residues n2, the
+// twiddles e^{2πi n2 k1 / L}, then M length-3 transforms, Z0 = u0 + s, Z1,2 = u0 - s/2 ± i(√3/2) d
+// with s = u1 + u2, d = u1 - u2.
+template <int L, class C>
+__device__ __forceinline__ void fft_bwd_3m(C (&v)[L]) {
+    using R = decltype(C::x);
+    constexpr int M = L / 3;
+    static_assert(3 * M == L && (M & (M - 1)) == 0 && L <= 96, "L = 3 * 2^a, L <= 96");
+    C y0[M], y1[M], y2[M];
+#pragma unroll
+    for (int n1 = 0; n1 < M; ++n1) { y0[n1] = v[3 * n1]; y1[n1] = v[3 * n1 + 1]; y2[n1] = v[3 * n1 + 2]; }
+    if constexpr (M > 1) {
+        fft_bwd<M>(y0);
+        fft_bwd<M>(y1);
+        fft_bwd<M>(y2);
+    }
+    const R h3 = (R)0.86602540378443864676;  // √3 / 2
+#pragma unroll
+    for (int k1 = 0; k1 < M; ++k1) {
+        const C a = y0[k1];
+        const C b = k1 == 0 ? y1[k1] : y1[k1] * twp96<C>(k1 * (96 / L));
+        const C c = k1 == 0 ? y2[k1] : y2[k1] * twp96<C>(2 * k1 * (96 / L));
+        const C sm = b + c, df = b - c;
+        const C hh = C{a.x - (R)0.5 * sm.x, a.y - (R)0.5 * sm.y};
+        const C rot = C{-h3 * df.y, h3 * df.x};
+        v[k1] = a + sm;
+        v[k1 + M] = hh + rot;
+        v[k1 + 2 * M] = hh - rot;
+    }
+}
+// backward DFT for the lattices with a register FFT: powers of two up to 32, and 3·2^a up to 24
+template <int L, class C>
+__device__ __forceinline__ void fft_bwd_any(C (&v)[L]) {
+    if constexpr ((L & (L - 1)) == 0) fft_bwd<L>(v);
+    else fft_bwd_3m<L>(v);
 }
 
 template <int L, class C, class G, bool TAN>
@@ -265,7 +309,7 @@ __global__ void k_bubble_fft(const G* GR, const G* tGR, cplx* pp, cplx* ph, Dims
         C v[L];
 #pragma unroll
         for (int x = 0; x < L; ++x) v[x] = row[x];
-        fft_bwd<L>(v);
+        fft_bwd_any<L>(v);
 #pragma unroll
         for (int x = 0; x < L; ++x) row[x] = v[x];
     }
@@ -275,7 +319,7 @@ __global__ void k_bubble_fft(const G* GR, const G* tGR, cplx* pp, cplx* ph, Dims
         C v[L];
 #pragma unroll
         for (int y = 0; y < L; ++y) v[y] = col[y * RS];
-        fft_bwd<L>(v);
+        fft_bwd_any<L>(v);
 #pragma unroll
         for (int y = 0; y < L; ++y) col[y * RS] = v[y];
     }
@@ -311,7 +355,7 @@ __global__ void k_fft2_rows(const cplx* in, cplx* out, int rows, int sign, doubl
         cplx v[L];
 #pragma unroll
         for (int x = 0; x < L; ++x) v[x] = row[x];
-        fft_bwd<L>(v);
+        fft_bwd_any<L>(v);
 #pragma unroll
         for (int x = 0; x < L; ++x) row[x] = v[x];
     }
@@ -321,7 +365,7 @@ __global__ void k_fft2_rows(const cplx* in, cplx* out, int rows, int sign, doubl
         cplx v[L];
 #pragma unroll
         for (int y = 0; y < L; ++y) v[y] = col[y * RS];
-        fft_bwd<L>(v);
+        fft_bwd_any<L>(v);
 #pragma unroll
         for (int y = 0; y < L; ++y) col[y * RS] = v[y];
     }
@@ -1588,6 +1632,10 @@ static cudaError_t bubble_f32_t(cudaStream_t s, const cplxf* GRf, const cplxf* t
         case 8: return launch_bubble_fft_f32<8, TAN>(s, GRf, tGRf, pp, ph, d);
         case 16: return launch_bubble_fft_f32<16, TAN>(s, GRf, tGRf, pp, ph, d);
         case 32: return launch_bubble_fft_f32<32, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 3: return launch_bubble_fft_f32<3, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 6: return launch_bubble_fft_f32<6, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 12: return launch_bubble_fft_f32<12, TAN>(s, GRf, tGRf, pp, ph, d);
+        case 24: return launch_bubble_fft_f32<24, TAN>(s, GRf, tGRf, pp, ph, d);
         default: return launch_bubble_dft<TAN, cplxf, cplxf>(s, GRf, tGRf, pp, ph, twp, d);
     }
 }
@@ -1608,6 +1656,14 @@ cudaError_t set_fft_twiddles() {
     }
     cudaError_t e = cudaMemcpyToSymbol(c_twp32, tw, sizeof(tw));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_twp32f, twf, sizeof(twf));
+    cplx t96[96];
+    cplxf t96f[96];
+    for (int j = 0; j < 96; ++j) {
+        t96[j] = mk(std::cos(2.0 * M_PI * j / 96.0), std::sin(2.0 * M_PI * j / 96.0));
+        t96f[j] = cplxf{(float)t96[j].x, (float)t96[j].y};
+    }
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_twp96, t96, sizeof(t96));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_twp96f, t96f, sizeof(t96f));
     return e;
 }
 
@@ -1625,6 +1681,10 @@ static cudaError_t bubble_t(cudaStream_t s, const cplx* G, const cplx* tG, const
         case 8: return launch_bubble_fft<8, TAN>(s, GR, tGR, pp, ph, d);
         case 16: return launch_bubble_fft<16, TAN>(s, GR, tGR, pp, ph, d);
         case 32: return launch_bubble_fft<32, TAN>(s, GR, tGR, pp, ph, d);
+        case 3: return launch_bubble_fft<3, TAN>(s, GR, tGR, pp, ph, d);
+        case 6: return launch_bubble_fft<6, TAN>(s, GR, tGR, pp, ph, d);
+        case 12: return launch_bubble_fft<12, TAN>(s, GR, tGR, pp, ph, d);
+        case 24: return launch_bubble_fft<24, TAN>(s, GR, tGR, pp, ph, d);
         default: break;
     }
     return launch_bubble_dft<TAN, cplx, cplx>(s, GR, tGR, pp, ph, twp, d);
@@ -1657,6 +1717,10 @@ cudaError_t launch_fft2(cudaStream_t s, const cplx* in, cplx* out, int rows, int
         case 4: return launch_fft2_tpl<4>(s, in, out, rows, sign, scale);
         case 8: return launch_fft2_tpl<8>(s, in, out, rows, sign, scale);
         case 16: return launch_fft2_tpl<16>(s, in, out, rows, sign, scale);
+        case 3: return launch_fft2_tpl<3>(s, in, out, rows, sign, scale);
+        case 6: return launch_fft2_tpl<6>(s, in, out, rows, sign, scale);
+        case 12: return launch_fft2_tpl<12>(s, in, out, rows, sign, scale);
+        case 24: return launch_fft2_tpl<24>(s, in, out, rows, sign, scale);
         default: break;
     }
     const int L = d.L, BS = L * (L + 1) + 1;

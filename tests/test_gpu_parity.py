@@ -22,11 +22,16 @@ ODD_NL = dict(kind="hubbard", T=0.4, U=1.5, mu=0.1, t1=1.0, L=3, nG=6, nK1=6, nK
               refvertex_noise=0.05, seed=3)
 
 
-# the lattice sizes of the precision (16x16, radix-2 FFT path) and differentiation (24x24, DFT path)
+# the lattice sizes of the precision (16x16, radix-2 FFT) and differentiation (24x24, 3·2^a FFT)
 # configurations, with small frequency boxes so that the oracle finishes in seconds
 NL16 = dict(kind="hubbard", T=0.5, U=3.0, mu=-0.3, t1=1.0, t2=-0.2, L=16, nG=4, nK1=4, nK2=(2, 2), nK3=(2, 2),
             mPi_factor=3)
 NL24 = dict(kind="hubbard", T=0.5, U=2.5, mu=0.0, t1=1.0, L=24, nG=4, nK1=4, nK2=(2, 2), nK3=(2, 2), mPi_factor=3)
+# the other lattices of the mixed-radix (3·2^a) register FFT
+NL6 = dict(kind="hubbard", T=0.5, U=2.0, mu=0.2, t1=1.0, t2=-0.1, L=6, nG=6, nK1=6, nK2=(3, 3), nK3=(2, 3),
+           mPi_factor=3, refvertex_noise=0.05, seed=5)
+NL12 = dict(kind="hubbard", T=0.5, U=2.5, mu=-0.1, t1=1.0, t2=-0.2, L=12, nG=4, nK1=4, nK2=(2, 2), nK3=(2, 2),
+            mPi_factor=3)
 
 
 def _state(S_or, rng, scale=0.05):
@@ -51,7 +56,7 @@ def test_map_parity(cfg, sym, strategy):
         x = y_orc + 0.01 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))
 
 
-@pytest.mark.parametrize("cfg", [NL16, NL24], ids=["nl16", "nl24"])
+@pytest.mark.parametrize("cfg", [NL16, NL24, NL6, NL12], ids=["nl16", "nl24", "nl6", "nl12"])
 def test_map_parity_large_lattice(cfg):
     """One map application from the PA start and one from a perturbed state, init_sym_grp! groups."""
     rng = np.random.default_rng(2)
