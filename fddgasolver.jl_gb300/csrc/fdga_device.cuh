@@ -45,6 +45,13 @@ __device__ __forceinline__ cplx ldg(const cplx* p) {
     double2 v = __ldg(reinterpret_cast<const double2*>(p));
     return cplx{v.x, v.y};
 }
+// 16-byte load and store of a device array element (cudaMalloc'd arrays indexed in cplx units are
+// 16-byte aligned; the struct itself is 8-byte aligned, which would split every access in two)
+__device__ __forceinline__ cplx ld16(const cplx* p) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    return cplx{v.x, v.y};
+}
+__device__ __forceinline__ void st16(cplx* p, cplx v) { *reinterpret_cast<double2*>(p) = make_double2(v.x, v.y); }
 // FP32 complex for the mixed-precision contractions (storage stays cplx)
 struct cplxf {
     float x, y;

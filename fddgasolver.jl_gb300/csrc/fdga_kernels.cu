@@ -1356,20 +1356,25 @@ __global__ void k_finalize3(Finalize3 f, int k2_epilogue, int t_recombine, size_
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     cplx v[3];
+    uint32_t e_prev = 0;
+    const uint32_t* map_prev = nullptr;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         v[c] = mk(0, 0);
         if (!f.out[c]) continue;
         if (f.map[c]) {
-            const uint32_t e = f.map[c][i];
-            v[c] = apply_op((int)(e & 3u), f.raw[c][e >> 2]);
+            // the t and a channels share the ph group: its map entry is read once
+            const uint32_t e = (f.map[c] == map_prev) ? e_prev : f.map[c][i];
+            map_prev = f.map[c];
+            e_prev = e;
+            v[c] = apply_op((int)(e & 3u), ld16(f.raw[c] + (e >> 2)));
         } else {
-            v[c] = f.raw[c][i];
+            v[c] = ld16(f.raw[c] + i);
         }
     }
     if (k2_epilogue) {
-        const cplx flt = f.FL[CH_T][i], fla = f.FL[CH_A][i];
-        v[CH_P] += f.FL[CH_P][i];
+        const cplx flt = ld16(f.FL[CH_T] + i), fla = ld16(f.FL[CH_A] + i);
+        v[CH_P] += ld16(f.FL[CH_P] + i);
         v[CH_A] += fla;
         v[CH_T] += cplx{twice_exact(flt.x), twice_exact(flt.y)};
         v[CH_T] -= fla;
@@ -1380,7 +1385,7 @@ __global__ void k_finalize3(Finalize3 f, int k2_epilogue, int t_recombine, size_
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        if (f.out[c]) f.out[c][i] = v[c];
+        if (f.out[c]) st16(f.out[c] + i, v[c]);
         if (f.outf[c]) f.outf[c][i] = to_c<cplxf>(v[c]);
     }
 }
