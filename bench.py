@@ -483,6 +483,22 @@ def run_batch(args, rank, world, dist):
         for S in solvers:
             S.iterate_solver("fdPA")  # one graph launch and one stream synchronisation per instance
     t_seq = (time.perf_counter() - t0) / args.steps
+    for S in solvers:
+        S.set_precision("mixed")
+        S.iterate_solver("fdPA")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for S in solvers:
+            S.iterate_solver("fdPA")
+    t_seq32 = (time.perf_counter() - t0) / args.steps
+    for S in solvers:
+        S.set_precision("fp64")
+    # the FP64 K3 GEMM work of all members (2 GEMMs x 3 channels x representative blocks x N^3
+    # complex products, 3 real FMAs = 6 flops each in the kernel's 3M form) at the measured FP64
+    # FMA rate: a floor under any FP64 batch iteration, however its launches are grouped
+    from fdgasolver.solver import _lib_query
+    fp64_rate = _lib_query("fp64_gflops") * 1e9
+    gemm_flops = sum(6.0 * S.query("k3_blocks") * 6.0 * S.query("k3_block_dim") ** 3 for S in solvers)
     errs = []
     for S, x in zip(solvers, xs):
         y64 = S.fixed_point(x) + x
@@ -505,6 +521,9 @@ def run_batch(args, rank, world, dist):
         "mixed_s_per_batch_iteration": ms32 / args.steps * 1e-3,
         "sequential_s_per_round": t_seq,
         "speedup_batch_vs_sequential": t_seq / t64,
+        "sequential_mixed_s_per_round": t_seq32,
+        "speedup_mixed_batch_vs_sequential": t_seq32 / (ms32 / args.steps * 1e-3),
+        "fp64_k3_gemm_floor_s": gemm_flops / fp64_rate,
         "kernels_per_batch_iteration": kernels, "gpu_launches": kernels * args.steps,
         "autotuned_k3_tiles_by_nu": tiles,
         "mixed_map_rel_err": {"max": max(errs), "median": float(np.median(errs))},
