@@ -80,6 +80,7 @@ def test_tensor_core_k3_tangent(cfg):
     gpu.close()
 
 
+@pytest.mark.gpu
 def test_fp64_to_fp32_rounding_matches_hardware():
     """The integer-path FP64 -> FP32 rounding used by every narrowing of the mixed map (d2f_rn)
     gives the hardware conversion's bits on 2^26 hashed inputs (ties of both parities, values next
