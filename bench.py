@@ -166,11 +166,17 @@ class ClockSampler:
 
 
 def build_problem(cfg_name, impl):
-    from fdgasolver.workloads import CONFIGS, make_inputs, make_solver
+    from fdgasolver.workloads import CONFIGS, make_solver
     cfg = dict(CONFIGS[cfg_name])
     if impl == "ours":
         return cfg, make_solver(cfg, True)
-    from oracle import oracle as O  # CPU baseline leg only
+    return cfg, oracle_problem(cfg)
+
+
+def oracle_problem(cfg):
+    """The oracle solver of a workload dict (CPU baseline legs only)."""
+    from fdgasolver.workloads import make_inputs
+    from oracle import oracle as O
     Gb, G0, S0, rv = make_inputs(cfg)
     local = cfg["kind"] == "siam"
     s = O.OracleSolver(nG=cfg["nG"], nK1=cfg["nK1"], nK2=cfg["nK2"], nK3=cfg["nK3"], T=cfg["T"], U=cfg["U"],
@@ -181,7 +187,7 @@ def build_problem(cfg_name, impl):
         s.set(name, a)
     s.finalize()
     s.init_sym_grp()
-    return cfg, s
+    return s
 
 
 def measured_peaks():
@@ -580,6 +586,82 @@ def run_differentiation(args, rank, world, dist):
     }
 
 
+def run_mfrg(args, rank, world, dist):
+    """The mfRG / Krylov-preconditioned solver (src/mfRG.jl) on the config-2 lattice and boxes as an
+    fdDΓA problem: the reference system's G0 is the bare G at μ = +0.25 (Π0 ≠ 0), F0 the bare U
+    (the map is then linear), Σ0 = 0.  Reports the time of one mfRG map application on the device
+    (graph replays inside a GMRES solve, per application), the preconditioned Anderson solve
+    (nlsolve m = 50, β = 0.85, Krylov rtol = atol = 1e-6, the reference's settings) against the plain
+    FP64 Anderson solve to the same tolerance, and the oracle's map on the host cores."""
+    import numpy as np
+    from fdgasolver.models import hubbard_bare_Green
+    from fdgasolver.workloads import CONFIGS, make_solver
+    cfg = dict(CONFIGS["hubbard8x8_b5_nk3_8x12"])
+    cfg.pop("refvertex_noise", None)
+    if args.U is not None:
+        cfg["U"] = args.U
+    cfg["G0"] = hubbard_bare_Green(cfg["T"], cfg["nG"], cfg["L"], mu=0.25, t1=cfg["t1"], t2=cfg.get("t2", 0.0))
+    S = make_solver(cfg, True)
+    x0 = S.flatten()
+    nF = x0.size - 2 * cfg["nG"] * cfg["L"] ** 2
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    S.synchronize()
+    t0 = time.perf_counter()
+    rp = S.solve("fdPA", maxiter=600, tol=1e-8, delta=0.85, mem=8)
+    t_plain = time.perf_counter() - t0
+    xp = S.flatten()
+    S.unflatten(x0)
+    S.solve_mfrg("fdPA", maxiter=1, tol=1e-8, delta=0.85, mem=50, update_sigma=True)  # capture the graphs
+    S.unflatten(x0)
+    S.synchronize()
+    t0 = time.perf_counter()
+    rm = S.solve_mfrg("fdPA", maxiter=40, tol=1e-8, delta=0.85, mem=50, update_sigma=True, krylov_maxiter=400)
+    t_mfrg = time.perf_counter() - t0
+    xm = S.flatten()
+    # one preconditioned residual: its Krylov iterations give the per-application cost
+    S.unflatten(xp + 1e-3 * (x0 - xp))
+    S.synchronize()
+    t0 = time.perf_counter()
+    _, info = S.fixed_point_preconditioned(xp + 1e-3 * (x0 - xp), "fdPA", update_sigma=True, krylov_maxiter=400,
+                                           krylov_rtol=1e-6, krylov_atol=1e-6)
+    t_res = time.perf_counter() - t0
+    clk = clocks.stop()
+    S.close()
+    # the oracle's map on the host cores (bounded sample)
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    orc = oracle_problem(cfg)
+    v = xp[:nF]
+    orc.mfrg_apply(v)
+    t0 = time.perf_counter()
+    orc.mfrg_apply(v)
+    t_orc = time.perf_counter() - t0
+    rel = float(np.abs(xm - xp).max() / np.abs(xp).max())
+    return {
+        "metric": "time to converge to max|R| < 1e-8, mfRG-preconditioned Anderson (Hubbard 8x8 fdDGA, G0 != 0)",
+        "value": t_mfrg, "unit": "s", "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": t_mfrg * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64 complex)",
+        "data": "synthetic (model inputs restated)",
+        "config": {"workload": "Hubbard 8x8 NL fdDGA: config-2 lattice and boxes, reference system G0 = bare G at "
+                               f"mu=0.25, Sigma0 = 0, F0 = bare U (U={cfg['U']}), init_sym_grp", "name": "hubbard8x8_b5_mfrg",
+                   "parallelism": "single GPU"},
+        "mfrg": {"seconds": t_mfrg, "converged": rm["converged"], "outer_iterations": rm["iterations"],
+                 "krylov_iterations": rm["krylov_iterations"], "residual": rm["residual"]},
+        "plain": {"seconds": t_plain, "converged": rp["converged"], "iterations": rp["iterations"],
+                  "residual": rp["residual"]},
+        "speedup_mfrg_vs_plain": t_plain / t_mfrg,
+        "mfrg_vs_plain_solution_rel_err": rel,
+        "preconditioned_residual": {"seconds": t_res, "krylov_iterations": info["krylov_iterations"],
+                                    "krylov_residual": info["krylov_residual"],
+                                    "ms_per_krylov_iteration": t_res * 1e3 / max(info["krylov_iterations"], 1)},
+        "cpu_baseline": {"value": t_orc, "unit": "s per mfRG map application", "cores": threads, "kind": "port",
+                         "sample": "1 application of the oracle's mfRG map after 1 warm-up (C++ restatement, OpenMP)"},
+        "clocks": clk,
+    }
+
+
 def run_reference(args, rank, world):
     from oracle import oracle as O
     threads = os.cpu_count() or 1
@@ -631,8 +713,10 @@ def main():
     if world > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     dist = Dist(world)
-    if args.config in ("siam_batch48", "hubbard24x24_b8_newton"):
-        if args.config == "hubbard24x24_b8_newton":
+    if args.config in ("siam_batch48", "hubbard24x24_b8_newton", "hubbard8x8_b5_mfrg"):
+        if args.config == "hubbard8x8_b5_mfrg":
+            out = run_mfrg(args, rank, world, dist)
+        elif args.config == "hubbard24x24_b8_newton":
             args.config = "hubbard24x24_b8_nk3_24x48"
             out = run_differentiation(args, rank, world, dist)
         else:
