@@ -339,7 +339,7 @@ __global__ void k_kr_givens(KrDevState* st, const double* c1, const double* c2) 
     st->g[j + 1] = -st->sn[j] * st->g[j];
     st->g[j] = st->cs[j] * st->g[j];
     st->est = fabs(st->g[j + 1]);
-    st->done = (st->est <= st->thr || hn == 0.0) ? 1 : 0;
+    st->done = (!(st->est > st->thr) || !(hn > 0.0)) ? 1 : 0;  // (a NaN estimate or norm stops the cycle)
 }
 // column j complete: advance, and continue the WHILE node while not done, j < m and the budget
 // allows one more application (j grows by one per pass, so the loop ends after at most m passes)
