@@ -1,0 +1,499 @@
+// fdga_k3_oz.cu -- the K3 Bethe-Salpeter contractions of the FP64 map on the tcgen05 tensor cores,
+// by exact digit slicing (the Ozaki scheme): FP64 results from BF16 products.
+//
+// Per (channel, representative (P, Ω) block) the BSE is one complex product C = A·M of Nν3 x Nν3
+// matrices (src/BSEa/BSEa_K3.jl:1-128; M formed elementwise in FP64 from the caches, Π, Π0 and FL,
+// exactly as the FP64 CUDA-core kernel forms it).  It runs as the real GEMM
+// D[ν][n] = Σ_k A_r[ν][k] B_r[k][n] in the 2x2 real form of the tcgen05 TF32 kernel (k = 2ω + q,
+// n = 2ν' + p), split in column tiles of NT = 32 real columns.
+//
+// Exact slicing.  Every entry v of the block of A, and of the tile of M, is written in fixed point
+// relative to a bound 2^(F-1022) > |v| with 56 fractional bits, Y = ⌊|v| 2^(56+1022-F)⌋ < 2^56, taken
+// straight from the FP64 significand by an integer shift, and Y is cut into S = 8 digits of 7 bits:
+//   v ≈ sign(v) Σ_s d_s 2^(F-1022-7(s+1)),  0 ≤ d_s ≤ 127  (truncation error < 2^-56 of the bound).
+// F_A is the largest exponent field over the block of A; F_M comes from an FP32 upper bound of |M|
+// over the tile formed from the magnitudes of M's factors (within a factor 2 of max|M| short of
+// cancellation), so that pass 1 spends no FP64 operation.  A digit times a sign is a BF16 number
+// exactly (8 significant bits).  The products of digit pairs (s, t) with s + t = g share one FP32
+// accumulator in tensor memory (g = 0..S-1, 8 x 32 columns): each product is an integer below 2^14,
+// so for K ≤ 2·128 the diagonals g ≤ 3 (at most 4 pairs) sum below 2^24 and are exact; the longer
+// diagonals pass 2^24 only when most digits of a row and a column are near 127 with equal signs,
+// and then round at 2^-24 of the accumulator (below 2^-41 of max|A| max|M| for g = 4, less for the
+// later ones).  The pairs with s + t ≥ S are dropped: with the truncation this leaves below ~2^-52
+// of max|A| max|M| per product term, the size of an FP64 rounding (a CPU emulation of these sums,
+// bounds included, on random blocks with entries spread over e^6 gives max|C - A·M| / max|A·M| ≤
+// 7e-15 at Nν = 96).  The epilogue joins the integer diagonals exactly in two 64-bit integers and
+// applies the block scales with one FP64 addition,
+//   D = 2^(F_A + F_M - 2044) Σ_g 2^(-7(g+2)) acc_g,
+// then the BSE's epilogue (T C and γL), as the FP64 kernel does.  A block of A or tile of M that
+// holds an infinity or NaN writes NaN, as the FP64 sum would.
+//
+// One CTA of 256 threads per (channel slot, block, column tile); K in chunks of 16 (8 ω), two
+// shared-memory stages of 8 + 8 digit operands; 36 MMAs (kind::f16, BF16 inputs, FP32 accumulation)
+// per chunk issued by one thread, tcgen05.commit -> mbarrier; every wait bounded (a timeout sets
+// *err and the kernel still releases its tensor memory).
+#include "fdga_kernels.h"
+
+namespace fdga {
+
+namespace {
+
+constexpr int OZ_THREADS = 256;
+constexpr int S = 8;                      // digits per operand
+constexpr int DB = 7;                     // bits per digit
+constexpr int KC = 16;                    // real K per chunk (one BF16 MMA)
+constexpr int CW = KC / 2;                // ω per chunk
+constexpr int NT = 32;                    // real columns per tile
+constexpr int A_DIG = 128 * KC * 2;       // one A digit operand: 128 rows x 16 BF16 = 4 KB
+constexpr int B_DIG = NT * KC * 2;        // one B digit operand: 32 rows x 16 BF16 = 1 KB
+constexpr int STAGE = S * (A_DIG + B_DIG);
+constexpr uint32_t SPIN_LIMIT = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// byte offset of element (row r, k) in a K-major no-swizzle operand of 16-bit elements, KC columns:
+// 8-row x 16-byte core matrices, K-adjacent ones 128 B apart, 8-row groups KC·16 = 256 B apart
+__device__ __forceinline__ uint32_t op16(int r, int k) {
+    return (uint32_t)((((r >> 3) * (KC / 8) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+}
+__device__ __forceinline__ uint64_t sdesc16(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((KC * 16) >> 4) << 32) |
+           (1ull << 46);
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        :
+        : "r"(dt), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+// the exponent field of an FP64 value
+__device__ __forceinline__ int efield(double v) {
+    return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffull);
+}
+// |v| in fixed point relative to the bound 2^(F-1022), 56 fractional bits: ⌊|v| 2^(56+1022-F)⌋
+// (0 for zero and subnormal v).  |v| < 2^(F-1022) gives ev ≤ F, so the shift F - ev - 3 is ≥ -3.
+__device__ __forceinline__ unsigned long long fixed56(double v, int F) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int ev = (int)((b >> 52) & 0x7ffull);
+    if (ev == 0 || F == 0) return 0ull;
+    const int rs = F - ev + (53 - S * DB);
+    const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    return rs < 0 ? (mant << (-rs)) : (rs < 64 ? (mant >> rs) : 0ull);
+}
+__device__ __forceinline__ uint32_t digit(unsigned long long Y, int s) {
+    return (uint32_t)(Y >> (DB * (S - 1 - s))) & 127u;
+}
+// two digits as a pair of BF16 numbers (low half first) with the sign bits sgn: the integer d < 2^23
+// is the FP32 value (2^23 + d) - 2^23, whose upper half is its BF16 pattern (exact for d < 2^8)
+__device__ __forceinline__ uint32_t bf_pair(uint32_t dlo, uint32_t dhi, uint32_t sgn) {
+    const float flo = __uint_as_float(0x4B000000u | dlo) - 8388608.0f;
+    const float fhi = __uint_as_float(0x4B000000u | dhi) - 8388608.0f;
+    return __byte_perm(__float_as_uint(flo), __float_as_uint(fhi), 0x7632) | sgn;
+}
+__device__ __forceinline__ uint32_t sbit(double v) {
+    return (uint32_t)((unsigned long long)__double_as_longlong(v) >> 63);
+}
+// the larger exponent field of the two parts of a complex number: both |x|, |y| < 2^(E - 1022)
+// (zero and subnormal parts included, with E = 0)
+__device__ __forceinline__ int cexpo(cplx v) { return max(efield(v.x), efield(v.y)); }
+// an FP32 upper bound of |x| from its top 23 significand bits (+1 ulp); 2^-126 below the FP32
+// normal range, +inf above it and for an infinity or NaN
+__device__ __forceinline__ float mag_up(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    const int e = (int)(b >> 52) - 896;  // the FP32 exponent field of |x|
+    if (e <= 0) return b ? __uint_as_float(0x00800000u) : 0.0f;
+    if (e >= 255) return __uint_as_float(0x7F800000u);
+    return __uint_as_float((((uint32_t)e << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu)) + 1u);
+}
+__device__ __forceinline__ float2 mag_up(cplx v) { return make_float2(mag_up(v.x), mag_up(v.y)); }
+// bounds of |Re(a b)| and |Im(a b)| from part bounds of a and b, added to acc
+__device__ __forceinline__ void prod_bound(float2 a, float2 b, float2& acc) {
+    acc.x = fmaf(a.x, b.x, fmaf(a.y, b.y, acc.x));
+    acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
+}
+// x · 2^e for an integer |x| < 2^53 (exact), built from its bits on the integer pipes; 0 below the
+// normal range
+__device__ __forceinline__ double i2d_scaled(long long x, int e) {
+    if (x == 0) return 0.0;
+    const unsigned long long sg = x < 0 ? (1ull << 63) : 0ull;
+    const unsigned long long u = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+    const int p = 63 - __clzll((long long)u);  // 2^p ≤ u < 2^(p+1), p ≤ 52
+    const int ef = p + e + 1023;
+    if (ef <= 0) return 0.0;
+    if (ef >= 2047) return __longlong_as_double((long long)(sg | 0x7FF0000000000000ull));
+    const unsigned long long mant = (u << (52 - p)) & 0xFFFFFFFFFFFFFull;
+    return __longlong_as_double((long long)(sg | ((unsigned long long)ef << 52) | mant));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims d, int ntile, int* err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    // the ω factors of M with their signs: [0] Π0 (mode 0) or s1 (Π - Π0), [1] s1 Π, [2] s2 Π, and
+    // the exponent bounds of [0] and of Π
+    __shared__ cplx qf[128][3];
+    __shared__ int qe[128][2];
+    __shared__ float2 qm[128][2];  // part bounds of [0] and of Π
+    // exponent field bound of A (block); FP32 bound of |M| (tile, as bits); exponent-sum bound of M
+    // (tile, when the FP32 bound is not finite); non-finite operands
+    __shared__ int fmax[4];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = d.N3n;
+    const int nchunks = N / CW;  // N is a multiple of 8
+    const int nb = args.nblocks;
+    const int tile = blockIdx.x % ntile;
+    const int rest = blockIdx.x / ntile;
+    const int slot = rest / nb;
+    const int blk = args.blocks ? args.blocks[rest % nb] : (int)(rest % nb);
+    const K3Args& a = args.a[slot];
+    const int CH = args.ch[slot];
+    const int m = blk % d.N3O - (d.n3O - 1), P = blk / d.N3O;
+    const size_t base = (size_t)blk * N * N;
+    const int col0 = tile * NT;                      // first real column of the tile
+    const int ncol = min(NT, 2 * N - col0);          // 16 or 32
+    const int cc0 = col0 / 2, ncc = ncol / 2;        // complex columns ν'
+    const double s1 = (CH == CH_A) ? 1.0 : -1.0, s2 = (CH == CH_T) ? -1.0 : 1.0;
+    const bool full = MODE == 1 && (a.flags & K3F_1LOOP) == 0;  // M has the Γ and γL terms
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_base))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid < N) {
+        const size_t ip = ixPi(d, P, m, tid - d.n3n);
+        const cplx pi0 = a.Pi0 ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
+        cplx q0 = pi0, q1 = mk(0.0, 0.0), q2 = mk(0.0, 0.0);
+        if (MODE >= 1) {
+            const cplx pi = ldg(a.Pi + ip);
+            q0 = (pi - pi0) * s1;
+            q1 = pi * s1;
+            q2 = pi * s2;
+        }
+        qf[tid][0] = q0;
+        qf[tid][1] = q1;
+        qf[tid][2] = q2;
+        qe[tid][0] = cexpo(q0);
+        qe[tid][1] = cexpo(q1);
+        qm[tid][0] = mag_up(q0);
+        qm[tid][1] = mag_up(q1);
+    }
+    if (tid < 4) fmax[tid] = 0;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    // γL at a K3 index in the channel's spin combination (t: 2 FL.γt - FL.γa)
+    auto gl_at = [&](size_t i) -> cplx {
+        if (CH == CH_T) {
+            const cplx t = ldg(a.FLt + i), u = ldg(a.FLa + i);
+            return cplx{fma(t.x, 2.0, -u.x), fma(t.y, 2.0, -u.y)};
+        }
+        return ldg(a.FLc + i);
+    };
+    // pass 1: the exponent field bound F_A of A over the block (exact max, integer pipes), and a
+    // bound of |M| over the tile from FP32 upper bounds of the parts of its factors (one product in
+    // mode 0 and one-loop, s1[(Π-Π0)F0 + Π Γ] + s2 Π γL otherwise; |Re(ab)| ≤ |a.x||b.x| + |a.y||b.y|,
+    // |Im(ab)| ≤ |a.x||b.y| + |a.y||b.x|), raised by 2^-16 for the FP32 roundings:
+    // |M| ≤ B < 2^(F_M - 1022) with F_M = (FP32 exponent field of B) + 896.  Where B is not finite
+    // (operands beyond the FP32 range, an infinity or a NaN), a second pass bounds M from the FP64
+    // exponent fields of its factors instead (a complex product of parts below 2^(Ea-1022) and
+    // 2^(Eb-1022) has parts below 2^(Ea+Eb-2043); at most three products: F_M = max(Ea + Eb) - 1019).
+    {
+        int fa = 0;
+        float bm = 0.0f;
+        for (int e = tid; e < N * N; e += OZ_THREADS) fa = max(fa, cexpo(ldg(a.A + base + e)));
+        for (int e = tid; e < N * ncc; e += OZ_THREADS) {
+            const int w = e / ncc, col = cc0 + e % ncc;
+            float2 mb = make_float2(0.0f, 0.0f);
+            prod_bound(qm[w][0], mag_up(ldg(a.B0 + base + (size_t)w * N + col)), mb);
+            if (full) {
+                const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
+                prod_bound(qm[w][1], mag_up(ldg(a.G + ig)), mb);
+                const int ot = cross(CH, m, w - d.n3n);
+                if (fin(ot, d.n3n)) {
+                    const size_t il = base + (size_t)(ot + d.n3n) * N + col;
+                    float2 gb;
+                    if (CH == CH_T) {
+                        const float2 tb = mag_up(ldg(a.FLt + il)), ub = mag_up(ldg(a.FLa + il));
+                        gb = make_float2(fmaf(2.0f, tb.x, ub.x), fmaf(2.0f, tb.y, ub.y));
+                    } else {
+                        gb = mag_up(ldg(a.FLc + il));
+                    }
+                    prod_bound(qm[w][1], gb, mb);
+                }
+            }
+            bm = fmaxf(bm, fmaxf(mb.x, mb.y));  // the parts are ≥ 0, so no NaN arises
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            fa = max(fa, __shfl_xor_sync(0xffffffffu, fa, o));
+            bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+        }
+        if (lane == 0) {
+            atomicMax(&fmax[0], fa);
+            atomicMax(&fmax[1], (int)__float_as_uint(bm));  // non-negative floats order as integers
+        }
+    }
+    __syncthreads();
+    if (fmax[1] >= 0x7F800000) {  // the FP32 bound overflowed: FP64 exponent bound (block-uniform branch)
+        int fs = 0, nf = 0;
+        for (int e = tid; e < N * ncc; e += OZ_THREADS) {
+            const int w = e / ncc, col = cc0 + e % ncc;
+            const int e0 = qe[w][0], ep = qe[w][1];
+            const int ef0 = cexpo(ldg(a.B0 + base + (size_t)w * N + col));
+            int sv = e0 + ef0;
+            nf |= (e0 == 0x7ff) | (ef0 == 0x7ff);
+            if (full) {
+                const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
+                const int egs = cexpo(ldg(a.G + ig));
+                nf |= (ep == 0x7ff) | (egs == 0x7ff);
+                sv = max(sv, ep + egs);
+                const int ot = cross(CH, m, w - d.n3n);
+                if (fin(ot, d.n3n)) {
+                    const size_t il = base + (size_t)(ot + d.n3n) * N + col;
+                    int egl;
+                    if (CH == CH_T) {
+                        const int et = cexpo(ldg(a.FLt + il)), eu = cexpo(ldg(a.FLa + il));
+                        nf |= (et == 0x7ff) | (eu == 0x7ff);
+                        egl = max(et + 1, eu) + 1;  // |2t - u| < 2^(max(Et+1, Eu)+1-1022)
+                    } else {
+                        egl = cexpo(ldg(a.FLc + il));
+                        nf |= (egl == 0x7ff);
+                    }
+                    sv = max(sv, ep + egl);
+                }
+            }
+            fs = max(fs, sv);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            fs = max(fs, __shfl_xor_sync(0xffffffffu, fs, o));
+            nf |= __shfl_xor_sync(0xffffffffu, nf, o);
+        }
+        if (lane == 0) {
+            atomicMax(&fmax[2], fs);
+            if (nf) atomicOr(&fmax[3], 1);
+        }
+        __syncthreads();
+    }
+    const int FA = fmax[0];
+    int FM;
+    if (fmax[1] >= 0x7F800000) {
+        FM = max(fmax[2] - 1019, 0);
+    } else {
+        const float B = __uint_as_float((uint32_t)fmax[1]);
+        const uint32_t eb = __float_as_uint(fmaf(B, 1.52587890625e-05f, B)) >> 23;  // B (1 + 2^-16)
+        FM = (B == 0.0f) ? 0 : (eb >= 255u ? 1152 : (int)eb + 896);
+    }
+    const bool nonfinite = FA == 0x7ff || fmax[3] != 0;
+    // instruction descriptor: D FP32, A and B BF16, both K-major, N = ncol, M = 128
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(ncol >> 3) << 17) | ((128u >> 4) << 24);
+    // A staging: thread tid holds row anu and the four ω 4·aq.. of the chunk (one 16-byte store per
+    // digit; eight threads cover 128 contiguous bytes)
+    const int aq = (tid >> 3) & 1, anu = (tid & 7) | ((tid >> 4) << 3);
+    // shared-memory descriptors of the first A and B digit operands of stage 0 (the start address
+    // field, bits 0-13, takes the byte offsets of the other operands >> 4 without carry: all of the
+    // shared memory lies below 2^18 bytes)
+    const uint64_t dA0 = sdesc16(smem_u32(sm)), dB0 = sdesc16(smem_u32(sm) + S * A_DIG);
+    // the A entries of the next chunk are loaded one chunk ahead
+    const cplx* asrc = a.A + base + (size_t)anu * N + 4 * aq;
+    cplx an[4];
+    if (anu < N) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) an[i] = ldg(asrc + i);
+    }
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+        const int st = c & 1;
+        if (c >= 2 && !mbar_wait(smem_u32(&mbar[st]), ((c - 2) >> 1) & 1)) ok = false;
+        uint8_t* Ad = sm + (size_t)st * STAGE;  // S A digit operands, then S B digit operands
+        uint8_t* Bd = Ad + S * A_DIG;
+        const int w0 = CW * c;
+        {
+            // A: row ν, k = 2ω_l holds Re A, 2ω_l + 1 holds Im A (rows ≥ N are zero)
+            uint32_t wd[S][4];
+            if (anu < N) {
+                cplx av[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) av[i] = an[i];
+                if (c + 1 < nchunks) {
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) an[i] = ldg(asrc + w0 + CW + i);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const cplx v = av[i];
+                    const unsigned long long yr = fixed56(v.x, FA), yi = fixed56(v.y, FA);
+                    const uint32_t sg = (sbit(v.x) << 15) | (sbit(v.y) << 31);
+#pragma unroll
+                    for (int s = 0; s < S; ++s) wd[s][i] = bf_pair(digit(yr, s), digit(yi, s), sg);
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < S; ++s) wd[s][0] = wd[s][1] = wd[s][2] = wd[s][3] = 0u;
+            }
+            const uint32_t off = op16(anu, 8 * aq);
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+                *reinterpret_cast<uint4*>(Ad + (size_t)s * A_DIG + off) = make_uint4(wd[s][0], wd[s][1], wd[s][2], wd[s][3]);
+        }
+        // B (rows n = 2ν'_l + p of the tile, k = 2ω_l + q): row 2ν'_l holds [Re M, -Im M], row
+        // 2ν'_l + 1 holds [Im M, Re M]; M formed in FP64 as the CUDA-core kernel forms it.  Warps 4-7
+        // stage B (warp 0 also issues the MMAs).
+        for (int e = tid - OZ_THREADS / 2; e >= 0 && e < CW * ncc; e += OZ_THREADS / 2) {
+            const int cl = e % ncc, wl = e / ncc, w = w0 + wl, col = cc0 + cl;
+            const cplx f0 = ldg(a.B0 + base + (size_t)w * N + col);
+            cplx v;
+            if (full) {
+                const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
+                v = cfma(qf[w][0], f0, qf[w][1] * ldg(a.G + ig));
+                const int ot = cross(CH, m, w - d.n3n);
+                if (fin(ot, d.n3n)) v = cfma(qf[w][2], gl_at(base + (size_t)(ot + d.n3n) * N + col), v);
+            } else {
+                v = qf[w][0] * f0;
+            }
+            const unsigned long long yr = fixed56(v.x, FM), yi = fixed56(v.y, FM);
+            const uint32_t sr = sbit(v.x), si = sbit(v.y);
+            const uint32_t o0 = op16(2 * cl, 2 * wl), o1 = op16(2 * cl + 1, 2 * wl);
+            const uint32_t sg0 = (sr << 15) | ((si ^ 1u) << 31), sg1 = (si << 15) | (sr << 31);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                uint8_t* b = Bd + (size_t)s * B_DIG;
+                const uint32_t dr = digit(yr, s), di = digit(yi, s);
+                *reinterpret_cast<uint32_t*>(b + o0) = bf_pair(dr, di, sg0);
+                *reinterpret_cast<uint32_t*>(b + o1) = bf_pair(di, dr, sg1);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint64_t so = (uint64_t)((st * STAGE) >> 4);
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+                for (int t = 0; t + s < S; ++t)
+                    mma_bf16(tmem + (uint32_t)((s + t) * NT), dA0 + so + (uint64_t)((s * A_DIG) >> 4),
+                             dB0 + so + (uint64_t)((t * B_DIG) >> 4), idesc, (c > 0 || s > 0) ? 1u : 0u);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&mbar[st]))
+                         : "memory");
+        }
+    }
+    if (nchunks >= 2 && !mbar_wait(smem_u32(&mbar[nchunks & 1]), ((nchunks - 2) >> 1) & 1)) ok = false;
+    const uint32_t last_bar = smem_u32(&mbar[(nchunks - 1) & 1]), last_par = ((nchunks - 1) >> 1) & 1;
+    if (!mbar_wait(last_bar, last_par)) ok = false;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int q = warp & 3, h = warp >> 2;
+    const int nu = 32 * q + lane;
+    if (!ok) {
+        // a wait gave up: report it, and give the MMAs in flight one more bounded wait before the
+        // tensor memory is released
+        if (tid == 0) atomicExch(err, 1);
+        mbar_wait(last_bar, last_par);
+    } else if (32 * q < N && 16 * h < ncol) {
+        // epilogue: warp w reads TMEM lanes 32(w%4).. (rows ν) and the 16-column half w/4 of the
+        // tile, 8 columns at a time.  The diagonals are integers (|acc_g| < 2^26); they are joined
+        // exactly in two 64-bit integers, hi = Σ_{g<4} acc_g 2^(7(3-g)) < 2^44 and
+        // lo = Σ_{g≥4} acc_g 2^(7(7-g)) < 2^46, so D = 2^(E-35) hi + 2^(E-63) lo (E = F_A + F_M - 2044)
+        // costs one FP64 addition.
+        const int E = FA + FM - 2044;
+        const bool zero = FA == 0 || FM == 0;
+#pragma unroll 1
+        for (int hh = 0; hh < 2; ++hh) {
+            long long hi[8], lo[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
+#pragma unroll
+            for (int g = 0; g < S; ++g) {
+                uint32_t r[8];
+                const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * NT + 16 * h + 8 * hh);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                               "=r"(r[7])
+                             : "r"(taddr)
+                             : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));
+                    if (g < 4) hi[j] = hi[j] * 128 + v;
+                    else lo[j] = lo[j] * 128 + v;
+                }
+            }
+            if (nu < N) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int col = cc0 + 8 * h + 4 * hh + j;
+                    const size_t io = base + (size_t)nu * N + col;
+                    cplx o;
+                    if (nonfinite) {
+                        const double qn = __longlong_as_double(0x7ff8000000000000ll);
+                        o = mk(qn, qn);
+                    } else {
+                        const cplx cv = zero ? mk(0.0, 0.0)
+                                             : cplx{i2d_scaled(hi[2 * j], E - 35) + i2d_scaled(lo[2 * j], E - 63),
+                                                    i2d_scaled(hi[2 * j + 1], E - 35) + i2d_scaled(lo[2 * j + 1], E - 63)};
+                        if (MODE == 0) {
+                            o = cv * (d.T * ((CH == CH_A) ? 1.0 : -1.0));
+                        } else if (a.flags & K3F_NOEPI) {
+                            o = cv * d.T;
+                        } else {
+                            const cplx g = gl_at(io);
+                            o = cplx{fma(cv.x, d.T, g.x), fma(cv.y, d.T, g.y)};
+                        }
+                        if (a.flags & K3F_ACC) o = a.out[io] + o;
+                    }
+                    a.out[io] = o;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+}
+
+}  // namespace
+
+bool k3_oz_supported(const Dims& d) {
+    // rows ν < N of the 128-lane accumulator; column tiles of 32 or a last one of 16 (MMA N % 16)
+    return d.N3n >= 8 && d.N3n <= 128 && (d.N3n % 8) == 0;
+}
+
+static size_t k3_oz_smem() { return 2 * (size_t)STAGE; }
+
+cudaError_t prepare_bse_K3_oz() {
+    static SmemRecord set0, set1;
+    cudaError_t e = raise_smem_limit(k_bse_K3_oz<0>, set0, k3_oz_smem(), 0);
+    if (e == cudaSuccess) e = raise_smem_limit(k_bse_K3_oz<1>, set1, k3_oz_smem(), 0);
+    return e;
+}
+
+cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int* err) {
+    if (!k3_oz_supported(d) || mode < 0 || mode > 1) return cudaErrorInvalidValue;
+    const int ntile = (2 * d.N3n + NT - 1) / NT;
+    const unsigned grid = (unsigned)(nslots * a.nblocks * ntile);
+    if (mode) k_bse_K3_oz<1><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
+    else k_bse_K3_oz<0><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
+    return cudaGetLastError();
+}
+
+}  // namespace fdga

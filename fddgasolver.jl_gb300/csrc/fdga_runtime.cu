@@ -82,6 +82,7 @@ struct fdga_handle {
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
     int k3_tma = 1;                              // ... in the TMA-fed warp-specialised kernel when it fits
+    int k3_oz = 2;  // FP64 K3 contractions on the tensor cores (exact digit slicing): 0 never, 1 where supported, 2 also Nν3 ≥ 32
     int jvp_tangent = 1;                         // GMRES Jacobian products by the tangent kernels (else differences)
     int newton_cycles = 1;                       // GMRES restart cycles per Newton step
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
@@ -578,6 +579,19 @@ cudaError_t launch_k3_tensor_cores(fdga_handle* h, cudaStream_t s, int mode, con
     return launch_bse_K3_tc(s, mode, a3f, 3, h->d, h->d_err);
 }
 
+// The FP64 map's K3 contraction: on the tensor cores by exact BF16 digit slicing when the option is
+// on and the box fits (fdga_k3_oz.cu), else the FP64 CUDA-core GEMM.
+// the FP64 K3 contractions (modes 0 and 1) on the tensor cores: where the digit-sliced kernel
+// supports the box, and by default from Nν3 = 32 on (below, the CUDA-core kernel is as fast)
+bool use_k3_oz(const fdga_handle* h) {
+    if (!h->d_err || !k3_oz_supported(h->d)) return false;
+    return h->k3_oz == 1 || (h->k3_oz == 2 && h->d.N3n >= 32);
+}
+cudaError_t launch_k3_fp64(fdga_handle* h, cudaStream_t s, int mode, const K3Args3& a3) {
+    if (mode <= 1 && use_k3_oz(h)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err);
+    return launch_bse_K3(s, mode, a3, 3, h->d, 0, h->k3_tile[FDGA_FP64][mode < 2 ? mode : 1]);
+}
+
 using StageHook = std::function<void(const char*)>;
 // enqueued on the main stream of a captured iteration: right after branch B (which needs only Σ)
 // has forked, and right after the new vertex is complete (before the SDE)
@@ -735,7 +749,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
             a3.nblocks = a3f.nblocks = h->nk3blocks;
             if (mixed && k3_tensor_cores(h, 0)) LC(launch_k3_tensor_cores(h, s, 0, a3f));
             else if (mixed) LC(launch_bse_K3_f32(s, 0, a3f, 3, d, h->k3_tile[FDGA_MIXED][0]));
-            else LC(launch_bse_K3(s, 0, a3, 3, d, 0, h->k3_tile[FDGA_FP64][0]));
+            else LC(launch_k3_fp64(h, s, 0, a3));
             stage("bse_L_K3_gemm");
             cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
             const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
@@ -817,7 +831,7 @@ int enqueue_iteration(fdga_handle* h, int strategy, bool update_sigma, bool hart
         a3.nblocks = a3f.nblocks = h->nk3blocks;
         if (mixed && k3_tensor_cores(h, 1)) LC(launch_k3_tensor_cores(h, s, 1, a3f));
         else if (mixed) LC(launch_bse_K3_f32(s, 1, a3f, 3, d, h->k3_tile[FDGA_MIXED][1]));
-        else LC(launch_bse_K3(s, 1, a3, 3, d, 0, h->k3_tile[FDGA_FP64][1]));
+        else LC(launch_k3_fp64(h, s, 1, a3));
         stage("bse_K3_gemm");
         cplx* out[3] = {chanK(h, h->yS, CH_P, 3), chanK(h, h->yS, CH_T, 3), chanK(h, h->yS, CH_A, 3)};
         const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
@@ -1015,7 +1029,7 @@ int enqueue_tangent(fdga_handle* h, int strategy, bool update_sigma, bool hartre
         const int tm = mode == 0 ? 0 : 1;
         if (mixed && k3_tensor_cores(h, mode)) return launch_k3_tensor_cores(h, s, mode, a3f);
         if (mixed) return launch_bse_K3_f32(s, mode, a3f, 3, d, h->k3_tile[FDGA_MIXED][tm]);
-        return launch_bse_K3(s, mode, a3, 3, d, 0, h->k3_tile[FDGA_FP64][tm]);
+        return launch_k3_fp64(h, s, mode, a3);
     };
     if (strategy == FDGA_FDPA) {
         {  // dFL.K2 = L_K2(dF)  (Π0 constant): branch C
@@ -1852,6 +1866,10 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_g_realspace(s, h->G, h->GR, h->twm, d));
     CK(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
     CK(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + nS, d, h->T0tail));
+    if (k3_oz_supported(d)) {
+        if (!h->d_err) AL(h->d_err, 1);
+        CK(prepare_bse_K3_oz());
+    }
     CK(cudaStreamSynchronize(s));
     h->finalized = true;
     h->c0_dirty = true;
@@ -2886,7 +2904,7 @@ int enqueue_mfrg(fdga_handle* h, int& nl) {
         a3.nblocks = a3f.nblocks = h->nk3blocks;
         if (mixed && k3_tensor_cores(h, 0)) LC(launch_k3_tensor_cores(h, s, 0, a3f));
         else if (mixed) LC(launch_bse_K3_f32(s, 0, a3f, 3, d, h->k3_tile[FDGA_MIXED][0]));
-        else LC(launch_bse_K3(s, 0, a3, 3, d, 0, h->k3_tile[FDGA_FP64][0]));
+        else LC(launch_k3_fp64(h, s, 0, a3));
         cplx* out[3] = {h->FLK3, h->FLK3 + h->n3, h->FLK3 + 2 * h->n3};
         const Group* grp[3] = {&h->gK3ppL, &h->gK3phL, &h->gK3phL};
         Finalize3 f3 = fin(3, h->raw3, out, grp);
@@ -2922,7 +2940,7 @@ int enqueue_mfrg(fdga_handle* h, int& nl) {
         a3.nblocks = a3f.nblocks = h->nk3blocks;
         if (mixed && k3_tensor_cores(h, 1)) LC(launch_k3_tensor_cores(h, s, 1, a3f));
         else if (mixed) LC(launch_bse_K3_f32(s, 1, a3f, 3, d, h->k3_tile[FDGA_MIXED][1]));
-        else LC(launch_bse_K3(s, 1, a3, 3, d, 0, h->k3_tile[FDGA_FP64][1]));
+        else LC(launch_k3_fp64(h, s, 1, a3));
         cplx* out[3] = {chanK(h, h->mf.y, CH_P, 3), chanK(h, h->mf.y, CH_T, 3), chanK(h, h->mf.y, CH_A, 3)};
         const Group* grp[3] = {&h->gK3pp, &h->gK3ph, &h->gK3ph};
         LC(launch_finalize3(s, fin(3, h->raw3, out, grp), 0, 1, h->n3));
@@ -3381,6 +3399,17 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
         h->kr_device_loop = value ? 1 : 0;
         return FDGA_OK;
     }
+    if (h && key && std::string(key) == "k3_fp64_tensor_cores") {
+        if (value < 0 || value > 2) return fail(h, FDGA_ERR_ARG, "k3_fp64_tensor_cores takes 0, 1 or 2");
+        if (value) {
+            if (!h->d_err) AL(h->d_err, 1);
+            CK(prepare_bse_K3_oz());
+            CK(cudaStreamSynchronize(h->st));
+        }
+        h->k3_oz = value;
+        drop_graphs(h);
+        return FDGA_OK;
+    }
     if (!h || !key) return FDGA_ERR_ARG;
     const std::string k(key);
     if (k == "k3_tensor_cores") {
@@ -3598,6 +3627,7 @@ int fdga_query(fdga_handle* h, const char* key, double* value) {
     if (k == "state_len") { *value = (double)h->nstate; return FDGA_OK; }
     if (k == "launches") { *value = h->last_launches; return FDGA_OK; }
     if (k == "precision") { *value = h->precision; return FDGA_OK; }
+    if (k == "k3_fp64_tensor_cores") { *value = use_k3_oz(h) ? 1.0 : 0.0; return FDGA_OK; }
     return fail(h, FDGA_ERR_ARG, "unknown query key " + k);
 }
 

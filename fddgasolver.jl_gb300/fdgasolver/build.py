@@ -13,7 +13,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(os.path.dirname(PKG), "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libfdga.so")
-SOURCES = ["fdga_kernels.cu", "fdga_runtime.cu", "fdga_noalloc.cu", "fdga_anderson.cu", "fdga_anderson32.cu", "fdga_krylov.cu", "fdga_k3_tc.cu", "fdga_k3_tma.cu", "fdga_mfrg.cu", "fdga_adjoint.cu", "fdga_interp.cu"]
+SOURCES = ["fdga_kernels.cu", "fdga_runtime.cu", "fdga_noalloc.cu", "fdga_anderson.cu", "fdga_anderson32.cu", "fdga_krylov.cu", "fdga_k3_tc.cu", "fdga_k3_tma.cu", "fdga_k3_oz.cu", "fdga_mfrg.cu", "fdga_adjoint.cu", "fdga_interp.cu"]
 HEADERS = ["fdga_device.cuh", "fdga_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

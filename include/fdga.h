@@ -124,7 +124,12 @@ int fdga_set_precision(fdga_handle* h, int precision);
  * fdga_frule); 0: by finite differences of the map.  "newton_gmres_cycles" (default 1): GMRES
  * restart cycles per Newton step of fdga_solve_newton (more for ill-conditioned fixed points).
  * "fused_residual" (default 1): fdga_residual on page-locked x and R runs as one CUDA graph whose
- * host copies overlap the iteration; 0: copy, iterate and copy back in sequence. */
+ * host copies overlap the iteration; 0: copy, iterate and copy back in sequence.
+ * "k3_fp64_tensor_cores" (default 2): the FP64 map's K3 contractions (BSE_L_K3 and BSE_K3) run on
+ * the tensor cores by exact digit slicing of the FP64 operands (8 BF16 digits of 7 bits, products
+ * summed by diagonal in FP32 tensor memory, joined exactly; FP64-level results, ~1e-14 relative
+ * to the CUDA-core FP64 GEMM) when Nν3 is a multiple of 8 between 8 and 128: 2 from Nν3 = 32 on,
+ * 1 at every such Nν3, 0 never (FP64 CUDA-core GEMMs). */
 int fdga_set_option(fdga_handle* h, const char* key, int value);
 
 /* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.
@@ -290,7 +295,8 @@ int fdga_susceptibility(fdga_handle* h, int channel, double* out, size_t n);
 
 /* Scalar facts of a handle, for benchmarks and tools: "k3_blocks" (the (P, Ω) blocks of the K3
  * mesh that hold class representatives), "k3_block_dim" (2·nK3ν), "state_len", "launches"
- * (kernels per iteration), "precision"; and, with h == NULL allowed, "fp64_gflops": a
+ * (kernels per iteration), "precision", "k3_fp64_tensor_cores" (1 when the FP64 map's K3
+ * contractions run on the tensor cores); and, with h == NULL allowed, "fp64_gflops": a
  * calibration of the GPU's FP64 FMA throughput (GFLOP/s, one short kernel). */
 int fdga_query(fdga_handle* h, const char* key, double* value);
 
