@@ -226,8 +226,11 @@ def profile_traffic(name):
 
 
 def k3_gemm_roofline(S, stages, cfg_name):
-    """Roofline of the fused K3 BSE GEMM (k_bse_K3_gemm, MODE 1): one complex Nν3 x Nν3 x Nν3 product
-    per (channel, representative (P, Ω) block); complex MAC = 8 real flops; FP64 pipe bound."""
+    """Roofline of the fused K3 BSE GEMM (MODE 1): one complex Nν3 x Nν3 x Nν3 product per (channel,
+    representative (P, Ω) block); complex MAC = 8 real flops.  On the FP64 CUDA-core kernel
+    (k_bse_K3_gemm) the FP64 pipe bounds it; on the digit-sliced tensor-core kernel (k_bse_K3_oz,
+    the default from Nν3 = 32 on) the BF16 MMAs it issues are compared with the measured bf16 peak
+    and its FP64-equivalent rate with the FP64 pipe."""
     nb, N = S.query("k3_blocks"), S.query("k3_block_dim")
     ms = stages["bse_K3_gemm"]
     flops = 3 * nb * 8 * N ** 3
@@ -236,6 +239,21 @@ def k3_gemm_roofline(S, stages, cfg_name):
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
     achieved = flops / (ms * 1e-3) / 1e12
+    if S.query("k3_fp64_tensor_cores") == 1:
+        # 36 BF16 MMAs (M = 128 rows, K = 16) per K chunk over all 2N real columns and 2N real K
+        mma_flops = 3 * nb * 36 * 2 * 128 * (2 * N) * (2 * N)
+        bf16 = peaks.get("bf16_tflops", 1900.0)
+        tc = mma_flops / (ms * 1e-3) / 1e12
+        return {"bound": "tensor", "kernel": "k_bse_K3_oz<1> (fused K3 BSE, FP64 by digit slicing on tcgen05)",
+                "achieved": tc, "peak": bf16, "unit": "TFLOP/s", "frac": tc / bf16,
+                "peak_source": "fallback" if peaks.get("fallback") else "measured (bf16_tflops)",
+                "flops_per_launch": mma_flops, "fp64_equivalent_tflops": achieved, "fp64_pipe_peak": fp64_peak,
+                "fp64_equivalent_frac": achieved / fp64_peak,
+                "traffic": profile_traffic(f"k_bse_K3_oz_{cfg_name}.md"), "algorithmic_bytes": byts,
+                "hbm_achieved_gbs": byts / (ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm,
+                "hbm_frac": byts / (ms * 1e-3) / 1e9 / hbm, "launch_ms": ms,
+                "share_of_iteration": ms / sum(stages.values()),
+                "stage_ms": {k: round(v, 4) for k, v in stages.items()}}
     traffic = profile_traffic(f"k_bse_K3_gemm_{cfg_name}.md")
     tile = 16 if N <= 16 else (24 if N <= 24 else 32)
     return {"bound": "fp64", "kernel": f"k_bse_K3_gemm<1,{tile},cplx> (fused K3 BSE, FP64)", "achieved": achieved,
@@ -500,11 +518,13 @@ def run_batch(args, rank, world, dist):
     for S in solvers:
         S.set_precision("fp64")
     # the FP64 K3 GEMM work of all members (2 GEMMs x 3 channels x representative blocks x N^3
-    # complex products, 3 real FMAs = 6 flops each in the kernel's 3M form) at the measured FP64
-    # FMA rate: a floor under any FP64 batch iteration, however its launches are grouped
+    # complex products, 3 real FMAs = 6 flops each in the CUDA-core kernel's 3M form) at the measured
+    # FP64 FMA rate: the floor of a batch iteration whose K3 GEMMs run on the FP64 pipe; members with
+    # Nν3 ≥ 32 run them on the tensor cores instead (digit slicing), which this floor does not bound
     from fdgasolver.solver import _lib_query
     fp64_rate = _lib_query("fp64_gflops") * 1e9
     gemm_flops = sum(6.0 * S.query("k3_blocks") * 6.0 * S.query("k3_block_dim") ** 3 for S in solvers)
+    tc_members = sum(int(S.query("k3_fp64_tensor_cores")) for S in solvers)
     errs = []
     for S, x in zip(solvers, xs):
         y64 = S.fixed_point(x) + x
@@ -529,7 +549,8 @@ def run_batch(args, rank, world, dist):
         "speedup_batch_vs_sequential": t_seq / t64,
         "sequential_mixed_s_per_round": t_seq32,
         "speedup_mixed_batch_vs_sequential": t_seq32 / (ms32 / args.steps * 1e-3),
-        "fp64_k3_gemm_floor_s": gemm_flops / fp64_rate,
+        "fp64_k3_gemm_cuda_core_floor_s": gemm_flops / fp64_rate,
+        "members_with_tensor_core_fp64_k3": tc_members,
         "kernels_per_batch_iteration": kernels, "gpu_launches": kernels * args.steps,
         "autotuned_k3_tiles_by_nu": tiles,
         "mixed_map_rel_err": {"max": max(errs), "median": float(np.median(errs))},
