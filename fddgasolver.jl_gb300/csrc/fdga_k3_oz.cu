@@ -142,9 +142,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
-    // the ω factors of M with their signs: [0] Π0 (mode 0) or s1 (Π - Π0), [1] s1 Π, [2] s2 Π, and
-    // the exponent bounds of [0] and of Π
-    __shared__ cplx qf[128][3];
+    // the ω factors of M with their signs: [0] Π0 (mode 0), s1 (Π - Π0) (mode 1) or s1 dΠ (mode 3),
+    // [1] s1 Π, [2] s2 Π, [3] s2 dΠ (mode 3), and the exponent bounds of [0] and of Π
+    __shared__ cplx qf[128][4];
     __shared__ int qe[128][2];
     __shared__ float2 qm[128][2];  // part bounds of [0] and of Π
     // exponent field bound of A (block); FP32 bound of |M| (tile, as bits); exponent-sum bound of M
@@ -166,7 +166,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     const int ncol = min(NT, 2 * N - col0);          // 16 or 32
     const int cc0 = col0 / 2, ncc = ncol / 2;        // complex columns ν'
     const double s1 = (CH == CH_A) ? 1.0 : -1.0, s2 = (CH == CH_T) ? -1.0 : 1.0;
-    const bool full = MODE == 1 && (a.flags & K3F_1LOOP) == 0;  // M has the Γ and γL terms
+    // M has the Γ and γL terms (mode 1 but the one-loop form; mode 3 always)
+    const bool full = MODE == 3 || (MODE == 1 && (a.flags & K3F_1LOOP) == 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_base))
                      : "memory");
@@ -174,17 +175,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     }
     if (tid < N) {
         const size_t ip = ixPi(d, P, m, tid - d.n3n);
-        const cplx pi0 = a.Pi0 ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
-        cplx q0 = pi0, q1 = mk(0.0, 0.0), q2 = mk(0.0, 0.0);
+        const cplx pi0 = (MODE != 3 && a.Pi0) ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
+        cplx q0 = pi0, q1 = mk(0.0, 0.0), q2 = mk(0.0, 0.0), q3 = mk(0.0, 0.0);
         if (MODE >= 1) {
             const cplx pi = ldg(a.Pi + ip);
-            q0 = (pi - pi0) * s1;
             q1 = pi * s1;
             q2 = pi * s2;
+            if (MODE == 3) {
+                const cplx tpi = ldg(a.tPi + ip);
+                q0 = tpi * s1;
+                q3 = tpi * s2;
+            } else {
+                q0 = (pi - pi0) * s1;
+            }
         }
         qf[tid][0] = q0;
         qf[tid][1] = q1;
         qf[tid][2] = q2;
+        qf[tid][3] = q3;
         qe[tid][0] = cexpo(q0);
         qe[tid][1] = cexpo(q1);
         qm[tid][0] = mag_up(q0);
@@ -200,13 +208,35 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base;
-    // γL at a K3 index in the channel's spin combination (t: 2 FL.γt - FL.γa)
-    auto gl_at = [&](size_t i) -> cplx {
+    // γL at a K3 index in the channel's spin combination (t: 2 FL.γt - FL.γa), of FL or of the
+    // tangent's dFL
+    auto gl_of = [&](const cplx* FLc, const cplx* FLt, const cplx* FLa, size_t i) -> cplx {
         if (CH == CH_T) {
-            const cplx t = ldg(a.FLt + i), u = ldg(a.FLa + i);
+            const cplx t = ldg(FLt + i), u = ldg(FLa + i);
             return cplx{fma(t.x, 2.0, -u.x), fma(t.y, 2.0, -u.y)};
         }
-        return ldg(a.FLc + i);
+        return ldg(FLc + i);
+    };
+    auto gl_at = [&](size_t i) -> cplx { return gl_of(a.FLc, a.FLt, a.FLa, i); };
+    auto glt_at = [&](size_t i) -> cplx { return gl_of(a.tFLc, a.tFLt, a.tFLa, i); };
+    // part bounds of γL (t: |2t - u| ≤ 2|t| + |u|)
+    auto gl_bound = [&](const cplx* FLc, const cplx* FLt, const cplx* FLa, size_t i) -> float2 {
+        if (CH == CH_T) {
+            const float2 tb = mag_up(ldg(FLt + i)), ub = mag_up(ldg(FLa + i));
+            return make_float2(fmaf(2.0f, tb.x, ub.x), fmaf(2.0f, tb.y, ub.y));
+        }
+        return mag_up(ldg(FLc + i));
+    };
+    // exponent bound of γL (t: |2t - u| < 2^(max(Et+1, Eu)+1-1022)) and whether it is finite
+    auto gl_expo = [&](const cplx* FLc, const cplx* FLt, const cplx* FLa, size_t i, int& nf) -> int {
+        if (CH == CH_T) {
+            const int et = cexpo(ldg(FLt + i)), eu = cexpo(ldg(FLa + i));
+            nf |= (et == 0x7ff) | (eu == 0x7ff);
+            return max(et + 1, eu) + 1;
+        }
+        const int e = cexpo(ldg(FLc + i));
+        nf |= (e == 0x7ff);
+        return e;
     };
     // pass 1: the exponent field bound F_A of A over the block (exact max, integer pipes), and a
     // bound of |M| over the tile from FP32 upper bounds of the parts of its factors (one product in
@@ -223,21 +253,27 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
         for (int e = tid; e < N * ncc; e += OZ_THREADS) {
             const int w = e / ncc, col = cc0 + e % ncc;
             float2 mb = make_float2(0.0f, 0.0f);
-            prod_bound(qm[w][0], mag_up(ldg(a.B0 + base + (size_t)w * N + col)), mb);
-            if (full) {
+            const float2 f0b = mag_up(ldg(a.B0 + base + (size_t)w * N + col));
+            if (MODE == 3) {
+                // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL]
                 const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
-                prod_bound(qm[w][1], mag_up(ldg(a.G + ig)), mb);
+                const float2 gb = mag_up(ldg(a.G + ig));
+                prod_bound(qm[w][0], make_float2(f0b.x + gb.x, f0b.y + gb.y), mb);
+                prod_bound(qm[w][1], mag_up(ldg(a.tG + ig)), mb);
                 const int ot = cross(CH, m, w - d.n3n);
                 if (fin(ot, d.n3n)) {
                     const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                    float2 gb;
-                    if (CH == CH_T) {
-                        const float2 tb = mag_up(ldg(a.FLt + il)), ub = mag_up(ldg(a.FLa + il));
-                        gb = make_float2(fmaf(2.0f, tb.x, ub.x), fmaf(2.0f, tb.y, ub.y));
-                    } else {
-                        gb = mag_up(ldg(a.FLc + il));
-                    }
-                    prod_bound(qm[w][1], gb, mb);
+                    prod_bound(qm[w][0], gl_bound(a.FLc, a.FLt, a.FLa, il), mb);
+                    prod_bound(qm[w][1], gl_bound(a.tFLc, a.tFLt, a.tFLa, il), mb);
+                }
+            } else {
+                prod_bound(qm[w][0], f0b, mb);
+                if (full) {
+                    const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
+                    prod_bound(qm[w][1], mag_up(ldg(a.G + ig)), mb);
+                    const int ot = cross(CH, m, w - d.n3n);
+                    if (fin(ot, d.n3n))
+                        prod_bound(qm[w][1], gl_bound(a.FLc, a.FLt, a.FLa, (size_t)(base + (size_t)(ot + d.n3n) * N + col)), mb);
                 }
             }
             bm = fmaxf(bm, fmaxf(mb.x, mb.y));  // the parts are ≥ 0, so no NaN arises
@@ -259,25 +295,27 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
             const int e0 = qe[w][0], ep = qe[w][1];
             const int ef0 = cexpo(ldg(a.B0 + base + (size_t)w * N + col));
             int sv = e0 + ef0;
-            nf |= (e0 == 0x7ff) | (ef0 == 0x7ff);
+            nf |= (e0 == 0x7ff) | (ef0 == 0x7ff) | (ep == 0x7ff);
             if (full) {
                 const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
                 const int egs = cexpo(ldg(a.G + ig));
-                nf |= (ep == 0x7ff) | (egs == 0x7ff);
-                sv = max(sv, ep + egs);
+                nf |= (egs == 0x7ff);
+                if (MODE == 3) {  // dΠ (F0 + Γ) + Π dΓ: |F0 + Γ| < 2^(max(E0, EΓ)+1-1022)
+                    const int etg = cexpo(ldg(a.tG + ig));
+                    nf |= (etg == 0x7ff);
+                    sv = max(e0 + max(ef0, egs) + 1, ep + etg);
+                } else {
+                    sv = max(sv, ep + egs);
+                }
                 const int ot = cross(CH, m, w - d.n3n);
                 if (fin(ot, d.n3n)) {
                     const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                    int egl;
-                    if (CH == CH_T) {
-                        const int et = cexpo(ldg(a.FLt + il)), eu = cexpo(ldg(a.FLa + il));
-                        nf |= (et == 0x7ff) | (eu == 0x7ff);
-                        egl = max(et + 1, eu) + 1;  // |2t - u| < 2^(max(Et+1, Eu)+1-1022)
+                    if (MODE == 3) {
+                        sv = max(sv, e0 + gl_expo(a.FLc, a.FLt, a.FLa, il, nf));
+                        sv = max(sv, ep + gl_expo(a.tFLc, a.tFLt, a.tFLa, il, nf));
                     } else {
-                        egl = cexpo(ldg(a.FLc + il));
-                        nf |= (egl == 0x7ff);
+                        sv = max(sv, ep + gl_expo(a.FLc, a.FLt, a.FLa, il, nf));
                     }
-                    sv = max(sv, ep + egl);
                 }
             }
             fs = max(fs, sv);
@@ -360,7 +398,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
             const int cl = e % ncc, wl = e / ncc, w = w0 + wl, col = cc0 + cl;
             const cplx f0 = ldg(a.B0 + base + (size_t)w * N + col);
             cplx v;
-            if (full) {
+            if (MODE == 3) {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL], as the CUDA-core kernel
+                const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
+                v = cfma(qf[w][0], f0 + ldg(a.G + ig), qf[w][1] * ldg(a.tG + ig));
+                const int ot = cross(CH, m, w - d.n3n);
+                if (fin(ot, d.n3n)) {
+                    const size_t il = base + (size_t)(ot + d.n3n) * N + col;
+                    v = cfma(qf[w][3], gl_at(il), cfma(qf[w][2], glt_at(il), v));
+                }
+            } else if (full) {
                 const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
                 v = cfma(qf[w][0], f0, qf[w][1] * ldg(a.G + ig));
                 const int ot = cross(CH, m, w - d.n3n);
@@ -455,7 +501,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
                         } else if (a.flags & K3F_NOEPI) {
                             o = cv * d.T;
                         } else {
-                            const cplx g = gl_at(io);
+                            const cplx g = (MODE == 3) ? glt_at(io) : gl_at(io);
                             o = cplx{fma(cv.x, d.T, g.x), fma(cv.y, d.T, g.y)};
                         }
                         if (a.flags & K3F_ACC) o = a.out[io] + o;
@@ -481,18 +527,37 @@ bool k3_oz_supported(const Dims& d) {
 static size_t k3_oz_smem() { return 2 * (size_t)STAGE; }
 
 cudaError_t prepare_bse_K3_oz() {
-    static SmemRecord set0, set1;
+    static SmemRecord set0, set1, set3;
     cudaError_t e = raise_smem_limit(k_bse_K3_oz<0>, set0, k3_oz_smem(), 0);
     if (e == cudaSuccess) e = raise_smem_limit(k_bse_K3_oz<1>, set1, k3_oz_smem(), 0);
+    if (e == cudaSuccess) e = raise_smem_limit(k_bse_K3_oz<3>, set3, k3_oz_smem(), 0);
     return e;
 }
 
+// mode 0 (BSE_L_K3), 1 (BSE_K3), 2 (the tangent dK3 = T (dA·M + A·dM) + dγL): mode 2 runs as two
+// launches, each with its own block scales (dA and A need not share a magnitude): the mode-1 kernel
+// on dA with the epilogue term left out, then the A·dM kernel adding T C + dγL into the output
 cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int* err) {
-    if (!k3_oz_supported(d) || mode < 0 || mode > 1) return cudaErrorInvalidValue;
+    if (!k3_oz_supported(d) || mode < 0 || mode > 2) return cudaErrorInvalidValue;
     const int ntile = (2 * d.N3n + NT - 1) / NT;
     const unsigned grid = (unsigned)(nslots * a.nblocks * ntile);
-    if (mode) k_bse_K3_oz<1><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
-    else k_bse_K3_oz<0><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
+    if (mode == 2) {
+        K3Args3 a1 = a, a3 = a;
+        for (int i = 0; i < nslots; ++i) {
+            if (a.a[i].flags & K3F_1LOOP) return cudaErrorInvalidValue;  // no tangent of the one-loop form
+            a1.a[i].A = a.a[i].tA;
+            a1.a[i].flags |= K3F_NOEPI;
+            a3.a[i].flags |= K3F_ACC;
+        }
+        k_bse_K3_oz<1><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a1, d, ntile, err);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_bse_K3_oz<3><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a3, d, ntile, err);
+    } else if (mode == 1) {
+        k_bse_K3_oz<1><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
+    } else {
+        k_bse_K3_oz<0><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
+    }
     return cudaGetLastError();
 }
 

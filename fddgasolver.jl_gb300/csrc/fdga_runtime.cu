@@ -581,14 +581,17 @@ cudaError_t launch_k3_tensor_cores(fdga_handle* h, cudaStream_t s, int mode, con
 
 // The FP64 map's K3 contraction: on the tensor cores by exact BF16 digit slicing when the option is
 // on and the box fits (fdga_k3_oz.cu), else the FP64 CUDA-core GEMM.
-// the FP64 K3 contractions (modes 0 and 1) on the tensor cores: where the digit-sliced kernel
-// supports the box, and by default from Nν3 = 32 on (below, the CUDA-core kernel is as fast)
+// the FP64 K3 contractions (modes 0, 1 and the tangent's mode 2) on the tensor cores: where the
+// digit-sliced kernel supports the box, and by default from Nν3 = 32 on (below, the CUDA-core
+// kernel is as fast)
 bool use_k3_oz(const fdga_handle* h) {
     if (!h->d_err || !k3_oz_supported(h->d)) return false;
     return h->k3_oz == 1 || (h->k3_oz == 2 && h->d.N3n >= 32);
 }
 cudaError_t launch_k3_fp64(fdga_handle* h, cudaStream_t s, int mode, const K3Args3& a3) {
-    if (mode <= 1 && use_k3_oz(h)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err);
+    bool oneloop = false;
+    for (int i = 0; i < 3; ++i) oneloop |= (a3.a[i].flags & K3F_1LOOP) != 0;
+    if (use_k3_oz(h) && (mode <= 1 || !oneloop)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err);
     return launch_bse_K3(s, mode, a3, 3, h->d, 0, h->k3_tile[FDGA_FP64][mode < 2 ? mode : 1]);
 }
 

@@ -3,8 +3,9 @@
 Option k3_fp64_tensor_cores: 2 (default) from Nν3 = 32 on, 1 at every supported Nν3 (a multiple of 8
 between 8 and 128), 0 never (FP64 CUDA-core GEMMs).  One FP64 map application with the digit-sliced
 kernel agrees with the FP64 CUDA-core GEMMs to 1e-12 per flatten block (about 1e-14 is seen) and with
-the oracle to the plain path's 1e-10; the tangent map, whose K3 modes 0 and 1 run the same kernel,
-agrees with its CUDA-core form likewise.  A NaN in the state reaches every K3 entry that the
+the oracle to the plain path's 1e-10; the tangent map, whose K3 contractions (modes 0 and 1, and
+mode 2 as a dA·M launch and an A·dM launch) run the same kernel, agrees with its CUDA-core form
+likewise.  A NaN in the state reaches every K3 entry that the
 CUDA-core path turns into NaN.  Cases: Nν3 = 8, 24 (the Hubbard 8x8 workload's box), 32 (local and
 4x4 lattice), 80, 96 and 128.
 """
