@@ -143,8 +143,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
     // the ω factors of M with their signs: [0] Π0 (mode 0), s1 (Π - Π0) (mode 1) or s1 dΠ (mode 3),
-    // [1] s1 Π, [2] s2 Π, [3] s2 dΠ (mode 3), and the exponent bounds of [0] and of Π
-    __shared__ cplx qf[128][4];
+    // [1] s1 Π, and the exponent bounds of [0] and of Π
+    __shared__ cplx qf[128][2];
     __shared__ int qe[128][2];
     __shared__ float2 qm[128][2];  // part bounds of [0] and of Π
     // exponent field bound of A (block); FP32 bound of |M| (tile, as bits); exponent-sum bound of M
@@ -176,23 +176,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     if (tid < N) {
         const size_t ip = ixPi(d, P, m, tid - d.n3n);
         const cplx pi0 = (MODE != 3 && a.Pi0) ? ldg(a.Pi0 + ip) : mk(0.0, 0.0);
-        cplx q0 = pi0, q1 = mk(0.0, 0.0), q2 = mk(0.0, 0.0), q3 = mk(0.0, 0.0);
+        cplx q0 = pi0, q1 = mk(0.0, 0.0);
         if (MODE >= 1) {
             const cplx pi = ldg(a.Pi + ip);
             q1 = pi * s1;
-            q2 = pi * s2;
-            if (MODE == 3) {
-                const cplx tpi = ldg(a.tPi + ip);
-                q0 = tpi * s1;
-                q3 = tpi * s2;
-            } else {
-                q0 = (pi - pi0) * s1;
-            }
+            q0 = (MODE == 3) ? ldg(a.tPi + ip) * s1 : (pi - pi0) * s1;
         }
         qf[tid][0] = q0;
         qf[tid][1] = q1;
-        qf[tid][2] = q2;
-        qf[tid][3] = q3;
         qe[tid][0] = cexpo(q0);
         qe[tid][1] = cexpo(q1);
         qm[tid][0] = mag_up(q0);
@@ -398,19 +389,28 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
             const int cl = e % ncc, wl = e / ncc, w = w0 + wl, col = cc0 + cl;
             const cplx f0 = ldg(a.B0 + base + (size_t)w * N + col);
             cplx v;
-            if (MODE == 3) {  // dM = s1 [dΠ (F0 + Γ) + Π dΓ] + s2 [dΠ γL + Π dγL], as the CUDA-core kernel
+            // s2 Π = ±s1 Π and s2 dΠ = ±s1 dΠ (sign s1 s2), so the γL terms join the Γ terms before
+            // the products: two complex products per element instead of three (four for dM)
+            if (MODE == 3) {  // dM = s1 dΠ (F0 + Γ ± γL) + s1 Π (dΓ ± dγL)
                 const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
-                v = cfma(qf[w][0], f0 + ldg(a.G + ig), qf[w][1] * ldg(a.tG + ig));
+                cplx x0 = f0 + ldg(a.G + ig), x1 = ldg(a.tG + ig);
                 const int ot = cross(CH, m, w - d.n3n);
                 if (fin(ot, d.n3n)) {
                     const size_t il = base + (size_t)(ot + d.n3n) * N + col;
-                    v = cfma(qf[w][3], gl_at(il), cfma(qf[w][2], glt_at(il), v));
+                    const cplx g = gl_at(il), gt = glt_at(il);
+                    x0 = (s1 == s2) ? x0 + g : x0 - g;
+                    x1 = (s1 == s2) ? x1 + gt : x1 - gt;
                 }
-            } else if (full) {
+                v = cfma(qf[w][0], x0, qf[w][1] * x1);
+            } else if (full) {  // M = s1 (Π - Π0) F0 + s1 Π (Γ ± γL)
                 const size_t ig = (CH == CH_P) ? base + (size_t)w * N + col : base + (size_t)col * N + w;
-                v = cfma(qf[w][0], f0, qf[w][1] * ldg(a.G + ig));
+                cplx x1 = ldg(a.G + ig);
                 const int ot = cross(CH, m, w - d.n3n);
-                if (fin(ot, d.n3n)) v = cfma(qf[w][2], gl_at(base + (size_t)(ot + d.n3n) * N + col), v);
+                if (fin(ot, d.n3n)) {
+                    const cplx g = gl_at(base + (size_t)(ot + d.n3n) * N + col);
+                    x1 = (s1 == s2) ? x1 + g : x1 - g;
+                }
+                v = cfma(qf[w][0], f0, qf[w][1] * x1);
             } else {
                 v = qf[w][0] * f0;
             }
