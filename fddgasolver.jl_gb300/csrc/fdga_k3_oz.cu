@@ -95,12 +95,14 @@ __device__ __forceinline__ unsigned long long fixed56(double v, int F) {
 __device__ __forceinline__ uint32_t digit(unsigned long long Y, int s) {
     return (uint32_t)(Y >> (DB * (S - 1 - s))) & 127u;
 }
-// two digits as a pair of BF16 numbers (low half first) with the sign bits sgn: the integer d < 2^23
-// is the FP32 value (2^23 + d) - 2^23, whose upper half is its BF16 pattern (exact for d < 2^8)
+// two digits d < 128 as a pair of signed BF16 numbers (low half first), sgn holding the sign bits
+// (bits 15 and 31): the pattern 0x4300 | d is the BF16 number 128 + d (0xC300 | d: -(128 + d)), and
+// one packed BF16 subtraction of ±128 leaves ±d exactly
 __device__ __forceinline__ uint32_t bf_pair(uint32_t dlo, uint32_t dhi, uint32_t sgn) {
-    const float flo = __uint_as_float(0x4B000000u | dlo) - 8388608.0f;
-    const float fhi = __uint_as_float(0x4B000000u | dhi) - 8388608.0f;
-    return __byte_perm(__float_as_uint(flo), __float_as_uint(fhi), 0x7632) | sgn;
+    const uint32_t b = 0x43004300u | sgn;
+    uint32_t r;
+    asm("sub.rn.bf16x2 %0, %1, %2;" : "=r"(r) : "r"(b | dlo | (dhi << 16)), "r"(b));
+    return r;
 }
 __device__ __forceinline__ uint32_t sbit(double v) {
     return (uint32_t)((unsigned long long)__double_as_longlong(v) >> 63);
@@ -137,8 +139,29 @@ __device__ __forceinline__ double i2d_scaled(long long x, int e) {
     return __longlong_as_double((long long)(sg | ((unsigned long long)ef << 52) | mant));
 }
 
+// F_A of every A block: the largest exponent field of its entries (both parts), one CTA per
+// (channel slot, block) in the contraction's block order; every column tile of the block reads it
+__global__ void __launch_bounds__(256) k_oz_amax(K3Args3 args, Dims d, int* fa_blk) {
+    __shared__ int wmax[8];
+    const int nb = args.nblocks;
+    const int slot = blockIdx.x / nb, bi = blockIdx.x % nb;
+    const int blk = args.blocks ? args.blocks[bi] : bi;
+    const int N = d.N3n;
+    const cplx* A = args.a[slot].A + (size_t)blk * N * N;
+    int mx = 0;
+    for (int e = threadIdx.x; e < N * N; e += 256) mx = max(mx, cexpo(ldg(A + e)));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w) mx = max(mx, wmax[w]);
+        fa_blk[blockIdx.x] = mx;
+    }
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims d, int ntile, int* err) {
+__global__ void __launch_bounds__(OZ_THREADS, 2)
+    k_bse_K3_oz(K3Args3 args, Dims d, int ntile, const int* __restrict__ fa_blk, int* err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
@@ -147,8 +170,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     __shared__ cplx qf[128][2];
     __shared__ int qe[128][2];
     __shared__ float2 qm[128][2];  // part bounds of [0] and of Π
-    // exponent field bound of A (block); FP32 bound of |M| (tile, as bits); exponent-sum bound of M
-    // (tile, when the FP32 bound is not finite); non-finite operands
+    // (unused); FP32 bound of |M| (tile, as bits); exponent-sum bound of M (tile, when the FP32 bound
+    // is not finite); non-finite operands
     __shared__ int fmax[4];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = d.N3n;
@@ -229,8 +252,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
         nf |= (e == 0x7ff);
         return e;
     };
-    // pass 1: the exponent field bound F_A of A over the block (exact max, integer pipes), and a
-    // bound of |M| over the tile from FP32 upper bounds of the parts of its factors (one product in
+    // pass 1: F_A, the exponent field bound of A over the block (its largest exponent field), comes
+    // from k_oz_amax, which reads every A block once for all its column tiles; here, a bound of |M|
+    // over the tile from FP32 upper bounds of the parts of its factors (one product in
     // mode 0 and one-loop, s1[(Π-Π0)F0 + Π Γ] + s2 Π γL otherwise; |Re(ab)| ≤ |a.x||b.x| + |a.y||b.y|,
     // |Im(ab)| ≤ |a.x||b.y| + |a.y||b.x|), raised by 2^-16 for the FP32 roundings:
     // |M| ≤ B < 2^(F_M - 1022) with F_M = (FP32 exponent field of B) + 896.  Where B is not finite
@@ -238,9 +262,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
     // exponent fields of its factors instead (a complex product of parts below 2^(Ea-1022) and
     // 2^(Eb-1022) has parts below 2^(Ea+Eb-2043); at most three products: F_M = max(Ea + Eb) - 1019).
     {
-        int fa = 0;
         float bm = 0.0f;
-        for (int e = tid; e < N * N; e += OZ_THREADS) fa = max(fa, cexpo(ldg(a.A + base + e)));
         for (int e = tid; e < N * ncc; e += OZ_THREADS) {
             const int w = e / ncc, col = cc0 + e % ncc;
             float2 mb = make_float2(0.0f, 0.0f);
@@ -269,14 +291,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
             }
             bm = fmaxf(bm, fmaxf(mb.x, mb.y));  // the parts are ≥ 0, so no NaN arises
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            fa = max(fa, __shfl_xor_sync(0xffffffffu, fa, o));
-            bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
-        }
-        if (lane == 0) {
-            atomicMax(&fmax[0], fa);
-            atomicMax(&fmax[1], (int)__float_as_uint(bm));  // non-negative floats order as integers
-        }
+        for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+        if (lane == 0) atomicMax(&fmax[1], (int)__float_as_uint(bm));  // non-negative floats order as integers
     }
     __syncthreads();
     if (fmax[1] >= 0x7F800000) {  // the FP32 bound overflowed: FP64 exponent bound (block-uniform branch)
@@ -321,7 +337,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_bse_K3_oz(K3Args3 args, Dims 
         }
         __syncthreads();
     }
-    const int FA = fmax[0];
+    const int FA = fa_blk[rest];
     int FM;
     if (fmax[1] >= 0x7F800000) {
         FM = max(fmax[2] - 1019, 0);
@@ -537,10 +553,19 @@ cudaError_t prepare_bse_K3_oz() {
 // mode 0 (BSE_L_K3), 1 (BSE_K3), 2 (the tangent dK3 = T (dA·M + A·dM) + dγL): mode 2 runs as two
 // launches, each with its own block scales (dA and A need not share a magnitude): the mode-1 kernel
 // on dA with the epilogue term left out, then the A·dM kernel adding T C + dγL into the output
-cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int* err) {
-    if (!k3_oz_supported(d) || mode < 0 || mode > 2) return cudaErrorInvalidValue;
+cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int* err,
+                             int* fa_scratch) {
+    if (!k3_oz_supported(d) || mode < 0 || mode > 2 || !fa_scratch) return cudaErrorInvalidValue;
     const int ntile = (2 * d.N3n + NT - 1) / NT;
-    const unsigned grid = (unsigned)(nslots * a.nblocks * ntile);
+    const unsigned nblk = (unsigned)(nslots * a.nblocks);
+    const unsigned grid = nblk * (unsigned)ntile;
+    auto run = [&](auto kernel, const K3Args3& ka) -> cudaError_t {
+        k_oz_amax<<<nblk, 256, 0, s>>>(ka, d, fa_scratch);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        kernel<<<grid, OZ_THREADS, k3_oz_smem(), s>>>(ka, d, ntile, fa_scratch, err);
+        return cudaGetLastError();
+    };
     if (mode == 2) {
         K3Args3 a1 = a, a3 = a;
         for (int i = 0; i < nslots; ++i) {
@@ -549,16 +574,13 @@ cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nsl
             a1.a[i].flags |= K3F_NOEPI;
             a3.a[i].flags |= K3F_ACC;
         }
-        k_bse_K3_oz<1><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a1, d, ntile, err);
-        const cudaError_t e = cudaGetLastError();
+        // stream order: the second launch's exponent pass overwrites the scratch after the first
+        // contraction has read it
+        const cudaError_t e = run(k_bse_K3_oz<1>, a1);
         if (e != cudaSuccess) return e;
-        k_bse_K3_oz<3><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a3, d, ntile, err);
-    } else if (mode == 1) {
-        k_bse_K3_oz<1><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
-    } else {
-        k_bse_K3_oz<0><<<grid, OZ_THREADS, k3_oz_smem(), s>>>(a, d, ntile, err);
+        return run(k_bse_K3_oz<3>, a3);
     }
-    return cudaGetLastError();
+    return mode == 1 ? run(k_bse_K3_oz<1>, a) : run(k_bse_K3_oz<0>, a);
 }
 
 }  // namespace fdga

@@ -80,6 +80,7 @@ struct fdga_handle {
     int fdpa_single_hartree = 0;  // option: subtract the reference system's Hartree term once
     size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
+    int* oz_fa = nullptr;                        // per-block exponent bounds of the digit-sliced K3 (3 Nq NΩ3)
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
     int k3_tma = 1;                              // ... in the TMA-fed warp-specialised kernel when it fits
     int k3_oz = 2;  // FP64 K3 contractions on the tensor cores (exact digit slicing): 0 never, 1 where supported, 2 also Nν3 ≥ 32
@@ -585,13 +586,13 @@ cudaError_t launch_k3_tensor_cores(fdga_handle* h, cudaStream_t s, int mode, con
 // digit-sliced kernel supports the box, and by default from Nν3 = 32 on (below, the CUDA-core
 // kernel is as fast)
 bool use_k3_oz(const fdga_handle* h) {
-    if (!h->d_err || !k3_oz_supported(h->d)) return false;
+    if (!h->d_err || !h->oz_fa || !k3_oz_supported(h->d)) return false;
     return h->k3_oz == 1 || (h->k3_oz == 2 && h->d.N3n >= 32);
 }
 cudaError_t launch_k3_fp64(fdga_handle* h, cudaStream_t s, int mode, const K3Args3& a3) {
     bool oneloop = false;
     for (int i = 0; i < 3; ++i) oneloop |= (a3.a[i].flags & K3F_1LOOP) != 0;
-    if (use_k3_oz(h) && (mode <= 1 || !oneloop)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err);
+    if (use_k3_oz(h) && (mode <= 1 || !oneloop)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err, h->oz_fa);
     return launch_bse_K3(s, mode, a3, 3, h->d, 0, h->k3_tile[FDGA_FP64][mode < 2 ? mode : 1]);
 }
 
@@ -1871,6 +1872,7 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + nS, d, h->T0tail));
     if (k3_oz_supported(d)) {
         if (!h->d_err) AL(h->d_err, 1);
+        if (!h->oz_fa) AL(h->oz_fa, 3 * (size_t)d.Nq * d.N3O);
         CK(prepare_bse_K3_oz());
     }
     CK(cudaStreamSynchronize(s));
@@ -3406,6 +3408,7 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
         if (value < 0 || value > 2) return fail(h, FDGA_ERR_ARG, "k3_fp64_tensor_cores takes 0, 1 or 2");
         if (value) {
             if (!h->d_err) AL(h->d_err, 1);
+            if (!h->oz_fa) AL(h->oz_fa, 3 * (size_t)h->d.Nq * h->d.N3O);
             CK(prepare_bse_K3_oz());
             CK(cudaStreamSynchronize(h->st));
         }
