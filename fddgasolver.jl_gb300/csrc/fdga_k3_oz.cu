@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256) k_oz_amax(K3Args3 args, Dims d, int* fa_b
 
 template <int MODE>
 __global__ void __launch_bounds__(OZ_THREADS, 2)
-    k_bse_K3_oz(K3Args3 args, Dims d, int ntile, const int* __restrict__ fa_blk, int* err) {
+    k_bse_K3_oz(K3Args3 args, Dims d, int ntile, const int* __restrict__ fa_blk, int ebound, int* err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
@@ -294,6 +294,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
         for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
         if (lane == 0) atomicMax(&fmax[1], (int)__float_as_uint(bm));  // non-negative floats order as integers
     }
+    if (ebound && tid == 0) atomicMax(&fmax[1], 0x7F800000);  // the exponent bound on request (tests)
     __syncthreads();
     if (fmax[1] >= 0x7F800000) {  // the FP32 bound overflowed: FP64 exponent bound (block-uniform branch)
         int fs = 0, nf = 0;
@@ -554,7 +555,7 @@ cudaError_t prepare_bse_K3_oz() {
 // launches, each with its own block scales (dA and A need not share a magnitude): the mode-1 kernel
 // on dA with the epilogue term left out, then the A·dM kernel adding T C + dγL into the output
 cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int* err,
-                             int* fa_scratch) {
+                             int* fa_scratch, int ebound) {
     if (!k3_oz_supported(d) || mode < 0 || mode > 2 || !fa_scratch) return cudaErrorInvalidValue;
     const int ntile = (2 * d.N3n + NT - 1) / NT;
     const unsigned nblk = (unsigned)(nslots * a.nblocks);
@@ -563,7 +564,7 @@ cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nsl
         k_oz_amax<<<nblk, 256, 0, s>>>(ka, d, fa_scratch);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        kernel<<<grid, OZ_THREADS, k3_oz_smem(), s>>>(ka, d, ntile, fa_scratch, err);
+        kernel<<<grid, OZ_THREADS, k3_oz_smem(), s>>>(ka, d, ntile, fa_scratch, ebound, err);
         return cudaGetLastError();
     };
     if (mode == 2) {

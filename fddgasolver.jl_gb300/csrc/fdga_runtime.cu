@@ -83,7 +83,9 @@ struct fdga_handle {
     int* oz_fa = nullptr;                        // per-block exponent bounds of the digit-sliced K3 (3 Nq NΩ3)
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
     int k3_tma = 1;                              // ... in the TMA-fed warp-specialised kernel when it fits
-    int k3_oz = 2;  // FP64 K3 contractions on the tensor cores (exact digit slicing): 0 never, 1 where supported, 2 also Nν3 ≥ 32
+    // FP64 K3 contractions on the tensor cores (exact digit slicing): 0 never, 1 where supported, 2 from
+    // Nν3 = 32 on, 3 as 1 with the FP64 exponent bound of M in every tile (tests)
+    int k3_oz = 2;
     int jvp_tangent = 1;                         // GMRES Jacobian products by the tangent kernels (else differences)
     int newton_cycles = 1;                       // GMRES restart cycles per Newton step
     cplx *Lpp = nullptr, *Lph = nullptr, *SigIn = nullptr, *SigU2 = nullptr, *C0 = nullptr;
@@ -587,12 +589,12 @@ cudaError_t launch_k3_tensor_cores(fdga_handle* h, cudaStream_t s, int mode, con
 // kernel is as fast)
 bool use_k3_oz(const fdga_handle* h) {
     if (!h->d_err || !h->oz_fa || !k3_oz_supported(h->d)) return false;
-    return h->k3_oz == 1 || (h->k3_oz == 2 && h->d.N3n >= 32);
+    return h->k3_oz == 1 || h->k3_oz == 3 || (h->k3_oz == 2 && h->d.N3n >= 32);
 }
 cudaError_t launch_k3_fp64(fdga_handle* h, cudaStream_t s, int mode, const K3Args3& a3) {
     bool oneloop = false;
     for (int i = 0; i < 3; ++i) oneloop |= (a3.a[i].flags & K3F_1LOOP) != 0;
-    if (use_k3_oz(h) && (mode <= 1 || !oneloop)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err, h->oz_fa);
+    if (use_k3_oz(h) && (mode <= 1 || !oneloop)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err, h->oz_fa, h->k3_oz == 3);
     return launch_bse_K3(s, mode, a3, 3, h->d, 0, h->k3_tile[FDGA_FP64][mode < 2 ? mode : 1]);
 }
 
@@ -3405,7 +3407,7 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
         return FDGA_OK;
     }
     if (h && key && std::string(key) == "k3_fp64_tensor_cores") {
-        if (value < 0 || value > 2) return fail(h, FDGA_ERR_ARG, "k3_fp64_tensor_cores takes 0, 1 or 2");
+        if (value < 0 || value > 3) return fail(h, FDGA_ERR_ARG, "k3_fp64_tensor_cores takes 0, 1, 2 or 3");
         if (value) {
             if (!h->d_err) AL(h->d_err, 1);
             if (!h->oz_fa) AL(h->oz_fa, 3 * (size_t)h->d.Nq * h->d.N3O);

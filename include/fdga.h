@@ -129,7 +129,9 @@ int fdga_set_precision(fdga_handle* h, int precision);
  * the tensor cores by exact digit slicing of the FP64 operands (8 BF16 digits of 7 bits, products
  * summed by diagonal in FP32 tensor memory, joined exactly; FP64-level results, ~1e-14 relative
  * to the CUDA-core FP64 GEMM) when Nν3 is a multiple of 8 between 8 and 128: 2 from Nν3 = 32 on,
- * 1 at every such Nν3, 0 never (FP64 CUDA-core GEMMs). */
+ * 1 at every such Nν3, 0 never (FP64 CUDA-core GEMMs); 3 as 1 with every tile of M bounded from
+ * the FP64 exponents of its factors, the path otherwise taken only when its FP32 bound overflows
+ * (for tests). */
 int fdga_set_option(fdga_handle* h, const char* key, int value);
 
 /* fixed_point!(R, x, S) (src/solve.jl:119-157): unflatten x, iterate, R = flatten(S) - x.

@@ -82,7 +82,30 @@ def test_default_follows_the_box():
     gpu.set_option("k3_fp64_tensor_cores", 0)
     assert gpu.query("k3_fp64_tensor_cores") == 0
     with pytest.raises(Exception):
-        gpu.set_option("k3_fp64_tensor_cores", 3)
+        gpu.set_option("k3_fp64_tensor_cores", 4)
+    gpu.close()
+
+
+@pytest.mark.parametrize("cfg", [NL24, NL32, LOCAL80], ids=["nl24", "nl32", "local80"])
+def test_digit_sliced_k3_exponent_bound(cfg):
+    """The bound of M from the FP64 exponents of its factors (a few bits looser than the FP32 bound,
+    taken when that bound overflows) keeps the map within 1e-12 of the CUDA-core GEMMs; the
+    tangent's two launches take it as well."""
+    rng = np.random.default_rng(25)
+    gpu = make_gpu(cfg, True)
+    y = _state(gpu, rng, "fdPA")
+    v = rng.standard_normal(y.size) + 1j * rng.standard_normal(y.size)
+    gpu.set_option("k3_fp64_tensor_cores", 0)
+    y_cc = gpu.fixed_point(y, "fdPA") + y
+    gpu.unflatten(y)
+    _, j_cc = gpu.frule(v)
+    gpu.set_option("k3_fp64_tensor_cores", 3)
+    assert gpu.query("k3_fp64_tensor_cores") == 1
+    y_eb = gpu.fixed_point(y, "fdPA") + y
+    gpu.unflatten(y)
+    _, j_eb = gpu.frule(v)
+    assert blockwise_rel_err(cfg, y_eb, y_cc) < 1e-12
+    assert blockwise_rel_err(cfg, j_eb, j_cc) < 1e-12
     gpu.close()
 
 
