@@ -576,8 +576,11 @@ __global__ void k_adj_build_M(K3Args3 args, int mode, Ptr3 Mout, Dims d) {
     }
     Mout.p[slot][base + (size_t)k * N + col] = v;
 }
-// batched C[b] = α op(A[b]) op(B[b]) over the listed N x N blocks (op: 0 = as is, 1 = conjugate transpose);
-// slot = blockIdx.z, 16 x 16 tiles
+// batched C[b] = α op(A[b]) op(B[b]) (C += when accumulating) over the listed N x N blocks, op: 0 = as
+// is, 1 = conjugate transpose; slot = blockIdx.z.  TILE x TILE output tiles (TILE = 16, 24 or 32 by N,
+// as the forward K3 GEMM picks them, so that no block is padded beyond its size), 2 x 2 outputs per
+// thread, K chunks of 8, and the forward GEMM's three-multiplication complex product:
+// t1 = Σ ar br, t2 = Σ ai bi, t3 = Σ (ar + ai)(br + bi), C = (t1 - t2) + i (t3 - t1 - t2).
 struct GemmBatch {
     const cplx* A[3];
     const cplx* B[3];
@@ -587,45 +590,87 @@ struct GemmBatch {
     const int* blocks;
     int nblocks;
 };
-template <int OPA, int OPB>
-__global__ void k_adj_gemm(GemmBatch g, Dims d) {
-    constexpr int TS = 16;
-    __shared__ cplx As[TS][TS + 1], Bs[TS][TS + 1];
+template <int OPA, int OPB, int TILE>
+__global__ void __launch_bounds__((TILE / 2) * (TILE / 2)) k_adj_gemm(GemmBatch g, Dims d) {
+    constexpr int TK = 8, H = TILE / 2, NT = H * H;
+    __shared__ cplx As[TILE][TK + 1];
+    __shared__ cplx Bs[TK][TILE + 1];
+    __shared__ double Asum[TILE][TK + 1], Bsum[TK][TILE + 1];
     const int N = d.N3n;
     const int slot = blockIdx.z;
-    const int nt = (N + TS - 1) / TS;
+    const int nt = (N + TILE - 1) / TILE;
     const int bidx = blockIdx.x / (nt * nt), tile = blockIdx.x % (nt * nt);
     const int blk = g.blocks ? g.blocks[bidx] : bidx;
     const size_t base = (size_t)blk * N * N;
-    const int row0 = (tile / nt) * TS, col0 = (tile % nt) * TS;
-    const int tx = threadIdx.x % TS, ty = threadIdx.x / TS;
-    const cplx* A = g.A[slot] + base;
-    const cplx* B = g.B[slot] + base;
-    cplx acc = mk(0, 0);
-    for (int k0 = 0; k0 < N; k0 += TS) {
-        {  // As[ty][tx] = op(A)[row0 + ty][k0 + tx]
-            const int r = row0 + ty, k = k0 + tx;
+    const int row0 = (tile / nt) * TILE, col0 = (tile % nt) * TILE;
+    const int tid = threadIdx.x, tx = tid % H, ty = tid / H;
+    // the slot's operands, chosen without indexing the parameter arrays by a run-time value (which
+    // would copy the parameters to local memory)
+    const cplx* A = (slot == 0 ? g.A[0] : slot == 1 ? g.A[1] : g.A[2]) + base;
+    const cplx* B = (slot == 0 ? g.B[0] : slot == 1 ? g.B[1] : g.B[2]) + base;
+    double t1[2][2] = {{0, 0}, {0, 0}}, t2[2][2] = {{0, 0}, {0, 0}}, t3[2][2] = {{0, 0}, {0, 0}};
+    for (int k0 = 0; k0 < N; k0 += TK) {
+        for (int e = tid; e < TILE * TK; e += NT) {
+            // op(A)[r][k]: as is, k runs along memory; conjugate transpose, r does
+            const int r = OPA ? e % TILE : e / TK, kk = OPA ? e / TILE : e % TK;
+            const int gr = row0 + r, gk = k0 + kk;
             cplx v = mk(0, 0);
-            if (r < N && k < N) v = OPA ? cj(A[(size_t)k * N + r]) : A[(size_t)r * N + k];
-            As[ty][tx] = v;
+            if (gr < N && gk < N) v = OPA ? cj(A[(size_t)gk * N + gr]) : A[(size_t)gr * N + gk];
+            As[r][kk] = v;
+            Asum[r][kk] = v.x + v.y;
         }
-        {  // Bs[ty][tx] = op(B)[k0 + ty][col0 + tx]
-            const int k = k0 + ty, c = col0 + tx;
+        for (int e = tid; e < TK * TILE; e += NT) {
+            // op(B)[k][c]: as is, c runs along memory; conjugate transpose, k does
+            const int kk = OPB ? e % TK : e / TILE, c = OPB ? e / TK : e % TILE;
+            const int gk = k0 + kk, gc = col0 + c;
             cplx v = mk(0, 0);
-            if (k < N && c < N) v = OPB ? cj(B[(size_t)c * N + k]) : B[(size_t)k * N + c];
-            Bs[ty][tx] = v;
+            if (gk < N && gc < N) v = OPB ? cj(B[(size_t)gc * N + gk]) : B[(size_t)gk * N + gc];
+            Bs[kk][c] = v;
+            Bsum[kk][c] = v.x + v.y;
         }
         __syncthreads();
 #pragma unroll
-        for (int kk = 0; kk < TS; ++kk) acc = cfma(As[ty][kk], Bs[kk][tx], acc);
+        for (int kk = 0; kk < TK; ++kk) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const cplx av = As[ty + H * i][kk];
+                const double sa = Asum[ty + H * i][kk];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const cplx bv = Bs[kk][tx + H * j];
+                    t1[i][j] = fma(av.x, bv.x, t1[i][j]);
+                    t2[i][j] = fma(av.y, bv.y, t2[i][j]);
+                    t3[i][j] = fma(sa, Bsum[kk][tx + H * j], t3[i][j]);
+                }
+            }
+        }
         __syncthreads();
     }
-    const int r = row0 + ty, c = col0 + tx;
-    if (r < N && c < N) {
-        cplx* C = g.C[slot] + base + (size_t)r * N + c;
-        const cplx v = acc * g.alpha[slot];
-        *C = g.accumulate ? *C + v : v;
-    }
+    const double alpha = slot == 0 ? g.alpha[0] : slot == 1 ? g.alpha[1] : g.alpha[2];
+    cplx* Cb = (slot == 0 ? g.C[0] : slot == 1 ? g.C[1] : g.C[2]) + base;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int r = row0 + ty + H * i, c = col0 + tx + H * j;
+            if (r < N && c < N) {
+                cplx* C = Cb + (size_t)r * N + c;
+                const cplx v = cplx{t1[i][j] - t2[i][j], t3[i][j] - (t1[i][j] + t2[i][j])} * alpha;
+                *C = g.accumulate ? *C + v : v;
+            }
+        }
+}
+template <int OPA, int OPB, int TILE>
+void launch_adj_gemm_tile(cudaStream_t s, const GemmBatch& g, const Dims& d) {
+    const int nt = (d.N3n + TILE - 1) / TILE;
+    const dim3 grid((unsigned)(g.nblocks * nt * nt), 1, 3);
+    k_adj_gemm<OPA, OPB, TILE><<<grid, (TILE / 2) * (TILE / 2), 0, s>>>(g, d);
+}
+template <int OPA, int OPB>
+void launch_adj_gemm(cudaStream_t s, const GemmBatch& g, const Dims& d) {
+    if (d.N3n <= 16) launch_adj_gemm_tile<OPA, OPB, 16>(s, g, d);
+    else if (d.N3n <= 24) launch_adj_gemm_tile<OPA, OPB, 24>(s, g, d);
+    else launch_adj_gemm_tile<OPA, OPB, 32>(s, g, d);
 }
 // mode 1: M̄ -> Π̄ (row sums), Γ̄s, γ̄L (box) and the epilogue γ̄L(ν,ν') += ō; warp per (slot, block, ω)
 __global__ void k_adj_distribute_M(K3Args3 args, Ptr3 Mbar, Ptr3 Obar, Ptr3 Gbar, cplx* Pbpp, cplx* Pbph, cplx* FLb0,
@@ -860,7 +905,6 @@ cudaError_t launch_adj_K3(cudaStream_t s, int mode, const K3Args3& a, const cplx
     const Ptr3 mo{{Mbuf[0], Mbuf[1], Mbuf[2]}};  // slot pointers travel by value
     k_adj_build_M<<<dim3(nb((size_t)a.nblocks * bs, 256), 3), 256, 0, s>>>(a, mode, mo, d);
     LCHK();
-    const int nt = (N + 15) / 16;
     const double T = d.T;
     GemmBatch g{};
     g.blocks = a.blocks;
@@ -873,8 +917,7 @@ cudaError_t launch_adj_K3(cudaStream_t s, int mode, const K3Args3& a, const cplx
         g.alpha[i] = mode == 0 ? T * ((ch == CH_A) ? 1.0 : -1.0) : T;
     }
     g.accumulate = 1;
-    dim3 grid((unsigned)(a.nblocks * nt * nt), 1, 3);
-    k_adj_gemm<0, 1><<<grid, 256, 0, s>>>(g, d);  // Ā += α ō Mᴴ
+    launch_adj_gemm<0, 1>(s, g, d);  // Ā += α ō Mᴴ
     LCHK();
     if (mode == 0) return cudaSuccess;
     GemmBatch h{};
@@ -887,7 +930,7 @@ cudaError_t launch_adj_K3(cudaStream_t s, int mode, const K3Args3& a, const cplx
         h.alpha[i] = T;
     }
     h.accumulate = 0;
-    k_adj_gemm<1, 0><<<grid, 256, 0, s>>>(h, d);  // M̄ = T Aᴴ ō
+    launch_adj_gemm<1, 0>(s, h, d);  // M̄ = T Aᴴ ō
     LCHK();
     const Ptr3 mb{{Mbar[0], Mbar[1], Mbar[2]}};
     const Ptr3 ob{{const_cast<cplx*>(Obar[0]), const_cast<cplx*>(Obar[1]), const_cast<cplx*>(Obar[2])}};
