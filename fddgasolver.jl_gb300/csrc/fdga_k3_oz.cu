@@ -28,10 +28,17 @@
 // then the BSE's epilogue (T C and γL), as the FP64 kernel does.  A block of A or tile of M that
 // holds an infinity or NaN writes NaN, as the FP64 sum would.
 //
-// One CTA of 256 threads per (channel slot, block, column tile); K in chunks of 16 (8 ω), two
-// shared-memory stages of 8 + 8 digit operands; 36 MMAs (kind::f16, BF16 inputs, FP32 accumulation)
-// per chunk issued by one thread, tcgen05.commit -> mbarrier; every wait bounded (a timeout sets
-// *err and the kernel still releases its tensor memory).
+// Per launch: k_oz_amax finds F_A of every A block; k_oz_adigits writes the A digit operands of a
+// group of blocks to a global buffer, once per block, in the shared-memory operand layout; then the
+// contraction runs one CTA of 256 threads per (channel slot, block, column tile), K in chunks of 16
+// (8 ω) with two shared-memory stages of 8 + 8 digit operands.  Per chunk one thread bulk-copies the
+// 8 A digit operands (cp.async.bulk, completing on an mbarrier) while warps 4-7 form the tile of M
+// in FP64 and digitise it; then the same thread issues the 36 MMAs (kind::f16, BF16 inputs, FP32
+// accumulation) and commits them to the stage's mbarrier.  Every wait is bounded (a timeout sets
+// *err; the kernel still waits, bounded, for its copies and MMAs in flight and releases its tensor
+// memory).
+#include <algorithm>
+
 #include "fdga_kernels.h"
 
 namespace fdga {
@@ -70,6 +77,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         if (ok) return true;
     }
     return false;
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// global -> shared bulk copy (16-byte aligned addresses, a multiple of 16 bytes), completing on bar
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
 }
 __device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
     asm volatile(
@@ -159,11 +175,46 @@ __global__ void __launch_bounds__(256) k_oz_amax(K3Args3 args, Dims d, int* fa_b
     }
 }
 
+// The A digit operands of the blocks r0, r0 + 1, ..: per block and chunk of 8 ω, S digit operands of
+// the block's N rows in the K-major no-swizzle layout of op16 (N·32 bytes each, rows ≥ N left out),
+// digitised once here instead of once per column tile; the contraction copies them into shared
+// memory.  One CTA per (block, chunk); thread e < 2N holds row e/2 and the four ω 4(e%2)...
+__global__ void __launch_bounds__(256) k_oz_adigits(K3Args3 args, Dims d, const int* __restrict__ fa_blk, uint8_t* adig,
+                                                    int r0) {
+    const int N = d.N3n, nchunks = N / CW;
+    const int rr = blockIdx.x / nchunks, c = blockIdx.x % nchunks;
+    const int rest = r0 + rr, nb = args.nblocks;
+    const int slot = rest / nb, bi = rest % nb;
+    const int blk = args.blocks ? args.blocks[bi] : bi;
+    const int e = threadIdx.x;
+    if (e >= 2 * N) return;
+    const int FA = fa_blk[rest];
+    const int row = e >> 1, quad = e & 1;
+    const cplx* A = slot == 0 ? args.a[0].A : slot == 1 ? args.a[1].A : args.a[2].A;
+    const cplx* src = A + (size_t)blk * N * N + (size_t)row * N + CW * c + 4 * quad;
+    uint32_t wd[S][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const cplx v = ldg(src + i);
+        const unsigned long long yr = fixed56(v.x, FA), yi = fixed56(v.y, FA);
+        const uint32_t sg = (sbit(v.x) << 15) | (sbit(v.y) << 31);
+#pragma unroll
+        for (int s = 0; s < S; ++s) wd[s][i] = bf_pair(digit(yr, s), digit(yi, s), sg);
+    }
+    const size_t arow = (size_t)N * 32;
+    uint8_t* dst = adig + ((size_t)rr * nchunks + c) * S * arow + op16(row, 8 * quad);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+        *reinterpret_cast<uint4*>(dst + (size_t)s * arow) = make_uint4(wd[s][0], wd[s][1], wd[s][2], wd[s][3]);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(OZ_THREADS, 2)
-    k_bse_K3_oz(K3Args3 args, Dims d, int ntile, const int* __restrict__ fa_blk, int ebound, int* err) {
+    k_bse_K3_oz(K3Args3 args, Dims d, int ntile, const int* __restrict__ fa_blk, const uint8_t* __restrict__ adig,
+                int r0, int ebound, int* err) {
     extern __shared__ __align__(1024) uint8_t sm[];
-    __shared__ uint64_t mbar[2];
+    __shared__ uint64_t mbar[2];   // per stage: the chunk's MMAs are done (tcgen05.commit)
+    __shared__ uint64_t afull[2];  // per stage: the chunk's A digit operands have arrived
     __shared__ uint32_t tmem_base;
     // the ω factors of M with their signs: [0] Π0 (mode 0), s1 (Π - Π0) (mode 1) or s1 dΠ (mode 3),
     // [1] s1 Π, and the exponent bounds of [0] and of Π
@@ -178,7 +229,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
     const int nchunks = N / CW;  // N is a multiple of 8
     const int nb = args.nblocks;
     const int tile = blockIdx.x % ntile;
-    const int rest = blockIdx.x / ntile;
+    const int rest = r0 + (int)(blockIdx.x / ntile);
     const int slot = rest / nb;
     const int blk = args.blocks ? args.blocks[rest % nb] : (int)(rest % nb);
     const K3Args& a = args.a[slot];
@@ -214,8 +265,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
     }
     if (tid < 4) fmax[tid] = 0;
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
+        for (int i = 0; i < 2; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[i])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&afull[i])) : "memory");
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -350,19 +403,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
     const bool nonfinite = FA == 0x7ff || fmax[3] != 0;
     // instruction descriptor: D FP32, A and B BF16, both K-major, N = ncol, M = 128
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(ncol >> 3) << 17) | ((128u >> 4) << 24);
-    // A staging: thread tid holds row anu and the four ω 4·aq.. of the chunk (one 16-byte store per
-    // digit; eight threads cover 128 contiguous bytes)
-    const int aq = (tid >> 3) & 1, anu = (tid & 7) | ((tid >> 4) << 3);
     // shared-memory descriptors of the first A and B digit operands of stage 0 (the start address
     // field, bits 0-13, takes the byte offsets of the other operands >> 4 without carry: all of the
     // shared memory lies below 2^18 bytes)
     const uint64_t dA0 = sdesc16(smem_u32(sm)), dB0 = sdesc16(smem_u32(sm) + S * A_DIG);
-    // the A entries of the next chunk are loaded one chunk ahead
-    const cplx* asrc = a.A + base + (size_t)anu * N + 4 * aq;
-    cplx an[4];
-    if (anu < N) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) an[i] = ldg(asrc + i);
+    // A digit operands (k_oz_adigits) arrive by bulk copies of the N rows of each digit; rows N..127
+    // of both stages are zero, written once here (the tail of each operand from byte N·32 on)
+    const uint32_t arow = (uint32_t)N * 32u;
+    const uint8_t* asrc = adig + (size_t)(rest - r0) * nchunks * S * arow;
+    {
+        const int per = (A_DIG - (int)arow) / 16;  // 16-byte words per digit operand tail
+        for (int e = tid; e < 2 * S * per; e += OZ_THREADS) {
+            const int op = e / per, wdx = e % per;
+            uint8_t* stg = sm + (size_t)(op / S) * STAGE + (size_t)(op % S) * A_DIG;
+            *reinterpret_cast<uint4*>(stg + arow + 16 * wdx) = make_uint4(0u, 0u, 0u, 0u);
+        }
     }
     bool ok = true;
     for (int c = 0; c < nchunks; ++c) {
@@ -371,33 +426,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
         uint8_t* Ad = sm + (size_t)st * STAGE;  // S A digit operands, then S B digit operands
         uint8_t* Bd = Ad + S * A_DIG;
         const int w0 = CW * c;
-        {
-            // A: row ν, k = 2ω_l holds Re A, 2ω_l + 1 holds Im A (rows ≥ N are zero)
-            uint32_t wd[S][4];
-            if (anu < N) {
-                cplx av[4];
+        if (tid == 0) {  // A: row ν, k = 2ω_l holds Re A, 2ω_l + 1 holds Im A
+            const uint32_t bar = smem_u32(&afull[st]);
+            mbar_expect_tx(bar, (uint32_t)S * arow);
+            const uint8_t* src = asrc + (size_t)c * S * arow;
 #pragma unroll
-                for (int i = 0; i < 4; ++i) av[i] = an[i];
-                if (c + 1 < nchunks) {
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) an[i] = ldg(asrc + w0 + CW + i);
-                }
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const cplx v = av[i];
-                    const unsigned long long yr = fixed56(v.x, FA), yi = fixed56(v.y, FA);
-                    const uint32_t sg = (sbit(v.x) << 15) | (sbit(v.y) << 31);
-#pragma unroll
-                    for (int s = 0; s < S; ++s) wd[s][i] = bf_pair(digit(yr, s), digit(yi, s), sg);
-                }
-            } else {
-#pragma unroll
-                for (int s = 0; s < S; ++s) wd[s][0] = wd[s][1] = wd[s][2] = wd[s][3] = 0u;
-            }
-            const uint32_t off = op16(anu, 8 * aq);
-#pragma unroll
-            for (int s = 0; s < S; ++s)
-                *reinterpret_cast<uint4*>(Ad + (size_t)s * A_DIG + off) = make_uint4(wd[s][0], wd[s][1], wd[s][2], wd[s][3]);
+            for (int s = 0; s < S; ++s) bulk_g2s(smem_u32(Ad + (size_t)s * A_DIG), src + (size_t)s * arow, arow, bar);
         }
         // B (rows n = 2ν'_l + p of the tile, k = 2ω_l + q): row 2ν'_l holds [Re M, -Im M], row
         // 2ν'_l + 1 holds [Im M, Re M]; M formed in FP64 as the CUDA-core kernel forms it.  Warps 4-7
@@ -446,6 +480,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
+            if (!mbar_wait(smem_u32(&afull[st]), (c >> 1) & 1)) ok = false;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint64_t so = (uint64_t)((st * STAGE) >> 4);
 #pragma unroll
@@ -468,7 +503,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
     if (!ok) {
         // a wait gave up: report it, and give the MMAs in flight one more bounded wait before the
         // tensor memory is released
-        if (tid == 0) atomicExch(err, 1);
+        if (tid == 0) {
+            atomicExch(err, 1);
+            // and for the A copies in flight (issued by this thread), likewise bounded
+            mbar_wait(smem_u32(&afull[(nchunks - 1) & 1]), ((nchunks - 1) >> 1) & 1);
+            if (nchunks >= 2) mbar_wait(smem_u32(&afull[nchunks & 1]), ((nchunks - 2) >> 1) & 1);
+        }
         mbar_wait(last_bar, last_par);
     } else if (32 * q < N && 16 * h < ncol) {
         // epilogue: warp w reads TMEM lanes 32(w%4).. (rows ν) and the 16-column half w/4 of the
@@ -555,17 +595,26 @@ cudaError_t prepare_bse_K3_oz() {
 // launches, each with its own block scales (dA and A need not share a magnitude): the mode-1 kernel
 // on dA with the epilogue term left out, then the A·dM kernel adding T C + dγL into the output
 cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int* err,
-                             int* fa_scratch, int ebound) {
-    if (!k3_oz_supported(d) || mode < 0 || mode > 2 || !fa_scratch) return cudaErrorInvalidValue;
-    const int ntile = (2 * d.N3n + NT - 1) / NT;
-    const unsigned nblk = (unsigned)(nslots * a.nblocks);
-    const unsigned grid = nblk * (unsigned)ntile;
+                             int* fa_scratch, uint8_t* adig, int adig_blocks, int ebound) {
+    if (!k3_oz_supported(d) || mode < 0 || mode > 2 || !fa_scratch || !adig || adig_blocks < 1)
+        return cudaErrorInvalidValue;
+    const int ntile = (2 * d.N3n + NT - 1) / NT, nchunks = d.N3n / CW;
+    const int nblk = nslots * a.nblocks;
+    // per launch: the blocks' exponent bounds, then groups of at most adig_blocks blocks (the size
+    // of the digit buffer), each digitised and contracted in stream order
     auto run = [&](auto kernel, const K3Args3& ka) -> cudaError_t {
         k_oz_amax<<<nblk, 256, 0, s>>>(ka, d, fa_scratch);
         cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        kernel<<<grid, OZ_THREADS, k3_oz_smem(), s>>>(ka, d, ntile, fa_scratch, ebound, err);
-        return cudaGetLastError();
+        for (int r0 = 0; e == cudaSuccess && r0 < nblk; r0 += adig_blocks) {
+            const int cnt = std::min(adig_blocks, nblk - r0);
+            k_oz_adigits<<<(unsigned)(cnt * nchunks), 256, 0, s>>>(ka, d, fa_scratch, adig, r0);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) break;
+            kernel<<<(unsigned)(cnt * ntile), OZ_THREADS, k3_oz_smem(), s>>>(ka, d, ntile, fa_scratch, adig, r0, ebound,
+                                                                            err);
+            e = cudaGetLastError();
+        }
+        return e;
     };
     if (mode == 2) {
         K3Args3 a1 = a, a3 = a;
@@ -575,7 +624,7 @@ cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nsl
             a1.a[i].flags |= K3F_NOEPI;
             a3.a[i].flags |= K3F_ACC;
         }
-        // stream order: the second launch's exponent pass overwrites the scratch after the first
+        // stream order: the second launch's passes overwrite the scratch after the first
         // contraction has read it
         const cudaError_t e = run(k_bse_K3_oz<1>, a1);
         if (e != cudaSuccess) return e;
@@ -583,5 +632,7 @@ cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nsl
     }
     return mode == 1 ? run(k_bse_K3_oz<1>, a) : run(k_bse_K3_oz<0>, a);
 }
+
+size_t k3_oz_digit_bytes(const Dims& d) { return (size_t)32 * d.N3n * d.N3n; }
 
 }  // namespace fdga

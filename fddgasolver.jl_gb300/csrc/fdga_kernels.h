@@ -344,13 +344,15 @@ cudaError_t launch_bse_K2_mfrg(cudaStream_t s, const VertP& F, const FLP& FL, co
                                const Dims& d);
 cudaError_t launch_scale(cudaStream_t s, cplx* out, const cplx* in, double sc, size_t n);
 // FP64 K3 contractions on the tensor cores by exact BF16 digit slicing (fdga_k3_oz.cu), modes 0, 1
-// and 2 (the tangent); fa_scratch holds nslots x nblocks ints (per-block exponent bounds); ebound
-// = 1 bounds every tile of M from the FP64 exponents of its factors (the path taken when the FP32
-// magnitude bound overflows), for tests
+// and 2 (the tangent); fa_scratch holds nslots x nblocks ints (per-block exponent bounds), adig the
+// A digit operands of adig_blocks blocks (k3_oz_digit_bytes each); ebound = 1 bounds every tile of
+// M from the FP64 exponents of its factors (the path taken when the FP32 magnitude bound
+// overflows), for tests
 bool k3_oz_supported(const Dims& d);
+size_t k3_oz_digit_bytes(const Dims& d);
 cudaError_t prepare_bse_K3_oz();
 cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nslots, const Dims& d, int* err,
-                             int* fa_scratch, int ebound);
+                             int* fa_scratch, uint8_t* adig, int adig_blocks, int ebound);
 cudaError_t launch_cache_broadcast(cudaStream_t s, cplx* c0, cplx* c1, cplx* c2, const uint32_t* map, size_t n);
 cudaError_t launch_cache_broadcast(cudaStream_t s, cplxf* c0, cplxf* c1, cplxf* c2, const uint32_t* map, size_t n);
 // GMRES building blocks (real inner products on the FP32 Krylov basis)

@@ -81,6 +81,8 @@ struct fdga_handle {
     size_t navg = 0;
     int* d_err = nullptr;                        // device error flag of bounded in-kernel waits
     int* oz_fa = nullptr;                        // per-block exponent bounds of the digit-sliced K3 (3 Nq NΩ3)
+    uint8_t* oz_adig = nullptr;                  // A digit operands of oz_adig_blocks blocks (at most 512 MB)
+    int oz_adig_blocks = 0;
     int k3_tc = 1;                               // mixed K3 contractions on the tensor cores when supported
     int k3_tma = 1;                              // ... in the TMA-fed warp-specialised kernel when it fits
     // FP64 K3 contractions on the tensor cores (exact digit slicing): 0 never, 1 where supported, 2 from
@@ -234,6 +236,21 @@ int ensure_mixed(fdga_handle* h) {
     return FDGA_OK;
 }
 // a tensor-core wait that timed out inside a kernel (bounded polling) is reported here
+// scratch of the digit-sliced K3: per-block exponent bounds and a digit buffer for up to 512 MB of
+// blocks (larger launches run in groups)
+int ensure_k3_oz(fdga_handle* h) {
+    const Dims& d = h->d;
+    const size_t nblk = 3 * (size_t)d.Nq * d.N3O;
+    if (!h->d_err) AL(h->d_err, 1);
+    if (!h->oz_fa) AL(h->oz_fa, nblk);
+    if (!h->oz_adig) {
+        const size_t per = k3_oz_digit_bytes(d);
+        const size_t cap = std::max<size_t>(1, std::min(nblk, ((size_t)512 << 20) / per));
+        AL(h->oz_adig, cap * per);
+        h->oz_adig_blocks = (int)cap;
+    }
+    return FDGA_OK;
+}
 int check_device_error(fdga_handle* h) {
     if (!h->d_err) return FDGA_OK;
     int v = 0;
@@ -588,13 +605,14 @@ cudaError_t launch_k3_tensor_cores(fdga_handle* h, cudaStream_t s, int mode, con
 // digit-sliced kernel supports the box, and by default from Nν3 = 32 on (below, the CUDA-core
 // kernel is as fast)
 bool use_k3_oz(const fdga_handle* h) {
-    if (!h->d_err || !h->oz_fa || !k3_oz_supported(h->d)) return false;
+    if (!h->d_err || !h->oz_fa || !h->oz_adig || !k3_oz_supported(h->d)) return false;
     return h->k3_oz == 1 || h->k3_oz == 3 || (h->k3_oz == 2 && h->d.N3n >= 32);
 }
 cudaError_t launch_k3_fp64(fdga_handle* h, cudaStream_t s, int mode, const K3Args3& a3) {
     bool oneloop = false;
     for (int i = 0; i < 3; ++i) oneloop |= (a3.a[i].flags & K3F_1LOOP) != 0;
-    if (use_k3_oz(h) && (mode <= 1 || !oneloop)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err, h->oz_fa, h->k3_oz == 3);
+    if (use_k3_oz(h) && (mode <= 1 || !oneloop)) return launch_bse_K3_oz(s, mode, a3, 3, h->d, h->d_err, h->oz_fa, h->oz_adig, h->oz_adig_blocks,
+                                                                h->k3_oz == 3);
     return launch_bse_K3(s, mode, a3, 3, h->d, 0, h->k3_tile[FDGA_FP64][mode < 2 ? mode : 1]);
 }
 
@@ -1873,8 +1891,7 @@ int fdga_finalize(fdga_handle* h) {
     CK(launch_bubble(s, h->G, h->GR, h->Pipp, h->Piph, h->twp, d));
     CK(launch_rowsum(s, h->Pipp, h->Piph, h->GR, h->SRtmp, h->twp, h->SPi, h->SPi + nS, d, h->T0tail));
     if (k3_oz_supported(d)) {
-        if (!h->d_err) AL(h->d_err, 1);
-        if (!h->oz_fa) AL(h->oz_fa, 3 * (size_t)d.Nq * d.N3O);
+        if (int r = ensure_k3_oz(h)) return r;
         CK(prepare_bse_K3_oz());
     }
     CK(cudaStreamSynchronize(s));
@@ -3408,9 +3425,8 @@ int fdga_set_option(fdga_handle* h, const char* key, int value) {
     }
     if (h && key && std::string(key) == "k3_fp64_tensor_cores") {
         if (value < 0 || value > 3) return fail(h, FDGA_ERR_ARG, "k3_fp64_tensor_cores takes 0, 1, 2 or 3");
-        if (value) {
-            if (!h->d_err) AL(h->d_err, 1);
-            if (!h->oz_fa) AL(h->oz_fa, 3 * (size_t)h->d.Nq * h->d.N3O);
+        if (value && k3_oz_supported(h->d)) {
+            if (int r = ensure_k3_oz(h)) return r;
             CK(prepare_bse_K3_oz());
             CK(cudaStreamSynchronize(h->st));
         }
