@@ -28,8 +28,8 @@
 // then the BSE's epilogue (T C and γL), as the FP64 kernel does.  A block of A or tile of M that
 // holds an infinity or NaN writes NaN, as the FP64 sum would.
 //
-// Per launch: k_oz_amax finds F_A of every A block; k_oz_adigits writes the A digit operands of a
-// group of blocks to a global buffer, once per block, in the shared-memory operand layout; then the
+// Per launch and group of blocks: k_oz_adigits finds F_A of every A block and writes its digit
+// operands to a global buffer, once per block, in the shared-memory operand layout; then the
 // contraction runs one CTA of 256 threads per (channel slot, block, column tile), K in chunks of 16
 // (8 ω) with two shared-memory stages of 8 + 8 digit operands.  Per chunk one thread bulk-copies the
 // 8 A digit operands (cp.async.bulk, completing on an mbarrier) while warps 4-7 form the tile of M
@@ -155,57 +155,46 @@ __device__ __forceinline__ double i2d_scaled(long long x, int e) {
     return __longlong_as_double((long long)(sg | ((unsigned long long)ef << 52) | mant));
 }
 
-// F_A of every A block: the largest exponent field of its entries (both parts), one CTA per
-// (channel slot, block) in the contraction's block order; every column tile of the block reads it
-__global__ void __launch_bounds__(256) k_oz_amax(K3Args3 args, Dims d, int* fa_blk) {
+// The A digit operands of the blocks r0, r0 + 1, ..: one CTA per block finds F_A, the largest
+// exponent field of the block's entries (both parts; stored in fa_blk for the contraction), then
+// writes, per chunk of 8 ω, S digit operands of the block's N rows in the K-major no-swizzle layout
+// of op16 (N·32 bytes each, rows ≥ N left out).  Each A block is so read and digitised once, not once
+// per column tile; the contraction copies the operands into shared memory.  Item e = (chunk, row,
+// quad) holds row `row` and the four ω 4·quad.. of the chunk.
+__global__ void __launch_bounds__(256) k_oz_adigits(K3Args3 args, Dims d, int* __restrict__ fa_blk, uint8_t* adig,
+                                                    int r0) {
     __shared__ int wmax[8];
-    const int nb = args.nblocks;
-    const int slot = blockIdx.x / nb, bi = blockIdx.x % nb;
+    const int N = d.N3n, nchunks = N / CW;
+    const int rr = blockIdx.x, rest = r0 + rr, nb = args.nblocks;
+    const int slot = rest / nb, bi = rest % nb;
     const int blk = args.blocks ? args.blocks[bi] : bi;
-    const int N = d.N3n;
-    const cplx* A = args.a[slot].A + (size_t)blk * N * N;
+    const cplx* A = (slot == 0 ? args.a[0].A : slot == 1 ? args.a[1].A : args.a[2].A) + (size_t)blk * N * N;
     int mx = 0;
     for (int e = threadIdx.x; e < N * N; e += 256) mx = max(mx, cexpo(ldg(A + e)));
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < 8; ++w) mx = max(mx, wmax[w]);
-        fa_blk[blockIdx.x] = mx;
-    }
-}
-
-// The A digit operands of the blocks r0, r0 + 1, ..: per block and chunk of 8 ω, S digit operands of
-// the block's N rows in the K-major no-swizzle layout of op16 (N·32 bytes each, rows ≥ N left out),
-// digitised once here instead of once per column tile; the contraction copies them into shared
-// memory.  One CTA per (block, chunk); thread e < 2N holds row e/2 and the four ω 4(e%2)...
-__global__ void __launch_bounds__(256) k_oz_adigits(K3Args3 args, Dims d, const int* __restrict__ fa_blk, uint8_t* adig,
-                                                    int r0) {
-    const int N = d.N3n, nchunks = N / CW;
-    const int rr = blockIdx.x / nchunks, c = blockIdx.x % nchunks;
-    const int rest = r0 + rr, nb = args.nblocks;
-    const int slot = rest / nb, bi = rest % nb;
-    const int blk = args.blocks ? args.blocks[bi] : bi;
-    const int e = threadIdx.x;
-    if (e >= 2 * N) return;
-    const int FA = fa_blk[rest];
-    const int row = e >> 1, quad = e & 1;
-    const cplx* A = slot == 0 ? args.a[0].A : slot == 1 ? args.a[1].A : args.a[2].A;
-    const cplx* src = A + (size_t)blk * N * N + (size_t)row * N + CW * c + 4 * quad;
-    uint32_t wd[S][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const cplx v = ldg(src + i);
-        const unsigned long long yr = fixed56(v.x, FA), yi = fixed56(v.y, FA);
-        const uint32_t sg = (sbit(v.x) << 15) | (sbit(v.y) << 31);
-#pragma unroll
-        for (int s = 0; s < S; ++s) wd[s][i] = bf_pair(digit(yr, s), digit(yi, s), sg);
-    }
+    int FA = wmax[0];
+    for (int w = 1; w < 8; ++w) FA = max(FA, wmax[w]);
+    if (threadIdx.x == 0) fa_blk[rest] = FA;
     const size_t arow = (size_t)N * 32;
-    uint8_t* dst = adig + ((size_t)rr * nchunks + c) * S * arow + op16(row, 8 * quad);
+    for (int e = threadIdx.x; e < 2 * N * nchunks; e += 256) {
+        const int c = e / (2 * N), rq = e % (2 * N), row = rq >> 1, quad = rq & 1;
+        const cplx* src = A + (size_t)row * N + CW * c + 4 * quad;
+        uint32_t wd[S][4];
 #pragma unroll
-    for (int s = 0; s < S; ++s)
-        *reinterpret_cast<uint4*>(dst + (size_t)s * arow) = make_uint4(wd[s][0], wd[s][1], wd[s][2], wd[s][3]);
+        for (int i = 0; i < 4; ++i) {
+            const cplx v = ldg(src + i);
+            const unsigned long long yr = fixed56(v.x, FA), yi = fixed56(v.y, FA);
+            const uint32_t sg = (sbit(v.x) << 15) | (sbit(v.y) << 31);
+#pragma unroll
+            for (int s = 0; s < S; ++s) wd[s][i] = bf_pair(digit(yr, s), digit(yi, s), sg);
+        }
+        uint8_t* dst = adig + ((size_t)rr * nchunks + c) * S * arow + op16(row, 8 * quad);
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+            *reinterpret_cast<uint4*>(dst + (size_t)s * arow) = make_uint4(wd[s][0], wd[s][1], wd[s][2], wd[s][3]);
+    }
 }
 
 template <int MODE>
@@ -306,7 +295,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
         return e;
     };
     // pass 1: F_A, the exponent field bound of A over the block (its largest exponent field), comes
-    // from k_oz_amax, which reads every A block once for all its column tiles; here, a bound of |M|
+    // from k_oz_adigits, which reads every A block once for all its column tiles; here, a bound of |M|
     // over the tile from FP32 upper bounds of the parts of its factors (one product in
     // mode 0 and one-loop, s1[(Π-Π0)F0 + Π Γ] + s2 Π γL otherwise; |Re(ab)| ≤ |a.x||b.x| + |a.y||b.y|,
     // |Im(ab)| ≤ |a.x||b.y| + |a.y||b.x|), raised by 2^-16 for the FP32 roundings:
@@ -598,16 +587,15 @@ cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nsl
                              int* fa_scratch, uint8_t* adig, int adig_blocks, int ebound) {
     if (!k3_oz_supported(d) || mode < 0 || mode > 2 || !fa_scratch || !adig || adig_blocks < 1)
         return cudaErrorInvalidValue;
-    const int ntile = (2 * d.N3n + NT - 1) / NT, nchunks = d.N3n / CW;
+    const int ntile = (2 * d.N3n + NT - 1) / NT;
     const int nblk = nslots * a.nblocks;
-    // per launch: the blocks' exponent bounds, then groups of at most adig_blocks blocks (the size
-    // of the digit buffer), each digitised and contracted in stream order
+    // per launch: groups of at most adig_blocks blocks (the size of the digit buffer), each
+    // digitised (with its exponent bounds) and contracted in stream order
     auto run = [&](auto kernel, const K3Args3& ka) -> cudaError_t {
-        k_oz_amax<<<nblk, 256, 0, s>>>(ka, d, fa_scratch);
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = cudaSuccess;
         for (int r0 = 0; e == cudaSuccess && r0 < nblk; r0 += adig_blocks) {
             const int cnt = std::min(adig_blocks, nblk - r0);
-            k_oz_adigits<<<(unsigned)(cnt * nchunks), 256, 0, s>>>(ka, d, fa_scratch, adig, r0);
+            k_oz_adigits<<<(unsigned)cnt, 256, 0, s>>>(ka, d, fa_scratch, adig, r0);
             e = cudaGetLastError();
             if (e != cudaSuccess) break;
             kernel<<<(unsigned)(cnt * ntile), OZ_THREADS, k3_oz_smem(), s>>>(ka, d, ntile, fa_scratch, adig, r0, ebound,
@@ -624,7 +612,7 @@ cudaError_t launch_bse_K3_oz(cudaStream_t s, int mode, const K3Args3& a, int nsl
             a1.a[i].flags |= K3F_NOEPI;
             a3.a[i].flags |= K3F_ACC;
         }
-        // stream order: the second launch's passes overwrite the scratch after the first
+        // stream order: the second launch's pre-pass overwrites the scratch after the first
         // contraction has read it
         const cudaError_t e = run(k_bse_K3_oz<1>, a1);
         if (e != cudaSuccess) return e;
