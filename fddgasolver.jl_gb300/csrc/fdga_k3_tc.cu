@@ -231,7 +231,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_bse_K3_tc(K3Args3F args, Dims
     if (!mbar_wait(smem_u32(&mbar[(nck - 1) & 1]), ((nck - 1) >> 1) & 1)) ok = false;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ok) {
+        // a wait gave up: report it, and give the MMAs in flight one more bounded wait before the
+        // tensor memory is released (the loop went on staging, so every thread still reaches the
+        // CTA barriers; the results are discarded with the error)
         if (tid == 0) atomicExch(err, 1);
+        mbar_wait(smem_u32(&mbar[(nck - 1) & 1]), ((nck - 1) >> 1) & 1);
     } else {
         // epilogue: warp w reads lanes 32(w%4).. (rows ν), every 4th group of 16 columns from 16(w/4)
         const int q = warp & 3, grp = warp >> 2;
