@@ -210,9 +210,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
     __shared__ cplx qf[128][2];
     __shared__ int qe[128][2];
     __shared__ float2 qm[128][2];  // part bounds of [0] and of Π
-    // (unused); FP32 bound of |M| (tile, as bits); exponent-sum bound of M (tile, when the FP32 bound
-    // is not finite); non-finite operands
-    __shared__ int fmax[4];
+    // bounds of the tile of M: [0] the FP32 bound of |M| (as bits), [1] the exponent-sum bound (when
+    // the FP32 bound is not finite), [2] non-finite operands
+    __shared__ int mbnd[3];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = d.N3n;
     const int nchunks = N / CW;  // N is a multiple of 8
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
         qm[tid][0] = mag_up(q0);
         qm[tid][1] = mag_up(q1);
     }
-    if (tid < 4) fmax[tid] = 0;
+    if (tid < 3) mbnd[tid] = 0;
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[i])) : "memory");
@@ -334,11 +334,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
             bm = fmaxf(bm, fmaxf(mb.x, mb.y));  // the parts are ≥ 0, so no NaN arises
         }
         for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
-        if (lane == 0) atomicMax(&fmax[1], (int)__float_as_uint(bm));  // non-negative floats order as integers
+        if (lane == 0) atomicMax(&mbnd[0], (int)__float_as_uint(bm));  // non-negative floats order as integers
     }
-    if (ebound && tid == 0) atomicMax(&fmax[1], 0x7F800000);  // the exponent bound on request (tests)
+    if (ebound && tid == 0) atomicMax(&mbnd[0], 0x7F800000);  // the exponent bound on request (tests)
     __syncthreads();
-    if (fmax[1] >= 0x7F800000) {  // the FP32 bound overflowed: FP64 exponent bound (block-uniform branch)
+    if (mbnd[0] >= 0x7F800000) {  // the FP32 bound overflowed: FP64 exponent bound (block-uniform branch)
         int fs = 0, nf = 0;
         for (int e = tid; e < N * ncc; e += OZ_THREADS) {
             const int w = e / ncc, col = cc0 + e % ncc;
@@ -375,21 +375,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 2)
             nf |= __shfl_xor_sync(0xffffffffu, nf, o);
         }
         if (lane == 0) {
-            atomicMax(&fmax[2], fs);
-            if (nf) atomicOr(&fmax[3], 1);
+            atomicMax(&mbnd[1], fs);
+            if (nf) atomicOr(&mbnd[2], 1);
         }
         __syncthreads();
     }
     const int FA = fa_blk[rest];
     int FM;
-    if (fmax[1] >= 0x7F800000) {
-        FM = max(fmax[2] - 1019, 0);
+    if (mbnd[0] >= 0x7F800000) {
+        FM = max(mbnd[1] - 1019, 0);
     } else {
-        const float B = __uint_as_float((uint32_t)fmax[1]);
+        const float B = __uint_as_float((uint32_t)mbnd[0]);
         const uint32_t eb = __float_as_uint(fmaf(B, 1.52587890625e-05f, B)) >> 23;  // B (1 + 2^-16)
         FM = (B == 0.0f) ? 0 : (eb >= 255u ? 1152 : (int)eb + 896);
     }
-    const bool nonfinite = FA == 0x7ff || fmax[3] != 0;
+    const bool nonfinite = FA == 0x7ff || mbnd[2] != 0;
     // instruction descriptor: D FP32, A and B BF16, both K-major, N = ncol, M = 128
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(ncol >> 3) << 17) | ((128u >> 4) << 24);
     // shared-memory descriptors of the first A and B digit operands of stage 0 (the start address
