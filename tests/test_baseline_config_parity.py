@@ -3,7 +3,8 @@ not reach: the local SIAM workload (nK1=64, nK2=(32,32), nK3=(16,16), mΠν_fact
 the Hubbard 16x16 precision workload (nK3=(20,40), Nν3 = 80) on a 4x4 lattice.
 
 Tolerances: the FP64 map agrees with the oracle to 1e-10 relative per flatten block (the plain path's
-parity bar); the mixed map, whose K3 contractions run on the tensor cores (tcgen05, TF32 hi/lo split,
+parity bar; at both shapes, Nν3 = 32 and 80, its K3 contractions run on the tensor cores by digit
+slicing, the default from Nν3 = 32 on); the mixed map, whose K3 contractions run on the tensor cores (tcgen05, TF32 hi/lo split,
 FP32 accumulation) at Nν3 = 80, agrees with the oracle's FP64 map to 1e-5 per block.  solve! on the
 device (Anderson m = 8, δ = 0.5, tol 1e-8, maxiter 50) follows the oracle's trajectory: the same
 iteration count and the same fixed point to 1e-9.
