@@ -30,6 +30,8 @@ LOCAL96 = dict(kind="siam", T=0.05, U=1.2, e=0.1, Delta=0.6, D=10.0, nG=48, nK1=
                mPi_factor=2)
 LOCAL128 = dict(kind="siam", T=0.04, U=1.0, e=0.0, Delta=0.5, D=float("inf"), nG=64, nK1=64, nK2=(4, 64),
                 nK3=(2, 64), mPi_factor=2)
+NL8 = dict(kind="hubbard", T=0.5, U=2.0, mu=0.3, t1=1.0, t2=-0.2, L=4, nG=8, nK1=8, nK2=(3, 4), nK3=(2, 4),
+           mPi_factor=4, refvertex_noise=0.05, seed=7)
 CASES = [LOCAL8, NL24, LOCAL32, NL32, LOCAL80, LOCAL96, LOCAL128]
 IDS = ["local8", "nl24", "local32", "nl32", "local80", "local96", "local128"]
 
@@ -138,4 +140,29 @@ def test_digit_sliced_k3_propagates_nan():
     nan_cc = np.isnan(r_cc)
     assert nan_cc.any()
     assert np.isnan(r_tc[nan_cc]).all()
+    gpu.close()
+
+
+@pytest.mark.parametrize("cfg,what", [(NL8, "fdPA_1loop"), (LOCAL8, "fdPA_new"), (LOCAL8, "scPA_new"), (NL8, "mfrg")],
+                         ids=["nl8-fdPA_1loop", "local8-fdPA_new", "local8-scPA_new", "nl8-mfrg"])
+def test_digit_sliced_k3_other_maps(cfg, what):
+    """The strategy variants (the one-loop K3 form among them) and the mfRG map run the same K3
+    contractions; at Nν3 = 8 with option 1 they agree with their CUDA-core form to 1e-12."""
+    rng = np.random.default_rng(26)
+    gpu = make_gpu(cfg, True)
+    x = gpu.flatten()
+    x = x + 0.05 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))
+    nF = blocks(cfg)[-1][1]  # the vertex part of the state
+
+    def run():
+        if what == "mfrg":
+            return np.concatenate([gpu.mfrg_apply(x[:nF]), x[nF:]])
+        return gpu.fixed_point(x, what) + x
+
+    gpu.set_option("k3_fp64_tensor_cores", 0)
+    y_cc = run()
+    gpu.set_option("k3_fp64_tensor_cores", 1)
+    assert gpu.query("k3_fp64_tensor_cores") == 1
+    y_tc = run()
+    assert blockwise_rel_err(cfg, y_tc, y_cc) < 1e-12
     gpu.close()
