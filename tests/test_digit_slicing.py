@@ -3,9 +3,9 @@ slicing of fdga_k3_oz.cu), emulated exactly in numpy integers: 56-bit fixed poin
 block bounds, 8 digits of 7 bits, the 36 digit-pair products summed by diagonal with each diagonal
 rounded to FP32 as the tensor-memory accumulator holds it, the diagonals joined in two 64-bit
 integers, and the FP32 magnitude bound of the M tile.  The emulated product must match A·M in FP64
-to 2e-14 of max|A·M| on blocks whose entries spread over e^6, for the one-product and the
-three-product forms of M.  The CUDA kernel itself is compared on the GPU
-(test_k3_fp64_tensor_cores.py).
+to 2e-14 of max|A·M| on blocks whose entries spread over e^6, for the forms of M of BSE_L_K3, BSE_K3
+and the tangent's A·dM launch, and the bound of M must lie within 2 binary orders of max|M|.  The
+CUDA kernel itself is compared on the GPU (test_k3_fp64_tensor_cores.py).
 """
 import numpy as np
 import pytest
@@ -69,11 +69,13 @@ def _digit_sliced_product(A, M, FM):
 
 
 def _bound_exponent(terms):
-    """F_M from the FP32 bound of |M| = |Σ q_i(ω) X_i(ω, ν')| (the kernel's pass 1)."""
+    """F_M from the FP32 bound of |M| = |Σ q_i(ω) Σ_j X_ij(ω, ν')| (the kernel's pass 1): the parts of
+    a sum of X's are bounded by the sums of their parts' bounds."""
     bx = by = np.float32(0)
-    for q, X in terms:
+    for q, Xs in terms:
         qx, qy = _mag_up(q.real)[:, None], _mag_up(q.imag)[:, None]
-        xx, xy = _mag_up(X.real), _mag_up(X.imag)
+        xx = sum(_mag_up(X.real) for X in Xs)
+        xy = sum(_mag_up(X.imag) for X in Xs)
         bx = bx + qx * xx + qy * xy
         by = by + qx * xy + qy * xx
     B = np.float32(max(bx.max(), by.max()))
@@ -82,19 +84,25 @@ def _bound_exponent(terms):
 
 
 @pytest.mark.parametrize("N", [8, 24, 96])
-@pytest.mark.parametrize("form", ["one", "three"])
+@pytest.mark.parametrize("form", ["one", "three", "tangent"])
 def test_digit_sliced_product_matches_fp64(N, form):
-    rng = np.random.default_rng(N + (0 if form == "one" else 1000))
+    """one: Π0 F0 (BSE_L_K3); three: s1 (Π - Π0) F0 + s1 Π (Γ ± γL) (BSE_K3); tangent:
+    s1 dΠ (F0 + Γ ± γL) + s1 Π (dΓ ± dγL) (the A·dM launch of the tangent)."""
+    rng = np.random.default_rng(N + {"one": 0, "three": 1000, "tangent": 2000}[form])
 
     def crand(*sh, spread=6.0):
         return (rng.standard_normal(sh) + 1j * rng.standard_normal(sh)) * np.exp(-rng.uniform(0, spread, sh))
 
     A = crand(N, N)
-    terms = [(crand(N, spread=10.0), crand(N, N))]
-    if form == "three":
+    if form == "one":
+        terms = [(crand(N, spread=10.0), [crand(N, N)])]
+    elif form == "three":
         p = crand(N, spread=10.0)
-        terms += [(p, crand(N, N)), (-p, crand(N, N))]
-    M = sum(q[:, None] * X for q, X in terms)
+        terms = [(crand(N, spread=10.0), [crand(N, N)]), (p, [crand(N, N), -crand(N, N)])]
+    else:
+        terms = [(crand(N, spread=10.0), [crand(N, N), crand(N, N), -crand(N, N)]),
+                 (crand(N, spread=10.0), [crand(N, N), -crand(N, N)])]
+    M = sum(q[:, None] * sum(Xs) for q, Xs in terms)
     FM = _bound_exponent(terms)
     assert _cexpo(M).max() <= FM <= _cexpo(M).max() + 2
     C = _digit_sliced_product(A, M, FM)
